@@ -1,0 +1,337 @@
+"""ctypes wrapper of the CPU oracle (oracle/qio_oracle.cc).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+as the checker, and by bench.py's CPU-baseline leg.  The product package never
+imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libqio_oracle.so")
+_lock = threading.Lock()
+_lib = None
+
+ISING, ISING_PLAIN, PUBO, PUBO_PLAIN, MAXSAT = 0, 1, 2, 3, 4
+SA, PT, PA = 0, 1, 2
+RNG_REPLAY, RNG_COUNTER = 0, 1
+SCHED_LINEAR, SCHED_GEOMETRIC, SCHED_CONSTANT, SCHED_LIST = 0, 1, 2, 3
+
+KIND_BY_NAME = {"ising": ISING, "ising_plain": ISING_PLAIN, "pubo": PUBO,
+                "pubo_plain": PUBO_PLAIN, "maxsat": MAXSAT}
+
+
+class Schedule(C.Structure):
+    _fields_ = [("type", C.c_int), ("initial", C.c_double),
+                ("final_value", C.c_double), ("has_start", C.c_int),
+                ("has_stop", C.c_int), ("has_count", C.c_int),
+                ("start", C.c_double), ("stop", C.c_double),
+                ("count", C.c_int), ("n_values", C.c_int),
+                ("values", C.POINTER(C.c_double))]
+
+
+class Params(C.Structure):
+    _fields_ = [("solver", C.c_int), ("seed", C.c_uint32),
+                ("step_limit", C.c_int64), ("restarts", C.c_int64),
+                ("use_inverse", C.c_int), ("sched", Schedule),
+                ("sweeps_per_replica", C.c_int64),
+                ("population", C.c_int64), ("alpha", C.c_double),
+                ("constant_population", C.c_int),
+                ("exp_repopulation", C.c_int), ("pa_threads", C.c_int),
+                ("rng_mode", C.c_int), ("threads", C.c_int),
+                ("number_of_solutions", C.c_int),
+                ("has_cost_limit", C.c_int), ("cost_limit", C.c_double),
+                ("full_maxsat_sweep", C.c_int)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with make (g++; a few seconds)."""
+    with _lock:
+        src = os.path.join(_HERE, "qio_oracle.cc")
+        if force or not os.path.exists(_LIB_PATH) or \
+                os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+            subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        vp, i64, u32, dbl, ip = C.c_void_p, C.c_int64, C.c_uint32, C.c_double, C.c_int
+        P = C.POINTER
+        L.orc_pcg_stream.argtypes = [u32, ip, ip, P(C.c_uint32)]
+        L.orc_pcg_uniform.argtypes = [u32, ip, ip, P(dbl)]
+        L.orc_pcg_fork_uniform.argtypes = [u32, ip, ip, P(dbl)]
+        L.orc_twister_uniform.argtypes = [u32, ip, ip, P(dbl)]
+        L.orc_uniform_ln.argtypes = [P(dbl)]
+        L.orc_metropolis_accept.argtypes = [dbl, dbl, P(C.c_uint32), ip, P(ip)]
+        L.orc_metropolis_accept.restype = ip
+        L.orc_counter_draw.argtypes = [C.c_uint64, C.c_uint64]
+        L.orc_counter_draw.restype = C.c_uint64
+        L.orc_counter_key.argtypes = [u32, C.c_uint64]
+        L.orc_counter_key.restype = C.c_uint64
+        L.orc_model_create.argtypes = [ip, i64, P(i64), P(C.c_int32), P(dbl), C.c_char_p, ip]
+        L.orc_model_create.restype = vp
+        L.orc_model_destroy.argtypes = [vp]
+        for f in ("orc_model_n_vars", "orc_model_n_terms"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = i64
+        for f in ("orc_model_const_cost", "orc_model_scale_factor"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = dbl
+        L.orc_model_var_names.argtypes = [vp, P(C.c_int32)]
+        L.orc_state_cost.argtypes = [vp, P(C.c_uint8)]
+        L.orc_state_cost.restype = dbl
+        L.orc_state_cost_difference.argtypes = [vp, P(C.c_uint8), i64]
+        L.orc_state_cost_difference.restype = dbl
+        L.orc_model_twister_min.argtypes = [vp, u32, ip, dbl]
+        L.orc_model_twister_min.restype = dbl
+        L.orc_run.argtypes = [vp, P(Params), C.c_char_p, ip]
+        L.orc_run.restype = vp
+        for f in ("orc_res_n_replicas", "orc_res_n_vars", "orc_res_last_step",
+                  "orc_res_n_solutions"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = i64
+        L.orc_res_replicas.argtypes = [vp, P(dbl), P(dbl), P(C.c_uint64), P(C.c_uint64)]
+        L.orc_res_states.argtypes = [vp, P(C.c_uint8)]
+        L.orc_res_lowest_states.argtypes = [vp, P(C.c_uint8)]
+        L.orc_res_best_cost.argtypes = [vp]
+        L.orc_res_best_cost.restype = dbl
+        L.orc_res_best_state.argtypes = [vp, P(C.c_uint8)]
+        L.orc_res_solutions.argtypes = [vp, P(dbl), P(C.c_uint8)]
+        L.orc_res_pt_observables.argtypes = [vp, P(dbl)]
+        L.orc_res_pa_trace.argtypes = [vp, P(i64), P(dbl), P(i64), i64]
+        L.orc_res_destroy.argtypes = [vp]
+        L.orc_pt_toy.argtypes = [u32, i64, P(dbl), ip, ip, P(dbl), P(dbl)]
+        L.orc_pt_toy.restype = ip
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+# ---------------------------------------------------------------- rng pins
+def pcg_stream(seed=None, n=8):
+    out = np.zeros(n, np.uint32)
+    lib().orc_pcg_stream(0 if seed is None else seed, 1 if seed is None else 0,
+                         n, _p(out, C.c_uint32))
+    return out
+
+
+def pcg_uniform(seed=None, n=8):
+    out = np.zeros(n, np.float64)
+    lib().orc_pcg_uniform(0 if seed is None else seed, 1 if seed is None else 0,
+                          n, _p(out, C.c_double))
+    return out
+
+
+def pcg_fork_uniform(seed, n_forks, n):
+    out = np.zeros((n, n_forks + 1), np.float64)
+    lib().orc_pcg_fork_uniform(seed, n_forks, n, _p(out, C.c_double))
+    return out
+
+
+def twister_uniform(seed=None, n=8):
+    out = np.zeros(n, np.float64)
+    lib().orc_twister_uniform(0 if seed is None else seed,
+                              1 if seed is None else 0, n, _p(out, C.c_double))
+    return out
+
+
+def uniform_ln():
+    out = np.zeros((4, 256), np.float64)
+    lib().orc_uniform_ln(_p(out, C.c_double))
+    return out
+
+
+def metropolis_accept(cost_diff, beta, draws):
+    d = np.ascontiguousarray(draws, np.uint32)
+    used = C.c_int(0)
+    a = lib().orc_metropolis_accept(float(cost_diff), float(beta),
+                                    _p(d, C.c_uint32), len(d), C.byref(used))
+    return bool(a), used.value
+
+
+def counter_key(seed, stream):
+    return lib().orc_counter_key(seed, stream)
+
+
+def counter_draw(key, ctr):
+    return lib().orc_counter_draw(key, ctr)
+
+
+# ---------------------------------------------------------------- model
+def flatten_terms(terms):
+    """terms: list of (coef, [ids]) -> (offsets int64, ids int32, coef f64)."""
+    off = np.zeros(len(terms) + 1, np.int64)
+    for i, (_, ids) in enumerate(terms):
+        off[i + 1] = off[i] + len(ids)
+    ids = np.fromiter((v for _, t in terms for v in t), np.int32, count=int(off[-1]))
+    coef = np.array([c for c, _ in terms], np.float64)
+    return off, ids, coef
+
+
+class Model:
+    def __init__(self, kind, terms=None, *, off=None, ids=None, coef=None):
+        if isinstance(kind, str):
+            kind = KIND_BY_NAME[kind]
+        if terms is not None:
+            off, ids, coef = flatten_terms(terms)
+        self.off = np.ascontiguousarray(off, np.int64)
+        self.ids = np.ascontiguousarray(ids, np.int32)
+        self.coef = np.ascontiguousarray(coef, np.float64)
+        self.kind = kind
+        err = C.create_string_buffer(512)
+        self.h = lib().orc_model_create(kind, len(self.coef), _p(self.off, C.c_int64),
+                                        _p(self.ids, C.c_int32), _p(self.coef, C.c_double),
+                                        err, 512)
+        if not self.h:
+            raise ValueError(err.value.decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_model_destroy(self.h)
+            self.h = None
+
+    @property
+    def n_vars(self):
+        return lib().orc_model_n_vars(self.h)
+
+    @property
+    def n_terms(self):
+        return lib().orc_model_n_terms(self.h)
+
+    @property
+    def const_cost(self):
+        return lib().orc_model_const_cost(self.h)
+
+    @property
+    def scale_factor(self):
+        return lib().orc_model_scale_factor(self.h)
+
+    def var_names(self):
+        out = np.zeros(self.n_vars, np.int32)
+        lib().orc_model_var_names(self.h, _p(out, C.c_int32))
+        return out
+
+    def cost(self, spins):
+        s = np.ascontiguousarray(spins, np.uint8)
+        return lib().orc_state_cost(self.h, _p(s, C.c_uint8))
+
+    def cost_difference(self, spins, var):
+        s = np.ascontiguousarray(spins, np.uint8)
+        return lib().orc_state_cost_difference(self.h, _p(s, C.c_uint8), int(var))
+
+    def twister_min(self, seed, iters, T):
+        return lib().orc_model_twister_min(self.h, seed, iters, T)
+
+
+def schedule(kind="linear", initial=0.0, final=0.0, values=None, start=None,
+             stop=None, count=None):
+    s = Schedule()
+    s.type = {"linear": SCHED_LINEAR, "geometric": SCHED_GEOMETRIC,
+              "constant": SCHED_CONSTANT, "list": SCHED_LIST}[kind]
+    s.initial, s.final_value = float(initial), float(final)
+    s.has_start, s.start = (start is not None), float(start or 0)
+    s.has_stop, s.stop = (stop is not None), float(stop or 0)
+    s.has_count, s.count = (count is not None), int(count or 0)
+    keep = None
+    if values is not None:
+        keep = np.ascontiguousarray(values, np.float64)
+        s.n_values = len(keep)
+        s.values = _p(keep, C.c_double)
+    return s, keep
+
+
+class Result:
+    def __init__(self, h):
+        self.h = h
+        L = lib()
+        n = L.orc_res_n_replicas(h)
+        self.n_vars = L.orc_res_n_vars(h)
+        self.last_step = L.orc_res_last_step(h)
+        self.cost = np.zeros(n)
+        self.lowest = np.zeros(n)
+        self.attempts = np.zeros(n, np.uint64)
+        self.accepts = np.zeros(n, np.uint64)
+        if n:
+            L.orc_res_replicas(h, _p(self.cost, C.c_double), _p(self.lowest, C.c_double),
+                               _p(self.attempts, C.c_uint64), _p(self.accepts, C.c_uint64))
+        self.states = np.zeros((n, self.n_vars), np.uint8)
+        self.lowest_states = np.zeros((n, self.n_vars), np.uint8)
+        if n and self.n_vars:
+            L.orc_res_states(h, _p(self.states, C.c_uint8))
+            L.orc_res_lowest_states(h, _p(self.lowest_states, C.c_uint8))
+        self.best_cost = L.orc_res_best_cost(h)
+        self.best_state = np.zeros(self.n_vars, np.uint8)
+        L.orc_res_best_state(h, _p(self.best_state, C.c_uint8))
+        ns = L.orc_res_n_solutions(h)
+        self.solution_costs = np.zeros(ns)
+        self.solution_states = np.zeros((ns, self.n_vars), np.uint8)
+        if ns:
+            L.orc_res_solutions(h, _p(self.solution_costs, C.c_double),
+                                _p(self.solution_states, C.c_uint8))
+        self.pt_obs = np.zeros((n, 5))
+        if n:
+            L.orc_res_pt_observables(h, _p(self.pt_obs, C.c_double))
+        steps = C.c_int64(0)
+        tb = np.zeros(1 << 16)
+        tp = np.zeros(1 << 16, np.int64)
+        L.orc_res_pa_trace(h, C.byref(steps), _p(tb, C.c_double), _p(tp, C.c_int64), 1 << 16)
+        self.pa_beta = tb[:steps.value].copy()
+        self.pa_population = tp[:steps.value].copy()
+        L.orc_res_destroy(h)
+        self.h = None
+
+
+def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
+        use_inverse=True, sched=("linear", 0.0, 0.01), sched_values=None,
+        sched_count=None, sweeps_per_replica=1, population=16, alpha=2.0,
+        constant_population=False, exp_repopulation=False, pa_threads=1,
+        rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
+        full_maxsat_sweep=False):
+    p = Params()
+    p.solver = {"sa": SA, "pt": PT, "pa": PA}[solver]
+    p.seed = seed & 0xFFFFFFFF
+    p.step_limit = step_limit
+    p.restarts = restarts
+    p.use_inverse = 1 if use_inverse else 0
+    kind, a, b = sched
+    p.sched, keep = schedule(kind, a, b, values=sched_values, count=sched_count)
+    p.sweeps_per_replica = sweeps_per_replica
+    p.population = population
+    p.alpha = alpha
+    p.constant_population = int(constant_population)
+    p.exp_repopulation = int(exp_repopulation)
+    p.pa_threads = pa_threads
+    p.rng_mode = RNG_REPLAY if rng_mode == "replay" else RNG_COUNTER
+    p.threads = threads
+    p.number_of_solutions = number_of_solutions
+    p.has_cost_limit = cost_limit is not None
+    p.cost_limit = float(cost_limit or 0.0)
+    p.full_maxsat_sweep = int(full_maxsat_sweep)
+    err = C.create_string_buffer(512)
+    h = lib().orc_run(model.h, C.byref(p), err, 512)
+    del keep
+    if not h:
+        raise ValueError(err.value.decode())
+    return Result(h)
+
+
+def pt_toy(seed, steps, temps, use_inverse=False):
+    t = np.ascontiguousarray(temps, np.float64)
+    obs = np.zeros((len(t), 5))
+    best = C.c_double(0)
+    lib().orc_pt_toy(seed, steps, _p(t, C.c_double), len(t), int(use_inverse),
+                     _p(obs, C.c_double), C.byref(best))
+    return obs, best.value

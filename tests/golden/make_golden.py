@@ -1,0 +1,196 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own tests.
+
+Run in a container where the QIOToolkit reference is mounted (read-only) at
+REFERENCE (default /root/reference).  The GPU machine never runs this script; it
+uses the committed JSON files.
+
+Sources (paths relative to the reference's cpp/ or data/ directory):
+  rng_pins.json      utils/test/random_generator_test.cc:18-79
+  pt_toy_pin.json    solver/test/parallel_tempering_test.cc:113-190
+  model_pins.json    model/test/ising_term_cached_test.cc:24-102,
+                     model/test/ising_test.cc:119-160,326-360,619-662,
+                     model/test/pubo_with_counter_test.cc:59-100,206-244,
+                     model/test/max_sat_test.cc:22-80
+  solver_pins.json   solver/test/simulated_annealing_test.cc:194-260,
+                     solver/test/parallel_tempering_test.cc:239-281,
+                     solver/test/population_annealing_test.cc:243-329,
+                     with their data/ inputs and data/params1.json
+  planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
+                     combined_4_local_N_16}_qualitytest (instances + energies)
+
+Expected values are parsed from the test sources where they are plain
+literals (EXPECT_* and ElementsAre lines), so a change in the reference shows
+up as a change in the fixtures.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+REFERENCE = os.environ.get("QIO_REFERENCE", "/root/reference")
+CPP = os.path.join(REFERENCE, "cpp")
+DATA = os.path.join(REFERENCE, "data")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def read(rel, base=CPP):
+    with open(os.path.join(base, rel)) as f:
+        return f.read()
+
+
+def lines(rel, a, b, base=CPP):
+    return read(rel, base).splitlines()[a - 1:b]
+
+
+def terms_of(model_json):
+    cf = model_json["cost_function"]
+    return {"type": cf["type"], "terms": [[t["c"], list(t["ids"])] for t in cf["terms"]]}
+
+
+def rng_pins():
+    src = "\n".join(lines("utils/test/random_generator_test.cc", 18, 79))
+    blocks = {}
+    for name in ("Twister, DefaultSeed", "Twister, CustomSeed", "PCG, DefaultSeed",
+                 "PCG, CustomSeed"):
+        body = src.split("TEST(" + name + ")")[1].split("TEST(")[0]
+        vals = [int(v) for v in re.findall(r"\*\s*100\),\s*(\d+)\)", body)]
+        blocks[name] = vals[:3]
+    forks = [list(map(int, m.split(","))) for m in
+             re.findall(r"ElementsAre\(([\d,\s]+)\)", src)]
+    return {
+        "source": "utils/test/random_generator_test.cc:18-79",
+        "twister_default": blocks["Twister, DefaultSeed"],
+        "twister_42": blocks["Twister, CustomSeed"],
+        "pcg_default": blocks["PCG, DefaultSeed"],
+        "pcg_42": blocks["PCG, CustomSeed"],
+        "pcg_42_fork": forks,  # master, fork1, fork2, fork3 (12 draws each)
+    }
+
+
+def pt_toy_pin():
+    src = "\n".join(lines("solver/test/parallel_tempering_test.cc", 113, 190))
+    rows = re.findall(r"\{\s*\"T\":\s*([\d.]+),\s*\"acc_rate\":\s*([\d.]+),\s*"
+                      r"\"avg_cost\":\s*([\d.]+),\s*\"avg_dir\":\s*([\d.]+)"
+                      r"(?:,\s*\"swap_rate\":\s*([\d.]+))?", src)
+    obs = [[float(x) if x else None for x in r] for r in rows]
+    return {"source": "solver/test/parallel_tempering_test.cc:113-190",
+            "seed": 42, "step_limit": 200,
+            "temperatures": {"type": "linear", "initial": 0.5, "final": 0.1, "count": 5},
+            "observables": obs,  # per replica: T, acc_rate, avg_cost, avg_dir, swap_rate
+            "format": "%f (std::to_string)"}
+
+
+def ring10(c=1):
+    return [[c, [i, (i + 1) % 10]] for i in range(10)]
+
+
+def model_pins():
+    pins = []
+    # ring of 10 ferromagnetic couplings: costs 10 / -4 / 6 / 4 / 10
+    # (ising_term_cached_test.cc:61-76, ising_test.cc:119-134) and Twister(188)
+    # Metropolis minimum -10 (ising_term_cached_test.cc:78-102)
+    pins.append({"name": "ising_ring10", "kind": "ising", "terms": ring10(),
+                 "source": "model/test/ising_term_cached_test.cc:24-102",
+                 "single_updates": {"cost0": 10, "diff0": -4, "cost1": 6, "diff1": 4,
+                                    "cost2": 10},
+                 "twister_min": {"seed": 188, "iters": 1000, "T": 0.5, "min": -10}})
+    # PUBO ring: 10 / -2 / 8 / 2 / 10, Twister min 0
+    # (pubo_with_counter_test.cc:59-100; the fixture is the same ring)
+    src = read("model/test/pubo_with_counter_test.cc")
+    m = re.search(r"R\"\((\{.*?\})\)\"", src, re.S)
+    pubo_fixture = terms_of(json.loads(m.group(1)))
+    pins.append({"name": "pubo_ring10", "kind": "pubo", "terms": pubo_fixture["terms"],
+                 "source": "model/test/pubo_with_counter_test.cc:24-100",
+                 "single_updates": {"cost0": 10, "diff0": -2, "cost1": 8, "diff1": 2,
+                                    "cost2": 10},
+                 "twister_min": {"seed": 188, "iters": 1000, "T": 0.5, "min": 0}})
+    # constant terms (ising_test.cc:326-360, pubo_with_counter_test.cc:227-244)
+    pins.append({"name": "ising_const", "kind": "ising",
+                 "terms": [[100, []], [2, []]], "const_cost": 102,
+                 "source": "model/test/ising_test.cc:326-343"})
+    pins.append({"name": "pubo_const", "kind": "pubo",
+                 "terms": [[1, []], [2, []]], "const_cost": 3,
+                 "source": "model/test/pubo_with_counter_test.cc:227-244"})
+    # duplicated ids in an Ising term throw (ising_test.cc:362)
+    pins.append({"name": "ising_dup", "kind": "ising", "terms": [[1, [0, 0]]],
+                 "throws": True, "source": "model/test/ising_test.cc:362-380"})
+    # disordered ids / renumbering (pubo_with_counter_test.cc:206-225)
+    pins.append({"name": "pubo_names", "kind": "pubo",
+                 "terms": [[1, [0]], [2, [2, 100]]], "var_names": [0, 2, 100],
+                 "source": "model/test/pubo_with_counter_test.cc:206-225"})
+    # MaxSAT 1(!x) + 4(x||y) + 2(!y): costs 4/1/2/3 and diffs
+    # (max_sat_test.cc:22-80)
+    pins.append({"name": "maxsat_small", "kind": "maxsat",
+                 "terms": [[1, [-1]], [4, [1, 2]], [2, [-2]]],
+                 "source": "model/test/max_sat_test.cc:22-80",
+                 "costs": {"00": 4, "10": 1, "01": 2, "11": 3},
+                 "diffs": {"00": [1 - 4, 2 - 4], "01": [3 - 2, 4 - 2],
+                           "10": [4 - 1, 3 - 1], "11": [2 - 3, 1 - 3]}})
+    # all solvers on a 3-spin instance -> -2 (ising_test.cc:619-662)
+    pins.append({"name": "ising_3spin", "kind": "ising",
+                 "terms": [[-1, [0, 1]], [1, [2]]], "seed": 88, "min": -2.0,
+                 "source": "model/test/ising_test.cc:619-662"})
+    return pins
+
+
+def solver_pins():
+    params1 = json.loads(read("params1.json", DATA))["params"]
+    cases = []
+    specs = [
+        # (solver, model kind, data file, expected cost, configuration pins, source)
+        ("sa", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/simulated_annealing_test.cc:194-202"),
+        ("sa", "pubo", "puboempty.json", 2, {}, "solver/test/simulated_annealing_test.cc:204-212"),
+        ("sa", "ising", "isingempty.json", 12, {}, "solver/test/simulated_annealing_test.cc:214-222"),
+        ("sa", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/simulated_annealing_test.cc:224-234"),
+        ("sa", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/simulated_annealing_test.cc:250-260"),
+        ("pt", "pubo", "puboempty.json", 2, {}, "solver/test/parallel_tempering_test.cc:239-247"),
+        ("pt", "ising", "isingempty.json", 12, {}, "solver/test/parallel_tempering_test.cc:249-257"),
+        ("pt", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/parallel_tempering_test.cc:259-269"),
+        ("pt", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/parallel_tempering_test.cc:271-281"),
+        ("pa", "pubo", "cpupubojobstest.json", "<=-12", {}, "solver/test/population_annealing_test.cc:243-251"),
+        ("pa", "ising", "ising1.json", -10, {}, "solver/test/population_annealing_test.cc:263-271"),
+        ("pa", "pubo", "puboempty.json", 2, {}, "solver/test/population_annealing_test.cc:283-291"),
+        ("pa", "ising", "isingempty.json", 12, {}, "solver/test/population_annealing_test.cc:293-301"),
+        ("pa", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/population_annealing_test.cc:303-315"),
+        ("pa", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/population_annealing_test.cc:317-329"),
+    ]
+    for solver, kind, fname, cost, conf, source in specs:
+        model = terms_of(json.loads(read(fname, DATA)))
+        assert model["type"] == kind
+        cases.append({"solver": solver, "kind": kind, "file": fname,
+                      "terms": model["terms"], "params": params1,
+                      "expected_cost": cost, "configuration": conf, "source": source})
+    return {"params_file": "data/params1.json", "cases": cases}
+
+
+def planted():
+    out = []
+    for d in ("wishart_planting_N_16_alpha_0.81_qualitytest",
+              "combined_4_local_N_16_qualitytest"):
+        base = os.path.join(DATA, "input_e2e_pipeline", d)
+        en = json.load(open(os.path.join(base, "energies.json")))
+        for case in en["cases"]:
+            model = terms_of(json.load(open(os.path.join(base, case["file"]))))
+            out.append({"set": d, "file": case["file"], "kind": model["type"],
+                        "terms": model["terms"], "energy": case["energy"]})
+    return {"source": "data/input_e2e_pipeline/*/energies.json", "instances": out}
+
+
+def main():
+    if not os.path.isdir(CPP):
+        print("reference not found at", REFERENCE, file=sys.stderr)
+        sys.exit(1)
+    files = {"rng_pins.json": rng_pins(), "pt_toy_pin.json": pt_toy_pin(),
+             "model_pins.json": model_pins(), "solver_pins.json": solver_pins(),
+             "planted.json": planted()}
+    for name, obj in files.items():
+        with open(os.path.join(OUT, name), "w") as f:
+            json.dump(obj, f, separators=(",", ":"))
+            f.write("\n")
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()
