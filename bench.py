@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Metropolis hot path (flip attempts/s).
+
+Default workload: parallel tempering on a random PUBO -- N=4096 binary
+variables, 20000 terms of order {1,2,3,4} w.p. {.1,.5,.3,.1}, weights N(0,1)
+FP64, 32 replicas on a geometric temperature ladder 0.05 -> 3.0, 500 sweeps
+with a replica swap after every sweep, 16 restarts (16 independent ladders).
+One step = one complete solve (init + 500 sweeps + 500 swap phases of all 512
+walkers) = 1.05e9 flip attempts.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload pt_pubo|sa_ising|pa_square]
+
+Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
+launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
+goes through the C ABI from host buffers (model build + upload, solve,
+results back to the host) on the host clock.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    "pt_pubo": dict(desc="PT on random PUBO N=4096, 20000 terms (orders 1-4), N(0,1) FP64, "
+                         "32 temps geometric 0.05->3.0, 500 sweeps, swap every sweep, 16 restarts",
+                    target="paralleltempering.qiotoolkit"),
+    "sa_ising": dict(desc="SA on sparse Ising N=1000, 3000 ER couplings +-1, 1000 fields U[-0.5,0.5], "
+                          "linear beta 0.1->5.0 over 1000 sweeps, 64 restarts, seed 0",
+                     target="simulatedannealing.qiotoolkit"),
+    "pa_square": dict(desc="PA on 2D periodic 256x256 +-J Ising, R=4096, 100 beta steps 0->3.0, "
+                           "10 sweeps per step",
+                      target="populationannealing.cpu"),
+}
+
+
+def make_workload(name):
+    from qiotoolkit_gb300 import instances as I
+    if name == "pt_pubo":
+        off, ids, coef = I.random_pubo(4096, 20000, seed=1)
+        params = {"seed": 0, "sweeps": 500, "restarts": 16, "rng_mode": "replay",
+                  "temperatures": {"type": "geometric", "initial": 0.05, "final": 3.0,
+                                   "count": 32}}
+        return "pubo", off, ids, coef, params
+    if name == "sa_ising":
+        off, ids, coef = I.er_ising(1000, 3000, seed=0)
+        params = {"seed": 0, "sweeps": 1000, "restarts": 64, "beta_start": 0.1,
+                  "beta_stop": 5.0}
+        return "ising", off, ids, coef, params
+    if name == "pa_square":
+        off, ids, coef = I.square_pm_j(256, seed=3)
+        params = {"seed": 0, "sweeps": 100, "population": 4096, "beta_start": 0.0,
+                  "beta_stop": 3.0, "sweeps_per_replica": 10, "rng_mode": "counter"}
+        return "ising", off, ids, coef, params
+    raise SystemExit(f"unknown workload {name}")
+
+
+def attempts_per_step(kind, n_vars, params):
+    if "temperatures" in params:
+        return params["restarts"] * params["temperatures"]["count"] * params["sweeps"] * n_vars
+    if "population" in params:
+        return params["population"] * params["sweeps"] * params["sweeps_per_replica"] * n_vars
+    return params["restarts"] * params["sweeps"] * n_vars
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.rows, self.proc, self.device = [], None, device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(workload):
+    """dram bytes per sweep launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"sweep_{workload}_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(kind, off, ids, coef, params, budget_s=12.0):
+    """The oracle (CPU restatement of the reference) on a bounded sample of
+    the same workload, all host threads (OpenMP over replicas)."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    m = O.Model(kind, off=off, ids=ids, coef=coef)
+    n = m.n_vars
+
+    def run(sweeps):
+        if "temperatures" in params:
+            t = params["temperatures"]
+            kw = dict(sched=(t["type"], t["initial"], t["final"]), sched_count=t["count"],
+                      use_inverse=False)
+            t0 = time.perf_counter()
+            O.run(m, "pt", seed=0, step_limit=sweeps, threads=threads, **kw)
+            dt = time.perf_counter() - t0
+            return t["count"] * sweeps * n, dt, f"1 restart x {t['count']} replicas x {sweeps} sweeps"
+        if "population" in params:
+            pop = min(params["population"], 256)
+            t0 = time.perf_counter()
+            O.run(m, "pa", seed=0, step_limit=sweeps, population=pop, pa_threads=threads,
+                  threads=threads, sched=("linear", params["beta_start"], params["beta_stop"]),
+                  sweeps_per_replica=params["sweeps_per_replica"])
+            dt = time.perf_counter() - t0
+            return pop * sweeps * params["sweeps_per_replica"] * n, dt, \
+                f"population {pop} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
+        R = params["restarts"]
+        t0 = time.perf_counter()
+        O.run(m, "sa", seed=0, step_limit=sweeps, restarts=R, threads=threads,
+              sched=("linear", params["beta_start"], params["beta_stop"]))
+        dt = time.perf_counter() - t0
+        return R * sweeps * n, dt, f"{R} restarts x {sweeps} sweeps"
+
+    a, dt, _ = run(4)
+    rate = a / max(dt, 1e-6)
+    per_sweep = a / 4
+    sweeps = max(4, int(budget_s * rate / per_sweep))
+    sweeps = min(sweeps, params.get("sweeps", sweeps))
+    a, dt, desc = run(sweeps)
+    return {"value": a / dt, "unit": "flip attempts/s", "cores": threads, "kind": "port",
+            "sample": f"oracle (C++ restatement) {desc}, {a:.3g} attempts in {dt:.2f} s"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return ws, rank
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    kind, off, ids, coef, params = make_workload(args.workload)
+    from oracle import oracle as O
+    O.build()
+    times, attempts, desc = [], 0, ""
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(kind, off, ids, coef, params, budget_s=4.0)
+        if i >= args.warmup:
+            times.append(cb["value"])
+            desc = cb["sample"]
+    v = statistics.median(times)
+    line = {"impl": "reference", "metric": "flip attempts/s", "value": v,
+            "unit": "flip attempts/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload]["desc"]},
+            "cpu_baseline": {"value": v, "unit": "flip attempts/s",
+                             "cores": os.cpu_count() or 1, "kind": "port", "sample": desc},
+            "e2e": {"value": v, "unit": "flip attempts/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's own build needs rapidjson/pcg-cpp/googletest/protobuf "
+                    "fetched at configure time (no network); timed: the oracle's C++ "
+                    "restatement of its CPU path with OpenMP over replicas"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pt_pubo", choices=list(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    ws, rank = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    import qiotoolkit_gb300 as q
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    q.load()
+    kind, off, ids, coef, params = make_workload(args.workload)
+    target = WORKLOADS[args.workload]["target"]
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    model = q.Model(kind, off=off, ids=ids, coef=coef)
+    tp = dict(params, profile_kernels=True)
+    solver = q.Solver(model, target, {"params": tp})
+    n = model.n_vars
+    A = attempts_per_step(kind, n, params)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def one_step():
+        flush.fill_(1)  # L2 flush (256 MB > 129 MB L2), outside the timed region
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.init(sh)
+        solver.run(sh)
+        e1.record(stream)
+        e1.synchronize()
+        st = solver.stats()
+        return e0.elapsed_time(e1), st
+
+    for _ in range(args.warmup):
+        one_step()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ms, sweep_ms, launches, att = [], [], 0, 0
+    sweep_launches = 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, st = one_step()
+            ms.append(t)
+            sweep_ms.append(st.sweep_kernel_ms)
+            launches += int(st.kernel_launches)
+            att += int(st.attempts)
+    torch.cuda.synchronize()
+    barrier(ws)
+    total_s = reduce_max(sum(ms) / 1e3, ws)
+    value = A * args.steps * ws / total_s
+    # the solver reports its launches cumulatively; count this window's
+    per_step_launches = launches / args.steps
+    sweeps_per_step = params["sweeps"] if target != "simulatedannealing.qiotoolkit" else 1
+    if target == "simulatedannealing.qiotoolkit":
+        sweep_launches_per_step = 1
+    else:
+        sweep_launches_per_step = params["sweeps"]
+    avg_sweep_launch_ms = statistics.mean(sweep_ms) / sweep_launches_per_step
+    walkers = A // (n * (params["sweeps"] if "temperatures" in params or "restarts" in params
+                         else params["sweeps"] * params["sweeps_per_replica"]))
+    attempts_per_launch = A / sweep_launches_per_step
+    K = model.info.n_incidences
+    bpa = 9.0 + 13.0 * K / n  # row bounds 8 + own state 1 + per incidence (id 4 + coef 8 + state 1)
+    achieved = bpa * attempts_per_launch / (avg_sweep_launch_ms / 1e3) / 1e9
+    peak, peak_src = peaks()
+    traffic = committed_traffic(args.workload)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(q, kind, off, ids, coef, params, target, A, args, stream)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(kind, off, ids, coef, params)
+
+    if rank == 0:
+        line = {
+            "metric": "flip attempts/s", "value": value, "unit": "flip attempts/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload]["desc"], "n_vars": n,
+                       "n_terms": model.n_terms, "attempts_per_step": A,
+                       "rng_mode": params.get("rng_mode", "replay"),
+                       "l2": "flushed before each step (256 MB write)"},
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_src, "kernel": "sweep_kernel",
+                         "bytes_per_attempt": bpa,
+                         "avg_launch_ms": avg_sweep_launch_ms},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def measure_e2e(q, kind, off, ids, coef, params, target, A, args, stream):
+    """Same metric through the C ABI from host buffers: model build from the
+    host term arrays, upload, solve, lowest costs and states back."""
+    import torch
+    times, h2d, d2h = [], 0, 0
+    for i in range(1 + min(args.steps, 3)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m = q.Model(kind, off=off, ids=ids, coef=coef)
+        s = q.Solver(m, target, {"params": params})
+        s.init(stream.cuda_stream)
+        s.run(stream.cuda_stream)
+        rep = s.replicas(states=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if i > 0:
+            times.append(dt)
+        h2d = int(m.info.device_bytes)
+        d2h = int(rep["lowest_states"].size + rep["states"].size + 32 * len(rep["cost"]))
+        s.close()
+        m.close()
+    return {"value": A / statistics.median(times), "unit": "flip attempts/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,178 @@
+/*
+ * qio_gb300.h -- C ABI of the GB300 Metropolis library (libqio_gb300.so).
+ *
+ * The reference (QIOToolkit) binds models and solvers at compile time as C++
+ * templates; this header is the plain-C boundary that a reference-side
+ * plugin binds instead.  Each entry point names the reference interface it
+ * replaces (paths relative to the reference's cpp/ directory).
+ *
+ * Conventions
+ *   - Every call returns qio_status; on failure qio_last_error_message()
+ *     (thread-local) holds the reason, worded like the reference's
+ *     exceptions where the reference pins a message.
+ *   - Host buffers only cross this boundary; device memory is owned by the
+ *     library.  `stream` arguments are cudaStream_t values passed as void*
+ *     (NULL = the legacy default stream).
+ *   - Spin/variable states are arrays of uint8 in the model's internal
+ *     variable order (0 = false, 1 = true).  For Ising, true = spin -1; for
+ *     PUBO, true = variable value 0 (the reference's convention,
+ *     model/pubo.h:191-276); for MaxSAT, true = variable true.
+ *   - Handles are independent; one handle is used by one host thread at a
+ *     time.
+ */
+#ifndef QIO_GB300_H
+#define QIO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum qio_status {
+  QIO_OK = 0,
+  QIO_INVALID_ARGUMENT = 1, /* utils::ValueException and friends           */
+  QIO_OUT_OF_MEMORY = 2,    /* utils::MemoryLimitedException               */
+  QIO_CUDA_ERROR = 3,       /* a CUDA call failed                          */
+  QIO_TIMEOUT = 4,          /* a bounded device wait gave up               */
+  QIO_NO_DEVICE = 5,        /* no CUDA device: there is no CPU fallback    */
+  QIO_INTERNAL = 6
+} qio_status;
+
+typedef enum qio_model_kind {
+  QIO_ISING = 0,       /* model::IsingTermCached, model/ising.h:331-342      */
+  QIO_ISING_PLAIN = 1, /* model::Ising, model/ising.h:292-301                */
+  QIO_PUBO = 2,        /* model::PuboWithCounter<T>, model/pubo.h:285-399    */
+  QIO_PUBO_PLAIN = 3,  /* model::Pubo, model/pubo.h:221-231                  */
+  QIO_MAXSAT = 4       /* model::MaxSat<T>, model/max_sat.h:96-599           */
+} qio_model_kind;
+
+typedef struct qio_model qio_model;
+typedef struct qio_solver qio_solver;
+
+typedef struct qio_model_info {
+  int32_t kind;
+  int32_t integer_weights; /* 1: all coefficients are small integers (exact
+                              integer arithmetic on the device)            */
+  int64_t n_vars;
+  int64_t n_terms;
+  int64_t n_incidences;    /* sum of term orders                          */
+  int32_t max_locality;
+  int32_t min_locality;
+  double const_cost;       /* Graph::get_const_cost, graph/graph.h:214   */
+  double scale_factor;     /* GraphProperties::rescale factor (1/max|c| if
+                              max|c| > 1), graph/graph_properties.h:24-40 */
+  double max_coupling;
+  int64_t device_bytes;    /* HBM held by the model                       */
+} qio_model_info;
+
+typedef struct qio_solver_stats {
+  int64_t replicas;        /* walkers (SA restarts, PT slots, PA citizens) */
+  int64_t last_step;       /* SteppingSolver step_, solver/stepping_solver.h:369 */
+  uint64_t attempts;       /* difference evaluations (flip attempts)       */
+  uint64_t accepts;        /* accepted transitions                         */
+  uint64_t kernel_launches;/* kernels launched by qio_solver_run           */
+  double sweep_kernel_ms;  /* CUDA-event time of the sweep kernels         */
+  double run_ms;           /* CUDA-event time of the whole run             */
+  uint64_t near_ties;      /* PT swaps whose device exp() was within 1e-15 of
+                              the uniform draw (replay parity caveat)      */
+  int64_t device_bytes;    /* HBM held by the solver                       */
+} qio_solver_stats;
+
+/* ---- library ---------------------------------------------------------- */
+const char* qio_last_error_message(void);
+const char* qio_version(void);
+/* Releases a buffer returned by the library (result JSON). */
+void qio_free(void* p);
+
+/* ---- model ------------------------------------------------------------ */
+
+/* Build a model from the raw term list of the reference's input format
+ * ("cost_function": {"terms": [{"c": c, "ids": [...]}, ...]}).
+ * Replaces GraphModel::configure -> Graph::init -> normalize_edges
+ * (graph/graph.h:368-397,517-534,74-177) for graph models and
+ * MaxSat::configure(clauses) (model/max_sat.h:262-397) for QIO_MAXSAT:
+ * ids are renumbered by first appearance (MaxSAT: sorted by name), member ids
+ * are sorted, duplicate ids throw (Ising) or merge (PUBO), empty terms fold
+ * into the constant cost.
+ *   term_offsets: n_terms + 1 offsets into term_ids
+ *   term_ids:     variable names (MaxSAT: signed literals, -v = negated) */
+qio_status qio_model_create(int32_t kind, int64_t n_terms,
+                            const int64_t* term_offsets,
+                            const int32_t* term_ids,
+                            const double* coefficients, qio_model** out);
+
+/* Same, from the reference's JSON input document ({"cost_function": {...}}).
+ * kind < 0 selects by "type" as app/runner.cc:255-429 does (ising ->
+ * QIO_ISING, pubo -> QIO_PUBO, maxsat -> QIO_MAXSAT). */
+qio_status qio_model_create_json(const char* input_json, int32_t kind,
+                                 qio_model** out);
+
+qio_status qio_model_get_info(const qio_model* model, qio_model_info* out);
+/* Original variable name of each internal variable (Graph::output_map,
+ * graph/graph.h:407-413; MaxSat variable_names_, model/max_sat.h:596). */
+qio_status qio_model_get_var_names(const qio_model* model, int32_t* names);
+qio_status qio_model_destroy(qio_model* model);
+
+/* ---- per-state contract (markov/model.h:79-149), evaluated on the GPU --- */
+
+/* calculate_cost for n_states states (n_states x n_vars bytes); the sum runs
+ * in the reference's term order, so results are bit-identical to it. */
+qio_status qio_states_cost(const qio_model* model, int64_t n_states,
+                           const uint8_t* states, double* costs, void* stream);
+/* calculate_cost_difference(state q, vars[q]) for n queries. */
+qio_status qio_states_cost_difference(const qio_model* model, int64_t n,
+                                      const uint8_t* states,
+                                      const int64_t* vars, double* diffs,
+                                      void* stream);
+/* apply_transition(vars[q]) on each state (host buffers, in place). */
+qio_status qio_states_apply(const qio_model* model, int64_t n,
+                            uint8_t* states, const int64_t* vars);
+
+/* ---- solvers ---------------------------------------------------------- */
+
+/* Create a solver for `target` ("simulatedannealing.qiotoolkit",
+ * "paralleltempering.qiotoolkit", "populationannealing.cpu") configured from
+ * the reference's params JSON ({"params": {...}}): replaces
+ * create_model_solver (app/runner.cc:134-193) + Solver::configure
+ * (solver/solver.h:156-218 and the solver-specific configure()).  GB300
+ * options ride in the same object (see the "gb300" keys in the design doc). */
+qio_status qio_solver_create(const qio_model* model, const char* target,
+                             const char* params_json, qio_solver** out);
+/* Solver::init (random initial states, solver/simulated_annealing.h:45-74). */
+qio_status qio_solver_init(qio_solver* s, void* stream);
+/* SteppingSolver::run (solver/stepping_solver.h:112-268): all steps on the
+ * device; returns after the stream has drained. */
+qio_status qio_solver_run(qio_solver* s, void* stream);
+/* finalize + get_result (solver/model_solver.h:111-150,301-308,
+ * solver/solver.h:147-153): result JSON {"benchmark": ..., "solutions": ...}.
+ * The string is released with qio_free. */
+qio_status qio_solver_result_json(qio_solver* s, char** out_json);
+/* Per-walker results (NULL outputs are skipped); *n receives the count.
+ * lowest_states / states: n x n_vars bytes. */
+qio_status qio_solver_replicas(qio_solver* s, int64_t* n, double* cost,
+                               double* lowest, uint64_t* attempts,
+                               uint64_t* accepts, uint8_t* lowest_states,
+                               uint8_t* states);
+/* Best solution over all walkers: cost includes the constant terms. */
+qio_status qio_solver_best(qio_solver* s, double* cost, uint8_t* state);
+qio_status qio_solver_get_stats(qio_solver* s, qio_solver_stats* out);
+/* PT observables averaged over steps per temperature slot and restart:
+ * (T or beta, acc_rate, avg_cost, avg_dir, swap_rate) x slots x restarts,
+ * as the reference's observer renders them
+ * (solver/parallel_tempering.h:142-186). */
+qio_status qio_solver_pt_observables(qio_solver* s, double* out5);
+qio_status qio_solver_destroy(qio_solver* s);
+
+/* ---- runner ----------------------------------------------------------- */
+
+/* app::Runner::run (app/runner.cc:215-631): problem JSON + params JSON +
+ * target -> the reference's result JSON ({"benchmark", "solutions"}). */
+qio_status qio_run_json(const char* input_json, const char* params_json,
+                        const char* target, char** out_json);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QIO_GB300_H */

@@ -1,0 +1,217 @@
+"""Python mirror of the reference's model/solver plugin API over the C ABI.
+
+Model      ~ markov::Model (calculate_cost / calculate_cost_difference /
+             apply_transition), built from the reference's term list or JSON.
+Solver     ~ solver::Solver (configure from params, init, run, get_result),
+             selected by the reference's `target` strings.
+run_json   ~ app::Runner::run.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from ._lib import ModelInfo, SolverStats, check, load
+
+KINDS = {"ising": 0, "ising_plain": 1, "pubo": 2, "pubo_plain": 3, "maxsat": 4}
+TARGETS = ("simulatedannealing.qiotoolkit", "paralleltempering.qiotoolkit",
+           "populationannealing.cpu")
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def flatten_terms(terms: Iterable[Sequence]):
+    """[(c, [ids...]), ...] -> (offsets int64, ids int32, coef float64)."""
+    terms = list(terms)
+    off = np.zeros(len(terms) + 1, np.int64)
+    for i, (_, ids) in enumerate(terms):
+        off[i + 1] = off[i] + len(ids)
+    ids = np.fromiter((v for _, t in terms for v in t), np.int32, count=int(off[-1]))
+    coef = np.array([c for c, _ in terms], np.float64)
+    return off, ids, coef
+
+
+class Model:
+    def __init__(self, kind, terms=None, *, off=None, ids=None, coef=None, _handle=None):
+        L = load()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            if isinstance(kind, str):
+                kind = KINDS[kind]
+            if terms is not None:
+                off, ids, coef = flatten_terms(terms)
+            off = np.ascontiguousarray(off, np.int64)
+            ids = np.ascontiguousarray(ids, np.int32)
+            coef = np.ascontiguousarray(coef, np.float64)
+            h = C.c_void_p()
+            check(L.qio_model_create(int(kind), len(coef), _ptr(off, C.c_int64),
+                                     _ptr(ids, C.c_int32), _ptr(coef, C.c_double),
+                                     C.byref(h)))
+            self._h = h
+        info = ModelInfo()
+        check(L.qio_model_get_info(self._h, C.byref(info)))
+        self.info = info
+
+    @classmethod
+    def from_json(cls, doc, kind: int = -1) -> "Model":
+        if not isinstance(doc, str):
+            doc = json.dumps(doc)
+        h = C.c_void_p()
+        check(load().qio_model_create_json(doc.encode(), int(kind), C.byref(h)))
+        return cls(None, _handle=h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().qio_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_vars(self) -> int:
+        return self.info.n_vars
+
+    @property
+    def n_terms(self) -> int:
+        return self.info.n_terms
+
+    @property
+    def const_cost(self) -> float:
+        return self.info.const_cost
+
+    def var_names(self) -> np.ndarray:
+        out = np.zeros(self.n_vars, np.int32)
+        check(load().qio_model_get_var_names(self._h, _ptr(out, C.c_int32)))
+        return out
+
+    def _states(self, states):
+        s = np.ascontiguousarray(states, np.uint8)
+        if s.ndim == 1:
+            s = s[None, :]
+        if s.shape[1] != self.n_vars:
+            raise ValueError("state width must equal n_vars")
+        return s
+
+    def calculate_cost(self, states, stream=None) -> np.ndarray:
+        s = self._states(states)
+        out = np.zeros(len(s))
+        check(load().qio_states_cost(self._h, len(s), _ptr(s, C.c_uint8),
+                                     _ptr(out, C.c_double), stream))
+        return out
+
+    def calculate_cost_difference(self, states, vars, stream=None) -> np.ndarray:
+        s = self._states(states)
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(vars, np.int64), (len(s),)))
+        out = np.zeros(len(s))
+        check(load().qio_states_cost_difference(self._h, len(s), _ptr(s, C.c_uint8),
+                                                _ptr(v, C.c_int64), _ptr(out, C.c_double),
+                                                stream))
+        return out
+
+    def apply_transition(self, states, vars) -> np.ndarray:
+        s = self._states(states).copy()
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(vars, np.int64), (len(s),)))
+        check(load().qio_states_apply(self._h, len(s), _ptr(s, C.c_uint8), _ptr(v, C.c_int64)))
+        return s
+
+
+class Solver:
+    def __init__(self, model: Model, target: str, params: dict | str):
+        if not isinstance(params, str):
+            params = json.dumps(params if "params" in params else {"params": params})
+        self.model = model
+        h = C.c_void_p()
+        check(load().qio_solver_create(model._h, target.encode(), params.encode(), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().qio_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, stream=None):
+        check(load().qio_solver_init(self._h, stream))
+        return self
+
+    def run(self, stream=None):
+        check(load().qio_solver_run(self._h, stream))
+        return self
+
+    def result(self) -> dict:
+        p = C.c_void_p()
+        L = load()
+        check(L.qio_solver_result_json(self._h, C.byref(p)))
+        try:
+            return json.loads(C.string_at(p).decode())
+        finally:
+            L.qio_free(p)
+
+    def replicas(self, states: bool = True) -> dict:
+        L = load()
+        n = C.c_int64(0)
+        check(L.qio_solver_replicas(self._h, C.byref(n), None, None, None, None, None, None))
+        n = n.value
+        N = self.model.n_vars
+        out = {"cost": np.zeros(n), "lowest": np.zeros(n),
+               "attempts": np.zeros(n, np.uint64), "accepts": np.zeros(n, np.uint64)}
+        ls = np.zeros((n, N), np.uint8) if states else None
+        st = np.zeros((n, N), np.uint8) if states else None
+        nn = C.c_int64(0)
+        check(L.qio_solver_replicas(
+            self._h, C.byref(nn), _ptr(out["cost"], C.c_double), _ptr(out["lowest"], C.c_double),
+            _ptr(out["attempts"], C.c_uint64), _ptr(out["accepts"], C.c_uint64),
+            _ptr(ls, C.c_uint8) if states and n and N else None,
+            _ptr(st, C.c_uint8) if states and n and N else None))
+        if states:
+            out["lowest_states"] = ls
+            out["states"] = st
+        return out
+
+    def best(self):
+        c = C.c_double(0)
+        s = np.zeros(max(self.model.n_vars, 1), np.uint8)
+        check(load().qio_solver_best(self._h, C.byref(c), _ptr(s, C.c_uint8)))
+        return c.value, s[:self.model.n_vars]
+
+    def stats(self) -> SolverStats:
+        s = SolverStats()
+        check(load().qio_solver_get_stats(self._h, C.byref(s)))
+        return s
+
+    def pt_observables(self) -> np.ndarray:
+        n = self.stats().replicas
+        out = np.zeros((n, 5))
+        if n:
+            check(load().qio_solver_pt_observables(self._h, _ptr(out, C.c_double)))
+        return out
+
+
+def run_json(input_json, params_json, target: str) -> dict:
+    """app::Runner::run: model JSON + params JSON + target -> result dict."""
+    if not isinstance(input_json, str):
+        input_json = json.dumps(input_json)
+    if not isinstance(params_json, str):
+        params_json = json.dumps(params_json)
+    L = load()
+    p = C.c_void_p()
+    check(L.qio_run_json(input_json.encode(), params_json.encode(), target.encode(), C.byref(p)))
+    try:
+        return json.loads(C.string_at(p).decode())
+    finally:
+        L.qio_free(p)

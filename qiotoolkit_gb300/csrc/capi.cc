@@ -1,0 +1,330 @@
+// capi.cc -- extern "C" entry points declared in include/qio_gb300.h.
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/qio_gb300.h"
+#include "host.h"
+
+using namespace qio;
+
+struct qio_model
+{
+  std::unique_ptr<HostModel> m;
+};
+struct qio_solver
+{
+  std::unique_ptr<Solver> s;
+  const qio_model* model = nullptr;
+};
+
+static thread_local std::string g_last_error;
+
+template <class F>
+static qio_status guard(F&& f)
+{
+  try
+  {
+    f();
+    g_last_error.clear();
+    return QIO_OK;
+  }
+  catch (const Error& e)
+  {
+    g_last_error = e.what();
+    return (qio_status)e.status;
+  }
+  catch (const std::bad_alloc&)
+  {
+    g_last_error = "host out of memory";
+    return QIO_OUT_OF_MEMORY;
+  }
+  catch (const std::exception& e)
+  {
+    g_last_error = e.what();
+    return QIO_INVALID_ARGUMENT;
+  }
+}
+
+static cudaStream_t as_stream(void* s) { return (cudaStream_t)s; }
+
+static char* dup_string(const std::string& s)
+{
+  char* p = (char*)malloc(s.size() + 1);
+  if (!p) throw std::bad_alloc();
+  memcpy(p, s.c_str(), s.size() + 1);
+  return p;
+}
+
+extern "C" {
+
+const char* qio_last_error_message(void) { return g_last_error.c_str(); }
+const char* qio_version(void) { return "qio_gb300 1.0 (sm_103a)"; }
+void qio_free(void* p) { free(p); }
+
+qio_status qio_model_create(int32_t kind, int64_t n_terms, const int64_t* term_offsets,
+                            const int32_t* term_ids, const double* coefficients,
+                            qio_model** out)
+{
+  return guard([&] {
+    if (!out) fail(1, "out must not be null");
+    *out = nullptr;
+    std::unique_ptr<qio_model> h(new qio_model());
+    h->m = build_model(kind, n_terms, term_offsets, term_ids, coefficients);
+    *out = h.release();
+  });
+}
+
+qio_status qio_model_create_json(const char* input_json, int32_t kind, qio_model** out)
+{
+  return guard([&] {
+    if (!out || !input_json) fail(1, "arguments must not be null");
+    *out = nullptr;
+    json::Value doc = json::parse(input_json, strlen(input_json));
+    std::unique_ptr<qio_model> h(new qio_model());
+    h->m = build_model_json(doc, kind);
+    *out = h.release();
+  });
+}
+
+qio_status qio_model_get_info(const qio_model* model, qio_model_info* out)
+{
+  return guard([&] {
+    if (!model || !out) fail(1, "arguments must not be null");
+    const HostModel& m = *model->m;
+    out->kind = m.kind;
+    out->integer_weights = m.int_mode ? 1 : 0;
+    out->n_vars = m.N;
+    out->n_terms = m.M;
+    out->n_incidences = m.K;
+    out->max_locality = m.max_loc;
+    out->min_locality = m.min_loc;
+    out->const_cost = m.const_cost;
+    out->scale_factor = m.scale_factor;
+    out->max_coupling = m.max_coupling;
+    out->device_bytes = (int64_t)(m.row.size() * 4 + m.inc.size() * 4 + m.coef.size() * 8 +
+                                  m.coef_i.size() * 4 + m.nbr.size() * 4 + m.trow.size() * 4 +
+                                  m.tvar.size() * 4 + m.tcost.size() * 8 + m.tcost_i.size() * 4);
+  });
+}
+
+qio_status qio_model_get_var_names(const qio_model* model, int32_t* names)
+{
+  return guard([&] {
+    if (!model || !names) fail(1, "arguments must not be null");
+    const HostModel& m = *model->m;
+    if (!m.names.empty()) memcpy(names, m.names.data(), m.names.size() * 4);
+  });
+}
+
+qio_status qio_model_destroy(qio_model* model)
+{
+  return guard([&] { delete model; });
+}
+
+static void pack_states(const HostModel& m, int64_t n, const uint8_t* states,
+                        std::vector<uint32_t>& words, int& nw)
+{
+  nw = (int)((m.N + 31) / 32);
+  if (nw == 0) nw = 1;
+  words.assign((size_t)n * nw, 0);
+  for (int64_t q = 0; q < n; q++)
+    for (int64_t v = 0; v < m.N; v++)
+      if (states[q * m.N + v]) words[q * nw + v / 32] |= 1u << (v % 32);
+}
+
+qio_status qio_states_cost(const qio_model* model, int64_t n, const uint8_t* states,
+                           double* costs, void* stream)
+{
+  return guard([&] {
+    if (!model || (n > 0 && (!states || !costs))) fail(1, "arguments must not be null");
+    const HostModel& m = *model->m;
+    if (n <= 0) return;
+    if (m.empty())
+    {
+      for (int64_t q = 0; q < n; q++) costs[q] = 0.0;
+      return;
+    }
+    ensure_device();
+    std::vector<uint32_t> words;
+    int nw;
+    pack_states(m, n, states, words, nw);
+    DevBuf d(words.size() * 4 + (size_t)n * 8);
+    cudaStream_t s = as_stream(stream);
+    cuda_check(cudaMemcpyAsync(d.ptr, words.data(), words.size() * 4, cudaMemcpyHostToDevice, s), "H2D");
+    double* out = (double*)((char*)d.ptr + words.size() * 4);
+    cuda_check(launch_eval_cost(m.device(), (int)n, (const uint32_t*)d.ptr, nw, out, s), "cost kernel");
+    cuda_check(cudaMemcpyAsync(costs, out, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "sync");
+  });
+}
+
+qio_status qio_states_cost_difference(const qio_model* model, int64_t n, const uint8_t* states,
+                                      const int64_t* vars, double* diffs, void* stream)
+{
+  return guard([&] {
+    if (!model || (n > 0 && (!states || !vars || !diffs))) fail(1, "arguments must not be null");
+    const HostModel& m = *model->m;
+    if (n <= 0) return;
+    for (int64_t q = 0; q < n; q++)
+      if (vars[q] < 0 || vars[q] >= m.N)
+        fail(1, "transition " + std::to_string(vars[q]) + " out of range [0, " + std::to_string(m.N) + ")");
+    ensure_device();
+    std::vector<uint32_t> words;
+    int nw;
+    pack_states(m, n, states, words, nw);
+    size_t wb = (words.size() * 4 + 255) & ~(size_t)255;
+    DevBuf d(wb + (size_t)n * 16);
+    cudaStream_t s = as_stream(stream);
+    long long* dv = (long long*)((char*)d.ptr + wb);
+    double* out = (double*)((char*)d.ptr + wb + (size_t)n * 8);
+    cuda_check(cudaMemcpyAsync(d.ptr, words.data(), words.size() * 4, cudaMemcpyHostToDevice, s), "H2D");
+    cuda_check(cudaMemcpyAsync(dv, vars, (size_t)n * 8, cudaMemcpyHostToDevice, s), "H2D");
+    cuda_check(launch_eval_diff(m.device(), (int)n, (const uint32_t*)d.ptr, nw, dv, out, s), "diff kernel");
+    cuda_check(cudaMemcpyAsync(diffs, out, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    cuda_check(cudaStreamSynchronize(s), "sync");
+  });
+}
+
+qio_status qio_states_apply(const qio_model* model, int64_t n, uint8_t* states, const int64_t* vars)
+{
+  return guard([&] {
+    if (!model || (n > 0 && (!states || !vars))) fail(1, "arguments must not be null");
+    const HostModel& m = *model->m;
+    for (int64_t q = 0; q < n; q++)
+    {
+      if (vars[q] < 0 || vars[q] >= m.N) fail(1, "transition out of range");
+      states[q * m.N + vars[q]] ^= 1;
+    }
+  });
+}
+
+qio_status qio_solver_create(const qio_model* model, const char* target, const char* params_json,
+                             qio_solver** out)
+{
+  return guard([&] {
+    if (!model || !target || !params_json || !out) fail(1, "arguments must not be null");
+    *out = nullptr;
+    json::Value doc = json::parse(params_json, strlen(params_json));
+    std::unique_ptr<qio_solver> h(new qio_solver());
+    h->s = make_solver(model->m.get(), target, doc);
+    h->model = model;
+    *out = h.release();
+  });
+}
+
+qio_status qio_solver_init(qio_solver* s, void* stream)
+{
+  return guard([&] {
+    if (!s) fail(1, "solver must not be null");
+    s->s->init(as_stream(stream));
+  });
+}
+
+qio_status qio_solver_run(qio_solver* s, void* stream)
+{
+  return guard([&] {
+    if (!s) fail(1, "solver must not be null");
+    s->s->run(as_stream(stream));
+    cuda_check(cudaStreamSynchronize(as_stream(stream)), "sync");
+    cuda_check(cudaGetLastError(), "run");
+  });
+}
+
+qio_status qio_solver_result_json(qio_solver* s, char** out_json)
+{
+  return guard([&] {
+    if (!s || !out_json) fail(1, "arguments must not be null");
+    *out_json = dup_string(s->s->result_json());
+  });
+}
+
+qio_status qio_solver_replicas(qio_solver* s, int64_t* n, double* cost, double* lowest,
+                               uint64_t* attempts, uint64_t* accepts, uint8_t* lowest_states,
+                               uint8_t* states)
+{
+  return guard([&] {
+    if (!s || !n) fail(1, "arguments must not be null");
+    std::vector<double> c, l;
+    std::vector<uint64_t> at, ac;
+    std::vector<uint8_t> ls, st;
+    s->s->fetch(c, l, at, ac, lowest_states ? &ls : nullptr, states ? &st : nullptr);
+    *n = (int64_t)c.size();
+    if (cost && !c.empty()) memcpy(cost, c.data(), c.size() * 8);
+    if (lowest && !l.empty()) memcpy(lowest, l.data(), l.size() * 8);
+    if (attempts && !at.empty()) memcpy(attempts, at.data(), at.size() * 8);
+    if (accepts && !ac.empty()) memcpy(accepts, ac.data(), ac.size() * 8);
+    if (lowest_states && !ls.empty()) memcpy(lowest_states, ls.data(), ls.size());
+    if (states && !st.empty()) memcpy(states, st.data(), st.size());
+  });
+}
+
+qio_status qio_solver_best(qio_solver* s, double* cost, uint8_t* state)
+{
+  return guard([&] {
+    if (!s || !cost) fail(1, "arguments must not be null");
+    std::vector<uint8_t> st;
+    s->s->best(*cost, st);
+    if (state && !st.empty()) memcpy(state, st.data(), st.size());
+  });
+}
+
+qio_status qio_solver_get_stats(qio_solver* s, qio_solver_stats* out)
+{
+  return guard([&] {
+    if (!s || !out) fail(1, "arguments must not be null");
+    Solver& v = *s->s;
+    std::vector<double> c, l;
+    std::vector<uint64_t> at, ac;
+    v.fetch(c, l, at, ac, nullptr, nullptr);
+    out->replicas = (int64_t)c.size();
+    out->last_step = v.last_step;
+    out->attempts = 0;
+    out->accepts = 0;
+    for (size_t i = 0; i < at.size(); i++)
+    {
+      out->attempts += at[i];
+      out->accepts += ac[i];
+    }
+    out->kernel_launches = v.launches;
+    out->sweep_kernel_ms = v.sweep_ms;
+    out->run_ms = v.run_ms;
+    out->near_ties = v.near_ties;
+    out->device_bytes = v.device_bytes;
+  });
+}
+
+qio_status qio_solver_pt_observables(qio_solver* s, double* out5)
+{
+  return guard([&] {
+    if (!s || !out5) fail(1, "arguments must not be null");
+    std::vector<double> o;
+    s->s->pt_observables(o);
+    if (!o.empty()) memcpy(out5, o.data(), o.size() * 8);
+  });
+}
+
+qio_status qio_solver_destroy(qio_solver* s)
+{
+  return guard([&] { delete s; });
+}
+
+qio_status qio_run_json(const char* input_json, const char* params_json, const char* target,
+                        char** out_json)
+{
+  return guard([&] {
+    if (!input_json || !params_json || !target || !out_json) fail(1, "arguments must not be null");
+    *out_json = nullptr;
+    json::Value doc = json::parse(input_json, strlen(input_json));
+    std::unique_ptr<HostModel> m = build_model_json(doc, -1);
+    json::Value pdoc = json::parse(params_json, strlen(params_json));
+    std::unique_ptr<Solver> s = make_solver(m.get(), target, pdoc);
+    cudaStream_t st = 0;
+    s->init(st);
+    s->run(st);
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    *out_json = dup_string(s->result_json());
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// host.h -- host-side model and solver objects behind the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "json.h"
+#include "qio_internal.h"
+
+namespace qio
+{
+// Errors carry the C-ABI status they map to.
+struct Error : std::runtime_error
+{
+  int status;
+  Error(int st, const std::string& m) : std::runtime_error(m), status(st) {}
+};
+[[noreturn]] void fail(int status, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+
+// Device buffer owned by RAII.
+struct DevBuf
+{
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() {}
+  explicit DevBuf(size_t n);
+  ~DevBuf();
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : ptr(o.ptr), bytes(o.bytes)
+  {
+    o.ptr = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept;
+  template <class T> T* as() const { return (T*)ptr; }
+};
+
+void ensure_device();  // selects the device, uploads tables once per device
+
+struct HostModel
+{
+  int kind = K_ISING;
+  int flavor = F_PARITY;
+  int64_t N = 0, M = 0, K = 0;
+  // variable -> incident terms (ascending term id), incidence payloads
+  std::vector<int> row;
+  std::vector<uint32_t> inc;
+  std::vector<double> coef;
+  std::vector<int> coef_i;
+  std::vector<uint32_t> nbr;
+  // term -> members
+  std::vector<int> trow;
+  std::vector<uint32_t> tvar;
+  std::vector<double> tcost;
+  std::vector<int> tcost_i;
+  double const_cost = 0, max_coupling = 0, scale_factor = 1.0;
+  int max_loc = 0, min_loc = 0;
+  std::vector<int32_t> names;  // internal id -> input name
+  std::vector<int32_t> free_vars;  // MaxSat free variables
+  bool int_mode = false;
+  // device copy, made on first use (model construction needs no GPU)
+  mutable DevBuf dmem;
+  mutable DevModel dev{};
+  mutable bool uploaded = false;
+
+  bool empty() const { return N == 0; }
+  void upload() const;
+  const DevModel& device() const
+  {
+    if (!uploaded) upload();
+    return dev;
+  }
+  DevModel device_view(bool full_maxsat_sweep) const;
+};
+
+// Build from the raw term list (reference input order).
+std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
+                                       const int64_t* off, const int32_t* ids,
+                                       const double* coef);
+std::unique_ptr<HostModel> build_model_json(const json::Value& doc, int kind);
+
+// Schedule (schedule/schedule.cc, linear.cc, geometric.cc, segments.cc).
+struct Schedule
+{
+  int type = 0;  // 0 linear, 1 geometric, 2 constant, 3 list
+  double initial = 0, final_ = 0;
+  bool has_start = false, has_stop = false, has_count = false;
+  double start_ = 0, stop_ = 1;
+  int count_ = 1;
+  std::vector<double> values;
+  double progress_value(double p) const;
+  double get_start() const;
+  double get_stop() const;
+  int get_count() const;
+  double get_value(double input) const;
+  std::vector<double> discretized() const;
+  std::string render() const;
+};
+Schedule parse_schedule(const json::Value& v, const std::string& name);
+
+class Solver;
+std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& target,
+                                    const json::Value& params_doc);
+
+class Solver
+{
+ public:
+  virtual ~Solver() {}
+  virtual void init(cudaStream_t s) = 0;
+  virtual void run(cudaStream_t s) = 0;
+  // results
+  virtual int64_t n_walkers() const = 0;
+  virtual void fetch(std::vector<double>& cost, std::vector<double>& lowest,
+                     std::vector<uint64_t>& att, std::vector<uint64_t>& acc,
+                     std::vector<uint8_t>* lowest_states,
+                     std::vector<uint8_t>* states) = 0;
+  virtual void pt_observables(std::vector<double>& out) { out.clear(); }
+  // lowest state ever seen by a population solver (it may have died)
+  virtual bool historical_lowest(double&, std::vector<uint8_t>&) { return false; }
+  virtual std::string target() const = 0;
+  std::string result_json();
+  void best(double& cost, std::vector<uint8_t>& state);
+
+  const HostModel* model = nullptr;
+  json::Value params;            // the "params" object as given
+  std::vector<std::pair<std::string, std::string>> output_params;  // rendered
+  uint32_t seed = 0;
+  int64_t step_limit = 10000;
+  int64_t last_step = 0;
+  bool has_cost_limit = false;
+  double cost_limit = 0;
+  bool has_time_limit = false;
+  double time_limit = 0;
+  int threads = 1;
+  int number_of_solutions = 1;
+  bool replay = true;
+  bool full_maxsat_sweep = false;
+  int warps_per_block = 0;  // 0: pick from the walker count
+  uint64_t launches = 0;
+  double sweep_ms = 0, run_ms = 0;
+  uint64_t near_ties = 0;
+  int64_t device_bytes = 0;
+  bool initialized = false, ran = false;
+  bool profile = false;  // bracket every sweep launch with CUDA events
+  // CUDA-event pairs around sweep launches (profile mode)
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
+  size_t prof_used = 0;
+  void prof_begin(cudaStream_t s);
+  void prof_end(cudaStream_t s);
+  double prof_total_ms();  // synchronises; resets the pairs
+};
+}  // namespace qio

@@ -1,0 +1,940 @@
+// kernels.cu -- sm_103a kernels of the Metropolis hot path.
+//
+// The ordered sweep of the reference (markov/walker.h:143-153) is a strictly
+// sequential chain: attempt i reads the state left by attempt i-1.  One warp
+// owns one walker and evaluates a WINDOW of 32 consecutive variables at once
+// (lane l takes variable i+l), each lane summing its own cost difference in
+// the reference's term order (bit-identical FP64).  Decisions are then
+// committed in lane order up to the first lane whose terms intersect an
+// earlier accepted flip in the window (its difference was computed on a
+// stale state) or that needs the Metropolis redraw path; the next window
+// starts there.  Replay streams are PCG32 positions: lane l's draw is the
+// stream advanced by the number of uphill lanes before it (an LCG jump), so
+// the committed prefix consumes exactly the draws the sequential chain would.
+// The result is the reference's trajectory, evaluated up to 32-wide.
+#include <cstdio>
+
+#include "qio_internal.h"
+
+namespace qio
+{
+static const unsigned kFull = 0xffffffffu;
+static const unsigned long long kMult = 6364136223846793005ULL;
+static const unsigned long long kInc = 1442695040888963407ULL;
+static const unsigned long long kGamma = 0x9E3779B97F4A7C15ULL;
+static const unsigned long long kInitCounterBase = 1ULL << 62;
+
+// ln table (utils/utils.cc:12-32, computed on the host with the C library's
+// log) and LCG jump tables: k steps (k = 0..64) and 2^k steps.
+__constant__ double c_ln[1024];
+__constant__ unsigned long long c_jA[65], c_jC[65];
+__constant__ unsigned long long c_pA[64], c_pC[64];
+
+__device__ __forceinline__ uint32_t pcg_out(uint64_t old)
+{
+  uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+  uint32_t rot = (uint32_t)(old >> 59u);
+  return __funnelshift_r(xs, xs, rot);
+}
+
+__device__ __forceinline__ uint64_t jump_any(uint64_t s, unsigned long long k)
+{
+  for (int b = 0; k; b++, k >>= 1)
+    if (k & 1ULL) s = c_pA[b] * s + c_pC[b];
+  return s;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint64_t counter_key(uint32_t seed, uint64_t stream)
+{
+  return mix64(((uint64_t)seed << 32) ^ mix64(stream + kGamma));
+}
+__device__ __forceinline__ uint64_t counter_draw(uint64_t key, uint64_t ctr)
+{
+  return mix64(key + ctr * kGamma);
+}
+
+// libstdc++ generate_canonical<double,53> over a 32-bit engine: two draws,
+// sum = a + b * 2^32 rounded once, divided by 2^64, clamped below 1.
+__device__ __forceinline__ double canonical(uint32_t a, uint32_t b)
+{
+  double s = __dadd_rn((double)a, __dmul_rn((double)b, 4294967296.0));
+  double u = __dmul_rn(s, 5.421010862427522170037e-20);  // 2^-64
+  if (u >= 1.0) u = 0.99999999999999988898;              // nextafter(1, 0)
+  return u;
+}
+
+// value < -dE * beta with value interpolated in ln[row] at bucket r & 255,
+// distance (r >> 8) / 16777214 (markov/metropolis.h:96-103).  Explicit _rn
+// intrinsics keep the reference's rounding (no fused multiply-add).
+__device__ __forceinline__ bool lut_less(const double* ln, uint32_t r, int row,
+                                         double thr)
+{
+  int b = (int)(r & 255u);
+  double y0 = ln[row * 256 + b - 1];
+  double y1 = ln[row * 256 + b];
+  double dist = __ddiv_rn((double)(r >> 8), 16777214.0);
+  double value = __dadd_rn(y0, __dmul_rn(dist, __dsub_rn(y1, y0)));
+  return value < thr;
+}
+
+// Metropolis::accept (markov/metropolis.h:64-104) for an uphill move with
+// the draws supplied by `draw(k)`; `used` receives the draw count.
+template <class F>
+__device__ __forceinline__ bool metropolis_uphill(double thr, const double* ln,
+                                                  F draw, int& used)
+{
+  int row = -1, b = 0;
+  uint32_t cur = 0;
+  used = 0;
+  while (b == 0)
+  {
+    if (row < 3)
+    {
+      cur = draw(used);
+      used++;
+      b = (int)(cur & 255u);
+      row++;
+    }
+    else
+      return true;
+  }
+  return lut_less(ln, cur, row, thr);
+}
+
+__device__ __forceinline__ uint32_t spin_of(const uint32_t* spins, int v)
+{
+  return (spins[v >> 5] >> (v & 31)) & 1u;
+}
+
+// Value of term t under `spins` for the full cost (calculate_cost) and a
+// skip flag for counter models (terms that do not contribute are skipped,
+// as the reference does, rather than added as 0).
+template <int FL, bool INT>
+__device__ __forceinline__ void term_value(const DevModel& m,
+                                           const uint32_t* spins, int t,
+                                           double& val, long long& ival,
+                                           bool& skip)
+{
+  int b = m.trow[t], e = m.trow[t + 1];
+  if (FL == F_PARITY || FL == F_PLAIN_ISING)
+  {
+    uint32_t par = 0;
+    for (int k = b; k < e; k++) par ^= spin_of(spins, (int)(m.tvar[k] & ~kNegBit));
+    skip = false;
+    if (INT) ival = par ? -(long long)m.tcost_i[t] : (long long)m.tcost_i[t];
+    else val = par ? -m.tcost[t] : m.tcost[t];
+  }
+  else
+  {
+    // counter: number of true literals; the term contributes when it is 0
+    int cnt = 0;
+    for (int k = b; k < e; k++)
+    {
+      uint32_t x = m.tvar[k];
+      cnt += (int)(spin_of(spins, (int)(x & ~kNegBit)) ^ (x >> 31));
+    }
+    skip = cnt != 0;
+    if (INT) ival = skip ? 0 : (long long)m.tcost_i[t];
+    else val = skip ? 0.0 : m.tcost[t];
+  }
+}
+
+// Sum of term values in term order by one warp: lanes evaluate 32 terms in
+// parallel, the sum itself runs sequentially (bit-identical to a loop).
+template <int FL, bool INT>
+__device__ void warp_cost(const DevModel& m, const uint32_t* spins, int lane,
+                          double& cost, long long& icost)
+{
+  double c = 0.0;
+  long long ic = 0;
+  for (int t0 = 0; t0 < m.n_terms; t0 += 32)
+  {
+    int t = t0 + lane;
+    double v = 0.0;
+    long long iv = 0;
+    bool skip = true;
+    if (t < m.n_terms) term_value<FL, INT>(m, spins, t, v, iv, skip);
+    unsigned keep = __ballot_sync(kFull, !skip);
+    while (keep)
+    {
+      int j = __ffs(keep) - 1;
+      keep &= keep - 1;
+      if (INT) ic += __shfl_sync(kFull, iv, j);
+      else c = __dadd_rn(c, __shfl_sync(kFull, v, j));
+    }
+  }
+  cost = c;
+  icost = ic;
+}
+
+// Term state byte from spins: parity (Ising) or true-literal count.
+template <int FL>
+__device__ __forceinline__ uint8_t term_state(const DevModel& m,
+                                              const uint32_t* spins, int t)
+{
+  int b = m.trow[t], e = m.trow[t + 1];
+  uint32_t acc = 0;
+  for (int k = b; k < e; k++)
+  {
+    uint32_t x = m.tvar[k];
+    uint32_t s = spin_of(spins, (int)(x & ~kNegBit));
+    if (FL == F_PARITY) acc ^= s;
+    else acc += s ^ (x >> 31);
+  }
+  return (uint8_t)acc;
+}
+
+// ---------------------------------------------------------------------------
+// init: random (or given) state, term cache, cost, lowest = current.
+// Walker::init (markov/walker.h:50-58) with get_random_spin_state /
+// get_random_binary_state (model/ising.h:23-41, model/pubo.h:16-34) or the
+// MaxSat per-variable uniform() < 0.5 (model/max_sat.h:144-150).
+// ---------------------------------------------------------------------------
+template <int FL, bool INT>
+__global__ void __launch_bounds__(128) init_kernel(InitArgs a)
+{
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= a.n_walkers) return;
+  const DevModel& m = a.m;
+  const int N = m.n_vars;
+  const int nwd = (N + 31) >> 5;
+  const int slot = a.slot_of ? a.slot_of[w] : w;
+  uint32_t* spins = a.p.spins + (size_t)slot * a.p.nw;
+  uint8_t* ts = a.p.tstate + (size_t)slot * a.p.mp;
+  uint32_t* lsp = a.p.lspins + (size_t)w * a.p.nw;
+  // a.replay: 0 counter, 1 PCG replay (one draw per 32 variables);
+  // 2 PCG replay / 3 counter with one uniform() per variable (MaxSat)
+  const bool var_uniform = (a.replay == 2 || a.replay == 3);
+  const bool replay = (a.replay == 1 || a.replay == 2);
+  uint64_t key = 0;
+  if (!replay)
+    key = counter_key(a.seed + (uint32_t)(w / a.key_div),
+                      a.key_base + (unsigned long long)(w % a.key_div));
+  uint64_t rs = replay ? a.rng[w] : 0;
+  for (int q0 = 0; q0 < nwd; q0 += 32)
+  {
+    int q = q0 + lane;
+    uint32_t word = 0;
+    if (a.given)
+    {
+      if (q < nwd)
+        for (int b = 0; b < 32; b++)
+        {
+          int v = q * 32 + b;
+          if (v < N && a.given[(size_t)w * N + v]) word |= 1u << b;
+        }
+    }
+    else if (!var_uniform)
+    {
+      if (q < nwd)
+      {
+        if (replay) word = pcg_out(jump_any(rs, (unsigned long long)q));
+        else word = (uint32_t)counter_draw(key, kInitCounterBase + (unsigned long long)q);
+      }
+    }
+    else
+    {
+      // MaxSat: bit b of word q0+j is variable 32*(q0+j)+b; lanes take one
+      // variable each, 32 words per pass
+      for (int j = 0; j < 32 && q0 + j < nwd; j++)
+      {
+        int v = (q0 + j) * 32 + lane;
+        bool bit = false;
+        if (v < N)
+        {
+          if (replay)
+          {
+            uint64_t s0 = jump_any(rs, 2ULL * (unsigned long long)v);
+            uint32_t d0 = pcg_out(s0);
+            uint32_t d1 = pcg_out(s0 * kMult + kInc);
+            bit = canonical(d0, d1) < 0.5;
+          }
+          else
+            bit = (counter_draw(key, kInitCounterBase + (unsigned long long)v) >> 63) == 0;
+        }
+        unsigned bw = __ballot_sync(kFull, bit);
+        if (lane == j) word = bw;
+      }
+    }
+    if (q < nwd)
+    {
+      if (q == nwd - 1 && (N & 31)) word &= (1u << (N & 31)) - 1u;
+      spins[q] = word;
+    }
+  }
+  for (int q = nwd + lane; q < a.p.nw; q += 32) spins[q] = 0;
+  if (replay && lane == 0)
+    a.rng[w] = jump_any(rs, var_uniform ? 2ULL * (unsigned long long)N
+                                        : (unsigned long long)nwd);
+  __syncwarp();
+  if (FL == F_PARITY || FL == F_COUNTER)
+    for (int t = lane; t < m.n_terms; t += 32) ts[t] = term_state<FL>(m, spins, t);
+  double cost;
+  long long icost;
+  warp_cost<FL, INT>(m, spins, lane, cost, icost);
+  if (INT) cost = (double)icost;
+  for (int q = lane; q < a.p.nw; q += 32) lsp[q] = spins[q];
+  if (lane == 0)
+  {
+    a.p.cost[slot] = cost;
+    a.p.lowest[w] = cost;
+    a.p.attempts[w] = 0;
+    a.p.accepts[w] = 0;
+    a.p.step_att[w] = 0;
+    a.p.step_acc[w] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Windowed sweep.
+// ---------------------------------------------------------------------------
+template <int FL, bool REPLAY, bool INT>
+__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a)
+{
+  __shared__ double s_ln[1024];
+  __shared__ unsigned long long s_A[65], s_C[65];
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) s_ln[t] = c_ln[t];
+  for (int t = threadIdx.x; t < 65; t += blockDim.x)
+  {
+    s_A[t] = c_jA[t];
+    s_C[t] = c_jC[t];
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= a.n_streams) return;
+  const DevModel m = a.m;
+  const int S = m.sweep_size;
+  const int nwd = (m.n_vars + 31) >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  uint64_t rs = REPLAY ? a.rng[w] : 0;
+
+  for (int r = w; r < a.n_walkers; r += a.n_streams)
+  {
+    const int slot = a.slot_of ? a.slot_of[r] : r;
+    uint32_t* spins = a.p.spins + (size_t)slot * a.p.nw;
+    uint8_t* ts = a.p.tstate + (size_t)slot * a.p.mp;
+    uint32_t* lsp = a.p.lspins + (size_t)r * a.p.nw;
+    double cost = a.p.cost[slot];
+    double low = a.p.lowest[r];
+    long long icost = INT ? (long long)cost : 0;
+    long long ilow = INT ? (long long)low : 0;
+    unsigned long long natt = 0, nacc = 0;
+    uint64_t key = 0;
+    if (!REPLAY)
+      key = counter_key(a.seed + (uint32_t)(r / a.key_div),
+                        a.key_base + (unsigned long long)(r % a.key_div));
+
+    for (int k = 0; k < a.n_sweeps; k++)
+    {
+      const long long sw = a.sweep_base + k;
+      const double beta = a.beta[(long long)r * a.bs_w + sw * a.bs_s];
+      const double nbeta = -beta;
+      const unsigned long long ctr0 = (unsigned long long)sw * (unsigned long long)S;
+      int i = 0;
+      while (i < S)
+      {
+        const int v = i + lane;
+        const bool valid = v < S;
+        double dE = 0.0;
+        long long idE = 0;
+        int rb = 0, re = 0;
+        uint32_t sv = 0;
+        if (valid)
+        {
+          rb = m.row[v];
+          re = m.row[v + 1];
+          sv = spin_of(spins, v);
+          if (FL == F_PARITY)
+          {
+            if (INT)
+            {
+              int acc = 0;
+#pragma unroll 4
+              for (int q = rb; q < re; q++)
+              {
+                uint32_t t = m.inc[q];
+                int c = m.coef_i[q];
+                acc += ts[t] ? -c : c;
+              }
+              idE = -2 * (long long)acc;
+            }
+            else
+            {
+              double diff = 0.0;
+#pragma unroll 4
+              for (int q = rb; q < re; q++)
+              {
+                uint32_t t = m.inc[q];
+                double c = m.coef[q];
+                diff = __dadd_rn(diff, ts[t] ? -c : c);
+              }
+              dE = __dmul_rn(2.0, -diff);
+            }
+          }
+          else if (FL == F_COUNTER)
+          {
+            if (INT)
+            {
+              int acc = 0;
+#pragma unroll 4
+              for (int q = rb; q < re; q++)
+              {
+                uint32_t e = m.inc[q];
+                uint8_t z = ts[e & ~kNegBit];
+                int c = m.coef_i[q];
+                if (sv ^ (e >> 31)) { if (z == 1) acc += c; }
+                else { if (z == 0) acc -= c; }
+              }
+              idE = acc;
+            }
+            else
+            {
+              double diff = 0.0;
+#pragma unroll 4
+              for (int q = rb; q < re; q++)
+              {
+                uint32_t e = m.inc[q];
+                uint8_t z = ts[e & ~kNegBit];
+                double c = m.coef[q];
+                if (sv ^ (e >> 31)) { if (z == 1) diff = __dadd_rn(diff, c); }
+                else { if (z == 0) diff = __dsub_rn(diff, c); }
+              }
+              dE = diff;
+            }
+          }
+          else
+          {
+            // plain models: gather the members of each incident term
+            double diff = 0.0;
+            long long iacc = 0;
+            for (int q = rb; q < re; q++)
+            {
+              int t = (int)m.inc[q];
+              int tb = m.trow[t], te = m.trow[t + 1];
+              if (FL == F_PLAIN_ISING)
+              {
+                uint32_t par = 0;
+                for (int u = tb; u < te; u++) par ^= spin_of(spins, (int)m.tvar[u]);
+                if (INT) iacc += par ? -(long long)m.coef_i[q] : (long long)m.coef_i[q];
+                else diff = __dadd_rn(diff, par ? -m.coef[q] : m.coef[q]);
+              }
+              else
+              {
+                bool zero = false;
+                for (int u = tb; u < te; u++)
+                {
+                  int x = (int)m.tvar[u];
+                  if (x != v && spin_of(spins, x)) { zero = true; break; }
+                }
+                if (!zero)
+                {
+                  if (INT) iacc += sv ? (long long)m.coef_i[q] : -(long long)m.coef_i[q];
+                  else diff = __dadd_rn(diff, sv ? m.coef[q] : -m.coef[q]);
+                }
+              }
+            }
+            if (FL == F_PLAIN_ISING)
+            {
+              if (INT) idE = -2 * iacc;
+              else dE = __dmul_rn(2.0, -diff);
+            }
+            else
+            {
+              if (INT) idE = iacc;
+              else dE = diff;
+            }
+          }
+          if (INT) dE = (double)idE;
+        }
+
+        // ---- acceptance --------------------------------------------------
+        const bool uphill = valid && !(dE <= 0.0);
+        bool acc = valid && !uphill;
+        bool redraw = false;
+        unsigned U = 0;
+        int pos = 0;
+        if (REPLAY)
+        {
+          U = __ballot_sync(kFull, uphill);
+          pos = __popc(U & lt);
+          if (uphill)
+          {
+            uint32_t r0 = pcg_out(s_A[pos] * rs + s_C[pos]);
+            redraw = (r0 & 255u) == 0;
+            if (!redraw) acc = lut_less(s_ln, r0, 0, __dmul_rn(dE, nbeta));
+          }
+        }
+        else if (uphill)
+        {
+          const unsigned long long ctr = ctr0 + (unsigned long long)v;
+          uint64_t w0 = counter_draw(key, 2ULL * ctr);
+          int used;
+          acc = metropolis_uphill(
+              __dmul_rn(dE, nbeta), s_ln,
+              [&](int q) -> uint32_t {
+                if (q == 0) return (uint32_t)w0;
+                if (q == 1) return (uint32_t)(w0 >> 32);
+                uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
+                return q == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+              },
+              used);
+        }
+        const unsigned A = __ballot_sync(kFull, acc);
+        bool conf = false;
+        if (valid && lane > 0) conf = (m.nbr[v] & (__brev(A) >> (32 - lane))) != 0u;
+        const unsigned Cm = __ballot_sync(kFull, conf);
+        const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
+        const int nvalid = min(32, S - i);
+        const unsigned stop = Cm | Rm;
+        int f = stop ? (__ffs(stop) - 1) : 32;
+        if (f > nvalid) f = nvalid;
+        const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
+        const unsigned commit = (f >= 32) ? kFull : ((1u << f) - 1u);
+        unsigned flips = A & commit;
+        int draws = REPLAY ? __popc(U & commit) : 0;
+        if (REPLAY && slow)
+        {
+          // lane f drew a zero bucket: finish its redraw chain sequentially
+          int sacc = 0, used = 0;
+          if (lane == f)
+          {
+            bool ok = metropolis_uphill(
+                __dmul_rn(dE, nbeta), s_ln,
+                [&](int q) -> uint32_t {
+                  return pcg_out(s_A[pos + q] * rs + s_C[pos + q]);
+                },
+                used);
+            sacc = ok ? 1 : 0;
+          }
+          sacc = __shfl_sync(kFull, sacc, f);
+          used = __shfl_sync(kFull, used, f);
+          if (sacc) flips |= 1u << f;
+          draws += used;
+        }
+        const int adv = f + (slow ? 1 : 0);
+
+        // ---- apply accepted flips (their term sets are disjoint) ----------
+        if ((flips >> lane) & 1u)
+        {
+          if (FL == F_PARITY)
+          {
+            for (int q = rb; q < re; q++) ts[m.inc[q]] ^= (uint8_t)1;
+          }
+          else if (FL == F_COUNTER)
+          {
+            for (int q = rb; q < re; q++)
+            {
+              uint32_t e = m.inc[q];
+              uint32_t t = e & ~kNegBit;
+              ts[t] = (uint8_t)(ts[t] + ((sv ^ (e >> 31)) ? 0xFFu : 1u));
+            }
+          }
+        }
+        const int wi = i >> 5, o = i & 31;
+        if (lane == 0 && flips)
+        {
+          spins[wi] ^= flips << o;
+          if (o)
+          {
+            unsigned hi = flips >> (32 - o);
+            if (hi) spins[wi + 1] ^= hi;
+          }
+        }
+        // ---- running cost and lowest state, in attempt order --------------
+        int lowpos = -1;
+        unsigned fl = flips;
+        while (fl)
+        {
+          const int j = __ffs(fl) - 1;
+          fl &= fl - 1;
+          if (INT)
+          {
+            icost += __shfl_sync(kFull, idE, j);
+            if (icost < ilow)
+            {
+              ilow = icost;
+              lowpos = j;
+            }
+          }
+          else
+          {
+            cost = __dadd_rn(cost, __shfl_sync(kFull, dE, j));
+            if (cost < low)
+            {
+              low = cost;
+              lowpos = j;
+            }
+          }
+        }
+        __syncwarp();
+        if (lowpos >= 0)
+        {
+          for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
+          __syncwarp();
+          const unsigned undo = flips & ~((2u << lowpos) - 1u);
+          if (lane == 0 && undo)
+          {
+            lsp[wi] ^= undo << o;
+            if (o)
+            {
+              unsigned hi = undo >> (32 - o);
+              if (hi) lsp[wi + 1] ^= hi;
+            }
+          }
+          __syncwarp();
+        }
+        natt += (unsigned long long)adv;
+        nacc += (unsigned long long)__popc(flips);
+        if (REPLAY) rs = s_A[draws] * rs + s_C[draws];
+        i += adv;
+      }
+    }
+    if (lane == 0)
+    {
+      a.p.cost[slot] = INT ? (double)icost : cost;
+      a.p.lowest[r] = INT ? (double)ilow : low;
+      a.p.attempts[r] += natt;
+      a.p.accepts[r] += nacc;
+      a.p.step_att[r] += natt;
+      a.p.step_acc[r] += nacc;
+    }
+    __syncwarp();
+  }
+  if (REPLAY && lane == 0) a.rng[w] = rs;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation kernels for the per-state contract.
+// ---------------------------------------------------------------------------
+template <int FL, bool INT>
+__global__ void eval_cost_kernel(DevModel m, int n, const uint32_t* spins,
+                                 int nw, double* out)
+{
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n) return;
+  double c;
+  long long ic;
+  warp_cost<FL, INT>(m, spins + (size_t)w * nw, lane, c, ic);
+  if (lane == 0) out[w] = INT ? (double)ic : c;
+}
+
+// calculate_cost_difference for query q: incident terms evaluated in
+// parallel, summed in order (model/ising.h:108-117, model/pubo.h:335-367,
+// model/pubo.cc:50-73, model/max_sat.h:173-236).
+template <int FL, bool INT>
+__global__ void eval_diff_kernel(DevModel m, int n, const uint32_t* spins,
+                                 int nw, const long long* vars, double* out)
+{
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n) return;
+  const uint32_t* sp = spins + (size_t)w * nw;
+  const int v = (int)vars[w];
+  const uint32_t sv = spin_of(sp, v);
+  const int rb = m.row[v], re = m.row[v + 1];
+  double diff = 0.0;
+  long long idiff = 0;
+  for (int q0 = rb; q0 < re; q0 += 32)
+  {
+    int q = q0 + lane;
+    double val = 0.0;
+    long long ival = 0;
+    bool skip = true;
+    if (q < re)
+    {
+      uint32_t e = m.inc[q];
+      int t = (int)(e & ~kNegBit);
+      int tb = m.trow[t], te = m.trow[t + 1];
+      if (FL == F_PARITY || FL == F_PLAIN_ISING)
+      {
+        uint32_t par = 0;
+        for (int u = tb; u < te; u++) par ^= spin_of(sp, (int)(m.tvar[u] & ~kNegBit));
+        skip = false;
+        if (INT) ival = par ? -(long long)m.coef_i[q] : (long long)m.coef_i[q];
+        else val = par ? -m.coef[q] : m.coef[q];
+      }
+      else
+      {
+        int cnt = 0;
+        for (int u = tb; u < te; u++)
+        {
+          uint32_t x = m.tvar[u];
+          cnt += (int)(spin_of(sp, (int)(x & ~kNegBit)) ^ (x >> 31));
+        }
+        const bool lit = (sv ^ (e >> 31)) != 0;
+        if (lit && cnt == 1)
+        {
+          skip = false;
+          if (INT) ival = m.coef_i[q]; else val = m.coef[q];
+        }
+        else if (!lit && cnt == 0)
+        {
+          skip = false;
+          if (INT) ival = -(long long)m.coef_i[q]; else val = -m.coef[q];
+        }
+      }
+    }
+    unsigned keep = __ballot_sync(kFull, !skip);
+    while (keep)
+    {
+      int j = __ffs(keep) - 1;
+      keep &= keep - 1;
+      if (INT) idiff += __shfl_sync(kFull, ival, j);
+      else diff = __dadd_rn(diff, __shfl_sync(kFull, val, j));
+    }
+  }
+  if (lane == 0)
+  {
+    if (FL == F_PARITY || FL == F_PLAIN_ISING)
+      out[w] = INT ? (double)(-2 * idiff) : __dmul_rn(2.0, -diff);
+    else
+      out[w] = INT ? (double)idiff : diff;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// PT: observations then alternating-parity neighbour swaps of the slot
+// labels (solver/parallel_tempering.h:134-189); one thread per restart.
+// ---------------------------------------------------------------------------
+__global__ void pt_swap_kernel(SwapArgs a)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.restarts) return;
+  const int T = a.n_temps;
+  const int base = k * T;
+  for (int p = 0; p < T; p++)
+  {
+    const int w = base + p;
+    const double att = (double)a.step_att_reset[w];
+    const double acc = (double)a.step_acc_reset[w];
+    a.obs_acc[w] = __dadd_rn(a.obs_acc[w], __ddiv_rn(acc, att));
+    a.obs_cost[w] = __dadd_rn(a.obs_cost[w], a.cost[a.slot_of[w]]);
+    a.obs_dir[w] = __dadd_rn(a.obs_dir[w], (double)a.dir[w]);
+    a.step_att_reset[w] = 0;
+    a.step_acc_reset[w] = 0;
+  }
+  uint64_t ms = a.replay ? a.master[k] : 0;
+  for (int i = (int)(a.step & 1); i < T - 1; i += 2)
+  {
+    double u;
+    if (a.replay)
+    {
+      uint32_t d0 = pcg_out(ms);
+      ms = ms * kMult + kInc;
+      uint32_t d1 = pcg_out(ms);
+      ms = ms * kMult + kInc;
+      u = canonical(d0, d1);
+    }
+    else
+    {
+      uint64_t wd = counter_draw(a.swap_key[k],
+                                 (unsigned long long)a.step * (unsigned long long)T +
+                                     (unsigned long long)i);
+      u = __dmul_rn((double)(wd >> 11), 1.0 / 9007199254740992.0);
+    }
+    const int wa = base + i, wb = base + i + 1;
+    const double x = __dmul_rn(__dsub_rn(a.cost[a.slot_of[wa]], a.cost[a.slot_of[wb]]),
+                               __dsub_rn(a.beta[wa], a.beta[wb]));
+    const double e = exp(x);
+    if (fabs(u - e) <= 1e-15 * e) atomicAdd(a.near_ties, 1ULL);
+    if (u < e)
+    {
+      int t = a.slot_of[wa];
+      a.slot_of[wa] = a.slot_of[wb];
+      a.slot_of[wb] = t;
+      int d = a.dir[wa];
+      a.dir[wa] = a.dir[wb];
+      a.dir[wb] = d;
+      a.swap_acc[wa] += 1;
+    }
+    a.swap_cnt[wa] += 1;
+  }
+  a.dir[base] = 0;
+  a.dir[base + T - 1] = 1;
+  if (a.replay) a.master[k] = ms;
+}
+
+// ---------------------------------------------------------------------------
+// PA resampling copies (Population::resample, solver/population.h:171-218):
+// every destination walker is an integer copy of its source walker.
+// ---------------------------------------------------------------------------
+__global__ void pa_copy_kernel(DevPop src, DevPop dst, const int* src_of, int n_dst)
+{
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= n_dst) return;
+  const int i = src_of[j];
+  const uint4* a = (const uint4*)(src.spins + (size_t)i * src.nw);
+  uint4* b = (uint4*)(dst.spins + (size_t)j * dst.nw);
+  for (int q = lane; q < src.nw / 4; q += 32) b[q] = a[q];
+  a = (const uint4*)(src.lspins + (size_t)i * src.nw);
+  b = (uint4*)(dst.lspins + (size_t)j * dst.nw);
+  for (int q = lane; q < src.nw / 4; q += 32) b[q] = a[q];
+  a = (const uint4*)(src.tstate + (size_t)i * src.mp);
+  b = (uint4*)(dst.tstate + (size_t)j * dst.mp);
+  for (int q = lane; q < src.mp / 16; q += 32) b[q] = a[q];
+  if (lane == 0)
+  {
+    dst.cost[j] = src.cost[i];
+    dst.lowest[j] = src.lowest[i];
+    dst.attempts[j] = src.attempts[i];
+    dst.accepts[j] = src.accepts[i];
+    dst.step_att[j] = 0;
+    dst.step_acc[j] = 0;
+  }
+}
+
+cudaError_t launch_pa_copy(const DevPop& src, const DevPop& dst, const int* src_of,
+                           int n_dst, cudaStream_t s)
+{
+  int blocks = (n_dst + 7) / 8;
+  if (blocks > 0) pa_copy_kernel<<<blocks, 256, 0, s>>>(src, dst, src_of, n_dst);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void upload_tables(int)
+{
+  double ln[1024];
+  for (int row = 0; row < 4; row++)
+    for (int i = 0; i < 256; i++)
+      ln[row * 256 + i] = log((i) / pow((double)256, (double)(row + 1)));
+  unsigned long long jA[65], jC[65], pA[64], pC[64];
+  jA[0] = 1;
+  jC[0] = 0;
+  for (int k = 1; k < 65; k++)
+  {
+    jA[k] = jA[k - 1] * kMult;
+    jC[k] = jC[k - 1] * kMult + kInc;
+  }
+  pA[0] = kMult;
+  pC[0] = kInc;
+  for (int k = 1; k < 64; k++)
+  {
+    pA[k] = pA[k - 1] * pA[k - 1];
+    pC[k] = pA[k - 1] * pC[k - 1] + pC[k - 1];
+  }
+  cudaMemcpyToSymbol(c_ln, ln, sizeof ln);
+  cudaMemcpyToSymbol(c_jA, jA, sizeof jA);
+  cudaMemcpyToSymbol(c_jC, jC, sizeof jC);
+  cudaMemcpyToSymbol(c_pA, pA, sizeof pA);
+  cudaMemcpyToSymbol(c_pC, pC, sizeof pC);
+}
+
+template <int FL, bool INT>
+static void init_dispatch(const InitArgs& a, cudaStream_t s)
+{
+  const int wpb = 4;
+  int blocks = (a.n_walkers + wpb - 1) / wpb;
+  if (blocks > 0) init_kernel<FL, INT><<<blocks, 32 * wpb, 0, s>>>(a);
+}
+
+cudaError_t launch_init(const InitArgs& a, cudaStream_t s)
+{
+  const bool I = a.m.int_mode != 0;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: I ? init_dispatch<F_PARITY, true>(a, s) : init_dispatch<F_PARITY, false>(a, s); break;
+    case F_COUNTER: I ? init_dispatch<F_COUNTER, true>(a, s) : init_dispatch<F_COUNTER, false>(a, s); break;
+    case F_PLAIN_ISING: I ? init_dispatch<F_PLAIN_ISING, true>(a, s) : init_dispatch<F_PLAIN_ISING, false>(a, s); break;
+    default: I ? init_dispatch<F_PLAIN_PUBO, true>(a, s) : init_dispatch<F_PLAIN_PUBO, false>(a, s); break;
+  }
+  return cudaGetLastError();
+}
+
+template <int FL, bool R, bool I>
+static void sweep_dispatch(const SweepArgs& a, cudaStream_t s, int wpb)
+{
+  int blocks = (a.n_streams + wpb - 1) / wpb;
+  if (blocks > 0) sweep_kernel<FL, R, I><<<blocks, 32 * wpb, 0, s>>>(a);
+}
+
+template <int FL>
+static void sweep_flavor(const SweepArgs& a, cudaStream_t s, int wpb)
+{
+  const bool I = a.m.int_mode != 0;
+  if (a.replay)
+    I ? sweep_dispatch<FL, true, true>(a, s, wpb) : sweep_dispatch<FL, true, false>(a, s, wpb);
+  else
+    I ? sweep_dispatch<FL, false, true>(a, s, wpb) : sweep_dispatch<FL, false, false>(a, s, wpb);
+}
+
+cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int wpb)
+{
+  if (wpb < 1) wpb = 1;
+  if (wpb > 8) wpb = 8;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: sweep_flavor<F_PARITY>(a, s, wpb); break;
+    case F_COUNTER: sweep_flavor<F_COUNTER>(a, s, wpb); break;
+    case F_PLAIN_ISING: sweep_flavor<F_PLAIN_ISING>(a, s, wpb); break;
+    default: sweep_flavor<F_PLAIN_PUBO>(a, s, wpb); break;
+  }
+  return cudaGetLastError();
+}
+
+template <int FL, bool I>
+static void cost_dispatch(const DevModel& m, int n, const uint32_t* sp, int nw,
+                          double* out, cudaStream_t s)
+{
+  int blocks = (n + 3) / 4;
+  if (blocks > 0) eval_cost_kernel<FL, I><<<blocks, 128, 0, s>>>(m, n, sp, nw, out);
+}
+
+cudaError_t launch_eval_cost(const DevModel& m, int n, const uint32_t* sp,
+                             int nw, double* out, cudaStream_t s)
+{
+  const bool I = m.int_mode != 0;
+  switch (m.flavor)
+  {
+    case F_PARITY: I ? cost_dispatch<F_PARITY, true>(m, n, sp, nw, out, s) : cost_dispatch<F_PARITY, false>(m, n, sp, nw, out, s); break;
+    case F_COUNTER: I ? cost_dispatch<F_COUNTER, true>(m, n, sp, nw, out, s) : cost_dispatch<F_COUNTER, false>(m, n, sp, nw, out, s); break;
+    case F_PLAIN_ISING: I ? cost_dispatch<F_PLAIN_ISING, true>(m, n, sp, nw, out, s) : cost_dispatch<F_PLAIN_ISING, false>(m, n, sp, nw, out, s); break;
+    default: I ? cost_dispatch<F_PLAIN_PUBO, true>(m, n, sp, nw, out, s) : cost_dispatch<F_PLAIN_PUBO, false>(m, n, sp, nw, out, s); break;
+  }
+  return cudaGetLastError();
+}
+
+template <int FL, bool I>
+static void diff_dispatch(const DevModel& m, int n, const uint32_t* sp, int nw,
+                          const long long* vars, double* out, cudaStream_t s)
+{
+  int blocks = (n + 3) / 4;
+  if (blocks > 0) eval_diff_kernel<FL, I><<<blocks, 128, 0, s>>>(m, n, sp, nw, vars, out);
+}
+
+cudaError_t launch_eval_diff(const DevModel& m, int n, const uint32_t* sp,
+                             int nw, const long long* vars, double* out,
+                             cudaStream_t s)
+{
+  const bool I = m.int_mode != 0;
+  switch (m.flavor)
+  {
+    case F_PARITY: I ? diff_dispatch<F_PARITY, true>(m, n, sp, nw, vars, out, s) : diff_dispatch<F_PARITY, false>(m, n, sp, nw, vars, out, s); break;
+    case F_COUNTER: I ? diff_dispatch<F_COUNTER, true>(m, n, sp, nw, vars, out, s) : diff_dispatch<F_COUNTER, false>(m, n, sp, nw, vars, out, s); break;
+    case F_PLAIN_ISING: I ? diff_dispatch<F_PLAIN_ISING, true>(m, n, sp, nw, vars, out, s) : diff_dispatch<F_PLAIN_ISING, false>(m, n, sp, nw, vars, out, s); break;
+    default: I ? diff_dispatch<F_PLAIN_PUBO, true>(m, n, sp, nw, vars, out, s) : diff_dispatch<F_PLAIN_PUBO, false>(m, n, sp, nw, vars, out, s); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pt_swap(const SwapArgs& a, cudaStream_t s)
+{
+  int threads = 64;
+  int blocks = (a.restarts + threads - 1) / threads;
+  pt_swap_kernel<<<blocks, threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+}  // namespace qio

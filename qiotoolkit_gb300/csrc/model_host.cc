@@ -1,0 +1,543 @@
+// model_host.cc -- model construction and upload, schedules, device setup.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+
+#include "host.h"
+
+namespace qio
+{
+void fail(int status, const std::string& msg) { throw Error(status, msg); }
+
+void cuda_check(cudaError_t e, const char* what)
+{
+  if (e == cudaSuccess) return;
+  if (e == cudaErrorMemoryAllocation)
+    fail(2, std::string(what) + ": out of device memory");
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    fail(5, std::string(what) + ": " + cudaGetErrorString(e));
+  fail(3, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DevBuf::DevBuf(size_t n) : bytes(n)
+{
+  if (n) cuda_check(cudaMalloc(&ptr, n), "cudaMalloc");
+}
+DevBuf::~DevBuf()
+{
+  if (ptr) cudaFree(ptr);
+}
+DevBuf& DevBuf::operator=(DevBuf&& o) noexcept
+{
+  if (this != &o)
+  {
+    if (ptr) cudaFree(ptr);
+    ptr = o.ptr;
+    bytes = o.bytes;
+    o.ptr = nullptr;
+    o.bytes = 0;
+  }
+  return *this;
+}
+
+void ensure_device()
+{
+  static std::mutex mu;
+  static std::set<int> ready;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0)
+    fail(5, "no CUDA device available: the GB300 library has no CPU fallback");
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> g(mu);
+  if (ready.count(dev)) return;
+  upload_tables(dev);
+  cuda_check(cudaGetLastError(), "upload_tables");
+  ready.insert(dev);
+}
+
+// ---------------------------------------------------------------------------
+// Graph models: normalize_edges (graph/graph.h:74-177).  Names are numbered
+// in order of first appearance; a repeated name in a term throws for Ising
+// ("Duplicated ids detected in term!") and is merged for PUBO
+// (model/pubo.h:82); members are sorted; terms without members add to the
+// constant cost; each variable lists its terms in ascending term id.
+// ---------------------------------------------------------------------------
+static void build_graph(HostModel& m, int64_t n_terms, const int64_t* off,
+                        const int32_t* ids, const double* coef)
+{
+  if (n_terms <= 0)
+    fail(1, "parameter `terms`: size must be greater than 0, found 0");
+  const bool merge = (m.kind == K_PUBO || m.kind == K_PUBO_PLAIN);
+  std::map<int32_t, int> name_to_id;
+  std::vector<std::vector<int>> members;
+  std::vector<std::vector<int>> node_edges;
+  m.min_loc = INT32_MAX;
+  for (int64_t t = 0; t < n_terms; t++)
+  {
+    if (off[t + 1] < off[t]) fail(1, "term offsets must be non-decreasing");
+    std::vector<int> mem;
+    for (int64_t k = off[t]; k < off[t + 1]; k++)
+    {
+      auto it = name_to_id.find(ids[k]);
+      int id;
+      if (it == name_to_id.end())
+      {
+        id = (int)m.names.size();
+        name_to_id.emplace(ids[k], id);
+        m.names.push_back(ids[k]);
+        node_edges.emplace_back();
+      }
+      else
+        id = it->second;
+      if (std::find(mem.begin(), mem.end(), id) == mem.end())
+      {
+        mem.push_back(id);
+        node_edges[id].push_back((int)members.size());
+      }
+      else if (!merge)
+        fail(1, "Duplicated ids detected in term!");
+    }
+    std::sort(mem.begin(), mem.end());
+    int loc = (int)mem.size();
+    m.max_loc = std::max(m.max_loc, loc);
+    m.min_loc = std::min(m.min_loc, loc);
+    if (!mem.empty())
+    {
+      m.max_coupling = std::max(m.max_coupling, std::fabs(coef[t]));
+      members.push_back(std::move(mem));
+      m.tcost.push_back(coef[t]);
+    }
+    else
+      m.const_cost += coef[t];
+  }
+  if (m.min_loc == INT32_MAX) m.min_loc = 0;
+  m.N = (int64_t)m.names.size();
+  m.M = (int64_t)members.size();
+  if (m.N > INT32_MAX / 2 || m.M > INT32_MAX / 2) fail(1, "model too large");
+  m.row.assign(m.N + 1, 0);
+  for (int64_t v = 0; v < m.N; v++) m.row[v + 1] = m.row[v] + (int)node_edges[v].size();
+  m.K = m.row[m.N];
+  m.inc.resize(m.K);
+  m.coef.resize(m.K);
+  for (int64_t v = 0; v < m.N; v++)
+    for (size_t j = 0; j < node_edges[v].size(); j++)
+    {
+      int t = node_edges[v][j];
+      m.inc[m.row[v] + j] = (uint32_t)t;
+      m.coef[m.row[v] + j] = m.tcost[t];
+    }
+  m.trow.assign(m.M + 1, 0);
+  for (int64_t t = 0; t < m.M; t++) m.trow[t + 1] = m.trow[t] + (int)members[t].size();
+  m.tvar.resize(m.trow[m.M]);
+  for (int64_t t = 0; t < m.M; t++)
+    for (size_t j = 0; j < members[t].size(); j++)
+      m.tvar[m.trow[t] + j] = (uint32_t)members[t][j];
+}
+
+// ---------------------------------------------------------------------------
+// MaxSat::configure(clauses) (model/max_sat.h:295-397): clauses containing a
+// variable and its negation are always true and dropped; variables used
+// only there are free (rendered as 1); the remaining variables are numbered
+// by ascending name; clause c (1-based in the reference, c-1 here) lists
+// each variable once, negated literals marked.
+// ---------------------------------------------------------------------------
+static void build_maxsat(HostModel& m, int64_t n_terms, const int64_t* off,
+                         const int32_t* ids, const double* coef)
+{
+  if (n_terms <= 0) fail(1, "parameter `terms` must not be empty");
+  std::vector<char> always(n_terms, 0);
+  std::set<int32_t> used, maybe_free;
+  for (int64_t c = 0; c < n_terms; c++)
+  {
+    std::set<int32_t> seen;
+    for (int64_t k = off[c]; k < off[c + 1]; k++)
+    {
+      int32_t v = ids[k];
+      if (v == 0 || v == INT32_MIN)
+        fail(1, "MaxSat variables cannot have the name " + std::to_string(v) +
+                    " since it cannot be negated to indicate 'not " +
+                    std::to_string(v) + "'.");
+      if (seen.count(-v)) always[c] = 1;
+      seen.insert(v);
+    }
+    for (int32_t v : seen) (always[c] ? maybe_free : used).insert(std::abs(v));
+  }
+  for (int32_t v : maybe_free)
+    if (!used.count(v)) m.free_vars.push_back(v);
+  m.names.assign(used.begin(), used.end());
+  m.N = (int64_t)m.names.size();
+  std::map<int32_t, int> name_to_id;
+  for (size_t i = 0; i < m.names.size(); i++) name_to_id[m.names[i]] = (int)i;
+  std::vector<std::vector<uint32_t>> affected(m.N);
+  std::vector<std::vector<uint32_t>> members;
+  m.min_loc = INT32_MAX;
+  for (int64_t c = 0; c < n_terms; c++)
+  {
+    if (always[c]) continue;
+    int t = (int)members.size();
+    m.tcost.push_back(coef[c]);
+    m.max_coupling = std::max(m.max_coupling, std::fabs(coef[c]));
+    std::vector<uint32_t> mem;
+    std::set<int> seen;
+    for (int64_t k = off[c]; k < off[c + 1]; k++)
+    {
+      int32_t name = ids[k];
+      int id = name_to_id[std::abs(name)];
+      if (seen.count(id)) continue;
+      seen.insert(id);
+      uint32_t neg = name < 0 ? kNegBit : 0u;
+      affected[id].push_back((uint32_t)t | neg);
+      mem.push_back((uint32_t)id | neg);
+    }
+    m.max_loc = std::max(m.max_loc, (int)mem.size());
+    m.min_loc = std::min(m.min_loc, (int)mem.size());
+    members.push_back(std::move(mem));
+  }
+  if (m.min_loc == INT32_MAX) m.min_loc = 0;
+  m.M = (int64_t)members.size();
+  if (m.M == 0)
+  {
+    // the model is "empty": every clause is always true
+    m.N = 0;
+    m.names.clear();
+  }
+  m.row.assign(m.N + 1, 0);
+  for (int64_t v = 0; v < m.N; v++) m.row[v + 1] = m.row[v] + (int)affected[v].size();
+  m.K = m.row[m.N];
+  m.inc.resize(m.K);
+  m.coef.resize(m.K);
+  for (int64_t v = 0; v < m.N; v++)
+    for (size_t j = 0; j < affected[v].size(); j++)
+    {
+      uint32_t e = affected[v][j];
+      m.inc[m.row[v] + j] = e;
+      m.coef[m.row[v] + j] = m.tcost[e & ~kNegBit];
+    }
+  m.trow.assign(m.M + 1, 0);
+  for (int64_t t = 0; t < m.M; t++) m.trow[t + 1] = m.trow[t] + (int)members[t].size();
+  m.tvar.resize(m.trow[m.M]);
+  for (int64_t t = 0; t < m.M; t++)
+    for (size_t j = 0; j < members[t].size(); j++) m.tvar[m.trow[t] + j] = members[t][j];
+}
+
+// Window-conflict masks: bit d-1 of nbr[v] is set when variable v-d (d in
+// 1..32) shares a term with v.
+static void build_nbr(HostModel& m)
+{
+  m.nbr.assign(m.N, 0u);
+  std::vector<int> mem;
+  for (int64_t t = 0; t < m.M; t++)
+  {
+    mem.clear();
+    for (int k = m.trow[t]; k < m.trow[t + 1]; k++) mem.push_back((int)(m.tvar[k] & ~kNegBit));
+    std::sort(mem.begin(), mem.end());
+    for (size_t j = 0; j < mem.size(); j++)
+      for (size_t i = j; i-- > 0;)
+      {
+        int d = mem[j] - mem[i];
+        if (d > 32) break;
+        if (d >= 1) m.nbr[mem[j]] |= 1u << (d - 1);
+      }
+  }
+}
+
+// Integer mode: every coefficient is an integer of magnitude <= 2^20 and the
+// per-variable sums stay below 2^30, so int32/int64 arithmetic gives the same
+// values as the reference's FP64 sums (all partial sums are exact).
+static void detect_int_mode(HostModel& m)
+{
+  bool ok = m.M > 0;
+  for (double c : m.tcost)
+    if (!(std::floor(c) == c && std::fabs(c) <= 1048576.0)) { ok = false; break; }
+  if (ok)
+    for (int64_t v = 0; v < m.N && ok; v++)
+    {
+      double s = 0;
+      for (int q = m.row[v]; q < m.row[v + 1]; q++) s += std::fabs(m.coef[q]);
+      if (2 * s >= 1073741824.0) ok = false;
+    }
+  m.int_mode = ok;
+  if (ok)
+  {
+    m.coef_i.resize(m.K);
+    for (int64_t q = 0; q < m.K; q++) m.coef_i[q] = (int)m.coef[q];
+    m.tcost_i.resize(m.M);
+    for (int64_t t = 0; t < m.M; t++) m.tcost_i[t] = (int)m.tcost[t];
+  }
+}
+
+std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
+                                       const int64_t* off, const int32_t* ids,
+                                       const double* coef)
+{
+  if (kind < 0 || kind > 4) fail(1, "unknown model kind " + std::to_string(kind));
+  if (n_terms < 0 || (n_terms > 0 && (!off || !coef)))
+    fail(1, "model arrays must not be null");
+  std::unique_ptr<HostModel> m(new HostModel());
+  m->kind = kind;
+  if (kind == K_MAXSAT) build_maxsat(*m, n_terms, off, ids, coef);
+  else build_graph(*m, n_terms, off, ids, coef);
+  switch (kind)
+  {
+    case K_ISING: m->flavor = F_PARITY; break;
+    case K_ISING_PLAIN: m->flavor = F_PLAIN_ISING; break;
+    case K_PUBO: m->flavor = F_COUNTER; break;
+    case K_PUBO_PLAIN: m->flavor = F_PLAIN_PUBO; break;
+    default: m->flavor = F_COUNTER; break;
+  }
+  // byte counters hold up to 255 members; wider PUBO terms use the
+  // counter-free evaluation (same results, model::Pubo semantics)
+  if (m->flavor == F_COUNTER && m->max_loc > 255)
+  {
+    if (kind == K_MAXSAT) fail(1, "MaxSat clauses with more than 255 variables are not supported");
+    m->flavor = F_PLAIN_PUBO;
+  }
+  // GraphProperties::rescale (graph/graph_properties.h:24-40)
+  // (MaxSat keeps markov::Model's default factor 1, markov/model.h:193)
+  m->scale_factor = (kind == K_MAXSAT || m->max_coupling <= 1 || m->max_coupling == 0)
+                        ? 1.0
+                        : 1.0 / m->max_coupling;
+  build_nbr(*m);
+  detect_int_mode(*m);
+  return m;
+}
+
+template <class T>
+static size_t put(std::vector<char>& blob, const std::vector<T>& v)
+{
+  size_t o = (blob.size() + 255) & ~(size_t)255;
+  blob.resize(o + v.size() * sizeof(T));
+  if (!v.empty()) memcpy(blob.data() + o, v.data(), v.size() * sizeof(T));
+  return o;
+}
+
+void HostModel::upload() const
+{
+  ensure_device();
+  std::vector<char> blob;
+  size_t o_row = put(blob, row), o_inc = put(blob, inc), o_coef = put(blob, coef),
+         o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
+         o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i);
+  blob.resize((blob.size() + 255) & ~(size_t)255);
+  dmem = DevBuf(blob.size());
+  cuda_check(cudaMemcpy(dmem.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice),
+             "model upload");
+  char* b = (char*)dmem.ptr;
+  dev.flavor = flavor;
+  dev.n_vars = (int)N;
+  dev.n_terms = (int)M;
+  dev.sweep_size = (int)N;
+  dev.int_mode = int_mode ? 1 : 0;
+  dev.row = (const int*)(b + o_row);
+  dev.inc = (const uint32_t*)(b + o_inc);
+  dev.coef = (const double*)(b + o_coef);
+  dev.coef_i = int_mode ? (const int*)(b + o_ci) : nullptr;
+  dev.nbr = (const uint32_t*)(b + o_nbr);
+  dev.trow = (const int*)(b + o_trow);
+  dev.tvar = (const uint32_t*)(b + o_tvar);
+  dev.tcost = (const double*)(b + o_tc);
+  dev.tcost_i = int_mode ? (const int*)(b + o_tci) : nullptr;
+  uploaded = true;
+}
+
+DevModel HostModel::device_view(bool full_maxsat_sweep) const
+{
+  DevModel d = device();
+  // MaxSat does not override get_sweep_size() (markov/model.h:169): one
+  // attempt (variable 0) per sweep unless the full sweep is requested.
+  if (kind == K_MAXSAT && !full_maxsat_sweep) d.sweep_size = N > 0 ? 1 : 0;
+  return d;
+}
+
+static std::vector<int32_t> flatten_ids(const json::Value& terms, std::vector<int64_t>& off,
+                                        std::vector<double>& coef)
+{
+  std::vector<int32_t> ids;
+  off.assign(1, 0);
+  for (const auto& t : terms.arr)
+  {
+    const json::Value* c = t.find("c");
+    const json::Value* i = t.find("ids");
+    if (!c || !c->is_number()) fail(1, "parameter `c` is required");
+    if (!i || !i->is_array()) fail(1, "parameter `ids` is required");
+    coef.push_back(c->num);
+    for (const auto& x : i->arr)
+    {
+      if (!x.is_number() || !x.is_int) fail(1, "ids must be integers");
+      ids.push_back((int32_t)x.i);
+    }
+    off.push_back((int64_t)ids.size());
+  }
+  return ids;
+}
+
+std::unique_ptr<HostModel> build_model_json(const json::Value& doc, int kind)
+{
+  const json::Value* cf = doc.find("cost_function");
+  if (!cf || !cf->is_object()) fail(1, "Input field `cost_function` is required.");
+  const json::Value* type = cf->find("type");
+  if (kind < 0)
+  {
+    if (!type || !type->is_string()) fail(1, "parameter `type` is required");
+    if (type->str == "ising") kind = K_ISING;
+    else if (type->str == "pubo") kind = K_PUBO;
+    else if (type->str == "maxsat") kind = K_MAXSAT;
+    else fail(1, "Unknown model type: " + type->str);
+  }
+  const json::Value* ver = cf->find("version");
+  if (ver && ver->is_string() && kind != K_MAXSAT && ver->str != "1.0" && ver->str != "1.1")
+    fail(1, "Expecting `version` equals 1.0 or 1.1, but found: " + ver->str);
+  const json::Value* terms = cf->find("terms");
+  if (!terms || !terms->is_array()) fail(1, "parameter `terms` is required");
+  std::vector<int64_t> off;
+  std::vector<double> coef;
+  std::vector<int32_t> ids = flatten_ids(*terms, off, coef);
+  return build_model(kind, (int64_t)coef.size(), off.data(), ids.data(), coef.data());
+}
+
+// ---------------------------------------------------------------------------
+// Schedules.  Linear a + p(b-a) (schedule/linear.cc:15-18), geometric
+// a(b/a)^p (schedule/geometric.cc:9-12), lists of constant points
+// (Segments of constants, schedule/segments.cc:15-43,45-110), input mapping
+// and clamping (schedule/schedule.cc:17-25), discretisation (38-89).
+// ---------------------------------------------------------------------------
+double Schedule::progress_value(double p) const
+{
+  switch (type)
+  {
+    case 0: return initial + p * (final_ - initial);
+    case 1: return initial * pow(final_ / initial, p);
+    case 2: return initial;
+    default:
+    {
+      double position = get_start() + p * (get_stop() - get_start());
+      if (position < 0) return values.front();
+      for (size_t i = 0; i < values.size(); i++)
+      {
+        double stop = (double)i;
+        if (position > stop) continue;
+        double start = (double)i;
+        if (i > 0 && position < start)
+        {
+          double last_stop = (double)(i - 1);
+          double q = (position - last_stop) / (start - last_stop);
+          return (1 - q) * values[i - 1] + q * values[i];
+        }
+        return values[i];
+      }
+      return values.back();
+    }
+  }
+}
+double Schedule::get_start() const { return has_start ? start_ : 0; }
+double Schedule::get_stop() const
+{
+  if (has_stop) return stop_;
+  if (type == 3) return (double)values.size() - 1;
+  return 1;
+}
+int Schedule::get_count() const
+{
+  if (has_count) return count_;
+  if (type == 3) return (int)values.size();
+  return (int)round(std::abs(get_stop() - get_start()));
+}
+double Schedule::get_value(double input) const
+{
+  double start = get_start(), stop = get_stop();
+  if (start == stop) return progress_value(0);
+  double progress = (input - start) / (stop - start);
+  return progress_value(std::min(1., std::max(0., progress)));
+}
+std::vector<double> Schedule::discretized() const
+{
+  int count = get_count();
+  if (count < 2) fail(1, "Can not get_discretized_values(count) for less than 2 values");
+  std::vector<double> d;
+  for (int i = 0; i < count; i++) d.push_back(progress_value(double(i) / (count - 1)));
+  return d;
+}
+std::string Schedule::render() const
+{
+  if (type == 0 || type == 1)
+    return std::string("{\"type\":\"") + (type == 0 ? "linear" : "geometric") +
+           "\",\"initial\":" + json::number(initial) + ",\"final\":" + json::number(final_) + "}";
+  if (type == 2) return json::number(initial);
+  std::string s = "{\"type\":\"segments\",\"segments\":[";
+  for (size_t i = 0; i < values.size(); i++)
+    s += (i ? "," : "") + std::string("{\"value\":") + json::number(values[i]) + "}";
+  return s + "]}";
+}
+
+Schedule parse_schedule(const json::Value& v, const std::string& name)
+{
+  Schedule s;
+  if (v.is_number())
+  {
+    s.type = 2;
+    s.initial = v.num;
+    return s;
+  }
+  if (v.is_array())
+  {
+    if (v.arr.empty())
+      fail(1, "parameter `" + name + "`: unable to initialize schedule:\n  Linear: parameter `type` is required\n  Geometric: parameter `type` is required\n  Segments: `segments` must be specified as a non-empty array.\n  Constant: expected double, found array");
+    s.type = 3;
+    for (const auto& x : v.arr)
+    {
+      if (!x.is_number()) fail(1, "parameter `" + name + "`: list values must be numbers");
+      s.values.push_back(x.num);
+    }
+    return s;
+  }
+  if (!v.is_object()) fail(1, "parameter `" + name + "`: unable to initialize schedule");
+  const json::Value* type = v.find("type");
+  std::string t = (type && type->is_string()) ? type->str : "";
+  auto num = [&](const char* k, double& out, bool required) {
+    const json::Value* x = v.find(k);
+    if (!x) { if (required) fail(1, "parameter `" + std::string(k) + "` is required"); return false; }
+    if (!x->is_number()) fail(1, "parameter `" + std::string(k) + "`: expected number");
+    out = x->num;
+    return true;
+  };
+  if (t == "linear" || t == "geometric")
+  {
+    s.type = t == "linear" ? 0 : 1;
+    num("initial", s.initial, true);
+    num("final", s.final_, true);
+    if (s.type == 1 && s.initial <= 0) fail(1, "initial must be positive for geometric");
+    if (s.type == 1 && s.final_ <= 0) fail(1, "final must be positive for geometric");
+  }
+  else if (t == "constant")
+  {
+    s.type = 2;
+    num("value", s.initial, true);
+  }
+  else if (t == "segments")
+  {
+    s.type = 3;
+    const json::Value* segs = v.find("segments");
+    if (!segs || !segs->is_array() || segs->arr.empty())
+      fail(1, "`segments` must be specified as a non-empty array.");
+    for (const auto& x : segs->arr)
+    {
+      if (x.is_number()) s.values.push_back(x.num);
+      else if (x.is_object() && x.find("value") && x["value"].is_number())
+        s.values.push_back(x["value"].num);
+      else fail(1, "only constant segments are supported");
+    }
+  }
+  else
+    fail(1, "parameter `" + name + "`: unable to initialize schedule:\n  Linear: parameter `type` is required");
+  double d;
+  if (num("start", d, false)) { s.has_start = true; s.start_ = d; }
+  if (num("stop", d, false)) { s.has_stop = true; s.stop_ = d; }
+  if (num("count", d, false)) { s.has_count = true; s.count_ = (int)d; }
+  return s;
+}
+}  // namespace qio

@@ -1,0 +1,673 @@
+// pa.cc -- population annealing driver (solver/population_annealing.h).
+//
+// Sweeps and replica copies run on the device.  The O(R) bookkeeping between
+// sweeps -- cost statistics, Boltzmann weights, resampling counts, family
+// census, restart test -- runs on the host in the reference's arithmetic
+// (sequential sums, the C library's exp, libstdc++'s Poisson and uniform
+// distributions on the master PCG stream), so that trajectories replay the
+// reference exactly.  Only R doubles and R ints cross PCIe per step; the
+// O(R * N) state traffic stays in HBM.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <numeric>
+#include <random>
+
+#include "host.h"
+
+namespace qio
+{
+uint64_t host_counter_key(uint32_t seed, uint64_t stream);
+void configure_common_public(Solver& s, const json::Value& doc);
+
+namespace
+{
+const uint64_t kMult = 6364136223846793005ULL;
+const uint64_t kInc = 1442695040888963407ULL;
+
+// pcg32 as a UniformRandomBitGenerator for the libstdc++ distributions the
+// reference uses (utils/random_generator.cc:47-58).
+struct PcgEngine
+{
+  using result_type = uint32_t;
+  static constexpr result_type min() { return 0; }
+  static constexpr result_type max() { return 0xffffffffu; }
+  uint64_t state = 0;
+  explicit PcgEngine(uint32_t s) { state = ((uint64_t)s + kInc) * kMult + kInc; }
+  result_type operator()()
+  {
+    uint64_t old = state;
+    state = old * kMult + kInc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+  }
+  double uniform()
+  {
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    return u(*this);
+  }
+  uint32_t poisson(double mean)
+  {
+    std::poisson_distribution<> p(mean);
+    return (uint32_t)p(*this);
+  }
+};
+
+// LCG jump: state after k further steps.
+uint64_t jump(uint64_t s, uint64_t k)
+{
+  uint64_t A = kMult, C = kInc;
+  while (k)
+  {
+    if (k & 1) s = A * s + C;
+    C = A * C + C;
+    A = A * A;
+    k >>= 1;
+  }
+  return s;
+}
+
+// utils::RandomSelector (utils/random_selector.cc:14-125) for the
+// constant-population residual draw.
+struct Selector
+{
+  std::vector<size_t> ids;
+  std::vector<double> weight{0, 0};
+  double total = 0;
+  double cumulative(size_t position) const
+  {
+    size_t p = 0;
+    double w = 0;
+    for (size_t k = weight.size() - 1; k > 0; k >>= 1)
+      if (position & k)
+      {
+        p |= k;
+        w += weight[p];
+      }
+    return w;
+  }
+  double get_weight(size_t position) const { return cumulative(position + 1) - cumulative(position); }
+  void add_weight(size_t position, double w)
+  {
+    for (size_t k = 1; k < weight.size(); k <<= 1)
+    {
+      if (position & k) position ^= k;
+      else weight[position + k] += w;
+    }
+  }
+  void insert(size_t id, double w)
+  {
+    size_t position = ids.size();
+    ids.push_back(id);
+    total += w;
+    if (position + 1 >= weight.size())
+    {
+      double t = weight.back();
+      weight.resize(2 * weight.size() - 1);
+      weight.back() = t;
+    }
+    add_weight(position, w);
+  }
+  size_t select_and_remove(double u)
+  {
+    if (ids.empty()) fail(6, "Random selector is empty.");
+    size_t position = 0;
+    if (ids.size() > 1)
+    {
+      double w = u * total;
+      for (size_t k = weight.size() - 1; k > 0; k >>= 1)
+        if (w >= weight[position + k])
+        {
+          position += k;
+          w -= weight[position];
+        }
+      if (position >= ids.size()) position = ids.size() - 1;
+    }
+    size_t id = ids[position];
+    ids[position] = ids.back();
+    ids.pop_back();
+    double before = get_weight(position);
+    double after = get_weight(ids.size());
+    total -= before;
+    add_weight(position, after - before);
+    add_weight(ids.size(), -after);
+    return id;
+  }
+};
+
+struct Pool
+{
+  DevBuf buf;
+  DevPop pop{};
+  int cap = 0;
+  void alloc(const HostModel& m, int capacity)
+  {
+    cap = capacity;
+    int nw = (int)(((m.N + 31) / 32 + 3) & ~3LL);
+    int mp = (int)((m.M + 15) & ~15LL);
+    if (m.flavor == F_PLAIN_ISING || m.flavor == F_PLAIN_PUBO) mp = 16;
+    size_t S = (size_t)capacity, off = 0;
+    auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+    size_t o_sp = take(S * nw * 4), o_ts = take(S * mp), o_c = take(S * 8), o_l = take(S * 8),
+           o_ls = take(S * nw * 4), o_at = take(S * 8), o_ac = take(S * 8), o_sa = take(S * 8),
+           o_sc = take(S * 8);
+    buf = DevBuf(off);
+    char* b = (char*)buf.ptr;
+    pop.n = capacity;
+    pop.nw = nw;
+    pop.mp = mp;
+    pop.spins = (uint32_t*)(b + o_sp);
+    pop.tstate = (uint8_t*)(b + o_ts);
+    pop.cost = (double*)(b + o_c);
+    pop.lowest = (double*)(b + o_l);
+    pop.lspins = (uint32_t*)(b + o_ls);
+    pop.attempts = (unsigned long long*)(b + o_at);
+    pop.accepts = (unsigned long long*)(b + o_ac);
+    pop.step_att = (unsigned long long*)(b + o_sa);
+    pop.step_acc = (unsigned long long*)(b + o_sc);
+  }
+};
+}  // namespace
+
+class PopulationAnnealing : public Solver
+{
+ public:
+  double alpha = 2.0;
+  size_t target_pop = 0;
+  size_t target_initial = 0;
+  bool constant_population = false;
+  std::string strategy = "linear_schedule";
+  Schedule beta;
+  double beta_start = 0;
+  int64_t spr = 1;
+  bool exp_repop = false;
+  int T = 1;  // emulated OpenMP threads = replay streams
+
+  Pool pools[2];
+  int cur = 0;
+  DevBuf aux;  // streams (T), per-walker init streams, src_of, beta
+  uint64_t* d_streams = nullptr;
+  uint64_t* d_init_rng = nullptr;
+  int* d_src = nullptr;
+  double* d_beta = nullptr;
+  int aux_cap = 0;
+
+  PcgEngine master{0};
+  std::vector<uint64_t> streams;  // host mirror of the replay streams
+  std::vector<size_t> family;
+  std::vector<double> wbeta;
+  size_t R = 0;
+  double cur_beta = 0;
+  uint64_t restart_base = 0, epoch = 0;
+  bool has_low = false;
+  double low_cost = 0;
+  std::vector<uint32_t> low_words;
+  std::vector<double> trace_beta;
+  std::vector<int64_t> trace_pop;
+
+  bool streams_on_device = false;
+
+  std::string target_name() const { return "populationannealing.cpu"; }
+
+  bool historical_lowest(double& c, std::vector<uint8_t>& st) override
+  {
+    if (!has_low) return false;
+    c = low_cost;
+    st.assign(model->N, 0);
+    for (int64_t v = 0; v < model->N; v++) st[v] = (low_words[v / 32] >> (v % 32)) & 1u;
+    return true;
+  }
+  std::string target() const override { return target_name(); }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common_pa(doc);
+  }
+
+  void configure_common_pa(const json::Value& doc);
+
+  int64_t n_walkers() const override { return model->empty() ? 0 : (int64_t)R; }
+
+  int draws_per_init() const
+  {
+    return model->kind == K_MAXSAT ? (int)(2 * model->N) : (int)((model->N + 31) / 32);
+  }
+
+  void ensure_aux(int capacity)
+  {
+    if (capacity <= aux_cap) return;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+    size_t o_s = take((size_t)T * 8), o_i = take((size_t)capacity * 8), o_src = take((size_t)capacity * 4),
+           o_b = take((size_t)capacity * 8);
+    DevBuf nb(off);
+    // carry the replay streams over
+    if (aux.ptr) cuda_check(cudaMemcpy((char*)nb.ptr + o_s, d_streams, (size_t)T * 8, cudaMemcpyDeviceToDevice), "D2D");
+    aux = std::move(nb);
+    char* b = (char*)aux.ptr;
+    d_streams = (uint64_t*)(b + o_s);
+    d_init_rng = (uint64_t*)(b + o_i);
+    d_src = (int*)(b + o_src);
+    d_beta = (double*)(b + o_b);
+    aux_cap = capacity;
+  }
+
+  void ensure_capacity(int n, cudaStream_t st)
+  {
+    if (n <= pools[cur].cap)
+    {
+      ensure_aux(pools[cur].cap);
+      return;
+    }
+    int cap = std::max(n + n / 2, 64);
+    Pool np[2];
+    np[0].alloc(*model, cap);
+    np[1].alloc(*model, cap);
+    ensure_aux(cap);
+    if (R > 0 && pools[cur].cap > 0)
+    {
+      std::vector<int> ident(R);
+      std::iota(ident.begin(), ident.end(), 0);
+      cuda_check(cudaMemcpyAsync(d_src, ident.data(), R * 4, cudaMemcpyHostToDevice, st), "H2D");
+      cuda_check(launch_pa_copy(pools[cur].pop, np[0].pop, d_src, (int)R, st), "copy");
+      cuda_check(cudaStreamSynchronize(st), "sync");
+    }
+    pools[0] = std::move(np[0]);
+    pools[1] = std::move(np[1]);
+    cur = 0;
+    device_bytes = (int64_t)(pools[0].buf.bytes + pools[1].buf.bytes + aux.bytes);
+  }
+
+  void upload_beta(cudaStream_t st)
+  {
+    cuda_check(cudaMemcpyAsync(d_beta, wbeta.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D beta");
+  }
+
+  // init_population (solver/population_annealing.h:141-167)
+  void init_population(cudaStream_t st)
+  {
+    size_t old = R;
+    if (R < target_pop)
+    {
+      ensure_capacity((int)target_pop, st);
+      wbeta.resize(target_pop, 0.0);
+      family.resize(target_pop, 0);
+      for (size_t i = old; i < target_pop; i++)
+        wbeta[i] = cur_beta <= 0 ? 0.0 : cur_beta;  // Metropolis::set_beta
+      R = target_pop;
+    }
+    for (size_t i = 0; i < target_pop; i++) family[i] = i;
+    InitArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = pools[cur].pop;
+    a.n_walkers = (int)R;
+    if (replay)
+    {
+      if (streams_on_device)
+      {
+        cuda_check(cudaMemcpyAsync(streams.data(), d_streams, (size_t)T * 8, cudaMemcpyDeviceToHost, st), "D2H");
+        cuda_check(cudaStreamSynchronize(st), "sync");
+      }
+      streams_on_device = true;
+      // walker i draws from stream i % T after the walkers before it
+      const uint64_t D = (uint64_t)draws_per_init();
+      std::vector<uint64_t> per(R);
+      for (size_t i = 0; i < R; i++) per[i] = jump(streams[i % T], (uint64_t)(i / T) * D);
+      for (int t = 0; t < T; t++)
+      {
+        uint64_t n_t = (R > (size_t)t) ? (uint64_t)((R - t + T - 1) / T) : 0;
+        streams[t] = jump(streams[t], n_t * D);
+      }
+      cuda_check(cudaMemcpyAsync(d_init_rng, per.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D");
+      cuda_check(cudaMemcpyAsync(d_streams, streams.data(), (size_t)T * 8, cudaMemcpyHostToDevice, st), "H2D");
+      a.replay = model->kind == K_MAXSAT ? 2 : 1;
+      a.rng = d_init_rng;
+      cuda_check(launch_init(a, st), "init kernel");
+      cuda_check(cudaStreamSynchronize(st), "sync");
+    }
+    else
+    {
+      a.replay = model->kind == K_MAXSAT ? 3 : 0;
+      a.seed = seed;
+      a.key_base = (0xFFFFFFFFULL - epoch) << 32;
+      a.key_div = (long long)1 << 40;
+      cuda_check(launch_init(a, st), "init kernel");
+    }
+    launches++;
+    upload_beta(st);
+  }
+
+  void init(cudaStream_t st) override
+  {
+    initialized = true;
+    if (model->empty()) return;
+    ensure_device();
+    streams_on_device = false;
+    has_low = false;
+    trace_beta.clear();
+    trace_pop.clear();
+    epoch = 0;
+    target_pop = target_initial;
+    master = PcgEngine(seed);
+    streams.assign(T, 0);
+    for (int t = 0; t < T; t++) streams[t] = PcgEngine(master()).state;  // rngs_[t] = fork()
+    cur_beta = beta_start;
+    restart_base = 0;
+    R = 0;
+    init_population(st);
+    // update_lowest_cost(population_[0]->cost(), population_[0]->state())
+    double c0;
+    cuda_check(cudaMemcpy(&c0, pools[cur].pop.cost, 8, cudaMemcpyDeviceToHost), "D2H");
+    has_low = true;
+    low_cost = c0;
+    low_words.resize(pools[cur].pop.nw);
+    cuda_check(cudaMemcpy(low_words.data(), pools[cur].pop.spins, low_words.size() * 4,
+                          cudaMemcpyDeviceToHost), "D2H");
+  }
+
+  void run(cudaStream_t st) override;
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
+             std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
+             std::vector<uint8_t>* states) override
+  {
+    int n = (int)n_walkers();
+    cost.resize(n);
+    lowest.resize(n);
+    att.resize(n);
+    acc.resize(n);
+    if (!n) return;
+    const DevPop& p = pools[cur].pop;
+    cuda_check(cudaMemcpy(cost.data(), p.cost, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(lowest.data(), p.lowest, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), p.attempts, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), p.accepts, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    std::vector<uint32_t> w((size_t)n * p.nw);
+    auto unpack = [&](std::vector<uint8_t>& out) {
+      out.assign((size_t)n * model->N, 0);
+      for (int r = 0; r < n; r++)
+        for (int64_t v = 0; v < model->N; v++)
+          out[(size_t)r * model->N + v] = (w[(size_t)r * p.nw + v / 32] >> (v % 32)) & 1u;
+    };
+    if (lowest_states)
+    {
+      cuda_check(cudaMemcpy(w.data(), p.lspins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      unpack(*lowest_states);
+    }
+    if (states)
+    {
+      cuda_check(cudaMemcpy(w.data(), p.spins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      unpack(*states);
+    }
+  }
+};
+
+void PopulationAnnealing::configure_common_pa(const json::Value& doc)
+{
+  configure_common_public(*this, doc);
+  const json::Value& p = params;
+  auto num = [&](const char* k, double def) {
+    const json::Value* v = p.find(k);
+    if (!v || v->is_null()) return def;
+    if (!v->is_number()) fail(1, std::string("parameter `") + k + "`: expected number");
+    return v->num;
+  };
+  alpha = num("alpha", 2.0);
+  if (!(alpha > 1.0)) fail(1, "parameter `alpha`: must be greater than 1, found " + json::number(alpha));
+  double pop = num("population", (double)threads);
+  if (!(pop > 0)) fail(1, "parameter `population`: must be greater than 0");
+  target_pop = (size_t)pop;
+  target_initial = target_pop;
+  const json::Value* cp = p.find("constant_population");
+  constant_population = cp && ((cp->type == json::Value::BOOL && cp->b) || (cp->is_number() && cp->num != 0));
+  const json::Value* rs = p.find("resampling_strategy");
+  if (rs && rs->is_string()) strategy = rs->str;
+  if (strategy != "linear_schedule" && strategy != "geometric_schedule")
+    fail(1, "`resampling strategy` must be one of ['linear_schedule', 'geometric_schedule'] on this solver");
+  bool geometric = strategy == "geometric_schedule";
+  if (p.find("beta"))
+    beta = parse_schedule(p["beta"], "beta");
+  else
+  {
+    double b0 = num("beta_start", geometric ? 0.01 : 0.0);
+    double b1 = num("beta_stop", 5.0);
+    if (!(b1 >= b0)) fail(1, "parameter `beta_stop`: must be greater than or equal to beta_start");
+    if (!geometric && b0 < 0) fail(1, "parameter `beta_start`: must be greater than or equal to 0");
+    if (geometric && (b0 <= 0 || b1 <= 0)) fail(1, "beta_start and beta_stop must be positive for geometric");
+    beta.type = geometric ? 1 : 0;
+    beta.initial = b0;
+    beta.final_ = b1;
+  }
+  if (beta.get_count() == 1)
+  {
+    if (step_limit > 1)
+    {
+      beta.has_stop = true;
+      beta.stop_ = std::max(1, (int)step_limit - 1);
+    }
+    else
+      fail(1, "Either a step_limit or schedule.count must be provided. "
+              "You can also set beta.{start,stop} to define the range.");
+  }
+  if (beta.progress_value(0) >= beta.progress_value(1))
+    fail(1, "the schedule for beta must be increasing (i.e., beta.initial < beta.final).");
+  beta_start = beta.get_value(0);
+  int64_t s = 1;
+  const json::Value* v = p.find("sweeps_per_replica");
+  if (v && v->is_number()) s = (int64_t)v->num;
+  if (s <= 0) fail(1, "parameter `sweeps_per_replica`: must be greater than 0");
+  spr = s;
+  // feature 2 = PA exponential repopulation (utils/config.h:49-61)
+  const json::Value* en = p.find("enabled_features");
+  if (en && en->is_array())
+    for (const auto& x : en->arr)
+      if (x.is_number() && x.num == 2) exp_repop = true;
+  // OpenMP stream emulation for replay: one stream per reference thread
+  T = threads;
+  output_params.push_back({"population", std::to_string(target_pop)});
+  output_params.push_back({"beta", beta.render()});
+  output_params.push_back({"alpha", json::number(alpha)});
+}
+
+void PopulationAnnealing::run(cudaStream_t st)
+{
+  if (!initialized) fail(1, "init() must be called before run()");
+  ran = true;
+  if (model->empty()) return;
+  const double scale = model->scale_factor;  // rescale() at init
+  std::vector<double> after, lowest;
+  int64_t step = 0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, st);
+  for (step = 0; step < step_limit;)
+  {
+    Pool& P = pools[cur];
+    const size_t Rn = R;
+    after.resize(Rn);
+    lowest.resize(Rn);
+    SweepArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = P.pop;
+    a.n_walkers = (int)Rn;
+    a.n_streams = replay ? std::min<int>(T, (int)Rn) : (int)Rn;
+    a.beta = d_beta;
+    a.bs_w = 1;
+    a.bs_s = 0;
+    a.sweep_base = 0;
+    a.n_sweeps = (int)spr;
+    a.replay = replay ? 1 : 0;
+    a.rng = d_streams;
+    a.seed = seed;
+    a.key_base = (unsigned long long)(step + 1) << 32;
+    a.key_div = (long long)1 << 40;
+    int wpb = std::max(1, std::min(4, a.n_streams / 152));
+    if (warps_per_block > 0) wpb = warps_per_block;
+    prof_begin(st);
+    cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+    prof_end(st);
+    launches++;
+    cuda_check(cudaMemcpyAsync(after.data(), P.pop.cost, Rn * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaMemcpyAsync(lowest.data(), P.pop.lowest, Rn * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    // update_lowest_cost over the citizens (solver/population_annealing.h:301-308)
+    int best = -1;
+    for (size_t i = 0; i < Rn; i++)
+      if (!has_low || lowest[i] < low_cost)
+      {
+        has_low = true;
+        low_cost = lowest[i];
+        best = (int)i;
+      }
+    if (best >= 0)
+    {
+      low_words.resize(P.pop.nw);
+      cuda_check(cudaMemcpy(low_words.data(), P.pop.lspins + (size_t)best * P.pop.nw,
+                            P.pop.nw * 4, cudaMemcpyDeviceToHost), "D2H");
+    }
+    // statistics (solver/population_annealing.h:310-382)
+    const double Rd = (double)Rn;
+    double avg_after = 0, min_cost = std::numeric_limits<double>::max();
+    for (size_t i = 0; i < Rn; i++)
+    {
+      avg_after += after[i];
+      min_cost = (after[i] < min_cost) ? after[i] : min_cost;
+    }
+    avg_after /= Rd;
+    double var_after = 0;
+    for (size_t i = 0; i < Rn; i++)
+    {
+      double d = after[i] - avg_after;
+      var_after += d * d;
+    }
+    var_after /= Rd;
+    for (size_t i = 0; i < Rn; i++) after[i] -= min_cost;
+    double delta_beta = beta.get_value((double)(step + 1 - (int64_t)restart_base)) -
+                        beta.get_value((double)(step - (int64_t)restart_base));
+    double rho_t = 1.0;
+    trace_beta.push_back(cur_beta);
+    if (delta_beta > 0)
+    {
+      // resample (solver/population_annealing.h:490-616)
+      std::vector<double> weight(Rn);
+      double total = 0.0;
+      for (size_t i = 0; i < Rn; i++)
+      {
+        weight[i] = exp(-delta_beta * after[i] * scale);
+        total += weight[i];
+      }
+      std::vector<size_t> count(Rn, 1);
+      if (constant_population)
+      {
+        size_t resampled = 0;
+        std::vector<double> residual(Rn);
+        for (size_t i = 0; i < Rn; i++)
+        {
+          double rel = (double)target_pop * weight[i] / total;
+          size_t iw = (size_t)floor(rel);
+          residual[i] = rel - (double)iw;
+          count[i] = iw;
+          resampled += iw;
+        }
+        Selector sel;
+        for (size_t i = 0; i < Rn; i++) sel.insert(i, residual[i]);
+        while (resampled < Rn)
+        {
+          count[sel.select_and_remove(master.uniform())] += 1;
+          resampled++;
+        }
+      }
+      else
+      {
+        double RRQ = (double)target_pop / total;
+        uint64_t curp = Rn;
+        for (size_t i = 0; i < Rn; i++)
+        {
+          size_t nc = (RRQ * weight[i]) > 0.0 ? (size_t)floor(master.poisson(RRQ * weight[i])) : 0;
+          if (nc == 0)
+          {
+            curp -= count[i];
+            count[i] = 0;
+          }
+          else if (nc > 1)
+          {
+            curp += nc - 1;
+            count[i] += nc - 1;
+          }
+        }
+        if (curp == 0)
+        {
+          size_t i = (size_t)floor(master.uniform() * Rn);
+          count[i] += 1;
+        }
+      }
+      // Population::resample: survivors in order, each followed... copies of
+      // citizen i (count - 1) precede the moved original; all are identical.
+      std::vector<int> src;
+      std::vector<size_t> fam;
+      std::vector<double> nb;
+      for (size_t i = 0; i < Rn; i++)
+        for (size_t c = 0; c < count[i]; c++)
+        {
+          src.push_back((int)i);
+          fam.push_back(family[i]);
+          nb.push_back(wbeta[i]);
+        }
+      size_t Rnew = src.size();
+      ensure_capacity((int)Rnew, st);
+      Pool& Pc = pools[cur];
+      Pool& Pn = pools[1 - cur];
+      cuda_check(cudaMemcpyAsync(d_src, src.data(), Rnew * 4, cudaMemcpyHostToDevice, st), "H2D");
+      cuda_check(launch_pa_copy(Pc.pop, Pn.pop, d_src, (int)Rnew, st), "copy kernel");
+      launches++;
+      cur = 1 - cur;
+      family.swap(fam);
+      wbeta.swap(nb);
+      R = Rnew;
+      std::map<size_t, size_t> census;
+      for (size_t f : family) census[f]++;
+      rho_t = 0;
+      for (auto& kv : census) rho_t += (double)kv.second * (double)kv.second;
+      rho_t /= Rd;
+    }
+    trace_pop.push_back((int64_t)R);
+    if (Rd / rho_t < alpha || var_after == 0)
+    {
+      cur_beta = beta_start;
+      restart_base = (uint64_t)step;
+      if (exp_repop) target_pop *= 2;
+      epoch++;
+      init_population(st);
+    }
+    else
+    {
+      cur_beta += delta_beta;
+      for (size_t i = 0; i < R; i++) wbeta[i] = cur_beta <= 0 ? 0.0 : cur_beta;
+      upload_beta(st);
+    }
+    step++;
+    if (has_cost_limit && has_low && low_cost <= cost_limit) break;
+  }
+  last_step = step;
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  run_ms = ms;
+  sweep_ms = profile ? prof_total_ms() : ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
+std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc)
+{
+  std::unique_ptr<PopulationAnnealing> s(new PopulationAnnealing());
+  s->model = m;
+  s->configure(doc);
+  return std::unique_ptr<Solver>(s.release());
+}
+}  // namespace qio

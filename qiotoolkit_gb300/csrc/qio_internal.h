@@ -1,0 +1,151 @@
+// qio_internal.h -- structures shared by the host shim (.cc) and the sm_103a
+// kernels (.cu).  No torch types, no C++ standard-library types cross into
+// device code.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace qio
+{
+// Model kinds, numbered as qio_model_kind in include/qio_gb300.h.
+enum Kind
+{
+  K_ISING = 0,
+  K_ISING_PLAIN = 1,
+  K_PUBO = 2,
+  K_PUBO_PLAIN = 3,
+  K_MAXSAT = 4
+};
+
+// Kernel flavour of a model.
+//   F_PARITY : Ising with a per-term parity byte (IsingTermCached)
+//   F_COUNTER: per-term counter byte with signed literals (PuboWithCounter is
+//              MaxSat with every literal positive: a PUBO variable whose
+//              spin is true has value 0, i.e. its "literal" is true)
+//   F_PLAIN_ISING / F_PLAIN_PUBO: no term state, members gathered per term
+enum Flavor
+{
+  F_PARITY = 0,
+  F_COUNTER = 1,
+  F_PLAIN_ISING = 2,
+  F_PLAIN_PUBO = 3
+};
+
+static const uint32_t kNegBit = 0x80000000u;
+
+// Read-only model in HBM.  Incidence k of variable v lies in
+// [row[v], row[v+1]) in ascending term id, the reference's order
+// (graph/graph.h:123).  inc[k] = term | kNegBit for a negated literal.
+struct DevModel
+{
+  int flavor;
+  int n_vars;
+  int n_terms;
+  int sweep_size;   // attempts per sweep (n_vars; 1 for MaxSat strict)
+  int int_mode;     // coefficients are small integers
+  const int* row;          // n_vars + 1
+  const uint32_t* inc;     // K
+  const double* coef;      // K  coefficient of the incidence's term
+  const int* coef_i;       // K  same, integer mode
+  const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
+  const int* trow;         // n_terms + 1
+  const uint32_t* tvar;    // K  members (| kNegBit for negated literals)
+  const double* tcost;     // n_terms
+  const int* tcost_i;      // n_terms
+};
+
+// Walker population in HBM (structure of arrays).  Spins are bit-packed,
+// 32 variables per word; term state is one byte per term.
+struct DevPop
+{
+  int n;                 // slots
+  int nw;                // words per spin vector
+  int mp;                // bytes per term-state vector
+  uint32_t* spins;       // n * nw
+  uint8_t* tstate;       // n * mp
+  double* cost;          // n (per slot)
+  double* lowest;        // n (per walker)
+  uint32_t* lspins;      // n * nw (per walker)
+  unsigned long long* attempts;   // n (per walker)
+  unsigned long long* accepts;    // n (per walker)
+  unsigned long long* step_att;   // n (per walker, since last observation)
+  unsigned long long* step_acc;   // n
+};
+
+struct SweepArgs
+{
+  DevModel m;
+  DevPop p;
+  int n_streams;        // one warp per stream
+  int n_walkers;        // stream w serves walkers w, w + n_streams, ...
+  const int* slot_of;   // walker -> slot (PT label swaps) or null
+  const double* beta;   // beta[walker * bs_w + sweep * bs_s]
+  long long bs_w, bs_s;
+  long long sweep_base; // absolute sweep index of this launch's first sweep
+  int n_sweeps;
+  int replay;           // 1: PCG streams (replay); 0: counter mode
+  uint64_t* rng;        // replay: PCG state per stream
+  uint32_t seed;        // counter mode: key = counter_key(seed + w / key_div,
+  unsigned long long key_base;  //                      key_base + w % key_div)
+  long long key_div;
+  int smem_state;       // stage spins + term state in shared memory
+};
+
+struct InitArgs
+{
+  DevModel m;
+  DevPop p;
+  int n_walkers;
+  const int* slot_of;
+  int replay;
+  uint64_t* rng;        // replay: per walker stream state (advanced in place)
+  uint32_t seed;
+  unsigned long long key_base;
+  long long key_div;
+  const uint8_t* given;     // optional: explicit states (n_walkers * n_vars)
+};
+
+// ---- launchers (kernels.cu) -------------------------------------------
+void upload_tables(int device);  // ln table + PCG jump tables
+cudaError_t launch_init(const InitArgs& a, cudaStream_t s);
+cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int warps_per_block);
+cudaError_t launch_eval_cost(const DevModel& m, int n_states,
+                             const uint32_t* spins, int nw, double* out,
+                             cudaStream_t s);
+cudaError_t launch_eval_diff(const DevModel& m, int n, const uint32_t* spins,
+                             int nw, const long long* vars, double* out,
+                             cudaStream_t s);
+
+// PT: label swaps + observables, one thread per restart.
+struct SwapArgs
+{
+  int restarts;
+  int n_temps;
+  int* slot_of;             // restarts * n_temps
+  const double* cost;       // per slot
+  const double* beta;       // per walker (position)
+  int* dir;                 // per walker
+  const unsigned long long* step_att;
+  unsigned long long* step_acc_reset;  // step counters (reset after reading)
+  unsigned long long* step_att_reset;
+  double* obs_acc;          // per walker: sum of per-step acc_rate
+  double* obs_cost;         // per walker: sum of costs
+  double* obs_dir;          // per walker: sum of directions
+  unsigned long long* swap_acc;  // per walker
+  unsigned long long* swap_cnt;  // per walker
+  unsigned long long* near_ties;
+  long long step;
+  int replay;
+  uint64_t* master;         // replay: per restart master PCG state
+  const unsigned long long* swap_key;  // counter: per restart key
+};
+cudaError_t launch_pt_swap(const SwapArgs& a, cudaStream_t s);
+
+// PA: bit-exact replica copies src -> dst (walker j of dst copies walker
+// src_of[j]); step counters of the copies start at zero.
+cudaError_t launch_pa_copy(const DevPop& src, const DevPop& dst, const int* src_of,
+                           int n_dst, cudaStream_t s);
+}  // namespace qio

@@ -1,0 +1,853 @@
+// solvers.cc -- host drivers of the simulated annealing and parallel
+// tempering solvers, configured from the reference's params JSON.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <thread>
+
+#include "host.h"
+
+namespace qio
+{
+// ---- host-side PCG32 and counter keys (same algorithms as the kernels) ----
+static const uint64_t kMult = 6364136223846793005ULL;
+static const uint64_t kInc = 1442695040888963407ULL;
+struct Pcg
+{
+  uint64_t state;
+  explicit Pcg(uint32_t s) { state = ((uint64_t)s + kInc) * kMult + kInc; }
+  uint32_t next()
+  {
+    uint64_t old = state;
+    state = old * kMult + kInc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+  }
+};
+static uint64_t mix64(uint64_t z)
+{
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+uint64_t host_counter_key(uint32_t seed, uint64_t stream)
+{
+  return mix64(((uint64_t)seed << 32) ^ mix64(stream + 0x9E3779B97F4A7C15ULL));
+}
+
+// ---- params helpers ------------------------------------------------------
+struct Params
+{
+  const json::Value& p;
+  explicit Params(const json::Value& v) : p(v) {}
+  const json::Value* get(const char* k, const char* alias = nullptr) const
+  {
+    const json::Value* v = p.find(k);
+    if (!v && alias) v = p.find(alias);
+    return v;
+  }
+  double num(const char* k, double def, const char* alias = nullptr) const
+  {
+    const json::Value* v = get(k, alias);
+    if (!v || v->is_null()) return def;
+    if (!v->is_number()) fail(1, std::string("parameter `") + k + "`: expected number");
+    return v->num;
+  }
+  int64_t integer(const char* k, int64_t def, const char* alias = nullptr) const
+  {
+    const json::Value* v = get(k, alias);
+    if (!v || v->is_null()) return def;
+    if (!v->is_number()) fail(1, std::string("parameter `") + k + "`: expected integer");
+    return v->is_int ? v->i : (int64_t)v->num;
+  }
+  bool boolean(const char* k, bool def) const
+  {
+    const json::Value* v = get(k);
+    if (!v || v->is_null()) return def;
+    if (v->type == json::Value::BOOL) return v->b;
+    if (v->is_number()) return v->num != 0;
+    fail(1, std::string("parameter `") + k + "`: expected boolean");
+  }
+  std::string str(const char* k, const std::string& def) const
+  {
+    const json::Value* v = get(k);
+    if (!v || v->is_null()) return def;
+    if (!v->is_string()) fail(1, std::string("parameter `") + k + "`: expected string");
+    return v->str;
+  }
+};
+
+static int default_threads()
+{
+  unsigned n = std::thread::hardware_concurrency();
+  return n ? (int)n : 1;
+}
+
+// Solver::configure + SteppingSolver::configure (solver/solver.h:156-218,
+// solver/stepping_solver.h:43-81) + ModelSolver::configure
+// (solver/model_solver.h:41-82).
+static void configure_common(Solver& s, const json::Value& doc)
+{
+  if (!doc.is_object() || !doc.find("params"))
+    fail(1, "Input field `params` is required.");
+  s.params = doc["params"];
+  Params p(s.params);
+  if (p.get("time_limit", "timeout"))
+  {
+    s.has_time_limit = true;
+    s.time_limit = p.num("time_limit", 0, "timeout");
+    if (s.time_limit < 0) fail(1, "timeout value must be non-negative");
+  }
+  if (p.get("cost_limit"))
+  {
+    s.has_cost_limit = true;
+    s.cost_limit = p.num("cost_limit", 0);
+  }
+  int t = (int)p.integer("threads", 0);
+  s.threads = (t > 0 && t < default_threads()) ? t : default_threads();
+  int64_t ns = p.integer("number_of_solutions", 1);
+  if (ns <= 0 || ns > 10)
+    fail(1, "parameter `number_of_solutions`: must be greater than 0 and less than or equal to 10, found " +
+                std::to_string(ns));
+  s.number_of_solutions = (int)ns;
+  s.step_limit = p.integer("step_limit", 10000, "sweeps");
+  if (s.step_limit < 0) fail(1, "parameter `step_limit` must be non-negative");
+  int64_t seed = p.integer("seed", (int64_t)std::chrono::system_clock::now().time_since_epoch().count());
+  s.seed = (uint32_t)seed;
+  std::string mode = p.str("rng_mode", "replay");
+  if (mode != "replay" && mode != "counter")
+    fail(1, "parameter `rng_mode` must be \"replay\" or \"counter\"");
+  s.replay = mode == "replay";
+  s.full_maxsat_sweep = p.boolean("maxsat_full_sweep", false);
+  s.warps_per_block = (int)p.integer("warps_per_block", 0);
+  s.profile = p.boolean("profile_kernels", false);
+  s.output_params.push_back({"seed", std::to_string(s.seed)});
+  s.output_params.push_back({"step_limit", std::to_string(s.step_limit)});
+}
+
+void configure_common_public(Solver& s, const json::Value& doc) { configure_common(s, doc); }
+
+void Solver::prof_begin(cudaStream_t s)
+{
+  if (!profile) return;
+  if (prof_used == prof_events.size())
+  {
+    cudaEvent_t a, b;
+    cuda_check(cudaEventCreate(&a), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&b), "cudaEventCreate");
+    prof_events.push_back({a, b});
+  }
+  cuda_check(cudaEventRecord(prof_events[prof_used].first, s), "cudaEventRecord");
+}
+
+void Solver::prof_end(cudaStream_t s)
+{
+  if (!profile) return;
+  cuda_check(cudaEventRecord(prof_events[prof_used].second, s), "cudaEventRecord");
+  prof_used++;
+}
+
+double Solver::prof_total_ms()
+{
+  double t = 0;
+  for (size_t i = 0; i < prof_used; i++)
+  {
+    cuda_check(cudaEventSynchronize(prof_events[i].second), "cudaEventSynchronize");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, prof_events[i].first, prof_events[i].second);
+    t += ms;
+  }
+  prof_used = 0;
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Population of walkers on the device.
+// ---------------------------------------------------------------------------
+struct Population
+{
+  DevBuf buf;
+  DevPop pop{};
+  int n = 0;
+  uint64_t* rng = nullptr;
+  int* slot_of = nullptr;
+  double* beta = nullptr;
+
+  void alloc(const HostModel& m, int slots, int streams, bool need_slots,
+             int64_t n_beta)
+  {
+    n = slots;
+    int nw = (int)(((m.N + 31) / 32 + 3) & ~3LL);
+    int mp = (int)((m.M + 15) & ~15LL);
+    if (m.flavor == F_PLAIN_ISING || m.flavor == F_PLAIN_PUBO) mp = 16;
+    size_t S = (size_t)slots;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+      size_t o = off;
+      off = (off + bytes + 255) & ~(size_t)255;
+      return o;
+    };
+    size_t o_sp = take(S * nw * 4), o_ts = take(S * mp), o_c = take(S * 8),
+           o_l = take(S * 8), o_ls = take(S * nw * 4), o_at = take(S * 8),
+           o_ac = take(S * 8), o_sa = take(S * 8), o_sc = take(S * 8),
+           o_rng = take((size_t)streams * 8), o_slot = take(need_slots ? S * 4 : 0),
+           o_beta = take((size_t)n_beta * 8);
+    buf = DevBuf(off);
+    char* b = (char*)buf.ptr;
+    pop.n = slots;
+    pop.nw = nw;
+    pop.mp = mp;
+    pop.spins = (uint32_t*)(b + o_sp);
+    pop.tstate = (uint8_t*)(b + o_ts);
+    pop.cost = (double*)(b + o_c);
+    pop.lowest = (double*)(b + o_l);
+    pop.lspins = (uint32_t*)(b + o_ls);
+    pop.attempts = (unsigned long long*)(b + o_at);
+    pop.accepts = (unsigned long long*)(b + o_ac);
+    pop.step_att = (unsigned long long*)(b + o_sa);
+    pop.step_acc = (unsigned long long*)(b + o_sc);
+    rng = (uint64_t*)(b + o_rng);
+    slot_of = need_slots ? (int*)(b + o_slot) : nullptr;
+    beta = (double*)(b + o_beta);
+  }
+
+  static void unpack(const std::vector<uint32_t>& words, int nw, int64_t N,
+                     int64_t count, std::vector<uint8_t>& out)
+  {
+    out.assign((size_t)count * N, 0);
+    for (int64_t r = 0; r < count; r++)
+      for (int64_t v = 0; v < N; v++)
+        out[r * N + v] = (words[r * nw + v / 32] >> (v % 32)) & 1u;
+  }
+};
+
+static int pick_wpb(int requested, int streams)
+{
+  if (requested > 0) return std::min(8, requested);
+  int w = streams / 152;
+  return std::max(1, std::min(4, w));
+}
+
+struct EventTimer
+{
+  cudaEvent_t a, b;
+  cudaStream_t s;
+  explicit EventTimer(cudaStream_t st) : s(st)
+  {
+    cuda_check(cudaEventCreate(&a), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&b), "cudaEventCreate");
+    cuda_check(cudaEventRecord(a, s), "cudaEventRecord");
+  }
+  double stop()
+  {
+    cuda_check(cudaEventRecord(b, s), "cudaEventRecord");
+    cuda_check(cudaEventSynchronize(b), "cudaEventSynchronize");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~EventTimer()
+  {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+// beta as Metropolis::set_beta / set_temperature store it
+// (markov/metropolis.h:35-61)
+static double beta_of(double value, bool inverse)
+{
+  if (inverse) return value <= 0 ? 0.0 : value;
+  return value <= 0 ? std::numeric_limits<double>::infinity() : 1.0 / value;
+}
+
+// ---------------------------------------------------------------------------
+// SimulatedAnnealing (solver/simulated_annealing.h:17-224)
+// ---------------------------------------------------------------------------
+class SimulatedAnnealing : public Solver
+{
+ public:
+  bool use_inverse = false;
+  int64_t restarts = 1;
+  Schedule schedule;
+  Population P;
+  std::vector<double> betas;
+
+  std::string target() const override { return "simulatedannealing.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    Params p(params);
+    use_inverse = p.boolean("use_inverse_temperature", false);
+    bool qio_format = false;
+    if (p.get("schedule"))
+      schedule = parse_schedule(params["schedule"], "schedule");
+    else
+    {
+      double b0 = p.num("beta_start", 0);
+      double b1 = p.num("beta_stop", 0.01);
+      if (b0 < 0)
+        fail(1, "parameter `beta_start`: must be greater than or equal to 0, found " + json::number(b0));
+      if (!(b1 > b0))
+        fail(1, "parameter `beta_stop`: must be greater than " + json::number(b0) + ", found " + json::number(b1));
+      use_inverse = true;
+      schedule.type = 0;
+      schedule.initial = b0;
+      schedule.final_ = b1;
+      qio_format = true;
+      output_params.push_back({"beta_start", json::number(b0)});
+      output_params.push_back({"beta_stop", json::number(b1)});
+    }
+    (void)qio_format;
+    // stretch to step_limit (solver/simulated_annealing.h:175-201)
+    if (schedule.get_start() == 0 && schedule.get_stop() == 1 && schedule.get_count() == 1)
+    {
+      if (step_limit > 1)
+      {
+        schedule.has_stop = true;
+        schedule.stop_ = std::max(1, (int)step_limit - 1);
+      }
+      else
+        fail(1, "The number of sweeps must be greater than 1.");
+    }
+    restarts = p.integer("restarts", threads);
+    if (restarts <= 0) fail(1, "parameter `restarts`: must be greater than 0");
+    if (restarts > (1 << 24)) fail(1, "parameter `restarts` too large");
+    output_params.push_back({"restarts", std::to_string(restarts)});
+    betas.resize(step_limit);
+    for (int64_t s = 0; s < step_limit; s++)
+      betas[s] = beta_of(schedule.get_value((double)s), use_inverse);
+  }
+
+  int64_t n_walkers() const override { return model->empty() ? 0 : restarts; }
+
+  void init(cudaStream_t st) override
+  {
+    initialized = true;
+    if (model->empty()) return;
+    ensure_device();
+    const int R = (int)restarts;
+    if (!P.buf.ptr) P.alloc(*model, R, R, false, std::max<int64_t>(1, step_limit));
+    device_bytes = (int64_t)P.buf.bytes;
+    // rngs_[i] = rng_->fork() in index order (solver/simulated_annealing.h:53-56)
+    std::vector<uint64_t> rs(R);
+    Pcg master(seed);
+    for (int i = 0; i < R; i++) rs[i] = Pcg(master.next()).state;
+    cuda_check(cudaMemcpyAsync(P.rng, rs.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D rng");
+    if (step_limit > 0)
+      cuda_check(cudaMemcpyAsync(P.beta, betas.data(), betas.size() * 8, cudaMemcpyHostToDevice, st),
+                 "H2D beta");
+    InitArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = P.pop;
+    a.n_walkers = R;
+    a.replay = replay ? (model->kind == K_MAXSAT ? 2 : 1) : (model->kind == K_MAXSAT ? 3 : 0);
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    cuda_check(launch_init(a, st), "init kernel");
+    launches++;
+  }
+
+  SweepArgs sweep_args() const
+  {
+    SweepArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = P.pop;
+    a.n_streams = (int)restarts;
+    a.n_walkers = (int)restarts;
+    a.beta = P.beta;
+    a.bs_w = 0;
+    a.bs_s = 1;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    return a;
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    EventTimer total(st);
+    SweepArgs a = sweep_args();
+    int wpb = pick_wpb(warps_per_block, a.n_streams);
+    if (!has_cost_limit && !has_time_limit)
+    {
+      a.sweep_base = 0;
+      a.n_sweeps = (int)step_limit;
+      if (step_limit > 0)
+      {
+        prof_begin(st);
+        cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+        prof_end(st);
+        launches++;
+      }
+      last_step = step_limit;
+    }
+    else
+    {
+      // per-step checks of the stepping loop (solver/stepping_solver.h:
+      // 124-258): cost limit after every step, time limit between chunks
+      auto t0 = std::chrono::steady_clock::now();
+      int64_t chunk = has_cost_limit ? 1 : std::max<int64_t>(1, step_limit / 100);
+      std::vector<double> low(restarts);
+      int64_t s = 0;
+      while (s < step_limit)
+      {
+        a.sweep_base = s;
+        a.n_sweeps = (int)std::min(chunk, step_limit - s);
+        prof_begin(st);
+        cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+        prof_end(st);
+        launches++;
+        s += a.n_sweeps;
+        if (has_cost_limit)
+        {
+          cuda_check(cudaMemcpyAsync(low.data(), P.pop.lowest, restarts * 8, cudaMemcpyDeviceToHost, st), "D2H");
+          cuda_check(cudaStreamSynchronize(st), "sync");
+          if (*std::min_element(low.begin(), low.end()) <= cost_limit) break;
+        }
+        if (has_time_limit)
+        {
+          cuda_check(cudaStreamSynchronize(st), "sync");
+          double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+          if (el >= time_limit) break;
+        }
+      }
+      last_step = s;
+    }
+    run_ms = total.stop();
+    sweep_ms = profile ? prof_total_ms() : run_ms;
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest,
+             std::vector<uint64_t>& att, std::vector<uint64_t>& acc,
+             std::vector<uint8_t>* lowest_states, std::vector<uint8_t>* states) override
+  {
+    int R = (int)n_walkers();
+    cost.resize(R);
+    lowest.resize(R);
+    att.resize(R);
+    acc.resize(R);
+    if (!R) return;
+    cuda_check(cudaMemcpy(cost.data(), P.pop.cost, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(lowest.data(), P.pop.lowest, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), P.pop.attempts, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), P.pop.accepts, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    std::vector<uint32_t> w((size_t)R * P.pop.nw);
+    if (lowest_states)
+    {
+      cuda_check(cudaMemcpy(w.data(), P.pop.lspins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, P.pop.nw, model->N, R, *lowest_states);
+    }
+    if (states)
+    {
+      cuda_check(cudaMemcpy(w.data(), P.pop.spins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, P.pop.nw, model->N, R, *states);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// ParallelTempering (solver/parallel_tempering.h:28-253).  The reference has
+// no restarts; the GB300 option "restarts" runs that many independent
+// tempering ladders, restart k seeded with seed + k (each identical to a
+// reference run with that seed).  Swaps exchange slot labels instead of
+// states; RNG streams, lowest states and counters stay with the temperature
+// position exactly as the reference's walkers do.
+// ---------------------------------------------------------------------------
+class ParallelTempering : public Solver
+{
+ public:
+  bool use_inverse = false;
+  int64_t spr = 1;
+  int restarts = 1;
+  Schedule ladder;
+  std::vector<double> temps;   // sorted
+  std::vector<double> betas;   // per position
+  Population P;
+  DevBuf aux;
+  int* dir = nullptr;
+  double *obs_acc = nullptr, *obs_cost = nullptr, *obs_dir = nullptr;
+  unsigned long long *swap_acc = nullptr, *swap_cnt = nullptr, *ties = nullptr;
+  uint64_t* master = nullptr;
+  unsigned long long* swap_key = nullptr;
+
+  std::string target() const override { return "paralleltempering.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    Params p(params);
+    spr = p.integer("sweeps_per_replica", 1);
+    if (spr <= 0) fail(1, "parameter `sweeps_per_replica`: must be greater than 0");
+    if (p.get("temperatures"))
+    {
+      ladder = parse_schedule(params["temperatures"], "temperatures");
+      use_inverse = false;
+    }
+    else if (p.get("all_betas"))
+    {
+      ladder = parse_schedule(params["all_betas"], "all_betas");
+      use_inverse = true;
+    }
+    else
+    {
+      ladder.type = 3;
+      ladder.values = {0.1, 0.5, 1., 2., 4.};
+      use_inverse = true;
+    }
+    output_params.push_back({use_inverse ? "all_betas" : "temperatures", ladder.render()});
+    temps = ladder.discretized();
+    if (use_inverse) std::sort(temps.begin(), temps.end(), std::greater<double>());
+    else std::sort(temps.begin(), temps.end(), std::less<double>());
+    betas.resize(temps.size());
+    for (size_t i = 0; i < temps.size(); i++) betas[i] = beta_of(temps[i], use_inverse);
+    restarts = (int)p.integer("restarts", 1);
+    if (restarts <= 0) fail(1, "parameter `restarts`: must be greater than 0");
+  }
+
+  int T() const { return (int)temps.size(); }
+  int64_t n_walkers() const override { return model->empty() ? 0 : (int64_t)restarts * T(); }
+
+  void init(cudaStream_t st) override
+  {
+    initialized = true;
+    if (model->empty()) return;
+    ensure_device();
+    const int W = restarts * T();
+    if (!P.buf.ptr) P.alloc(*model, W, W, true, W);
+    size_t K = (size_t)restarts;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+    size_t o_dir = take(W * 4), o_oa = take(W * 8), o_oc = take(W * 8), o_od = take(W * 8),
+           o_sa = take(W * 8), o_sc = take(W * 8), o_t = take(8), o_m = take(K * 8),
+           o_k = take(K * 8);
+    if (!aux.ptr) aux = DevBuf(off);
+    char* b = (char*)aux.ptr;
+    dir = (int*)(b + o_dir);
+    obs_acc = (double*)(b + o_oa);
+    obs_cost = (double*)(b + o_oc);
+    obs_dir = (double*)(b + o_od);
+    swap_acc = (unsigned long long*)(b + o_sa);
+    swap_cnt = (unsigned long long*)(b + o_sc);
+    ties = (unsigned long long*)(b + o_t);
+    master = (uint64_t*)(b + o_m);
+    swap_key = (unsigned long long*)(b + o_k);
+    cuda_check(cudaMemsetAsync(aux.ptr, 0, off, st), "memset");
+    device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
+    std::vector<uint64_t> rs(W), ms(K), keys(K);
+    std::vector<int> slots(W);
+    std::vector<double> bw(W);
+    for (int k = 0; k < restarts; k++)
+    {
+      Pcg m(seed + (uint32_t)k);
+      for (int i = 0; i < T(); i++)
+      {
+        rs[k * T() + i] = Pcg(m.next()).state;
+        slots[k * T() + i] = k * T() + i;
+        bw[k * T() + i] = betas[i];
+      }
+      ms[k] = m.state;
+      keys[k] = host_counter_key(seed + (uint32_t)k, 0xFFFFFFFFULL);
+    }
+    cuda_check(cudaMemcpyAsync(P.rng, rs.data(), W * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(P.slot_of, slots.data(), W * 4, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(P.beta, bw.data(), W * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(master, ms.data(), K * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(swap_key, keys.data(), K * 8, cudaMemcpyHostToDevice, st), "H2D");
+    InitArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = P.pop;
+    a.n_walkers = W;
+    a.slot_of = nullptr;  // identity at init
+    a.replay = replay ? (model->kind == K_MAXSAT ? 2 : 1) : (model->kind == K_MAXSAT ? 3 : 0);
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = T();
+    cuda_check(launch_init(a, st), "init kernel");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    // the sweep/swap loop keeps its own copies of the stream so that a
+    // host-side pageable copy above cannot race with kernels
+    launches++;
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    EventTimer total(st);
+    const int W = restarts * T();
+    SweepArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = P.pop;
+    a.n_streams = W;
+    a.n_walkers = W;
+    a.slot_of = P.slot_of;
+    a.beta = P.beta;
+    a.bs_w = 1;
+    a.bs_s = 0;
+    a.n_sweeps = (int)spr;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = T();
+    SwapArgs sw{};
+    sw.restarts = restarts;
+    sw.n_temps = T();
+    sw.slot_of = P.slot_of;
+    sw.cost = P.pop.cost;
+    sw.beta = P.beta;
+    sw.dir = dir;
+    sw.step_acc_reset = P.pop.step_acc;
+    sw.step_att_reset = P.pop.step_att;
+    sw.obs_acc = obs_acc;
+    sw.obs_cost = obs_cost;
+    sw.obs_dir = obs_dir;
+    sw.swap_acc = swap_acc;
+    sw.swap_cnt = swap_cnt;
+    sw.near_ties = ties;
+    sw.replay = replay ? 1 : 0;
+    sw.master = master;
+    sw.swap_key = swap_key;
+    int wpb = pick_wpb(warps_per_block, W);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> low(W);
+    int64_t s = 0;
+    for (s = 0; s < step_limit;)
+    {
+      a.sweep_base = s * spr;
+      prof_begin(st);
+      cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+      prof_end(st);
+      sw.step = s;
+      cuda_check(launch_pt_swap(sw, st), "swap kernel");
+      launches += 2;
+      s++;
+      if (has_cost_limit)
+      {
+        cuda_check(cudaMemcpyAsync(low.data(), P.pop.lowest, W * 8, cudaMemcpyDeviceToHost, st), "D2H");
+        cuda_check(cudaStreamSynchronize(st), "sync");
+        if (*std::min_element(low.begin(), low.end()) <= cost_limit) break;
+      }
+      if (has_time_limit && (s % 16 == 0))
+      {
+        cuda_check(cudaStreamSynchronize(st), "sync");
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= time_limit)
+          break;
+      }
+    }
+    last_step = s;
+    run_ms = total.stop();
+    sweep_ms = profile ? prof_total_ms() : run_ms;
+    unsigned long long nt = 0;
+    cuda_check(cudaMemcpy(&nt, ties, 8, cudaMemcpyDeviceToHost), "D2H");
+    near_ties = nt;
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest,
+             std::vector<uint64_t>& att, std::vector<uint64_t>& acc,
+             std::vector<uint8_t>* lowest_states, std::vector<uint8_t>* states) override
+  {
+    int W = (int)n_walkers();
+    cost.resize(W);
+    lowest.resize(W);
+    att.resize(W);
+    acc.resize(W);
+    if (!W) return;
+    std::vector<double> slot_cost(W);
+    std::vector<int> slots(W);
+    cuda_check(cudaMemcpy(slot_cost.data(), P.pop.cost, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(slots.data(), P.slot_of, W * 4, cudaMemcpyDeviceToHost), "D2H");
+    for (int w = 0; w < W; w++) cost[w] = slot_cost[slots[w]];
+    cuda_check(cudaMemcpy(lowest.data(), P.pop.lowest, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), P.pop.attempts, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), P.pop.accepts, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    std::vector<uint32_t> wds((size_t)W * P.pop.nw);
+    if (lowest_states)
+    {
+      cuda_check(cudaMemcpy(wds.data(), P.pop.lspins, wds.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(wds, P.pop.nw, model->N, W, *lowest_states);
+    }
+    if (states)
+    {
+      cuda_check(cudaMemcpy(wds.data(), P.pop.spins, wds.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      std::vector<uint8_t> by_slot;
+      Population::unpack(wds, P.pop.nw, model->N, W, by_slot);
+      states->resize(by_slot.size());
+      for (int w = 0; w < W; w++)
+        memcpy(states->data() + (size_t)w * model->N, by_slot.data() + (size_t)slots[w] * model->N,
+               model->N);
+    }
+  }
+
+  void pt_observables(std::vector<double>& out) override
+  {
+    int W = (int)n_walkers();
+    out.assign((size_t)W * 5, 0);
+    if (!W) return;
+    std::vector<double> oa(W), oc(W), od(W);
+    std::vector<unsigned long long> sa(W), sc(W);
+    cuda_check(cudaMemcpy(oa.data(), obs_acc, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(oc.data(), obs_cost, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(od.data(), obs_dir, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(sa.data(), swap_acc, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(sc.data(), swap_cnt, W * 8, cudaMemcpyDeviceToHost), "D2H");
+    double st = (double)last_step;
+    for (int w = 0; w < W; w++)
+    {
+      int i = w % T();
+      out[w * 5 + 0] = use_inverse ? betas[i] : (betas[i] > 0 ? 1.0 / betas[i] : INFINITY);
+      if (!use_inverse) out[w * 5 + 0] = temps[i] <= 0 ? 0.0 : temps[i];
+      out[w * 5 + 1] = oa[w] / st;
+      out[w * 5 + 2] = oc[w] / st;
+      out[w * 5 + 3] = od[w] / st;
+      out[w * 5 + 4] = sc[w] ? (double)sa[w] / (double)sc[w] : NAN;
+    }
+  }
+};
+
+std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc);
+
+std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& target,
+                                    const json::Value& doc)
+{
+  if (target == "simulatedannealing.qiotoolkit")
+  {
+    std::unique_ptr<SimulatedAnnealing> s(new SimulatedAnnealing());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
+  if (target == "paralleltempering.qiotoolkit")
+  {
+    std::unique_ptr<ParallelTempering> s(new ParallelTempering());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
+  if (target == "populationannealing.cpu") return make_pa_solver(m, doc);
+  fail(1, "Unknown solver: " + target);
+}
+
+// ---------------------------------------------------------------------------
+// Results: populate_solutions / get_solutions (solver/model_solver.h:111-150,
+// 261-308): walkers ordered by lowest cost (ties by walker index), the first
+// number_of_solutions of them returned, costs include the constant terms.
+// ---------------------------------------------------------------------------
+static std::string render_config(const HostModel& m, const uint8_t* s)
+{
+  std::string o = "{";
+  for (int64_t v = 0; v < m.N; v++)
+  {
+    int val;
+    if (m.kind == K_ISING || m.kind == K_ISING_PLAIN) val = s[v] ? -1 : 1;
+    else if (m.kind == K_MAXSAT) val = s[v] ? 1 : 0;
+    else val = s[v] ? 0 : 1;
+    o += (v ? "," : "") + json::quote(std::to_string(m.names[v])) + ":" + std::to_string(val);
+  }
+  for (size_t i = 0; i < m.free_vars.size(); i++)
+    o += ((m.N || i) ? "," : "") + json::quote(std::to_string(m.free_vars[i])) + ":1";
+  return o + "}";
+}
+
+void Solver::best(double& cost, std::vector<uint8_t>& state)
+{
+  std::vector<double> c, low;
+  std::vector<uint64_t> at, ac;
+  std::vector<uint8_t> ls;
+  fetch(c, low, at, ac, &ls, nullptr);
+  if (low.empty())
+  {
+    cost = model->const_cost;
+    state.clear();
+    return;
+  }
+  size_t b = 0;
+  for (size_t i = 1; i < low.size(); i++)
+    if (low[i] < low[b]) b = i;
+  cost = low[b] + model->const_cost;
+  state.assign(ls.begin() + b * model->N, ls.begin() + (b + 1) * model->N);
+  double hc;
+  std::vector<uint8_t> hs;
+  if (historical_lowest(hc, hs) && hc < low[b])
+  {
+    cost = hc + model->const_cost;
+    state = hs;
+  }
+}
+
+std::string Solver::result_json()
+{
+  std::vector<double> c, low;
+  std::vector<uint64_t> at, ac;
+  std::vector<uint8_t> ls;
+  fetch(c, low, at, ac, &ls, nullptr);
+  uint64_t attempts = 0, accepts = 0;
+  for (size_t i = 0; i < at.size(); i++)
+  {
+    attempts += at[i];
+    accepts += ac[i];
+  }
+  std::string sol = "{\"version\":\"1.0\"";
+  if (!low.empty())
+  {
+    std::vector<size_t> idx(low.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return low[a] < low[b]; });
+    size_t k = std::min((size_t)number_of_solutions, idx.size());
+    // population solvers may have lost their historical lowest
+    // (solver/model_solver.h:280-290): it then comes first
+    std::vector<std::pair<double, const uint8_t*>> list;
+    double hc;
+    std::vector<uint8_t> hs;
+    if (historical_lowest(hc, hs) && hc < low[idx[0]])
+    {
+      list.push_back({hc, hs.data()});
+      k--;
+    }
+    for (size_t j = 0; j < k; j++) list.push_back({low[idx[j]], ls.data() + idx[j] * model->N});
+    sol += ",\"cost\":" + json::number(list[0].first + model->const_cost);
+    sol += ",\"configuration\":" + render_config(*model, list[0].second);
+    sol += ",\"solutions\":[";
+    for (size_t j = 0; j < list.size(); j++)
+      sol += (j ? "," : "") + std::string("{\"cost\":") + json::number(list[j].first + model->const_cost) +
+             ",\"configuration\":" + render_config(*model, list[j].second) + "}";
+    sol += "]";
+  }
+  else
+    sol += ",\"cost\":" + json::number(model->const_cost);
+  sol += ",\"parameters\":{";
+  for (size_t i = 0; i < output_params.size(); i++)
+    sol += (i ? "," : "") + json::quote(output_params[i].first) + ":" + output_params[i].second;
+  sol += "}}";
+  std::string bench = "{\"cost_function_evaluation_count\":" + std::to_string(n_walkers()) +
+                      ",\"cost_difference_evaluation_count\":" + std::to_string(attempts) +
+                      ",\"variable_count\":" + std::to_string(model->N) +
+                      ",\"term_count\":" + std::to_string(model->M) +
+                      ",\"max_locality\":" + std::to_string(model->max_loc) +
+                      ",\"min_locality\":" + std::to_string(model->min_loc) +
+                      ",\"counters\":{\"function_evaluations\":" + std::to_string(n_walkers()) +
+                      ",\"difference_evaluations\":" + std::to_string(attempts) +
+                      ",\"accepted_transitions\":" + std::to_string(accepts) + "}" +
+                      ",\"solver\":{\"last_step\":" + std::to_string(last_step) +
+                      (ran ? "" : ",\"not_run\":true") + "}" +
+                      ",\"gb300\":{\"run_ms\":" + json::number(run_ms) +
+                      ",\"kernel_launches\":" + std::to_string(launches) +
+                      ",\"rng_mode\":" + json::quote(replay ? "replay" : "counter") + "}}";
+  return "{\"benchmark\":" + bench + ",\"solutions\":" + sol + "}";
+}
+}  // namespace qio

@@ -1,0 +1,190 @@
+"""CUDA path against the oracle, through the C ABI (GPU required).
+
+Bar: bit-exact.  Under replayed PCG streams the device must reproduce the
+reference's trajectories exactly: every walker's final cost, lowest cost,
+attempt/accept counts and final/lowest states equal the oracle's.  Costs are
+compared with ==, not a tolerance (FP64 sums run in the reference's order).
+"""
+import numpy as np
+import pytest
+
+import qiotoolkit_gb300 as q
+from qiotoolkit_gb300 import instances as I
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SA = "simulatedannealing.qiotoolkit"
+PT = "paralleltempering.qiotoolkit"
+PA = "populationannealing.cpu"
+
+
+def both(kind, off, ids, coef):
+    return (q.Model(kind, off=off, ids=ids, coef=coef),
+            O.Model(kind, off=off, ids=ids, coef=coef))
+
+
+def assert_same_walkers(g, o, check_states=True):
+    np.testing.assert_array_equal(g["cost"], o.cost)
+    np.testing.assert_array_equal(g["lowest"], o.lowest)
+    np.testing.assert_array_equal(g["attempts"], o.attempts)
+    np.testing.assert_array_equal(g["accepts"], o.accepts)
+    if check_states:
+        np.testing.assert_array_equal(g["states"], o.states)
+        np.testing.assert_array_equal(g["lowest_states"], o.lowest_states)
+
+
+MODELS = {
+    "ising_real": ("ising", lambda: I.er_ising(300, 900, seed=11)),
+    "ising_int": ("ising", lambda: I.cubic_pm_j(6, seed=12)),
+    "ising_plain": ("ising_plain", lambda: I.er_ising(200, 600, seed=13)),
+    "pubo_real": ("pubo", lambda: I.random_pubo(400, 1600, seed=14)),
+    "pubo_int": ("pubo", lambda: I.random_pubo(300, 1200, seed=15, integer=True)),
+    "pubo_plain": ("pubo_plain", lambda: I.random_pubo(200, 700, seed=16)),
+    "maxsat_real": ("maxsat", lambda: I.weighted_maxsat(150, seed=17)),
+    "maxsat_int": ("maxsat", lambda: I.weighted_maxsat(150, seed=18, integer=True)),
+}
+
+
+@pytest.mark.parametrize("name", list(MODELS))
+def test_state_contract(name):
+    kind, gen = MODELS[name]
+    off, ids, coef = gen()
+    g, o = both(kind, off, ids, coef)
+    rng = np.random.default_rng(1)
+    S = rng.integers(0, 2, (16, g.n_vars)).astype(np.uint8)
+    costs = g.calculate_cost(S)
+    assert [o.cost(s) for s in S] == list(costs)
+    vars_ = rng.integers(0, g.n_vars, 16)
+    diffs = g.calculate_cost_difference(S, vars_)
+    assert [o.cost_difference(s, v) for s, v in zip(S, vars_)] == list(diffs)
+    # apply + recompute is consistent with the difference
+    S2 = g.apply_transition(S, vars_)
+    c2 = g.calculate_cost(S2)
+    np.testing.assert_allclose(c2 - costs, diffs, rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", list(MODELS))
+@pytest.mark.parametrize("mode", ["replay", "counter"])
+def test_sa_trajectories(name, mode):
+    kind, gen = MODELS[name]
+    off, ids, coef = gen()
+    g, o = both(kind, off, ids, coef)
+    params = {"seed": 123, "sweeps": 60, "restarts": 12, "beta_start": 0.1,
+              "beta_stop": 3.0, "rng_mode": mode, "maxsat_full_sweep": kind == "maxsat"}
+    s = q.Solver(g, SA, {"params": params}).init().run()
+    r = O.run(o, "sa", seed=123, step_limit=60, restarts=12, sched=("linear", 0.1, 3.0),
+              rng_mode=mode, threads=4, full_maxsat_sweep=kind == "maxsat")
+    assert_same_walkers(s.replicas(), r)
+    c, st = s.best()
+    assert c == r.best_cost
+    # every returned lowest state recomputes to its lowest cost
+    rep = s.replicas()
+    np.testing.assert_array_equal(g.calculate_cost(rep["lowest_states"]), rep["lowest"])
+
+
+def test_sa_maxsat_strict_sweep():
+    """MaxSat's sweep size is 1 in the reference (markov/model.h:169)."""
+    off, ids, coef = I.weighted_maxsat(60, seed=19)
+    g, o = both("maxsat", off, ids, coef)
+    s = q.Solver(g, SA, {"params": {"seed": 5, "sweeps": 500, "restarts": 4}}).init().run()
+    r = O.run(o, "sa", seed=5, step_limit=500, restarts=4, sched=("linear", 0.0, 0.01))
+    assert_same_walkers(s.replicas(), r)
+    assert int(s.replicas()["attempts"][0]) == 500
+
+
+@pytest.mark.parametrize("name", ["ising_real", "pubo_real", "pubo_int", "maxsat_int"])
+@pytest.mark.parametrize("mode", ["replay", "counter"])
+def test_pt_trajectories_and_observables(name, mode):
+    kind, gen = MODELS[name]
+    off, ids, coef = gen()
+    g, o = both(kind, off, ids, coef)
+    temps = {"type": "geometric", "initial": 0.05, "final": 3.0, "count": 8}
+    params = {"seed": 42, "sweeps": 40, "temperatures": temps, "rng_mode": mode,
+              "sweeps_per_replica": 2, "maxsat_full_sweep": True}
+    s = q.Solver(g, PT, {"params": params}).init().run()
+    r = O.run(o, "pt", seed=42, step_limit=40, use_inverse=False,
+              sched=("geometric", 0.05, 3.0), sched_count=8, sweeps_per_replica=2,
+              rng_mode=mode, threads=4, full_maxsat_sweep=True)
+    assert s.stats().near_ties == 0
+    assert_same_walkers(s.replicas(), r)
+    obs = s.pt_observables()
+    np.testing.assert_array_equal(obs[:, :4], r.pt_obs[:, :4])
+    np.testing.assert_array_equal(obs[:-1, 4], r.pt_obs[:-1, 4])
+
+
+def test_pt_restarts_are_independent_seeds():
+    off, ids, coef = MODELS["pubo_real"][1]()
+    g, o = both("pubo", off, ids, coef)
+    params = {"seed": 7, "sweeps": 20, "all_betas": [0.2, 0.7, 1.5, 3.0], "restarts": 3}
+    s = q.Solver(g, PT, {"params": params}).init().run()
+    rep = s.replicas()
+    for k in range(3):
+        r = O.run(o, "pt", seed=7 + k, step_limit=20, sched=("list", 0, 0),
+                  sched_values=[0.2, 0.7, 1.5, 3.0])
+        sl = slice(4 * k, 4 * k + 4)
+        np.testing.assert_array_equal(rep["cost"][sl], r.cost)
+        np.testing.assert_array_equal(rep["lowest"][sl], r.lowest)
+        np.testing.assert_array_equal(rep["lowest_states"][sl], r.lowest_states)
+
+
+@pytest.mark.parametrize("name", ["ising_real", "ising_int", "pubo_real"])
+@pytest.mark.parametrize("constant", [False, True])
+def test_pa_trajectories(name, constant):
+    kind, gen = MODELS[name]
+    off, ids, coef = gen()
+    g, o = both(kind, off, ids, coef)
+    params = {"seed": 9, "sweeps": 25, "population": 24, "threads": 4, "beta_start": 0.0,
+              "beta_stop": 2.0, "sweeps_per_replica": 2, "constant_population": constant}
+    s = q.Solver(g, PA, {"params": params}).init().run()
+    r = O.run(o, "pa", seed=9, step_limit=25, population=24, pa_threads=4,
+              sched=("linear", 0.0, 2.0), sweeps_per_replica=2,
+              constant_population=constant)
+    assert_same_walkers(s.replicas(), r)
+    c, _ = s.best()
+    assert c == r.best_cost
+
+
+def test_reference_solver_pins_on_gpu(golden):
+    """The reference's solver end-result tests, run on the GPU."""
+    for case in golden("solver_pins.json")["cases"]:
+        p = dict(case["params"])
+        doc = {"cost_function": {"type": case["kind"], "version": "1.0",
+                                 "terms": [{"c": c, "ids": ids} for c, ids in case["terms"]]}}
+        if case["solver"] == "pa":
+            p = {"seed": p["seed"], "sweeps": p["sweeps"], "population": 8, "threads": 4}
+        target = {"sa": SA, "pt": PT, "pa": PA}[case["solver"]]
+        res = q.run_json(doc, {"params": p}, target)
+        cost = res["solutions"]["cost"]
+        exp = case["expected_cost"]
+        if isinstance(exp, str):
+            assert cost >= float(exp[2:]) - 1e-9
+        else:
+            assert cost == exp
+        for name, val in case["configuration"].items():
+            assert res["solutions"]["configuration"][name] == val
+
+
+def test_planted_ground_energies_on_gpu(golden):
+    for inst in golden("planted.json")["instances"]:
+        m = q.Model(inst["kind"], inst["terms"])
+        bmax = 3.0 / max(abs(c) for c, _ in inst["terms"])
+        s = q.Solver(m, SA, {"params": {"seed": 7, "sweeps": 200, "restarts": 16,
+                                        "beta_start": 0.0, "beta_stop": bmax}}).init().run()
+        c, _ = s.best()
+        assert c == pytest.approx(inst["energy"], abs=1e-6)
+
+
+def test_ks_independent_streams():
+    """Counter-mode (independent streams) best energies vs the reference's
+    PCG streams over 256 restarts: two-sample KS p > 0.01."""
+    scipy_stats = pytest.importorskip("scipy.stats")
+    off, ids, coef = I.er_ising(300, 900, seed=21)
+    g, o = both("ising", off, ids, coef)
+    s = q.Solver(g, SA, {"params": {"seed": 3, "sweeps": 100, "restarts": 256,
+                                    "beta_start": 0.1, "beta_stop": 3.0,
+                                    "rng_mode": "counter"}}).init().run()
+    r = O.run(o, "sa", seed=3, step_limit=100, restarts=256, sched=("linear", 0.1, 3.0),
+              threads=8)
+    p = scipy_stats.ks_2samp(s.replicas(states=False)["lowest"], r.lowest).pvalue
+    assert p > 0.01
