@@ -78,6 +78,8 @@ typedef struct qio_solver_stats {
   uint64_t near_ties;      /* PT swaps whose device exp() was within 1e-15 of
                               the uniform draw (replay parity caveat)      */
   int64_t device_bytes;    /* HBM held by the solver                       */
+  uint64_t windows;        /* 32-variable evaluation windows committed; the
+                              mean committed window is attempts / windows */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */
@@ -136,8 +138,16 @@ qio_status qio_states_apply(const qio_model* model, int64_t n,
  * "paralleltempering.qiotoolkit", "populationannealing.cpu") configured from
  * the reference's params JSON ({"params": {...}}): replaces
  * create_model_solver (app/runner.cc:134-193) + Solver::configure
- * (solver/solver.h:156-218 and the solver-specific configure()).  GB300
- * options ride in the same object (see the "gb300" keys in the design doc). */
+ * (solver/solver.h:156-218 and the solver-specific configure()).  Options
+ * beyond the reference's ride in the same object:
+ *   "rng_mode": "replay" (default; the reference's PCG streams, trajectories
+ *               identical to it) or "counter" (independent counter-based
+ *               streams keyed by walker, sweep and variable);
+ *   "restarts" (PT): independent tempering ladders, ladder k seeded seed+k;
+ *   "maxsat_full_sweep": attempt every MaxSAT variable per sweep (the
+ *               reference's MaxSat sweep is one attempt, markov/model.h:169);
+ *   "warps_per_block", "profile_kernels": launch shape and per-launch
+ *               CUDA-event timing of the sweep kernels. */
 qio_status qio_solver_create(const qio_model* model, const char* target,
                              const char* params_json, qio_solver** out);
 /* Solver::init (random initial states, solver/simulated_annealing.h:45-74). */

@@ -40,7 +40,7 @@ class SolverStats(C.Structure):
                 ("attempts", C.c_uint64), ("accepts", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("sweep_kernel_ms", C.c_double),
                 ("run_ms", C.c_double), ("near_ties", C.c_uint64),
-                ("device_bytes", C.c_int64)]
+                ("device_bytes", C.c_int64), ("windows", C.c_uint64)]
 
 
 # every symbol include/qio_gb300.h declares, with its ctypes signature

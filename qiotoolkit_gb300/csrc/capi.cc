@@ -291,6 +291,7 @@ qio_status qio_solver_get_stats(qio_solver* s, qio_solver_stats* out)
     out->run_ms = v.run_ms;
     out->near_ties = v.near_ties;
     out->device_bytes = v.device_bytes;
+    out->windows = v.total_windows();
   });
 }
 

@@ -123,6 +123,7 @@ class Solver
   // lowest state ever seen by a population solver (it may have died)
   virtual bool historical_lowest(double&, std::vector<uint8_t>&) { return false; }
   virtual std::string target() const = 0;
+  virtual uint64_t total_windows() { return 0; }
   std::string result_json();
   void best(double& cost, std::vector<uint8_t>& state);
 

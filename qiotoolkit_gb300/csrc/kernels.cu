@@ -78,7 +78,13 @@ __device__ __forceinline__ bool lut_less(const double* ln, uint32_t r, int row,
   int b = (int)(r & 255u);
   double y0 = ln[row * 256 + b - 1];
   double y1 = ln[row * 256 + b];
-  double dist = __ddiv_rn((double)(r >> 8), 16777214.0);
+  // (r >> 8) / 16777214 correctly rounded: reciprocal product corrected by
+  // one fused residual step (Markstein); equal to the IEEE quotient for all
+  // 2^24 inputs (checked exhaustively by the oracle's test).
+  const double x = (double)(r >> 8);
+  const double inv = 5.9604648328104515e-08;  // RN(1 / 16777214)
+  const double d0 = __dmul_rn(x, inv);
+  const double dist = __fma_rn(__fma_rn(-d0, 16777214.0, x), inv, d0);
   double value = __dadd_rn(y0, __dmul_rn(dist, __dsub_rn(y1, y0)));
   return value < thr;
 }
@@ -289,6 +295,7 @@ __global__ void __launch_bounds__(128) init_kernel(InitArgs a)
     a.p.accepts[w] = 0;
     a.p.step_att[w] = 0;
     a.p.step_acc[w] = 0;
+    if (a.p.windows) a.p.windows[w] = 0;
   }
 }
 
@@ -327,7 +334,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a)
     double low = a.p.lowest[r];
     long long icost = INT ? (long long)cost : 0;
     long long ilow = INT ? (long long)low : 0;
-    unsigned long long natt = 0, nacc = 0;
+    unsigned long long natt = 0, nacc = 0, nwin = 0;
     uint64_t key = 0;
     if (!REPLAY)
       key = counter_key(a.seed + (uint32_t)(r / a.key_div),
@@ -593,6 +600,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a)
           __syncwarp();
         }
         natt += (unsigned long long)adv;
+        nwin++;
         nacc += (unsigned long long)__popc(flips);
         if (REPLAY) rs = s_A[draws] * rs + s_C[draws];
         i += adv;
@@ -606,6 +614,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a)
       a.p.accepts[r] += nacc;
       a.p.step_att[r] += natt;
       a.p.step_acc[r] += nacc;
+      if (a.p.windows) a.p.windows[r] += nwin;
     }
     __syncwarp();
   }
@@ -791,6 +800,7 @@ __global__ void pa_copy_kernel(DevPop src, DevPop dst, const int* src_of, int n_
     dst.accepts[j] = src.accepts[i];
     dst.step_att[j] = 0;
     dst.step_acc[j] = 0;
+    if (dst.windows) dst.windows[j] = src.windows ? src.windows[i] : 0;
   }
 }
 

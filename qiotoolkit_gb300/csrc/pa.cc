@@ -21,6 +21,7 @@ namespace qio
 {
 uint64_t host_counter_key(uint32_t seed, uint64_t stream);
 void configure_common_public(Solver& s, const json::Value& doc);
+uint64_t sum_windows(const DevPop& p, int n);
 
 namespace
 {
@@ -153,7 +154,7 @@ struct Pool
     auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
     size_t o_sp = take(S * nw * 4), o_ts = take(S * mp), o_c = take(S * 8), o_l = take(S * 8),
            o_ls = take(S * nw * 4), o_at = take(S * 8), o_ac = take(S * 8), o_sa = take(S * 8),
-           o_sc = take(S * 8);
+           o_sc = take(S * 8), o_wi = take(S * 8);
     buf = DevBuf(off);
     char* b = (char*)buf.ptr;
     pop.n = capacity;
@@ -168,6 +169,7 @@ struct Pool
     pop.accepts = (unsigned long long*)(b + o_ac);
     pop.step_att = (unsigned long long*)(b + o_sa);
     pop.step_acc = (unsigned long long*)(b + o_sc);
+    pop.windows = (unsigned long long*)(b + o_wi);
   }
 };
 }  // namespace
@@ -221,6 +223,7 @@ class PopulationAnnealing : public Solver
     return true;
   }
   std::string target() const override { return target_name(); }
+  uint64_t total_windows() override { return sum_windows(pools[cur].pop, (int)n_walkers()); }
 
   void configure(const json::Value& doc)
   {

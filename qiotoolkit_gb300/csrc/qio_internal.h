@@ -73,6 +73,7 @@ struct DevPop
   unsigned long long* accepts;    // n (per walker)
   unsigned long long* step_att;   // n (per walker, since last observation)
   unsigned long long* step_acc;   // n
+  unsigned long long* windows;    // n (per walker: window iterations), or null
 };
 
 struct SweepArgs

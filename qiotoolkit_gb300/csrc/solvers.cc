@@ -193,7 +193,7 @@ struct Population
     };
     size_t o_sp = take(S * nw * 4), o_ts = take(S * mp), o_c = take(S * 8),
            o_l = take(S * 8), o_ls = take(S * nw * 4), o_at = take(S * 8),
-           o_ac = take(S * 8), o_sa = take(S * 8), o_sc = take(S * 8),
+           o_ac = take(S * 8), o_sa = take(S * 8), o_sc = take(S * 8), o_wi = take(S * 8),
            o_rng = take((size_t)streams * 8), o_slot = take(need_slots ? S * 4 : 0),
            o_beta = take((size_t)n_beta * 8);
     buf = DevBuf(off);
@@ -210,6 +210,7 @@ struct Population
     pop.accepts = (unsigned long long*)(b + o_ac);
     pop.step_att = (unsigned long long*)(b + o_sa);
     pop.step_acc = (unsigned long long*)(b + o_sc);
+    pop.windows = (unsigned long long*)(b + o_wi);
     rng = (uint64_t*)(b + o_rng);
     slot_of = need_slots ? (int*)(b + o_slot) : nullptr;
     beta = (double*)(b + o_beta);
@@ -224,6 +225,16 @@ struct Population
         out[r * N + v] = (words[r * nw + v / 32] >> (v % 32)) & 1u;
   }
 };
+
+uint64_t sum_windows(const DevPop& p, int n)
+{
+  if (n <= 0 || !p.windows) return 0;
+  std::vector<unsigned long long> w(n);
+  cuda_check(cudaMemcpy(w.data(), p.windows, (size_t)n * 8, cudaMemcpyDeviceToHost), "D2H");
+  uint64_t t = 0;
+  for (auto x : w) t += x;
+  return t;
+}
 
 static int pick_wpb(int requested, int streams)
 {
@@ -429,6 +440,8 @@ class SimulatedAnnealing : public Solver
     run_ms = total.stop();
     sweep_ms = profile ? prof_total_ms() : run_ms;
   }
+
+  uint64_t total_windows() override { return sum_windows(P.pop, (int)n_walkers()); }
 
   void fetch(std::vector<double>& cost, std::vector<double>& lowest,
              std::vector<uint64_t>& att, std::vector<uint64_t>& acc,
@@ -657,6 +670,8 @@ class ParallelTempering : public Solver
     cuda_check(cudaMemcpy(&nt, ties, 8, cudaMemcpyDeviceToHost), "D2H");
     near_ties = nt;
   }
+
+  uint64_t total_windows() override { return sum_windows(P.pop, (int)n_walkers()); }
 
   void fetch(std::vector<double>& cost, std::vector<double>& lowest,
              std::vector<uint64_t>& att, std::vector<uint64_t>& acc,

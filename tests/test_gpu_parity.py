@@ -78,9 +78,13 @@ def test_sa_trajectories(name, mode):
     assert_same_walkers(s.replicas(), r)
     c, st = s.best()
     assert c == r.best_cost
-    # every returned lowest state recomputes to its lowest cost
+    # every returned lowest state recomputes to its lowest cost; the running
+    # cost accumulates rounding like the reference's cost_ += diff, so a full
+    # recompute agrees to rounding only (the reference's own debug check is
+    # |recalculated - lowest| < 0.1, solver/simulated_annealing.h:112-121)
     rep = s.replicas()
-    np.testing.assert_array_equal(g.calculate_cost(rep["lowest_states"]), rep["lowest"])
+    np.testing.assert_allclose(g.calculate_cost(rep["lowest_states"]), rep["lowest"],
+                               rtol=1e-12, atol=1e-9)
 
 
 def test_sa_maxsat_strict_sweep():
