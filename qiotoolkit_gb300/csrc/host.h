@@ -41,6 +41,8 @@ struct DevBuf
 };
 
 void ensure_device();  // selects the device, uploads tables once per device
+int* device_error_flag();       // per-device int set by kernels whose bounded waits gave up
+void check_device_error(cudaStream_t s);  // throws QIO_TIMEOUT (status 4) when set
 
 struct HostModel
 {
@@ -148,6 +150,7 @@ class Solver
   int64_t device_bytes = 0;
   bool initialized = false, ran = false;
   bool profile = false;  // bracket every sweep launch with CUDA events
+  bool smem_state = true;  // walker state in shared memory when it fits
   // CUDA-event pairs around sweep launches (profile mode)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   size_t prof_used = 0;

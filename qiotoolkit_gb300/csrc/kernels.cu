@@ -291,334 +291,15 @@ __global__ void __launch_bounds__(128) init_kernel(InitArgs a)
   {
     a.p.cost[slot] = cost;
     a.p.lowest[w] = cost;
-    a.p.attempts[w] = 0;
-    a.p.accepts[w] = 0;
+    if (!a.keep_counters)
+    {
+      a.p.attempts[w] = 0;
+      a.p.accepts[w] = 0;
+    }
     a.p.step_att[w] = 0;
     a.p.step_acc[w] = 0;
     if (a.p.windows) a.p.windows[w] = 0;
   }
-}
-
-// ---------------------------------------------------------------------------
-// Windowed sweep.
-// ---------------------------------------------------------------------------
-template <int FL, bool REPLAY, bool INT>
-__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a)
-{
-  __shared__ double s_ln[1024];
-  __shared__ unsigned long long s_A[65], s_C[65];
-  for (int t = threadIdx.x; t < 1024; t += blockDim.x) s_ln[t] = c_ln[t];
-  for (int t = threadIdx.x; t < 65; t += blockDim.x)
-  {
-    s_A[t] = c_jA[t];
-    s_C[t] = c_jC[t];
-  }
-  __syncthreads();
-
-  const int lane = threadIdx.x & 31;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= a.n_streams) return;
-  const DevModel m = a.m;
-  const int S = m.sweep_size;
-  const int nwd = (m.n_vars + 31) >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  uint64_t rs = REPLAY ? a.rng[w] : 0;
-
-  for (int r = w; r < a.n_walkers; r += a.n_streams)
-  {
-    const int slot = a.slot_of ? a.slot_of[r] : r;
-    uint32_t* spins = a.p.spins + (size_t)slot * a.p.nw;
-    uint8_t* ts = a.p.tstate + (size_t)slot * a.p.mp;
-    uint32_t* lsp = a.p.lspins + (size_t)r * a.p.nw;
-    double cost = a.p.cost[slot];
-    double low = a.p.lowest[r];
-    long long icost = INT ? (long long)cost : 0;
-    long long ilow = INT ? (long long)low : 0;
-    unsigned long long natt = 0, nacc = 0, nwin = 0;
-    uint64_t key = 0;
-    if (!REPLAY)
-      key = counter_key(a.seed + (uint32_t)(r / a.key_div),
-                        a.key_base + (unsigned long long)(r % a.key_div));
-
-    for (int k = 0; k < a.n_sweeps; k++)
-    {
-      const long long sw = a.sweep_base + k;
-      const double beta = a.beta[(long long)r * a.bs_w + sw * a.bs_s];
-      const double nbeta = -beta;
-      const unsigned long long ctr0 = (unsigned long long)sw * (unsigned long long)S;
-      int i = 0;
-      while (i < S)
-      {
-        const int v = i + lane;
-        const bool valid = v < S;
-        double dE = 0.0;
-        long long idE = 0;
-        int rb = 0, re = 0;
-        uint32_t sv = 0;
-        if (valid)
-        {
-          rb = m.row[v];
-          re = m.row[v + 1];
-          sv = spin_of(spins, v);
-          if (FL == F_PARITY)
-          {
-            if (INT)
-            {
-              int acc = 0;
-#pragma unroll 4
-              for (int q = rb; q < re; q++)
-              {
-                uint32_t t = m.inc[q];
-                int c = m.coef_i[q];
-                acc += ts[t] ? -c : c;
-              }
-              idE = -2 * (long long)acc;
-            }
-            else
-            {
-              double diff = 0.0;
-#pragma unroll 4
-              for (int q = rb; q < re; q++)
-              {
-                uint32_t t = m.inc[q];
-                double c = m.coef[q];
-                diff = __dadd_rn(diff, ts[t] ? -c : c);
-              }
-              dE = __dmul_rn(2.0, -diff);
-            }
-          }
-          else if (FL == F_COUNTER)
-          {
-            if (INT)
-            {
-              int acc = 0;
-#pragma unroll 4
-              for (int q = rb; q < re; q++)
-              {
-                uint32_t e = m.inc[q];
-                uint8_t z = ts[e & ~kNegBit];
-                int c = m.coef_i[q];
-                if (sv ^ (e >> 31)) { if (z == 1) acc += c; }
-                else { if (z == 0) acc -= c; }
-              }
-              idE = acc;
-            }
-            else
-            {
-              double diff = 0.0;
-#pragma unroll 4
-              for (int q = rb; q < re; q++)
-              {
-                uint32_t e = m.inc[q];
-                uint8_t z = ts[e & ~kNegBit];
-                double c = m.coef[q];
-                if (sv ^ (e >> 31)) { if (z == 1) diff = __dadd_rn(diff, c); }
-                else { if (z == 0) diff = __dsub_rn(diff, c); }
-              }
-              dE = diff;
-            }
-          }
-          else
-          {
-            // plain models: gather the members of each incident term
-            double diff = 0.0;
-            long long iacc = 0;
-            for (int q = rb; q < re; q++)
-            {
-              int t = (int)m.inc[q];
-              int tb = m.trow[t], te = m.trow[t + 1];
-              if (FL == F_PLAIN_ISING)
-              {
-                uint32_t par = 0;
-                for (int u = tb; u < te; u++) par ^= spin_of(spins, (int)m.tvar[u]);
-                if (INT) iacc += par ? -(long long)m.coef_i[q] : (long long)m.coef_i[q];
-                else diff = __dadd_rn(diff, par ? -m.coef[q] : m.coef[q]);
-              }
-              else
-              {
-                bool zero = false;
-                for (int u = tb; u < te; u++)
-                {
-                  int x = (int)m.tvar[u];
-                  if (x != v && spin_of(spins, x)) { zero = true; break; }
-                }
-                if (!zero)
-                {
-                  if (INT) iacc += sv ? (long long)m.coef_i[q] : -(long long)m.coef_i[q];
-                  else diff = __dadd_rn(diff, sv ? m.coef[q] : -m.coef[q]);
-                }
-              }
-            }
-            if (FL == F_PLAIN_ISING)
-            {
-              if (INT) idE = -2 * iacc;
-              else dE = __dmul_rn(2.0, -diff);
-            }
-            else
-            {
-              if (INT) idE = iacc;
-              else dE = diff;
-            }
-          }
-          if (INT) dE = (double)idE;
-        }
-
-        // ---- acceptance --------------------------------------------------
-        const bool uphill = valid && !(dE <= 0.0);
-        bool acc = valid && !uphill;
-        bool redraw = false;
-        unsigned U = 0;
-        int pos = 0;
-        if (REPLAY)
-        {
-          U = __ballot_sync(kFull, uphill);
-          pos = __popc(U & lt);
-          if (uphill)
-          {
-            uint32_t r0 = pcg_out(s_A[pos] * rs + s_C[pos]);
-            redraw = (r0 & 255u) == 0;
-            if (!redraw) acc = lut_less(s_ln, r0, 0, __dmul_rn(dE, nbeta));
-          }
-        }
-        else if (uphill)
-        {
-          const unsigned long long ctr = ctr0 + (unsigned long long)v;
-          uint64_t w0 = counter_draw(key, 2ULL * ctr);
-          int used;
-          acc = metropolis_uphill(
-              __dmul_rn(dE, nbeta), s_ln,
-              [&](int q) -> uint32_t {
-                if (q == 0) return (uint32_t)w0;
-                if (q == 1) return (uint32_t)(w0 >> 32);
-                uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
-                return q == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
-              },
-              used);
-        }
-        const unsigned A = __ballot_sync(kFull, acc);
-        bool conf = false;
-        if (valid && lane > 0) conf = (m.nbr[v] & (__brev(A) >> (32 - lane))) != 0u;
-        const unsigned Cm = __ballot_sync(kFull, conf);
-        const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
-        const int nvalid = min(32, S - i);
-        const unsigned stop = Cm | Rm;
-        int f = stop ? (__ffs(stop) - 1) : 32;
-        if (f > nvalid) f = nvalid;
-        const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
-        const unsigned commit = (f >= 32) ? kFull : ((1u << f) - 1u);
-        unsigned flips = A & commit;
-        int draws = REPLAY ? __popc(U & commit) : 0;
-        if (REPLAY && slow)
-        {
-          // lane f drew a zero bucket: finish its redraw chain sequentially
-          int sacc = 0, used = 0;
-          if (lane == f)
-          {
-            bool ok = metropolis_uphill(
-                __dmul_rn(dE, nbeta), s_ln,
-                [&](int q) -> uint32_t {
-                  return pcg_out(s_A[pos + q] * rs + s_C[pos + q]);
-                },
-                used);
-            sacc = ok ? 1 : 0;
-          }
-          sacc = __shfl_sync(kFull, sacc, f);
-          used = __shfl_sync(kFull, used, f);
-          if (sacc) flips |= 1u << f;
-          draws += used;
-        }
-        const int adv = f + (slow ? 1 : 0);
-
-        // ---- apply accepted flips (their term sets are disjoint) ----------
-        if ((flips >> lane) & 1u)
-        {
-          if (FL == F_PARITY)
-          {
-            for (int q = rb; q < re; q++) ts[m.inc[q]] ^= (uint8_t)1;
-          }
-          else if (FL == F_COUNTER)
-          {
-            for (int q = rb; q < re; q++)
-            {
-              uint32_t e = m.inc[q];
-              uint32_t t = e & ~kNegBit;
-              ts[t] = (uint8_t)(ts[t] + ((sv ^ (e >> 31)) ? 0xFFu : 1u));
-            }
-          }
-        }
-        const int wi = i >> 5, o = i & 31;
-        if (lane == 0 && flips)
-        {
-          spins[wi] ^= flips << o;
-          if (o)
-          {
-            unsigned hi = flips >> (32 - o);
-            if (hi) spins[wi + 1] ^= hi;
-          }
-        }
-        // ---- running cost and lowest state, in attempt order --------------
-        int lowpos = -1;
-        unsigned fl = flips;
-        while (fl)
-        {
-          const int j = __ffs(fl) - 1;
-          fl &= fl - 1;
-          if (INT)
-          {
-            icost += __shfl_sync(kFull, idE, j);
-            if (icost < ilow)
-            {
-              ilow = icost;
-              lowpos = j;
-            }
-          }
-          else
-          {
-            cost = __dadd_rn(cost, __shfl_sync(kFull, dE, j));
-            if (cost < low)
-            {
-              low = cost;
-              lowpos = j;
-            }
-          }
-        }
-        __syncwarp();
-        if (lowpos >= 0)
-        {
-          for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
-          __syncwarp();
-          const unsigned undo = flips & ~((2u << lowpos) - 1u);
-          if (lane == 0 && undo)
-          {
-            lsp[wi] ^= undo << o;
-            if (o)
-            {
-              unsigned hi = undo >> (32 - o);
-              if (hi) lsp[wi + 1] ^= hi;
-            }
-          }
-          __syncwarp();
-        }
-        natt += (unsigned long long)adv;
-        nwin++;
-        nacc += (unsigned long long)__popc(flips);
-        if (REPLAY) rs = s_A[draws] * rs + s_C[draws];
-        i += adv;
-      }
-    }
-    if (lane == 0)
-    {
-      a.p.cost[slot] = INT ? (double)icost : cost;
-      a.p.lowest[r] = INT ? (double)ilow : low;
-      a.p.attempts[r] += natt;
-      a.p.accepts[r] += nacc;
-      a.p.step_att[r] += natt;
-      a.p.step_acc[r] += nacc;
-      if (a.p.windows) a.p.windows[r] += nwin;
-    }
-    __syncwarp();
-  }
-  if (REPLAY && lane == 0) a.rng[w] = rs;
 }
 
 // ---------------------------------------------------------------------------
@@ -815,6 +496,9 @@ cudaError_t launch_pa_copy(const DevPop& src, const DevPop& dst, const int* src_
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+void sw_upload(const double* ln, const float* scr, const unsigned long long* jA,
+               const unsigned long long* jC);
+
 void upload_tables(int)
 {
   double ln[1024];
@@ -841,6 +525,26 @@ void upload_tables(int)
   cudaMemcpyToSymbol(c_jC, jC, sizeof jC);
   cudaMemcpyToSymbol(c_pA, pA, sizeof pA);
   cudaMemcpyToSymbol(c_pC, pC, sizeof pC);
+  // FP32 screen of the ln-table comparison: per (row, bucket) the double
+  // y0 and RN(y1 - y0) rounded to float, and an error margin 2^-19 (|y0| +
+  // |dy|) that covers the float rounding of y0, dy, the distance and the
+  // multiply-add against the double expression
+  float scr[3072];
+  for (int row = 0; row < 4; row++)
+    for (int b = 0; b < 256; b++)
+    {
+      float* e = scr + (row * 256 + b) * 3;
+      if (b < 2)
+      {
+        e[0] = e[1] = e[2] = 0.f;
+        continue;
+      }
+      double y0 = ln[row * 256 + b - 1], dy = ln[row * 256 + b] - y0;
+      e[0] = (float)y0;
+      e[1] = (float)dy;
+      e[2] = (float)(ldexp(fabs(y0) + fabs(dy), -19));
+    }
+  sw_upload(ln, scr, jA, jC);
 }
 
 template <int FL, bool INT>
@@ -860,37 +564,6 @@ cudaError_t launch_init(const InitArgs& a, cudaStream_t s)
     case F_COUNTER: I ? init_dispatch<F_COUNTER, true>(a, s) : init_dispatch<F_COUNTER, false>(a, s); break;
     case F_PLAIN_ISING: I ? init_dispatch<F_PLAIN_ISING, true>(a, s) : init_dispatch<F_PLAIN_ISING, false>(a, s); break;
     default: I ? init_dispatch<F_PLAIN_PUBO, true>(a, s) : init_dispatch<F_PLAIN_PUBO, false>(a, s); break;
-  }
-  return cudaGetLastError();
-}
-
-template <int FL, bool R, bool I>
-static void sweep_dispatch(const SweepArgs& a, cudaStream_t s, int wpb)
-{
-  int blocks = (a.n_streams + wpb - 1) / wpb;
-  if (blocks > 0) sweep_kernel<FL, R, I><<<blocks, 32 * wpb, 0, s>>>(a);
-}
-
-template <int FL>
-static void sweep_flavor(const SweepArgs& a, cudaStream_t s, int wpb)
-{
-  const bool I = a.m.int_mode != 0;
-  if (a.replay)
-    I ? sweep_dispatch<FL, true, true>(a, s, wpb) : sweep_dispatch<FL, true, false>(a, s, wpb);
-  else
-    I ? sweep_dispatch<FL, false, true>(a, s, wpb) : sweep_dispatch<FL, false, false>(a, s, wpb);
-}
-
-cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int wpb)
-{
-  if (wpb < 1) wpb = 1;
-  if (wpb > 8) wpb = 8;
-  switch (a.m.flavor)
-  {
-    case F_PARITY: sweep_flavor<F_PARITY>(a, s, wpb); break;
-    case F_COUNTER: sweep_flavor<F_COUNTER>(a, s, wpb); break;
-    case F_PLAIN_ISING: sweep_flavor<F_PLAIN_ISING>(a, s, wpb); break;
-    default: sweep_flavor<F_PLAIN_PUBO>(a, s, wpb); break;
   }
   return cudaGetLastError();
 }

@@ -43,9 +43,35 @@ DevBuf& DevBuf::operator=(DevBuf&& o) noexcept
   return *this;
 }
 
+static std::mutex g_dev_mu;
+static std::map<int, int*> g_err;
+
+int* device_error_flag()
+{
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> g(g_dev_mu);
+  auto it = g_err.find(dev);
+  return it == g_err.end() ? nullptr : it->second;
+}
+
+void check_device_error(cudaStream_t s)
+{
+  int* e = device_error_flag();
+  if (!e) return;
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, e, 4, cudaMemcpyDeviceToHost, s), "D2H error flag");
+  cuda_check(cudaStreamSynchronize(s), "sync");
+  if (h)
+  {
+    cuda_check(cudaMemsetAsync(e, 0, 4, s), "memset");
+    fail(4, "a device-side wait for a bulk copy gave up (bounded wait); results are invalid");
+  }
+}
+
 void ensure_device()
 {
-  static std::mutex mu;
+  static std::mutex& mu = g_dev_mu;
   static std::set<int> ready;
   int count = 0;
   cudaError_t e = cudaGetDeviceCount(&count);
@@ -57,6 +83,10 @@ void ensure_device()
   if (ready.count(dev)) return;
   upload_tables(dev);
   cuda_check(cudaGetLastError(), "upload_tables");
+  int* flag = nullptr;
+  cuda_check(cudaMalloc(&flag, 4), "cudaMalloc");
+  cuda_check(cudaMemset(flag, 0, 4), "cudaMemset");
+  g_err[dev] = flag;
   ready.insert(dev);
 }
 
@@ -323,7 +353,9 @@ void HostModel::upload() const
   size_t o_row = put(blob, row), o_inc = put(blob, inc), o_coef = put(blob, coef),
          o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i);
-  blob.resize((blob.size() + 255) & ~(size_t)255);
+  // 256 bytes of tail padding: bulk copies of incidence ranges round their
+  // end up to 16 bytes
+  blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
   dmem = DevBuf(blob.size());
   cuda_check(cudaMemcpy(dmem.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice),
              "model upload");

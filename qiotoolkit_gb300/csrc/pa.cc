@@ -22,6 +22,7 @@ namespace qio
 uint64_t host_counter_key(uint32_t seed, uint64_t stream);
 void configure_common_public(Solver& s, const json::Value& doc);
 uint64_t sum_windows(const DevPop& p, int n);
+int pick_wpb(int requested, int streams);
 
 namespace
 {
@@ -304,6 +305,14 @@ class PopulationAnnealing : public Solver
     }
     for (size_t i = 0; i < target_pop; i++) family[i] = i;
     InitArgs a{};
+    // citizens that already exist keep their counters across a restart;
+    // new ones start from zero (their slots are cleared first)
+    a.keep_counters = 1;
+    if (old < R)
+    {
+      cuda_check(cudaMemsetAsync(pools[cur].pop.attempts + old, 0, (R - old) * 8, st), "memset");
+      cuda_check(cudaMemsetAsync(pools[cur].pop.accepts + old, 0, (R - old) * 8, st), "memset");
+    }
     a.m = model->device_view(full_maxsat_sweep);
     a.p = pools[cur].pop;
     a.n_walkers = (int)R;
@@ -508,8 +517,9 @@ void PopulationAnnealing::run(cudaStream_t st)
     a.seed = seed;
     a.key_base = (unsigned long long)(step + 1) << 32;
     a.key_div = (long long)1 << 40;
-    int wpb = std::max(1, std::min(4, a.n_streams / 152));
-    if (warps_per_block > 0) wpb = warps_per_block;
+    a.smem_state = smem_state ? 1 : 0;
+    a.err = device_error_flag();
+    int wpb = pick_wpb(warps_per_block, a.n_streams);
     prof_begin(st);
     cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
     prof_end(st);
@@ -664,6 +674,7 @@ void PopulationAnnealing::run(cudaStream_t st)
   sweep_ms = profile ? prof_total_ms() : ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  check_device_error(st);
 }
 
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc)

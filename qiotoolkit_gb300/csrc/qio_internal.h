@@ -93,6 +93,7 @@ struct SweepArgs
   unsigned long long key_base;  //                      key_base + w % key_div)
   long long key_div;
   int smem_state;       // stage spins + term state in shared memory
+  int* err;             // device error flag (a bounded wait gave up)
 };
 
 struct InitArgs
@@ -107,6 +108,7 @@ struct InitArgs
   unsigned long long key_base;
   long long key_div;
   const uint8_t* given;     // optional: explicit states (n_walkers * n_vars)
+  int keep_counters;        // 1: keep attempt/accept totals (population re-init)
 };
 
 // ---- launchers (kernels.cu) -------------------------------------------

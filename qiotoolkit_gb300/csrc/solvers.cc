@@ -125,6 +125,7 @@ static void configure_common(Solver& s, const json::Value& doc)
   s.full_maxsat_sweep = p.boolean("maxsat_full_sweep", false);
   s.warps_per_block = (int)p.integer("warps_per_block", 0);
   s.profile = p.boolean("profile_kernels", false);
+  s.smem_state = p.boolean("smem_state", true);
   s.output_params.push_back({"seed", std::to_string(s.seed)});
   s.output_params.push_back({"step_limit", std::to_string(s.step_limit)});
 }
@@ -236,11 +237,14 @@ uint64_t sum_windows(const DevPop& p, int n)
   return t;
 }
 
-static int pick_wpb(int requested, int streams)
+// warps per block: enough that the grid needs at most one block per SM
+// (152 SMs), so every sub-partition runs at most one walker's warp when the
+// walkers are fewer than the sub-partitions
+int pick_wpb(int requested, int streams)
 {
   if (requested > 0) return std::min(8, requested);
-  int w = streams / 152;
-  return std::max(1, std::min(4, w));
+  int w = (streams + 151) / 152;
+  return std::max(1, std::min(8, w));
 }
 
 struct EventTimer
@@ -381,6 +385,8 @@ class SimulatedAnnealing : public Solver
     a.seed = seed;
     a.key_base = 0;
     a.key_div = (long long)1 << 40;
+    a.smem_state = smem_state ? 1 : 0;
+    a.err = device_error_flag();
     return a;
   }
 
@@ -439,6 +445,7 @@ class SimulatedAnnealing : public Solver
     }
     run_ms = total.stop();
     sweep_ms = profile ? prof_total_ms() : run_ms;
+    check_device_error(st);
   }
 
   uint64_t total_windows() override { return sum_windows(P.pop, (int)n_walkers()); }
@@ -618,6 +625,8 @@ class ParallelTempering : public Solver
     a.seed = seed;
     a.key_base = 0;
     a.key_div = T();
+    a.smem_state = smem_state ? 1 : 0;
+    a.err = device_error_flag();
     SwapArgs sw{};
     sw.restarts = restarts;
     sw.n_temps = T();
@@ -666,6 +675,7 @@ class ParallelTempering : public Solver
     last_step = s;
     run_ms = total.stop();
     sweep_ms = profile ? prof_total_ms() : run_ms;
+    check_device_error(st);
     unsigned long long nt = 0;
     cuda_check(cudaMemcpy(&nt, ties, 8, cudaMemcpyDeviceToHost), "D2H");
     near_ties = nt;

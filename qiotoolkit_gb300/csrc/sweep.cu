@@ -1,0 +1,793 @@
+// sweep.cu -- the windowed Metropolis sweep (sm_103a).
+//
+// One warp owns one walker.  A window of 32 consecutive variables is
+// evaluated at once (lane l takes variable i + l), each lane summing its own
+// cost difference in the reference's term order; decisions are committed in
+// lane order up to the first lane whose terms intersect an earlier accepted
+// flip in the window, or whose draw needs the redraw path (markov/
+// metropolis.h:93-103); the next window starts there.  Replay streams are
+// PCG32 positions: lane l's draw is the stream advanced by the number of
+// uphill lanes before it, so the committed prefix consumes exactly the
+// draws of the sequential chain (markov/walker.h:143-153,209-229).
+//
+// GB300 specifics.  A warp-wide FP64 instruction costs one sub-partition
+// ~64 cycles whatever its active mask, so FP64 is spent only where the
+// reference's rounding must be reproduced: the ordered cost-difference sums
+// (compacted to the terms that contribute, for PUBO/MaxSAT) and the running
+// cost.  Sign tests and cost comparisons use integer keys of the IEEE bit
+// patterns, the x(-2) of the Ising difference is an exponent increment, and
+// the ln-table comparison runs in FP32 with a rigorous error margin, falling
+// back to the exact FP64 expression only inside the margin.  Walker state
+// (term bytes, spins, lowest spins) lives in shared memory when it fits.
+#include <type_traits>
+
+#include "qio_internal.h"
+
+namespace qio
+{
+namespace sw
+{
+static const unsigned kFull = 0xffffffffu;
+static const unsigned long long kGamma = 0x9E3779B97F4A7C15ULL;
+static const int kScratch = 32;  // compaction chunk (incidences per lane)
+
+__constant__ double c_ln[1024];
+__constant__ float c_scr[1024 * 3];  // y0, dy, err per (row, bucket)
+__constant__ unsigned long long c_jA[65], c_jC[65];
+
+__device__ __forceinline__ uint32_t pcg_out(uint64_t old)
+{
+  uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+  uint32_t rot = (uint32_t)(old >> 59u);
+  return __funnelshift_r(xs, xs, rot);
+}
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint64_t counter_key(uint32_t seed, uint64_t stream)
+{
+  return mix64(((uint64_t)seed << 32) ^ mix64(stream + kGamma));
+}
+__device__ __forceinline__ uint64_t counter_draw(uint64_t key, uint64_t ctr)
+{
+  return mix64(key + ctr * kGamma);
+}
+
+// ---- IEEE bit helpers (integer pipe) ------------------------------------
+// x <= 0 for a non-NaN double
+__device__ __forceinline__ bool le_zero(double x)
+{
+  long long b = __double_as_longlong(x);
+  if (b == 0) return true;
+  unsigned long long mag = (unsigned long long)b & 0x7FFFFFFFFFFFFFFFULL;
+  return b < 0 && mag <= 0x7FF0000000000000ULL;
+}
+// monotone integer key: key(a) < key(b) <=> a < b (non-NaN; -0 taken as +0)
+__device__ __forceinline__ long long order_key(double x)
+{
+  long long b = __double_as_longlong(x);
+  if (b == (long long)0x8000000000000000LL) b = 0;
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+// exact -2x (Ising: 2.0 * (-diff), model/ising.h:116) by exponent arithmetic
+__device__ __forceinline__ double neg2x(double x)
+{
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFULL;
+  unsigned long long sgn = (b ^ 0x8000000000000000ULL) & 0x8000000000000000ULL;
+  if (mag < 0x0010000000000000ULL) return __longlong_as_double((long long)(sgn | (mag << 1)));
+  if (mag < 0x7FE0000000000000ULL)
+    return __longlong_as_double((long long)(sgn | (mag + 0x0010000000000000ULL)));
+  return __dmul_rn(2.0, -x);
+}
+// float approximation of a double from its bits, |rel err| < 2^-23
+__device__ __forceinline__ float approx_float(double x)
+{
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  unsigned s = (unsigned)(b >> 63) << 31;
+  int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1023 - 126) return __int_as_float((int)s);
+  if (e > 1023 + 127) return __int_as_float((int)(s | 0x7F800000u));
+  unsigned m = (unsigned)((b >> 29) & 0x7FFFFFu);
+  return __int_as_float((int)(s | ((unsigned)(e - 1023 + 127) << 23) | m));
+}
+
+// exact comparison of markov/metropolis.h:96-103 with the distance
+// (r >> 8) / 16777214 correctly rounded via a corrected reciprocal
+__device__ __forceinline__ bool lut_less_exact(const double* ln, uint32_t r, int row,
+                                               double thr)
+{
+  int b = (int)(r & 255u);
+  double y0 = ln[row * 256 + b - 1];
+  double y1 = ln[row * 256 + b];
+  const double x = (double)(r >> 8);
+  const double inv = 5.9604648328104515e-08;  // RN(1 / 16777214)
+  const double d0 = __dmul_rn(x, inv);
+  const double dist = __fma_rn(__fma_rn(-d0, 16777214.0, x), inv, d0);
+  double value = __dadd_rn(y0, __dmul_rn(dist, __dsub_rn(y1, y0)));
+  return value < thr;
+}
+
+// value < thr decided in FP32 when the margin allows it.  thr = dE * (-beta)
+// rounded to double; thr_f approximates it within 2^-21.7 |thr_f|; the margin
+// used is 2^-19 |thr_f| (+1e-30).  The value side uses the per-bucket margin
+// 2^-19 (|y0| + |dy|) against a bound of 2^-21.5 (|y0| + |dy|).
+// Returns 1 accept, 0 reject, -1 undecided.
+__device__ __forceinline__ int lut_screen(const float* scr, uint32_t r, int row, float thr_f)
+{
+  int b = (int)(r & 255u);
+  if (b == 1) return 0;  // y0 = log(0): the value is NaN and never less
+  int k = (row * 256 + b) * 3;
+  float y0 = scr[k], dy = scr[k + 1], ev = scr[k + 2];
+  float dist = __fmul_rn((float)(r >> 8), 5.96046483e-08f);
+  float value = __fmaf_rn(dist, dy, y0);
+  float et = __fmaf_rn(fabsf(thr_f), 1.9073486328125e-06f, 1e-30f);  // 2^-19
+  if (__fadd_rn(value, ev) < __fsub_rn(thr_f, et)) return 1;
+  if (__fsub_rn(value, ev) > __fadd_rn(thr_f, et)) return 0;
+  return -1;
+}
+
+struct Smem
+{
+  double* ln;
+  const float* scr;
+  unsigned long long* jA;
+  unsigned long long* jC;
+};
+
+template <bool INT>
+__device__ __forceinline__ bool uphill_accept(const Smem& S, uint32_t r0, int row, double dE,
+                                              long long idE, double beta, float nbeta_f)
+{
+  if (isinf(beta)) return false;
+  float thr_f = INT ? __fmul_rn((float)idE, nbeta_f) : __fmul_rn(approx_float(dE), nbeta_f);
+  int d = lut_screen(S.scr, r0, row, thr_f);
+  if (d >= 0) return d == 1;
+  return lut_less_exact(S.ln, r0, row, __dmul_rn(INT ? (double)idE : dE, -beta));
+}
+
+__device__ __forceinline__ uint32_t spin_of(const uint32_t* spins, int v)
+{
+  return (spins[v >> 5] >> (v & 31)) & 1u;
+}
+
+// warp-cooperative copy of `words` 32-bit words (16-byte aligned, multiple of 4)
+__device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* src, int words, int lane)
+{
+  const uint4* s = (const uint4*)src;
+  uint4* d = (uint4*)dst;
+  for (int q = lane; q < words / 4; q += 32) d[q] = s[q];
+}
+
+// ---- TMA bulk copies into shared memory, completion on an mbarrier -------
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long* bar, unsigned bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_1d(void* dst, const void* src, unsigned bytes,
+                                       unsigned long long* bar)
+{
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parity)
+{
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false when the copy never completed (error reported)
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int* err)
+{
+  for (int it = 0; it < (1 << 22); it++)
+    if (mbar_try(bar, parity)) return true;
+  if (err) atomicExch(err, 1);
+  return false;
+}
+
+// Per-warp tile of the CSR incidences of one 32-variable block: term ids and
+// coefficients of [q0, q0 + n) copied with two bulk copies.  Bulk copies move
+// 16-byte aligned, 16-byte multiple ranges, so each starts at the aligned
+// address below its first element and records the element offset.
+template <bool INT>
+struct Tile
+{
+  static const int kCap = 512;  // incidences held in shared memory
+  uint32_t inc[kCap + 8];
+  typename std::conditional<INT, int, double>::type coef[kCap + 8];
+};
+
+template <bool INT>
+__device__ __forceinline__ void tile_issue(Tile<INT>* t, unsigned long long* bar, const DevModel& m,
+                                           int q0, int q1, int& o_inc, int& o_coef)
+{
+  using C = typename std::conditional<INT, int, double>::type;
+  const int n = min(q1 - q0, Tile<INT>::kCap);
+  const C* cbase = INT ? (const C*)m.coef_i : (const C*)m.coef;
+  const char* a_inc = (const char*)(m.inc + q0);
+  const char* a_coef = (const char*)(cbase + q0);
+  const char* s_inc = (const char*)((size_t)a_inc & ~(size_t)15);
+  const char* s_coef = (const char*)((size_t)a_coef & ~(size_t)15);
+  o_inc = (int)((a_inc - s_inc) / 4);
+  o_coef = (int)((a_coef - s_coef) / (int)sizeof(C));
+  unsigned b_inc = (unsigned)(((a_inc + 4 * (size_t)n) - s_inc + 15) & ~(size_t)15);
+  unsigned b_coef = (unsigned)(((a_coef + sizeof(C) * (size_t)n) - s_coef + 15) & ~(size_t)15);
+  if (n <= 0)
+  {
+    b_inc = 16;
+    b_coef = 16;
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect(bar, b_inc + b_coef);
+  tma_1d(t->inc, s_inc, b_inc, bar);
+  tma_1d(t->coef, s_coef, b_coef, bar);
+}
+
+template <int FL, bool REPLAY, bool INT, bool SMEM>
+__global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
+{
+  using C = typename std::conditional<INT, int, double>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* s_ln = (double*)smem;                                    // 8192 B
+  float* s_scr = (float*)(smem + 8192);                            // 12288 B
+  unsigned long long* s_A = (unsigned long long*)(smem + 20480);  // 520 B
+  unsigned long long* s_C = s_A + 65;                              // 520 B
+  unsigned char* s_warp = smem + 21760;
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) s_ln[t] = c_ln[t];
+  for (int t = threadIdx.x; t < 3072; t += blockDim.x) s_scr[t] = c_scr[t];
+  for (int t = threadIdx.x; t < 65; t += blockDim.x)
+  {
+    s_A[t] = c_jA[t];
+    s_C[t] = c_jC[t];
+  }
+  __syncthreads();
+  const Smem S{s_ln, s_scr, s_A, s_C};
+
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int w = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (w >= a.n_streams) return;
+  const DevModel m = a.m;
+  const int Sz = m.sweep_size;
+  const int nwd = (m.n_vars + 31) >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const bool compact = (FL == F_COUNTER) && !INT;
+  const bool staged = (FL == F_PARITY || FL == F_COUNTER);
+  // per-warp region: [bars 16][tiles 2][scratch][term bytes][spins][lowest]
+  const int tile_bytes = staged ? (int)((sizeof(Tile<INT>) + 15) & ~15) : 0;
+  const int scratch_bytes = compact ? kScratch * 32 * 4 : 0;
+  const int state_bytes = SMEM ? (a.p.mp + 8 * a.p.nw) : 0;
+  unsigned char* my = s_warp + (size_t)wib * (16 + 2 * tile_bytes + scratch_bytes + state_bytes);
+  unsigned long long* bars = (unsigned long long*)my;
+  Tile<INT>* tiles = (Tile<INT>*)(my + 16);
+  uint32_t* scratch = (uint32_t*)(my + 16 + 2 * tile_bytes);
+  unsigned char* my_state = my + 16 + 2 * tile_bytes + scratch_bytes;
+  if (staged && lane == 0)
+  {
+    mbar_init(&bars[0]);
+    mbar_init(&bars[1]);
+  }
+  __syncwarp();
+  unsigned phase0 = 0, phase1 = 0;
+  uint64_t rs = REPLAY ? a.rng[w] : 0;
+
+  for (int r = w; r < a.n_walkers; r += a.n_streams)
+  {
+    const int slot = a.slot_of ? a.slot_of[r] : r;
+    uint32_t* g_spins = a.p.spins + (size_t)slot * a.p.nw;
+    uint8_t* g_ts = a.p.tstate + (size_t)slot * a.p.mp;
+    uint32_t* g_lsp = a.p.lspins + (size_t)r * a.p.nw;
+    uint8_t* ts;
+    uint32_t* spins;
+    uint32_t* lsp;
+    if (SMEM)
+    {
+      ts = my_state;
+      spins = (uint32_t*)(my_state + a.p.mp);
+      lsp = spins + a.p.nw;
+      copy_words((uint32_t*)ts, (const uint32_t*)g_ts, a.p.mp / 4, lane);
+      copy_words(spins, g_spins, a.p.nw, lane);
+      copy_words(lsp, g_lsp, a.p.nw, lane);
+      __syncwarp();
+    }
+    else
+    {
+      ts = g_ts;
+      spins = g_spins;
+      lsp = g_lsp;
+    }
+    double cost = a.p.cost[slot];
+    double low = a.p.lowest[r];
+    long long icost = INT ? (long long)cost : 0;
+    long long ilow = INT ? (long long)low : 0;
+    long long klow = order_key(low);
+    unsigned long long natt = 0, nacc = 0, nwin = 0;
+    uint64_t key = 0;
+    if (!REPLAY)
+      key = counter_key(a.seed + (uint32_t)(r / a.key_div),
+                        a.key_base + (unsigned long long)(r % a.key_div));
+    const int nblocks = (Sz + 31) >> 5;
+    const int total_blocks = nblocks * a.n_sweeps;
+    // prefetch the first block's tile
+    int o_inc[2] = {0, 0}, o_coef[2] = {0, 0}, tq0[2] = {0, 0};
+    if (staged && total_blocks > 0 && lane == 0)
+    {
+      int q0 = __ldg(m.row + 0), q1 = __ldg(m.row + min(32, Sz));
+      tile_issue<INT>(&tiles[0], &bars[0], m, q0, q1, o_inc[0], o_coef[0]);
+      tq0[0] = q0;
+    }
+    bool aborted = false;
+    for (int gb = 0; gb < total_blocks; gb++)
+    {
+      const int k = gb / nblocks;
+      const int bi = gb - k * nblocks;
+      const int buf = gb & 1;
+      const long long swp = a.sweep_base + k;
+      const double beta = a.beta[(long long)r * a.bs_w + swp * a.bs_s];
+      const float nbeta_f = -approx_float(beta);
+      const unsigned long long ctr0 = (unsigned long long)swp * (unsigned long long)Sz;
+      const int i0 = bi << 5;
+      Tile<INT>* tile = &tiles[buf];
+      if (staged)
+      {
+        // issue the next block's tile into the other buffer, then wait for ours
+        if (gb + 1 < total_blocks && lane == 0)
+        {
+          int nb = (bi + 1 < nblocks) ? bi + 1 : 0;
+          int q0 = __ldg(m.row + (nb << 5)), q1 = __ldg(m.row + min((nb << 5) + 32, Sz));
+          tile_issue<INT>(&tiles[buf ^ 1], &bars[buf ^ 1], m, q0, q1, o_inc[buf ^ 1],
+                          o_coef[buf ^ 1]);
+          tq0[buf ^ 1] = q0;
+        }
+        bool ok = mbar_wait(&bars[buf], buf ? phase1 : phase0, a.err);
+        if (buf) phase1 ^= 1u; else phase0 ^= 1u;
+        if (!__all_sync(kFull, ok))
+        {
+          aborted = true;
+          break;
+        }
+      }
+      const int t_q0 = __shfl_sync(kFull, tq0[buf], 0);
+      const int t_oi = __shfl_sync(kFull, o_inc[buf], 0);
+      const int t_oc = __shfl_sync(kFull, o_coef[buf], 0);
+      const int v = i0 + lane;
+      const bool valid = v < Sz;
+      const int nvalid = min(32, Sz - i0);
+      int rb = 0, re = 0;
+      uint32_t sv = 0, nb = 0;
+      if (valid)
+      {
+        rb = __ldg(m.row + v);
+        re = __ldg(m.row + v + 1);
+        sv = spin_of(spins, v);
+        nb = __ldg(m.nbr + v);
+      }
+      // incidence q -> (term | neg, coefficient) from the tile or, past its
+      // capacity, from global memory
+      auto inc_at = [&](int q) -> uint32_t {
+        int j = q - t_q0;
+        return (staged && j < Tile<INT>::kCap) ? tile->inc[t_oi + j] : __ldg(m.inc + q);
+      };
+      auto coef_at = [&](int q) -> C {
+        int j = q - t_q0;
+        if (staged && j < Tile<INT>::kCap) return tile->coef[t_oc + j];
+        return INT ? (C)__ldg(m.coef_i + q) : (C)__ldg(m.coef + q);
+      };
+
+      int cursor = 0;
+      while (cursor < nvalid)
+      {
+        const bool active = valid && lane >= cursor;
+        double dE = 0.0;
+        long long idE = 0;
+        if (active)
+        {
+          if (FL == F_PARITY)
+          {
+            if (INT)
+            {
+              int acc = 0;
+#pragma unroll 4
+              for (int q = rb; q < re; q++)
+              {
+                int c = (int)coef_at(q);
+                acc += ts[inc_at(q)] ? -c : c;
+              }
+              idE = -2 * (long long)acc;
+            }
+            else
+            {
+              double diff = 0.0;
+#pragma unroll 4
+              for (int q = rb; q < re; q++)
+              {
+                double c = (double)coef_at(q);
+                diff = __dadd_rn(diff, ts[inc_at(q)] ? -c : c);
+              }
+              dE = neg2x(diff);
+            }
+          }
+          else if (FL == F_COUNTER && INT)
+          {
+            int acc = 0;
+#pragma unroll 4
+            for (int q = rb; q < re; q++)
+            {
+              uint32_t e = inc_at(q);
+              uint8_t z = ts[e & ~kNegBit];
+              int c = (int)coef_at(q);
+              if (sv ^ (e >> 31)) acc += (z == 1) ? c : 0;
+              else acc -= (z == 0) ? c : 0;
+            }
+            idE = acc;
+          }
+        }
+        if (FL == F_COUNTER && !INT)
+        {
+          // contributing terms only: collect a chunk of them, then sum in order
+          double diff = 0.0;
+          const int qe_all = active ? re : rb;
+          for (int q0 = rb; __any_sync(kFull, q0 < qe_all); q0 += kScratch)
+          {
+            int n = 0;
+            const int qe = min(qe_all, q0 + kScratch);
+            for (int q = q0; q < qe; q++)
+            {
+              uint32_t e = inc_at(q);
+              uint8_t z = ts[e & ~kNegBit];
+              bool lit = (sv ^ (e >> 31)) != 0;
+              if (lit ? (z == 1) : (z == 0))
+              {
+                scratch[n * 32 + lane] = (uint32_t)q | (lit ? 0u : kNegBit);
+                n++;
+              }
+            }
+            for (int j = 0; j < n; j++)
+            {
+              uint32_t x = scratch[j * 32 + lane];
+              double c = (double)coef_at((int)(x & ~kNegBit));
+              diff = (x & kNegBit) ? __dsub_rn(diff, c) : __dadd_rn(diff, c);
+            }
+          }
+          dE = diff;
+        }
+        if (FL == F_PLAIN_ISING || FL == F_PLAIN_PUBO)
+        {
+          if (active)
+          {
+            double diff = 0.0;
+            long long iacc = 0;
+            for (int q = rb; q < re; q++)
+            {
+              int t = (int)__ldg(m.inc + q);
+              int tb = __ldg(m.trow + t), te = __ldg(m.trow + t + 1);
+              if (FL == F_PLAIN_ISING)
+              {
+                uint32_t par = 0;
+                for (int u = tb; u < te; u++) par ^= spin_of(spins, (int)__ldg(m.tvar + u));
+                if (INT) iacc += par ? -(long long)__ldg(m.coef_i + q) : (long long)__ldg(m.coef_i + q);
+                else diff = __dadd_rn(diff, par ? -__ldg(m.coef + q) : __ldg(m.coef + q));
+              }
+              else
+              {
+                bool zero = false;
+                for (int u = tb; u < te; u++)
+                {
+                  int x = (int)__ldg(m.tvar + u);
+                  if (x != v && spin_of(spins, x)) { zero = true; break; }
+                }
+                if (!zero)
+                {
+                  if (INT) iacc += sv ? (long long)__ldg(m.coef_i + q) : -(long long)__ldg(m.coef_i + q);
+                  else diff = sv ? __dadd_rn(diff, __ldg(m.coef + q)) : __dsub_rn(diff, __ldg(m.coef + q));
+                }
+              }
+            }
+            if (FL == F_PLAIN_ISING)
+            {
+              if (INT) idE = -2 * iacc;
+              else dE = neg2x(diff);
+            }
+            else
+            {
+              if (INT) idE = iacc;
+              else dE = diff;
+            }
+          }
+        }
+
+        // ---- acceptance (markov/metropolis.h:64-104) ----------------------
+        const unsigned before = lt & ~((1u << cursor) - 1u);  // lanes in [cursor, lane)
+        const bool uphill = active && (INT ? (idE > 0) : !le_zero(dE));
+        bool acc = active && !uphill;
+        bool redraw = false;
+        unsigned U = 0;
+        int pos = 0;
+        if (REPLAY)
+        {
+          U = __ballot_sync(kFull, uphill);
+          pos = __popc(U & before);
+          if (uphill)
+          {
+            uint32_t r0 = pcg_out(S.jA[pos] * rs + S.jC[pos]);
+            redraw = (r0 & 255u) == 0;
+            if (!redraw) acc = uphill_accept<INT>(S, r0, 0, dE, idE, beta, nbeta_f);
+          }
+        }
+        else if (uphill)
+        {
+          const unsigned long long ctr = ctr0 + (unsigned long long)v;
+          const uint64_t w0 = counter_draw(key, 2ULL * ctr);
+          int row = -1, b = 0, used = 0;
+          uint32_t cur = 0;
+          bool decided = false;
+          while (b == 0)
+          {
+            if (row < 3)
+            {
+              if (used == 0) cur = (uint32_t)w0;
+              else if (used == 1) cur = (uint32_t)(w0 >> 32);
+              else
+              {
+                uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
+                cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+              }
+              used++;
+              b = (int)(cur & 255u);
+              row++;
+            }
+            else
+            {
+              decided = true;
+              break;
+            }
+          }
+          acc = decided ? true : uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f);
+        }
+        const unsigned A = __ballot_sync(kFull, acc);
+        bool conf = false;
+        if (active && lane > cursor)
+          conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+        const unsigned Cm = __ballot_sync(kFull, conf);
+        const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
+        const unsigned stop = Cm | Rm;
+        int f = stop ? (__ffs(stop) - 1) : 32;
+        if (f > nvalid) f = nvalid;
+        const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
+        const unsigned commit = ((f >= 32) ? kFull : ((1u << f) - 1u)) & ~((1u << cursor) - 1u);
+        unsigned flips = A & commit;
+        int draws = REPLAY ? __popc(U & commit) : 0;
+        if (REPLAY && slow)
+        {
+          int sacc = 0, used = 0;
+          if (lane == f)
+          {
+            int row = -1, b = 0;
+            uint32_t cur = 0;
+            bool decided = false;
+            while (b == 0)
+            {
+              if (row < 3)
+              {
+                cur = pcg_out(S.jA[pos + used] * rs + S.jC[pos + used]);
+                used++;
+                b = (int)(cur & 255u);
+                row++;
+              }
+              else
+              {
+                decided = true;
+                break;
+              }
+            }
+            bool ok = decided ? true : uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f);
+            sacc = ok ? 1 : 0;
+          }
+          sacc = __shfl_sync(kFull, sacc, f);
+          used = __shfl_sync(kFull, used, f);
+          if (sacc) flips |= 1u << f;
+          draws += used;
+        }
+        const int adv = f + (slow ? 1 : 0) - cursor;
+
+        // ---- apply accepted flips (their term sets are disjoint) ----------
+        if ((flips >> lane) & 1u)
+        {
+          if (FL == F_PARITY)
+          {
+            for (int q = rb; q < re; q++) ts[inc_at(q)] ^= (uint8_t)1;
+          }
+          else if (FL == F_COUNTER)
+          {
+            for (int q = rb; q < re; q++)
+            {
+              uint32_t e = inc_at(q);
+              uint32_t t = e & ~kNegBit;
+              ts[t] = (uint8_t)(ts[t] + ((sv ^ (e >> 31)) ? 0xFFu : 1u));
+            }
+          }
+        }
+        const int wi = i0 >> 5;
+        if (lane == 0 && flips) spins[wi] ^= flips;
+        // ---- running cost and lowest state, in attempt order --------------
+        int lowpos = -1;
+        unsigned fl = flips;
+        while (fl)
+        {
+          const int j = __ffs(fl) - 1;
+          fl &= fl - 1;
+          if (INT)
+          {
+            icost += __shfl_sync(kFull, idE, j);
+            if (icost < ilow)
+            {
+              ilow = icost;
+              lowpos = j;
+            }
+          }
+          else
+          {
+            cost = __dadd_rn(cost, __shfl_sync(kFull, dE, j));
+            long long kc = order_key(cost);
+            if (kc < klow)
+            {
+              klow = kc;
+              low = cost;
+              lowpos = j;
+            }
+          }
+        }
+        __syncwarp();
+        if (lowpos >= 0)
+        {
+          for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
+          __syncwarp();
+          const unsigned undo = flips & ~((2u << lowpos) - 1u);
+          if (lane == 0 && undo) lsp[wi] ^= undo;
+          __syncwarp();
+        }
+        natt += (unsigned long long)adv;
+        nacc += (unsigned long long)__popc(flips);
+        nwin++;
+        if (REPLAY) rs = S.jA[draws] * rs + S.jC[draws];
+        cursor += adv;
+      }
+      __syncwarp();
+    }
+    if (aborted) return;
+    if (SMEM)
+    {
+      __syncwarp();
+      copy_words((uint32_t*)g_ts, (const uint32_t*)ts, a.p.mp / 4, lane);
+      copy_words(g_spins, spins, a.p.nw, lane);
+      copy_words(g_lsp, lsp, a.p.nw, lane);
+    }
+    if (lane == 0)
+    {
+      a.p.cost[slot] = INT ? (double)icost : cost;
+      a.p.lowest[r] = INT ? (double)ilow : low;
+      a.p.attempts[r] += natt;
+      a.p.accepts[r] += nacc;
+      a.p.step_att[r] += natt;
+      a.p.step_acc[r] += nacc;
+      if (a.p.windows) a.p.windows[r] += nwin;
+    }
+    __syncwarp();
+  }
+  if (REPLAY && lane == 0) a.rng[w] = rs;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static const int kTableBytes = 21760;
+
+int warp_region_bytes(const SweepArgs& a, bool smem_state)
+{
+  const bool INT = a.m.int_mode != 0;
+  const bool compact = (a.m.flavor == F_COUNTER) && !INT;
+  const bool staged = (a.m.flavor == F_PARITY || a.m.flavor == F_COUNTER);
+  const int tile = staged ? (int)(((INT ? sizeof(Tile<true>) : sizeof(Tile<false>)) + 15) & ~15) : 0;
+  return 16 + 2 * tile + (compact ? kScratch * 32 * 4 : 0) + (smem_state ? a.p.mp + 8 * a.p.nw : 0);
+}
+
+template <int FL, bool R, bool I, bool SM>
+static cudaError_t go(const SweepArgs& a, cudaStream_t s, int wpb, int smem)
+{
+  auto k = sweep2_kernel<FL, R, I, SM>;
+  static int configured = -1;
+  if (smem > 48 * 1024 && configured < smem)
+  {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    configured = smem;
+  }
+  int blocks = (a.n_streams + wpb - 1) / wpb;
+  if (blocks > 0) k<<<blocks, 32 * wpb, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int FL, bool R, bool I>
+static cudaError_t go_sm(const SweepArgs& a, cudaStream_t s, int wpb, int smem, bool sm)
+{
+  return sm ? go<FL, R, I, true>(a, s, wpb, smem) : go<FL, R, I, false>(a, s, wpb, smem);
+}
+
+template <int FL>
+static cudaError_t go_fl(const SweepArgs& a, cudaStream_t s, int wpb, int smem, bool sm)
+{
+  const bool I = a.m.int_mode != 0;
+  if (a.replay)
+    return I ? go_sm<FL, true, true>(a, s, wpb, smem, sm) : go_sm<FL, true, false>(a, s, wpb, smem, sm);
+  return I ? go_sm<FL, false, true>(a, s, wpb, smem, sm) : go_sm<FL, false, false>(a, s, wpb, smem, sm);
+}
+
+void upload_sweep_tables(const double* ln, const float* scr, const unsigned long long* jA,
+                         const unsigned long long* jC)
+{
+  cudaMemcpyToSymbol(c_ln, ln, 1024 * sizeof(double));
+  cudaMemcpyToSymbol(c_scr, scr, 3072 * sizeof(float));
+  cudaMemcpyToSymbol(c_jA, jA, 65 * sizeof(unsigned long long));
+  cudaMemcpyToSymbol(c_jC, jC, 65 * sizeof(unsigned long long));
+}
+}  // namespace sw
+
+// Launch: warps per block chosen so that the grid spreads over the SMs;
+// walker state goes to shared memory when the per-warp region fits.
+cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int wpb)
+{
+  using namespace sw;
+  if (wpb < 1) wpb = 1;
+  if (wpb > 8) wpb = 8;
+  const int max_smem = 227 * 1024;
+  bool sm = a.smem_state != 0;
+  int per = warp_region_bytes(a, sm);
+  if (sm)
+  {
+    while (wpb > 1 && kTableBytes + wpb * per > max_smem) wpb--;
+    if (kTableBytes + wpb * per > max_smem)
+    {
+      sm = false;
+      per = warp_region_bytes(a, false);
+    }
+  }
+  int smem = kTableBytes + wpb * per;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: return go_fl<F_PARITY>(a, s, wpb, smem, sm);
+    case F_COUNTER: return go_fl<F_COUNTER>(a, s, wpb, smem, sm);
+    case F_PLAIN_ISING: return go_fl<F_PLAIN_ISING>(a, s, wpb, smem, sm);
+    default: return go_fl<F_PLAIN_PUBO>(a, s, wpb, smem, sm);
+  }
+}
+}  // namespace qio
+
+namespace qio
+{
+void sw_upload(const double* ln, const float* scr, const unsigned long long* jA,
+               const unsigned long long* jC)
+{
+  sw::upload_sweep_tables(ln, scr, jA, jC);
+}
+}  // namespace qio
