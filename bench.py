@@ -268,6 +268,8 @@ def main():
     A = attempts_per_step(kind, n, params)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
+    last = {"launches": 0}
+
     def one_step():
         flush.fill_(1)  # L2 flush (256 MB > 129 MB L2), outside the timed region
         e0 = torch.cuda.Event(enable_timing=True)
@@ -278,35 +280,32 @@ def main():
         e1.record(stream)
         e1.synchronize()
         st = solver.stats()
-        return e0.elapsed_time(e1), st
+        # the solver counts launches cumulatively: keep this step's
+        n = int(st.kernel_launches) - last["launches"]
+        last["launches"] = int(st.kernel_launches)
+        return e0.elapsed_time(e1), st, n
 
     for _ in range(args.warmup):
         one_step()
     barrier(ws)
     torch.cuda.synchronize()
     ms, sweep_ms, launches, att = [], [], 0, 0
-    sweep_launches = 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            t, st = one_step()
+            t, st, n_launch = one_step()
             ms.append(t)
             sweep_ms.append(st.sweep_kernel_ms)
-            launches += int(st.kernel_launches)
+            launches += n_launch
             att += int(st.attempts)
     torch.cuda.synchronize()
     barrier(ws)
     total_s = reduce_max(sum(ms) / 1e3, ws)
     value = A * args.steps * ws / total_s
-    # the solver reports its launches cumulatively; count this window's
-    per_step_launches = launches / args.steps
-    sweeps_per_step = params["sweeps"] if target != "simulatedannealing.qiotoolkit" else 1
     if target == "simulatedannealing.qiotoolkit":
         sweep_launches_per_step = 1
     else:
         sweep_launches_per_step = params["sweeps"]
     avg_sweep_launch_ms = statistics.mean(sweep_ms) / sweep_launches_per_step
-    walkers = A // (n * (params["sweeps"] if "temperatures" in params or "restarts" in params
-                         else params["sweeps"] * params["sweeps_per_replica"]))
     attempts_per_launch = A / sweep_launches_per_step
     K = model.info.n_incidences
     bpa = 9.0 + 13.0 * K / n  # row bounds 8 + own state 1 + per incidence (id 4 + coef 8 + state 1)

@@ -142,7 +142,6 @@ template <bool INT>
 __device__ __forceinline__ bool uphill_accept(const Smem& S, uint32_t r0, int row, double dE,
                                               long long idE, double beta, float nbeta_f)
 {
-  if (isinf(beta)) return false;
   float thr_f = INT ? __fmul_rn((float)idE, nbeta_f) : __fmul_rn(approx_float(dE), nbeta_f);
   int d = lut_screen(S.scr, r0, row, thr_f);
   if (d >= 0) return d == 1;
@@ -213,7 +212,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 template <bool INT>
 struct Tile
 {
-  static const int kCap = 512;  // incidences held in shared memory
+  static const int kCap = 768;  // incidences held in shared memory
   uint32_t inc[kCap + 8];
   typename std::conditional<INT, int, double>::type coef[kCap + 8];
 };
@@ -244,6 +243,497 @@ __device__ __forceinline__ void tile_issue(Tile<INT>* t, unsigned long long* bar
   tma_1d(t->coef, s_coef, b_coef, bar);
 }
 
+// Mutable per-walker state of the sweep.
+struct Walk
+{
+  double cost, low;
+  long long icost, ilow, klow;
+  unsigned long long natt, nacc, nwin;
+  uint64_t rs, key;
+};
+
+// All rounds of one 32-variable block.  TILE: the block's incidences are in
+// the shared tile (term ids at tinc[bi + k], coefficients at tcoef[bc + k]);
+// otherwise they are read from global memory at [rb, re).
+template <int FL, bool REPLAY, bool INT, bool TILE>
+__device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, Walk& W,
+                                             uint8_t* ts, uint32_t* spins, uint32_t* lsp,
+                                             uint32_t* scratch, const uint32_t* tinc,
+                                             const typename std::conditional<INT, int, double>::type* tcoef,
+                                             int i0, int Sz, int nwd, double beta, float nbeta_f,
+                                             bool beta_inf, unsigned long long ctr0)
+{
+  using C = typename std::conditional<INT, int, double>::type;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int v = i0 + lane;
+  const bool valid = v < Sz;
+  const int nvalid = min(32, Sz - i0);
+  int rb = 0, deg = 0;
+  uint32_t sv = 0, nb = 0;
+  if (valid)
+  {
+    rb = __ldg(m.row + v);
+    deg = __ldg(m.row + v + 1) - rb;
+    sv = spin_of(spins, v);
+    nb = __ldg(m.nbr + v);
+  }
+  // incidence k of this lane's variable
+  const uint32_t* pinc = TILE ? tinc : (const uint32_t*)(m.inc + rb);
+  const C* pcoef = TILE ? tcoef : (INT ? (const C*)(m.coef_i + rb) : (const C*)(m.coef + rb));
+  auto INC = [&](int k) -> uint32_t { return TILE ? pinc[k] : __ldg(pinc + k); };
+  auto COEF = [&](int k) -> C { return TILE ? pcoef[k] : __ldg(pcoef + k); };
+
+  int cursor = 0;
+  while (cursor < nvalid)
+  {
+    const bool active = valid && lane >= cursor;
+    const int dk = active ? deg : 0;
+    double dE = 0.0;
+    long long idE = 0;
+    if (FL == F_PARITY)
+    {
+      if (INT)
+      {
+        int acc = 0;
+#pragma unroll 4
+        for (int k = 0; k < dk; k++)
+        {
+          int c = (int)COEF(k);
+          acc += ts[INC(k)] ? -c : c;
+        }
+        idE = -2 * (long long)acc;
+      }
+      else
+      {
+        double diff = 0.0;
+#pragma unroll 4
+        for (int k = 0; k < dk; k++)
+        {
+          long long cb = __double_as_longlong((double)COEF(k));
+          cb ^= (long long)ts[INC(k)] << 63;
+          diff = __dadd_rn(diff, __longlong_as_double(cb));
+        }
+        dE = neg2x(diff);
+      }
+    }
+    else
+    {
+      if (INT)
+      {
+        int acc = 0;
+#pragma unroll 4
+        for (int k = 0; k < dk; k++)
+        {
+          uint32_t e = INC(k);
+          uint8_t z = ts[e & ~kNegBit];
+          int c = (int)COEF(k);
+          if (sv ^ (e >> 31)) acc += (z == 1) ? c : 0;
+          else acc -= (z == 0) ? c : 0;
+        }
+        idE = acc;
+      }
+      else
+      {
+        // contributing terms only (sign folded in), then one ordered FP64 add
+        // each; the warp issues max-over-lanes adds per chunk
+        double diff = 0.0;
+        for (int k0 = 0; __any_sync(kFull, k0 < dk); k0 += kScratch)
+        {
+          int n = 0;
+          const int ke = min(dk, k0 + kScratch);
+          for (int k = k0; k < ke; k++)
+          {
+            uint32_t e = INC(k);
+            uint8_t z = ts[e & ~kNegBit];
+            bool lit = (sv ^ (e >> 31)) != 0;
+            if (lit ? (z == 1) : (z == 0))
+            {
+              scratch[n * 32 + lane] = (uint32_t)k | (lit ? 0u : kNegBit);
+              n++;
+            }
+          }
+          for (int j = 0; j < n; j++)
+          {
+            uint32_t x = scratch[j * 32 + lane];
+            long long cb = __double_as_longlong((double)COEF((int)(x & ~kNegBit)));
+            cb ^= (long long)(x >> 31) << 63;
+            diff = __dadd_rn(diff, __longlong_as_double(cb));
+          }
+        }
+        dE = diff;
+      }
+    }
+
+    // ---- acceptance (markov/metropolis.h:64-104) ----------------------
+    const unsigned before = lt & ~((1u << cursor) - 1u);  // lanes in [cursor, lane)
+    const bool uphill = active && (INT ? (idE > 0) : !le_zero(dE));
+    bool acc = active && !uphill;
+    bool redraw = false;
+    unsigned U = 0;
+    int pos = 0;
+    if (REPLAY)
+    {
+      U = __ballot_sync(kFull, uphill);
+      pos = __popc(U & before);
+      if (uphill)
+      {
+        uint32_t r0 = pcg_out(S.jA[pos] * W.rs + S.jC[pos]);
+        redraw = (r0 & 255u) == 0;
+        if (!redraw) acc = !beta_inf && uphill_accept<INT>(S, r0, 0, dE, idE, beta, nbeta_f);
+      }
+    }
+    else if (uphill)
+    {
+      const unsigned long long ctr = ctr0 + (unsigned long long)v;
+      const uint64_t w0 = counter_draw(W.key, 2ULL * ctr);
+      int row = -1, b = 0, used = 0;
+      uint32_t cur = 0;
+      bool decided = false;
+      while (b == 0)
+      {
+        if (row < 3)
+        {
+          if (used == 0) cur = (uint32_t)w0;
+          else if (used == 1) cur = (uint32_t)(w0 >> 32);
+          else
+          {
+            uint64_t w1 = counter_draw(W.key, 2ULL * ctr + 1ULL);
+            cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+          }
+          used++;
+          b = (int)(cur & 255u);
+          row++;
+        }
+        else
+        {
+          decided = true;
+          break;
+        }
+      }
+      acc = decided ? true : (!beta_inf && uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f));
+    }
+    const unsigned A = __ballot_sync(kFull, acc);
+    bool conf = false;
+    if (active && lane > cursor)
+      conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+    const unsigned Cm = __ballot_sync(kFull, conf);
+    const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
+    const unsigned stop = Cm | Rm;
+    int f = stop ? (__ffs(stop) - 1) : 32;
+    if (f > nvalid) f = nvalid;
+    const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
+    const unsigned commit = ((f >= 32) ? kFull : ((1u << f) - 1u)) & ~((1u << cursor) - 1u);
+    unsigned flips = A & commit;
+    int draws = REPLAY ? __popc(U & commit) : 0;
+    if (REPLAY && slow)
+    {
+      int sacc = 0, used = 0;
+      if (lane == f)
+      {
+        int row = -1, b = 0;
+        uint32_t cur = 0;
+        bool decided = false;
+        while (b == 0)
+        {
+          if (row < 3)
+          {
+            cur = pcg_out(S.jA[pos + used] * W.rs + S.jC[pos + used]);
+            used++;
+            b = (int)(cur & 255u);
+            row++;
+          }
+          else
+          {
+            decided = true;
+            break;
+          }
+        }
+        bool ok = decided ? true
+                          : (!beta_inf && uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f));
+        sacc = ok ? 1 : 0;
+      }
+      sacc = __shfl_sync(kFull, sacc, f);
+      used = __shfl_sync(kFull, used, f);
+      if (sacc) flips |= 1u << f;
+      draws += used;
+    }
+    const int adv = f + (slow ? 1 : 0) - cursor;
+
+    // ---- apply accepted flips (their term sets are disjoint) ----------
+    if ((flips >> lane) & 1u)
+    {
+      if (FL == F_PARITY)
+      {
+        for (int k = 0; k < deg; k++) ts[INC(k)] ^= (uint8_t)1;
+      }
+      else
+      {
+        for (int k = 0; k < deg; k++)
+        {
+          uint32_t e = INC(k);
+          uint32_t t = e & ~kNegBit;
+          ts[t] = (uint8_t)(ts[t] + ((sv ^ (e >> 31)) ? 0xFFu : 1u));
+        }
+      }
+    }
+    const int wi = i0 >> 5;
+    if (lane == 0 && flips) spins[wi] ^= flips;
+    // ---- running cost and lowest state, in attempt order --------------
+    int lowpos = -1;
+    unsigned fl = flips;
+    while (fl)
+    {
+      const int j = __ffs(fl) - 1;
+      fl &= fl - 1;
+      if (INT)
+      {
+        W.icost += __shfl_sync(kFull, idE, j);
+        if (W.icost < W.ilow)
+        {
+          W.ilow = W.icost;
+          lowpos = j;
+        }
+      }
+      else
+      {
+        W.cost = __dadd_rn(W.cost, __shfl_sync(kFull, dE, j));
+        long long kc = order_key(W.cost);
+        if (kc < W.klow)
+        {
+          W.klow = kc;
+          W.low = W.cost;
+          lowpos = j;
+        }
+      }
+    }
+    __syncwarp();
+    if (lowpos >= 0)
+    {
+      for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
+      __syncwarp();
+      const unsigned undo = flips & ~((2u << lowpos) - 1u);
+      if (lane == 0 && undo) lsp[wi] ^= undo;
+      __syncwarp();
+    }
+    W.natt += (unsigned long long)adv;
+    W.nacc += (unsigned long long)__popc(flips);
+    W.nwin++;
+    if (REPLAY) W.rs = S.jA[draws] * W.rs + S.jC[draws];
+    cursor += adv;
+  }
+  __syncwarp();
+}
+
+// Counter-free models (model::Ising, model::Pubo): the cost difference
+// gathers the member spins of each incident term; windows slide.
+template <int FL, bool REPLAY, bool INT>
+__device__ __forceinline__ void block_rounds_plain(const Smem& S, const DevModel& m, Walk& W,
+                                                   uint32_t* spins, uint32_t* lsp, int i0, int Sz,
+                                                   int nwd, double beta, float nbeta_f,
+                                                   bool beta_inf, unsigned long long ctr0)
+{
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int v = i0 + lane;
+  const bool valid = v < Sz;
+  const int nvalid = min(32, Sz - i0);
+  int rb = 0, re = 0;
+  uint32_t sv = 0, nb = 0;
+  if (valid)
+  {
+    rb = __ldg(m.row + v);
+    re = __ldg(m.row + v + 1);
+    sv = spin_of(spins, v);
+    nb = __ldg(m.nbr + v);
+  }
+  int cursor = 0;
+  while (cursor < nvalid)
+  {
+    const bool active = valid && lane >= cursor;
+    double dE = 0.0;
+    long long idE = 0;
+    if (active)
+    {
+      double diff = 0.0;
+      long long iacc = 0;
+      for (int q = rb; q < re; q++)
+      {
+        int t = (int)__ldg(m.inc + q);
+        int tb = __ldg(m.trow + t), te = __ldg(m.trow + t + 1);
+        if (FL == F_PLAIN_ISING)
+        {
+          uint32_t par = 0;
+          for (int u = tb; u < te; u++) par ^= spin_of(spins, (int)__ldg(m.tvar + u));
+          if (INT) iacc += par ? -(long long)__ldg(m.coef_i + q) : (long long)__ldg(m.coef_i + q);
+          else diff = __dadd_rn(diff, par ? -__ldg(m.coef + q) : __ldg(m.coef + q));
+        }
+        else
+        {
+          bool zero = false;
+          for (int u = tb; u < te; u++)
+          {
+            int x = (int)__ldg(m.tvar + u);
+            if (x != v && spin_of(spins, x)) { zero = true; break; }
+          }
+          if (!zero)
+          {
+            if (INT) iacc += sv ? (long long)__ldg(m.coef_i + q) : -(long long)__ldg(m.coef_i + q);
+            else diff = sv ? __dadd_rn(diff, __ldg(m.coef + q)) : __dsub_rn(diff, __ldg(m.coef + q));
+          }
+        }
+      }
+      if (FL == F_PLAIN_ISING)
+      {
+        if (INT) idE = -2 * iacc;
+        else dE = neg2x(diff);
+      }
+      else
+      {
+        if (INT) idE = iacc;
+        else dE = diff;
+      }
+    }
+    const unsigned before = lt & ~((1u << cursor) - 1u);
+    const bool uphill = active && (INT ? (idE > 0) : !le_zero(dE));
+    bool acc = active && !uphill;
+    bool redraw = false;
+    unsigned U = 0;
+    int pos = 0;
+    if (REPLAY)
+    {
+      U = __ballot_sync(kFull, uphill);
+      pos = __popc(U & before);
+      if (uphill)
+      {
+        uint32_t r0 = pcg_out(S.jA[pos] * W.rs + S.jC[pos]);
+        redraw = (r0 & 255u) == 0;
+        if (!redraw) acc = !beta_inf && uphill_accept<INT>(S, r0, 0, dE, idE, beta, nbeta_f);
+      }
+    }
+    else if (uphill)
+    {
+      const unsigned long long ctr = ctr0 + (unsigned long long)v;
+      const uint64_t w0 = counter_draw(W.key, 2ULL * ctr);
+      int row = -1, b = 0, used = 0;
+      uint32_t cur = 0;
+      bool decided = false;
+      while (b == 0)
+      {
+        if (row < 3)
+        {
+          if (used == 0) cur = (uint32_t)w0;
+          else if (used == 1) cur = (uint32_t)(w0 >> 32);
+          else
+          {
+            uint64_t w1 = counter_draw(W.key, 2ULL * ctr + 1ULL);
+            cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+          }
+          used++;
+          b = (int)(cur & 255u);
+          row++;
+        }
+        else
+        {
+          decided = true;
+          break;
+        }
+      }
+      acc = decided ? true : (!beta_inf && uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f));
+    }
+    const unsigned A = __ballot_sync(kFull, acc);
+    bool conf = false;
+    if (active && lane > cursor)
+      conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+    const unsigned Cm = __ballot_sync(kFull, conf);
+    const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
+    const unsigned stop = Cm | Rm;
+    int f = stop ? (__ffs(stop) - 1) : 32;
+    if (f > nvalid) f = nvalid;
+    const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
+    const unsigned commit = ((f >= 32) ? kFull : ((1u << f) - 1u)) & ~((1u << cursor) - 1u);
+    unsigned flips = A & commit;
+    int draws = REPLAY ? __popc(U & commit) : 0;
+    if (REPLAY && slow)
+    {
+      int sacc = 0, used = 0;
+      if (lane == f)
+      {
+        int row = -1, b = 0;
+        uint32_t cur = 0;
+        bool decided = false;
+        while (b == 0)
+        {
+          if (row < 3)
+          {
+            cur = pcg_out(S.jA[pos + used] * W.rs + S.jC[pos + used]);
+            used++;
+            b = (int)(cur & 255u);
+            row++;
+          }
+          else
+          {
+            decided = true;
+            break;
+          }
+        }
+        bool ok = decided ? true
+                          : (!beta_inf && uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f));
+        sacc = ok ? 1 : 0;
+      }
+      sacc = __shfl_sync(kFull, sacc, f);
+      used = __shfl_sync(kFull, used, f);
+      if (sacc) flips |= 1u << f;
+      draws += used;
+    }
+    const int adv = f + (slow ? 1 : 0) - cursor;
+    const int wi = i0 >> 5;
+    if (lane == 0 && flips) spins[wi] ^= flips;
+    int lowpos = -1;
+    unsigned fl = flips;
+    while (fl)
+    {
+      const int j = __ffs(fl) - 1;
+      fl &= fl - 1;
+      if (INT)
+      {
+        W.icost += __shfl_sync(kFull, idE, j);
+        if (W.icost < W.ilow)
+        {
+          W.ilow = W.icost;
+          lowpos = j;
+        }
+      }
+      else
+      {
+        W.cost = __dadd_rn(W.cost, __shfl_sync(kFull, dE, j));
+        long long kc = order_key(W.cost);
+        if (kc < W.klow)
+        {
+          W.klow = kc;
+          W.low = W.cost;
+          lowpos = j;
+        }
+      }
+    }
+    __syncwarp();
+    if (lowpos >= 0)
+    {
+      for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
+      __syncwarp();
+      const unsigned undo = flips & ~((2u << lowpos) - 1u);
+      if (lane == 0 && undo) lsp[wi] ^= undo;
+      __syncwarp();
+    }
+    W.natt += (unsigned long long)adv;
+    W.nacc += (unsigned long long)__popc(flips);
+    W.nwin++;
+    if (REPLAY) W.rs = S.jA[draws] * W.rs + S.jC[draws];
+    cursor += adv;
+  }
+  __syncwarp();
+}
+
 template <int FL, bool REPLAY, bool INT, bool SMEM>
 __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
 {
@@ -271,7 +761,6 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
   const DevModel m = a.m;
   const int Sz = m.sweep_size;
   const int nwd = (m.n_vars + 31) >> 5;
-  const unsigned lt = (1u << lane) - 1u;
   const bool compact = (FL == F_COUNTER) && !INT;
   const bool staged = (FL == F_PARITY || FL == F_COUNTER);
   // per-warp region: [bars 16][tiles 2][scratch][term bytes][spins][lowest]
@@ -290,7 +779,8 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
   }
   __syncwarp();
   unsigned phase0 = 0, phase1 = 0;
-  uint64_t rs = REPLAY ? a.rng[w] : 0;
+  Walk W;
+  W.rs = REPLAY ? a.rng[w] : 0;
 
   for (int r = w; r < a.n_walkers; r += a.n_streams)
   {
@@ -317,25 +807,25 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
       spins = g_spins;
       lsp = g_lsp;
     }
-    double cost = a.p.cost[slot];
-    double low = a.p.lowest[r];
-    long long icost = INT ? (long long)cost : 0;
-    long long ilow = INT ? (long long)low : 0;
-    long long klow = order_key(low);
-    unsigned long long natt = 0, nacc = 0, nwin = 0;
-    uint64_t key = 0;
+    W.cost = a.p.cost[slot];
+    W.low = a.p.lowest[r];
+    W.icost = INT ? (long long)W.cost : 0;
+    W.ilow = INT ? (long long)W.low : 0;
+    W.klow = order_key(W.low);
+    W.natt = W.nacc = W.nwin = 0;
+    W.key = 0;
     if (!REPLAY)
-      key = counter_key(a.seed + (uint32_t)(r / a.key_div),
-                        a.key_base + (unsigned long long)(r % a.key_div));
+      W.key = counter_key(a.seed + (uint32_t)(r / a.key_div),
+                          a.key_base + (unsigned long long)(r % a.key_div));
     const int nblocks = (Sz + 31) >> 5;
     const int total_blocks = nblocks * a.n_sweeps;
-    // prefetch the first block's tile
-    int o_inc[2] = {0, 0}, o_coef[2] = {0, 0}, tq0[2] = {0, 0};
+    int o_inc[2] = {0, 0}, o_coef[2] = {0, 0}, tq0[2] = {0, 0}, tq1[2] = {0, 0};
     if (staged && total_blocks > 0 && lane == 0)
     {
       int q0 = __ldg(m.row + 0), q1 = __ldg(m.row + min(32, Sz));
       tile_issue<INT>(&tiles[0], &bars[0], m, q0, q1, o_inc[0], o_coef[0]);
       tq0[0] = q0;
+      tq1[0] = q1;
     }
     bool aborted = false;
     for (int gb = 0; gb < total_blocks; gb++)
@@ -345,10 +835,12 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
       const int buf = gb & 1;
       const long long swp = a.sweep_base + k;
       const double beta = a.beta[(long long)r * a.bs_w + swp * a.bs_s];
+      const bool beta_inf =
+          ((unsigned long long)__double_as_longlong(beta) & 0x7FFFFFFFFFFFFFFFULL) ==
+          0x7FF0000000000000ULL;
       const float nbeta_f = -approx_float(beta);
       const unsigned long long ctr0 = (unsigned long long)swp * (unsigned long long)Sz;
       const int i0 = bi << 5;
-      Tile<INT>* tile = &tiles[buf];
       if (staged)
       {
         // issue the next block's tile into the other buffer, then wait for ours
@@ -359,6 +851,7 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
           tile_issue<INT>(&tiles[buf ^ 1], &bars[buf ^ 1], m, q0, q1, o_inc[buf ^ 1],
                           o_coef[buf ^ 1]);
           tq0[buf ^ 1] = q0;
+          tq1[buf ^ 1] = q1;
         }
         bool ok = mbar_wait(&bars[buf], buf ? phase1 : phase0, a.err);
         if (buf) phase1 ^= 1u; else phase0 ^= 1u;
@@ -367,313 +860,28 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
           aborted = true;
           break;
         }
+        const int t_q0 = __shfl_sync(kFull, tq0[buf], 0);
+        const int t_q1 = __shfl_sync(kFull, tq1[buf], 0);
+        const int t_oi = __shfl_sync(kFull, o_inc[buf], 0);
+        const int t_oc = __shfl_sync(kFull, o_coef[buf], 0);
+        if (t_q1 - t_q0 <= Tile<INT>::kCap)
+        {
+          const int v = i0 + lane;
+          const int rb = (v < Sz) ? __ldg(m.row + v) : t_q0;
+          const Tile<INT>* tile = &tiles[buf];
+          block_rounds<FL, REPLAY, INT, true>(S, m, W, ts, spins, lsp, scratch,
+                                              tile->inc + t_oi + (rb - t_q0),
+                                              tile->coef + t_oc + (rb - t_q0), i0, Sz, nwd, beta,
+                                              nbeta_f, beta_inf, ctr0);
+        }
+        else
+          block_rounds<FL, REPLAY, INT, false>(S, m, W, ts, spins, lsp, scratch, nullptr,
+                                               nullptr, i0, Sz, nwd, beta, nbeta_f, beta_inf,
+                                               ctr0);
       }
-      const int t_q0 = __shfl_sync(kFull, tq0[buf], 0);
-      const int t_oi = __shfl_sync(kFull, o_inc[buf], 0);
-      const int t_oc = __shfl_sync(kFull, o_coef[buf], 0);
-      const int v = i0 + lane;
-      const bool valid = v < Sz;
-      const int nvalid = min(32, Sz - i0);
-      int rb = 0, re = 0;
-      uint32_t sv = 0, nb = 0;
-      if (valid)
-      {
-        rb = __ldg(m.row + v);
-        re = __ldg(m.row + v + 1);
-        sv = spin_of(spins, v);
-        nb = __ldg(m.nbr + v);
-      }
-      // incidence q -> (term | neg, coefficient) from the tile or, past its
-      // capacity, from global memory
-      auto inc_at = [&](int q) -> uint32_t {
-        int j = q - t_q0;
-        return (staged && j < Tile<INT>::kCap) ? tile->inc[t_oi + j] : __ldg(m.inc + q);
-      };
-      auto coef_at = [&](int q) -> C {
-        int j = q - t_q0;
-        if (staged && j < Tile<INT>::kCap) return tile->coef[t_oc + j];
-        return INT ? (C)__ldg(m.coef_i + q) : (C)__ldg(m.coef + q);
-      };
-
-      int cursor = 0;
-      while (cursor < nvalid)
-      {
-        const bool active = valid && lane >= cursor;
-        double dE = 0.0;
-        long long idE = 0;
-        if (active)
-        {
-          if (FL == F_PARITY)
-          {
-            if (INT)
-            {
-              int acc = 0;
-#pragma unroll 4
-              for (int q = rb; q < re; q++)
-              {
-                int c = (int)coef_at(q);
-                acc += ts[inc_at(q)] ? -c : c;
-              }
-              idE = -2 * (long long)acc;
-            }
-            else
-            {
-              double diff = 0.0;
-#pragma unroll 4
-              for (int q = rb; q < re; q++)
-              {
-                double c = (double)coef_at(q);
-                diff = __dadd_rn(diff, ts[inc_at(q)] ? -c : c);
-              }
-              dE = neg2x(diff);
-            }
-          }
-          else if (FL == F_COUNTER && INT)
-          {
-            int acc = 0;
-#pragma unroll 4
-            for (int q = rb; q < re; q++)
-            {
-              uint32_t e = inc_at(q);
-              uint8_t z = ts[e & ~kNegBit];
-              int c = (int)coef_at(q);
-              if (sv ^ (e >> 31)) acc += (z == 1) ? c : 0;
-              else acc -= (z == 0) ? c : 0;
-            }
-            idE = acc;
-          }
-        }
-        if (FL == F_COUNTER && !INT)
-        {
-          // contributing terms only: collect a chunk of them, then sum in order
-          double diff = 0.0;
-          const int qe_all = active ? re : rb;
-          for (int q0 = rb; __any_sync(kFull, q0 < qe_all); q0 += kScratch)
-          {
-            int n = 0;
-            const int qe = min(qe_all, q0 + kScratch);
-            for (int q = q0; q < qe; q++)
-            {
-              uint32_t e = inc_at(q);
-              uint8_t z = ts[e & ~kNegBit];
-              bool lit = (sv ^ (e >> 31)) != 0;
-              if (lit ? (z == 1) : (z == 0))
-              {
-                scratch[n * 32 + lane] = (uint32_t)q | (lit ? 0u : kNegBit);
-                n++;
-              }
-            }
-            for (int j = 0; j < n; j++)
-            {
-              uint32_t x = scratch[j * 32 + lane];
-              double c = (double)coef_at((int)(x & ~kNegBit));
-              diff = (x & kNegBit) ? __dsub_rn(diff, c) : __dadd_rn(diff, c);
-            }
-          }
-          dE = diff;
-        }
-        if (FL == F_PLAIN_ISING || FL == F_PLAIN_PUBO)
-        {
-          if (active)
-          {
-            double diff = 0.0;
-            long long iacc = 0;
-            for (int q = rb; q < re; q++)
-            {
-              int t = (int)__ldg(m.inc + q);
-              int tb = __ldg(m.trow + t), te = __ldg(m.trow + t + 1);
-              if (FL == F_PLAIN_ISING)
-              {
-                uint32_t par = 0;
-                for (int u = tb; u < te; u++) par ^= spin_of(spins, (int)__ldg(m.tvar + u));
-                if (INT) iacc += par ? -(long long)__ldg(m.coef_i + q) : (long long)__ldg(m.coef_i + q);
-                else diff = __dadd_rn(diff, par ? -__ldg(m.coef + q) : __ldg(m.coef + q));
-              }
-              else
-              {
-                bool zero = false;
-                for (int u = tb; u < te; u++)
-                {
-                  int x = (int)__ldg(m.tvar + u);
-                  if (x != v && spin_of(spins, x)) { zero = true; break; }
-                }
-                if (!zero)
-                {
-                  if (INT) iacc += sv ? (long long)__ldg(m.coef_i + q) : -(long long)__ldg(m.coef_i + q);
-                  else diff = sv ? __dadd_rn(diff, __ldg(m.coef + q)) : __dsub_rn(diff, __ldg(m.coef + q));
-                }
-              }
-            }
-            if (FL == F_PLAIN_ISING)
-            {
-              if (INT) idE = -2 * iacc;
-              else dE = neg2x(diff);
-            }
-            else
-            {
-              if (INT) idE = iacc;
-              else dE = diff;
-            }
-          }
-        }
-
-        // ---- acceptance (markov/metropolis.h:64-104) ----------------------
-        const unsigned before = lt & ~((1u << cursor) - 1u);  // lanes in [cursor, lane)
-        const bool uphill = active && (INT ? (idE > 0) : !le_zero(dE));
-        bool acc = active && !uphill;
-        bool redraw = false;
-        unsigned U = 0;
-        int pos = 0;
-        if (REPLAY)
-        {
-          U = __ballot_sync(kFull, uphill);
-          pos = __popc(U & before);
-          if (uphill)
-          {
-            uint32_t r0 = pcg_out(S.jA[pos] * rs + S.jC[pos]);
-            redraw = (r0 & 255u) == 0;
-            if (!redraw) acc = uphill_accept<INT>(S, r0, 0, dE, idE, beta, nbeta_f);
-          }
-        }
-        else if (uphill)
-        {
-          const unsigned long long ctr = ctr0 + (unsigned long long)v;
-          const uint64_t w0 = counter_draw(key, 2ULL * ctr);
-          int row = -1, b = 0, used = 0;
-          uint32_t cur = 0;
-          bool decided = false;
-          while (b == 0)
-          {
-            if (row < 3)
-            {
-              if (used == 0) cur = (uint32_t)w0;
-              else if (used == 1) cur = (uint32_t)(w0 >> 32);
-              else
-              {
-                uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
-                cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
-              }
-              used++;
-              b = (int)(cur & 255u);
-              row++;
-            }
-            else
-            {
-              decided = true;
-              break;
-            }
-          }
-          acc = decided ? true : uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f);
-        }
-        const unsigned A = __ballot_sync(kFull, acc);
-        bool conf = false;
-        if (active && lane > cursor)
-          conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
-        const unsigned Cm = __ballot_sync(kFull, conf);
-        const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
-        const unsigned stop = Cm | Rm;
-        int f = stop ? (__ffs(stop) - 1) : 32;
-        if (f > nvalid) f = nvalid;
-        const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
-        const unsigned commit = ((f >= 32) ? kFull : ((1u << f) - 1u)) & ~((1u << cursor) - 1u);
-        unsigned flips = A & commit;
-        int draws = REPLAY ? __popc(U & commit) : 0;
-        if (REPLAY && slow)
-        {
-          int sacc = 0, used = 0;
-          if (lane == f)
-          {
-            int row = -1, b = 0;
-            uint32_t cur = 0;
-            bool decided = false;
-            while (b == 0)
-            {
-              if (row < 3)
-              {
-                cur = pcg_out(S.jA[pos + used] * rs + S.jC[pos + used]);
-                used++;
-                b = (int)(cur & 255u);
-                row++;
-              }
-              else
-              {
-                decided = true;
-                break;
-              }
-            }
-            bool ok = decided ? true : uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f);
-            sacc = ok ? 1 : 0;
-          }
-          sacc = __shfl_sync(kFull, sacc, f);
-          used = __shfl_sync(kFull, used, f);
-          if (sacc) flips |= 1u << f;
-          draws += used;
-        }
-        const int adv = f + (slow ? 1 : 0) - cursor;
-
-        // ---- apply accepted flips (their term sets are disjoint) ----------
-        if ((flips >> lane) & 1u)
-        {
-          if (FL == F_PARITY)
-          {
-            for (int q = rb; q < re; q++) ts[inc_at(q)] ^= (uint8_t)1;
-          }
-          else if (FL == F_COUNTER)
-          {
-            for (int q = rb; q < re; q++)
-            {
-              uint32_t e = inc_at(q);
-              uint32_t t = e & ~kNegBit;
-              ts[t] = (uint8_t)(ts[t] + ((sv ^ (e >> 31)) ? 0xFFu : 1u));
-            }
-          }
-        }
-        const int wi = i0 >> 5;
-        if (lane == 0 && flips) spins[wi] ^= flips;
-        // ---- running cost and lowest state, in attempt order --------------
-        int lowpos = -1;
-        unsigned fl = flips;
-        while (fl)
-        {
-          const int j = __ffs(fl) - 1;
-          fl &= fl - 1;
-          if (INT)
-          {
-            icost += __shfl_sync(kFull, idE, j);
-            if (icost < ilow)
-            {
-              ilow = icost;
-              lowpos = j;
-            }
-          }
-          else
-          {
-            cost = __dadd_rn(cost, __shfl_sync(kFull, dE, j));
-            long long kc = order_key(cost);
-            if (kc < klow)
-            {
-              klow = kc;
-              low = cost;
-              lowpos = j;
-            }
-          }
-        }
-        __syncwarp();
-        if (lowpos >= 0)
-        {
-          for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
-          __syncwarp();
-          const unsigned undo = flips & ~((2u << lowpos) - 1u);
-          if (lane == 0 && undo) lsp[wi] ^= undo;
-          __syncwarp();
-        }
-        natt += (unsigned long long)adv;
-        nacc += (unsigned long long)__popc(flips);
-        nwin++;
-        if (REPLAY) rs = S.jA[draws] * rs + S.jC[draws];
-        cursor += adv;
-      }
-      __syncwarp();
+      else
+        block_rounds_plain<FL, REPLAY, INT>(S, m, W, spins, lsp, i0, Sz, nwd, beta, nbeta_f,
+                                            beta_inf, ctr0);
     }
     if (aborted) return;
     if (SMEM)
@@ -685,17 +893,17 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
     }
     if (lane == 0)
     {
-      a.p.cost[slot] = INT ? (double)icost : cost;
-      a.p.lowest[r] = INT ? (double)ilow : low;
-      a.p.attempts[r] += natt;
-      a.p.accepts[r] += nacc;
-      a.p.step_att[r] += natt;
-      a.p.step_acc[r] += nacc;
-      if (a.p.windows) a.p.windows[r] += nwin;
+      a.p.cost[slot] = INT ? (double)W.icost : W.cost;
+      a.p.lowest[r] = INT ? (double)W.ilow : W.low;
+      a.p.attempts[r] += W.natt;
+      a.p.accepts[r] += W.nacc;
+      a.p.step_att[r] += W.natt;
+      a.p.step_acc[r] += W.nacc;
+      if (a.p.windows) a.p.windows[r] += W.nwin;
     }
     __syncwarp();
   }
-  if (REPLAY && lane == 0) a.rng[w] = rs;
+  if (REPLAY && lane == 0) a.rng[w] = W.rs;
 }
 
 // ---------------------------------------------------------------------------
