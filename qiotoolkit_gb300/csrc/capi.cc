@@ -3,7 +3,7 @@
 #include <cstring>
 #include <string>
 
-#include "../../include/qio_gb300.h"
+#include "qio_gb300.h"
 #include "host.h"
 
 using namespace qio;

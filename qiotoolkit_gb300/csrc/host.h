@@ -54,6 +54,9 @@ struct HostModel
   std::vector<uint32_t> inc;
   std::vector<double> coef;
   std::vector<int> coef_i;
+  std::vector<float> coef_f;
+  std::vector<unsigned long long> near;
+  bool fscreen = true, scan32 = false;
   std::vector<uint32_t> nbr;
   // term -> members
   std::vector<int> trow;

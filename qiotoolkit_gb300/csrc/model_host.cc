@@ -276,6 +276,40 @@ static void build_nbr(HostModel& m)
   }
 }
 
+// Later co-members for the per-block field updates: for incidence k of v
+// (term t), each member u of t with 0 < u - v <= 31 and a row of at most 32
+// incidences, encoded as (u - v, position of t in u's row).  When u flips
+// nothing is posted (it has been decided already); when v flips, these are
+// the undecided variables of the same 32-variable block whose cost
+// difference changes.
+static void build_near(HostModel& m)
+{
+  m.near.assign(m.K, 0ULL);
+  for (int64_t v = 0; v < m.N; v++)
+    for (int q = m.row[v]; q < m.row[v + 1]; q++)
+    {
+      uint32_t t = m.inc[q] & ~kNegBit;
+      unsigned long long w = 0;
+      int cnt = 0;
+      bool over = false;
+      for (int j = m.trow[t]; j < m.trow[t + 1]; j++)
+      {
+        int64_t u = (int64_t)(m.tvar[j] & ~kNegBit);
+        int64_t d = u - v;
+        if (d < 1 || d > 31) continue;
+        if (m.row[u + 1] - m.row[u] > 32) continue;
+        int kp = -1;
+        for (int x = m.row[u]; x < m.row[u + 1]; x++)
+          if ((m.inc[x] & ~kNegBit) == t) { kp = x - m.row[u]; break; }
+        if (kp < 0) continue;
+        if (cnt == 6) { over = true; break; }
+        w |= ((unsigned long long)d | ((unsigned long long)kp << 5)) << (10 * cnt);
+        cnt++;
+      }
+      m.near[q] = over ? (7ULL << 61) : (w | ((unsigned long long)cnt << 61));
+    }
+}
+
 // Integer mode: every coefficient is an integer of magnitude <= 2^20 and the
 // per-variable sums stay below 2^30, so int32/int64 arithmetic gives the same
 // values as the reference's FP64 sums (all partial sums are exact).
@@ -292,6 +326,29 @@ static void detect_int_mode(HostModel& m)
       if (2 * s >= 1073741824.0) ok = false;
     }
   m.int_mode = ok;
+  m.fscreen = true;
+  m.scan32 = false;
+  if (!ok)
+  {
+    m.coef_f.resize(m.K);
+    for (int64_t q = 0; q < m.K; q++)
+    {
+      const double a = std::fabs(m.coef[q]);
+      if (!(a == 0.0 || (a >= 1e-30 && a <= 1e30))) m.fscreen = false;
+      m.coef_f[q] = (float)m.coef[q];
+    }
+  }
+  else
+  {
+    double mx = 0;
+    for (int64_t v = 0; v < m.N; v++)
+    {
+      double s = 0;
+      for (int q = m.row[v]; q < m.row[v + 1]; q++) s += std::fabs(m.coef[q]);
+      mx = std::max(mx, 2 * s);
+    }
+    m.scan32 = 32.0 * mx < 2147483647.0;
+  }
   if (ok)
   {
     m.coef_i.resize(m.K);
@@ -334,6 +391,7 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
                         : 1.0 / m->max_coupling;
   build_nbr(*m);
   detect_int_mode(*m);
+  if (m->flavor == F_PARITY || m->flavor == F_COUNTER) build_near(*m);
   return m;
 }
 
@@ -352,7 +410,8 @@ void HostModel::upload() const
   std::vector<char> blob;
   size_t o_row = put(blob, row), o_inc = put(blob, inc), o_coef = put(blob, coef),
          o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
-         o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i);
+         o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
+         o_cf = put(blob, coef_f), o_near = put(blob, near);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -374,6 +433,10 @@ void HostModel::upload() const
   dev.tvar = (const uint32_t*)(b + o_tvar);
   dev.tcost = (const double*)(b + o_tc);
   dev.tcost_i = int_mode ? (const int*)(b + o_tci) : nullptr;
+  dev.coef_f = int_mode ? nullptr : (const float*)(b + o_cf);
+  dev.near = near.empty() ? nullptr : (const unsigned long long*)(b + o_near);
+  dev.fscreen = fscreen ? 1 : 0;
+  dev.scan32 = scan32 ? 1 : 0;
   uploaded = true;
 }
 

@@ -50,6 +50,14 @@ struct DevModel
   const uint32_t* inc;     // K
   const double* coef;      // K  coefficient of the incidence's term
   const int* coef_i;       // K  same, integer mode
+  const float* coef_f;     // K  same rounded to float (FP32 screen), FP64 mode
+  // near[k]: the later members u of incidence k's term (0 < u - v <= 31)
+  // whose rows hold at most 32 incidences, as 10-bit entries (u - v: bits
+  // 0-4, the term's position in u's row: bits 5-9), up to six of them; the
+  // count is in bits 61-63, 7 meaning "too many to list"
+  const unsigned long long* near;
+  int fscreen;             // FP64 coefficients all within the FP32 screen's range
+  int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1
   const uint32_t* tvar;    // K  members (| kNegBit for negated literals)

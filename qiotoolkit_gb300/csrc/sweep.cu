@@ -19,6 +19,7 @@
 // the ln-table comparison runs in FP32 with a rigorous error margin, falling
 // back to the exact FP64 expression only inside the margin.  Walker state
 // (term bytes, spins, lowest spins) lives in shared memory when it fits.
+#include <climits>
 #include <type_traits>
 
 #include "qio_internal.h"
@@ -28,8 +29,8 @@ namespace qio
 namespace sw
 {
 static const unsigned kFull = 0xffffffffu;
+static const int kHdr = 160;  // per-warp header: 2 mbarriers, 33 dirty words
 static const unsigned long long kGamma = 0x9E3779B97F4A7C15ULL;
-static const int kScratch = 32;  // compaction chunk (incidences per lane)
 
 __constant__ double c_ln[1024];
 __constant__ float c_scr[1024 * 3];  // y0, dy, err per (row, bucket)
@@ -153,6 +154,32 @@ __device__ __forceinline__ uint32_t spin_of(const uint32_t* spins, int v)
   return (spins[v >> 5] >> (v & 31)) & 1u;
 }
 
+// any contributing incidence (rows of more than 32 incidences are "wide")
+__device__ __forceinline__ bool nq_nonzero(uint32_t qm, bool wide) { return wide || qm != 0u; }
+
+// Exact reference-order FP64 difference for a row of more than 32
+// incidences, recomputed from the term states (rare: high-degree variables).
+template <int FL, class C>
+__device__ __forceinline__ double exact_dE_wide(bool part, uint32_t sv, const uint8_t* ts,
+                                                const uint32_t* pinc, const C* pcoef, int deg)
+{
+  double diff = 0.0;
+  const int n = part ? deg : 0;
+  for (int k = 0; k < n; k++)
+  {
+    uint32_t e = pinc[k];
+    uint8_t z = ts[e & ~kNegBit];
+    double c = (double)pcoef[k];
+    if (FL == F_PARITY) diff = __dadd_rn(diff, z ? -c : c);
+    else
+    {
+      const bool lit = (sv ^ (e >> 31)) != 0;
+      if (lit ? (z == 1) : (z == 0)) diff = lit ? __dadd_rn(diff, c) : __dsub_rn(diff, c);
+    }
+  }
+  return (FL == F_PARITY) ? neg2x(diff) : diff;
+}
+
 // warp-cooperative copy of `words` 32-bit words (16-byte aligned, multiple of 4)
 __device__ __forceinline__ void copy_words(uint32_t* dst, const uint32_t* src, int words, int lane)
 {
@@ -205,42 +232,50 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
   return false;
 }
 
-// Per-warp tile of the CSR incidences of one 32-variable block: term ids and
-// coefficients of [q0, q0 + n) copied with two bulk copies.  Bulk copies move
-// 16-byte aligned, 16-byte multiple ranges, so each starts at the aligned
-// address below its first element and records the element offset.
+// Per-warp tile of the CSR incidences of one 32-variable block: term ids,
+// coefficients and later-co-member words of [q0, q0 + n) brought in by bulk
+// copies.  Bulk copies move 16-byte aligned, 16-byte multiple ranges, so each
+// starts at the aligned address below its first element and records the
+// element offset.  FP64 models carry the coefficients twice: rounded to float
+// for the screen and exact for the reference-order sums.
 template <bool INT>
 struct Tile
 {
-  static const int kCap = 768;  // incidences held in shared memory
+  static const int kCap = INT ? 768 : 640;  // incidences held in shared memory
   uint32_t inc[kCap + 8];
+  float coef_f[INT ? 4 : kCap + 8];
   typename std::conditional<INT, int, double>::type coef[kCap + 8];
+  unsigned long long near[kCap + 8];
 };
 
 template <bool INT>
 __device__ __forceinline__ void tile_issue(Tile<INT>* t, unsigned long long* bar, const DevModel& m,
-                                           int q0, int q1, int& o_inc, int& o_coef)
+                                           int q0, int q1, int* off)
 {
   using C = typename std::conditional<INT, int, double>::type;
   const int n = min(q1 - q0, Tile<INT>::kCap);
   const C* cbase = INT ? (const C*)m.coef_i : (const C*)m.coef;
-  const char* a_inc = (const char*)(m.inc + q0);
-  const char* a_coef = (const char*)(cbase + q0);
-  const char* s_inc = (const char*)((size_t)a_inc & ~(size_t)15);
-  const char* s_coef = (const char*)((size_t)a_coef & ~(size_t)15);
-  o_inc = (int)((a_inc - s_inc) / 4);
-  o_coef = (int)((a_coef - s_coef) / (int)sizeof(C));
-  unsigned b_inc = (unsigned)(((a_inc + 4 * (size_t)n) - s_inc + 15) & ~(size_t)15);
-  unsigned b_coef = (unsigned)(((a_coef + sizeof(C) * (size_t)n) - s_coef + 15) & ~(size_t)15);
-  if (n <= 0)
+  const void* src[4] = {m.inc + q0, cbase + q0, m.near + q0,
+                        INT ? (const void*)m.inc : (const void*)(m.coef_f + q0)};
+  const int esz[4] = {4, (int)sizeof(C), 8, 4};
+  void* dst[4] = {t->inc, t->coef, t->near, t->coef_f};
+  const int ncopy = INT ? 3 : 4;
+  unsigned bytes[4];
+  const char* start[4];
+  unsigned total = 0;
+#pragma unroll
+  for (int c = 0; c < ncopy; c++)
   {
-    b_inc = 16;
-    b_coef = 16;
+    const char* a = (const char*)src[c];
+    start[c] = (const char*)((size_t)a & ~(size_t)15);
+    off[c] = (int)((a - start[c]) / esz[c]);
+    bytes[c] = (unsigned)(((a + (size_t)esz[c] * (size_t)(n > 0 ? n : 1)) - start[c] + 15) & ~(size_t)15);
+    total += bytes[c];
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  mbar_expect(bar, b_inc + b_coef);
-  tma_1d(t->inc, s_inc, b_inc, bar);
-  tma_1d(t->coef, s_coef, b_coef, bar);
+  mbar_expect(bar, total);
+#pragma unroll
+  for (int c = 0; c < ncopy; c++) tma_1d(dst[c], start[c], bytes[c], bar);
 }
 
 // Mutable per-walker state of the sweep.
@@ -252,14 +287,74 @@ struct Walk
   uint64_t rs, key;
 };
 
-// All rounds of one 32-variable block.  TILE: the block's incidences are in
-// the shared tile (term ids at tinc[bi + k], coefficients at tcoef[bc + k]);
-// otherwise they are read from global memory at [rb, re).
+// warp-inclusive prefix sums
+__device__ __forceinline__ long long warp_scan64(long long x, int lane)
+{
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1)
+  {
+    long long y = __shfl_up_sync(kFull, x, d);
+    if (lane >= d) x += y;
+  }
+  return x;
+}
+__device__ __forceinline__ int warp_scan32(int x, int lane)
+{
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1)
+  {
+    int y = __shfl_up_sync(kFull, x, d);
+    if (lane >= d) x += y;
+  }
+  return x;
+}
+
+// Exact reference-order FP64 cost difference from the masks: bit k of qm =
+// incidence k contributes, bit k of sm = its sign (counter: literal true ->
+// +c; parity: term bit set -> -c).  The warp issues one FP64 add per set bit
+// of the longest mask among participating lanes.
+template <int FL>
+__device__ __forceinline__ double exact_dE(bool part, uint32_t qm, uint32_t sm, const double* pc)
+{
+  double diff = 0.0;
+  uint32_t q = part ? qm : 0u;
+  while (__any_sync(kFull, q != 0u))
+  {
+    if (q)
+    {
+      const int k = __ffs(q) - 1;
+      q &= q - 1;
+      long long cb = __double_as_longlong(pc[k]);
+      const bool neg = (FL == F_PARITY) ? ((sm >> k) & 1u) != 0u : ((sm >> k) & 1u) == 0u;
+      cb ^= (long long)neg << 63;
+      diff = __dadd_rn(diff, __longlong_as_double(cb));
+    }
+  }
+  return (FL == F_PARITY) ? neg2x(diff) : diff;
+}
+
+// All rounds of one 32-variable block.  Lane l holds variable i0 + l.  On
+// entry every lane reads its row once into per-incidence masks (qm: the
+// incidence contributes to the cost difference, sm: its sign) and a field
+// (the integer difference, or an FP32 estimate with a rigorous error bound).
+// A round decides the undecided lanes from their fields, commits the prefix
+// up to the first lane that shares a term with an earlier accepted lane of
+// the round (or that needs the redraw path), and applies the committed
+// flips: term bytes change by shared-memory atomics and each flip marks the
+// incidences of later undecided lanes that share its terms (the per-lane
+// dirty words, dirty[32] = "recompute all"), which those lanes re-read at
+// the start of the next round.  Rows of more than 32 incidences ("wide")
+// are recomputed every round.  FP64 cost differences are summed exactly, in
+// the reference's term order, only for lanes whose sign or comparison the
+// screen leaves open and for the flips that may be committed.
+// TILE: the block's incidences are in the shared tile; otherwise they are
+// read from global memory.
 template <int FL, bool REPLAY, bool INT, bool TILE>
 __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, Walk& W,
                                              uint8_t* ts, uint32_t* spins, uint32_t* lsp,
-                                             uint32_t* scratch, const uint32_t* tinc,
+                                             uint32_t* dirty, const uint32_t* tinc,
                                              const typename std::conditional<INT, int, double>::type* tcoef,
+                                             const float* tcf, const unsigned long long* tnear,
                                              int i0, int Sz, int nwd, double beta, float nbeta_f,
                                              bool beta_inf, unsigned long long ctr0)
 {
@@ -278,147 +373,308 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     sv = spin_of(spins, v);
     nb = __ldg(m.nbr + v);
   }
-  // incidence k of this lane's variable
   const uint32_t* pinc = TILE ? tinc : (const uint32_t*)(m.inc + rb);
   const C* pcoef = TILE ? tcoef : (INT ? (const C*)(m.coef_i + rb) : (const C*)(m.coef + rb));
+  const float* pcf = TILE ? tcf : (INT ? nullptr : m.coef_f + rb);
+  const unsigned long long* pnear = TILE ? tnear : m.near + rb;
   auto INC = [&](int k) -> uint32_t { return TILE ? pinc[k] : __ldg(pinc + k); };
   auto COEF = [&](int k) -> C { return TILE ? pcoef[k] : __ldg(pcoef + k); };
+  auto CF = [&](int k) -> float { return TILE ? pcf[k] : __ldg(pcf + k); };
+  auto NEAR = [&](int k) -> unsigned long long { return TILE ? pnear[k] : __ldg(pnear + k); };
+  const bool wide = deg > 32;
+  const bool narrow = valid && !wide;
+  uint32_t* ts32 = (uint32_t*)ts;
+
+  uint32_t qm = 0, sm = 0;
+  int ifield = 0;
+  float ffield = 0.f, fsabs = 0.f;
+  int nops = 0;
+  // the whole row: masks (first 32 incidences) and field
+  auto gather = [&]() {
+    uint32_t q = 0, sg = 0;
+    int ia = 0;
+    float fa = 0.f, fs = 0.f;
+    for (int k = 0; k < deg; k++)
+    {
+      const uint32_t e = INC(k);
+      const uint32_t z = ts[e & ~kNegBit];
+      if (FL == F_PARITY)
+      {
+        if (INT)
+        {
+          const int c = (int)COEF(k);
+          ia += z ? -c : c;
+        }
+        else
+        {
+          const float c = CF(k);
+          fa = __fadd_rn(fa, z ? -c : c);
+          fs = __fadd_rn(fs, fabsf(c));
+        }
+        if (k < 32) sg |= z << k;
+      }
+      else
+      {
+        const uint32_t lit = (sv ^ (e >> 31)) & 1u;
+        const uint32_t qual = lit ? (z == 1u) : (z == 0u);
+        if (INT)
+        {
+          const int c = (int)COEF(k);
+          ia += qual ? (lit ? c : -c) : 0;
+        }
+        else
+        {
+          const float c = CF(k);
+          fa = __fadd_rn(fa, qual ? (lit ? c : -c) : 0.f);
+          fs = __fadd_rn(fs, fabsf(c));
+        }
+        if (k < 32)
+        {
+          q |= qual << k;
+          sg |= lit << k;
+        }
+      }
+    }
+    qm = (FL == F_PARITY) ? ((deg >= 32) ? kFull : ((1u << deg) - 1u)) : q;
+    sm = sg;
+    ifield = ia;
+    ffield = fa;
+    fsabs = fs;
+    nops = deg;
+  };
+  // re-read the marked incidences and correct the field
+  auto refresh = [&](uint32_t dm) {
+    while (dm)
+    {
+      const int k = __ffs(dm) - 1;
+      dm &= dm - 1;
+      const uint32_t e = INC(k);
+      const uint32_t z = ts[e & ~kNegBit];
+      if (FL == F_PARITY)
+      {
+        if (z != ((sm >> k) & 1u))
+        {
+          sm ^= 1u << k;
+          if (INT)
+          {
+            const int c = (int)COEF(k);
+            ifield += z ? -2 * c : 2 * c;
+          }
+          else
+          {
+            const float c = CF(k);
+            ffield = __fadd_rn(ffield, z ? -2.f * c : 2.f * c);
+            nops += 2;
+          }
+        }
+      }
+      else
+      {
+        const uint32_t lit = (sm >> k) & 1u;
+        const uint32_t qual = lit ? (z == 1u) : (z == 0u);
+        if (qual != ((qm >> k) & 1u))
+        {
+          qm ^= 1u << k;
+          if (INT)
+          {
+            const int c = (int)COEF(k);
+            const int d = lit ? c : -c;
+            ifield += qual ? d : -d;
+          }
+          else
+          {
+            const float c = CF(k);
+            const float d = lit ? c : -c;
+            ffield = __fadd_rn(ffield, qual ? d : -d);
+            nops += 2;
+          }
+        }
+      }
+    }
+  };
+
+  if (narrow) gather();
+  dirty[lane] = 0u;
+  if (lane == 0) dirty[32] = 0u;
+  __syncwarp();
 
   int cursor = 0;
+  bool first = true;
   while (cursor < nvalid)
   {
     const bool active = valid && lane >= cursor;
-    const int dk = active ? deg : 0;
-    double dE = 0.0;
-    long long idE = 0;
-    if (FL == F_PARITY)
+    if (!first)
     {
-      if (INT)
+      const uint32_t all = dirty[32];
+      const uint32_t dm = dirty[lane];
+      __syncwarp();
+      if (active && narrow)
       {
-        int acc = 0;
-#pragma unroll 4
-        for (int k = 0; k < dk; k++)
-        {
-          int c = (int)COEF(k);
-          acc += ts[INC(k)] ? -c : c;
-        }
-        idE = -2 * (long long)acc;
+        if (all) gather();
+        else refresh(dm);
       }
-      else
-      {
-        double diff = 0.0;
-#pragma unroll 4
-        for (int k = 0; k < dk; k++)
-        {
-          long long cb = __double_as_longlong((double)COEF(k));
-          cb ^= (long long)ts[INC(k)] << 63;
-          diff = __dadd_rn(diff, __longlong_as_double(cb));
-        }
-        dE = neg2x(diff);
-      }
+      if (dm) dirty[lane] = 0u;
+      if (lane == 0 && all) dirty[32] = 0u;
+      __syncwarp();
+    }
+    first = false;
+
+    // ---- cost difference: exact where known, screened otherwise --------
+    long long idE = 0;
+    double dE = 0.0;
+    bool have_exact = false;
+    float dEf = 0.f, bound = 0.f;
+    if constexpr (INT)
+    {
+      if (active && wide) gather();
+      idE = (FL == F_PARITY) ? -2LL * (long long)ifield : (long long)ifield;
     }
     else
     {
-      if (INT)
+      if (__any_sync(kFull, active && wide))
       {
-        int acc = 0;
-#pragma unroll 4
-        for (int k = 0; k < dk; k++)
+        const double ex = exact_dE_wide<FL>(active && wide, sv, ts, pinc, pcoef, deg);
+        if (active && wide)
         {
-          uint32_t e = INC(k);
-          uint8_t z = ts[e & ~kNegBit];
-          int c = (int)COEF(k);
-          if (sv ^ (e >> 31)) acc += (z == 1) ? c : 0;
-          else acc -= (z == 0) ? c : 0;
+          dE = ex;
+          have_exact = true;
         }
-        idE = acc;
       }
-      else
+      if (active && narrow)
       {
-        // contributing terms only (sign folded in), then one ordered FP64 add
-        // each; the warp issues max-over-lanes adds per chunk
-        double diff = 0.0;
-        for (int k0 = 0; __any_sync(kFull, k0 < dk); k0 += kScratch)
+        dEf = (FL == F_PARITY) ? -2.f * ffield : ffield;
+        bound = m.fscreen ? __fmaf_rn((FL == F_PARITY ? 2.f : 1.f) * fsabs,
+                                      (float)(nops + 2) * 9.5367431640625e-07f, 1e-35f)  // 2^-20
+                          : INFINITY;
+        // no contributing term: the reference's sum is exactly +0.0
+        if (FL != F_PARITY && qm == 0u) have_exact = true;
+      }
+      const bool undecided = active && narrow && !have_exact && !(fabsf(dEf) > bound);
+      if (__any_sync(kFull, undecided))
+      {
+        const double ex = exact_dE<FL>(undecided, qm, sm, pcoef);
+        if (undecided)
         {
-          int n = 0;
-          const int ke = min(dk, k0 + kScratch);
-          for (int k = k0; k < ke; k++)
-          {
-            uint32_t e = INC(k);
-            uint8_t z = ts[e & ~kNegBit];
-            bool lit = (sv ^ (e >> 31)) != 0;
-            if (lit ? (z == 1) : (z == 0))
-            {
-              scratch[n * 32 + lane] = (uint32_t)k | (lit ? 0u : kNegBit);
-              n++;
-            }
-          }
-          for (int j = 0; j < n; j++)
-          {
-            uint32_t x = scratch[j * 32 + lane];
-            long long cb = __double_as_longlong((double)COEF((int)(x & ~kNegBit)));
-            cb ^= (long long)(x >> 31) << 63;
-            diff = __dadd_rn(diff, __longlong_as_double(cb));
-          }
+          dE = ex;
+          have_exact = true;
         }
-        dE = diff;
       }
     }
 
     // ---- acceptance (markov/metropolis.h:64-104) ----------------------
     const unsigned before = lt & ~((1u << cursor) - 1u);  // lanes in [cursor, lane)
-    const bool uphill = active && (INT ? (idE > 0) : !le_zero(dE));
+    bool uphill;
+    if (INT) uphill = active && idE > 0;
+    else uphill = active && (have_exact ? !le_zero(dE) : (dEf > 0.f));
     bool acc = active && !uphill;
     bool redraw = false;
     unsigned U = 0;
     int pos = 0;
+    // FP32-screened comparison value < dE * (-beta); -1 inside the margin
+    auto decide = [&](uint32_t r, int row) -> int {
+      if (beta_inf) return 0;
+      if (INT || have_exact)
+      {
+        const float thr_f = INT ? __fmul_rn((float)idE, nbeta_f) : __fmul_rn(approx_float(dE), nbeta_f);
+        return lut_screen(S.scr, r, row, thr_f);
+      }
+      const float thr_f = __fmul_rn(dEf, nbeta_f);
+      // widen the margin by the screen's own error times beta
+      const float et_extra = __fmul_rn(bound, -nbeta_f) * 1.0000002f;
+      const int b = (int)(r & 255u);
+      if (b == 1) return 0;
+      const int kk = (row * 256 + b) * 3;
+      const float y0 = S.scr[kk], dy = S.scr[kk + 1], ev = S.scr[kk + 2];
+      const float dist = __fmul_rn((float)(r >> 8), 5.96046483e-08f);
+      const float value = __fmaf_rn(dist, dy, y0);
+      const float et = __fmaf_rn(fabsf(thr_f), 1.9073486328125e-06f, 1e-30f) + et_extra;
+      if (__fadd_rn(value, ev) < __fsub_rn(thr_f, et)) return 1;
+      if (__fsub_rn(value, ev) > __fadd_rn(thr_f, et)) return 0;
+      return -1;
+    };
     if (REPLAY)
     {
       U = __ballot_sync(kFull, uphill);
       pos = __popc(U & before);
-      if (uphill)
-      {
-        uint32_t r0 = pcg_out(S.jA[pos] * W.rs + S.jC[pos]);
-        redraw = (r0 & 255u) == 0;
-        if (!redraw) acc = !beta_inf && uphill_accept<INT>(S, r0, 0, dE, idE, beta, nbeta_f);
-      }
     }
-    else if (uphill)
+    uint32_t dr = 0;
+    int drow = 0;
+    int dec = 1;  // 1 accept, 0 reject, -1 needs the exact expression
+    if (uphill)
     {
-      const unsigned long long ctr = ctr0 + (unsigned long long)v;
-      const uint64_t w0 = counter_draw(W.key, 2ULL * ctr);
-      int row = -1, b = 0, used = 0;
-      uint32_t cur = 0;
-      bool decided = false;
-      while (b == 0)
+      if (REPLAY)
       {
-        if (row < 3)
+        dr = pcg_out(S.jA[pos] * W.rs + S.jC[pos]);
+        redraw = (dr & 255u) == 0;
+        if (!redraw) dec = decide(dr, 0);
+      }
+      else
+      {
+        const unsigned long long ctr = ctr0 + (unsigned long long)v;
+        const uint64_t w0 = counter_draw(W.key, 2ULL * ctr);
+        int row = -1, b = 0, used = 0;
+        uint32_t cur = 0;
+        bool all_zero = false;
+        while (b == 0)
         {
-          if (used == 0) cur = (uint32_t)w0;
-          else if (used == 1) cur = (uint32_t)(w0 >> 32);
+          if (row < 3)
+          {
+            if (used == 0) cur = (uint32_t)w0;
+            else if (used == 1) cur = (uint32_t)(w0 >> 32);
+            else
+            {
+              uint64_t w1 = counter_draw(W.key, 2ULL * ctr + 1ULL);
+              cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+            }
+            used++;
+            b = (int)(cur & 255u);
+            row++;
+          }
           else
           {
-            uint64_t w1 = counter_draw(W.key, 2ULL * ctr + 1ULL);
-            cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+            all_zero = true;
+            break;
           }
-          used++;
-          b = (int)(cur & 255u);
-          row++;
         }
-        else
+        dr = cur;
+        drow = row;
+        dec = all_zero ? 1 : decide(cur, row);
+      }
+    }
+    const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
+    if constexpr (!INT)
+    {
+      // Exact differences for the lanes that may be committed: up to the
+      // first stop under the surely accepted lanes (more acceptances can
+      // only move the stop earlier).
+      const bool sure = active && (!uphill || (!redraw && dec == 1));
+      const unsigned As = __ballot_sync(kFull, sure);
+      bool cs = false;
+      if (active && lane > cursor)
+        cs = (nb & (__brev(As) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+      const unsigned stop_s = __ballot_sync(kFull, cs) | Rm;
+      const int fs = stop_s ? (__ffs(stop_s) - 1) : 32;
+      const bool cand = active && lane <= fs && !have_exact && (!uphill || redraw || dec != 0);
+      if (__any_sync(kFull, cand))
+      {
+        const double ex = exact_dE<FL>(cand, qm, sm, pcoef);
+        if (cand)
         {
-          decided = true;
-          break;
+          dE = ex;
+          have_exact = true;
         }
       }
-      acc = decided ? true : (!beta_inf && uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f));
+      if (lane > fs && dec < 0) dec = 0;  // cannot be committed this round
     }
+    // lanes inside the screen's margin: exact comparison
+    if (uphill && !redraw && dec < 0)
+      dec = lut_less_exact(S.ln, dr, drow, __dmul_rn(INT ? (double)idE : dE, -beta)) ? 1 : 0;
+    if (uphill && !redraw) acc = dec == 1;
     const unsigned A = __ballot_sync(kFull, acc);
     bool conf = false;
     if (active && lane > cursor)
       conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
     const unsigned Cm = __ballot_sync(kFull, conf);
-    const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
     const unsigned stop = Cm | Rm;
     int f = stop ? (__ffs(stop) - 1) : 32;
     if (f > nvalid) f = nvalid;
@@ -428,6 +684,7 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     int draws = REPLAY ? __popc(U & commit) : 0;
     if (REPLAY && slow)
     {
+      // lane f drew a zero bucket: its redraw chain (markov/metropolis.h:93-103)
       int sacc = 0, used = 0;
       if (lane == f)
       {
@@ -449,8 +706,10 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
             break;
           }
         }
-        bool ok = decided ? true
-                          : (!beta_inf && uphill_accept<INT>(S, cur, row, dE, idE, beta, nbeta_f));
+        bool ok;
+        if (decided) ok = true;
+        else if (beta_inf) ok = false;
+        else ok = lut_less_exact(S.ln, cur, row, __dmul_rn(INT ? (double)idE : dE, -beta));
         sacc = ok ? 1 : 0;
       }
       sacc = __shfl_sync(kFull, sacc, f);
@@ -459,44 +718,71 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
       draws += used;
     }
     const int adv = f + (slow ? 1 : 0) - cursor;
+    const bool mine = ((flips >> lane) & 1u) != 0u;
 
-    // ---- apply accepted flips (their term sets are disjoint) ----------
-    if ((flips >> lane) & 1u)
+    // ---- apply: term bytes by atomics, marks for later co-members ------
+    if (mine)
     {
-      if (FL == F_PARITY)
+      for (int k = 0; k < deg; k++)
       {
-        for (int k = 0; k < deg; k++) ts[INC(k)] ^= (uint8_t)1;
-      }
-      else
-      {
-        for (int k = 0; k < deg; k++)
-        {
-          uint32_t e = INC(k);
-          uint32_t t = e & ~kNegBit;
-          ts[t] = (uint8_t)(ts[t] + ((sv ^ (e >> 31)) ? 0xFFu : 1u));
-        }
+        const uint32_t e = INC(k);
+        const unsigned long long nw = NEAR(k);
+        const uint32_t t = e & ~kNegBit;
+        const unsigned sh = (t & 3u) << 3;
+        if (FL == F_PARITY) atomicXor(ts32 + (t >> 2), 1u << sh);
+        else atomicAdd(ts32 + (t >> 2), ((sv ^ (e >> 31)) & 1u) ? (0u - (1u << sh)) : (1u << sh));
+        const int cnt = (int)(nw >> 61);
+        if (cnt == 7) atomicOr(dirty + 32, 1u);
+        else
+          for (int i = 0; i < cnt; i++)
+          {
+            const int u = lane + (int)((nw >> (10 * i)) & 31u);
+            if (u < 32) atomicOr(dirty + u, 1u << (unsigned)((nw >> (10 * i + 5)) & 31u));
+          }
       }
     }
     const int wi = i0 >> 5;
     if (lane == 0 && flips) spins[wi] ^= flips;
     // ---- running cost and lowest state, in attempt order --------------
     int lowpos = -1;
-    unsigned fl = flips;
-    while (fl)
+    if (INT)
     {
-      const int j = __ffs(fl) - 1;
-      fl &= fl - 1;
-      if (INT)
+      if (flips)
       {
-        W.icost += __shfl_sync(kFull, idE, j);
-        if (W.icost < W.ilow)
+        if (m.scan32)
         {
-          W.ilow = W.icost;
-          lowpos = j;
+          const int pre = warp_scan32(mine ? (int)idE : 0, lane);
+          const int mn = __reduce_min_sync(kFull, mine ? pre : INT_MAX);
+          if ((long long)mn < W.ilow - W.icost)
+          {
+            lowpos = __ffs(__ballot_sync(kFull, mine && pre == mn)) - 1;
+            W.ilow = W.icost + mn;
+          }
+          W.icost += __shfl_sync(kFull, pre, 31);
+        }
+        else
+        {
+          const long long pre = warp_scan64(mine ? idE : 0LL, lane);
+          const long long ci = W.icost + pre;
+          long long mn = mine ? ci : LLONG_MAX;
+#pragma unroll
+          for (int d = 16; d; d >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, d));
+          if (mn < W.ilow)
+          {
+            lowpos = __ffs(__ballot_sync(kFull, mine && ci == mn)) - 1;
+            W.ilow = mn;
+          }
+          W.icost += __shfl_sync(kFull, pre, 31);
         }
       }
-      else
+    }
+    else
+    {
+      unsigned fl = flips;
+      while (fl)
       {
+        const int j = __ffs(fl) - 1;
+        fl &= fl - 1;
         W.cost = __dadd_rn(W.cost, __shfl_sync(kFull, dE, j));
         long long kc = order_key(W.cost);
         if (kc < W.klow)
@@ -761,17 +1047,15 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
   const DevModel m = a.m;
   const int Sz = m.sweep_size;
   const int nwd = (m.n_vars + 31) >> 5;
-  const bool compact = (FL == F_COUNTER) && !INT;
   const bool staged = (FL == F_PARITY || FL == F_COUNTER);
-  // per-warp region: [bars 16][tiles 2][scratch][term bytes][spins][lowest]
+  // per-warp region: [bars 16][dirty words 144][tiles 2][term bytes][spins][lowest]
   const int tile_bytes = staged ? (int)((sizeof(Tile<INT>) + 15) & ~15) : 0;
-  const int scratch_bytes = compact ? kScratch * 32 * 4 : 0;
   const int state_bytes = SMEM ? (a.p.mp + 8 * a.p.nw) : 0;
-  unsigned char* my = s_warp + (size_t)wib * (16 + 2 * tile_bytes + scratch_bytes + state_bytes);
+  unsigned char* my = s_warp + (size_t)wib * (kHdr + 2 * tile_bytes + state_bytes);
   unsigned long long* bars = (unsigned long long*)my;
-  Tile<INT>* tiles = (Tile<INT>*)(my + 16);
-  uint32_t* scratch = (uint32_t*)(my + 16 + 2 * tile_bytes);
-  unsigned char* my_state = my + 16 + 2 * tile_bytes + scratch_bytes;
+  uint32_t* dirty = (uint32_t*)(my + 16);
+  Tile<INT>* tiles = (Tile<INT>*)(my + kHdr);
+  unsigned char* my_state = my + kHdr + 2 * tile_bytes;
   if (staged && lane == 0)
   {
     mbar_init(&bars[0]);
@@ -819,11 +1103,11 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
                           a.key_base + (unsigned long long)(r % a.key_div));
     const int nblocks = (Sz + 31) >> 5;
     const int total_blocks = nblocks * a.n_sweeps;
-    int o_inc[2] = {0, 0}, o_coef[2] = {0, 0}, tq0[2] = {0, 0}, tq1[2] = {0, 0};
+    int toff[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, tq0[2] = {0, 0}, tq1[2] = {0, 0};
     if (staged && total_blocks > 0 && lane == 0)
     {
       int q0 = __ldg(m.row + 0), q1 = __ldg(m.row + min(32, Sz));
-      tile_issue<INT>(&tiles[0], &bars[0], m, q0, q1, o_inc[0], o_coef[0]);
+      tile_issue<INT>(&tiles[0], &bars[0], m, q0, q1, toff[0]);
       tq0[0] = q0;
       tq1[0] = q1;
     }
@@ -848,8 +1132,7 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
         {
           int nb = (bi + 1 < nblocks) ? bi + 1 : 0;
           int q0 = __ldg(m.row + (nb << 5)), q1 = __ldg(m.row + min((nb << 5) + 32, Sz));
-          tile_issue<INT>(&tiles[buf ^ 1], &bars[buf ^ 1], m, q0, q1, o_inc[buf ^ 1],
-                          o_coef[buf ^ 1]);
+          tile_issue<INT>(&tiles[buf ^ 1], &bars[buf ^ 1], m, q0, q1, toff[buf ^ 1]);
           tq0[buf ^ 1] = q0;
           tq1[buf ^ 1] = q1;
         }
@@ -862,22 +1145,26 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
         }
         const int t_q0 = __shfl_sync(kFull, tq0[buf], 0);
         const int t_q1 = __shfl_sync(kFull, tq1[buf], 0);
-        const int t_oi = __shfl_sync(kFull, o_inc[buf], 0);
-        const int t_oc = __shfl_sync(kFull, o_coef[buf], 0);
+        const int t_oi = __shfl_sync(kFull, toff[buf][0], 0);
+        const int t_oc = __shfl_sync(kFull, toff[buf][1], 0);
+        const int t_on = __shfl_sync(kFull, toff[buf][2], 0);
+        const int t_of = __shfl_sync(kFull, toff[buf][3], 0);
         if (t_q1 - t_q0 <= Tile<INT>::kCap)
         {
           const int v = i0 + lane;
           const int rb = (v < Sz) ? __ldg(m.row + v) : t_q0;
           const Tile<INT>* tile = &tiles[buf];
-          block_rounds<FL, REPLAY, INT, true>(S, m, W, ts, spins, lsp, scratch,
+          block_rounds<FL, REPLAY, INT, true>(S, m, W, ts, spins, lsp, dirty,
                                               tile->inc + t_oi + (rb - t_q0),
-                                              tile->coef + t_oc + (rb - t_q0), i0, Sz, nwd, beta,
-                                              nbeta_f, beta_inf, ctr0);
+                                              tile->coef + t_oc + (rb - t_q0),
+                                              tile->coef_f + t_of + (rb - t_q0),
+                                              tile->near + t_on + (rb - t_q0), i0, Sz, nwd,
+                                              beta, nbeta_f, beta_inf, ctr0);
         }
         else
-          block_rounds<FL, REPLAY, INT, false>(S, m, W, ts, spins, lsp, scratch, nullptr,
-                                               nullptr, i0, Sz, nwd, beta, nbeta_f, beta_inf,
-                                               ctr0);
+          block_rounds<FL, REPLAY, INT, false>(S, m, W, ts, spins, lsp, dirty, nullptr, nullptr,
+                                               nullptr, nullptr, i0, Sz, nwd, beta, nbeta_f,
+                                               beta_inf, ctr0);
       }
       else
         block_rounds_plain<FL, REPLAY, INT>(S, m, W, spins, lsp, i0, Sz, nwd, beta, nbeta_f,
@@ -914,10 +1201,9 @@ static const int kTableBytes = 21760;
 int warp_region_bytes(const SweepArgs& a, bool smem_state)
 {
   const bool INT = a.m.int_mode != 0;
-  const bool compact = (a.m.flavor == F_COUNTER) && !INT;
   const bool staged = (a.m.flavor == F_PARITY || a.m.flavor == F_COUNTER);
   const int tile = staged ? (int)(((INT ? sizeof(Tile<true>) : sizeof(Tile<false>)) + 15) & ~15) : 0;
-  return 16 + 2 * tile + (compact ? kScratch * 32 * 4 : 0) + (smem_state ? a.p.mp + 8 * a.p.nw : 0);
+  return kHdr + 2 * tile + (smem_state ? a.p.mp + 8 * a.p.nw : 0);
 }
 
 template <int FL, bool R, bool I, bool SM>
