@@ -318,7 +318,9 @@ __device__ __forceinline__ double exact_dE(bool part, uint32_t qm, uint32_t sm, 
 {
   double diff = 0.0;
   uint32_t q = part ? qm : 0u;
-  while (__any_sync(kFull, q != 0u))
+  const int n = (int)__reduce_max_sync(kFull, (unsigned)__popc(q));
+#pragma unroll 2
+  for (int i = 0; i < n; i++)
   {
     if (q)
     {
@@ -364,11 +366,12 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
   const int v = i0 + lane;
   const bool valid = v < Sz;
   const int nvalid = min(32, Sz - i0);
-  int rb = 0, deg = 0;
+  // rows of lanes past the end start at the block's first row (the row
+  // pointers below and the owner offsets of the apply step rely on it)
+  int rb = __ldg(m.row + (valid ? v : i0)), deg = 0;
   uint32_t sv = 0, nb = 0;
   if (valid)
   {
-    rb = __ldg(m.row + v);
     deg = __ldg(m.row + v + 1) - rb;
     sv = spin_of(spins, v);
     nb = __ldg(m.nbr + v);
@@ -499,11 +502,11 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
   __syncwarp();
 
   int cursor = 0;
-  bool first = true;
+  bool pending = false;  // the last round flipped something: marks may be set
   while (cursor < nvalid)
   {
     const bool active = valid && lane >= cursor;
-    if (!first)
+    if (pending)
     {
       const uint32_t all = dirty[32];
       const uint32_t dm = dirty[lane];
@@ -517,7 +520,6 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
       if (lane == 0 && all) dirty[32] = 0u;
       __syncwarp();
     }
-    first = false;
 
     // ---- cost difference: exact where known, screened otherwise --------
     long long idE = 0;
@@ -720,25 +722,52 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     const int adv = f + (slow ? 1 : 0) - cursor;
     const bool mine = ((flips >> lane) & 1u) != 0u;
 
-    // ---- apply: term bytes by atomics, marks for later co-members ------
-    if (mine)
+    // ---- apply: the flips' incidences spread over the warp; term bytes
+    // change by atomics (different terms may share a word), and each
+    // incidence marks the later co-members of its term ----------------------
+    pending = flips != 0u;
+    if (pending)
     {
-      for (int k = 0; k < deg; k++)
+      const int mydeg = mine ? deg : 0;
+      const int incl = warp_scan32(mydeg, lane);
+      const int excl = incl - mydeg;
+      const int total = __shfl_sync(kFull, incl, 31);
+      for (int base = 0; base < total; base += 32)
       {
-        const uint32_t e = INC(k);
-        const unsigned long long nw = NEAR(k);
-        const uint32_t t = e & ~kNegBit;
-        const unsigned sh = (t & 3u) << 3;
-        if (FL == F_PARITY) atomicXor(ts32 + (t >> 2), 1u << sh);
-        else atomicAdd(ts32 + (t >> 2), ((sv ^ (e >> 31)) & 1u) ? (0u - (1u << sh)) : (1u << sh));
-        const int cnt = (int)(nw >> 61);
-        if (cnt == 7) atomicOr(dirty + 32, 1u);
-        else
-          for (int i = 0; i < cnt; i++)
-          {
-            const int u = lane + (int)((nw >> (10 * i)) & 31u);
-            if (u < 32) atomicOr(dirty + u, 1u << (unsigned)((nw >> (10 * i + 5)) & 31u));
-          }
+        // start positions of the flips' runs inside this chunk
+        const int rel = excl - base;
+        const unsigned starts = __reduce_or_sync(kFull, (mine && mydeg > 0 && rel >= 0 && rel < 32) ? (1u << rel) : 0u);
+        const int nbefore = __popc(__ballot_sync(kFull, mine && mydeg > 0 && rel < 0));
+        const int g = base + lane;
+        const int idx = nbefore + __popc(starts & ((2u << lane) - 1u)) - 1;
+        // idx-th flipping lane with a non-empty row
+        const unsigned F = __ballot_sync(kFull, mine && mydeg > 0);
+        // smallest j with popc(F & bits 0..j) > idx
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1)
+          if (__popc(F & ((2u << (j + step - 1)) - 1u)) <= idx) j += step;
+        const int ej = __shfl_sync(kFull, excl, j & 31);
+        const int rj = __shfl_sync(kFull, rb, j & 31);
+        const uint32_t svj = __shfl_sync(kFull, sv, j & 31);
+        if (g < total)
+        {
+          const int k = g - ej + (rj - rb);  // position relative to this lane's row
+          const uint32_t e = INC(k);
+          const unsigned long long nw = NEAR(k);
+          const uint32_t t = e & ~kNegBit;
+          const unsigned sh = (t & 3u) << 3;
+          if (FL == F_PARITY) atomicXor(ts32 + (t >> 2), 1u << sh);
+          else atomicAdd(ts32 + (t >> 2), ((svj ^ (e >> 31)) & 1u) ? (0u - (1u << sh)) : (1u << sh));
+          const int cnt = (int)(nw >> 61);
+          if (cnt == 7) atomicOr(dirty + 32, 1u);
+          else
+            for (int i = 0; i < cnt; i++)
+            {
+              const int u = j + (int)((nw >> (10 * i)) & 31u);
+              if (u < 32) atomicOr(dirty + u, 1u << (unsigned)((nw >> (10 * i + 5)) & 31u));
+            }
+        }
       }
     }
     const int wi = i0 >> 5;
@@ -751,14 +780,21 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
       {
         if (m.scan32)
         {
-          const int pre = warp_scan32(mine ? (int)idE : 0, lane);
-          const int mn = __reduce_min_sync(kFull, mine ? pre : INT_MAX);
-          if ((long long)mn < W.ilow - W.icost)
+          const int d = mine ? (int)idE : 0;
+          const int dsum = __reduce_add_sync(kFull, d);
+          const int negsum = __reduce_add_sync(kFull, d < 0 ? d : 0);
+          // the lowest prefix cost is at least icost + negsum
+          if ((long long)negsum < W.ilow - W.icost)
           {
-            lowpos = __ffs(__ballot_sync(kFull, mine && pre == mn)) - 1;
-            W.ilow = W.icost + mn;
+            const int pre = warp_scan32(d, lane);
+            const int mn = __reduce_min_sync(kFull, mine ? pre : INT_MAX);
+            if ((long long)mn < W.ilow - W.icost)
+            {
+              lowpos = __ffs(__ballot_sync(kFull, mine && pre == mn)) - 1;
+              W.ilow = W.icost + mn;
+            }
           }
-          W.icost += __shfl_sync(kFull, pre, 31);
+          W.icost += dsum;
         }
         else
         {
@@ -779,17 +815,27 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     else
     {
       unsigned fl = flips;
-      while (fl)
+      if (fl)
       {
-        const int j = __ffs(fl) - 1;
+        int j = __ffs(fl) - 1;
         fl &= fl - 1;
-        W.cost = __dadd_rn(W.cost, __shfl_sync(kFull, dE, j));
-        long long kc = order_key(W.cost);
-        if (kc < W.klow)
+        double d = __shfl_sync(kFull, dE, j);
+        while (true)
         {
-          W.klow = kc;
-          W.low = W.cost;
-          lowpos = j;
+          const int jn = fl ? (__ffs(fl) - 1) : j;
+          const double dn = __shfl_sync(kFull, dE, jn);  // ahead of the dependent add
+          W.cost = __dadd_rn(W.cost, d);
+          const long long kc = order_key(W.cost);
+          if (kc < W.klow)
+          {
+            W.klow = kc;
+            W.low = W.cost;
+            lowpos = j;
+          }
+          if (!fl) break;
+          fl &= fl - 1;
+          j = jn;
+          d = dn;
         }
       }
     }
