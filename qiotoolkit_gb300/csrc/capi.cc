@@ -149,10 +149,12 @@ qio_status qio_states_cost(const qio_model* model, int64_t n, const uint8_t* sta
     std::vector<uint32_t> words;
     int nw;
     pack_states(m, n, states, words, nw);
-    DevBuf d(words.size() * 4 + (size_t)n * 8);
+    // the costs start on a 256-byte boundary after the packed words
+    size_t wb = (words.size() * 4 + 255) & ~(size_t)255;
+    DevBuf d(wb + (size_t)n * 8);
     cudaStream_t s = as_stream(stream);
     cuda_check(cudaMemcpyAsync(d.ptr, words.data(), words.size() * 4, cudaMemcpyHostToDevice, s), "H2D");
-    double* out = (double*)((char*)d.ptr + words.size() * 4);
+    double* out = (double*)((char*)d.ptr + wb);
     cuda_check(launch_eval_cost(m.device(), (int)n, (const uint32_t*)d.ptr, nw, out, s), "cost kernel");
     cuda_check(cudaMemcpyAsync(costs, out, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H");
     cuda_check(cudaStreamSynchronize(s), "sync");

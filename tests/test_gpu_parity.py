@@ -52,10 +52,12 @@ def test_state_contract(name):
     off, ids, coef = gen()
     g, o = both(kind, off, ids, coef)
     rng = np.random.default_rng(1)
-    S = rng.integers(0, 2, (16, g.n_vars)).astype(np.uint8)
+    # an odd number of states: the packed words need not end on an 8-byte
+    # boundary, the costs after them must still be aligned
+    S = rng.integers(0, 2, (17, g.n_vars)).astype(np.uint8)
     costs = g.calculate_cost(S)
     assert [o.cost(s) for s in S] == list(costs)
-    vars_ = rng.integers(0, g.n_vars, 16)
+    vars_ = rng.integers(0, g.n_vars, 17)
     diffs = g.calculate_cost_difference(S, vars_)
     assert [o.cost_difference(s, v) for s, v in zip(S, vars_)] == list(diffs)
     # apply + recompute is consistent with the difference
