@@ -123,6 +123,21 @@ qio_status qio_model_destroy(qio_model* model);
  * in the reference's term order, so results are bit-identical to it. */
 qio_status qio_states_cost(const qio_model* model, int64_t n_states,
                            const uint8_t* states, double* costs, void* stream);
+/* calculate_cost for n_states states that are already in device memory
+ * (states: n_states x n_vars bytes, costs: n_states doubles, both device
+ * pointers), with no allocation: no counterpart in the reference.  For
+ * callers that must not allocate device memory during a call (a serving
+ * loop whose HBM is held by resident solves; a thread that cannot take the
+ * device-wide synchronisation of cudaMalloc/cudaFree).  Scratch is a fixed
+ * 1 MiB array inside the library: n_states * ceil(n_vars / 32) must not
+ * exceed 262144 words (QIO_INVALID_ARGUMENT otherwise).  All calls share it:
+ * overlapping calls (other streams or threads) race and must be serialised
+ * by the caller.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  The model must already be on the
+ * current device (an earlier qio_states_cost or solver call).  Results equal
+ * qio_states_cost's; the call is asynchronous on `stream`. */
+qio_status qio_states_cost_noalloc(const qio_model* model, int64_t n_states,
+                                   const uint8_t* states, double* costs, void* stream);
 /* calculate_cost_difference(state q, vars[q]) for n queries. */
 qio_status qio_states_cost_difference(const qio_model* model, int64_t n,
                                       const uint8_t* states,

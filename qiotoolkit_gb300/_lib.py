@@ -58,6 +58,7 @@ def _signatures():
         "qio_model_get_var_names": (st, [vp, P(C.c_int32)]),
         "qio_model_destroy": (st, [vp]),
         "qio_states_cost": (st, [vp, i64, P(C.c_uint8), P(dbl), vp]),
+        "qio_states_cost_noalloc": (st, [vp, i64, vp, vp, vp]),
         "qio_states_cost_difference": (st, [vp, i64, P(C.c_uint8), P(i64), P(dbl), vp]),
         "qio_states_apply": (st, [vp, i64, P(C.c_uint8), P(i64)]),
         "qio_solver_create": (st, [vp, cp, cp, P(vp)]),

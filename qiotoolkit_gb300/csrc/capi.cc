@@ -161,6 +161,40 @@ qio_status qio_states_cost(const qio_model* model, int64_t n, const uint8_t* sta
   });
 }
 
+// Allocation-free cost of device-resident states: the scratch lives in a
+// fixed array of the library (kernels.cu), so this call allocates nothing and
+// does not set up the device or upload the model; the model must already be
+// on the current device from an earlier GPU call (qio_states_cost, a solver).
+// Asynchronous: the costs are ready once the stream reaches this point.
+qio_status qio_states_cost_noalloc(const qio_model* model, int64_t n, const uint8_t* states,
+                                   double* costs, void* stream)
+{
+  return guard([&] {
+    if (!model || (n > 0 && (!states || !costs))) fail(1, "arguments must not be null");
+    const HostModel& m = *model->m;
+    if (n <= 0) return;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+      fail(5, "no CUDA device available: the GB300 library has no CPU fallback");
+    cudaStream_t s = as_stream(stream);
+    if (m.empty())
+    {
+      cuda_check(cudaMemsetAsync(costs, 0, (size_t)n * 8, s), "cudaMemsetAsync");
+      return;
+    }
+    if (!m.uploaded)
+      fail(1, "qio_states_cost_noalloc: the model is not on the device yet; run it on the GPU "
+              "once (qio_states_cost or a solver) before the allocation-free call");
+    const int64_t nw = m.N > 0 ? (m.N + 31) / 32 : 1;
+    if (n > INT32_MAX || n * nw > (int64_t)kNoAllocScratchWords)
+      fail(1, "qio_states_cost_noalloc: " + std::to_string(n) + " states of " + std::to_string(m.N) +
+                  " variables need " + std::to_string(n * nw) + " scratch words; the maximum is " +
+                  std::to_string(kNoAllocScratchWords) + " (1 MiB)");
+    cuda_check(launch_eval_cost_noalloc(m.dev, (int)n, states, (int)m.N, (int)nw, costs, s),
+               "allocation-free cost kernel");
+  });
+}
+
 qio_status qio_states_cost_difference(const qio_model* model, int64_t n, const uint8_t* states,
                                       const int64_t* vars, double* diffs, void* stream)
 {

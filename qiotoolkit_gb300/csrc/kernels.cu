@@ -13,6 +13,7 @@
 // the committed prefix consumes exactly the draws the sequential chain would.
 // The result is the reference's trajectory, evaluated up to 32-wide.
 #include <cstdio>
+#include <mutex>
 
 #include "qio_internal.h"
 
@@ -618,6 +619,92 @@ cudaError_t launch_pt_swap(const SwapArgs& a, cudaStream_t s)
   int threads = 64;
   int blocks = (a.restarts + threads - 1) / threads;
   pt_swap_kernel<<<blocks, threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free cost evaluation.  Callers that must not allocate device
+// memory while they run -- a serving loop that has handed the free HBM to
+// resident solves, or a host thread that cannot afford the device-wide
+// synchronisation cudaMalloc / cudaFree bring -- evaluate the cost of states
+// that already sit on the device here.  The packed spin words, the only
+// scratch the cost kernel needs, go to the fixed file-scope array below
+// instead of a buffer allocated per call.
+//
+// Limits and sharing: the array holds kNoAllocScratchWords 32-bit words
+// (1 MiB); a call needs n_states * ceil(n_vars / 32) words, and the entry
+// point rejects larger requests before launching.  Every word a call uses
+// is written before it is read, so nothing in the array has to start at
+// zero.  All calls on one device share the array: calls that overlap in
+// time (different streams or host threads) race on it and must be
+// serialised by the caller.  The first call on each device looks up the
+// array's device address (cudaGetSymbolAddress) with that device current;
+// make that first call before any stream capture.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords];
+
+template <int FL, bool INT>
+__global__ void eval_cost_noalloc_kernel(DevModel m, int n, const uint8_t* states, int n_vars,
+                                         int nw, uint32_t* scratch, double* out)
+{
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n) return;
+  // pack this state's bytes into its own scratch words (coalesced reads)
+  const uint8_t* st = states + (size_t)w * n_vars;
+  uint32_t* sp = scratch + (size_t)w * nw;
+  for (int q = 0; q < nw; q++)
+  {
+    const int v = q * 32 + lane;
+    const unsigned word = __ballot_sync(kFull, v < n_vars && st[v] != 0);
+    if (lane == 0) sp[q] = word;
+  }
+  __syncwarp();
+  double c;
+  long long ic;
+  warp_cost<FL, INT>(m, sp, lane, c, ic);
+  if (lane == 0) out[w] = INT ? (double)ic : c;
+}
+
+template <int FL, bool I>
+static void cost_noalloc_dispatch(const DevModel& m, int n, const uint8_t* st, int n_vars, int nw,
+                                  uint32_t* scratch, double* out, cudaStream_t s)
+{
+  int blocks = (n + 3) / 4;
+  if (blocks > 0) eval_cost_noalloc_kernel<FL, I><<<blocks, 128, 0, s>>>(m, n, st, n_vars, nw, scratch, out);
+}
+
+cudaError_t launch_eval_cost_noalloc(const DevModel& m, int n, const uint8_t* states, int n_vars,
+                                     int nw, double* out, cudaStream_t s)
+{
+  if ((long long)n * (long long)nw > (long long)kNoAllocScratchWords) return cudaErrorInvalidValue;
+  // set-up once per device, with that device current: the array's address
+  static std::mutex mu;
+  static uint32_t* addr[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  uint32_t* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (!addr[dev])
+    {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) return e;
+      addr[dev] = (uint32_t*)p;
+    }
+    scratch = addr[dev];
+  }
+  const bool I = m.int_mode != 0;
+  switch (m.flavor)
+  {
+    case F_PARITY: I ? cost_noalloc_dispatch<F_PARITY, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_PARITY, false>(m, n, states, n_vars, nw, scratch, out, s); break;
+    case F_COUNTER: I ? cost_noalloc_dispatch<F_COUNTER, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_COUNTER, false>(m, n, states, n_vars, nw, scratch, out, s); break;
+    case F_PLAIN_ISING: I ? cost_noalloc_dispatch<F_PLAIN_ISING, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_PLAIN_ISING, false>(m, n, states, n_vars, nw, scratch, out, s); break;
+    default: I ? cost_noalloc_dispatch<F_PLAIN_PUBO, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_PLAIN_PUBO, false>(m, n, states, n_vars, nw, scratch, out, s); break;
+  }
   return cudaGetLastError();
 }
 }  // namespace qio

@@ -126,6 +126,12 @@ cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int warps_per_block
 cudaError_t launch_eval_cost(const DevModel& m, int n_states,
                              const uint32_t* spins, int nw, double* out,
                              cudaStream_t s);
+// Allocation-free variant: states are n x n_vars bytes on the device, packed
+// into a fixed file-scope scratch array of kNoAllocScratchWords words.
+static const int kNoAllocScratchWords = 1 << 18;
+static const int kMaxDevices = 64;
+cudaError_t launch_eval_cost_noalloc(const DevModel& m, int n, const uint8_t* states, int n_vars,
+                                     int nw, double* out, cudaStream_t s);
 cudaError_t launch_eval_diff(const DevModel& m, int n, const uint32_t* spins,
                              int nw, const long long* vars, double* out,
                              cudaStream_t s);
