@@ -139,47 +139,57 @@ def committed_traffic(workload):
         return None
 
 
-def cpu_baseline(kind, off, ids, coef, params, budget_s=12.0):
+def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
     """The oracle (CPU restatement of the reference) on a bounded sample of
-    the same workload, all host threads (OpenMP over replicas)."""
+    the same workload: the full workload when it fits the time budget, else
+    fewer sweeps (then fewer restarts / a smaller population).  `threads`
+    host threads (OpenMP over replicas, as the reference); default all."""
     from oracle import oracle as O
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     m = O.Model(kind, off=off, ids=ids, coef=coef)
     n = m.n_vars
 
-    def run(sweeps):
+    def run(restarts, sweeps):
+        t0 = time.perf_counter()
         if "temperatures" in params:
             t = params["temperatures"]
-            kw = dict(sched=(t["type"], t["initial"], t["final"]), sched_count=t["count"],
-                      use_inverse=False)
-            t0 = time.perf_counter()
-            O.run(m, "pt", seed=0, step_limit=sweeps, threads=threads, **kw)
-            dt = time.perf_counter() - t0
-            return t["count"] * sweeps * n, dt, f"1 restart x {t['count']} replicas x {sweeps} sweeps"
-        if "population" in params:
-            pop = min(params["population"], 256)
-            t0 = time.perf_counter()
-            O.run(m, "pa", seed=0, step_limit=sweeps, population=pop, pa_threads=threads,
+            O.run(m, "pt", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
+                  sched=(t["type"], t["initial"], t["final"]), sched_count=t["count"],
+                  use_inverse=False)
+            a = restarts * t["count"] * sweeps * n
+            d = f"{restarts} restarts x {t['count']} replicas x {sweeps} sweeps"
+        elif "population" in params:
+            O.run(m, "pa", seed=0, step_limit=sweeps, population=restarts, pa_threads=threads,
                   threads=threads, sched=("linear", params["beta_start"], params["beta_stop"]),
-                  sweeps_per_replica=params["sweeps_per_replica"])
-            dt = time.perf_counter() - t0
-            return pop * sweeps * params["sweeps_per_replica"] * n, dt, \
-                f"population {pop} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
-        R = params["restarts"]
-        t0 = time.perf_counter()
-        O.run(m, "sa", seed=0, step_limit=sweeps, restarts=R, threads=threads,
-              sched=("linear", params["beta_start"], params["beta_stop"]))
-        dt = time.perf_counter() - t0
-        return R * sweeps * n, dt, f"{R} restarts x {sweeps} sweeps"
+                  sweeps_per_replica=params["sweeps_per_replica"], rng_mode="counter")
+            a = restarts * sweeps * params["sweeps_per_replica"] * n
+            d = f"population {restarts} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
+        else:
+            O.run(m, "sa", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
+                  sched=("linear", params["beta_start"], params["beta_stop"]))
+            a = restarts * sweeps * n
+            d = f"{restarts} restarts x {sweeps} sweeps"
+        return a, time.perf_counter() - t0, d
 
-    a, dt, _ = run(4)
-    rate = a / max(dt, 1e-6)
-    per_sweep = a / 4
-    sweeps = max(4, int(budget_s * rate / per_sweep))
-    sweeps = min(sweeps, params.get("sweeps", sweeps))
-    a, dt, desc = run(sweeps)
+    full_r = params.get("restarts", params.get("population", 1))
+    full_s = params["sweeps"]
+    # the parallel dimension first (replicas keep the cores busy), then sweeps
+    r0 = min(full_r, max(threads, 1)) if "temperatures" not in params else 1
+    restarts, sweeps = r0, min(full_s, 4)
+    a, dt, desc = run(restarts, sweeps)
+    per = a / (restarts * sweeps)  # attempts per (restart, sweep)
+    for _ in range(3):  # grow the sample until it fills about half the budget
+        full = restarts == full_r and sweeps == full_s
+        if full or dt >= 0.5 * budget_s:
+            break
+        want = budget_s * a / max(dt, 1e-6)
+        sweeps = min(full_s, max(sweeps, int(want / (per * restarts))))
+        restarts = min(full_r, max(restarts, int(want / (per * sweeps))))
+        a, dt, desc = run(restarts, sweeps)
+    full = restarts == full_r and sweeps == full_s
     return {"value": a / dt, "unit": "flip attempts/s", "cores": threads, "kind": "port",
-            "sample": f"oracle (C++ restatement) {desc}, {a:.3g} attempts in {dt:.2f} s"}
+            "sample": f"oracle (C++ restatement, OpenMP over replicas) {desc}"
+                      f"{' (the full workload)' if full else ''}, {a:.3g} attempts in {dt:.2f} s"}
 
 
 def dist_setup():
@@ -320,6 +330,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(kind, off, ids, coef, params)
+        one = cpu_baseline(kind, off, ids, coef, params, budget_s=8.0, threads=1)
+        cpu["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
 
     if rank == 0:
         line = {
