@@ -152,12 +152,15 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
     def run(restarts, sweeps):
         t0 = time.perf_counter()
         if "temperatures" in params:
+            # one reference run per restart (restart k is the run seeded k),
+            # each parallel over its replicas
             t = params["temperatures"]
-            O.run(m, "pt", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
-                  sched=(t["type"], t["initial"], t["final"]), sched_count=t["count"],
-                  use_inverse=False)
+            for k in range(restarts):
+                O.run(m, "pt", seed=k, step_limit=sweeps, threads=threads,
+                      sched=(t["type"], t["initial"], t["final"]), sched_count=t["count"],
+                      use_inverse=False)
             a = restarts * t["count"] * sweeps * n
-            d = f"{restarts} restarts x {t['count']} replicas x {sweeps} sweeps"
+            d = f"{restarts} runs (seeds 0..{restarts - 1}) x {t['count']} replicas x {sweeps} sweeps"
         elif "population" in params:
             O.run(m, "pa", seed=0, step_limit=sweeps, population=restarts, pa_threads=threads,
                   threads=threads, sched=("linear", params["beta_start"], params["beta_stop"]),
@@ -255,6 +258,8 @@ def main():
     ap.add_argument("--workload", default="pt_pubo", choices=list(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--sweeps", type=int, default=None,
+                    help="override the workload's sweeps (small cases for profiler captures)")
     args = ap.parse_args()
     ws, rank = dist_setup()
     if args.impl == "reference":
@@ -267,6 +272,8 @@ def main():
     torch.cuda.set_device(local)
     q.load()
     kind, off, ids, coef, params = make_workload(args.workload)
+    if args.sweeps:
+        params["sweeps"] = args.sweeps
     target = WORKLOADS[args.workload]["target"]
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
