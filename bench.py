@@ -130,13 +130,17 @@ def peaks():
 
 
 def committed_traffic(workload):
-    """dram bytes per sweep launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"sweep_{workload}_traffic.json")
+    """dram bytes per sweep launch from the committed ncu summary, if any
+    (the `dram_bytes_per_launch:` line of profiles/sweep_<workload>_ncu.md)."""
+    path = os.path.join(ROOT, "profiles", f"sweep_{workload}_ncu.md")
     try:
         with open(path) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
     except (OSError, ValueError):
         return None
+    return None
 
 
 def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
