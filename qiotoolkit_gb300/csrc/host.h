@@ -57,6 +57,10 @@ struct HostModel
   std::vector<float> coef_f;
   std::vector<unsigned long long> near;
   bool fscreen = true, scan32 = false;
+  // Ising models whose terms all have one or two members: the other member
+  // of each incidence (-1 for a one-member term)
+  bool pair_only = false;
+  std::vector<int> other;
   std::vector<uint32_t> nbr;
   // term -> members
   std::vector<int> trow;
@@ -154,6 +158,7 @@ class Solver
   bool initialized = false, ran = false;
   bool profile = false;  // bracket every sweep launch with CUDA events
   bool smem_state = true;  // walker state in shared memory when it fits
+  int kernel = 0;          // sweep kernel: 0 auto, 1 one walker per warp, 2 one walker per lane
   // CUDA-event pairs around sweep launches (profile mode)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   size_t prof_used = 0;

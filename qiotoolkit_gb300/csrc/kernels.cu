@@ -546,6 +546,7 @@ void upload_tables(int)
       e[2] = (float)(ldexp(fabs(y0) + fabs(dy), -19));
     }
   sw_upload(ln, scr, jA, jC);
+  lw_upload(ln, scr);
 }
 
 template <int FL, bool INT>

@@ -1,0 +1,402 @@
+// lanes.cu -- lane-per-walker Metropolis sweeps for Ising models whose terms
+// have one or two members (lattices, sparse graphs with fields).
+//
+// Each thread runs one walker's sweeps exactly as the reference's ordered
+// sweep does (markov/walker.h:143-153,209-229): variable by variable, the
+// cost difference summed over the incident terms in ascending term order
+// (model/ising.h:108-117), the Metropolis decision (markov/metropolis.h:
+// 64-104) on the walker's own stream, the flip, cost += diff and the lowest
+// check.  The 32 walkers of a warp form a group whose spins are stored
+// bit-packed and interleaved: word w (spins 32w .. 32w+31) of lane l at
+// group word w*32 + l, so the warp's accesses to one word index are one
+// 128-byte line, and the row loads of a model are shared by the lanes that
+// run it.
+//
+// Term parity from spins: with at most two members, the cached term bit of
+// IsingTermCached is the XOR of the variable's own spin and the other
+// member's spin (or the own spin alone), so the state is the spins alone
+// and a flip is one word update.
+//
+// Lowest state: the reference copies the spins whenever the cost drops below
+// the lowest (markov/walker.h:269-280).  Here a new lowest only records that
+// the current state is the lowest; later flips are logged, and the lowest
+// spins are written out (current words with the logged flips undone) when
+// the log fills or the launch ends -- the same state, fewer copies.  The
+// Metropolis tables sit in shared memory: lanes look up different buckets.
+#include <algorithm>
+
+#include "metropolis.cuh"
+#include "qio_internal.h"
+
+namespace qio
+{
+namespace lw
+{
+using namespace qio::mc;
+static const unsigned long long kMult = 6364136223846793005ULL;
+static const unsigned long long kInc = 1442695040888963407ULL;
+
+__constant__ double c_ln[1024];
+__constant__ float c_scr[1024 * 3];
+
+// Metropolis decision for an uphill move with threshold dE * (-beta):
+// FP32 screen first, the exact FP64 expression inside its margin.
+__device__ __forceinline__ bool lut_accept(const double* ln, const float* scr, uint32_t r, int row,
+                                           double dE, double beta, float nbeta_f)
+{
+  const float thr_f = __fmul_rn(approx_float(dE), nbeta_f);
+  const int d = lut_screen(scr, r, row, thr_f);
+  if (d >= 0) return d == 1;
+  return lut_less_exact(ln, r, row, __dmul_rn(dE, -beta));
+}
+
+// SMEM: the group's current spin words live in shared memory for the launch
+// (copied in at the start, out at the end); the lowest words stay in global
+// memory.  Tables in the block's first 20 KB, group words after them.
+template <bool REPLAY, bool INT, bool SMEM>
+__global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
+{
+  extern __shared__ __align__(16) unsigned char lw_smem[];
+  double* s_ln = (double*)lw_smem;
+  float* s_scr = (float*)(lw_smem + 8192);
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) s_ln[t] = c_ln[t];
+  for (int t = threadIdx.x; t < 3072; t += blockDim.x) s_scr[t] = c_scr[t];
+  __syncthreads();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.n_walkers) return;  // no warp-wide operations below
+  const int lane = threadIdx.x & 31;
+  const int g = r >> 5;
+  const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
+  const int* __restrict__ row = md->row;
+  const int* __restrict__ oth = md->other;
+  const double* __restrict__ coef = md->coef;
+  const int* __restrict__ coef_i = md->coef_i;
+  const int Sz = md->sweep_size;
+  const int nwd = (md->n_vars + 31) >> 5;
+  const int gw = a.g_nw[g];
+  uint32_t* base = (uint32_t*)(a.arena + a.g_off[g]);
+  uint32_t* gsp = base + lane;              // word w at gsp[w * 32]
+  uint32_t* lsp = base + (size_t)gw * 32 + lane;
+  uint32_t* lg = base + (size_t)gw * 64 + lane;
+  uint32_t* sp = gsp;
+  if (SMEM)
+  {
+    sp = (uint32_t*)(lw_smem + 20480) + (size_t)(threadIdx.x >> 5) * smem_words * 32 + lane;
+    for (int w = 0; w < nwd; w++) sp[(size_t)w * 32] = gsp[(size_t)w * 32];
+  }
+
+  const int slot = a.slot_of ? a.slot_of[r] : r;
+  double cost = a.p.cost[slot], low = a.p.lowest[r];
+  long long icost = INT ? (long long)cost : 0, ilow = INT ? (long long)low : 0;
+  long long klow = order_key(low);
+  uint64_t rs = REPLAY ? a.rng[r] : 0;
+  uint64_t key = 0;
+  if (!REPLAY)
+    key = counter_key(a.seed + (uint32_t)(r / a.key_div), a.key_base + (unsigned long long)(r % a.key_div));
+  unsigned long long natt = 0, nacc = 0;
+  bool pend = false;  // the lowest is the current state with the logged flips undone
+  int nlog = 0;
+  auto write_lowest = [&]() {
+    for (int w = 0; w < nwd; w++) lsp[(size_t)w * 32] = sp[(size_t)w * 32];
+    for (int i = 0; i < nlog; i++)
+    {
+      const uint32_t v = lg[(size_t)i * 32];
+      lsp[(size_t)(v >> 5) * 32] ^= 1u << (v & 31);
+    }
+    pend = false;
+    nlog = 0;
+  };
+
+  for (int k = 0; k < a.n_sweeps; k++)
+  {
+    const long long swp = a.sweep_base + k;
+    const double beta = a.beta[(long long)r * a.bs_w + swp * a.bs_s];
+    const bool beta_inf =
+        ((unsigned long long)__double_as_longlong(beta) & 0x7FFFFFFFFFFFFFFFULL) == 0x7FF0000000000000ULL;
+    const float nbeta_f = -approx_float(beta);
+    const unsigned long long ctr0 = (unsigned long long)swp * (unsigned long long)Sz;
+    int q = __ldg(row);
+    uint32_t cw = 0;  // current word of v
+    for (int v = 0; v < Sz; v++)
+    {
+      const int qe = __ldg(row + v + 1);
+      if ((v & 31) == 0) cw = sp[(size_t)(v >> 5) * 32];
+      const uint32_t sv = (cw >> (v & 31)) & 1u;
+      long long idE = 0;
+      double dE = 0.0;
+      {
+        int iacc = 0;
+        double diff = 0.0;
+        for (; q < qe; q++)
+        {
+          const int u = __ldg(oth + q);
+          uint32_t su = 0;
+          if (u >= 0)
+          {
+            const uint32_t wu = ((u >> 5) == (v >> 5)) ? cw : sp[(size_t)(u >> 5) * 32];
+            su = (wu >> (u & 31)) & 1u;
+          }
+          const uint32_t z = sv ^ su;
+          if (INT)
+          {
+            const int c = __ldg(coef_i + q);
+            iacc += z ? -c : c;
+          }
+          else
+          {
+            const double c = __ldg(coef + q);
+            diff = __dadd_rn(diff, z ? -c : c);
+          }
+        }
+        if (INT) idE = -2LL * (long long)iacc;
+        else dE = neg2x(diff);
+      }
+      natt++;
+      bool acc;
+      if (INT ? idE <= 0 : le_zero(dE)) acc = true;
+      else
+      {
+        int rw = -1, b = 0;
+        uint32_t cur = 0;
+        bool all_zero = false;
+        if (REPLAY)
+        {
+          while (b == 0)
+          {
+            if (rw < 3)
+            {
+              cur = pcg_out(rs);
+              rs = rs * kMult + kInc;
+              b = (int)(cur & 255u);
+              rw++;
+            }
+            else
+            {
+              all_zero = true;
+              break;
+            }
+          }
+        }
+        else
+        {
+          const unsigned long long ctr = ctr0 + (unsigned long long)v;
+          const uint64_t w0 = counter_draw(key, 2ULL * ctr);
+          int used = 0;
+          while (b == 0)
+          {
+            if (rw < 3)
+            {
+              if (used == 0) cur = (uint32_t)w0;
+              else if (used == 1) cur = (uint32_t)(w0 >> 32);
+              else
+              {
+                const uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
+                cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+              }
+              used++;
+              b = (int)(cur & 255u);
+              rw++;
+            }
+            else
+            {
+              all_zero = true;
+              break;
+            }
+          }
+        }
+        if (all_zero) acc = true;
+        else if (beta_inf) acc = false;
+        else acc = lut_accept(s_ln, s_scr, cur, rw, INT ? (double)idE : dE, beta, nbeta_f);
+      }
+      if (acc)
+      {
+        nacc++;
+        cw ^= 1u << (v & 31);
+        sp[(size_t)(v >> 5) * 32] = cw;
+        bool newlow;
+        if (INT)
+        {
+          icost += idE;
+          newlow = icost < ilow;
+          if (newlow) ilow = icost;
+        }
+        else
+        {
+          cost = __dadd_rn(cost, dE);
+          const long long kc = order_key(cost);
+          newlow = kc < klow;
+          if (newlow)
+          {
+            klow = kc;
+            low = cost;
+          }
+        }
+        if (newlow)
+        {
+          pend = true;
+          nlog = 0;
+        }
+        else if (pend)
+        {
+          if (nlog == kLwLog)
+          {
+            // the log is full: write the lowest out, this flip excluded
+            write_lowest();
+            lsp[(size_t)(v >> 5) * 32] ^= 1u << (v & 31);
+          }
+          else
+          {
+            lg[(size_t)nlog * 32] = (uint32_t)v;
+            nlog++;
+          }
+        }
+      }
+    }
+  }
+  if (pend) write_lowest();
+  if (SMEM)
+    for (int w = 0; w < nwd; w++) gsp[(size_t)w * 32] = sp[(size_t)w * 32];
+  a.p.cost[slot] = INT ? (double)icost : cost;
+  a.p.lowest[r] = INT ? (double)ilow : low;
+  a.p.attempts[r] += natt;
+  a.p.accepts[r] += nacc;
+  a.p.step_att[r] += natt;
+  a.p.step_acc[r] += nacc;
+  if (a.p.windows) a.p.windows[r] += natt;
+  if (REPLAY) a.rng[r] = rs;
+}
+
+// Population (bit-packed spins per slot, lowest spins per walker) <-> group
+// words.  Thread (g, lane) of block (g, word block) moves words of walker
+// g*32 + lane; a warp's accesses to one word index are one line.
+template <bool LOAD>
+__global__ void lw_move_kernel(LwArgs a, int words_per_block)
+{
+  const int g = blockIdx.x, lane = threadIdx.x;
+  const int r = g * 32 + lane;
+  if (r >= a.n_walkers) return;
+  const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
+  const int nwd = (md->n_vars + 31) >> 5;
+  const int slot = a.slot_of ? a.slot_of[r] : r;
+  const int gw = a.g_nw[g];
+  uint32_t* base = (uint32_t*)(a.arena + a.g_off[g]);
+  const int q0 = blockIdx.y * words_per_block, q1 = min(nwd, q0 + words_per_block);
+  for (int q = q0; q < q1; q++)
+  {
+    uint32_t* sp = base + (size_t)q * 32 + lane;
+    uint32_t* lsp = base + (size_t)(gw + q) * 32 + lane;
+    uint32_t* ps = a.p.spins + (size_t)slot * a.p.nw + q;
+    uint32_t* pl = a.p.lspins + (size_t)r * a.p.nw + q;
+    if (LOAD)
+    {
+      *sp = *ps;
+      *lsp = *pl;
+    }
+    else
+    {
+      *ps = *sp;
+      *pl = *lsp;
+    }
+  }
+}
+
+// term parity bytes of the population from its spins (IsingTermCachedState),
+// one thread per (walker, term) pair, grid-stride
+__global__ void lw_terms_kernel(LwArgs a, int max_terms)
+{
+  const long long total = (long long)a.n_walkers * max_terms;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x)
+  {
+    const int r = (int)(i / max_terms);
+    const int t = (int)(i - (long long)r * max_terms);
+    const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
+    if (t >= md->n_terms) continue;
+    const int slot = a.slot_of ? a.slot_of[r] : r;
+    const uint32_t* s = a.p.spins + (size_t)slot * a.p.nw;
+    uint32_t par = 0;
+    for (int k = md->trow[t]; k < md->trow[t + 1]; k++)
+    {
+      const uint32_t x = md->tvar[k] & ~kNegBit;
+      par ^= (s[x >> 5] >> (x & 31)) & 1u;
+    }
+    a.p.tstate[(size_t)slot * a.p.mp + t] = (uint8_t)par;
+  }
+}
+}  // namespace lw
+
+void lw_upload(const double* ln, const float* scr)
+{
+  cudaMemcpyToSymbol(lw::c_ln, ln, 1024 * sizeof(double));
+  cudaMemcpyToSymbol(lw::c_scr, scr, 3072 * sizeof(float));
+}
+
+template <bool R, bool I, bool SM>
+static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb, int smem_words)
+{
+  auto k = lw::lw_sweep_kernel<R, I, SM>;
+  const int bytes = 20480 + (SM ? wpb * smem_words * 128 : 0);
+  static int configured = 48 * 1024;
+  if (bytes > configured)
+  {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    configured = bytes;
+  }
+  const int threads = 32 * wpb;
+  const int blocks = (a.n_walkers + threads - 1) / threads;
+  if (blocks > 0) k<<<blocks, threads, bytes, s>>>(a, smem_words);
+  return cudaGetLastError();
+}
+
+template <bool R, bool I>
+static cudaError_t lw_go_sm(const LwArgs& a, cudaStream_t s, int wpb, int smem_words)
+{
+  return smem_words > 0 ? lw_go<R, I, true>(a, s, wpb, smem_words) : lw_go<R, I, false>(a, s, wpb, 0);
+}
+
+// Warps per block: enough that the groups spread over the 152 SMs; the
+// group words go to shared memory when max_words words per lane fit.
+cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, cudaStream_t s)
+{
+  const int groups = (a.n_walkers + 31) / 32;
+  if (groups == 0) return cudaSuccess;
+  int wpb = std::max(1, std::min(4, (groups + 151) / 152));
+  int smem_words = 0;
+  const int avail = 227 * 1024 - 20480;
+  if (smem_ok && max_words > 0)
+  {
+    while (wpb > 1 && wpb * max_words * 128 > avail) wpb--;
+    if (wpb * max_words * 128 <= avail) smem_words = max_words;
+  }
+  if (a.replay)
+    return a.int_mode ? lw_go_sm<true, true>(a, s, wpb, smem_words) : lw_go_sm<true, false>(a, s, wpb, smem_words);
+  return a.int_mode ? lw_go_sm<false, true>(a, s, wpb, smem_words) : lw_go_sm<false, false>(a, s, wpb, smem_words);
+}
+
+static const int kMoveWords = 64;  // words per thread in the transposes
+
+cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s)
+{
+  const int groups = (a.n_walkers + 31) / 32;
+  if (groups == 0 || max_words == 0) return cudaSuccess;
+  const int wb = (max_words + kMoveWords - 1) / kMoveWords;
+  lw::lw_move_kernel<true><<<dim3(groups, wb), 32, 0, s>>>(a, kMoveWords);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s)
+{
+  const int groups = (a.n_walkers + 31) / 32;
+  if (groups == 0 || max_words == 0) return cudaSuccess;
+  const int wb = (max_words + kMoveWords - 1) / kMoveWords;
+  lw::lw_move_kernel<false><<<dim3(groups, wb), 32, 0, s>>>(a, kMoveWords);
+  if (max_terms > 0)
+  {
+    const long long total = (long long)a.n_walkers * max_terms;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
+    lw::lw_terms_kernel<<<blocks, 256, 0, s>>>(a, max_terms);
+  }
+  return cudaGetLastError();
+}
+}  // namespace qio

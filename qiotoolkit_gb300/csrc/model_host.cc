@@ -392,6 +392,28 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
   build_nbr(*m);
   detect_int_mode(*m);
   if (m->flavor == F_PARITY || m->flavor == F_COUNTER) build_near(*m);
+  if (m->flavor == F_PARITY)
+  {
+    // term parity from the member spins: with one or two members per term
+    // the cached term bit is the other member's spin (or a constant)
+    bool pair = m->M > 0;
+    for (int64_t t = 0; t < m->M && pair; t++) pair = m->trow[t + 1] - m->trow[t] <= 2;
+    m->pair_only = pair;
+    if (pair)
+    {
+      m->other.assign(m->K, -1);
+      for (int64_t v = 0; v < m->N; v++)
+        for (int q = m->row[v]; q < m->row[v + 1]; q++)
+        {
+          uint32_t t = m->inc[q] & ~kNegBit;
+          for (int j = m->trow[t]; j < m->trow[t + 1]; j++)
+          {
+            int u = (int)(m->tvar[j] & ~kNegBit);
+            if (u != v) m->other[q] = u;
+          }
+        }
+    }
+  }
   return m;
 }
 
@@ -411,7 +433,7 @@ void HostModel::upload() const
   size_t o_row = put(blob, row), o_inc = put(blob, inc), o_coef = put(blob, coef),
          o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
-         o_cf = put(blob, coef_f), o_near = put(blob, near);
+         o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -437,6 +459,8 @@ void HostModel::upload() const
   dev.near = near.empty() ? nullptr : (const unsigned long long*)(b + o_near);
   dev.fscreen = fscreen ? 1 : 0;
   dev.scan32 = scan32 ? 1 : 0;
+  dev.pair_only = pair_only ? 1 : 0;
+  dev.other = other.empty() ? nullptr : (const int*)(b + o_oth);
   uploaded = true;
 }
 

@@ -57,6 +57,8 @@ struct DevModel
   // count is in bits 61-63, 7 meaning "too many to list"
   const unsigned long long* near;
   int fscreen;             // FP64 coefficients all within the FP32 screen's range
+  int pair_only;           // Ising, every term has one or two members
+  const int* other;        // K  the other member of the incidence's term, or -1
   int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1
@@ -126,6 +128,36 @@ cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int warps_per_block
 cudaError_t launch_eval_cost(const DevModel& m, int n_states,
                              const uint32_t* spins, int nw, double* out,
                              cudaStream_t s);
+// Lane-per-walker sweeps (lanes.cu) for Ising models with one- or
+// two-member terms.  Walker r is lane r % 32 of group r / 32; a group's
+// block in the arena holds 32-bit words [spins gw*32][lowest spins gw*32]
+// [flip log kLwLog*32], word w of lane l at index w*32 + l.
+static const int kLwLog = 64;
+struct LwArgs
+{
+  const DevModel* models;   // device array
+  const int* model_of;      // per walker (null: every walker runs models[0])
+  int n_walkers;
+  DevPop p;                 // per-walker cost, lowest, counters; spins for the transposes
+  const int* slot_of;       // null: slot = walker
+  uint8_t* arena;
+  const long long* g_off;   // per group: byte offset of its block
+  const int* g_nw;          // per group: spin words per lane (block layout)
+  const double* beta;       // beta[r * bs_w + sweep * bs_s]
+  long long bs_w, bs_s;
+  long long sweep_base;
+  int n_sweeps;
+  int replay, int_mode;
+  uint64_t* rng;
+  uint32_t seed;
+  long long key_div;
+  unsigned long long key_base;
+};
+cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, cudaStream_t s);
+cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s);
+cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s);
+void lw_upload(const double* ln, const float* scr);
+
 // Allocation-free variant: states are n x n_vars bytes on the device, packed
 // into a fixed file-scope scratch array of kNoAllocScratchWords words.
 static const int kNoAllocScratchWords = 1 << 18;

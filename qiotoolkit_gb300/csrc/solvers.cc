@@ -126,6 +126,11 @@ static void configure_common(Solver& s, const json::Value& doc)
   s.warps_per_block = (int)p.integer("warps_per_block", 0);
   s.profile = p.boolean("profile_kernels", false);
   s.smem_state = p.boolean("smem_state", true);
+  std::string kern = p.str("kernel", "auto");
+  if (kern == "auto") s.kernel = 0;
+  else if (kern == "warp") s.kernel = 1;
+  else if (kern == "lanes") s.kernel = 2;
+  else fail(1, "parameter `kernel` must be \"auto\", \"warp\" or \"lanes\"");
   s.output_params.push_back({"seed", std::to_string(s.seed)});
   s.output_params.push_back({"step_limit", std::to_string(s.step_limit)});
 }
@@ -272,6 +277,80 @@ struct EventTimer
   }
 };
 
+// Lane-per-walker execution (lanes.cu): the group layout of the walkers,
+// the device copy of their model descriptors, and the transposes between the
+// population's bit-packed layout and the groups' interleaved bytes.
+struct LaneRunner
+{
+  DevBuf meta, arena;
+  LwArgs a{};
+  int max_words = 0, max_terms = 0;
+  bool ready = false;
+
+  // walker r runs models[model_of[r]] (model_of empty: models[0] for all)
+  void setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers)
+  {
+    const int G = (n_walkers + 31) / 32;
+    std::vector<long long> off(G);
+    std::vector<int> nv(G);
+    long long total = 0;
+    max_words = max_terms = 0;
+    for (int g = 0; g < G; g++)
+    {
+      int n = 0;
+      for (int l = 0; l < 32 && g * 32 + l < n_walkers; l++)
+      {
+        const DevModel& m = models[model_of.empty() ? 0 : model_of[g * 32 + l]];
+        n = std::max(n, m.n_vars);
+        max_words = std::max(max_words, (m.n_vars + 31) / 32);
+        max_terms = std::max(max_terms, m.n_terms);
+      }
+      nv[g] = (n + 31) / 32;  // spin words per lane
+      off[g] = total;
+      total += ((long long)nv[g] * 256 + (long long)kLwLog * 128 + 255) & ~255LL;
+    }
+
+    size_t o_m = 0, o_mo = (models.size() * sizeof(DevModel) + 255) & ~(size_t)255;
+    size_t o_off = o_mo + ((model_of.size() * 4 + 255) & ~(size_t)255);
+    size_t o_nv = o_off + (((size_t)G * 8 + 255) & ~(size_t)255);
+    size_t bytes = o_nv + (size_t)G * 4 + 16;
+    meta = DevBuf(bytes);
+    arena = DevBuf((size_t)std::max<long long>(total, 256));
+    char* b = (char*)meta.ptr;
+    cuda_check(cudaMemcpy(b + o_m, models.data(), models.size() * sizeof(DevModel), cudaMemcpyHostToDevice), "H2D");
+    if (!model_of.empty())
+      cuda_check(cudaMemcpy(b + o_mo, model_of.data(), model_of.size() * 4, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemcpy(b + o_off, off.data(), (size_t)G * 8, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemcpy(b + o_nv, nv.data(), (size_t)G * 4, cudaMemcpyHostToDevice), "H2D");
+    a = LwArgs{};
+    a.models = (const DevModel*)(b + o_m);
+    a.model_of = model_of.empty() ? nullptr : (const int*)(b + o_mo);
+    a.n_walkers = n_walkers;
+    a.arena = (uint8_t*)arena.ptr;
+    a.g_off = (const long long*)(b + o_off);
+    a.g_nw = (const int*)(b + o_nv);
+    ready = true;
+  }
+  size_t bytes() const { return meta.bytes + arena.bytes; }
+};
+
+// The lane kernel runs Ising models whose terms have one or two members.
+static bool lanes_eligible(const HostModel& m) { return m.flavor == F_PARITY && m.pair_only; }
+
+// kernel choice: one walker per lane when there are enough walkers to fill
+// warps of 32 many times over (or when asked for)
+static bool use_lanes(const Solver& s, const HostModel& m, int64_t walkers)
+{
+  if (s.kernel == 2)
+  {
+    if (!lanes_eligible(m))
+      fail(1, "parameter `kernel`: \"lanes\" needs an Ising model whose terms have at most two members");
+    return true;
+  }
+  if (s.kernel == 1) return false;
+  return lanes_eligible(m) && walkers >= 1024;
+}
+
 // beta as Metropolis::set_beta / set_temperature store it
 // (markov/metropolis.h:35-61)
 static double beta_of(double value, bool inverse)
@@ -291,6 +370,8 @@ class SimulatedAnnealing : public Solver
   Schedule schedule;
   Population P;
   std::vector<double> betas;
+  LaneRunner L;
+  bool lanes = false;
 
   std::string target() const override { return "simulatedannealing.qiotoolkit"; }
 
@@ -368,6 +449,49 @@ class SimulatedAnnealing : public Solver
     a.key_div = (long long)1 << 40;
     cuda_check(launch_init(a, st), "init kernel");
     launches++;
+    lanes = use_lanes(*this, *model, restarts);
+    if (lanes && !L.ready)
+    {
+      L.setup({model->device_view(full_maxsat_sweep)}, {}, R);
+      device_bytes += (int64_t)L.bytes();
+    }
+  }
+
+  LwArgs lane_args() const
+  {
+    LwArgs a = L.a;
+    a.p = P.pop;
+    a.slot_of = nullptr;
+    a.beta = P.beta;
+    a.bs_w = 0;
+    a.bs_s = 1;
+    a.replay = replay ? 1 : 0;
+    a.int_mode = model->int_mode ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    return a;
+  }
+
+  // one launch of sweeps [base, base + n) with the chosen kernel
+  void sweep_launch(SweepArgs& a, LwArgs& la, int wpb, int64_t base, int64_t n, cudaStream_t st)
+  {
+    prof_begin(st);
+    if (lanes)
+    {
+      la.sweep_base = base;
+      la.n_sweeps = (int)n;
+      cuda_check(launch_lw_sweep(la, L.max_words, smem_state ? 1 : 0, st), "lane sweep kernel");
+    }
+    else
+    {
+      a.sweep_base = base;
+      a.n_sweeps = (int)n;
+      cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+    }
+    prof_end(st);
+    launches++;
   }
 
   SweepArgs sweep_args() const
@@ -397,18 +521,16 @@ class SimulatedAnnealing : public Solver
     if (model->empty()) return;
     EventTimer total(st);
     SweepArgs a = sweep_args();
+    LwArgs la = lanes ? lane_args() : LwArgs{};
     int wpb = pick_wpb(warps_per_block, a.n_streams);
+    if (lanes)
+    {
+      cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
+      launches++;
+    }
     if (!has_cost_limit && !has_time_limit)
     {
-      a.sweep_base = 0;
-      a.n_sweeps = (int)step_limit;
-      if (step_limit > 0)
-      {
-        prof_begin(st);
-        cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
-        prof_end(st);
-        launches++;
-      }
+      if (step_limit > 0) sweep_launch(a, la, wpb, 0, step_limit, st);
       last_step = step_limit;
     }
     else
@@ -421,13 +543,9 @@ class SimulatedAnnealing : public Solver
       int64_t s = 0;
       while (s < step_limit)
       {
-        a.sweep_base = s;
-        a.n_sweeps = (int)std::min(chunk, step_limit - s);
-        prof_begin(st);
-        cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
-        prof_end(st);
-        launches++;
-        s += a.n_sweeps;
+        const int64_t n = std::min(chunk, step_limit - s);
+        sweep_launch(a, la, wpb, s, n, st);
+        s += n;
         if (has_cost_limit)
         {
           cuda_check(cudaMemcpyAsync(low.data(), P.pop.lowest, restarts * 8, cudaMemcpyDeviceToHost, st), "D2H");
@@ -442,6 +560,11 @@ class SimulatedAnnealing : public Solver
         }
       }
       last_step = s;
+    }
+    if (lanes)
+    {
+      cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
+      launches++;
     }
     run_ms = total.stop();
     sweep_ms = profile ? prof_total_ms() : run_ms;
