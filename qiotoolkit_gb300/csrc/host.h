@@ -61,6 +61,10 @@ struct HostModel
   // of each incidence (-1 for a one-member term)
   bool pair_only = false;
   std::vector<int> other;
+  // per incidence (other member, coefficient) records of the lane kernel; a
+  // one-member term points at the padding spin n_words * 32 (always 0)
+  std::vector<int> rec_i;     // 2 ints per incidence (integer mode)
+  std::vector<double> rec_f;  // 2 doubles per incidence: (other as bits, coef)
   std::vector<uint32_t> nbr;
   // term -> members
   std::vector<int> trow;

@@ -53,9 +53,27 @@ __device__ __forceinline__ bool lut_accept(const double* ln, const float* scr, u
 // SMEM: the group's current spin words live in shared memory for the launch
 // (copied in at the start, out at the end); the lowest words stay in global
 // memory.  Tables in the block's first 20 KB, group words after them.
+// per incidence record: (other member or the padding spin, coefficient)
+template <bool INT>
+struct Rec;
+template <>
+struct Rec<true>
+{
+  using T = int2;
+  static __device__ __forceinline__ int other(const int2& r) { return r.x; }
+};
+template <>
+struct Rec<false>
+{
+  using T = double2;
+  static __device__ __forceinline__ int other(const double2& r) { return (int)__double_as_longlong(r.x); }
+};
+static const int kPre = 8;  // records of the next variable loaded one attempt ahead
+
 template <bool REPLAY, bool INT, bool SMEM>
 __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
 {
+  using R = typename Rec<INT>::T;
   extern __shared__ __align__(16) unsigned char lw_smem[];
   double* s_ln = (double*)lw_smem;
   float* s_scr = (float*)(lw_smem + 8192);
@@ -68,11 +86,9 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
   const int g = r >> 5;
   const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
   const int* __restrict__ row = md->row;
-  const int* __restrict__ oth = md->other;
-  const double* __restrict__ coef = md->coef;
-  const int* __restrict__ coef_i = md->coef_i;
+  const R* __restrict__ rec = INT ? (const R*)md->rec_i : (const R*)md->rec_f;
   const int Sz = md->sweep_size;
-  const int nwd = (md->n_vars + 31) >> 5;
+  const int nwd = (md->n_vars + 31) >> 5;  // word nwd is the padding spin word (0)
   const int gw = a.g_nw[g];
   uint32_t* base = (uint32_t*)(a.arena + a.g_off[g]);
   uint32_t* gsp = base + lane;              // word w at gsp[w * 32]
@@ -84,6 +100,7 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
     sp = (uint32_t*)(lw_smem + 20480) + (size_t)(threadIdx.x >> 5) * smem_words * 32 + lane;
     for (int w = 0; w < nwd; w++) sp[(size_t)w * 32] = gsp[(size_t)w * 32];
   }
+  sp[(size_t)nwd * 32] = 0u;
 
   const int slot = a.slot_of ? a.slot_of[r] : r;
   double cost = a.p.cost[slot], low = a.p.lowest[r];
@@ -106,6 +123,7 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
     pend = false;
     nlog = 0;
   };
+  auto spin = [&](int u) -> uint32_t { return (sp[(size_t)(u >> 5) * 32] >> (u & 31)) & 1u; };
 
   for (int k = 0; k < a.n_sweeps; k++)
   {
@@ -115,11 +133,22 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
         ((unsigned long long)__double_as_longlong(beta) & 0x7FFFFFFFFFFFFFFFULL) == 0x7FF0000000000000ULL;
     const float nbeta_f = -approx_float(beta);
     const unsigned long long ctr0 = (unsigned long long)swp * (unsigned long long)Sz;
-    int q = __ldg(row);
+    natt += (unsigned long long)Sz;
+    int qb = __ldg(row), qe = __ldg(row + 1);
+    R cur[kPre];
+#pragma unroll
+    for (int j = 0; j < kPre; j++)
+      if (qb + j < qe) cur[j] = __ldg(rec + qb + j);
     uint32_t cw = 0;  // current word of v
     for (int v = 0; v < Sz; v++)
     {
-      const int qe = __ldg(row + v + 1);
+      // the next variable's records, one attempt ahead
+      const int qb1 = qe;
+      const int qe1 = (v + 1 < Sz) ? __ldg(row + v + 2) : qe;
+      R nxt[kPre];
+#pragma unroll
+      for (int j = 0; j < kPre; j++)
+        if (qb1 + j < qe1) nxt[j] = __ldg(rec + qb1 + j);
       if ((v & 31) == 0) cw = sp[(size_t)(v >> 5) * 32];
       const uint32_t sv = (cw >> (v & 31)) & 1u;
       long long idE = 0;
@@ -127,31 +156,44 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
       {
         int iacc = 0;
         double diff = 0.0;
-        for (; q < qe; q++)
-        {
-          const int u = __ldg(oth + q);
-          uint32_t su = 0;
-          if (u >= 0)
+#pragma unroll
+        for (int j = 0; j < kPre; j++)
+          if (qb + j < qe)
           {
-            const uint32_t wu = ((u >> 5) == (v >> 5)) ? cw : sp[(size_t)(u >> 5) * 32];
-            su = (wu >> (u & 31)) & 1u;
+            const uint32_t z = sv ^ spin(Rec<INT>::other(cur[j]));
+            if (INT)
+            {
+              const int c = ((const int2*)&cur[j])->y;
+              iacc += z ? -c : c;
+            }
+            else
+            {
+              const double c = ((const double2*)&cur[j])->y;
+              diff = __dadd_rn(diff, z ? -c : c);
+            }
           }
-          const uint32_t z = sv ^ su;
+        for (int q = qb + kPre; q < qe; q++)
+        {
+          const R rq = __ldg(rec + q);
+          const uint32_t z = sv ^ spin(Rec<INT>::other(rq));
           if (INT)
           {
-            const int c = __ldg(coef_i + q);
+            const int c = ((const int2*)&rq)->y;
             iacc += z ? -c : c;
           }
           else
           {
-            const double c = __ldg(coef + q);
+            const double c = ((const double2*)&rq)->y;
             diff = __dadd_rn(diff, z ? -c : c);
           }
         }
         if (INT) idE = -2LL * (long long)iacc;
         else dE = neg2x(diff);
       }
-      natt++;
+#pragma unroll
+      for (int j = 0; j < kPre; j++) cur[j] = nxt[j];
+      qb = qb1;
+      qe = qe1;
       bool acc;
       if (INT ? idE <= 0 : le_zero(dE)) acc = true;
       else

@@ -412,6 +412,28 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
             if (u != v) m->other[q] = u;
           }
         }
+      const int pad = (int)(((m->N + 31) / 32) * 32);  // the padding spin
+      if (m->int_mode)
+      {
+        m->rec_i.resize(2 * m->K);
+        for (int64_t q = 0; q < m->K; q++)
+        {
+          m->rec_i[2 * q] = m->other[q] >= 0 ? m->other[q] : pad;
+          m->rec_i[2 * q + 1] = m->coef_i[q];
+        }
+      }
+      else
+      {
+        m->rec_f.resize(2 * m->K);
+        for (int64_t q = 0; q < m->K; q++)
+        {
+          long long u = m->other[q] >= 0 ? m->other[q] : pad;
+          double ub;
+          memcpy(&ub, &u, 8);
+          m->rec_f[2 * q] = ub;
+          m->rec_f[2 * q + 1] = m->coef[q];
+        }
+      }
     }
   }
   return m;
@@ -433,7 +455,8 @@ void HostModel::upload() const
   size_t o_row = put(blob, row), o_inc = put(blob, inc), o_coef = put(blob, coef),
          o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
-         o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other);
+         o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other),
+         o_ri = put(blob, rec_i), o_rf = put(blob, rec_f);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -461,6 +484,8 @@ void HostModel::upload() const
   dev.scan32 = scan32 ? 1 : 0;
   dev.pair_only = pair_only ? 1 : 0;
   dev.other = other.empty() ? nullptr : (const int*)(b + o_oth);
+  dev.rec_i = rec_i.empty() ? nullptr : (const int2*)(b + o_ri);
+  dev.rec_f = rec_f.empty() ? nullptr : (const double2*)(b + o_rf);
   uploaded = true;
 }
 

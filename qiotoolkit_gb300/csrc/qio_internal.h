@@ -59,6 +59,8 @@ struct DevModel
   int fscreen;             // FP64 coefficients all within the FP32 screen's range
   int pair_only;           // Ising, every term has one or two members
   const int* other;        // K  the other member of the incidence's term, or -1
+  const int2* rec_i;       // K  (other or padding spin, integer coefficient), pair-only
+  const double2* rec_f;    // K  (other as an integer in the low word, coefficient)
   int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1

@@ -305,7 +305,7 @@ struct LaneRunner
         max_words = std::max(max_words, (m.n_vars + 31) / 32);
         max_terms = std::max(max_terms, m.n_terms);
       }
-      nv[g] = (n + 31) / 32;  // spin words per lane
+      nv[g] = (n + 31) / 32 + 1;  // spin words per lane, and the padding word
       off[g] = total;
       total += ((long long)nv[g] * 256 + (long long)kLwLog * 128 + 255) & ~255LL;
     }
@@ -482,7 +482,7 @@ class SimulatedAnnealing : public Solver
     {
       la.sweep_base = base;
       la.n_sweeps = (int)n;
-      cuda_check(launch_lw_sweep(la, L.max_words, smem_state ? 1 : 0, st), "lane sweep kernel");
+      cuda_check(launch_lw_sweep(la, L.max_words + 1, smem_state ? 1 : 0, st), "lane sweep kernel");
     }
     else
     {
