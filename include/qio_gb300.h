@@ -190,6 +190,37 @@ qio_status qio_solver_get_stats(qio_solver* s, qio_solver_stats* out);
 qio_status qio_solver_pt_observables(qio_solver* s, double* out5);
 qio_status qio_solver_destroy(qio_solver* s);
 
+/* ---- batches: many independent solves in one device graph ------------
+ * No counterpart in the reference, which solves one model per run
+ * (app/runner.cc:513-631).  Every instance gets the same target and params;
+ * instance i's result equals a plain solve of models[i] with them (the same
+ * walkers, streams, counters and result JSON).  Target
+ * "simulatedannealing.qiotoolkit".  Extra params keys: "autotune" (time the
+ * lane-kernel launch shapes on a short trial, default true), "graph"
+ * (capture the whole run in one CUDA graph, default true), "kernel".
+ * The models must outlive the batch. */
+typedef struct qio_batch qio_batch;
+typedef struct qio_batch_stats {
+  double run_ms;            /* last run: CUDA events around it              */
+  int64_t launches;         /* kernel launches per run                      */
+  int64_t walkers;          /* instances x restarts                         */
+  int64_t device_bytes;     /* population + lane groups                     */
+  int32_t kernel;           /* 1: one walker per warp, 2: one walker per lane */
+  int32_t warps_per_block;  /* lane plan (0: spread the groups over the SMs) */
+  int32_t smem;             /* 1: walker words in shared memory             */
+  int32_t graph;            /* 1: each run is one captured CUDA graph       */
+} qio_batch_stats;
+qio_status qio_batch_create(const qio_model* const* models, int32_t n_models, const char* target,
+                            const char* params_json, qio_batch** out);
+/* init + all sweeps of every instance; returns when they are done */
+qio_status qio_batch_run(qio_batch* batch, void* stream);
+/* instance's result JSON, the shape qio_solver_result_json gives */
+qio_status qio_batch_result_json(qio_batch* batch, int32_t instance, char** out_json);
+/* best cost per instance (lowest over its walkers + constant terms) */
+qio_status qio_batch_lowest(qio_batch* batch, double* costs);
+qio_status qio_batch_get_stats(const qio_batch* batch, qio_batch_stats* out);
+qio_status qio_batch_destroy(qio_batch* batch);
+
 /* ---- runner ----------------------------------------------------------- */
 
 /* app::Runner::run (app/runner.cc:215-631): problem JSON + params JSON +

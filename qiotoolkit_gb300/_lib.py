@@ -43,6 +43,12 @@ class SolverStats(C.Structure):
                 ("device_bytes", C.c_int64), ("windows", C.c_uint64)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("run_ms", C.c_double), ("launches", C.c_int64), ("walkers", C.c_int64),
+                ("device_bytes", C.c_int64), ("kernel", C.c_int32),
+                ("warps_per_block", C.c_int32), ("smem", C.c_int32), ("graph", C.c_int32)]
+
+
 # every symbol include/qio_gb300.h declares, with its ctypes signature
 def _signatures():
     vp, i32, i64, dbl, cp = C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_char_p
@@ -71,6 +77,12 @@ def _signatures():
         "qio_solver_get_stats": (st, [vp, P(SolverStats)]),
         "qio_solver_pt_observables": (st, [vp, P(dbl)]),
         "qio_solver_destroy": (st, [vp]),
+        "qio_batch_create": (st, [P(vp), i32, cp, cp, P(vp)]),
+        "qio_batch_run": (st, [vp, vp]),
+        "qio_batch_result_json": (st, [vp, i32, P(C.c_void_p)]),
+        "qio_batch_lowest": (st, [vp, P(dbl)]),
+        "qio_batch_get_stats": (st, [vp, P(BatchStats)]),
+        "qio_batch_destroy": (st, [vp]),
         "qio_run_json": (st, [cp, cp, cp, P(C.c_void_p)]),
     }
 

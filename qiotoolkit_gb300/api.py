@@ -215,3 +215,56 @@ def run_json(input_json, params_json, target: str) -> dict:
         return json.loads(C.string_at(p).decode())
     finally:
         L.qio_free(p)
+
+
+class Batch:
+    """Independent solves of many models with one target and params, run as
+    one captured CUDA graph (qio_batch_*).  Instance i's result equals
+    Solver(models[i], target, params).init().run().result()."""
+
+    def __init__(self, models, target: str, params: dict | str):
+        if not isinstance(params, str):
+            params = json.dumps(params if "params" in params else {"params": params})
+        self.models = list(models)
+        arr = (C.c_void_p * len(self.models))(*[m._h.value if isinstance(m._h, C.c_void_p) else m._h
+                                                for m in self.models])
+        h = C.c_void_p()
+        check(load().qio_batch_create(arr, len(self.models), target.encode(), params.encode(),
+                                      C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().qio_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, stream=None):
+        check(load().qio_batch_run(self._h, stream))
+        return self
+
+    def result(self, i: int) -> dict:
+        p = C.c_void_p()
+        L = load()
+        check(L.qio_batch_result_json(self._h, i, C.byref(p)))
+        try:
+            return json.loads(C.string_at(p).decode())
+        finally:
+            L.qio_free(p)
+
+    def lowest(self) -> np.ndarray:
+        out = np.zeros(len(self.models))
+        check(load().qio_batch_lowest(self._h, _ptr(out, C.c_double)))
+        return out
+
+    def stats(self):
+        from ._lib import BatchStats
+        st = BatchStats()
+        check(load().qio_batch_get_stats(self._h, C.byref(st)))
+        return st
+

@@ -17,6 +17,10 @@ struct qio_solver
   std::unique_ptr<Solver> s;
   const qio_model* model = nullptr;
 };
+struct qio_batch
+{
+  std::unique_ptr<Batch> b;
+};
 
 static thread_local std::string g_last_error;
 
@@ -344,6 +348,71 @@ qio_status qio_solver_pt_observables(qio_solver* s, double* out5)
 qio_status qio_solver_destroy(qio_solver* s)
 {
   return guard([&] { delete s; });
+}
+
+qio_status qio_batch_create(const qio_model* const* models, int32_t n_models, const char* target,
+                            const char* params_json, qio_batch** out)
+{
+  return guard([&] {
+    if (!models || !target || !params_json || !out) fail(1, "arguments must not be null");
+    *out = nullptr;
+    if (n_models <= 0) fail(1, "a batch needs at least one model");
+    std::vector<const HostModel*> ms(n_models);
+    for (int32_t i = 0; i < n_models; i++)
+    {
+      if (!models[i]) fail(1, "batch model " + std::to_string(i) + " is null");
+      ms[i] = models[i]->m.get();
+    }
+    json::Value doc = json::parse(params_json, strlen(params_json));
+    std::unique_ptr<qio_batch> h(new qio_batch());
+    h->b = make_batch(ms, target, doc);
+    *out = h.release();
+  });
+}
+
+qio_status qio_batch_run(qio_batch* batch, void* stream)
+{
+  return guard([&] {
+    if (!batch) fail(1, "batch must not be null");
+    batch->b->run(as_stream(stream));
+  });
+}
+
+qio_status qio_batch_result_json(qio_batch* batch, int32_t instance, char** out_json)
+{
+  return guard([&] {
+    if (!batch || !out_json) fail(1, "arguments must not be null");
+    *out_json = dup_string(batch->b->result_json(instance));
+  });
+}
+
+qio_status qio_batch_lowest(qio_batch* batch, double* costs)
+{
+  return guard([&] {
+    if (!batch || !costs) fail(1, "arguments must not be null");
+    batch->b->lowest(costs);
+  });
+}
+
+qio_status qio_batch_get_stats(const qio_batch* batch, qio_batch_stats* out)
+{
+  return guard([&] {
+    if (!batch || !out) fail(1, "arguments must not be null");
+    const BatchStats& st = batch->b->stats();
+    out->run_ms = st.run_ms;
+    out->launches = st.launches;
+    out->walkers = st.walkers;
+    out->device_bytes = st.device_bytes;
+    out->kernel = st.kernel;
+    out->warps_per_block = st.warps_per_block;
+    out->smem = st.smem;
+    out->graph = st.graph;
+  });
+}
+
+qio_status qio_batch_destroy(qio_batch* batch)
+{
+  return guard([&] { delete batch; });
 }
 
 qio_status qio_run_json(const char* input_json, const char* params_json, const char* target,

@@ -170,4 +170,26 @@ class Solver
   void prof_end(cudaStream_t s);
   double prof_total_ms();  // synchronises; resets the pairs
 };
+// Many independent solves of the same target and params (one per model).
+struct BatchStats
+{
+  double run_ms = 0;
+  int64_t launches = 0, walkers = 0, device_bytes = 0;
+  int kernel = 0, warps_per_block = 0, smem = 0, graph = 0;
+};
+class Batch
+{
+ public:
+  virtual ~Batch() {}
+  virtual void run(cudaStream_t s) = 0;
+  virtual int n_instances() const = 0;
+  virtual std::string result_json(int instance) = 0;
+  virtual void lowest(double* out) = 0;  // per instance: best lowest cost + const cost
+  const BatchStats& stats() const { return stats_; }
+
+ protected:
+  BatchStats stats_;
+};
+std::unique_ptr<Batch> make_batch(const std::vector<const HostModel*>& models, const std::string& target,
+                                  const json::Value& params_doc);
 }  // namespace qio

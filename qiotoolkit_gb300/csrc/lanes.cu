@@ -109,7 +109,10 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
   uint64_t rs = REPLAY ? a.rng[r] : 0;
   uint64_t key = 0;
   if (!REPLAY)
-    key = counter_key(a.seed + (uint32_t)(r / a.key_div), a.key_base + (unsigned long long)(r % a.key_div));
+  {
+    const long long lr = a.local_of ? a.local_of[r] : r;
+    key = counter_key(a.seed + (uint32_t)(lr / a.key_div), a.key_base + (unsigned long long)(lr % a.key_div));
+  }
   unsigned long long natt = 0, nacc = 0;
   bool pend = false;  // the lowest is the current state with the logged flips undone
   int nlog = 0;
@@ -399,11 +402,12 @@ static cudaError_t lw_go_sm(const LwArgs& a, cudaStream_t s, int wpb, int smem_w
 
 // Warps per block: enough that the groups spread over the 152 SMs; the
 // group words go to shared memory when max_words words per lane fit.
-cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, cudaStream_t s)
+cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, int wpb, cudaStream_t s)
 {
   const int groups = (a.n_walkers + 31) / 32;
   if (groups == 0) return cudaSuccess;
-  int wpb = std::max(1, std::min(4, (groups + 151) / 152));
+  if (wpb <= 0) wpb = std::max(1, std::min(4, (groups + 151) / 152));
+  wpb = std::min(wpb, 4);
   int smem_words = 0;
   const int avail = 227 * 1024 - 20480;
   if (smem_ok && max_words > 0)

@@ -154,8 +154,11 @@ struct LwArgs
   uint32_t seed;
   long long key_div;
   unsigned long long key_base;
+  const int* local_of;      // per walker: index within its solve for counter keys (null: r)
 };
-cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, cudaStream_t s);
+// wpb: warps per block (0: spread the groups over the SMs); smem_ok: keep
+// the group words in shared memory when max_words words per lane fit
+cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, int wpb, cudaStream_t s);
 cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s);
 cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s);
 void lw_upload(const double* ln, const float* scr);

@@ -186,10 +186,16 @@ struct Population
   void alloc(const HostModel& m, int slots, int streams, bool need_slots,
              int64_t n_beta)
   {
+    const bool plain = m.flavor == F_PLAIN_ISING || m.flavor == F_PLAIN_PUBO;
+    alloc_sizes(m.N, plain ? 0 : m.M, slots, streams, need_slots, n_beta);
+  }
+
+  // strides for models of up to N variables and M term-state bytes
+  void alloc_sizes(int64_t N, int64_t M, int slots, int streams, bool need_slots, int64_t n_beta)
+  {
     n = slots;
-    int nw = (int)(((m.N + 31) / 32 + 3) & ~3LL);
-    int mp = (int)((m.M + 15) & ~15LL);
-    if (m.flavor == F_PLAIN_ISING || m.flavor == F_PLAIN_PUBO) mp = 16;
+    int nw = (int)(((N + 31) / 32 + 3) & ~3LL);
+    int mp = std::max(16, (int)((M + 15) & ~15LL));
     size_t S = (size_t)slots;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -288,7 +294,8 @@ struct LaneRunner
   bool ready = false;
 
   // walker r runs models[model_of[r]] (model_of empty: models[0] for all)
-  void setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers)
+  void setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers,
+             const std::vector<int>& local_of = {})
   {
     const int G = (n_walkers + 31) / 32;
     std::vector<long long> off(G);
@@ -313,7 +320,8 @@ struct LaneRunner
     size_t o_m = 0, o_mo = (models.size() * sizeof(DevModel) + 255) & ~(size_t)255;
     size_t o_off = o_mo + ((model_of.size() * 4 + 255) & ~(size_t)255);
     size_t o_nv = o_off + (((size_t)G * 8 + 255) & ~(size_t)255);
-    size_t bytes = o_nv + (size_t)G * 4 + 16;
+    size_t o_lo = o_nv + (((size_t)G * 4 + 255) & ~(size_t)255);
+    size_t bytes = o_lo + local_of.size() * 4 + 16;
     meta = DevBuf(bytes);
     arena = DevBuf((size_t)std::max<long long>(total, 256));
     char* b = (char*)meta.ptr;
@@ -322,6 +330,8 @@ struct LaneRunner
       cuda_check(cudaMemcpy(b + o_mo, model_of.data(), model_of.size() * 4, cudaMemcpyHostToDevice), "H2D");
     cuda_check(cudaMemcpy(b + o_off, off.data(), (size_t)G * 8, cudaMemcpyHostToDevice), "H2D");
     cuda_check(cudaMemcpy(b + o_nv, nv.data(), (size_t)G * 4, cudaMemcpyHostToDevice), "H2D");
+    if (!local_of.empty())
+      cuda_check(cudaMemcpy(b + o_lo, local_of.data(), local_of.size() * 4, cudaMemcpyHostToDevice), "H2D");
     a = LwArgs{};
     a.models = (const DevModel*)(b + o_m);
     a.model_of = model_of.empty() ? nullptr : (const int*)(b + o_mo);
@@ -329,6 +339,7 @@ struct LaneRunner
     a.arena = (uint8_t*)arena.ptr;
     a.g_off = (const long long*)(b + o_off);
     a.g_nw = (const int*)(b + o_nv);
+    a.local_of = local_of.empty() ? nullptr : (const int*)(b + o_lo);
     ready = true;
   }
   size_t bytes() const { return meta.bytes + arena.bytes; }
@@ -482,7 +493,7 @@ class SimulatedAnnealing : public Solver
     {
       la.sweep_base = base;
       la.n_sweeps = (int)n;
-      cuda_check(launch_lw_sweep(la, L.max_words + 1, smem_state ? 1 : 0, st), "lane sweep kernel");
+      cuda_check(launch_lw_sweep(la, L.max_words + 1, smem_state ? 1 : 0, 0, st), "lane sweep kernel");
     }
     else
     {
@@ -889,6 +900,378 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
   }
   if (target == "populationannealing.cpu") return make_pa_solver(m, doc);
   fail(1, "Unknown solver: " + target);
+}
+
+// ---------------------------------------------------------------------------
+// Batches: independent simulated-annealing solves of many models with the
+// same params, in one population and one captured CUDA graph (the init
+// kernels, and one sweep launch for all instances when every model runs on
+// the lane kernel; one sweep launch per instance otherwise).  Instance i's
+// walkers, streams and results equal a plain solve of model i with the same
+// params: its walkers are numbered 0..restarts-1 for stream forks and
+// counter keys, exactly as in its own solve.
+// ---------------------------------------------------------------------------
+class BatchView : public SimulatedAnnealing
+{
+ public:
+  const Population* BP = nullptr;
+  int first = 0;
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest,
+             std::vector<uint64_t>& att, std::vector<uint64_t>& acc,
+             std::vector<uint8_t>* lowest_states, std::vector<uint8_t>* states) override
+  {
+    const int R = (int)n_walkers();
+    cost.resize(R);
+    lowest.resize(R);
+    att.resize(R);
+    acc.resize(R);
+    if (!R) return;
+    const DevPop& p = BP->pop;
+    cuda_check(cudaMemcpy(cost.data(), p.cost + first, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(lowest.data(), p.lowest + first, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), p.attempts + first, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), p.accepts + first, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    std::vector<uint32_t> w((size_t)R * p.nw);
+    if (lowest_states)
+    {
+      cuda_check(cudaMemcpy(w.data(), p.lspins + (size_t)first * p.nw, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, p.nw, model->N, R, *lowest_states);
+    }
+    if (states)
+    {
+      cuda_check(cudaMemcpy(w.data(), p.spins + (size_t)first * p.nw, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, p.nw, model->N, R, *states);
+    }
+  }
+};
+
+static DevPop pop_slice(const DevPop& p, int first, int count)
+{
+  DevPop v = p;
+  v.n = count;
+  v.spins = p.spins + (size_t)first * p.nw;
+  v.tstate = p.tstate + (size_t)first * p.mp;
+  v.cost = p.cost + first;
+  v.lowest = p.lowest + first;
+  v.lspins = p.lspins + (size_t)first * p.nw;
+  v.attempts = p.attempts + first;
+  v.accepts = p.accepts + first;
+  v.step_att = p.step_att + first;
+  v.step_acc = p.step_acc + first;
+  v.windows = p.windows ? p.windows + first : nullptr;
+  return v;
+}
+
+class SABatch : public Batch
+{
+ public:
+  std::vector<const HostModel*> models;
+  std::vector<std::unique_ptr<BatchView>> views;
+  int R = 0, W = 0;
+  int64_t steps = 0;
+  bool replay = true, lanes = false, autotune = true, use_graph = true, smem = true;
+  uint32_t seed = 0;
+  int kernel = 0;
+  Population P;
+  LaneRunner L;
+  DevBuf rng0;
+  bool prepared = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int plan_wpb = 0, plan_smem = 1;
+  int64_t graph_launches = 0;
+
+  ~SABatch() override
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+
+  void configure(const std::vector<const HostModel*>& ms, const json::Value& doc)
+  {
+    if (ms.empty()) fail(1, "a batch needs at least one model");
+    models = ms;
+    for (size_t i = 0; i < ms.size(); i++)
+    {
+      if (!ms[i]) fail(1, "batch model " + std::to_string(i) + " is null");
+      if (ms[i]->empty()) fail(1, "batch model " + std::to_string(i) + " has no variables");
+      std::unique_ptr<BatchView> v(new BatchView());
+      v->model = ms[i];
+      v->configure(doc);
+      if (v->has_cost_limit || v->has_time_limit)
+        fail(1, "batches run every instance for its full sweep count: `cost_limit` and `timeout` are not supported");
+      views.push_back(std::move(v));
+    }
+    const BatchView& v0 = *views[0];
+    R = (int)v0.restarts;
+    if ((int64_t)R * (int64_t)ms.size() > (1 << 26)) fail(1, "batch too large");
+    W = R * (int)ms.size();
+    steps = v0.step_limit;
+    replay = v0.replay;
+    seed = v0.seed;
+    kernel = v0.kernel;
+    smem = v0.smem_state;
+    Params p(doc["params"]);
+    autotune = p.boolean("autotune", true);
+    use_graph = p.boolean("graph", true);
+    bool eligible = true;
+    for (auto* m : ms)
+      eligible = eligible && lanes_eligible(*m) && m->int_mode == ms[0]->int_mode;
+    if (kernel == 2 && !eligible)
+      fail(1, "parameter `kernel`: \"lanes\" needs Ising models whose terms have at most two members "
+              "and the same coefficient kind");
+    lanes = eligible && kernel != 1;
+  }
+
+  int n_instances() const override { return (int)models.size(); }
+
+  void prepare(cudaStream_t st)
+  {
+    ensure_device();
+    int64_t N = 0, M = 0;
+    for (auto* m : models)
+    {
+      N = std::max(N, m->N);
+      const bool plain = m->flavor == F_PLAIN_ISING || m->flavor == F_PLAIN_PUBO;
+      M = std::max(M, plain ? (int64_t)0 : m->M);
+    }
+    P.alloc_sizes(N, M, W, W, false, std::max<int64_t>(1, steps));
+    // every model on the device before any capture (uploads allocate)
+    for (auto* m : models) m->device_view(false);
+    for (auto& v : views)
+    {
+      v->BP = &P;
+      v->first = (int)(&v - &views[0]) * R;
+    }
+    // stream forks of each instance: rngs_[i] = rng_->fork() in index order
+    // (solver/simulated_annealing.h:53-56), the same for every instance
+    std::vector<uint64_t> rs(W);
+    Pcg master(seed);
+    for (int i = 0; i < R; i++) rs[i] = Pcg(master.next()).state;
+    for (int k = 1; k < (int)models.size(); k++) std::copy(rs.begin(), rs.begin() + R, rs.begin() + (size_t)k * R);
+    rng0 = DevBuf((size_t)W * 8);
+    cuda_check(cudaMemcpy(rng0.ptr, rs.data(), (size_t)W * 8, cudaMemcpyHostToDevice), "H2D rng");
+    const auto& betas = views[0]->betas;
+    if (steps > 0)
+      cuda_check(cudaMemcpy(P.beta, betas.data(), betas.size() * 8, cudaMemcpyHostToDevice), "H2D beta");
+    if (lanes)
+    {
+      std::vector<DevModel> dm;
+      for (auto* m : models) dm.push_back(m->device_view(false));
+      std::vector<int> model_of(W), local_of(W);
+      for (int r = 0; r < W; r++)
+      {
+        model_of[r] = r / R;
+        local_of[r] = r % R;
+      }
+      L.setup(dm, model_of, W, local_of);
+    }
+    (void)st;
+    prepared = true;
+  }
+
+  LwArgs lane_args() const
+  {
+    LwArgs a = L.a;
+    a.p = P.pop;
+    a.slot_of = nullptr;
+    a.beta = P.beta;
+    a.bs_w = 0;
+    a.bs_s = 1;
+    a.replay = replay ? 1 : 0;
+    a.int_mode = models[0]->int_mode ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    return a;
+  }
+
+  // the whole solve, enqueued on st: streams reset, init, sweeps
+  void enqueue(cudaStream_t st, int64_t n_sweeps, int& n_launch)
+  {
+    n_launch = 0;
+    cuda_check(cudaMemcpyAsync(P.rng, rng0.ptr, (size_t)W * 8, cudaMemcpyDeviceToDevice, st), "D2D rng");
+    for (size_t i = 0; i < models.size(); i++)
+    {
+      InitArgs a{};
+      a.m = models[i]->device_view(false);
+      a.p = pop_slice(P.pop, (int)i * R, R);
+      a.n_walkers = R;
+      a.replay = replay ? 1 : 0;
+      a.rng = P.rng + (size_t)i * R;
+      a.seed = seed;
+      a.key_base = 0;
+      a.key_div = (long long)1 << 40;
+      cuda_check(launch_init(a, st), "init kernel");
+      n_launch++;
+    }
+    if (n_sweeps <= 0) return;
+    if (lanes)
+    {
+      LwArgs la = lane_args();
+      la.sweep_base = 0;
+      la.n_sweeps = (int)n_sweeps;
+      cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
+      cuda_check(launch_lw_sweep(la, L.max_words + 1, plan_smem, plan_wpb, st), "lane sweep kernel");
+      cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
+      n_launch += 3;
+    }
+    else
+      for (size_t i = 0; i < models.size(); i++)
+      {
+        SweepArgs a{};
+        a.m = models[i]->device_view(false);
+        a.p = pop_slice(P.pop, (int)i * R, R);
+        a.n_streams = R;
+        a.n_walkers = R;
+        a.beta = P.beta;
+        a.bs_w = 0;
+        a.bs_s = 1;
+        a.replay = replay ? 1 : 0;
+        a.rng = P.rng + (size_t)i * R;
+        a.seed = seed;
+        a.key_base = 0;
+        a.key_div = (long long)1 << 40;
+        a.smem_state = plan_smem;
+        a.err = device_error_flag();
+        a.sweep_base = 0;
+        a.n_sweeps = (int)n_sweeps;
+        cuda_check(launch_sweep(a, st, pick_wpb(plan_wpb, R)), "sweep kernel");
+        n_launch++;
+      }
+  }
+
+  // Launch plan for the lane kernel: warps per block and shared-memory
+  // groups, timed on a short trial of the batch itself.
+  void tune(cudaStream_t st)
+  {
+    plan_smem = smem ? 1 : 0;
+    plan_wpb = 0;
+    if (!autotune || !lanes || steps <= 0) return;
+    const int64_t trial = std::max<int64_t>(1, std::min<int64_t>(steps, (steps + 99) / 100));
+    double best = 1e300;
+    int best_wpb = 0, best_sm = plan_smem;
+    for (int sm = smem ? 1 : 0; sm >= 0; sm--)
+      for (int wpb : {1, 2, 4})
+      {
+        int n;
+        plan_wpb = wpb;
+        plan_smem = sm;
+        enqueue(st, 0, n);
+        LwArgs la = lane_args();
+        la.sweep_base = 0;
+        la.n_sweeps = (int)trial;
+        cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
+        EventTimer t(st);
+        cuda_check(launch_lw_sweep(la, L.max_words + 1, sm, wpb, st), "lane sweep kernel");
+        double ms = t.stop();
+        if (ms < best)
+        {
+          best = ms;
+          best_wpb = wpb;
+          best_sm = sm;
+        }
+      }
+    plan_wpb = best_wpb;
+    plan_smem = best_sm;
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!prepared)
+    {
+      prepare(st);
+      tune(st);
+    }
+    EventTimer total(st);
+    int n = 0;
+    if (use_graph)
+    {
+      if (!exec || graph_stream != st)
+      {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        // a private stream for the capture (the caller's may be the legacy
+        // default stream, which cannot be captured)
+        cudaStream_t cs;
+        cuda_check(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        try
+        {
+          enqueue(cs, steps, n);
+        }
+        catch (...)
+        {
+          cudaGraph_t g;
+          cudaStreamEndCapture(cs, &g);
+          if (g) cudaGraphDestroy(g);
+          cudaStreamDestroy(cs);
+          throw;
+        }
+        cuda_check(cudaStreamEndCapture(cs, &graph), "cudaStreamEndCapture");
+        cudaStreamDestroy(cs);
+        cuda_check(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+        graph_stream = st;
+        graph_launches = n;
+      }
+      cuda_check(cudaGraphLaunch(exec, st), "cudaGraphLaunch");
+      n = (int)graph_launches;
+    }
+    else
+      enqueue(st, steps, n);
+    const double ms = total.stop();
+    check_device_error(st);
+    for (auto& v : views)
+    {
+      v->initialized = v->ran = true;
+      v->last_step = steps;
+      v->run_ms = ms;
+      v->launches = (uint64_t)n;
+    }
+    stats_.run_ms = ms;
+    stats_.launches = n;
+    stats_.kernel = lanes ? 2 : 1;
+    stats_.warps_per_block = plan_wpb;
+    stats_.smem = plan_smem;
+    stats_.graph = use_graph ? 1 : 0;
+    stats_.walkers = W;
+    stats_.device_bytes = (int64_t)(P.buf.bytes + L.bytes() + rng0.bytes);
+  }
+
+  std::string result_json(int i) override
+  {
+    if (i < 0 || i >= (int)views.size()) fail(1, "instance " + std::to_string(i) + " out of range");
+    if (!views[i]->ran) fail(1, "run() must be called before reading results");
+    return views[i]->result_json();
+  }
+
+  void lowest(double* out) override
+  {
+    std::vector<double> low(W);
+    if (!views[0]->ran) fail(1, "run() must be called before reading results");
+    cuda_check(cudaMemcpy(low.data(), P.pop.lowest, (size_t)W * 8, cudaMemcpyDeviceToHost), "D2H");
+    for (size_t i = 0; i < models.size(); i++)
+    {
+      double b = low[i * R];
+      for (int k = 1; k < R; k++) b = std::min(b, low[i * R + k]);
+      out[i] = b + models[i]->const_cost;
+    }
+  }
+};
+
+std::unique_ptr<Batch> make_batch(const std::vector<const HostModel*>& models, const std::string& target,
+                                  const json::Value& doc)
+{
+  if (target != "simulatedannealing.qiotoolkit")
+    fail(1, "batches run \"simulatedannealing.qiotoolkit\"; found " + target);
+  std::unique_ptr<SABatch> b(new SABatch());
+  b->configure(models, doc);
+  return std::unique_ptr<Batch>(b.release());
 }
 
 // ---------------------------------------------------------------------------

@@ -105,3 +105,22 @@ def test_no_cpu_fallback_without_device():
     assert e.value.status in (3, 5)
     with pytest.raises(q.QioError):
         m.calculate_cost(np.zeros(2, np.uint8))
+
+
+def test_batch_configuration_errors():
+    """Batch parameter checks run on the host (no device needed)."""
+    from qiotoolkit_gb300 import instances as I
+    off, ids, coef = I.random_pubo(30, 60, seed=1)
+    pubo = q.Model("pubo", off=off, ids=ids, coef=coef)
+    off, ids, coef = I.cubic_pm_j(3, seed=1)
+    cube = q.Model("ising", off=off, ids=ids, coef=coef)
+    sa = "simulatedannealing.qiotoolkit"
+    with pytest.raises(q.QioError, match="batches run"):
+        q.Batch([cube], "paralleltempering.qiotoolkit", {"params": {"sweeps": 5}})
+    with pytest.raises(q.QioError, match="at most two members"):
+        q.Batch([cube, pubo], sa, {"params": {"sweeps": 5, "kernel": "lanes"}})
+    with pytest.raises(q.QioError, match="cost_limit"):
+        q.Batch([cube], sa, {"params": {"sweeps": 5, "cost_limit": -3}})
+    b = q.Batch([cube, pubo], sa, {"params": {"sweeps": 5, "restarts": 2}})
+    with pytest.raises(q.QioError, match="run\\(\\) must be called"):
+        b.result(0)
