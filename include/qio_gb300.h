@@ -209,6 +209,8 @@ typedef struct qio_batch_stats {
   int32_t warps_per_block;  /* lane plan (0: spread the groups over the SMs) */
   int32_t smem;             /* 1: walker words in shared memory             */
   int32_t graph;            /* 1: each run is one captured CUDA graph       */
+  double sweep_kernel_ms;   /* "graph": false with "profile_kernels": true:
+                               CUDA events around the sweep launches       */
 } qio_batch_stats;
 qio_status qio_batch_create(const qio_model* const* models, int32_t n_models, const char* target,
                             const char* params_json, qio_batch** out);

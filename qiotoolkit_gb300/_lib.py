@@ -46,7 +46,8 @@ class SolverStats(C.Structure):
 class BatchStats(C.Structure):
     _fields_ = [("run_ms", C.c_double), ("launches", C.c_int64), ("walkers", C.c_int64),
                 ("device_bytes", C.c_int64), ("kernel", C.c_int32),
-                ("warps_per_block", C.c_int32), ("smem", C.c_int32), ("graph", C.c_int32)]
+                ("warps_per_block", C.c_int32), ("smem", C.c_int32), ("graph", C.c_int32),
+                ("sweep_kernel_ms", C.c_double)]
 
 
 # every symbol include/qio_gb300.h declares, with its ctypes signature

@@ -407,6 +407,7 @@ qio_status qio_batch_get_stats(const qio_batch* batch, qio_batch_stats* out)
     out->warps_per_block = st.warps_per_block;
     out->smem = st.smem;
     out->graph = st.graph;
+    out->sweep_kernel_ms = st.sweep_kernel_ms;
   });
 }
 

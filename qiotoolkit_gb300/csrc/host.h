@@ -176,6 +176,7 @@ struct BatchStats
   double run_ms = 0;
   int64_t launches = 0, walkers = 0, device_bytes = 0;
   int kernel = 0, warps_per_block = 0, smem = 0, graph = 0;
+  double sweep_kernel_ms = 0;
 };
 class Batch
 {

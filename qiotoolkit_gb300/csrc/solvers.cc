@@ -982,6 +982,8 @@ class SABatch : public Batch
   cudaStream_t graph_stream = nullptr;
   int plan_wpb = 0, plan_smem = 1;
   int64_t graph_launches = 0;
+  bool profile = false;  // events around the sweep launches (runs without a graph)
+  double sweep_ms = 0;
 
   ~SABatch() override
   {
@@ -1016,6 +1018,7 @@ class SABatch : public Batch
     Params p(doc["params"]);
     autotune = p.boolean("autotune", true);
     use_graph = p.boolean("graph", true);
+    profile = v0.profile && !use_graph;
     bool eligible = true;
     for (auto* m : ms)
       eligible = eligible && lanes_eligible(*m) && m->int_mode == ms[0]->int_mode;
@@ -1115,11 +1118,15 @@ class SABatch : public Batch
       la.sweep_base = 0;
       la.n_sweeps = (int)n_sweeps;
       cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
+      std::unique_ptr<EventTimer> t(profile ? new EventTimer(st) : nullptr);
       cuda_check(launch_lw_sweep(la, L.max_words + 1, plan_smem, plan_wpb, st), "lane sweep kernel");
+      if (t) sweep_ms = t->stop();
       cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
       n_launch += 3;
     }
     else
+    {
+      std::unique_ptr<EventTimer> t(profile ? new EventTimer(st) : nullptr);
       for (size_t i = 0; i < models.size(); i++)
       {
         SweepArgs a{};
@@ -1142,6 +1149,8 @@ class SABatch : public Batch
         cuda_check(launch_sweep(a, st, pick_wpb(plan_wpb, R)), "sweep kernel");
         n_launch++;
       }
+      if (t) sweep_ms = t->stop();
+    }
   }
 
   // Launch plan for the lane kernel: warps per block and shared-memory
@@ -1241,6 +1250,7 @@ class SABatch : public Batch
     stats_.graph = use_graph ? 1 : 0;
     stats_.walkers = W;
     stats_.device_bytes = (int64_t)(P.buf.bytes + L.bytes() + rng0.bytes);
+    stats_.sweep_kernel_ms = profile ? sweep_ms : 0.0;
   }
 
   std::string result_json(int i) override
