@@ -47,7 +47,7 @@ class Params(C.Structure):
                 ("rng_mode", C.c_int), ("threads", C.c_int),
                 ("number_of_solutions", C.c_int),
                 ("has_cost_limit", C.c_int), ("cost_limit", C.c_double),
-                ("full_maxsat_sweep", C.c_int)]
+                ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int)]
 
 
 def build(force: bool = False) -> str:
@@ -76,6 +76,8 @@ def lib():
         L.orc_metropolis_accept.restype = ip
         L.orc_counter_draw.argtypes = [C.c_uint64, C.c_uint64]
         L.orc_counter_draw.restype = C.c_uint64
+        L.orc_qexp.argtypes = [C.c_double]
+        L.orc_qexp.restype = C.c_double
         L.orc_counter_key.argtypes = [u32, C.c_uint64]
         L.orc_counter_key.restype = C.c_uint64
         L.orc_model_create.argtypes = [ip, i64, P(i64), P(C.c_int32), P(dbl), C.c_char_p, ip]
@@ -299,7 +301,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         sched_count=None, sweeps_per_replica=1, population=16, alpha=2.0,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
-        full_maxsat_sweep=False):
+        full_maxsat_sweep=False, resampling="reference"):
     p = Params()
     p.solver = {"sa": SA, "pt": PT, "pa": PA}[solver]
     p.seed = seed & 0xFFFFFFFF
@@ -320,12 +322,18 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
     p.has_cost_limit = cost_limit is not None
     p.cost_limit = float(cost_limit or 0.0)
     p.full_maxsat_sweep = int(full_maxsat_sweep)
+    p.resampling = {"reference": 0, "multinomial": 1}[resampling]
     err = C.create_string_buffer(512)
     h = lib().orc_run(model.h, C.byref(p), err, 512)
     del keep
     if not h:
         raise ValueError(err.value.decode())
     return Result(h)
+
+
+def qexp(x):
+    """exp of the multinomial resampling mode (x <= 0)."""
+    return lib().orc_qexp(float(x))
 
 
 def pt_toy(seed, steps, temps, use_inverse=False):

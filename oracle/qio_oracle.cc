@@ -1228,6 +1228,44 @@ struct Selector
   }
 };
 
+// ---------------------------------------------------------------------------
+// Multinomial resampling mode of the GB300 library (params "resampling":
+// "multinomial", counter streams), restated: the library's exp (Cody-Waite
+// reduction with the fdlibm split of ln 2, degree-13 Taylor polynomial by
+// fused multiply-adds, 2^k by exponent bits), fixed-point weights
+// floor(w 2^40), exact integer prefix sums, parent j = first i with
+// prefix_i > hi64(draw_j * total).
+// ---------------------------------------------------------------------------
+static double multinomial_exp(double x)
+{
+  if (x < -745.2) return 0.0;
+  const double k = std::nearbyint(x * 1.4426950408889634);
+  double r = std::fma(-k, 6.93147180369123816490e-01, x);
+  r = std::fma(-k, 1.90821492927058770002e-10, r);
+  static const double inv_fact[14] = {1.0 / 6227020800.0, 1.0 / 479001600.0, 1.0 / 39916800.0,
+                                      1.0 / 3628800.0,    1.0 / 362880.0,    1.0 / 40320.0,
+                                      1.0 / 5040.0,       1.0 / 720.0,       1.0 / 120.0,
+                                      1.0 / 24.0,         1.0 / 6.0,         0.5,
+                                      1.0,                1.0};
+  double poly = inv_fact[0];
+  for (int j = 1; j < 14; j++) poly = std::fma(poly, r, inv_fact[j]);
+  int ki = (int)k;
+  if (ki < -1020)
+  {
+    poly *= 5.551115123125783e-17;  // 2^-54
+    ki += 54;
+  }
+  uint64_t bits = (uint64_t)(int64_t)(ki + 1023) << 52;
+  double scale;
+  std::memcpy(&scale, &bits, 8);
+  return poly * scale;
+}
+
+static uint64_t mul_hi64(uint64_t a, uint64_t b)
+{
+  return (uint64_t)(((unsigned __int128)a * (unsigned __int128)b) >> 64);
+}
+
 static Result run_pa(Model& m, const orc_params& p)
 {
   Result r;
@@ -1341,7 +1379,42 @@ static Result run_pa(Model& m, const orc_params& p)
     double delta_beta = beta.get_value((double)(step + 1 - restart_base)) -
                         beta.get_value((double)(step - restart_base));
     double rho_t = 1.0;
-    if (delta_beta > 0)
+    bool all_equal = false;
+    if (p.resampling == 1)
+    {
+      double cmax = -std::numeric_limits<double>::max();
+      for (size_t i = 0; i < R; i++) cmax = std::max(cmax, after[i] + min_cost);
+      all_equal = cmax == min_cost;
+    }
+    if (delta_beta > 0 && p.resampling == 1)
+    {
+      // multinomial on counter draws: the population size stays R
+      std::vector<uint64_t> prefix(R);
+      uint64_t run = 0;
+      for (size_t i = 0; i < R; i++)
+      {
+        const double w = multinomial_exp(-(delta_beta * m.scale_factor) * after[i]);
+        run += (uint64_t)(w * 1099511627776.0);
+        prefix[i] = run;
+      }
+      const uint64_t key = counter_key(p.seed, (0x7FFFFFFFULL << 32) | (uint64_t)step);
+      std::vector<std::unique_ptr<Citizen>> next;
+      for (size_t j = 0; j < R; j++)
+      {
+        const uint64_t u = mul_hi64(counter_draw(key, (uint64_t)j), run);
+        const size_t parent = (size_t)(std::upper_bound(prefix.begin(), prefix.end(), u) - prefix.begin());
+        std::unique_ptr<Citizen> cp(new Citizen(*pop[parent]));
+        cp->count = 1;
+        next.push_back(std::move(cp));
+      }
+      pop.swap(next);
+      std::map<size_t, size_t> fam;
+      for (auto& c : pop) fam[c->family]++;
+      uint64_t sq = 0;
+      for (auto& f : fam) sq += (uint64_t)f.second * (uint64_t)f.second;
+      rho_t = (double)sq / Rd;
+    }
+    else if (delta_beta > 0)
     {
       // resample, solver/population_annealing.h:490-616
       double total = 0.0;
@@ -1424,7 +1497,7 @@ static Result run_pa(Model& m, const orc_params& p)
     }
     r.pa_beta.push_back(cur_beta);
     r.pa_pop.push_back((int64_t)pop.size());
-    if (Rd / rho_t < p.alpha || var_after == 0)
+    if (Rd / rho_t < p.alpha || (p.resampling == 1 ? all_equal : var_after == 0))
     {
       cur_beta = beta_start;
       restart_base = step;
@@ -1598,6 +1671,8 @@ uint64_t orc_counter_draw(uint64_t key, uint64_t ctr)
 {
   return counter_draw(key, ctr);
 }
+
+double orc_qexp(double x) { return multinomial_exp(x); }
 uint64_t orc_counter_key(uint32_t seed, uint64_t stream)
 {
   return counter_key(seed, stream);

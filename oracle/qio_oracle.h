@@ -62,6 +62,9 @@ typedef struct orc_params {
   int has_cost_limit;
   double cost_limit;
   int full_maxsat_sweep;      /* MaxSAT: N attempts per sweep instead of 1 */
+  int resampling;             /* PA: 0 the reference's (Poisson / constant),
+                                 1 multinomial on counter draws (the GB300
+                                 library's device mode, restated here) */
 } orc_params;
 
 /* ---- random generator pins ---- */
@@ -74,6 +77,8 @@ void orc_uniform_ln(double* out /* 4*256 */);
 int orc_metropolis_accept(double cost_diff, double beta, const uint32_t* draws,
                           int n_draws, int* used);
 uint64_t orc_counter_draw(uint64_t key, uint64_t ctr);
+/* exp(x) for x <= 0 as the multinomial resampling mode defines it */
+double orc_qexp(double x);
 uint64_t orc_counter_key(uint32_t seed, uint64_t stream);
 
 /* ---- model ---- */

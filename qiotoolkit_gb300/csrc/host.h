@@ -170,6 +170,26 @@ class Solver
   void prof_end(cudaStream_t s);
   double prof_total_ms();  // synchronises; resets the pairs
 };
+// Lane-per-walker execution (lanes.cu): the group layout of the walkers,
+// the device copy of their model descriptors, and the transposes between a
+// population's bit-packed layout and the groups' interleaved words.
+struct LaneRunner
+{
+  DevBuf meta, arena;
+  LwArgs a{};
+  int max_words = 0, max_terms = 0;
+  bool ready = false;
+  // walker r runs models[model_of[r]] (model_of empty: models[0] for all);
+  // local_of[r]: its index within its own solve, for counter keys
+  void setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers,
+             const std::vector<int>& local_of = {});
+  size_t bytes() const { return meta.bytes + arena.bytes; }
+};
+bool lanes_eligible(const HostModel& m);
+// the lane kernel for this solver and walker count (params "kernel"; auto:
+// eligible models with at least 1024 walkers)
+bool lanes_for(const Solver& s, const HostModel& m, int64_t walkers);
+
 // Many independent solves of the same target and params (one per model).
 struct BatchStats
 {

@@ -213,6 +213,18 @@ class PopulationAnnealing : public Solver
 
   bool streams_on_device = false;
 
+  // multinomial device resampling (counter streams) and lane-kernel sweeps
+  bool multinomial = false;
+  bool lanes = false;
+  DevBuf dres;  // prefix sums, two family arrays, census counts, scalars
+  unsigned long long* d_prefix = nullptr;
+  int* d_family[2] = {nullptr, nullptr};
+  unsigned int* d_counts = nullptr;
+  PaScalars* d_scal = nullptr;
+  int res_cap = 0, fcur = 0;
+  LaneRunner L;
+  int lane_walkers = 0;
+
   std::string target_name() const { return "populationannealing.cpu"; }
 
   bool historical_lowest(double& c, std::vector<uint8_t>& st) override
@@ -257,6 +269,29 @@ class PopulationAnnealing : public Solver
     d_src = (int*)(b + o_src);
     d_beta = (double*)(b + o_b);
     aux_cap = capacity;
+    if (multinomial) ensure_res(capacity);
+  }
+
+  void ensure_res(int capacity)
+  {
+    if (capacity <= res_cap) return;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+    size_t o_p = take((size_t)capacity * 8), o_f0 = take((size_t)capacity * 4), o_f1 = take((size_t)capacity * 4),
+           o_c = take((size_t)capacity * 4), o_s = take(sizeof(PaScalars));
+    DevBuf nb(off);
+    char* b = (char*)nb.ptr;
+    int* nf0 = (int*)(b + o_f0);
+    if (res_cap > 0 && R > 0)  // carry the families over
+      cuda_check(cudaMemcpy(nf0, d_family[fcur], R * 4, cudaMemcpyDeviceToDevice), "D2D");
+    dres = std::move(nb);
+    d_prefix = (unsigned long long*)(b + o_p);
+    d_family[0] = nf0;
+    d_family[1] = (int*)(b + o_f1);
+    d_counts = (unsigned int*)(b + o_c);
+    d_scal = (PaScalars*)(b + o_s);
+    fcur = 0;
+    res_cap = capacity;
   }
 
   void ensure_capacity(int n, cudaStream_t st)
@@ -350,6 +385,12 @@ class PopulationAnnealing : public Solver
     }
     launches++;
     upload_beta(st);
+    if (multinomial)
+    {
+      ensure_res(pools[cur].cap);
+      cuda_check(launch_pa_iota(d_family[fcur], (int)R, st), "family ids");
+      launches++;
+    }
   }
 
   void init(cudaStream_t st) override
@@ -369,6 +410,9 @@ class PopulationAnnealing : public Solver
     cur_beta = beta_start;
     restart_base = 0;
     R = 0;
+    // lanes need independent streams per walker: counter mode only
+    lanes = !replay && lanes_for(*this, *model, (int64_t)target_pop);
+    if (replay && kernel == 2) fail(1, "parameter `kernel`: \"lanes\" needs \"rng_mode\": \"counter\" here");
     init_population(st);
     // update_lowest_cost(population_[0]->cost(), population_[0]->state())
     double c0;
@@ -381,6 +425,7 @@ class PopulationAnnealing : public Solver
   }
 
   void run(cudaStream_t st) override;
+  void step_multinomial(cudaStream_t st, int64_t step);
 
   void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
              std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
@@ -477,11 +522,86 @@ void PopulationAnnealing::configure_common_pa(const json::Value& doc)
   if (en && en->is_array())
     for (const auto& x : en->arr)
       if (x.is_number() && x.num == 2) exp_repop = true;
+  const json::Value* rsm = p.find("resampling");
+  if (rsm && !rsm->is_null())
+  {
+    if (!rsm->is_string() || (rsm->str != "reference" && rsm->str != "multinomial"))
+      fail(1, "parameter `resampling` must be \"reference\" or \"multinomial\"");
+    multinomial = rsm->str == "multinomial";
+    if (multinomial && replay)
+      fail(1, "parameter `resampling`: \"multinomial\" needs \"rng_mode\": \"counter\"");
+  }
   // OpenMP stream emulation for replay: one stream per reference thread
   T = threads;
   output_params.push_back({"population", std::to_string(target_pop)});
   output_params.push_back({"beta", beta.render()});
   output_params.push_back({"alpha", json::number(alpha)});
+}
+
+// One resampling step on the device (pa_device.cu): weights, prefix sums,
+// parents, replica copies and the family census run as kernels; the host
+// reads back one small record (cost range, best lowest, census).
+void PopulationAnnealing::step_multinomial(cudaStream_t st, int64_t step)
+{
+  const double scale = model->scale_factor;
+  const size_t Rn = R;
+  const double Rd = (double)Rn;
+  Pool& P = pools[cur];
+  double delta_beta = beta.get_value((double)(step + 1 - (int64_t)restart_base)) -
+                      beta.get_value((double)(step - (int64_t)restart_base));
+  trace_beta.push_back(cur_beta);
+  cuda_check(launch_pa_weights(P.pop.cost, P.pop.lowest, (int)Rn, delta_beta > 0 ? delta_beta * scale : 0.0,
+                               d_prefix, d_scal, st),
+             "weights kernel");
+  launches++;
+  if (delta_beta > 0)
+  {
+    const uint64_t key = host_counter_key(seed, (0x7FFFFFFFULL << 32) | (uint64_t)step);
+    Pool& Pn = pools[1 - cur];
+    cuda_check(launch_pa_parents(d_prefix, (int)Rn, (int)Rn, key, d_scal, d_family[fcur], d_src,
+                                 d_family[1 - fcur], st),
+               "parents kernel");
+    cuda_check(launch_pa_copy(P.pop, Pn.pop, d_src, (int)Rn, st), "copy kernel");
+    fcur = 1 - fcur;
+    cuda_check(launch_pa_census(d_family[fcur], (int)Rn, d_counts, (int)Rn, d_scal, st), "census");
+    launches += 4;
+  }
+  PaScalars sc{};
+  cuda_check(cudaMemcpyAsync(&sc, d_scal, sizeof sc, cudaMemcpyDeviceToHost, st), "D2H");
+  cuda_check(cudaStreamSynchronize(st), "sync");
+  // update_lowest_cost (solver/population_annealing.h:301-308): the first
+  // citizen with the smallest lowest cost, on the population swept this step
+  if (!has_low || sc.best_lowest < low_cost)
+  {
+    has_low = true;
+    low_cost = sc.best_lowest;
+    low_words.resize(P.pop.nw);
+    cuda_check(cudaMemcpy(low_words.data(), P.pop.lspins + (size_t)sc.best_index * P.pop.nw,
+                          P.pop.nw * 4, cudaMemcpyDeviceToHost), "D2H");
+  }
+  double rho_t = 1.0;
+  if (delta_beta > 0)
+  {
+    cur = 1 - cur;
+    rho_t = (double)sc.census / Rd;
+  }
+  trace_pop.push_back((int64_t)R);
+  if (Rd / rho_t < alpha || sc.cmax == sc.cmin)
+  {
+    cur_beta = beta_start;
+    restart_base = (uint64_t)step;
+    if (exp_repop) target_pop *= 2;
+    epoch++;
+    init_population(st);
+  }
+  else
+  {
+    cur_beta += delta_beta;
+    const double b = cur_beta <= 0 ? 0.0 : cur_beta;
+    std::fill(wbeta.begin(), wbeta.begin() + R, b);  // host mirror for a later restart
+    cuda_check(launch_pa_fill(d_beta, (int)R, b, st), "beta fill");
+    launches++;
+  }
 }
 
 void PopulationAnnealing::run(cudaStream_t st)
@@ -520,10 +640,49 @@ void PopulationAnnealing::run(cudaStream_t st)
     a.smem_state = smem_state ? 1 : 0;
     a.err = device_error_flag();
     int wpb = pick_wpb(warps_per_block, a.n_streams);
-    prof_begin(st);
-    cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
-    prof_end(st);
-    launches++;
+    if (lanes)
+    {
+      if (!L.ready || lane_walkers < (int)Rn)
+      {
+        L.setup({model->device_view(full_maxsat_sweep)}, {}, (int)Rn);
+        lane_walkers = (int)Rn;
+      }
+      LwArgs la = L.a;
+      la.p = P.pop;
+      la.n_walkers = (int)Rn;
+      la.beta = d_beta;
+      la.bs_w = 1;
+      la.bs_s = 0;
+      la.sweep_base = 0;
+      la.n_sweeps = (int)spr;
+      la.replay = 0;
+      la.int_mode = model->int_mode ? 1 : 0;
+      la.seed = seed;
+      la.key_base = a.key_base;
+      la.key_div = a.key_div;
+      cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
+      prof_begin(st);
+      cuda_check(launch_lw_sweep(la, L.max_words + 1, smem_state ? 1 : 0, 0, st), "lane sweep kernel");
+      prof_end(st);
+      // the term bytes are not kept up to date: every reader of this
+      // population in this mode uses the spins
+      cuda_check(launch_lw_store(la, L.max_words, 0, st), "lane store");
+      launches += 3;
+    }
+    else
+    {
+      prof_begin(st);
+      cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+      prof_end(st);
+      launches++;
+    }
+    if (multinomial)
+    {
+      step_multinomial(st, step);
+      step++;
+      if (has_cost_limit && has_low && low_cost <= cost_limit) break;
+      continue;
+    }
     cuda_check(cudaMemcpyAsync(after.data(), P.pop.cost, Rn * 8, cudaMemcpyDeviceToHost, st), "D2H");
     cuda_check(cudaMemcpyAsync(lowest.data(), P.pop.lowest, Rn * 8, cudaMemcpyDeviceToHost, st), "D2H");
     cuda_check(cudaStreamSynchronize(st), "sync");

@@ -163,6 +163,25 @@ cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s);
 cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s);
 void lw_upload(const double* ln, const float* scr);
 
+// Device resampling of population annealing (pa_device.cu, multinomial).
+struct PaScalars
+{
+  double cmin, cmax, best_lowest;
+  int best_index;
+  unsigned long long total;   // sum of the fixed-point weights
+  unsigned long long census;  // sum over families of count^2
+};
+cudaError_t launch_pa_weights(const double* cost, const double* lowest, int R, double dbeta_scale,
+                              unsigned long long* prefix, PaScalars* out, cudaStream_t s);
+cudaError_t launch_pa_parents(const unsigned long long* prefix, int R, int R_new, uint64_t key,
+                              const PaScalars* sc, const int* family, int* src, int* family_new,
+                              cudaStream_t s);
+cudaError_t launch_pa_census(const int* family, int R, unsigned int* counts, int n_families, PaScalars* out,
+                             cudaStream_t s);
+cudaError_t launch_pa_iota(int* a, int n, cudaStream_t s);
+cudaError_t launch_pa_fill(double* a, int n, double v, cudaStream_t s);
+cudaError_t launch_qexp(const double* x, double* y, int n, cudaStream_t s);
+
 // Allocation-free variant: states are n x n_vars bytes on the device, packed
 // into a fixed file-scope scratch array of kNoAllocScratchWords words.
 static const int kNoAllocScratchWords = 1 << 18;

@@ -286,17 +286,9 @@ struct EventTimer
 // Lane-per-walker execution (lanes.cu): the group layout of the walkers,
 // the device copy of their model descriptors, and the transposes between the
 // population's bit-packed layout and the groups' interleaved bytes.
-struct LaneRunner
+void LaneRunner::setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers,
+                       const std::vector<int>& local_of)
 {
-  DevBuf meta, arena;
-  LwArgs a{};
-  int max_words = 0, max_terms = 0;
-  bool ready = false;
-
-  // walker r runs models[model_of[r]] (model_of empty: models[0] for all)
-  void setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers,
-             const std::vector<int>& local_of = {})
-  {
     const int G = (n_walkers + 31) / 32;
     std::vector<long long> off(G);
     std::vector<int> nv(G);
@@ -341,16 +333,14 @@ struct LaneRunner
     a.g_nw = (const int*)(b + o_nv);
     a.local_of = local_of.empty() ? nullptr : (const int*)(b + o_lo);
     ready = true;
-  }
-  size_t bytes() const { return meta.bytes + arena.bytes; }
-};
+}
 
 // The lane kernel runs Ising models whose terms have one or two members.
-static bool lanes_eligible(const HostModel& m) { return m.flavor == F_PARITY && m.pair_only; }
+bool lanes_eligible(const HostModel& m) { return m.flavor == F_PARITY && m.pair_only; }
 
 // kernel choice: one walker per lane when there are enough walkers to fill
 // warps of 32 many times over (or when asked for)
-static bool use_lanes(const Solver& s, const HostModel& m, int64_t walkers)
+bool lanes_for(const Solver& s, const HostModel& m, int64_t walkers)
 {
   if (s.kernel == 2)
   {
@@ -460,7 +450,7 @@ class SimulatedAnnealing : public Solver
     a.key_div = (long long)1 << 40;
     cuda_check(launch_init(a, st), "init kernel");
     launches++;
-    lanes = use_lanes(*this, *model, restarts);
+    lanes = lanes_for(*this, *model, restarts);
     if (lanes && !L.ready)
     {
       L.setup({model->device_view(full_maxsat_sweep)}, {}, R);

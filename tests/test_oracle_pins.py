@@ -169,3 +169,18 @@ def test_planted_ground_energies(golden):
                   sched=("linear", 0.0, 3.0 / max(abs(c) for c, _ in inst["terms"])),
                   threads=4)
         assert r.best_cost == pytest.approx(inst["energy"], abs=1e-6)
+
+
+def test_multinomial_exp_accuracy():
+    """The resampling mode's own exp stays within 1 ulp of the C library's
+    over the normal range (and underflows to 0 like it)."""
+    import math
+    xs = -np.concatenate([np.random.default_rng(0).uniform(0, 745, 4000),
+                          np.random.default_rng(1).uniform(0, 1e-3, 1000), [0.0, 1e-300, 700.0]])
+    worst = 0.0
+    for x in xs:
+        a, b = O.qexp(x), math.exp(x)
+        if b > 2.2250738585072014e-308:
+            worst = max(worst, abs(a - b) / math.ulp(b))
+    assert worst <= 1.0
+    assert O.qexp(0.0) == 1.0 and O.qexp(-800.0) == 0.0
