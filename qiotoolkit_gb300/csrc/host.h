@@ -181,8 +181,10 @@ struct LaneRunner
   bool ready = false;
   // walker r runs models[model_of[r]] (model_of empty: models[0] for all);
   // local_of[r]: its index within its own solve, for counter keys
+  // smem: hold the group words in shared memory when they fit (with fewer
+  // than 32 lanes per group if that is what makes them fit)
   void setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers,
-             const std::vector<int>& local_of = {});
+             const std::vector<int>& local_of = {}, bool smem = true);
   size_t bytes() const { return meta.bytes + arena.bytes; }
 };
 bool lanes_eligible(const HostModel& m);

@@ -6,11 +6,12 @@
 // cost difference summed over the incident terms in ascending term order
 // (model/ising.h:108-117), the Metropolis decision (markov/metropolis.h:
 // 64-104) on the walker's own stream, the flip, cost += diff and the lowest
-// check.  The 32 walkers of a warp form a group whose spins are stored
-// bit-packed and interleaved: word w (spins 32w .. 32w+31) of lane l at
-// group word w*32 + l, so the warp's accesses to one word index are one
-// 128-byte line, and the row loads of a model are shared by the lanes that
-// run it.
+// check.  The G walkers of a warp (G <= 32 lanes; fewer when a group's
+// spins would not fit in shared memory otherwise) form a group whose spins
+// are stored bit-packed and interleaved: word w (spins 32w .. 32w+31) of
+// lane l at group word w*G + l, so the warp's accesses to one word index are
+// one line, and the row loads of a model are shared by the lanes that run
+// it.
 //
 // Term parity from spins: with at most two members, the cached term bit of
 // IsingTermCached is the XOR of the variable's own spin and the other
@@ -22,7 +23,8 @@
 // the current state is the lowest; later flips are logged, and the lowest
 // spins are written out (current words with the logged flips undone) when
 // the log fills or the launch ends -- the same state, fewer copies.  The
-// Metropolis tables sit in shared memory: lanes look up different buckets.
+// Metropolis tables are read through L1 from global memory: lanes look up
+// different buckets, which constant memory would serialise.
 #include <algorithm>
 
 #include "metropolis.cuh"
@@ -36,8 +38,8 @@ using namespace qio::mc;
 static const unsigned long long kMult = 6364136223846793005ULL;
 static const unsigned long long kInc = 1442695040888963407ULL;
 
-__constant__ double c_ln[1024];
-__constant__ float c_scr[1024 * 3];
+__device__ double g_ln[1024];
+__device__ float g_scr[1024 * 3];
 
 // Metropolis decision for an uphill move with threshold dE * (-beta):
 // FP32 screen first, the exact FP64 expression inside its margin.
@@ -71,19 +73,18 @@ struct Rec<false>
 static const int kPre = 8;  // records of the next variable loaded one attempt ahead
 
 template <bool REPLAY, bool INT, bool SMEM>
-__global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
+__global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
 {
   using R = typename Rec<INT>::T;
   extern __shared__ __align__(16) unsigned char lw_smem[];
-  double* s_ln = (double*)lw_smem;
-  float* s_scr = (float*)(lw_smem + 8192);
-  for (int t = threadIdx.x; t < 1024; t += blockDim.x) s_ln[t] = c_ln[t];
-  for (int t = threadIdx.x; t < 3072; t += blockDim.x) s_scr[t] = c_scr[t];
-  __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= a.n_walkers) return;  // no warp-wide operations below
+  const double* s_ln = g_ln;
+  const float* s_scr = g_scr;
+  const int G = a.G;
   const int lane = threadIdx.x & 31;
-  const int g = r >> 5;
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int r = g * G + lane;
+  if (lane >= G || r >= a.n_walkers) return;  // no warp-wide operations below
+  const int smem_words = a.smem_words;
   const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
   const int* __restrict__ row = md->row;
   const R* __restrict__ rec = INT ? (const R*)md->rec_i : (const R*)md->rec_f;
@@ -91,16 +92,16 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
   const int nwd = (md->n_vars + 31) >> 5;  // word nwd is the padding spin word (0)
   const int gw = a.g_nw[g];
   uint32_t* base = (uint32_t*)(a.arena + a.g_off[g]);
-  uint32_t* gsp = base + lane;              // word w at gsp[w * 32]
-  uint32_t* lsp = base + (size_t)gw * 32 + lane;
-  uint32_t* lg = base + (size_t)gw * 64 + lane;
+  uint32_t* gsp = base + lane;              // word w at gsp[w * G]
+  uint32_t* lsp = base + (size_t)gw * G + lane;
+  uint32_t* lg = base + (size_t)gw * 2 * G + lane;
   uint32_t* sp = gsp;
   if (SMEM)
   {
-    sp = (uint32_t*)(lw_smem + 20480) + (size_t)(threadIdx.x >> 5) * smem_words * 32 + lane;
-    for (int w = 0; w < nwd; w++) sp[(size_t)w * 32] = gsp[(size_t)w * 32];
+    sp = (uint32_t*)lw_smem + (size_t)(threadIdx.x >> 5) * smem_words * G + lane;
+    for (int w = 0; w < nwd; w++) sp[(size_t)w * G] = gsp[(size_t)w * G];
   }
-  sp[(size_t)nwd * 32] = 0u;
+  sp[(size_t)nwd * G] = 0u;
 
   const int slot = a.slot_of ? a.slot_of[r] : r;
   double cost = a.p.cost[slot], low = a.p.lowest[r];
@@ -117,16 +118,16 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
   bool pend = false;  // the lowest is the current state with the logged flips undone
   int nlog = 0;
   auto write_lowest = [&]() {
-    for (int w = 0; w < nwd; w++) lsp[(size_t)w * 32] = sp[(size_t)w * 32];
+    for (int w = 0; w < nwd; w++) lsp[(size_t)w * G] = sp[(size_t)w * G];
     for (int i = 0; i < nlog; i++)
     {
-      const uint32_t v = lg[(size_t)i * 32];
-      lsp[(size_t)(v >> 5) * 32] ^= 1u << (v & 31);
+      const uint32_t v = lg[(size_t)i * G];
+      lsp[(size_t)(v >> 5) * G] ^= 1u << (v & 31);
     }
     pend = false;
     nlog = 0;
   };
-  auto spin = [&](int u) -> uint32_t { return (sp[(size_t)(u >> 5) * 32] >> (u & 31)) & 1u; };
+  auto spin = [&](int u) -> uint32_t { return (sp[(size_t)(u >> 5) * G] >> (u & 31)) & 1u; };
 
   for (int k = 0; k < a.n_sweeps; k++)
   {
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
 #pragma unroll
       for (int j = 0; j < kPre; j++)
         if (qb1 + j < qe1) nxt[j] = __ldg(rec + qb1 + j);
-      if ((v & 31) == 0) cw = sp[(size_t)(v >> 5) * 32];
+      if ((v & 31) == 0) cw = sp[(size_t)(v >> 5) * G];
       const uint32_t sv = (cw >> (v & 31)) & 1u;
       long long idE = 0;
       double dE = 0.0;
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
       {
         nacc++;
         cw ^= 1u << (v & 31);
-        sp[(size_t)(v >> 5) * 32] = cw;
+        sp[(size_t)(v >> 5) * G] = cw;
         bool newlow;
         if (INT)
         {
@@ -287,11 +288,11 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
           {
             // the log is full: write the lowest out, this flip excluded
             write_lowest();
-            lsp[(size_t)(v >> 5) * 32] ^= 1u << (v & 31);
+            lsp[(size_t)(v >> 5) * G] ^= 1u << (v & 31);
           }
           else
           {
-            lg[(size_t)nlog * 32] = (uint32_t)v;
+            lg[(size_t)nlog * G] = (uint32_t)v;
             nlog++;
           }
         }
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
   }
   if (pend) write_lowest();
   if (SMEM)
-    for (int w = 0; w < nwd; w++) gsp[(size_t)w * 32] = sp[(size_t)w * 32];
+    for (int w = 0; w < nwd; w++) gsp[(size_t)w * G] = sp[(size_t)w * G];
   a.p.cost[slot] = INT ? (double)icost : cost;
   a.p.lowest[r] = INT ? (double)ilow : low;
   a.p.attempts[r] += natt;
@@ -313,13 +314,14 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a, int smem_words)
 
 // Population (bit-packed spins per slot, lowest spins per walker) <-> group
 // words.  Thread (g, lane) of block (g, word block) moves words of walker
-// g*32 + lane; a warp's accesses to one word index are one line.
+// g*G + lane; a warp's accesses to one word index are one line.
 template <bool LOAD>
 __global__ void lw_move_kernel(LwArgs a, int words_per_block)
 {
+  const int G = a.G;
   const int g = blockIdx.x, lane = threadIdx.x;
-  const int r = g * 32 + lane;
-  if (r >= a.n_walkers) return;
+  const int r = g * G + lane;
+  if (lane >= G || r >= a.n_walkers) return;
   const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
   const int nwd = (md->n_vars + 31) >> 5;
   const int slot = a.slot_of ? a.slot_of[r] : r;
@@ -328,8 +330,8 @@ __global__ void lw_move_kernel(LwArgs a, int words_per_block)
   const int q0 = blockIdx.y * words_per_block, q1 = min(nwd, q0 + words_per_block);
   for (int q = q0; q < q1; q++)
   {
-    uint32_t* sp = base + (size_t)q * 32 + lane;
-    uint32_t* lsp = base + (size_t)(gw + q) * 32 + lane;
+    uint32_t* sp = base + (size_t)q * G + lane;
+    uint32_t* lsp = base + (size_t)(gw + q) * G + lane;
     uint32_t* ps = a.p.spins + (size_t)slot * a.p.nw + q;
     uint32_t* pl = a.p.lspins + (size_t)r * a.p.nw + q;
     if (LOAD)
@@ -372,15 +374,15 @@ __global__ void lw_terms_kernel(LwArgs a, int max_terms)
 
 void lw_upload(const double* ln, const float* scr)
 {
-  cudaMemcpyToSymbol(lw::c_ln, ln, 1024 * sizeof(double));
-  cudaMemcpyToSymbol(lw::c_scr, scr, 3072 * sizeof(float));
+  cudaMemcpyToSymbol(lw::g_ln, ln, 1024 * sizeof(double));
+  cudaMemcpyToSymbol(lw::g_scr, scr, 3072 * sizeof(float));
 }
 
 template <bool R, bool I, bool SM>
-static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb, int smem_words)
+static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb)
 {
   auto k = lw::lw_sweep_kernel<R, I, SM>;
-  const int bytes = 20480 + (SM ? wpb * smem_words * 128 : 0);
+  const int bytes = SM ? wpb * a.smem_words * a.G * 4 : 0;
   static int configured = 48 * 1024;
   if (bytes > configured)
   {
@@ -388,43 +390,42 @@ static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb, int smem_word
     if (e != cudaSuccess) return e;
     configured = bytes;
   }
-  const int threads = 32 * wpb;
-  const int blocks = (a.n_walkers + threads - 1) / threads;
-  if (blocks > 0) k<<<blocks, threads, bytes, s>>>(a, smem_words);
+  const int groups = (a.n_walkers + a.G - 1) / a.G;
+  const int blocks = (groups + wpb - 1) / wpb;
+  if (blocks > 0) k<<<blocks, 32 * wpb, bytes, s>>>(a);
   return cudaGetLastError();
 }
 
 template <bool R, bool I>
-static cudaError_t lw_go_sm(const LwArgs& a, cudaStream_t s, int wpb, int smem_words)
+static cudaError_t lw_go_sm(const LwArgs& a, cudaStream_t s, int wpb)
 {
-  return smem_words > 0 ? lw_go<R, I, true>(a, s, wpb, smem_words) : lw_go<R, I, false>(a, s, wpb, 0);
+  return a.smem_words > 0 ? lw_go<R, I, true>(a, s, wpb) : lw_go<R, I, false>(a, s, wpb);
 }
 
-// Warps per block: enough that the groups spread over the 152 SMs; the
-// group words go to shared memory when max_words words per lane fit.
-cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, int wpb, cudaStream_t s)
+// Warps per block: enough that the groups spread over the 152 SMs, as many
+// as the groups' shared-memory words allow.
+cudaError_t launch_lw_sweep(const LwArgs& a, int wpb, cudaStream_t s)
 {
-  const int groups = (a.n_walkers + 31) / 32;
+  if (a.G < 1 || a.G > 32) return cudaErrorInvalidValue;
+  const int groups = (a.n_walkers + a.G - 1) / a.G;
   if (groups == 0) return cudaSuccess;
   if (wpb <= 0) wpb = std::max(1, std::min(4, (groups + 151) / 152));
   wpb = std::min(wpb, 4);
-  int smem_words = 0;
-  const int avail = 227 * 1024 - 20480;
-  if (smem_ok && max_words > 0)
+  if (a.smem_words > 0)
   {
-    while (wpb > 1 && wpb * max_words * 128 > avail) wpb--;
-    if (wpb * max_words * 128 <= avail) smem_words = max_words;
+    while (wpb > 1 && wpb * a.smem_words * a.G * 4 > kLwSmemBytes) wpb--;
+    if (a.smem_words * a.G * 4 > kLwSmemBytes) return cudaErrorInvalidValue;
   }
   if (a.replay)
-    return a.int_mode ? lw_go_sm<true, true>(a, s, wpb, smem_words) : lw_go_sm<true, false>(a, s, wpb, smem_words);
-  return a.int_mode ? lw_go_sm<false, true>(a, s, wpb, smem_words) : lw_go_sm<false, false>(a, s, wpb, smem_words);
+    return a.int_mode ? lw_go_sm<true, true>(a, s, wpb) : lw_go_sm<true, false>(a, s, wpb);
+  return a.int_mode ? lw_go_sm<false, true>(a, s, wpb) : lw_go_sm<false, false>(a, s, wpb);
 }
 
 static const int kMoveWords = 64;  // words per thread in the transposes
 
 cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s)
 {
-  const int groups = (a.n_walkers + 31) / 32;
+  const int groups = (a.n_walkers + a.G - 1) / a.G;
   if (groups == 0 || max_words == 0) return cudaSuccess;
   const int wb = (max_words + kMoveWords - 1) / kMoveWords;
   lw::lw_move_kernel<true><<<dim3(groups, wb), 32, 0, s>>>(a, kMoveWords);
@@ -433,7 +434,7 @@ cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s)
 
 cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s)
 {
-  const int groups = (a.n_walkers + 31) / 32;
+  const int groups = (a.n_walkers + a.G - 1) / a.G;
   if (groups == 0 || max_words == 0) return cudaSuccess;
   const int wb = (max_words + kMoveWords - 1) / kMoveWords;
   lw::lw_move_kernel<false><<<dim3(groups, wb), 32, 0, s>>>(a, kMoveWords);

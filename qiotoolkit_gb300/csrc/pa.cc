@@ -644,7 +644,7 @@ void PopulationAnnealing::run(cudaStream_t st)
     {
       if (!L.ready || lane_walkers < (int)Rn)
       {
-        L.setup({model->device_view(full_maxsat_sweep)}, {}, (int)Rn);
+        L.setup({model->device_view(full_maxsat_sweep)}, {}, (int)Rn, {}, smem_state);
         lane_walkers = (int)Rn;
       }
       LwArgs la = L.a;
@@ -662,7 +662,7 @@ void PopulationAnnealing::run(cudaStream_t st)
       la.key_div = a.key_div;
       cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
       prof_begin(st);
-      cuda_check(launch_lw_sweep(la, L.max_words + 1, smem_state ? 1 : 0, 0, st), "lane sweep kernel");
+      cuda_check(launch_lw_sweep(la, 0, st), "lane sweep kernel");
       prof_end(st);
       // the term bytes are not kept up to date: every reader of this
       // population in this mode uses the spins

@@ -131,10 +131,11 @@ cudaError_t launch_eval_cost(const DevModel& m, int n_states,
                              const uint32_t* spins, int nw, double* out,
                              cudaStream_t s);
 // Lane-per-walker sweeps (lanes.cu) for Ising models with one- or
-// two-member terms.  Walker r is lane r % 32 of group r / 32; a group's
-// block in the arena holds 32-bit words [spins gw*32][lowest spins gw*32]
-// [flip log kLwLog*32], word w of lane l at index w*32 + l.
+// two-member terms.  Walker r is lane r % G of group r / G (G <= 32 lanes of
+// one warp); a group's block in the arena holds 32-bit words [spins gw*G]
+// [lowest spins gw*G][flip log kLwLog*G], word w of lane l at index w*G + l.
 static const int kLwLog = 64;
+static const int kLwSmemBytes = 227 * 1024;  // dynamic shared memory per block
 struct LwArgs
 {
   const DevModel* models;   // device array
@@ -155,10 +156,11 @@ struct LwArgs
   long long key_div;
   unsigned long long key_base;
   const int* local_of;      // per walker: index within its solve for counter keys (null: r)
+  int G;                    // walkers (lanes) per group
+  int smem_words;           // group words per lane held in shared memory (0: global)
 };
-// wpb: warps per block (0: spread the groups over the SMs); smem_ok: keep
-// the group words in shared memory when max_words words per lane fit
-cudaError_t launch_lw_sweep(const LwArgs& a, int max_words, int smem_ok, int wpb, cudaStream_t s);
+// wpb: warps per block (0: spread the groups over the SMs)
+cudaError_t launch_lw_sweep(const LwArgs& a, int wpb, cudaStream_t s);
 cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s);
 cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s);
 void lw_upload(const double* ln, const float* scr);

@@ -287,26 +287,44 @@ struct EventTimer
 // the device copy of their model descriptors, and the transposes between the
 // population's bit-packed layout and the groups' interleaved bytes.
 void LaneRunner::setup(const std::vector<DevModel>& models, const std::vector<int>& model_of, int n_walkers,
-                       const std::vector<int>& local_of)
+                       const std::vector<int>& local_of, bool smem)
 {
-    const int G = (n_walkers + 31) / 32;
+    max_words = max_terms = 0;
+    for (int r = 0; r < n_walkers; r++)
+    {
+      const DevModel& m = models[model_of.empty() ? 0 : model_of[r]];
+      max_words = std::max(max_words, (m.n_vars + 31) / 32);
+      max_terms = std::max(max_terms, m.n_terms);
+      if (model_of.empty()) break;
+    }
+    // lanes per group: 32 when a group's words (and the padding word) fit in
+    // shared memory, else as many as fit (at least 8), else 32 in global memory
+    const int words = max_words + 1;
+    int lanes = 32, smem_words = 0;
+    if (smem)
+    {
+      if (32 * words * 4 <= kLwSmemBytes) smem_words = words;
+      else if (8 * words * 4 <= kLwSmemBytes)
+      {
+        lanes = kLwSmemBytes / (words * 4);
+        smem_words = words;
+      }
+    }
+    const int G = (n_walkers + lanes - 1) / lanes;
     std::vector<long long> off(G);
     std::vector<int> nv(G);
     long long total = 0;
-    max_words = max_terms = 0;
     for (int g = 0; g < G; g++)
     {
       int n = 0;
-      for (int l = 0; l < 32 && g * 32 + l < n_walkers; l++)
+      for (int l = 0; l < lanes && g * lanes + l < n_walkers; l++)
       {
-        const DevModel& m = models[model_of.empty() ? 0 : model_of[g * 32 + l]];
+        const DevModel& m = models[model_of.empty() ? 0 : model_of[g * lanes + l]];
         n = std::max(n, m.n_vars);
-        max_words = std::max(max_words, (m.n_vars + 31) / 32);
-        max_terms = std::max(max_terms, m.n_terms);
       }
       nv[g] = (n + 31) / 32 + 1;  // spin words per lane, and the padding word
       off[g] = total;
-      total += ((long long)nv[g] * 256 + (long long)kLwLog * 128 + 255) & ~255LL;
+      total += ((long long)nv[g] * 8 * lanes + (long long)kLwLog * 4 * lanes + 255) & ~255LL;
     }
 
     size_t o_m = 0, o_mo = (models.size() * sizeof(DevModel) + 255) & ~(size_t)255;
@@ -332,6 +350,8 @@ void LaneRunner::setup(const std::vector<DevModel>& models, const std::vector<in
     a.g_off = (const long long*)(b + o_off);
     a.g_nw = (const int*)(b + o_nv);
     a.local_of = local_of.empty() ? nullptr : (const int*)(b + o_lo);
+    a.G = lanes;
+    a.smem_words = smem_words;
     ready = true;
 }
 
@@ -453,7 +473,7 @@ class SimulatedAnnealing : public Solver
     lanes = lanes_for(*this, *model, restarts);
     if (lanes && !L.ready)
     {
-      L.setup({model->device_view(full_maxsat_sweep)}, {}, R);
+      L.setup({model->device_view(full_maxsat_sweep)}, {}, R, {}, smem_state);
       device_bytes += (int64_t)L.bytes();
     }
   }
@@ -483,7 +503,7 @@ class SimulatedAnnealing : public Solver
     {
       la.sweep_base = base;
       la.n_sweeps = (int)n;
-      cuda_check(launch_lw_sweep(la, L.max_words + 1, smem_state ? 1 : 0, 0, st), "lane sweep kernel");
+      cuda_check(launch_lw_sweep(la, 0, st), "lane sweep kernel");
     }
     else
     {
@@ -1059,7 +1079,7 @@ class SABatch : public Batch
         model_of[r] = r / R;
         local_of[r] = r % R;
       }
-      L.setup(dm, model_of, W, local_of);
+      L.setup(dm, model_of, W, local_of, smem);
     }
     (void)st;
     prepared = true;
@@ -1109,7 +1129,8 @@ class SABatch : public Batch
       la.n_sweeps = (int)n_sweeps;
       cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
       std::unique_ptr<EventTimer> t(profile ? new EventTimer(st) : nullptr);
-      cuda_check(launch_lw_sweep(la, L.max_words + 1, plan_smem, plan_wpb, st), "lane sweep kernel");
+      if (!plan_smem) la.smem_words = 0;
+      cuda_check(launch_lw_sweep(la, plan_wpb, st), "lane sweep kernel");
       if (t) sweep_ms = t->stop();
       cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
       n_launch += 3;
@@ -1153,7 +1174,7 @@ class SABatch : public Batch
     const int64_t trial = std::max<int64_t>(1, std::min<int64_t>(steps, (steps + 99) / 100));
     double best = 1e300;
     int best_wpb = 0, best_sm = plan_smem;
-    for (int sm = smem ? 1 : 0; sm >= 0; sm--)
+    for (int sm = L.a.smem_words > 0 ? 1 : 0; sm >= 0; sm--)
       for (int wpb : {1, 2, 4})
       {
         int n;
@@ -1163,9 +1184,10 @@ class SABatch : public Batch
         LwArgs la = lane_args();
         la.sweep_base = 0;
         la.n_sweeps = (int)trial;
+        if (!sm) la.smem_words = 0;
         cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
         EventTimer t(st);
-        cuda_check(launch_lw_sweep(la, L.max_words + 1, sm, wpb, st), "lane sweep kernel");
+        cuda_check(launch_lw_sweep(la, wpb, st), "lane sweep kernel");
         double ms = t.stop();
         if (ms < best)
         {
