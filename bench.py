@@ -40,7 +40,7 @@ WORKLOADS = {
                           "linear beta 0.1->5.0 over 1000 sweeps, 64 restarts, seed 0",
                      target="simulatedannealing.qiotoolkit"),
     "pa_square": dict(desc="PA on 2D periodic 256x256 +-J Ising, R=4096, 100 beta steps 0->3.0, "
-                           "10 sweeps per step",
+                           "10 sweeps per step, device-side multinomial resampling, counter streams",
                       target="populationannealing.cpu"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
@@ -76,7 +76,8 @@ def make_workload(name):
     if name == "pa_square":
         off, ids, coef = I.square_pm_j(256, seed=3)
         params = {"seed": 0, "sweeps": 100, "population": 4096, "beta_start": 0.0,
-                  "beta_stop": 3.0, "sweeps_per_replica": 10, "rng_mode": "counter"}
+                  "beta_stop": 3.0, "sweeps_per_replica": 10, "rng_mode": "counter",
+                  "resampling": "multinomial"}
         return "ising", off, ids, coef, params
     raise SystemExit(f"unknown workload {name}")
 
@@ -183,7 +184,8 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
         elif "population" in params:
             O.run(m, "pa", seed=0, step_limit=sweeps, population=restarts, pa_threads=threads,
                   threads=threads, sched=("linear", params["beta_start"], params["beta_stop"]),
-                  sweeps_per_replica=params["sweeps_per_replica"], rng_mode="counter")
+                  sweeps_per_replica=params["sweeps_per_replica"], rng_mode="counter",
+                  resampling=params.get("resampling", "reference"))
             a = restarts * sweeps * params["sweeps_per_replica"] * n
             d = f"population {restarts} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
         else:
