@@ -223,6 +223,45 @@ qio_status qio_batch_lowest(qio_batch* batch, double* costs);
 qio_status qio_batch_get_stats(const qio_batch* batch, qio_batch_stats* out);
 qio_status qio_batch_destroy(qio_batch* batch);
 
+/* ---- serving: continuous batching of solve requests -------------------
+ * No counterpart in the reference (one solve per process).  A worker thread
+ * admits requests in arrival order when a slot is free and their device
+ * footprint (model + walker population) fits the memory budget (a later
+ * request may overtake one that does not fit yet), keeps each admitted
+ * solve resident on the device, advances all of them in overlapping pieces
+ * on their own streams, and retires a solve when its sweep budget is spent.
+ * A request's result JSON equals qio_solver_*'s for the same model, target
+ * and params, alone or in any mix.  Targets: simulated annealing and
+ * parallel tempering; `cost_limit` / `timeout` are rejected.
+ * config_json: {"memory_budget_bytes": B (default: half the free device
+ * memory), "max_active": A (default 64), "sa_sweeps_per_piece": 64,
+ * "pt_steps_per_piece": 16}. */
+typedef struct qio_server qio_server;
+typedef struct qio_server_stats {
+  int64_t submitted, completed, failed, active, pending;
+  int64_t used_bytes, budget_bytes, peak_active;
+  double elapsed_s;          /* since creation                               */
+  double p50_ms, p99_ms, max_ms;  /* submit-to-done latency of completed ones */
+} qio_server_stats;
+qio_status qio_server_create(const char* config_json, qio_server** out);
+/* the model must stay alive until the request has finished */
+qio_status qio_server_submit(qio_server* server, const qio_model* model, const char* target,
+                             const char* params_json, int64_t* request_id);
+/* state: 0 pending, 1 running, 2 done (*out_json = result), 3 failed
+ * (*out_json = message); *out_json is set only then (free with qio_free) */
+qio_status qio_server_poll(qio_server* server, int64_t request_id, int32_t* state, char** out_json);
+/* as poll, blocking until the request is done or failed (timeout_s < 0:
+ * no limit) */
+qio_status qio_server_wait(qio_server* server, int64_t request_id, double timeout_s, int32_t* state,
+                           char** out_json);
+/* drop a finished request's stored result */
+qio_status qio_server_forget(qio_server* server, int64_t request_id);
+/* the device footprint the server admits the request by */
+qio_status qio_server_request_bytes(qio_server* server, int64_t request_id, int64_t* bytes);
+qio_status qio_server_get_stats(qio_server* server, qio_server_stats* out);
+/* stops the worker; requests not yet finished are dropped */
+qio_status qio_server_destroy(qio_server* server);
+
 /* ---- runner ----------------------------------------------------------- */
 
 /* app::Runner::run (app/runner.cc:215-631): problem JSON + params JSON +

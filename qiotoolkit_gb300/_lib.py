@@ -50,6 +50,13 @@ class BatchStats(C.Structure):
                 ("sweep_kernel_ms", C.c_double)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("active", C.c_int64), ("pending", C.c_int64), ("used_bytes", C.c_int64),
+                ("budget_bytes", C.c_int64), ("peak_active", C.c_int64), ("elapsed_s", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double)]
+
+
 # every symbol include/qio_gb300.h declares, with its ctypes signature
 def _signatures():
     vp, i32, i64, dbl, cp = C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_char_p
@@ -84,6 +91,14 @@ def _signatures():
         "qio_batch_lowest": (st, [vp, P(dbl)]),
         "qio_batch_get_stats": (st, [vp, P(BatchStats)]),
         "qio_batch_destroy": (st, [vp]),
+        "qio_server_create": (st, [cp, P(vp)]),
+        "qio_server_submit": (st, [vp, vp, cp, cp, P(i64)]),
+        "qio_server_poll": (st, [vp, i64, P(i32), P(C.c_void_p)]),
+        "qio_server_wait": (st, [vp, i64, dbl, P(i32), P(C.c_void_p)]),
+        "qio_server_forget": (st, [vp, i64]),
+        "qio_server_request_bytes": (st, [vp, i64, P(i64)]),
+        "qio_server_get_stats": (st, [vp, P(ServerStats)]),
+        "qio_server_destroy": (st, [vp]),
         "qio_run_json": (st, [cp, cp, cp, P(C.c_void_p)]),
     }
 

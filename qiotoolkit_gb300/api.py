@@ -14,7 +14,7 @@ from typing import Iterable, Sequence
 
 import numpy as np
 
-from ._lib import ModelInfo, SolverStats, check, load
+from ._lib import ModelInfo, QioError, SolverStats, check, load
 
 KINDS = {"ising": 0, "ising_plain": 1, "pubo": 2, "pubo_plain": 3, "maxsat": 4}
 TARGETS = ("simulatedannealing.qiotoolkit", "paralleltempering.qiotoolkit",
@@ -266,5 +266,85 @@ class Batch:
         from ._lib import BatchStats
         st = BatchStats()
         check(load().qio_batch_get_stats(self._h, C.byref(st)))
+        return st
+
+
+class Server:
+    """Continuous batching of solve requests (qio_server_*): requests are
+    admitted by device footprint, solved resident on the device in
+    overlapping pieces, and retired when their sweeps are spent.  A result
+    equals Solver(model, target, params)'s for the same inputs."""
+
+    PENDING, RUNNING, DONE, FAILED = 0, 1, 2, 3
+
+    def __init__(self, memory_budget_bytes: int = 0, max_active: int = 64,
+                 sa_sweeps_per_piece: int = 64, pt_steps_per_piece: int = 16):
+        cfg = json.dumps({"memory_budget_bytes": memory_budget_bytes, "max_active": max_active,
+                          "sa_sweeps_per_piece": sa_sweeps_per_piece,
+                          "pt_steps_per_piece": pt_steps_per_piece})
+        h = C.c_void_p()
+        check(load().qio_server_create(cfg.encode(), C.byref(h)))
+        self._h = h
+        self._models = {}  # keep models alive until their requests finish
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().qio_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, model: Model, target: str, params: dict | str) -> int:
+        if not isinstance(params, str):
+            params = json.dumps(params if "params" in params else {"params": params})
+        rid = C.c_int64()
+        check(load().qio_server_submit(self._h, model._h, target.encode(), params.encode(),
+                                       C.byref(rid)))
+        self._models[rid.value] = model
+        return rid.value
+
+    def _finish(self, rid, state, p):
+        L = load()
+        text = None
+        if p.value:
+            try:
+                text = C.string_at(p).decode()
+            finally:
+                L.qio_free(p)
+        if state >= self.DONE:
+            self._models.pop(rid, None)
+        if state == self.DONE:
+            return json.loads(text)
+        if state == self.FAILED:
+            raise QioError(6, text or "request failed")
+        return None
+
+    def poll(self, rid: int):
+        """The result dict when done, None while pending or running."""
+        st, p = C.c_int32(), C.c_void_p()
+        check(load().qio_server_poll(self._h, rid, C.byref(st), C.byref(p)))
+        return self._finish(rid, st.value, p)
+
+    def wait(self, rid: int, timeout_s: float = -1.0):
+        st, p = C.c_int32(), C.c_void_p()
+        check(load().qio_server_wait(self._h, rid, float(timeout_s), C.byref(st), C.byref(p)))
+        return self._finish(rid, st.value, p)
+
+    def forget(self, rid: int):
+        check(load().qio_server_forget(self._h, rid))
+
+    def request_bytes(self, rid: int) -> int:
+        b = C.c_int64()
+        check(load().qio_server_request_bytes(self._h, rid, C.byref(b)))
+        return b.value
+
+    def stats(self):
+        from ._lib import ServerStats
+        st = ServerStats()
+        check(load().qio_server_get_stats(self._h, C.byref(st)))
         return st
 

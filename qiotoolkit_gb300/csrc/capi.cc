@@ -21,6 +21,10 @@ struct qio_batch
 {
   std::unique_ptr<Batch> b;
 };
+struct qio_server
+{
+  std::unique_ptr<Server> s;
+};
 
 static thread_local std::string g_last_error;
 
@@ -414,6 +418,110 @@ qio_status qio_batch_get_stats(const qio_batch* batch, qio_batch_stats* out)
 qio_status qio_batch_destroy(qio_batch* batch)
 {
   return guard([&] { delete batch; });
+}
+
+qio_status qio_server_create(const char* config_json, qio_server** out)
+{
+  return guard([&] {
+    if (!out) fail(1, "arguments must not be null");
+    *out = nullptr;
+    int64_t budget = 0, sa_piece = 64, pt_piece = 16;
+    int max_active = 64;
+    if (config_json && *config_json)
+    {
+      json::Value c = json::parse(config_json, strlen(config_json));
+      if (!c.is_object()) fail(1, "server configuration must be a JSON object");
+      auto num = [&](const char* k, double def) {
+        const json::Value* v = c.find(k);
+        if (!v || v->is_null()) return def;
+        if (!v->is_number()) fail(1, std::string("server configuration `") + k + "`: expected a number");
+        return v->num;
+      };
+      budget = (int64_t)num("memory_budget_bytes", 0);
+      max_active = (int)num("max_active", 64);
+      sa_piece = (int64_t)num("sa_sweeps_per_piece", 64);
+      pt_piece = (int64_t)num("pt_steps_per_piece", 16);
+    }
+    std::unique_ptr<qio_server> h(new qio_server());
+    h->s = make_server(budget, max_active, sa_piece, pt_piece);
+    *out = h.release();
+  });
+}
+
+qio_status qio_server_submit(qio_server* server, const qio_model* model, const char* target,
+                             const char* params_json, int64_t* request_id)
+{
+  return guard([&] {
+    if (!server || !model || !target || !params_json || !request_id) fail(1, "arguments must not be null");
+    json::Value doc = json::parse(params_json, strlen(params_json));
+    *request_id = server->s->submit(model->m.get(), target, doc);
+  });
+}
+
+static void server_out(int state, const std::string& text, int32_t* st, char** out)
+{
+  *st = state;
+  if (out) *out = (state >= 2) ? dup_string(text) : nullptr;
+}
+
+qio_status qio_server_poll(qio_server* server, int64_t request_id, int32_t* state, char** out_json)
+{
+  return guard([&] {
+    if (!server || !state) fail(1, "arguments must not be null");
+    std::string text;
+    server_out(server->s->poll(request_id, &text), text, state, out_json);
+  });
+}
+
+qio_status qio_server_wait(qio_server* server, int64_t request_id, double timeout_s, int32_t* state,
+                           char** out_json)
+{
+  return guard([&] {
+    if (!server || !state) fail(1, "arguments must not be null");
+    std::string text;
+    server_out(server->s->wait(request_id, timeout_s, &text), text, state, out_json);
+  });
+}
+
+qio_status qio_server_forget(qio_server* server, int64_t request_id)
+{
+  return guard([&] {
+    if (!server) fail(1, "server must not be null");
+    server->s->forget(request_id);
+  });
+}
+
+qio_status qio_server_request_bytes(qio_server* server, int64_t request_id, int64_t* bytes)
+{
+  return guard([&] {
+    if (!server || !bytes) fail(1, "arguments must not be null");
+    *bytes = server->s->request_bytes(request_id);
+  });
+}
+
+qio_status qio_server_get_stats(qio_server* server, qio_server_stats* out)
+{
+  return guard([&] {
+    if (!server || !out) fail(1, "arguments must not be null");
+    ServerStats st = server->s->stats();
+    out->submitted = st.submitted;
+    out->completed = st.completed;
+    out->failed = st.failed;
+    out->active = st.active;
+    out->pending = st.pending;
+    out->used_bytes = st.used_bytes;
+    out->budget_bytes = st.budget_bytes;
+    out->peak_active = st.peak_active;
+    out->elapsed_s = st.elapsed_s;
+    out->p50_ms = st.p50_ms;
+    out->p99_ms = st.p99_ms;
+    out->max_ms = st.max_ms;
+  });
+}
+
+qio_status qio_server_destroy(qio_server* server)
+{
+  return guard([&] { delete server; });
 }
 
 qio_status qio_run_json(const char* input_json, const char* params_json, const char* target,

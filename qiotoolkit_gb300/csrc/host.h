@@ -137,6 +137,12 @@ class Solver
   virtual bool historical_lowest(double&, std::vector<uint8_t>&) { return false; }
   virtual std::string target() const = 0;
   virtual uint64_t total_windows() { return 0; }
+  // Serving: the solve in pieces.  After init(), advance() enqueues up to n
+  // further steps on the stream and returns true once the step budget is
+  // spent (results are read after the stream has finished).  The pieces
+  // give the same trajectory as run().
+  virtual bool advance(cudaStream_t s, int64_t n);
+  int64_t step_pos = 0;
   std::string result_json();
   void best(double& cost, std::vector<uint8_t>& state);
 
@@ -215,4 +221,26 @@ class Batch
 };
 std::unique_ptr<Batch> make_batch(const std::vector<const HostModel*>& models, const std::string& target,
                                   const json::Value& params_doc);
+// Continuous batching of solve requests (serve.cc).
+struct ServerStats
+{
+  int64_t submitted = 0, completed = 0, failed = 0, active = 0, pending = 0;
+  int64_t used_bytes = 0, budget_bytes = 0, peak_active = 0;
+  double elapsed_s = 0, p50_ms = 0, p99_ms = 0, max_ms = 0;
+};
+class Server
+{
+ public:
+  virtual ~Server() {}
+  // validates params; the model must stay alive until the request finishes
+  virtual int64_t submit(const HostModel* m, const std::string& target, const json::Value& params_doc) = 0;
+  // 0 pending, 1 running, 2 done (out: result JSON), 3 failed (out: message)
+  virtual int poll(int64_t id, std::string* out) = 0;
+  virtual int wait(int64_t id, double timeout_s, std::string* out) = 0;
+  virtual void forget(int64_t id) = 0;
+  virtual int64_t request_bytes(int64_t id) = 0;  // device footprint used for admission
+  virtual ServerStats stats() = 0;
+};
+// budget_bytes <= 0: half of the device's free memory
+std::unique_ptr<Server> make_server(int64_t budget_bytes, int max_active, int64_t sa_piece, int64_t pt_piece);
 }  // namespace qio

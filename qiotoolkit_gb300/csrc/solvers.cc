@@ -137,6 +137,11 @@ static void configure_common(Solver& s, const json::Value& doc)
 
 void configure_common_public(Solver& s, const json::Value& doc) { configure_common(s, doc); }
 
+bool Solver::advance(cudaStream_t, int64_t)
+{
+  fail(1, "solver " + target() + " cannot run in pieces");
+}
+
 void Solver::prof_begin(cudaStream_t s)
 {
   if (!profile) return;
@@ -592,6 +597,35 @@ class SimulatedAnnealing : public Solver
     check_device_error(st);
   }
 
+  bool advance(cudaStream_t st, int64_t n) override
+  {
+    if (!initialized) fail(1, "init() must be called before advance()");
+    ran = true;
+    if (model->empty() || step_limit <= 0)
+    {
+      last_step = step_limit;
+      return true;
+    }
+    SweepArgs a = sweep_args();
+    LwArgs la = lanes ? lane_args() : LwArgs{};
+    if (lanes && step_pos == 0)
+    {
+      cuda_check(launch_lw_load(la, L.max_words, st), "lane load");
+      launches++;
+    }
+    const int64_t todo = std::min(n, step_limit - step_pos);
+    if (todo > 0) sweep_launch(a, la, pick_wpb(warps_per_block, a.n_streams), step_pos, todo, st);
+    step_pos += todo;
+    last_step = step_pos;
+    if (step_pos < step_limit) return false;
+    if (lanes)
+    {
+      cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
+      launches++;
+    }
+    return true;
+  }
+
   uint64_t total_windows() override { return sum_windows(P.pop, (int)n_walkers()); }
 
   void fetch(std::vector<double>& cost, std::vector<double>& lowest,
@@ -823,6 +857,65 @@ class ParallelTempering : public Solver
     unsigned long long nt = 0;
     cuda_check(cudaMemcpy(&nt, ties, 8, cudaMemcpyDeviceToHost), "D2H");
     near_ties = nt;
+  }
+
+  bool advance(cudaStream_t st, int64_t n) override
+  {
+    if (!initialized) fail(1, "init() must be called before advance()");
+    ran = true;
+    if (model->empty())
+    {
+      last_step = step_limit;
+      return true;
+    }
+    const int W = restarts * T();
+    SweepArgs a{};
+    a.m = model->device_view(full_maxsat_sweep);
+    a.p = P.pop;
+    a.n_streams = W;
+    a.n_walkers = W;
+    a.slot_of = P.slot_of;
+    a.beta = P.beta;
+    a.bs_w = 1;
+    a.bs_s = 0;
+    a.n_sweeps = (int)spr;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = T();
+    a.smem_state = smem_state ? 1 : 0;
+    a.err = device_error_flag();
+    SwapArgs sw{};
+    sw.restarts = restarts;
+    sw.n_temps = T();
+    sw.slot_of = P.slot_of;
+    sw.cost = P.pop.cost;
+    sw.beta = P.beta;
+    sw.dir = dir;
+    sw.step_acc_reset = P.pop.step_acc;
+    sw.step_att_reset = P.pop.step_att;
+    sw.obs_acc = obs_acc;
+    sw.obs_cost = obs_cost;
+    sw.obs_dir = obs_dir;
+    sw.swap_acc = swap_acc;
+    sw.swap_cnt = swap_cnt;
+    sw.near_ties = ties;
+    sw.replay = replay ? 1 : 0;
+    sw.master = master;
+    sw.swap_key = swap_key;
+    const int wpb = pick_wpb(warps_per_block, W);
+    const int64_t end = std::min(step_limit, step_pos + n);
+    for (; step_pos < end; step_pos++)
+    {
+      a.sweep_base = step_pos * spr;
+      cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+      sw.step = step_pos;
+      cuda_check(launch_pt_swap(sw, st), "swap kernel");
+      launches += 2;
+    }
+    last_step = step_pos;
+    return step_pos >= step_limit;
   }
 
   uint64_t total_windows() override { return sum_windows(P.pop, (int)n_walkers()); }
