@@ -42,6 +42,11 @@ WORKLOADS = {
     "pa_square": dict(desc="PA on 2D periodic 256x256 +-J Ising, R=4096, 100 beta steps 0->3.0, "
                            "10 sweeps per step, device-side multinomial resampling, counter streams",
                       target="populationannealing.cpu"),
+    "serving": dict(desc="Serving: Poisson arrivals at 200 req/s, 48 requests; kinds uniform over "
+                         "ER Ising (mean degree U[4,16], N(0,1) FP32), PUBO (orders U{1,2,3}, N(0,1), "
+                         "3 terms per variable), weighted 3-SAT (ratio 4.2, U[1,10]); N log-uniform "
+                         "[100, 1e4]; sweeps U{200..5000}; SA (8 restarts) or PT (8 temperatures)",
+                    target="mixed"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
@@ -289,6 +294,9 @@ def main():
     if args.workload == "batch_cubic":
         main_batch(args, ws, rank)
         return
+    if args.workload == "serving":
+        main_serving(args, ws, rank)
+        return
 
     import torch
     import qiotoolkit_gb300 as q
@@ -381,6 +389,121 @@ def main():
                          "peak_source": peak_src, "kernel": "sweep_kernel",
                          "bytes_per_attempt": bpa,
                          "avg_launch_ms": avg_sweep_launch_ms},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def serving_requests(n=48, rate=200.0, seed=4):
+    """Requests of the serving configuration (bounded sample: N up to 1e4)."""
+    import numpy as np
+    from qiotoolkit_gb300 import instances as I
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    out = []
+    for i in range(n):
+        kind = int(rng.integers(0, 3))
+        N = int(np.exp(rng.uniform(np.log(100), np.log(1e4))))
+        sweeps = int(rng.integers(200, 5001))
+        pt = bool(rng.integers(0, 2))
+        if kind == 0:
+            k, inst = "ising", I.er_ising_gauss(N, float(rng.uniform(4, 16)), seed=100 + i)
+        elif kind == 1:
+            k, inst = "pubo", I.random_pubo(N, 3 * N, seed=100 + i, orders=(1, 2, 3),
+                                            probs=(1 / 3, 1 / 3, 1 / 3))
+        else:
+            k, inst = "maxsat", I.weighted_maxsat(N, seed=100 + i)
+        if pt:
+            target = "paralleltempering.qiotoolkit"
+            params = {"seed": i, "sweeps": sweeps, "temperatures": {"type": "geometric", "initial": 0.1,
+                                                                    "final": 3.0, "count": 8}}
+        else:
+            target = "simulatedannealing.qiotoolkit"
+            params = {"seed": i, "sweeps": sweeps, "restarts": 8, "beta_start": 0.1, "beta_stop": 3.0}
+        out.append((float(t[i]), k, inst, target, params))
+    return out
+
+
+def main_serving(args, ws, rank):
+    """Continuous batching against the same request stream served one at a
+    time (a queue alone): instances/s, p50/p99 submit-to-done latency."""
+    import numpy as np
+    import torch
+    import qiotoolkit_gb300 as q
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    q.load()
+    reqs = serving_requests()
+    models = [q.Model(k, off=o, ids=i, coef=c) for _, k, (o, i, c), _, _ in reqs]
+
+    def attempts(m, target, p):
+        w = 8
+        per = m.n_vars if m.info.kind != 4 else 1  # MaxSat: one attempt per sweep
+        return w * p["sweeps"] * per
+
+    n_att = sum(attempts(m, t, p) for m, (_, _, _, t, p) in zip(models, reqs))
+
+    def serve(max_active):
+        srv = q.Server(max_active=max_active)
+        t0 = time.perf_counter()
+        ids = []
+        for m, (ta, _, _, target, p) in zip(models, reqs):
+            d = t0 + ta - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            ids.append(srv.submit(m, target, {"params": p}))
+        best = [srv.wait(i)["solutions"]["cost"] for i in ids]
+        dt = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        return dt, st, best
+
+    serve(64)  # warm-up: module loading, table uploads
+    with ClockSampler(local) as clk:
+        dt_mix, st_mix, best_mix = serve(64)
+    dt_one, st_one, best_one = serve(1)
+    same = best_mix == best_one
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        t_cpu, a_cpu = 0.0, 0
+        for j in range(0, len(reqs), 6):
+            _, k, (o, i, c), target, p = reqs[j]
+            om = O.Model(k, off=o, ids=i, coef=c)
+            t0 = time.perf_counter()
+            if target.startswith("parallel"):
+                O.run(om, "pt", seed=p["seed"], step_limit=p["sweeps"], threads=threads,
+                      sched=("geometric", 0.1, 3.0), sched_count=8, use_inverse=False)
+            else:
+                O.run(om, "sa", seed=p["seed"], step_limit=p["sweeps"], restarts=8, threads=threads,
+                      sched=("linear", 0.1, 3.0))
+            t_cpu += time.perf_counter() - t0
+            a_cpu += attempts(models[j], target, p)
+        rate = a_cpu / t_cpu
+        cpu = {"value": len(reqs) / (n_att / rate), "unit": "instances/s", "cores": threads,
+               "kind": "port",
+               "sample": f"oracle on every 6th request ({a_cpu:.3g} attempts in {t_cpu:.1f} s), "
+                         f"requests one after another, extrapolated by attempts"}
+    if rank == 0:
+        line = {
+            "metric": "instances/s served; p50/p99 solve latency", "value": len(reqs) / dt_mix,
+            "unit": "instances/s", "n_gpus": ws, "steps": 1, "warmup": 1,
+            "ms_per_step": dt_mix * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS["serving"]["desc"], "requests": len(reqs),
+                       "attempts": n_att, "max_active": 64},
+            "latency_ms": {"p50": st_mix.p50_ms, "p99": st_mix.p99_ms, "max": st_mix.max_ms},
+            "attempts_per_s": n_att / dt_mix,
+            "peak_active": int(st_mix.peak_active),
+            "queue_alone": {"value": len(reqs) / dt_one, "unit": "instances/s",
+                            "latency_ms": {"p50": st_one.p50_ms, "p99": st_one.p99_ms}},
+            "speedup_vs_queue_alone": dt_one / dt_mix,
+            "same_results_alone_and_in_mix": bool(same),
+            "e2e": {"value": len(reqs) / dt_mix, "unit": "instances/s",
+                    "h2d_bytes_per_step": int(sum(m.info.device_bytes for m in models)),
+                    "d2h_bytes_per_step": int(sum(8 * m.n_vars for m in models))},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

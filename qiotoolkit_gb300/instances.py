@@ -101,3 +101,24 @@ def to_json(kind, off, ids, coef) -> str:
     terms = [{"c": float(coef[t]), "ids": [int(x) for x in ids[off[t]:off[t + 1]]]}
              for t in range(len(coef))]
     return json.dumps({"cost_function": {"type": kind, "version": "1.0", "terms": terms}})
+
+
+def er_ising_gauss(n, mean_degree, seed=0):
+    """Sparse Erdos-Renyi Ising model: round(n * mean_degree / 2) distinct
+    couplings with N(0,1) weights rounded to FP32 (no fields)."""
+    rng = np.random.default_rng(seed)
+    m = int(round(n * mean_degree / 2))
+    edges = set()
+    while len(edges) < m:
+        a = rng.integers(0, n, 2 * (m - len(edges)) + 8)
+        b = rng.integers(0, n, a.size)
+        for x, y in zip(a.tolist(), b.tolist()):
+            if x != y:
+                edges.add((min(x, y), max(x, y)))
+                if len(edges) == m:
+                    break
+    edges = sorted(edges)
+    ids = [[a, b] for a, b in edges]
+    coef = rng.standard_normal(m).astype(np.float32).astype(np.float64)
+    return _pack(ids, coef)
+
