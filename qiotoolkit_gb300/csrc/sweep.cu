@@ -409,6 +409,10 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
 
   int cursor = 0;
   bool pending = false;  // the last round flipped something: marks may be set
+  unsigned blk_flips = 0;  // committed flips of the block
+  long long fidE = 0;      // a flipped lane's difference (integer mode)
+  double fdE = 0.0;        // ... FP64, exact when fexact
+  bool fexact = false;
   while (cursor < nvalid)
   {
     const bool active = valid && lane >= cursor;
@@ -552,9 +556,10 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
     if constexpr (!INT)
     {
-      // Exact differences for the lanes that may be committed: up to the
-      // first stop under the surely accepted lanes (more acceptances can
-      // only move the stop earlier).
+      // Exact differences for the lanes inside the LUT margin that may be
+      // committed: up to the first stop under the surely accepted lanes
+      // (more acceptances can only move the stop earlier).  Committed flips
+      // get theirs at the end of the block.
       const bool sure = active && (!uphill || (!redraw && dec == 1));
       const unsigned As = __ballot_sync(kFull, sure);
       bool cs = false;
@@ -562,7 +567,7 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
         cs = (nb & (__brev(As) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
       const unsigned stop_s = __ballot_sync(kFull, cs) | Rm;
       const int fs = stop_s ? (__ffs(stop_s) - 1) : 32;
-      const bool cand = active && lane <= fs && !have_exact && (!uphill || redraw || dec != 0);
+      const bool cand = active && lane <= fs && !have_exact && uphill && !redraw && dec < 0;
       if (__any_sync(kFull, cand))
       {
         const double ex = exact_dE<FL>(cand, qm, sm, pcoef);
@@ -593,6 +598,19 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     if (REPLAY && slow)
     {
       // lane f drew a zero bucket: its redraw chain (markov/metropolis.h:93-103)
+      if constexpr (!INT)
+      {
+        const bool nx = lane == f && !have_exact;
+        if (__any_sync(kFull, nx))
+        {
+          const double ex = exact_dE<FL>(nx, qm, sm, pcoef);
+          if (nx)
+          {
+            dE = ex;
+            have_exact = true;
+          }
+        }
+      }
       int sacc = 0, used = 0;
       if (lane == f)
       {
@@ -627,6 +645,14 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     }
     const int adv = f + (slow ? 1 : 0) - cursor;
     const bool mine = ((flips >> lane) & 1u) != 0u;
+    if (mine)
+    {
+      // a committed lane keeps its masks: its exact difference can wait
+      // for the end of the block
+      fidE = idE;
+      fdE = dE;
+      fexact = INT || have_exact;
+    }
 
     // ---- apply: the flips' incidences spread over the warp; term bytes
     // change by atomics (different terms may share a word), and each
@@ -678,89 +704,94 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     }
     const int wi = i0 >> 5;
     if (lane == 0 && flips) spins[wi] ^= flips;
-    // ---- running cost and lowest state, in attempt order --------------
-    int lowpos = -1;
-    if (INT)
-    {
-      if (flips)
-      {
-        if (m.scan32)
-        {
-          const int d = mine ? (int)idE : 0;
-          const int dsum = __reduce_add_sync(kFull, d);
-          const int negsum = __reduce_add_sync(kFull, d < 0 ? d : 0);
-          // the lowest prefix cost is at least icost + negsum
-          if ((long long)negsum < W.ilow - W.icost)
-          {
-            const int pre = warp_scan32(d, lane);
-            const int mn = __reduce_min_sync(kFull, mine ? pre : INT_MAX);
-            if ((long long)mn < W.ilow - W.icost)
-            {
-              lowpos = __ffs(__ballot_sync(kFull, mine && pre == mn)) - 1;
-              W.ilow = W.icost + mn;
-            }
-          }
-          W.icost += dsum;
-        }
-        else
-        {
-          const long long pre = warp_scan64(mine ? idE : 0LL, lane);
-          const long long ci = W.icost + pre;
-          long long mn = mine ? ci : LLONG_MAX;
-#pragma unroll
-          for (int d = 16; d; d >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, d));
-          if (mn < W.ilow)
-          {
-            lowpos = __ffs(__ballot_sync(kFull, mine && ci == mn)) - 1;
-            W.ilow = mn;
-          }
-          W.icost += __shfl_sync(kFull, pre, 31);
-        }
-      }
-    }
-    else
-    {
-      unsigned fl = flips;
-      if (fl)
-      {
-        int j = __ffs(fl) - 1;
-        fl &= fl - 1;
-        double d = __shfl_sync(kFull, dE, j);
-        while (true)
-        {
-          const int jn = fl ? (__ffs(fl) - 1) : j;
-          const double dn = __shfl_sync(kFull, dE, jn);  // ahead of the dependent add
-          W.cost = __dadd_rn(W.cost, d);
-          const long long kc = order_key(W.cost);
-          if (kc < W.klow)
-          {
-            W.klow = kc;
-            W.low = W.cost;
-            lowpos = j;
-          }
-          if (!fl) break;
-          fl &= fl - 1;
-          j = jn;
-          d = dn;
-        }
-      }
-    }
-    __syncwarp();
-    if (lowpos >= 0)
-    {
-      for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
-      __syncwarp();
-      const unsigned undo = flips & ~((2u << lowpos) - 1u);
-      if (lane == 0 && undo) lsp[wi] ^= undo;
-      __syncwarp();
-    }
     W.natt += (unsigned long long)adv;
     W.nacc += (unsigned long long)__popc(flips);
     W.nwin++;
     if (REPLAY) W.rs = S.jA[draws] * W.rs + S.jC[draws];
     cursor += adv;
+    blk_flips |= flips;
   }
   __syncwarp();
+
+  // ---- running cost and lowest state over the block's flips, in attempt
+  // order (they are in lane order) -----------------------------------------
+  if (blk_flips == 0u) return;
+  const bool fl_mine = ((blk_flips >> lane) & 1u) != 0u;
+  int lowpos = -1;
+  if constexpr (INT)
+  {
+    if (m.scan32)
+    {
+      const int d = fl_mine ? (int)fidE : 0;
+      const int dsum = __reduce_add_sync(kFull, d);
+      const int negsum = __reduce_add_sync(kFull, d < 0 ? d : 0);
+      // the lowest prefix cost is at least icost + negsum
+      if ((long long)negsum < W.ilow - W.icost)
+      {
+        const int pre = warp_scan32(d, lane);
+        const int mn = __reduce_min_sync(kFull, fl_mine ? pre : INT_MAX);
+        if ((long long)mn < W.ilow - W.icost)
+        {
+          lowpos = __ffs(__ballot_sync(kFull, fl_mine && pre == mn)) - 1;
+          W.ilow = W.icost + mn;
+        }
+      }
+      W.icost += dsum;
+    }
+    else
+    {
+      const long long pre = warp_scan64(fl_mine ? fidE : 0LL, lane);
+      const long long ci = W.icost + pre;
+      long long mn = fl_mine ? ci : LLONG_MAX;
+#pragma unroll
+      for (int d = 16; d; d >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, d));
+      if (mn < W.ilow)
+      {
+        lowpos = __ffs(__ballot_sync(kFull, fl_mine && ci == mn)) - 1;
+        W.ilow = mn;
+      }
+      W.icost += __shfl_sync(kFull, pre, 31);
+    }
+  }
+  else
+  {
+    const bool nx = fl_mine && !fexact;
+    if (__any_sync(kFull, nx))
+    {
+      const double ex = exact_dE<FL>(nx, qm, sm, pcoef);
+      if (nx) fdE = ex;
+    }
+    unsigned fl = blk_flips;
+    int j = __ffs(fl) - 1;
+    fl &= fl - 1;
+    double d = __shfl_sync(kFull, fdE, j);
+    while (true)
+    {
+      const int jn = fl ? (__ffs(fl) - 1) : j;
+      const double dn = __shfl_sync(kFull, fdE, jn);  // ahead of the dependent add
+      W.cost = __dadd_rn(W.cost, d);
+      const long long kc = order_key(W.cost);
+      if (kc < W.klow)
+      {
+        W.klow = kc;
+        W.low = W.cost;
+        lowpos = j;
+      }
+      if (!fl) break;
+      fl &= fl - 1;
+      j = jn;
+      d = dn;
+    }
+  }
+  if (lowpos >= 0)
+  {
+    // the state at the last improvement: the block's later flips undone
+    for (int q = lane; q < nwd; q += 32) lsp[q] = spins[q];
+    __syncwarp();
+    const unsigned undo = blk_flips & ~((2u << lowpos) - 1u);
+    if (lane == 0 && undo) lsp[i0 >> 5] ^= undo;
+    __syncwarp();
+  }
 }
 
 // Counter-free models (model::Ising, model::Pubo): the cost difference
