@@ -658,12 +658,47 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     // change by atomics (different terms may share a word), and each
     // incidence marks the later co-members of its term ----------------------
     pending = flips != 0u;
-    if (pending)
+    // apply: term bytes change by atomics (different terms may share a
+    // word) and each incidence marks the later co-members of its term
+    auto apply_one = [&](int j, int kk, uint32_t svj) {
+      const uint32_t e = INC(kk);
+      const unsigned long long nw = NEAR(kk);
+      const uint32_t t = e & ~kNegBit;
+      const unsigned sh = (t & 3u) << 3;
+      if (FL == F_PARITY) atomicXor(ts32 + (t >> 2), 1u << sh);
+      else atomicAdd(ts32 + (t >> 2), ((svj ^ (e >> 31)) & 1u) ? (0u - (1u << sh)) : (1u << sh));
+      const int cnt = (int)(nw >> 61);
+      if (cnt == 7) atomicOr(dirty + 32, 1u);
+      else
+        for (int i = 0; i < cnt; i++)
+        {
+          const int u = j + (int)((nw >> (10 * i)) & 31u);
+          if (u < 32) atomicOr(dirty + u, 1u << (unsigned)((nw >> (10 * i + 5)) & 31u));
+        }
+    };
+    if (__popc(flips) <= 2)
     {
+      // few flips: one flipping lane at a time, the warp over its incidences
+      unsigned fl = flips;
+      while (fl)
+      {
+        const int j = __ffs(fl) - 1;
+        fl &= fl - 1;
+        const int dj = __shfl_sync(kFull, deg, j);
+        const int rj = __shfl_sync(kFull, rb, j);
+        const uint32_t svj = __shfl_sync(kFull, sv, j);
+        for (int k0 = 0; k0 < dj; k0 += 32)
+          if (k0 + lane < dj) apply_one(j, k0 + lane + (rj - rb), svj);
+      }
+    }
+    else
+    {
+      // many flips: their incidences laid out back to back over the warp
       const int mydeg = mine ? deg : 0;
       const int incl = warp_scan32(mydeg, lane);
       const int excl = incl - mydeg;
       const int total = __shfl_sync(kFull, incl, 31);
+      const unsigned F = __ballot_sync(kFull, mine && mydeg > 0);
       for (int base = 0; base < total; base += 32)
       {
         // start positions of the flips' runs inside this chunk
@@ -672,9 +707,8 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
         const int nbefore = __popc(__ballot_sync(kFull, mine && mydeg > 0 && rel < 0));
         const int g = base + lane;
         const int idx = nbefore + __popc(starts & ((2u << lane) - 1u)) - 1;
-        // idx-th flipping lane with a non-empty row
-        const unsigned F = __ballot_sync(kFull, mine && mydeg > 0);
-        // smallest j with popc(F & bits 0..j) > idx
+        // the idx-th flipping lane with a non-empty row: smallest j with
+        // popc(F & bits 0..j) > idx
         int j = 0;
 #pragma unroll
         for (int step = 16; step; step >>= 1)
@@ -682,24 +716,7 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
         const int ej = __shfl_sync(kFull, excl, j & 31);
         const int rj = __shfl_sync(kFull, rb, j & 31);
         const uint32_t svj = __shfl_sync(kFull, sv, j & 31);
-        if (g < total)
-        {
-          const int k = g - ej + (rj - rb);  // position relative to this lane's row
-          const uint32_t e = INC(k);
-          const unsigned long long nw = NEAR(k);
-          const uint32_t t = e & ~kNegBit;
-          const unsigned sh = (t & 3u) << 3;
-          if (FL == F_PARITY) atomicXor(ts32 + (t >> 2), 1u << sh);
-          else atomicAdd(ts32 + (t >> 2), ((svj ^ (e >> 31)) & 1u) ? (0u - (1u << sh)) : (1u << sh));
-          const int cnt = (int)(nw >> 61);
-          if (cnt == 7) atomicOr(dirty + 32, 1u);
-          else
-            for (int i = 0; i < cnt; i++)
-            {
-              const int u = j + (int)((nw >> (10 * i)) & 31u);
-              if (u < 32) atomicOr(dirty + u, 1u << (unsigned)((nw >> (10 * i + 5)) & 31u));
-            }
-        }
+        if (g < total) apply_one(j, g - ej + (rj - rb), svj);
       }
     }
     const int wi = i0 >> 5;
