@@ -352,53 +352,60 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     nops = deg;
   };
   // re-read the marked incidences and correct the field
+  auto fix = [&](int k, uint32_t e, uint32_t z) {
+    if (FL == F_PARITY)
+    {
+      if (z != ((sm >> k) & 1u))
+      {
+        sm ^= 1u << k;
+        if (INT)
+        {
+          const int c = (int)COEF(k);
+          ifield += z ? -2 * c : 2 * c;
+        }
+        else
+        {
+          const float c = CF(k);
+          ffield = __fadd_rn(ffield, z ? -2.f * c : 2.f * c);
+          nops += 2;
+        }
+      }
+    }
+    else
+    {
+      const uint32_t lit = (sm >> k) & 1u;
+      const uint32_t qual = lit ? (z == 1u) : (z == 0u);
+      if (qual != ((qm >> k) & 1u))
+      {
+        qm ^= 1u << k;
+        if (INT)
+        {
+          const int c = (int)COEF(k);
+          const int d = lit ? c : -c;
+          ifield += qual ? d : -d;
+        }
+        else
+        {
+          const float c = CF(k);
+          const float d = lit ? c : -c;
+          ffield = __fadd_rn(ffield, qual ? d : -d);
+          nops += 2;
+        }
+      }
+    }
+  };
   auto refresh = [&](uint32_t dm) {
     while (dm)
     {
-      const int k = __ffs(dm) - 1;
+      // two marked incidences at a time: their loads overlap
+      const int k1 = __ffs(dm) - 1;
       dm &= dm - 1;
-      const uint32_t e = INC(k);
-      const uint32_t z = ts[e & ~kNegBit];
-      if (FL == F_PARITY)
-      {
-        if (z != ((sm >> k) & 1u))
-        {
-          sm ^= 1u << k;
-          if (INT)
-          {
-            const int c = (int)COEF(k);
-            ifield += z ? -2 * c : 2 * c;
-          }
-          else
-          {
-            const float c = CF(k);
-            ffield = __fadd_rn(ffield, z ? -2.f * c : 2.f * c);
-            nops += 2;
-          }
-        }
-      }
-      else
-      {
-        const uint32_t lit = (sm >> k) & 1u;
-        const uint32_t qual = lit ? (z == 1u) : (z == 0u);
-        if (qual != ((qm >> k) & 1u))
-        {
-          qm ^= 1u << k;
-          if (INT)
-          {
-            const int c = (int)COEF(k);
-            const int d = lit ? c : -c;
-            ifield += qual ? d : -d;
-          }
-          else
-          {
-            const float c = CF(k);
-            const float d = lit ? c : -c;
-            ffield = __fadd_rn(ffield, qual ? d : -d);
-            nops += 2;
-          }
-        }
-      }
+      const int k2 = dm ? __ffs(dm) - 1 : k1;
+      dm &= dm - 1;
+      const uint32_t e1 = INC(k1), e2 = INC(k2);
+      const uint32_t z1 = ts[e1 & ~kNegBit], z2 = ts[e2 & ~kNegBit];
+      fix(k1, e1, z1);
+      if (k2 != k1) fix(k2, e2, z2);
     }
   };
 
@@ -556,28 +563,31 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
     if constexpr (!INT)
     {
-      // Exact differences for the lanes inside the LUT margin that may be
-      // committed: up to the first stop under the surely accepted lanes
-      // (more acceptances can only move the stop earlier).  Committed flips
-      // get theirs at the end of the block.
-      const bool sure = active && (!uphill || (!redraw && dec == 1));
-      const unsigned As = __ballot_sync(kFull, sure);
-      bool cs = false;
-      if (active && lane > cursor)
-        cs = (nb & (__brev(As) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
-      const unsigned stop_s = __ballot_sync(kFull, cs) | Rm;
-      const int fs = stop_s ? (__ffs(stop_s) - 1) : 32;
-      const bool cand = active && lane <= fs && !have_exact && uphill && !redraw && dec < 0;
-      if (__any_sync(kFull, cand))
+      if (__any_sync(kFull, uphill && !redraw && dec < 0))
       {
-        const double ex = exact_dE<FL>(cand, qm, sm, pcoef);
-        if (cand)
+        // Exact differences for the lanes inside the LUT margin that may be
+        // committed: up to the first stop under the surely accepted lanes
+        // (more acceptances can only move the stop earlier).  Committed flips
+        // get theirs at the end of the block.
+        const bool sure = active && (!uphill || (!redraw && dec == 1));
+        const unsigned As = __ballot_sync(kFull, sure);
+        bool cs = false;
+        if (active && lane > cursor)
+          cs = (nb & (__brev(As) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+        const unsigned stop_s = __ballot_sync(kFull, cs) | Rm;
+        const int fs = stop_s ? (__ffs(stop_s) - 1) : 32;
+        const bool cand = active && lane <= fs && !have_exact && uphill && !redraw && dec < 0;
+        if (__any_sync(kFull, cand))
         {
-          dE = ex;
-          have_exact = true;
+          const double ex = exact_dE<FL>(cand, qm, sm, pcoef);
+          if (cand)
+          {
+            dE = ex;
+            have_exact = true;
+          }
         }
+        if (lane > fs && dec < 0) dec = 0;  // cannot be committed this round
       }
-      if (lane > fs && dec < 0) dec = 0;  // cannot be committed this round
     }
     // lanes inside the screen's margin: exact comparison
     if (uphill && !redraw && dec < 0)
