@@ -152,8 +152,9 @@ __device__ __forceinline__ void term_value(const DevModel& m,
   }
 }
 
-// Sum of term values in term order by one warp: lanes evaluate 32 terms in
-// parallel, the sum itself runs sequentially (bit-identical to a loop).
+// Sum of term values by one warp: lanes evaluate 32 terms in parallel; the
+// FP64 sum runs sequentially in term order (bit-identical to a loop), the
+// integer sum (exact in any order) as per-lane partial sums and a reduction.
 template <int FL, bool INT>
 __device__ void warp_cost(const DevModel& m, const uint32_t* spins, int lane,
                           double& cost, long long& icost)
@@ -167,14 +168,24 @@ __device__ void warp_cost(const DevModel& m, const uint32_t* spins, int lane,
     long long iv = 0;
     bool skip = true;
     if (t < m.n_terms) term_value<FL, INT>(m, spins, t, v, iv, skip);
+    if (INT)
+    {
+      // integer sums are exact in any order: per-lane partial sums
+      if (!skip) ic += iv;
+      continue;
+    }
     unsigned keep = __ballot_sync(kFull, !skip);
     while (keep)
     {
       int j = __ffs(keep) - 1;
       keep &= keep - 1;
-      if (INT) ic += __shfl_sync(kFull, iv, j);
-      else c = __dadd_rn(c, __shfl_sync(kFull, v, j));
+      c = __dadd_rn(c, __shfl_sync(kFull, v, j));
     }
+  }
+  if (INT)
+  {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) ic += __shfl_xor_sync(kFull, ic, d);
   }
   cost = c;
   icost = ic;
