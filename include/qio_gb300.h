@@ -111,6 +111,11 @@ qio_status qio_model_create(int32_t kind, int64_t n_terms,
 qio_status qio_model_create_json(const char* input_json, int32_t kind,
                                  qio_model** out);
 
+/* MaxSAT model from DIMACS cnf / wcnf text (utils/dimacs.cc, read by
+ * app/runner.cc:87-89 into model::MaxSat): the same accepted input and
+ * error messages. */
+qio_status qio_model_create_dimacs(const char* text, qio_model** out);
+
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out);
 /* Original variable name of each internal variable (Graph::output_map,
  * graph/graph.h:407-413; MaxSat variable_names_, model/max_sat.h:596). */

@@ -66,6 +66,13 @@ class Model:
         check(load().qio_model_create_json(doc.encode(), int(kind), C.byref(h)))
         return cls(None, _handle=h)
 
+    @classmethod
+    def from_dimacs(cls, text: str) -> "Model":
+        """MaxSAT model from DIMACS cnf / wcnf text."""
+        h = C.c_void_p()
+        check(load().qio_model_create_dimacs(text.encode(), C.byref(h)))
+        return cls(None, _handle=h)
+
     def close(self):
         if getattr(self, "_h", None):
             load().qio_model_destroy(self._h)

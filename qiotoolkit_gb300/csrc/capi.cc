@@ -95,6 +95,17 @@ qio_status qio_model_create_json(const char* input_json, int32_t kind, qio_model
   });
 }
 
+qio_status qio_model_create_dimacs(const char* text, qio_model** out)
+{
+  return guard([&] {
+    if (!out || !text) fail(1, "arguments must not be null");
+    *out = nullptr;
+    std::unique_ptr<qio_model> h(new qio_model());
+    h->m = build_model_dimacs(std::string(text));
+    *out = h.release();
+  });
+}
+
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out)
 {
   return guard([&] {

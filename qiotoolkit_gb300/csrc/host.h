@@ -96,6 +96,8 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
                                        const int64_t* off, const int32_t* ids,
                                        const double* coef);
 std::unique_ptr<HostModel> build_model_json(const json::Value& doc, int kind);
+// DIMACS cnf / wcnf text -> MaxSat model (dimacs.cc)
+std::unique_ptr<HostModel> build_model_dimacs(const std::string& text);
 
 // Schedule (schedule/schedule.cc, linear.cc, geometric.cc, segments.cc).
 struct Schedule

@@ -17,6 +17,7 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
                      with their data/ inputs and data/params1.json
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
+  dimacs_pins.json   utils/test/dimacs_test.cc (inputs and expected parses)
 
 Expected values are parsed from the test sources where they are plain
 literals (EXPECT_* and ElementsAre lines), so a change in the reference shows
@@ -178,13 +179,46 @@ def planted():
     return {"source": "data/input_e2e_pipeline/*/energies.json", "instances": out}
 
 
+def dimacs_pins():
+    """Each TEST(Dimacs, ...) block: the input text and the expected type,
+    counts, variables, clauses (literals, weights) and top."""
+    src = read("utils/test/dimacs_test.cc")
+    cases = []
+    for m in re.finditer(r'TEST\(Dimacs, (\w+)\)\s*\{(.*?)\n\}', src, re.S):
+        name, body = m.group(1), m.group(2)
+        t = re.search(r'read\(R"\((.*?)\)"\);', body, re.S)
+        if not t:
+            continue
+        case = {"name": name, "text": t.group(1), "clauses": {}, "weights": {}}
+        for e in re.finditer(r'EXPECT_EQ\((.*?), (.*?)\);', body):
+            lhs, rhs = e.group(1).strip(), e.group(2).strip()
+            if "get_type" in lhs:
+                case["type"] = rhs.strip('"')
+            elif "get_nvar" in lhs:
+                case["nvar"] = int(rhs)
+            elif "get_ncl" in lhs:
+                case["ncl"] = int(rhs)
+            elif "get_top" in lhs:
+                case["top"] = float(rhs)
+            elif "get_variables" in lhs:
+                case["variables"] = [int(x) for x in re.findall(r'-?\d+', rhs)]
+            else:
+                c = re.match(r'clauses\[(\d+)\]\.(variables|weight)', lhs)
+                if c and c.group(2) == "variables":
+                    case["clauses"][c.group(1)] = [int(x) for x in re.findall(r'-?\d+', rhs)]
+                elif c:
+                    case["weights"][c.group(1)] = float(rhs)
+        cases.append(case)
+    return {"source": "utils/test/dimacs_test.cc", "cases": cases}
+
+
 def main():
     if not os.path.isdir(CPP):
         print("reference not found at", REFERENCE, file=sys.stderr)
         sys.exit(1)
     files = {"rng_pins.json": rng_pins(), "pt_toy_pin.json": pt_toy_pin(),
              "model_pins.json": model_pins(), "solver_pins.json": solver_pins(),
-             "planted.json": planted()}
+             "planted.json": planted(), "dimacs_pins.json": dimacs_pins()}
     for name, obj in files.items():
         with open(os.path.join(OUT, name), "w") as f:
             json.dump(obj, f, separators=(",", ":"))

@@ -121,3 +121,24 @@ def test_edge_pt(name):
     s = q.Solver(g, PT, {"params": {"seed": 8, "sweeps": 25, "all_betas": temps}}).init().run()
     r = O.run(o, "pt", seed=8, step_limit=25, sched=("list", 0, 0), sched_values=temps, threads=4)
     _same(s.replicas(), r)
+
+
+def test_dimacs_model_solves_like_term_lists():
+    from qiotoolkit_gb300 import instances as I
+    off, ids, coef = I.weighted_maxsat(60, seed=71)
+    lines = [f"p wcnf 60 {len(coef)}"]
+    for k in range(len(coef)):
+        lits = " ".join(str(int(x)) for x in ids[off[k]:off[k + 1]])
+        lines.append(f"{coef[k]!r} {lits} 0")
+    text = "\n".join(lines) + "\n"
+    d = q.Model.from_dimacs(text)
+    g = q.Model("maxsat", off=off, ids=ids, coef=coef)
+    o = O.Model("maxsat", off=off, ids=ids, coef=coef)
+    params = {"seed": 5, "sweeps": 50, "restarts": 4, "beta_start": 0.1, "beta_stop": 2.0,
+              "maxsat_full_sweep": True}
+    rd = q.Solver(d, SA, {"params": params}).init().run()
+    rg = q.Solver(g, SA, {"params": params}).init().run()
+    assert rd.result()["solutions"] == rg.result()["solutions"]
+    r = O.run(o, "sa", seed=5, step_limit=50, restarts=4, sched=("linear", 0.1, 2.0), threads=4,
+              full_maxsat_sweep=True)
+    _same(rd.replicas(), r)
