@@ -129,7 +129,7 @@ def test_dimacs_model_solves_like_term_lists():
     lines = [f"p wcnf 60 {len(coef)}"]
     for k in range(len(coef)):
         lits = " ".join(str(int(x)) for x in ids[off[k]:off[k + 1]])
-        lines.append(f"{coef[k]!r} {lits} 0")
+        lines.append(f"{float(coef[k])!r} {lits} 0")
     text = "\n".join(lines) + "\n"
     d = q.Model.from_dimacs(text)
     g = q.Model("maxsat", off=off, ids=ids, coef=coef)
