@@ -65,6 +65,7 @@ struct HostModel
   // one-member term points at the padding spin n_words * 32 (always 0)
   std::vector<int> rec_i;     // 2 ints per incidence (integer mode)
   std::vector<double> rec_f;  // 2 doubles per incidence: (other as bits, coef)
+  std::vector<unsigned int> rec_p;  // other << 8 | coefficient, when |coef| <= 127
   std::vector<uint32_t> nbr;
   // term -> members
   std::vector<int> trow;

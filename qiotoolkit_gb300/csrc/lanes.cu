@@ -55,27 +55,48 @@ __device__ __forceinline__ bool lut_accept(const double* ln, const float* scr, u
 // SMEM: the group's current spin words live in shared memory for the launch
 // (copied in at the start, out at the end); the lowest words stay in global
 // memory.  Tables in the block's first 20 KB, group words after them.
-// per incidence record: (other member or the padding spin, coefficient)
-template <bool INT>
+// per incidence record: (other member or the padding spin, coefficient), as
+// int2, packed into 32 bits (other << 8 | 8-bit coefficient) when every
+// coefficient fits, or as double2 (other's bits in x) for FP64 models
+enum RecKind
+{
+  RK_INT2 = 0,
+  RK_PACK = 1,
+  RK_F64 = 2
+};
+template <int RK>
 struct Rec;
 template <>
-struct Rec<true>
+struct Rec<RK_INT2>
 {
   using T = int2;
-  static __device__ __forceinline__ int other(const int2& r) { return r.x; }
+  static __device__ __forceinline__ int other(const T& r) { return r.x; }
+  static __device__ __forceinline__ int icoef(const T& r) { return r.y; }
+  static __device__ __forceinline__ double dcoef(const T& r) { return (double)r.y; }
 };
 template <>
-struct Rec<false>
+struct Rec<RK_PACK>
+{
+  using T = unsigned int;
+  static __device__ __forceinline__ int other(const T& r) { return (int)(r >> 8); }
+  static __device__ __forceinline__ int icoef(const T& r) { return (int)(signed char)(r & 0xFFu); }
+  static __device__ __forceinline__ double dcoef(const T& r) { return (double)icoef(r); }
+};
+template <>
+struct Rec<RK_F64>
 {
   using T = double2;
-  static __device__ __forceinline__ int other(const double2& r) { return (int)__double_as_longlong(r.x); }
+  static __device__ __forceinline__ int other(const T& r) { return (int)__double_as_longlong(r.x); }
+  static __device__ __forceinline__ int icoef(const T&) { return 0; }
+  static __device__ __forceinline__ double dcoef(const T& r) { return r.y; }
 };
 static const int kPre = 8;  // records of the next variable loaded one attempt ahead
 
-template <bool REPLAY, bool INT, bool SMEM>
+template <bool REPLAY, int RK, bool SMEM>
 __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
 {
-  using R = typename Rec<INT>::T;
+  constexpr bool INT = RK != RK_F64;
+  using R = typename Rec<RK>::T;
   extern __shared__ __align__(16) unsigned char lw_smem[];
   const double* s_ln = g_ln;
   const float* s_scr = g_scr;
@@ -87,7 +108,8 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
   const int smem_words = a.smem_words;
   const DevModel* md = a.models + (a.model_of ? a.model_of[r] : 0);
   const int* __restrict__ row = md->row;
-  const R* __restrict__ rec = INT ? (const R*)md->rec_i : (const R*)md->rec_f;
+  const R* __restrict__ rec = RK == RK_PACK ? (const R*)md->rec_p
+                              : (RK == RK_INT2 ? (const R*)md->rec_i : (const R*)md->rec_f);
   const int Sz = md->sweep_size;
   const int nwd = (md->n_vars + 31) >> 5;  // word nwd is the padding spin word (0)
   const int gw = a.g_nw[g];
@@ -164,30 +186,30 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
         for (int j = 0; j < kPre; j++)
           if (qb + j < qe)
           {
-            const uint32_t z = sv ^ spin(Rec<INT>::other(cur[j]));
+            const uint32_t z = sv ^ spin(Rec<RK>::other(cur[j]));
             if (INT)
             {
-              const int c = ((const int2*)&cur[j])->y;
+              const int c = Rec<RK>::icoef(cur[j]);
               iacc += z ? -c : c;
             }
             else
             {
-              const double c = ((const double2*)&cur[j])->y;
+              const double c = Rec<RK>::dcoef(cur[j]);
               diff = __dadd_rn(diff, z ? -c : c);
             }
           }
         for (int q = qb + kPre; q < qe; q++)
         {
           const R rq = __ldg(rec + q);
-          const uint32_t z = sv ^ spin(Rec<INT>::other(rq));
+          const uint32_t z = sv ^ spin(Rec<RK>::other(rq));
           if (INT)
           {
-            const int c = ((const int2*)&rq)->y;
+            const int c = Rec<RK>::icoef(rq);
             iacc += z ? -c : c;
           }
           else
           {
-            const double c = ((const double2*)&rq)->y;
+            const double c = Rec<RK>::dcoef(rq);
             diff = __dadd_rn(diff, z ? -c : c);
           }
         }
@@ -378,10 +400,10 @@ void lw_upload(const double* ln, const float* scr)
   cudaMemcpyToSymbol(lw::g_scr, scr, 3072 * sizeof(float));
 }
 
-template <bool R, bool I, bool SM>
+template <bool R, int RK, bool SM>
 static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb)
 {
-  auto k = lw::lw_sweep_kernel<R, I, SM>;
+  auto k = lw::lw_sweep_kernel<R, RK, SM>;
   const int bytes = SM ? wpb * a.smem_words * a.G * 4 : 0;
   static int configured = 48 * 1024;
   if (bytes > configured)
@@ -396,10 +418,17 @@ static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb)
   return cudaGetLastError();
 }
 
-template <bool R, bool I>
+template <bool R, int RK>
 static cudaError_t lw_go_sm(const LwArgs& a, cudaStream_t s, int wpb)
 {
-  return a.smem_words > 0 ? lw_go<R, I, true>(a, s, wpb) : lw_go<R, I, false>(a, s, wpb);
+  return a.smem_words > 0 ? lw_go<R, RK, true>(a, s, wpb) : lw_go<R, RK, false>(a, s, wpb);
+}
+
+template <bool R>
+static cudaError_t lw_go_rk(const LwArgs& a, cudaStream_t s, int wpb)
+{
+  if (!a.int_mode) return lw_go_sm<R, lw::RK_F64>(a, s, wpb);
+  return a.packed ? lw_go_sm<R, lw::RK_PACK>(a, s, wpb) : lw_go_sm<R, lw::RK_INT2>(a, s, wpb);
 }
 
 // Warps per block: enough that the groups spread over the 152 SMs, as many
@@ -416,9 +445,7 @@ cudaError_t launch_lw_sweep(const LwArgs& a, int wpb, cudaStream_t s)
     while (wpb > 1 && wpb * a.smem_words * a.G * 4 > kLwSmemBytes) wpb--;
     if (a.smem_words * a.G * 4 > kLwSmemBytes) return cudaErrorInvalidValue;
   }
-  if (a.replay)
-    return a.int_mode ? lw_go_sm<true, true>(a, s, wpb) : lw_go_sm<true, false>(a, s, wpb);
-  return a.int_mode ? lw_go_sm<false, true>(a, s, wpb) : lw_go_sm<false, false>(a, s, wpb);
+  return a.replay ? lw_go_rk<true>(a, s, wpb) : lw_go_rk<false>(a, s, wpb);
 }
 
 static const int kMoveWords = 64;  // words per thread in the transposes

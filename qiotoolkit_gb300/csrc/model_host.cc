@@ -416,10 +416,18 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
       if (m->int_mode)
       {
         m->rec_i.resize(2 * m->K);
+        bool small = pad < (1 << 24);
         for (int64_t q = 0; q < m->K; q++)
         {
           m->rec_i[2 * q] = m->other[q] >= 0 ? m->other[q] : pad;
           m->rec_i[2 * q + 1] = m->coef_i[q];
+          small = small && m->coef_i[q] >= -128 && m->coef_i[q] <= 127;
+        }
+        if (small)
+        {
+          m->rec_p.resize(m->K);
+          for (int64_t q = 0; q < m->K; q++)
+            m->rec_p[q] = ((unsigned)m->rec_i[2 * q] << 8) | ((unsigned)m->coef_i[q] & 0xFFu);
         }
       }
       else
@@ -456,7 +464,7 @@ void HostModel::upload() const
          o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
          o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other),
-         o_ri = put(blob, rec_i), o_rf = put(blob, rec_f);
+         o_ri = put(blob, rec_i), o_rf = put(blob, rec_f), o_rp = put(blob, rec_p);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -486,6 +494,7 @@ void HostModel::upload() const
   dev.other = other.empty() ? nullptr : (const int*)(b + o_oth);
   dev.rec_i = rec_i.empty() ? nullptr : (const int2*)(b + o_ri);
   dev.rec_f = rec_f.empty() ? nullptr : (const double2*)(b + o_rf);
+  dev.rec_p = rec_p.empty() ? nullptr : (const unsigned int*)(b + o_rp);
   uploaded = true;
 }
 

@@ -61,6 +61,7 @@ struct DevModel
   const int* other;        // K  the other member of the incidence's term, or -1
   const int2* rec_i;       // K  (other or padding spin, integer coefficient), pair-only
   const double2* rec_f;    // K  (other as an integer in the low word, coefficient)
+  const unsigned int* rec_p;  // K  other << 8 | 8-bit coefficient (small integer ones)
   int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1
@@ -158,6 +159,7 @@ struct LwArgs
   const int* local_of;      // per walker: index within its solve for counter keys (null: r)
   int G;                    // walkers (lanes) per group
   int smem_words;           // group words per lane held in shared memory (0: global)
+  int packed;               // every model has 32-bit records (rec_p)
 };
 // wpb: warps per block (0: spread the groups over the SMs)
 cudaError_t launch_lw_sweep(const LwArgs& a, int wpb, cudaStream_t s);

@@ -51,7 +51,7 @@ int64_t model_bytes(const HostModel& m)
   return (int64_t)(m.row.size() * 4 + m.inc.size() * 4 + m.coef.size() * 8 + m.coef_i.size() * 4 +
                    m.coef_f.size() * 4 + m.near.size() * 8 + m.nbr.size() * 4 + m.trow.size() * 4 +
                    m.tvar.size() * 4 + m.tcost.size() * 8 + m.tcost_i.size() * 4 + m.other.size() * 4 +
-                   m.rec_i.size() * 4 + m.rec_f.size() * 8 + 16 * 256);
+                   m.rec_i.size() * 4 + m.rec_f.size() * 8 + m.rec_p.size() * 4 + 16 * 256);
 }
 
 // device bytes of a solve: the model blob and the walker population

@@ -357,6 +357,9 @@ void LaneRunner::setup(const std::vector<DevModel>& models, const std::vector<in
     a.local_of = local_of.empty() ? nullptr : (const int*)(b + o_lo);
     a.G = lanes;
     a.smem_words = smem_words;
+    bool packed = true;
+    for (const DevModel& m : models) packed = packed && m.rec_p != nullptr;
+    a.packed = packed ? 1 : 0;
     ready = true;
 }
 

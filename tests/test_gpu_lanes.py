@@ -16,8 +16,19 @@ pytestmark = pytest.mark.gpu
 
 SA = "simulatedannealing.qiotoolkit"
 
+def _er_int(n, m, seed, big=300):
+    """ER couplings with integer weights up to +-big (|c| > 127: the lane
+    kernel's int2 records rather than the packed 32-bit ones)."""
+    import numpy as np
+    off, ids, _ = I.er_ising(n, m, seed=seed)
+    rng = np.random.default_rng(seed)
+    coef = rng.integers(-big, big + 1, len(off) - 1).astype(float)
+    return off, ids, coef
+
+
 MODELS = {
     "er_real": lambda: I.er_ising(300, 900, seed=21),
+    "er_bigint": lambda: _er_int(200, 700, 25),
     "cubic_int": lambda: I.cubic_pm_j(6, seed=22),
     "square_int": lambda: I.square_pm_j(16, seed=23),
     "cubic_odd": lambda: I.cubic_pm_j(5, seed=24),
