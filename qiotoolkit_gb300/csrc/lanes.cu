@@ -90,11 +90,12 @@ struct Rec<RK_F64>
   static __device__ __forceinline__ int icoef(const T&) { return 0; }
   static __device__ __forceinline__ double dcoef(const T& r) { return r.y; }
 };
-static const int kPre = 8;  // records of the next variable loaded one attempt ahead
-
-template <bool REPLAY, int RK, bool SMEM>
+// KPRE: records of the next variable loaded one attempt ahead (4, 6 or 8,
+// at least the largest row when it is that small)
+template <bool REPLAY, int RK, bool SMEM, int KPRE>
 __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
 {
+  constexpr int kPre = KPRE;
   constexpr bool INT = RK != RK_F64;
   using R = typename Rec<RK>::T;
   extern __shared__ __align__(16) unsigned char lw_smem[];
@@ -400,10 +401,10 @@ void lw_upload(const double* ln, const float* scr)
   cudaMemcpyToSymbol(lw::g_scr, scr, 3072 * sizeof(float));
 }
 
-template <bool R, int RK, bool SM>
-static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb)
+template <bool R, int RK, bool SM, int KP>
+static cudaError_t lw_go_k(const LwArgs& a, cudaStream_t s, int wpb)
 {
-  auto k = lw::lw_sweep_kernel<R, RK, SM>;
+  auto k = lw::lw_sweep_kernel<R, RK, SM, KP>;
   const int bytes = SM ? wpb * a.smem_words * a.G * 4 : 0;
   static int configured = 48 * 1024;
   if (bytes > configured)
@@ -416,6 +417,14 @@ static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb)
   const int blocks = (groups + wpb - 1) / wpb;
   if (blocks > 0) k<<<blocks, 32 * wpb, bytes, s>>>(a);
   return cudaGetLastError();
+}
+
+template <bool R, int RK, bool SM>
+static cudaError_t lw_go(const LwArgs& a, cudaStream_t s, int wpb)
+{
+  if (a.unroll == 4) return lw_go_k<R, RK, SM, 4>(a, s, wpb);
+  if (a.unroll == 6) return lw_go_k<R, RK, SM, 6>(a, s, wpb);
+  return lw_go_k<R, RK, SM, 8>(a, s, wpb);
 }
 
 template <bool R, int RK>

@@ -491,6 +491,9 @@ void HostModel::upload() const
   dev.fscreen = fscreen ? 1 : 0;
   dev.scan32 = scan32 ? 1 : 0;
   dev.pair_only = pair_only ? 1 : 0;
+  int md = 0;
+  for (int64_t v = 0; v < N; v++) md = std::max(md, row[v + 1] - row[v]);
+  dev.max_deg = md;
   dev.other = other.empty() ? nullptr : (const int*)(b + o_oth);
   dev.rec_i = rec_i.empty() ? nullptr : (const int2*)(b + o_ri);
   dev.rec_f = rec_f.empty() ? nullptr : (const double2*)(b + o_rf);

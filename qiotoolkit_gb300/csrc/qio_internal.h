@@ -62,6 +62,7 @@ struct DevModel
   const int2* rec_i;       // K  (other or padding spin, integer coefficient), pair-only
   const double2* rec_f;    // K  (other as an integer in the low word, coefficient)
   const unsigned int* rec_p;  // K  other << 8 | 8-bit coefficient (small integer ones)
+  int max_deg;             // largest row (incidences of one variable)
   int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1
@@ -160,6 +161,7 @@ struct LwArgs
   int G;                    // walkers (lanes) per group
   int smem_words;           // group words per lane held in shared memory (0: global)
   int packed;               // every model has 32-bit records (rec_p)
+  int unroll;               // records per attempt held in registers: 4, 6 or 8
 };
 // wpb: warps per block (0: spread the groups over the SMs)
 cudaError_t launch_lw_sweep(const LwArgs& a, int wpb, cudaStream_t s);

@@ -358,8 +358,14 @@ void LaneRunner::setup(const std::vector<DevModel>& models, const std::vector<in
     a.G = lanes;
     a.smem_words = smem_words;
     bool packed = true;
-    for (const DevModel& m : models) packed = packed && m.rec_p != nullptr;
+    int md = 0;
+    for (const DevModel& m : models)
+    {
+      packed = packed && m.rec_p != nullptr;
+      md = std::max(md, m.max_deg);
+    }
     a.packed = packed ? 1 : 0;
+    a.unroll = md <= 4 ? 4 : (md <= 6 ? 6 : 8);
     ready = true;
 }
 
