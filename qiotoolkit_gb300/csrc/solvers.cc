@@ -695,6 +695,9 @@ class ParallelTempering : public Solver
   void configure(const json::Value& doc)
   {
     configure_common(*this, doc);
+    if (kernel == 2)
+      fail(1, "parameter `kernel`: \"lanes\" is not available for parallel tempering (swaps exchange "
+              "temperature labels between walkers)");
     Params p(params);
     spr = p.integer("sweeps_per_replica", 1);
     if (spr <= 0) fail(1, "parameter `sweeps_per_replica`: must be greater than 0");
