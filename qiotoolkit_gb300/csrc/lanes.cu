@@ -275,7 +275,14 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
         }
         if (all_zero) acc = true;
         else if (beta_inf) acc = false;
-        else acc = lut_accept(s_ln, s_scr, cur, rw, INT ? (double)idE : dE, beta, nbeta_f);
+        else if (INT)
+        {
+          // integer difference: its float is exact below 2^24, within the
+          // screen's 2^-19 margin above
+          const int d = lut_screen(s_scr, cur, rw, __fmul_rn((float)idE, nbeta_f));
+          acc = d >= 0 ? d == 1 : lut_less_exact(s_ln, cur, rw, __dmul_rn((double)idE, -beta));
+        }
+        else acc = lut_accept(s_ln, s_scr, cur, rw, dE, beta, nbeta_f);
       }
       if (acc)
       {
