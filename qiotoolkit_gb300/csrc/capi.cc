@@ -542,8 +542,23 @@ qio_status qio_run_json(const char* input_json, const char* params_json, const c
     if (!input_json || !params_json || !target || !out_json) fail(1, "arguments must not be null");
     *out_json = nullptr;
     json::Value doc = json::parse(input_json, strlen(input_json));
-    std::unique_ptr<HostModel> m = build_model_json(doc, -1);
     json::Value pdoc = json::parse(params_json, strlen(params_json));
+    // feature 3 (utils/config.h:49-61), the reference's memory-saving models
+    // IsingCompact / PuboCompact (app/runner.cc:262-327): no per-term cache,
+    // terms recomputed from member spins -- the counter-free flavours
+    int kind = -1;
+    const json::Value* pp = pdoc.is_object() ? pdoc.find("params") : nullptr;
+    const json::Value* ef = pp && pp->is_object() ? pp->find("enabled_features") : nullptr;
+    bool memory_saving = false;
+    if (ef && ef->is_array())
+      for (const auto& x : ef->arr) memory_saving = memory_saving || (x.is_number() && x.num == 3);
+    if (memory_saving && doc.is_object() && doc.find("cost_function"))
+    {
+      const json::Value* t = doc["cost_function"].find("type");
+      if (t && t->is_string() && t->str == "ising") kind = K_ISING_PLAIN;
+      if (t && t->is_string() && t->str == "pubo") kind = K_PUBO_PLAIN;
+    }
+    std::unique_ptr<HostModel> m = build_model_json(doc, kind);
     std::unique_ptr<Solver> s = make_solver(m.get(), target, pdoc);
     cudaStream_t st = 0;
     s->init(st);

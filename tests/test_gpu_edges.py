@@ -142,3 +142,37 @@ def test_dimacs_model_solves_like_term_lists():
     r = O.run(o, "sa", seed=5, step_limit=50, restarts=4, sched=("linear", 0.1, 2.0), threads=4,
               full_maxsat_sweep=True)
     _same(rd.replicas(), r)
+
+
+def test_memory_saving_feature_gives_the_same_result():
+    """enabled_features [3] selects the reference's memory-saving models
+    (IsingCompact / PuboCompact): here the counter-free flavours; the result
+    is the same as with the cached models."""
+    from qiotoolkit_gb300 import instances as I
+    for kind, (off, ids, coef) in (("ising", I.er_ising(150, 400, seed=81)),
+                                   ("pubo", I.random_pubo(120, 360, seed=82))):
+        doc = {"cost_function": {"type": kind, "version": "1.0",
+                                 "terms": [{"c": float(coef[k]), "ids": [int(x) for x in ids[off[k]:off[k + 1]]]}
+                                           for k in range(len(coef))]}}
+        p = {"seed": 4, "sweeps": 60, "restarts": 4, "beta_start": 0.1, "beta_stop": 2.0}
+        a = q.run_json(doc, {"params": p}, SA)
+        b = q.run_json(doc, {"params": dict(p, enabled_features=[3])}, SA)
+        assert a["solutions"]["cost"] == b["solutions"]["cost"]
+        assert a["solutions"]["configuration"] == b["solutions"]["configuration"]
+
+
+def test_compact_model_single_term_pins():
+    """IsingCompact SingleTerm (model/test/ising_test.cc:572-611): seven
+    one-spin terms; all spins down costs -7, each flip costs +2."""
+    for kind in ("ising", "ising_plain"):
+        m = q.Model(kind, [(1.0, [i]) for i in range(7)])
+        st = np.ones((1, 7), np.uint8)
+        assert m.calculate_cost(st)[0] == -7
+        for i in range(7):
+            assert m.calculate_cost_difference(st, [i])[0] == 2
+            st = m.apply_transition(st, [i])
+            assert m.calculate_cost(st)[0] == (i + 1) * 2 - 7
+        for i in range(7):
+            assert m.calculate_cost_difference(st, [i])[0] == -2
+            st = m.apply_transition(st, [i])
+            assert m.calculate_cost(st)[0] == 7 - 2 * (i + 1)
