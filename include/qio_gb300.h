@@ -115,6 +115,11 @@ qio_status qio_model_create_json(const char* input_json, int32_t kind,
  * app/runner.cc:87-89 into model::MaxSat): the same accepted input and
  * error messages. */
 qio_status qio_model_create_dimacs(const char* text, qio_model** out);
+/* Model from a protobuf problem folder <name>/<name>_0.pb, _1.pb, ...
+ * (utils/proto_reader.h:28-150, schema utils/problem.proto, read by
+ * utils::configure_from_proto_folder): the first file holds the type,
+ * version and first terms, later files more terms. */
+qio_status qio_model_create_proto_folder(const char* folder_path, qio_model** out);
 
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out);
 /* Original variable name of each internal variable (Graph::output_map,

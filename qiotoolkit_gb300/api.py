@@ -67,6 +67,13 @@ class Model:
         return cls(None, _handle=h)
 
     @classmethod
+    def from_proto_folder(cls, path: str) -> "Model":
+        """Model from a protobuf problem folder (<name>/<name>_<k>.pb)."""
+        h = C.c_void_p()
+        check(load().qio_model_create_proto_folder(str(path).encode(), C.byref(h)))
+        return cls(None, _handle=h)
+
+    @classmethod
     def from_dimacs(cls, text: str) -> "Model":
         """MaxSAT model from DIMACS cnf / wcnf text."""
         h = C.c_void_p()

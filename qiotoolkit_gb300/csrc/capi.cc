@@ -106,6 +106,17 @@ qio_status qio_model_create_dimacs(const char* text, qio_model** out)
   });
 }
 
+qio_status qio_model_create_proto_folder(const char* folder_path, qio_model** out)
+{
+  return guard([&] {
+    if (!out || !folder_path) fail(1, "arguments must not be null");
+    *out = nullptr;
+    std::unique_ptr<qio_model> h(new qio_model());
+    h->m = build_model_proto_folder(std::string(folder_path));
+    *out = h.release();
+  });
+}
+
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out)
 {
   return guard([&] {

@@ -99,6 +99,8 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
 std::unique_ptr<HostModel> build_model_json(const json::Value& doc, int kind);
 // DIMACS cnf / wcnf text -> MaxSat model (dimacs.cc)
 std::unique_ptr<HostModel> build_model_dimacs(const std::string& text);
+// protobuf problem folder <name>/<name>_<k>.pb -> model (proto.cc)
+std::unique_ptr<HostModel> build_model_proto_folder(const std::string& folder_path);
 
 // Schedule (schedule/schedule.cc, linear.cc, geometric.cc, segments.cc).
 struct Schedule

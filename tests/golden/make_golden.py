@@ -18,6 +18,12 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
   dimacs_pins.json   utils/test/dimacs_test.cc (inputs and expected parses)
+  proto_pins.json    data/*_pb/*.pb (bytes as written by the reference's
+                     protobuf serialiser) with the terms their writers put
+                     in: utils/test/stream_test.h:145-168,
+                     model/test/test_utils.h:11-55, graph/test/graph_test.cc:
+                     28-48, and the assertions of utils/test/
+                     stream_proto_test.cc (ProtoMessagesTest)
 
 Expected values are parsed from the test sources where they are plain
 literals (EXPECT_* and ElementsAre lines), so a change in the reference shows
@@ -212,13 +218,55 @@ def dimacs_pins():
     return {"source": "utils/test/dimacs_test.cc", "cases": cases}
 
 
+def proto_pins():
+    """The protobuf problem folders shipped in data/, byte for byte, and the
+    cost functions their writers serialised into them."""
+    folders = {}
+    for name in sorted(os.listdir(DATA)):
+        d = os.path.join(DATA, name)
+        if not (name.endswith("_pb") and os.path.isdir(d)):
+            continue
+        files, k = [], 0
+        while os.path.exists(os.path.join(d, f"{name}_{k}.pb")):
+            with open(os.path.join(d, f"{name}_{k}.pb"), "rb") as f:
+                files.append(f.read().hex())
+            k += 1
+        folders[name] = files
+    # writers (loops restated as term lists)
+    stream = []  # stream_test.h:148-166: file p holds terms i = 0..p
+    for p in range(4):
+        stream += [[i + 2.5, [i, i + 1]] for i in range(p + 1)]
+    ring = [[1.0, [i, 0 if i == 9 else i + 1]] for i in range(10)]  # test_utils.h:18-24
+    ring2 = [[-9.5 if i == 9 else (-1.0 * (i + 1) if i % 2 == 0 else float(i + 1)),
+              [i, 0 if i == 9 else i + 1]] for i in range(10)]  # test_utils.h:40-47
+    square = [[1.0, [i, 0 if i == 3 else i + 1]] for i in range(4)]  # graph_test.cc:35-41
+    body = read("utils/test/stream_proto_test.cc").split("TEST(Stream, ProtoMessagesTest)")[1]
+    body = body.split("TEST(")[0]
+    n_edges = int(re.search(r"edges\.size\(\), (\d+)\)", body).group(1))
+    c0 = float(re.search(r"edges\[0\]\.c, ([-\d.]+)\)", body).group(1))
+    nodes0 = [int(x) for x in re.search(r"edges\[0\]\.nodes, std::vector<int>\(\{(.*?)\}", body)
+              .group(1).split(",")]
+    return {"folders": folders,
+            "expected": {
+                "input_problem_pb": {"type": "ising", "version": "1.0", "terms": stream,
+                                     "n_edges": n_edges, "c0": c0, "nodes0": nodes0},
+                # the last writer of this folder in the reference's test order
+                # is create_proto_test_problem(PUBO); proto3 leaves the type
+                # (0) out of the bytes
+                "models_input_problem_pb": {"type": "pubo", "version": "1.0", "terms": ring},
+                "models_input_problem2_pb": {"type": "ising", "version": "1.0", "terms": ring2},
+                "graph_input_problem_pb": {"type": "ising", "version": "1.0", "terms": square},
+                "ex_input_problem_pb": {"type": "softspin", "version": "0.1"}}}
+
+
 def main():
     if not os.path.isdir(CPP):
         print("reference not found at", REFERENCE, file=sys.stderr)
         sys.exit(1)
     files = {"rng_pins.json": rng_pins(), "pt_toy_pin.json": pt_toy_pin(),
              "model_pins.json": model_pins(), "solver_pins.json": solver_pins(),
-             "planted.json": planted(), "dimacs_pins.json": dimacs_pins()}
+             "planted.json": planted(), "dimacs_pins.json": dimacs_pins(),
+             "proto_pins.json": proto_pins()}
     for name, obj in files.items():
         with open(os.path.join(OUT, name), "w") as f:
             json.dump(obj, f, separators=(",", ":"))

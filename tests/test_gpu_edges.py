@@ -176,3 +176,26 @@ def test_compact_model_single_term_pins():
             assert m.calculate_cost_difference(st, [i])[0] == -2
             st = m.apply_transition(st, [i])
             assert m.calculate_cost(st)[0] == 7 - 2 * (i + 1)
+
+
+def test_proto_folders_cost_like_the_oracle(golden, tmp_path):
+    """Models read from the reference's protobuf folders (data/*_pb) price
+    states exactly as the oracle's model of the terms their writers put in."""
+    g = golden("proto_pins.json")
+    rng = np.random.default_rng(12)
+    for name, exp in g["expected"].items():
+        if exp["type"] == "softspin":
+            continue
+        d = tmp_path / name
+        d.mkdir()
+        for k, h in enumerate(g["folders"][name]):
+            (d / f"{name}_{k}.pb").write_bytes(bytes.fromhex(h))
+        m = q.Model.from_proto_folder(str(d))
+        o = O.Model(exp["type"], [(c, ids) for c, ids in exp["terms"]])
+        states = rng.integers(0, 2, (64, m.n_vars), dtype=np.uint8)
+        got = m.calculate_cost(states)
+        want = np.array([o.cost(s) for s in states])
+        np.testing.assert_array_equal(got, want, err_msg=name)
+        dg = m.calculate_cost_difference(states, 1)
+        dw = np.array([o.cost_difference(s, 1) for s in states])
+        np.testing.assert_array_equal(dg, dw, err_msg=name)
