@@ -65,6 +65,11 @@ typedef struct qio_model_info {
                               max|c| > 1), graph/graph_properties.h:24-40 */
   double max_coupling;
   int64_t device_bytes;    /* HBM held by the model                       */
+  int32_t n_levels;        /* level schedule of the ordered sweep (integer
+                              Ising models with one- or two-member terms):
+                              levels and chunks of the level kernel, or 0 */
+  int32_t n_chunks;
+  int32_t level_kernel;    /* 1: the level kernel can run this model      */
 } qio_model_info;
 
 typedef struct qio_solver_stats {
@@ -80,6 +85,8 @@ typedef struct qio_solver_stats {
   int64_t device_bytes;    /* HBM held by the solver                       */
   uint64_t windows;        /* 32-variable evaluation windows committed; the
                               mean committed window is attempts / windows */
+  int32_t sweep_kernel;    /* kernel of the last sweeps: 1 one walker per
+                              warp, 2 one walker per lane, 3 level schedule */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */

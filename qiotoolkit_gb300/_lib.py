@@ -32,7 +32,8 @@ class ModelInfo(C.Structure):
                 ("n_incidences", C.c_int64), ("max_locality", C.c_int32),
                 ("min_locality", C.c_int32), ("const_cost", C.c_double),
                 ("scale_factor", C.c_double), ("max_coupling", C.c_double),
-                ("device_bytes", C.c_int64)]
+                ("device_bytes", C.c_int64), ("n_levels", C.c_int32),
+                ("n_chunks", C.c_int32), ("level_kernel", C.c_int32)]
 
 
 class SolverStats(C.Structure):
@@ -40,7 +41,8 @@ class SolverStats(C.Structure):
                 ("attempts", C.c_uint64), ("accepts", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("sweep_kernel_ms", C.c_double),
                 ("run_ms", C.c_double), ("near_ties", C.c_uint64),
-                ("device_bytes", C.c_int64), ("windows", C.c_uint64)]
+                ("device_bytes", C.c_int64), ("windows", C.c_uint64),
+                ("sweep_kernel", C.c_int32)]
 
 
 class BatchStats(C.Structure):

@@ -135,6 +135,9 @@ qio_status qio_model_get_info(const qio_model* model, qio_model_info* out)
     out->device_bytes = (int64_t)(m.row.size() * 4 + m.inc.size() * 4 + m.coef.size() * 8 +
                                   m.coef_i.size() * 4 + m.nbr.size() * 4 + m.trow.size() * 4 +
                                   m.tvar.size() * 4 + m.tcost.size() * 8 + m.tcost_i.size() * 4);
+    out->n_levels = m.n_levels;
+    out->n_chunks = m.chunk.empty() ? 0 : (int32_t)m.chunk.size() - 1;
+    out->level_kernel = levels_eligible(m) ? 1 : 0;
   });
 }
 
@@ -358,6 +361,7 @@ qio_status qio_solver_get_stats(qio_solver* s, qio_solver_stats* out)
     out->near_ties = v.near_ties;
     out->device_bytes = v.device_bytes;
     out->windows = v.total_windows();
+    out->sweep_kernel = v.used_kernel;
   });
 }
 

@@ -66,6 +66,11 @@ struct HostModel
   std::vector<int> rec_i;     // 2 ints per incidence (integer mode)
   std::vector<double> rec_f;  // 2 doubles per incidence: (other as bits, coef)
   std::vector<unsigned int> rec_p;  // other << 8 | coefficient, when |coef| <= 127
+  // level schedule (levels.cu): level of each variable, chunk starts
+  std::vector<uint16_t> lvl;
+  std::vector<int> chunk;
+  int n_levels = 0;
+  bool lv_ok = false, lv_p16 = false;
   std::vector<uint32_t> nbr;
   // term -> members
   std::vector<int> trow;
@@ -170,10 +175,12 @@ class Solver
   double sweep_ms = 0, run_ms = 0;
   uint64_t near_ties = 0;
   int64_t device_bytes = 0;
+  int used_kernel = 1;     // kernel of the last sweeps (numbered as `kernel`)
   bool initialized = false, ran = false;
   bool profile = false;  // bracket every sweep launch with CUDA events
   bool smem_state = true;  // walker state in shared memory when it fits
-  int kernel = 0;          // sweep kernel: 0 auto, 1 one walker per warp, 2 one walker per lane
+  int kernel = 0;          // sweep kernel: 0 auto, 1 one walker per warp, 2 one walker per lane,
+                           // 3 level schedule (one walker per warp, counter streams)
   // CUDA-event pairs around sweep launches (profile mode)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   size_t prof_used = 0;
@@ -202,6 +209,8 @@ bool lanes_eligible(const HostModel& m);
 // the lane kernel for this solver and walker count (params "kernel"; auto:
 // eligible models with at least 1024 walkers)
 bool lanes_for(const Solver& s, const HostModel& m, int64_t walkers);
+bool levels_eligible(const HostModel& m);
+bool levels_for(const Solver& s, const HostModel& m);
 
 // Many independent solves of the same target and params (one per model).
 struct BatchStats

@@ -558,6 +558,7 @@ void upload_tables(int)
     }
   sw_upload(ln, scr, jA, jC);
   lw_upload(ln, scr);
+  lv_upload(ln, scr);
 }
 
 template <int FL, bool INT>

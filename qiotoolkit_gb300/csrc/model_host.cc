@@ -282,6 +282,8 @@ static void build_nbr(HostModel& m)
 // nothing is posted (it has been decided already); when v flips, these are
 // the undecided variables of the same 32-variable block whose cost
 // difference changes.
+static void build_levels(HostModel& m);
+
 static void build_near(HostModel& m)
 {
   m.near.assign(m.K, 0ULL);
@@ -429,6 +431,7 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
           for (int64_t q = 0; q < m->K; q++)
             m->rec_p[q] = ((unsigned)m->rec_i[2 * q] << 8) | ((unsigned)m->coef_i[q] & 0xFFu);
         }
+        build_levels(*m);
       }
       else
       {
@@ -445,6 +448,57 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
     }
   }
   return m;
+}
+
+// Level schedule of an ordered sweep (levels.cu): level(v) = 1 + the largest
+// level among v's neighbours u < v, 0 without one, so neighbours never share
+// a level and each variable comes after its lower neighbours and before its
+// higher ones.  Chunks are the maximal runs of consecutive variables whose
+// level does not decrease.  The kernel keeps per-chunk sums in 32-bit
+// integers (16-bit halves when they stay below 2^15) and levels and chunk
+// lengths in 16 bits: models outside those bounds, or with more chunks than
+// it tracks, stay on the other kernels.
+static void build_levels(HostModel& m)
+{
+  m.lv_ok = m.lv_p16 = false;
+  m.n_levels = 0;
+  m.lvl.clear();
+  m.chunk.clear();
+  if (m.N <= 0) return;
+  std::vector<int> L((size_t)m.N, 0);
+  int maxl = 0;
+  for (int64_t v = 0; v < m.N; v++)
+  {
+    int l = 0;
+    for (int q = m.row[v]; q < m.row[v + 1]; q++)
+    {
+      const int u = m.other[q];
+      if (u >= 0 && u < v) l = std::max(l, L[u] + 1);
+    }
+    L[v] = l;
+    maxl = std::max(maxl, l);
+  }
+  std::vector<int> chunk{0};
+  for (int64_t v = 1; v < m.N; v++)
+    if (L[v] < L[v - 1]) chunk.push_back((int)v);
+  chunk.push_back((int)m.N);
+  const int nch = (int)chunk.size() - 1;
+  bool ok = maxl < 65535 && nch <= kLvMaxChunks;
+  long long worst = 0;  // largest sum of |cost differences| over a chunk
+  for (int c = 0; c < nch && ok; c++)
+  {
+    ok = chunk[c + 1] - chunk[c] <= 65536;
+    long long bound = 0;
+    for (int v = chunk[c]; v < chunk[c + 1]; v++)
+      for (int q = m.row[v]; q < m.row[v + 1]; q++) bound += 2LL * std::llabs((long long)m.coef_i[q]);
+    worst = std::max(worst, bound);
+  }
+  if (!ok || worst >= (1LL << 30)) return;
+  m.lvl.assign(L.begin(), L.end());
+  m.chunk.swap(chunk);
+  m.n_levels = maxl + 1;
+  m.lv_p16 = worst < 32767;
+  m.lv_ok = true;
 }
 
 template <class T>
@@ -464,7 +518,8 @@ void HostModel::upload() const
          o_ci = put(blob, coef_i), o_nbr = put(blob, nbr), o_trow = put(blob, trow),
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
          o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other),
-         o_ri = put(blob, rec_i), o_rf = put(blob, rec_f), o_rp = put(blob, rec_p);
+         o_ri = put(blob, rec_i), o_rf = put(blob, rec_f), o_rp = put(blob, rec_p),
+         o_lv = put(blob, lvl), o_ch = put(blob, chunk);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -498,6 +553,12 @@ void HostModel::upload() const
   dev.rec_i = rec_i.empty() ? nullptr : (const int2*)(b + o_ri);
   dev.rec_f = rec_f.empty() ? nullptr : (const double2*)(b + o_rf);
   dev.rec_p = rec_p.empty() ? nullptr : (const unsigned int*)(b + o_rp);
+  dev.lv_ok = lv_ok ? 1 : 0;
+  dev.lvl = lv_ok ? (const unsigned short*)(b + o_lv) : nullptr;
+  dev.chunk = lv_ok ? (const int*)(b + o_ch) : nullptr;
+  dev.n_levels = lv_ok ? n_levels : 0;
+  dev.n_chunks = lv_ok ? (int)chunk.size() - 1 : 0;
+  dev.lv_p16 = lv_p16 ? 1 : 0;
   uploaded = true;
 }
 

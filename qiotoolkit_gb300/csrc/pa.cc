@@ -215,7 +215,9 @@ class PopulationAnnealing : public Solver
 
   // multinomial device resampling (counter streams) and lane-kernel sweeps
   bool multinomial = false;
-  bool lanes = false;
+  bool lanes = false, levels = false;
+  DevBuf lv_start;  // level kernel: spins at the start of the sweep, per walker
+  int lv_cap = 0;
   DevBuf dres;  // prefix sums, two family arrays, census counts, scalars
   unsigned long long* d_prefix = nullptr;
   int* d_family[2] = {nullptr, nullptr};
@@ -241,6 +243,7 @@ class PopulationAnnealing : public Solver
   void configure(const json::Value& doc)
   {
     configure_common_pa(doc);
+    if (kernel == 3 && !model->empty()) levels_for(*this, *model);  // validates the request
   }
 
   void configure_common_pa(const json::Value& doc);
@@ -411,8 +414,10 @@ class PopulationAnnealing : public Solver
     restart_base = 0;
     R = 0;
     // lanes need independent streams per walker: counter mode only
-    lanes = !replay && lanes_for(*this, *model, (int64_t)target_pop);
+    levels = levels_for(*this, *model);
+    lanes = !levels && !replay && lanes_for(*this, *model, (int64_t)target_pop);
     if (replay && kernel == 2) fail(1, "parameter `kernel`: \"lanes\" needs \"rng_mode\": \"counter\" here");
+    used_kernel = levels ? 3 : (lanes ? 2 : 1);
     init_population(st);
     // update_lowest_cost(population_[0]->cost(), population_[0]->state())
     double c0;
@@ -640,7 +645,34 @@ void PopulationAnnealing::run(cudaStream_t st)
     a.smem_state = smem_state ? 1 : 0;
     a.err = device_error_flag();
     int wpb = pick_wpb(warps_per_block, a.n_streams);
-    if (lanes)
+    if (levels)
+    {
+      if (lv_cap < (int)Rn)
+      {
+        lv_start = DevBuf((size_t)Rn * P.pop.nw * 4);
+        lv_cap = (int)Rn;
+      }
+      LvArgs v{};
+      v.m = a.m;
+      v.p = P.pop;
+      v.n_walkers = (int)Rn;
+      v.beta = d_beta;
+      v.bs_w = 1;
+      v.bs_s = 0;
+      v.sweep_base = 0;
+      v.n_sweeps = (int)spr;
+      v.seed = seed;
+      v.key_base = a.key_base;
+      v.key_div = a.key_div;
+      v.start = (uint32_t*)lv_start.ptr;
+      prof_begin(st);
+      cuda_check(launch_lv_sweep(v, st), "level sweep kernel");
+      prof_end(st);
+      // the term bytes are not kept up to date: every reader of this
+      // population in this mode uses the spins
+      launches++;
+    }
+    else if (lanes)
     {
       if (!L.ready || lane_walkers < (int)Rn)
       {

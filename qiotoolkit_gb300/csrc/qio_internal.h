@@ -63,6 +63,14 @@ struct DevModel
   const double2* rec_f;    // K  (other as an integer in the low word, coefficient)
   const unsigned int* rec_p;  // K  other << 8 | 8-bit coefficient (small integer ones)
   int max_deg;             // largest row (incidences of one variable)
+  // level schedule (levels.cu), integer pair-only Ising models: lvl[v] = 1 +
+  // the largest level of v's lower neighbours (0 without one); chunk[c] ..
+  // chunk[c+1] the maximal runs of variables with increasing level
+  const unsigned short* lvl;
+  const int* chunk;
+  int n_levels, n_chunks;
+  int lv_ok;               // the level kernel can run this model
+  int lv_p16;              // every chunk's |differences| sum below 2^15
   int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1
@@ -168,6 +176,36 @@ cudaError_t launch_lw_sweep(const LwArgs& a, int wpb, cudaStream_t s);
 cudaError_t launch_lw_load(const LwArgs& a, int max_words, cudaStream_t s);
 cudaError_t launch_lw_store(const LwArgs& a, int max_words, int max_terms, cudaStream_t s);
 void lw_upload(const double* ln, const float* scr);
+
+// Level-scheduled sweeps (levels.cu): one warp per walker, counter streams,
+// integer pair-only Ising models with lv_ok.  The walker's spins stay in
+// shared memory for the launch (word w at w + w / 32); `start` holds each
+// walker's spins at the start of the current sweep (nw words per walker).
+static const int kLvMaxWarps = 28;
+static const int kLvMaxChunks = 512;
+static const int kLvSmemBytes = 227 * 1024;
+struct LvArgs
+{
+  DevModel m;
+  DevPop p;
+  int n_walkers;
+  const int* slot_of;       // null: slot = walker
+  const double* beta;       // beta[r * bs_w + sweep * bs_s]
+  long long bs_w, bs_s;
+  long long sweep_base;
+  int n_sweeps;
+  uint32_t seed;            // key of walker r: counter_key(seed + r / key_div,
+  unsigned long long key_base;  //                   key_base + r % key_div)
+  long long key_div;
+  uint32_t* start;          // n_walkers * p.nw words
+};
+// shared-memory words per walker, 0 when the model does not fit
+int lv_stride_words(int n_vars);
+cudaError_t launch_lv_sweep(const LvArgs& a, cudaStream_t s);
+// term parity bytes from the spins (after level sweeps)
+cudaError_t launch_lv_terms(const DevModel& m, const DevPop& p, int n_walkers, const int* slot_of,
+                            cudaStream_t s);
+void lv_upload(const double* ln, const float* scr);
 
 // Device resampling of population annealing (pa_device.cu, multinomial).
 struct PaScalars

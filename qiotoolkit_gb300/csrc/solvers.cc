@@ -130,7 +130,8 @@ static void configure_common(Solver& s, const json::Value& doc)
   if (kern == "auto") s.kernel = 0;
   else if (kern == "warp") s.kernel = 1;
   else if (kern == "lanes") s.kernel = 2;
-  else fail(1, "parameter `kernel` must be \"auto\", \"warp\" or \"lanes\"");
+  else if (kern == "levels") s.kernel = 3;
+  else fail(1, "parameter `kernel` must be \"auto\", \"warp\", \"lanes\" or \"levels\"");
   s.output_params.push_back({"seed", std::to_string(s.seed)});
   s.output_params.push_back({"step_limit", std::to_string(s.step_limit)});
 }
@@ -382,8 +383,31 @@ bool lanes_for(const Solver& s, const HostModel& m, int64_t walkers)
       fail(1, "parameter `kernel`: \"lanes\" needs an Ising model whose terms have at most two members");
     return true;
   }
-  if (s.kernel == 1) return false;
+  if (s.kernel == 1 || s.kernel == 3) return false;
   return lanes_eligible(m) && walkers >= 1024;
+}
+
+// The level kernel runs integer pair-only Ising models whose level schedule
+// fits its bounds, with counter streams (its attempts run out of order).
+bool levels_eligible(const HostModel& m)
+{
+  return m.flavor == F_PARITY && m.pair_only && m.int_mode && m.lv_ok && lv_stride_words((int)m.N) > 0;
+}
+
+// auto: large models (a lane group of them would not fit an SM's shared
+// memory many times over), counter streams
+bool levels_for(const Solver& s, const HostModel& m)
+{
+  if (s.kernel == 3)
+  {
+    if (s.replay) fail(1, "parameter `kernel`: \"levels\" needs \"rng_mode\": \"counter\"");
+    if (!levels_eligible(m))
+      fail(1, "parameter `kernel`: \"levels\" needs an Ising model with integer coefficients whose "
+              "terms have at most two members and whose level schedule fits (see the model's lv_ok)");
+    return true;
+  }
+  if (s.kernel != 0) return false;
+  return !s.replay && levels_eligible(m) && m.N >= 4096;
 }
 
 // beta as Metropolis::set_beta / set_temperature store it
@@ -406,7 +430,8 @@ class SimulatedAnnealing : public Solver
   Population P;
   std::vector<double> betas;
   LaneRunner L;
-  bool lanes = false;
+  bool lanes = false, levels = false;
+  DevBuf lv_start;
 
   std::string target() const override { return "simulatedannealing.qiotoolkit"; }
 
@@ -453,6 +478,7 @@ class SimulatedAnnealing : public Solver
     betas.resize(step_limit);
     for (int64_t s = 0; s < step_limit; s++)
       betas[s] = beta_of(schedule.get_value((double)s), use_inverse);
+    if (kernel == 3 && !model->empty()) levels_for(*this, *model);  // validates the request
   }
 
   int64_t n_walkers() const override { return model->empty() ? 0 : restarts; }
@@ -484,7 +510,14 @@ class SimulatedAnnealing : public Solver
     a.key_div = (long long)1 << 40;
     cuda_check(launch_init(a, st), "init kernel");
     launches++;
-    lanes = lanes_for(*this, *model, restarts);
+    levels = levels_for(*this, *model);
+    lanes = !levels && lanes_for(*this, *model, restarts);
+    used_kernel = levels ? 3 : (lanes ? 2 : 1);
+    if (levels && !lv_start.ptr)
+    {
+      lv_start = DevBuf((size_t)R * P.pop.nw * 4);
+      device_bytes += (int64_t)lv_start.bytes;
+    }
     if (lanes && !L.ready)
     {
       L.setup({model->device_view(full_maxsat_sweep)}, {}, R, {}, smem_state);
@@ -509,11 +542,39 @@ class SimulatedAnnealing : public Solver
     return a;
   }
 
+  LvArgs level_args(int64_t base, int64_t n) const
+  {
+    LvArgs v{};
+    v.m = model->device_view(full_maxsat_sweep);
+    v.p = P.pop;
+    v.n_walkers = (int)restarts;
+    v.beta = P.beta;
+    v.bs_w = 0;
+    v.bs_s = 1;
+    v.sweep_base = base;
+    v.n_sweeps = (int)n;
+    v.seed = seed;
+    v.key_base = 0;
+    v.key_div = (long long)1 << 40;
+    v.start = (uint32_t*)lv_start.ptr;
+    return v;
+  }
+
+  // term bytes from the spins once the level kernel is done with them
+  void levels_finish(cudaStream_t st)
+  {
+    cuda_check(launch_lv_terms(model->device_view(full_maxsat_sweep), P.pop, (int)restarts, nullptr, st),
+               "term rebuild");
+    launches++;
+  }
+
   // one launch of sweeps [base, base + n) with the chosen kernel
   void sweep_launch(SweepArgs& a, LwArgs& la, int wpb, int64_t base, int64_t n, cudaStream_t st)
   {
     prof_begin(st);
-    if (lanes)
+    if (levels)
+      cuda_check(launch_lv_sweep(level_args(base, n), st), "level sweep kernel");
+    else if (lanes)
     {
       la.sweep_base = base;
       la.n_sweeps = (int)n;
@@ -601,6 +662,7 @@ class SimulatedAnnealing : public Solver
       cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
       launches++;
     }
+    if (levels) levels_finish(st);
     run_ms = total.stop();
     sweep_ms = profile ? prof_total_ms() : run_ms;
     check_device_error(st);
@@ -632,6 +694,7 @@ class SimulatedAnnealing : public Solver
       cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
       launches++;
     }
+    if (levels) levels_finish(st);
     return true;
   }
 
@@ -695,9 +758,9 @@ class ParallelTempering : public Solver
   void configure(const json::Value& doc)
   {
     configure_common(*this, doc);
-    if (kernel == 2)
-      fail(1, "parameter `kernel`: \"lanes\" is not available for parallel tempering (swaps exchange "
-              "temperature labels between walkers)");
+    if (kernel == 2 || kernel == 3)
+      fail(1, std::string("parameter `kernel`: \"") + (kernel == 2 ? "lanes" : "levels") +
+                  "\" is not available for parallel tempering (swaps exchange temperature labels between walkers)");
     Params p(params);
     spr = p.integer("sweeps_per_replica", 1);
     if (spr <= 0) fail(1, "parameter `sweeps_per_replica`: must be greater than 0");
@@ -1137,6 +1200,7 @@ class SABatch : public Batch
     bool eligible = true;
     for (auto* m : ms)
       eligible = eligible && lanes_eligible(*m) && m->int_mode == ms[0]->int_mode;
+    if (kernel == 3) fail(1, "parameter `kernel`: \"levels\" is not available for batches");
     if (kernel == 2 && !eligible)
       fail(1, "parameter `kernel`: \"lanes\" needs Ising models whose terms have at most two members "
               "and the same coefficient kind");

@@ -130,9 +130,26 @@ def test_kernel_parameter_validation():
     from qiotoolkit_gb300 import instances as I
     off, ids, coef = I.cubic_pm_j(3, seed=1)
     m = q.Model("ising", off=off, ids=ids, coef=coef)
-    with pytest.raises(q.QioError, match='must be "auto", "warp" or "lanes"'):
+    with pytest.raises(q.QioError, match='must be "auto", "warp", "lanes" or "levels"'):
         q.Solver(m, "simulatedannealing.qiotoolkit", {"params": {"sweeps": 5, "kernel": "fast"}})
     with pytest.raises(q.QioError, match="not available for parallel tempering"):
         q.Solver(m, "paralleltempering.qiotoolkit", {"params": {"sweeps": 5, "kernel": "lanes"}})
     with pytest.raises(q.QioError, match='needs "rng_mode": "counter"'):
         q.Solver(m, "populationannealing.cpu", {"params": {"sweeps": 5, "resampling": "multinomial"}})
+    sa = "simulatedannealing.qiotoolkit"
+    with pytest.raises(q.QioError, match='"levels" needs "rng_mode": "counter"'):
+        q.Solver(m, sa, {"params": {"sweeps": 5, "kernel": "levels"}})
+    with pytest.raises(q.QioError, match='"levels" is not available for parallel tempering'):
+        q.Solver(m, "paralleltempering.qiotoolkit", {"params": {"sweeps": 5, "kernel": "levels"}})
+    with pytest.raises(q.QioError, match='"levels" is not available for batches'):
+        q.Batch([m], sa, {"params": {"sweeps": 5, "kernel": "levels", "rng_mode": "counter"}})
+    off, ids, coef = I.er_ising(50, 120, seed=3)  # real couplings: no integer level schedule
+    r = q.Model("ising", off=off, ids=ids, coef=coef)
+    with pytest.raises(q.QioError, match='"levels" needs an Ising model with integer coefficients'):
+        q.Solver(r, sa, {"params": {"sweeps": 5, "kernel": "levels", "rng_mode": "counter"}})
+    pubo = q.Model("pubo", [(1.0, [0, 1, 2]), (2.0, [1, 3])])
+    with pytest.raises(q.QioError, match='"levels" needs an Ising model'):
+        q.Solver(pubo, "populationannealing.cpu",
+                 {"params": {"sweeps": 5, "kernel": "levels", "rng_mode": "counter"}})
+    # eligible: created without complaint (no device needed before init)
+    q.Solver(m, sa, {"params": {"sweeps": 5, "kernel": "levels", "rng_mode": "counter"}}).close()
