@@ -67,8 +67,9 @@ typedef struct qio_model_info {
   int64_t device_bytes;    /* HBM held by the model                       */
   int32_t n_levels;        /* level schedule of the ordered sweep (integer
                               Ising models with one- or two-member terms):
-                              levels and chunks of the level kernel, or 0 */
-  int32_t n_chunks;
+                              its levels and the most variables in one
+                              level, or 0                                 */
+  int32_t max_level_width;
   int32_t level_kernel;    /* 1: the level kernel can run this model      */
 } qio_model_info;
 

@@ -33,7 +33,7 @@ class ModelInfo(C.Structure):
                 ("min_locality", C.c_int32), ("const_cost", C.c_double),
                 ("scale_factor", C.c_double), ("max_coupling", C.c_double),
                 ("device_bytes", C.c_int64), ("n_levels", C.c_int32),
-                ("n_chunks", C.c_int32), ("level_kernel", C.c_int32)]
+                ("max_level_width", C.c_int32), ("level_kernel", C.c_int32)]
 
 
 class SolverStats(C.Structure):

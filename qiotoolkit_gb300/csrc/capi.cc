@@ -136,7 +136,7 @@ qio_status qio_model_get_info(const qio_model* model, qio_model_info* out)
                                   m.coef_i.size() * 4 + m.nbr.size() * 4 + m.trow.size() * 4 +
                                   m.tvar.size() * 4 + m.tcost.size() * 8 + m.tcost_i.size() * 4);
     out->n_levels = m.n_levels;
-    out->n_chunks = m.chunk.empty() ? 0 : (int32_t)m.chunk.size() - 1;
+    out->max_level_width = m.lv_width;
     out->level_kernel = levels_eligible(m) ? 1 : 0;
   });
 }

@@ -66,11 +66,11 @@ struct HostModel
   std::vector<int> rec_i;     // 2 ints per incidence (integer mode)
   std::vector<double> rec_f;  // 2 doubles per incidence: (other as bits, coef)
   std::vector<unsigned int> rec_p;  // other << 8 | coefficient, when |coef| <= 127
-  // level schedule (levels.cu): level of each variable, chunk starts
-  std::vector<uint16_t> lvl;
-  std::vector<int> chunk;
-  int n_levels = 0;
-  bool lv_ok = false, lv_p16 = false;
+  // level schedule (levels.cu): entries grouped by level, their offsets
+  std::vector<int> lv_off, lv_pos;
+  std::vector<uint32_t> lv_ent;
+  int n_levels = 0, lv_ew = 0, lv_width = 0;
+  bool lv_ok = false, lv_d8 = false;
   std::vector<uint32_t> nbr;
   // term -> members
   std::vector<int> trow;
@@ -191,6 +191,22 @@ class Solver
 // Lane-per-walker execution (lanes.cu): the group layout of the walkers,
 // the device copy of their model descriptors, and the transposes between a
 // population's bit-packed layout and the groups' interleaved words.
+// Sweep log of the level kernel (levels.cu): per walker and logged sweep its
+// start spins, start cost and attempt differences.  Launches longer than the
+// log's sweeps are cut into pieces of that many sweeps.
+struct LevelLog
+{
+  DevBuf buf;
+  int walkers = 0, sweeps = 0;
+  size_t off_cost = 0, off_diff = 0;
+  long long stride = 0;
+  int bytes_per_diff = 1;
+  // room for R walkers and up to K sweeps (fewer when the log would exceed
+  // its byte budget); returns the bytes held
+  size_t ensure(int R, int64_t K, const HostModel& m, int nw);
+  void fill(LvArgs& a) const;
+};
+
 struct LaneRunner
 {
   DevBuf meta, arena;

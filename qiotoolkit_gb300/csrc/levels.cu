@@ -10,28 +10,26 @@
 // schedule that runs v after all its lower neighbours and before all its
 // higher ones makes the same decisions and reaches the same spins.  The host
 // gives each variable level(v) = 1 + the largest level of its lower
-// neighbours (0 without one): the variables of one level share no term, run
-// at once across the warp, and the levels run in order.  An L x L periodic
-// lattice has 2L - 1 levels of up to L variables.
+// neighbours (0 without one): the variables of one level share no term, are
+// spread over the warp's lanes, and the levels run in order.  An L x L
+// periodic lattice has about 2L levels of up to L variables.
 //
 // Cost and lowest: the reference adds each accepted difference to the cost
 // and keeps the first state whose cost drops below the lowest seen
-// (markov/walker.h:209-229,269-280).  The host cuts 0..N-1 into chunks,
-// maximal runs of consecutive variables whose level does not decrease: a
-// chunk's variables are visited in index order, those of one level by its
-// lane one after the other.  Lane l owns
-// chunks l, l + 32, ... and keeps for each the sum of its accepted
-// differences, the smallest of its prefix sums and the variable where that
-// first occurred.  After the sweep a scan over the chunks in index order puts
-// the running cost of the reference at every accepted flip within reach: its
-// minimum, and the first variable reaching it, are the sweep's candidate for
-// a new lowest (all in integers, so the sums are the reference's exactly).
-// The lowest spins are then the end-of-sweep spins up to that variable and
-// the start-of-sweep spins (copied out when the sweep starts) after it.
+// (markov/walker.h:209-229,269-280).  The sweep kernel adds up each sweep's
+// accepted differences for the cost and logs, per sweep, its start spins,
+// its start cost and the difference of every attempt (0 when rejected) at
+// the attempt's level entry, where consecutive lanes write consecutive
+// bytes.  The lowest kernel then replays the log sweep by sweep: it puts the
+// differences back in variable order (through each variable's entry),
+// follows the running cost in index order -- integers, the reference's
+// exact sums --, and keeps the first variable where it drops below the
+// lowest.  Each variable is tried once per sweep, so the state at that point
+// is the sweep's end spins up to the variable and its start spins after it.
 //
-// Spins live in shared memory for the whole launch, bit-packed, word w at
-// w + w / 32 so that lanes walking rows of a lattice hit different banks.
-// Flips are shared-memory XORs: two variables of one level may share a word.
+// Spins live in shared memory for the whole sweep launch, bit-packed, word w
+// at w + w / 32 so that the lanes' words fall in different banks.  Flips are
+// shared-memory XORs: two variables of one level may share a word.
 #include <algorithm>
 #include <climits>
 
@@ -49,83 +47,50 @@ __device__ float g_scr[1024 * 3];
 
 __host__ __device__ __forceinline__ int phys(int w) { return w + (w >> 5); }
 
-template <bool PACK>
-struct Rec;
-template <>
-struct Rec<true>
-{
-  using T = unsigned int;
-  static __device__ __forceinline__ int other(T r) { return (int)(r >> 8); }
-  static __device__ __forceinline__ int coef(T r) { return (int)(signed char)(r & 0xFFu); }
-};
-template <>
-struct Rec<false>
-{
-  using T = int2;
-  static __device__ __forceinline__ int other(T r) { return r.x; }
-  static __device__ __forceinline__ int coef(T r) { return r.y; }
-};
+__device__ __forceinline__ int rec_other(unsigned int r) { return (int)(r >> 8); }
+__device__ __forceinline__ int rec_coef(unsigned int r) { return (int)(signed char)(r & 0xFFu); }
 
-// Running sum of a chunk's accepted differences and its smallest prefix sum:
-// two ints, or one word of two 16-bit halves (low: sum, high: minimum) when
-// every chunk's differences add up to less than 2^15 in magnitude.
-template <bool P16>
-struct ChunkSum;
-template <>
-struct ChunkSum<false>
+// Metropolis::accept (markov/metropolis.h:64-104) for an uphill integer
+// difference on the draws of attempt ctr: words 2 ctr and 2 ctr + 1, two
+// draws each
+__device__ __forceinline__ bool accept_up(uint64_t key, unsigned long long ctr, int idE, double beta,
+                                          bool beta_inf, float nbeta_f)
 {
-  int s, m;
-  __device__ __forceinline__ void init()
+  const uint64_t w0 = counter_draw(key, 2ULL * ctr);
+  uint32_t cur = (uint32_t)w0;
+  int rw = 0;
+  if ((cur & 255u) == 0u)
   {
-    s = 0;
-    m = INT_MAX;
-  }
-  __device__ __forceinline__ bool add(int d)  // true: a new smallest prefix
-  {
-    s += d;
-    if (s < m)
+    cur = (uint32_t)(w0 >> 32);
+    rw = 1;
+    if ((cur & 255u) == 0u)
     {
-      m = s;
-      return true;
+      const uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
+      cur = (uint32_t)w1;
+      rw = 2;
+      if ((cur & 255u) == 0u)
+      {
+        cur = (uint32_t)(w1 >> 32);
+        rw = 3;
+      }
     }
-    return false;
   }
-  __device__ __forceinline__ int sum() const { return s; }
-  __device__ __forceinline__ int min() const { return m; }
-};
-template <>
-struct ChunkSum<true>
-{
-  unsigned w;
-  __device__ __forceinline__ void init() { w = 0x7FFF0000u; }
-  __device__ __forceinline__ bool add(int d)
-  {
-    const int s = (int)(short)(w & 0xFFFFu) + d;
-    if (s < ((int)w >> 16))
-    {
-      w = ((unsigned)s << 16) | ((unsigned)s & 0xFFFFu);
-      return true;
-    }
-    w = (w & 0xFFFF0000u) | ((unsigned)s & 0xFFFFu);
-    return false;
-  }
-  __device__ __forceinline__ int sum() const { return (int)(short)(w & 0xFFFFu); }
-  __device__ __forceinline__ int min() const { return (int)w >> 16; }
-};
+  if ((cur & 255u) == 0u) return true;  // four zero buckets: accept
+  if (beta_inf) return false;
+  // the difference is an integer: its float is exact below 2^24, within the
+  // screen's margin above
+  const int d = lut_screen(g_scr, cur, rw, __fmul_rn((float)idE, nbeta_f));
+  return d >= 0 ? d == 1 : lut_less_exact(g_ln, cur, rw, __dmul_rn((double)idE, -beta));
+}
 
-// warps per block the kernel is compiled for: 28 (72 registers) up to 8
-// chunks per lane, 16 (128 registers) for 16
-template <int CPL>
-struct LvWarps
+// EW: words per level entry (1: the variable only, records from row / rec;
+// 4, 8, 16: the variable and its packed records).  PACK: 32-bit records.
+// D8: every cost difference fits in 8 bits (logged as bytes, else as 32-bit
+// integers).
+template <int EW, bool PACK, bool D8>
+__global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a, int stride)
 {
-  static const int value = CPL >= 16 ? 16 : kLvMaxWarps;
-};
-
-// CPL: chunks per lane (the model's chunks <= 32 * CPL)
-template <int CPL, bool PACK, bool P16>
-__global__ void __launch_bounds__(LvWarps<CPL>::value * 32, 1) lv_sweep_kernel(LvArgs a, int stride)
-{
-  using R = typename Rec<PACK>::T;
+  static_assert(EW == 1 || PACK, "entries with records hold packed records");
   extern __shared__ __align__(16) uint32_t lv_smem[];
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -133,27 +98,46 @@ __global__ void __launch_bounds__(LvWarps<CPL>::value * 32, 1) lv_sweep_kernel(L
   if (r >= a.n_walkers) return;  // whole warps leave together
   const int N = a.m.n_vars, nwd = (N + 31) >> 5;
   const int* __restrict__ row = a.m.row;
-  const unsigned short* __restrict__ lvl = a.m.lvl;
-  const int* __restrict__ chunk = a.m.chunk;
-  const R* __restrict__ rec = PACK ? (const R*)a.m.rec_p : (const R*)a.m.rec_i;
-  const int nch = a.m.n_chunks, nlev = a.m.n_levels;
-  const double* ln = g_ln;
-  const float* scr = g_scr;
+  const unsigned int* __restrict__ recp = a.m.rec_p;
+  const int2* __restrict__ reci = a.m.rec_i;
+  const int* __restrict__ loff = a.m.lv_off;
+  const uint32_t* __restrict__ ent = a.m.lv_ent;
+  const int nlev = a.m.n_levels;
 
   uint32_t* sp = lv_smem + (size_t)wib * stride;
   const int slot = a.slot_of ? a.slot_of[r] : r;
   uint32_t* gs = a.p.spins + (size_t)slot * a.p.nw;
-  uint32_t* ls = a.p.lspins + (size_t)r * a.p.nw;
-  uint32_t* st = a.start + (size_t)r * a.p.nw;
   for (int w = lane; w < nwd; w += 32) sp[phys(w)] = gs[w];
   if (lane == 0) sp[phys(nwd)] = 0u;  // the padding spin of one-member terms
   __syncwarp();
 
-  long long icost = (long long)a.p.cost[slot], ilow = (long long)a.p.lowest[r];
+  long long icost = (long long)a.p.cost[slot];
   const uint64_t key = counter_key(a.seed + (uint32_t)((long long)r / a.key_div),
                                    a.key_base + (unsigned long long)((long long)r % a.key_div));
   unsigned long long nacc = 0;
   auto spin = [&](int u) -> uint32_t { return (sp[phys(u >> 5)] >> (u & 31)) & 1u; };
+  // a variable's terms from the row arrays
+  auto row_sum = [&](int v, uint32_t sv) -> int {
+    int iacc = 0;
+    for (int q = __ldg(row + v), qe = __ldg(row + v + 1); q < qe; q++)
+    {
+      int u, cf;
+      if (PACK)
+      {
+        const unsigned int rq = __ldg(recp + q);
+        u = rec_other(rq);
+        cf = rec_coef(rq);
+      }
+      else
+      {
+        const int2 rq = __ldg(reci + q);
+        u = rq.x;
+        cf = rq.y;
+      }
+      iacc += (sv ^ spin(u)) ? -cf : cf;
+    }
+    return iacc;
+  };
 
   for (int k = 0; k < a.n_sweeps; k++)
   {
@@ -163,157 +147,99 @@ __global__ void __launch_bounds__(LvWarps<CPL>::value * 32, 1) lv_sweep_kernel(L
         ((unsigned long long)__double_as_longlong(beta) & 0x7FFFFFFFFFFFFFFFULL) == 0x7FF0000000000000ULL;
     const float nbeta_f = -approx_float(beta);
     const unsigned long long ctr0 = (unsigned long long)swp * (unsigned long long)N;
+    // the log of this sweep: start spins, start cost, differences by entry
+    const size_t lk = (size_t)r * a.log_sweeps + k;
+    uint32_t* st = a.start + lk * a.p.nw;
     for (int w = lane; w < nwd; w += 32) st[w] = sp[phys(w)];
+    if (lane == 0) a.cost0[lk] = icost;
+    signed char* de8 = (signed char*)a.diffs + lk * a.diff_stride;
+    int* de32 = (int*)a.diffs + lk * a.diff_stride;
 
-    // per chunk: next variable, (variables left after it << 16 | its level),
-    // sum of accepted differences, smallest prefix sum and where it fell
-    int pos[CPL], ppos[CPL];
-    ChunkSum<P16> cs[CPL];
-    unsigned rl[CPL];
+    int tot = 0;  // this lane's accepted differences
     unsigned int sacc = 0;
-#pragma unroll
-    for (int c = 0; c < CPL; c++)
-    {
-      const int kc = c * 32 + lane;
-      cs[c].init();
-      ppos[c] = -1;
-      pos[c] = 0;
-      rl[c] = 0xFFFFu;
-      if (kc < nch)
+    auto attempt = [&](int e, int v, int iacc) {
+      const int idE = -2 * iacc;
+      const bool acc = idE <= 0 || accept_up(key, ctr0 + (unsigned long long)v, idE, beta, beta_inf, nbeta_f);
+      if (D8) de8[e] = (signed char)(acc ? idE : 0);
+      else de32[e] = acc ? idE : 0;
+      if (acc)
       {
-        const int b = __ldg(chunk + kc), e = __ldg(chunk + kc + 1);
-        pos[c] = b;
-        rl[c] = ((unsigned)(e - b - 1) << 16) | (unsigned)__ldg(lvl + b);
+        atomicXor(&sp[phys(v >> 5)], 1u << (v & 31));
+        sacc++;
+        tot += idE;
       }
-    }
+    };
+    int e1 = __ldg(loff);
     for (int t = 0; t < nlev; t++)
     {
-#pragma unroll
-      for (int c = 0; c < CPL; c++)
+      const int e0 = e1;
+      e1 = __ldg(loff + t + 1);
+      if constexpr (EW == 1)
       {
-        // the chunk's variables at this level, in index order
-        while ((int)(rl[c] & 0xFFFFu) == t)
+        for (int e = e0 + lane; e < e1; e += 32)
         {
-        const int v = pos[c];
-        const uint32_t sv = spin(v);
-        const int qb = __ldg(row + v), qe = __ldg(row + v + 1);
-        int iacc = 0;
-#pragma unroll 4
-        for (int q = qb; q < qe; q++)
-        {
-          const R rq = __ldg(rec + q);
-          const int cf = Rec<PACK>::coef(rq);
-          iacc += (sv ^ spin(Rec<PACK>::other(rq))) ? -cf : cf;
+          const int v = (int)__ldg(ent + e);
+          attempt(e, v, row_sum(v, spin(v)));
         }
-        const int idE = -2 * iacc;
-        bool acc = idE <= 0;
-        if (!acc)
+      }
+      else
+      {
+        // entries of this level, one per lane at a time; the next entry's
+        // words are loaded while this one is tried
+        constexpr int NQ = EW >= 4 ? EW / 4 : 1;
+        int e = e0 + lane;
+        uint4 nx[NQ];
+        if (e < e1)
         {
-          // Metropolis::accept (markov/metropolis.h:64-104) on the draws of
-          // attempt ctr0 + v: words 2 ctr and 2 ctr + 1, two draws each
-          const unsigned long long ctr = ctr0 + (unsigned long long)v;
-          const uint64_t w0 = counter_draw(key, 2ULL * ctr);
-          uint32_t cur = (uint32_t)w0;
-          int rw = 0;
-          if ((cur & 255u) == 0u)
+#pragma unroll
+          for (int j = 0; j < NQ; j++) nx[j] = __ldg((const uint4*)(ent + (size_t)e * EW) + j);
+        }
+        while (e < e1)
+        {
+          uint4 cu[NQ];
+#pragma unroll
+          for (int j = 0; j < NQ; j++) cu[j] = nx[j];
+          const int en = e + 32;
+          if (en < e1)
           {
-            cur = (uint32_t)(w0 >> 32);
-            rw = 1;
-            if ((cur & 255u) == 0u)
+#pragma unroll
+            for (int j = 0; j < NQ; j++) nx[j] = __ldg((const uint4*)(ent + (size_t)en * EW) + j);
+          }
+          const int v = (int)cu[0].x;
+          const uint32_t sv = spin(v);
+          int iacc = 0;
+#pragma unroll
+          for (int j = 0; j < NQ; j++)
+          {
+            if (j > 0)
             {
-              const uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
-              cur = (uint32_t)w1;
-              rw = 2;
-              if ((cur & 255u) == 0u)
-              {
-                cur = (uint32_t)(w1 >> 32);
-                rw = 3;
-              }
+              const int cf = rec_coef(cu[j].x);
+              iacc += (sv ^ spin(rec_other(cu[j].x))) ? -cf : cf;
+            }
+            {
+              const int cf = rec_coef(cu[j].y);
+              iacc += (sv ^ spin(rec_other(cu[j].y))) ? -cf : cf;
+            }
+            {
+              const int cf = rec_coef(cu[j].z);
+              iacc += (sv ^ spin(rec_other(cu[j].z))) ? -cf : cf;
+            }
+            {
+              const int cf = rec_coef(cu[j].w);
+              iacc += (sv ^ spin(rec_other(cu[j].w))) ? -cf : cf;
             }
           }
-          if ((cur & 255u) == 0u) acc = true;  // four zero buckets: accept
-          else if (beta_inf) acc = false;
-          else
-          {
-            // the difference is an integer: its float is exact below 2^24,
-            // within the screen's margin above
-            const int d = lut_screen(scr, cur, rw, __fmul_rn((float)idE, nbeta_f));
-            acc = d >= 0 ? d == 1 : lut_less_exact(ln, cur, rw, __dmul_rn((double)idE, -beta));
-          }
-        }
-        if (acc)
-        {
-          atomicXor(&sp[phys(v >> 5)], 1u << (v & 31));
-          sacc++;
-          if (cs[c].add(idE)) ppos[c] = v;
-        }
-        if (rl[c] >> 16)
-        {
-          pos[c] = v + 1;
-          rl[c] = (((rl[c] >> 16) - 1u) << 16) | (unsigned)__ldg(lvl + v + 1);
-        }
-        else
-          rl[c] = 0xFFFFu;
+          attempt(e, v, iacc);
+          e = en;
         }
       }
       __syncwarp();
     }
     nacc += sacc;
-
-    // chunks in index order (c major, lane minor): running cost at each
-    // chunk's start, the sweep's lowest point and its first variable
-    long long carry = 0, best = LLONG_MAX;
-    int bestk = INT_MAX, bestv = -1;
+    long long total = tot;
 #pragma unroll
-    for (int c = 0; c < CPL; c++)
-    {
-      const int csum = cs[c].sum();
-      long long x = csum;
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1)
-      {
-        const long long y = __shfl_up_sync(kFull, x, d);
-        if (lane >= d) x += y;
-      }
-      const long long before = carry + x - csum;
-      carry += __shfl_sync(kFull, x, 31);
-      if (ppos[c] >= 0)
-      {
-        const long long cand = before + cs[c].min();
-        if (cand < best)
-        {
-          best = cand;
-          bestk = c * 32 + lane;
-          bestv = ppos[c];
-        }
-      }
-    }
-#pragma unroll
-    for (int d = 16; d; d >>= 1)
-    {
-      const long long ob = __shfl_xor_sync(kFull, best, d);
-      const int ok = __shfl_xor_sync(kFull, bestk, d);
-      const int ov = __shfl_xor_sync(kFull, bestv, d);
-      if (ob < best || (ob == best && ok < bestk))
-      {
-        best = ob;
-        bestk = ok;
-        bestv = ov;
-      }
-    }
-    if (bestv >= 0 && icost + best < ilow)
-    {
-      ilow = icost + best;
-      const int ws = bestv >> 5;
-      const uint32_t keep = (2u << (bestv & 31)) - 1u;  // bits 0 .. bestv % 32
-      for (int w = lane; w < nwd; w += 32)
-      {
-        const uint32_t now = sp[phys(w)], old = st[w];
-        ls[w] = w < ws ? now : (w > ws ? old : ((now & keep) | (old & ~keep)));
-      }
-    }
-    icost += carry;
-    __syncwarp();
+    for (int d = 16; d; d >>= 1) total += __shfl_xor_sync(kFull, total, d);
+    icost += total;
   }
 
   for (int w = lane; w < nwd; w += 32) gs[w] = sp[phys(w)];
@@ -323,12 +249,154 @@ __global__ void __launch_bounds__(LvWarps<CPL>::value * 32, 1) lv_sweep_kernel(L
   {
     const unsigned long long natt = (unsigned long long)a.n_sweeps * (unsigned long long)N;
     a.p.cost[slot] = (double)icost;
-    a.p.lowest[r] = (double)ilow;
     a.p.attempts[r] += natt;
     a.p.accepts[r] += nacc;
     a.p.step_att[r] += natt;
     a.p.step_acc[r] += nacc;
     if (a.p.windows) a.p.windows[r] += natt;
+  }
+}
+
+// The lowest of the logged sweeps, one block per walker (a persistent grid
+// over the walkers).  STAGE: each logged sweep's differences are copied into
+// shared memory and read there in variable order; otherwise they are read
+// through L1.  Thread i follows a contiguous run of variables; a block scan
+// places its running sum in the sweep's running cost, and the smallest
+// (value, thread) pair gives the first variable where the cost is lowest.
+template <bool D8, bool STAGE>
+__global__ void __launch_bounds__(kLvLowThreads, 2) lv_lowest_kernel(LvArgs a)
+{
+  extern __shared__ __align__(16) unsigned char lv_row[];
+  __shared__ long long s_tot[kLvLowThreads / 32], s_val[kLvLowThreads / 32];
+  __shared__ int s_thr[kLvLowThreads / 32], s_var[kLvLowThreads / 32];
+  __shared__ long long s_low;
+  __shared__ int s_k, s_v;
+  const unsigned kFull = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  constexpr int kW = kLvLowThreads / 32;
+  const int N = a.m.n_vars, nwd = (N + 31) >> 5;
+  const int* __restrict__ epos = a.m.lv_pos;
+  const int vpt = ((N + kLvLowThreads - 1) / kLvLowThreads + 3) & ~3;  // a multiple of 4
+  const int v0 = min(N, tid * vpt), v1 = min(N, v0 + vpt);
+  for (int r = blockIdx.x; r < a.n_walkers; r += gridDim.x)
+  {
+    const int slot = a.slot_of ? a.slot_of[r] : r;
+    if (tid == 0)
+    {
+      s_low = (long long)a.p.lowest[r];
+      s_k = -1;
+      s_v = -1;
+    }
+    for (int k = 0; k < a.n_sweeps; k++)
+    {
+      const size_t lk = (size_t)r * a.log_sweeps + k;
+      const long long c0 = a.cost0[lk];
+      const signed char* de8 = (const signed char*)a.diffs + lk * a.diff_stride;
+      const int* de32 = (const int*)a.diffs + lk * a.diff_stride;
+      if (STAGE)
+      {
+        __syncthreads();  // the previous sweep's readers are done with the row
+        const int n16 = (int)((a.diff_stride * (D8 ? 1 : 4)) >> 4);
+        const uint4* src = D8 ? (const uint4*)de8 : (const uint4*)de32;
+#pragma unroll 4
+        for (int i = tid; i < n16; i += kLvLowThreads) ((uint4*)lv_row)[i] = src[i];
+        __syncthreads();
+      }
+      const signed char* r8 = STAGE ? (const signed char*)lv_row : de8;
+      const int* r32 = STAGE ? (const int*)lv_row : de32;
+      long long run = 0, mn = LLONG_MAX;
+      int pos = -1;
+      for (int v = v0; v < v1; v += 4)
+      {
+        const int4 p4 = __ldg((const int4*)(epos + v));
+        const int pp[4] = {p4.x, p4.y, p4.z, p4.w};
+        int dv[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) dv[j] = v + j < v1 ? (D8 ? (int)r8[pp[j]] : r32[pp[j]]) : 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (dv[j] != 0)
+          {
+            run += dv[j];
+            if (run < mn)
+            {
+              mn = run;
+              pos = v + j;
+            }
+          }
+      }
+      // exclusive scan of the threads' sums, in thread (= variable) order
+      long long x = run;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1)
+      {
+        const long long y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+      }
+      if (lane == 31) s_tot[wid] = x;
+      __syncthreads();
+      long long before = x - run;
+      for (int w = 0; w < wid; w++) before += s_tot[w];
+      long long best = pos >= 0 ? before + mn : LLONG_MAX;
+      int bt = pos >= 0 ? tid : INT_MAX, bv = pos;
+#pragma unroll
+      for (int d = 16; d; d >>= 1)
+      {
+        const long long ob = __shfl_xor_sync(kFull, best, d);
+        const int ot = __shfl_xor_sync(kFull, bt, d);
+        const int ov = __shfl_xor_sync(kFull, bv, d);
+        if (ob < best || (ob == best && ot < bt))
+        {
+          best = ob;
+          bt = ot;
+          bv = ov;
+        }
+      }
+      if (lane == 0)
+      {
+        s_val[wid] = best;
+        s_thr[wid] = bt;
+        s_var[wid] = bv;
+      }
+      __syncthreads();
+      if (tid == 0)
+      {
+        for (int w = 1; w < kW; w++)
+          if (s_val[w] < best || (s_val[w] == best && s_thr[w] < bt))
+          {
+            best = s_val[w];
+            bt = s_thr[w];
+            bv = s_var[w];
+          }
+        if (bv >= 0 && c0 + best < s_low)
+        {
+          s_low = c0 + best;
+          s_k = k;
+          s_v = bv;
+        }
+      }
+      // s_tot is rewritten by the next sweep only after the barrier above it
+    }
+    __syncthreads();
+    const int best_k = s_k, best_v = s_v;
+    if (best_k >= 0)
+    {
+      // the end spins of that sweep up to best_v, its start spins after
+      const size_t lk = (size_t)r * a.log_sweeps + best_k;
+      const uint32_t* s0 = a.start + lk * a.p.nw;
+      const uint32_t* s1 = best_k + 1 < a.n_sweeps ? a.start + (lk + 1) * a.p.nw
+                                                    : a.p.spins + (size_t)slot * a.p.nw;
+      uint32_t* ls = a.p.lspins + (size_t)r * a.p.nw;
+      const int ws = best_v >> 5;
+      const uint32_t keep = (2u << (best_v & 31)) - 1u;  // bits 0 .. best_v % 32
+      for (int w = tid; w < nwd; w += kLvLowThreads)
+      {
+        const uint32_t now = s1[w], old = s0[w];
+        ls[w] = w < ws ? now : (w > ws ? old : ((now & keep) | (old & ~keep)));
+      }
+      if (tid == 0) a.p.lowest[r] = (double)s_low;
+    }
+    __syncthreads();  // s_low / s_k / s_v are reset for the next walker
   }
 }
 
@@ -368,15 +436,15 @@ int lv_stride_words(int n_vars)
   return words * 4 <= kLvSmemBytes ? words : 0;
 }
 
-// Warps (walkers) per block: as many as the shared memory and the kernel's
-// register budget allow, then evened out so that the last wave's blocks are
-// as full as the others.
-template <int CPL, bool PACK, bool P16>
+// Warps (walkers) per block: as many as the shared memory and the register
+// budget allow, then evened out so that the last wave's blocks are as full
+// as the others.
+template <int EW, bool PACK, bool D8>
 static cudaError_t lv_go(const LvArgs& a, int stride, cudaStream_t s)
 {
-  auto k = lv::lv_sweep_kernel<CPL, PACK, P16>;
+  auto k = lv::lv_sweep_kernel<EW, PACK, D8>;
   const long long sms = 152;
-  const int cap = std::min(lv::LvWarps<CPL>::value, kLvSmemBytes / (stride * 4));  // warps per SM
+  const int cap = std::min(kLvMaxWarps, kLvSmemBytes / (stride * 4));  // warps per SM
   const long long waves = ((long long)a.n_walkers + sms * cap - 1) / (sms * cap);
   const long long even = ((long long)a.n_walkers + sms * waves - 1) / (sms * waves);
   const int wpb = (int)std::max(1LL, std::min<long long>(cap, even));
@@ -393,25 +461,67 @@ static cudaError_t lv_go(const LvArgs& a, int stride, cudaStream_t s)
   return cudaGetLastError();
 }
 
-template <bool PACK>
-static cudaError_t lv_go_cpl(const LvArgs& a, int stride, cudaStream_t s)
+template <bool D8, bool STAGE>
+static cudaError_t lv_low(const LvArgs& a, cudaStream_t s)
 {
-  const int need = (a.m.n_chunks + 31) / 32;
-  const bool p16 = a.m.lv_p16 != 0;
-  if (need <= 1) return lv_go<1, PACK, false>(a, stride, s);
-  if (need <= 2) return lv_go<2, PACK, false>(a, stride, s);
-  if (need <= 4) return lv_go<4, PACK, false>(a, stride, s);
-  if (need <= 8) return p16 ? lv_go<8, PACK, true>(a, stride, s) : lv_go<8, PACK, false>(a, stride, s);
-  return p16 ? lv_go<16, PACK, true>(a, stride, s) : lv_go<16, PACK, false>(a, stride, s);
+  auto k = lv::lv_lowest_kernel<D8, STAGE>;
+  const int bytes = STAGE ? (int)(a.diff_stride * (D8 ? 1 : 4)) : 0;
+  static int configured = 48 * 1024;
+  if (bytes > configured)
+  {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kLvRowBytes);
+    if (e != cudaSuccess) return e;
+    configured = kLvRowBytes;
+  }
+  const int blocks = (int)std::min<long long>(152LL * 4, a.n_walkers);  // persistent over the walkers
+  k<<<blocks, kLvLowThreads, bytes, s>>>(a);
+  return cudaGetLastError();
 }
 
-cudaError_t launch_lv_sweep(const LvArgs& a, cudaStream_t s)
+static cudaError_t lv_sweep_only(const LvArgs& a, int stride, bool d8, cudaStream_t s)
 {
-  if (a.n_walkers <= 0 || a.n_sweeps <= 0) return cudaSuccess;
-  if (!a.m.lv_ok || a.m.n_chunks > kLvMaxChunks || !a.m.rec_i || !a.start) return cudaErrorInvalidValue;
-  const int stride = lv_stride_words(a.m.n_vars);
+  switch (a.m.lv_ew)
+  {
+    case 4: return !a.m.rec_p ? cudaErrorInvalidValue
+                   : (d8 ? lv_go<4, true, true>(a, stride, s) : lv_go<4, true, false>(a, stride, s));
+    case 8: return !a.m.rec_p ? cudaErrorInvalidValue
+                   : (d8 ? lv_go<8, true, true>(a, stride, s) : lv_go<8, true, false>(a, stride, s));
+    case 16: return !a.m.rec_p ? cudaErrorInvalidValue
+                    : (d8 ? lv_go<16, true, true>(a, stride, s) : lv_go<16, true, false>(a, stride, s));
+    case 1:
+      if (a.m.rec_p) return d8 ? lv_go<1, true, true>(a, stride, s) : lv_go<1, true, false>(a, stride, s);
+      return d8 ? lv_go<1, false, true>(a, stride, s) : lv_go<1, false, false>(a, stride, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_lv_sweep(const LvArgs& a0, cudaStream_t s)
+{
+  if (a0.n_walkers <= 0 || a0.n_sweeps <= 0) return cudaSuccess;
+  if (!a0.m.lv_ok || !a0.m.lv_ent || !a0.m.lv_pos || !a0.m.rec_i || !a0.start || !a0.cost0 || !a0.diffs ||
+      a0.log_sweeps < 1)
+    return cudaErrorInvalidValue;
+  const int stride = lv_stride_words(a0.m.n_vars);
   if (stride == 0) return cudaErrorInvalidValue;
-  return a.m.rec_p ? lv_go_cpl<true>(a, stride, s) : lv_go_cpl<false>(a, stride, s);
+  const bool d8 = a0.m.lv_d8 != 0;
+  if (a0.diff_bytes != (d8 ? 1 : 4) || a0.diff_stride < a0.m.n_vars || (a0.diff_stride & 31) ||
+      ((uintptr_t)a0.diffs & 255))
+    return cudaErrorInvalidValue;
+  const bool stage = a0.diff_stride * a0.diff_bytes <= kLvRowBytes;
+  // the log holds log_sweeps sweeps: sweep launches of at most that many,
+  // each followed by its lowest pass
+  for (int done = 0; done < a0.n_sweeps; done += a0.log_sweeps)
+  {
+    LvArgs a = a0;
+    a.sweep_base = a0.sweep_base + done;
+    a.n_sweeps = std::min(a0.log_sweeps, a0.n_sweeps - done);
+    cudaError_t e = lv_sweep_only(a, stride, d8, s);
+    if (e != cudaSuccess) return e;
+    if (d8) e = stage ? lv_low<true, true>(a, s) : lv_low<true, false>(a, s);
+    else e = stage ? lv_low<false, true>(a, s) : lv_low<false, false>(a, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_lv_terms(const DevModel& m, const DevPop& p, int n_walkers, const int* slot_of,

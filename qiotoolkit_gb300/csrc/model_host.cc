@@ -453,20 +453,23 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
 // Level schedule of an ordered sweep (levels.cu): level(v) = 1 + the largest
 // level among v's neighbours u < v, 0 without one, so neighbours never share
 // a level and each variable comes after its lower neighbours and before its
-// higher ones.  Chunks are the maximal runs of consecutive variables whose
-// level does not decrease.  The kernel keeps per-chunk sums in 32-bit
-// integers (16-bit halves when they stay below 2^15) and levels and chunk
-// lengths in 16 bits: models outside those bounds, or with more chunks than
-// it tracks, stay on the other kernels.
+// higher ones.  Entries list the variables level by level (index order
+// within a level); with 8-bit coefficients and at most 15 incidences per
+// variable an entry carries the variable's records too (4, 8 or 16 words),
+// else it is the variable alone.  The kernel sums a lane's differences in
+// 32-bit integers: models whose differences could overflow them stay on the
+// other kernels.
 static void build_levels(HostModel& m)
 {
-  m.lv_ok = m.lv_p16 = false;
-  m.n_levels = 0;
-  m.lvl.clear();
-  m.chunk.clear();
+  m.lv_ok = m.lv_d8 = false;
+  m.n_levels = m.lv_ew = m.lv_width = 0;
+  m.lv_off.clear();
+  m.lv_ent.clear();
+  m.lv_pos.clear();
   if (m.N <= 0) return;
   std::vector<int> L((size_t)m.N, 0);
-  int maxl = 0;
+  int maxl = 0, maxdeg = 0;
+  long long bound = 0, widest = 0;  // sum and largest of the variables' |largest difference|
   for (int64_t v = 0; v < m.N; v++)
   {
     int l = 0;
@@ -474,30 +477,46 @@ static void build_levels(HostModel& m)
     {
       const int u = m.other[q];
       if (u >= 0 && u < v) l = std::max(l, L[u] + 1);
+      bound += 2LL * std::llabs((long long)m.coef_i[q]);
     }
+    long long dv = 0;
+    for (int q = m.row[v]; q < m.row[v + 1]; q++) dv += 2LL * std::llabs((long long)m.coef_i[q]);
+    widest = std::max(widest, dv);
     L[v] = l;
     maxl = std::max(maxl, l);
+    maxdeg = std::max(maxdeg, m.row[v + 1] - m.row[v]);
   }
-  std::vector<int> chunk{0};
-  for (int64_t v = 1; v < m.N; v++)
-    if (L[v] < L[v - 1]) chunk.push_back((int)v);
-  chunk.push_back((int)m.N);
-  const int nch = (int)chunk.size() - 1;
-  bool ok = maxl < 65535 && nch <= kLvMaxChunks;
-  long long worst = 0;  // largest sum of |cost differences| over a chunk
-  for (int c = 0; c < nch && ok; c++)
+  if (bound >= (1LL << 31)) return;
+  const int nl = maxl + 1;
+  std::vector<int> off((size_t)nl + 1, 0);
+  for (int64_t v = 0; v < m.N; v++) off[L[v] + 1]++;
+  int width = 0;
+  for (int t = 0; t < nl; t++)
   {
-    ok = chunk[c + 1] - chunk[c] <= 65536;
-    long long bound = 0;
-    for (int v = chunk[c]; v < chunk[c + 1]; v++)
-      for (int q = m.row[v]; q < m.row[v + 1]; q++) bound += 2LL * std::llabs((long long)m.coef_i[q]);
-    worst = std::max(worst, bound);
+    width = std::max(width, off[t + 1]);
+    off[t + 1] += off[t];
   }
-  if (!ok || worst >= (1LL << 30)) return;
-  m.lvl.assign(L.begin(), L.end());
-  m.chunk.swap(chunk);
-  m.n_levels = maxl + 1;
-  m.lv_p16 = worst < 32767;
+  int ew = 1;
+  if (!m.rec_p.empty()) ew = maxdeg <= 3 ? 4 : (maxdeg <= 7 ? 8 : (maxdeg <= 15 ? 16 : 1));
+  const int pad = (int)(((m.N + 31) / 32) * 32);
+  std::vector<int> fill(off.begin(), off.end() - 1);
+  std::vector<uint32_t> ent((size_t)m.N * ew, (uint32_t)pad << 8);
+  std::vector<int> pos((size_t)((m.N + 31) / 32) * 32, 0);
+  for (int64_t v = 0; v < m.N; v++)
+  {
+    pos[v] = fill[L[v]];
+    uint32_t* e = &ent[(size_t)fill[L[v]]++ * ew];
+    e[0] = (uint32_t)v;
+    if (ew > 1)
+      for (int q = m.row[v], j = 1; q < m.row[v + 1]; q++, j++) e[j] = m.rec_p[q];
+  }
+  m.lv_off.swap(off);
+  m.lv_ent.swap(ent);
+  m.lv_pos.swap(pos);
+  m.n_levels = nl;
+  m.lv_ew = ew;
+  m.lv_width = width;
+  m.lv_d8 = widest <= 127;
   m.lv_ok = true;
 }
 
@@ -519,7 +538,7 @@ void HostModel::upload() const
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
          o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other),
          o_ri = put(blob, rec_i), o_rf = put(blob, rec_f), o_rp = put(blob, rec_p),
-         o_lv = put(blob, lvl), o_ch = put(blob, chunk);
+         o_lo = put(blob, lv_off), o_le = put(blob, lv_ent), o_lp = put(blob, lv_pos);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -554,11 +573,12 @@ void HostModel::upload() const
   dev.rec_f = rec_f.empty() ? nullptr : (const double2*)(b + o_rf);
   dev.rec_p = rec_p.empty() ? nullptr : (const unsigned int*)(b + o_rp);
   dev.lv_ok = lv_ok ? 1 : 0;
-  dev.lvl = lv_ok ? (const unsigned short*)(b + o_lv) : nullptr;
-  dev.chunk = lv_ok ? (const int*)(b + o_ch) : nullptr;
+  dev.lv_off = lv_ok ? (const int*)(b + o_lo) : nullptr;
+  dev.lv_ent = lv_ok ? (const uint32_t*)(b + o_le) : nullptr;
+  dev.lv_pos = lv_ok ? (const int*)(b + o_lp) : nullptr;
   dev.n_levels = lv_ok ? n_levels : 0;
-  dev.n_chunks = lv_ok ? (int)chunk.size() - 1 : 0;
-  dev.lv_p16 = lv_p16 ? 1 : 0;
+  dev.lv_ew = lv_ok ? lv_ew : 0;
+  dev.lv_d8 = lv_d8 ? 1 : 0;
   uploaded = true;
 }
 

@@ -216,8 +216,7 @@ class PopulationAnnealing : public Solver
   // multinomial device resampling (counter streams) and lane-kernel sweeps
   bool multinomial = false;
   bool lanes = false, levels = false;
-  DevBuf lv_start;  // level kernel: spins at the start of the sweep, per walker
-  int lv_cap = 0;
+  LevelLog lvlog;  // level kernel sweep log
   DevBuf dres;  // prefix sums, two family arrays, census counts, scalars
   unsigned long long* d_prefix = nullptr;
   int* d_family[2] = {nullptr, nullptr};
@@ -647,11 +646,7 @@ void PopulationAnnealing::run(cudaStream_t st)
     int wpb = pick_wpb(warps_per_block, a.n_streams);
     if (levels)
     {
-      if (lv_cap < (int)Rn)
-      {
-        lv_start = DevBuf((size_t)Rn * P.pop.nw * 4);
-        lv_cap = (int)Rn;
-      }
+      lvlog.ensure((int)Rn, spr, *model, P.pop.nw);
       LvArgs v{};
       v.m = a.m;
       v.p = P.pop;
@@ -664,7 +659,7 @@ void PopulationAnnealing::run(cudaStream_t st)
       v.seed = seed;
       v.key_base = a.key_base;
       v.key_div = a.key_div;
-      v.start = (uint32_t*)lv_start.ptr;
+      lvlog.fill(v);
       prof_begin(st);
       cuda_check(launch_lv_sweep(v, st), "level sweep kernel");
       prof_end(st);

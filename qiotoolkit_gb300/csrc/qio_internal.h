@@ -63,14 +63,18 @@ struct DevModel
   const double2* rec_f;    // K  (other as an integer in the low word, coefficient)
   const unsigned int* rec_p;  // K  other << 8 | 8-bit coefficient (small integer ones)
   int max_deg;             // largest row (incidences of one variable)
-  // level schedule (levels.cu), integer pair-only Ising models: lvl[v] = 1 +
-  // the largest level of v's lower neighbours (0 without one); chunk[c] ..
-  // chunk[c+1] the maximal runs of variables with increasing level
-  const unsigned short* lvl;
-  const int* chunk;
-  int n_levels, n_chunks;
+  // level schedule (levels.cu), integer pair-only Ising models: level(v) =
+  // 1 + the largest level of v's lower neighbours (0 without one); the
+  // variables of level t are entries lv_off[t] .. lv_off[t+1] of lv_ent, in
+  // index order, lv_ew words each: the variable, then (lv_ew > 1) its
+  // records as in rec_p, padded with zero-coefficient padding-spin records
+  const int* lv_off;
+  const uint32_t* lv_ent;
+  const int* lv_pos;       // entry of each variable (n_vars rounded up to 32)
+  int n_levels;
+  int lv_ew;               // words per entry: 1 (records from row / rec), 4, 8 or 16
   int lv_ok;               // the level kernel can run this model
-  int lv_p16;              // every chunk's |differences| sum below 2^15
+  int lv_d8;               // every cost difference within -128 .. 127
   int scan32;              // 32 cost differences always sum within int32
   const uint32_t* nbr;     // n_vars: bit d-1 set if v-d shares a term with v
   const int* trow;         // n_terms + 1
@@ -179,10 +183,9 @@ void lw_upload(const double* ln, const float* scr);
 
 // Level-scheduled sweeps (levels.cu): one warp per walker, counter streams,
 // integer pair-only Ising models with lv_ok.  The walker's spins stay in
-// shared memory for the launch (word w at w + w / 32); `start` holds each
-// walker's spins at the start of the current sweep (nw words per walker).
+// shared memory for the launch (word w at w + w / 32); each sweep is logged
+// and a second kernel finds the lowest from the log.
 static const int kLvMaxWarps = 28;
-static const int kLvMaxChunks = 512;
 static const int kLvSmemBytes = 227 * 1024;
 struct LvArgs
 {
@@ -197,8 +200,23 @@ struct LvArgs
   uint32_t seed;            // key of walker r: counter_key(seed + r / key_div,
   unsigned long long key_base;  //                   key_base + r % key_div)
   long long key_div;
-  uint32_t* start;          // n_walkers * p.nw words
+  // the sweep log, log_sweeps sweeps per walker (sweep k of walker r at
+  // r * log_sweeps + k): start spins (p.nw words), start cost, and the
+  // difference of every attempt (0 when rejected) at its level entry
+  int log_sweeps;
+  uint32_t* start;
+  long long* cost0;
+  void* diffs;
+  long long diff_stride;    // elements per logged sweep (>= n_vars, a multiple of 32)
+  int diff_bytes;           // 1 (models with lv_d8) or 4
 };
+// lowest pass: threads per block (one block per walker), log bytes staged
+// in shared memory per block
+static const int kLvLowThreads = 512;
+static const int kLvRowBytes = 96 * 1024;
+// bytes per logged difference for a model (1 or 4)
+inline int lv_diff_bytes(const DevModel& m) { return m.lv_d8 ? 1 : 4; }
+inline long long lv_diff_stride(int n_vars) { return ((long long)n_vars + 31) & ~31LL; }
 // shared-memory words per walker, 0 when the model does not fit
 int lv_stride_words(int n_vars);
 cudaError_t launch_lv_sweep(const LvArgs& a, cudaStream_t s);

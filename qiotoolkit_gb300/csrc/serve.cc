@@ -51,8 +51,8 @@ int64_t model_bytes(const HostModel& m)
   return (int64_t)(m.row.size() * 4 + m.inc.size() * 4 + m.coef.size() * 8 + m.coef_i.size() * 4 +
                    m.coef_f.size() * 4 + m.near.size() * 8 + m.nbr.size() * 4 + m.trow.size() * 4 +
                    m.tvar.size() * 4 + m.tcost.size() * 8 + m.tcost_i.size() * 4 + m.other.size() * 4 +
-                   m.rec_i.size() * 4 + m.rec_f.size() * 8 + m.rec_p.size() * 4 + m.lvl.size() * 2 +
-                   m.chunk.size() * 4 + 18 * 256);
+                   m.rec_i.size() * 4 + m.rec_f.size() * 8 + m.rec_p.size() * 4 + m.lv_off.size() * 4 +
+                   m.lv_ent.size() * 4 + m.lv_pos.size() * 4 + 19 * 256);
 }
 
 // device bytes of a solve: the model blob and the walker population
@@ -61,9 +61,17 @@ int64_t footprint_of(const HostModel& m, const Solver& s)
   const int64_t W = std::max<int64_t>(1, s.n_walkers());
   const int64_t nw = ((m.N + 31) / 32 + 3) & ~3LL;
   const int64_t mp = std::max<int64_t>(16, (m.M + 15) & ~15LL);
-  const int64_t per = 3 * nw * 4 + mp + 10 * 8;  // spins, lowest spins, a sweep-start copy
+  // spins, lowest spins, term states, per-walker scalars
+  const int64_t per = 2 * nw * 4 + mp + 10 * 8;
   const int64_t steps = std::max<int64_t>(1, s.step_limit);
-  return model_bytes(m) + W * per + steps * 8 + W * 64 + 64 * 1024;
+  // the level kernel's sweep log (at most 64 sweeps, at most 4 GiB)
+  int64_t lv = 0;
+  if (m.lv_ok)
+  {
+    const int64_t per_sweep = nw * 4 + 8 + ((m.N + 31) & ~31LL) * (m.lv_d8 ? 1 : 4);
+    lv = std::min<int64_t>((int64_t)4 << 30, W * std::min<int64_t>(64, steps) * per_sweep);
+  }
+  return model_bytes(m) + W * per + steps * 8 + W * 64 + lv + 64 * 1024;
 }
 }  // namespace
 

@@ -394,6 +394,37 @@ bool levels_eligible(const HostModel& m)
   return m.flavor == F_PARITY && m.pair_only && m.int_mode && m.lv_ok && lv_stride_words((int)m.N) > 0;
 }
 
+static const size_t kLevelLogBudget = (size_t)4 << 30;
+
+size_t LevelLog::ensure(int R, int64_t K, const HostModel& m, int nw)
+{
+  const size_t db = m.lv_d8 ? 1 : 4;
+  const long long st = lv_diff_stride((int)m.N);
+  const size_t per = (size_t)nw * 4 + 8 + (size_t)st * db;  // one walker, one sweep
+  const int64_t fit = (int64_t)(kLevelLogBudget / std::max<size_t>(1, per * (size_t)std::max(1, R)));
+  const int k = (int)std::max<int64_t>(1, std::min<int64_t>({K, fit, 64}));
+  if (buf.ptr && R <= walkers && k <= sweeps) return buf.bytes;
+  const size_t n = (size_t)R * k;
+  off_cost = (n * nw * 4 + 255) & ~(size_t)255;
+  off_diff = (off_cost + n * 8 + 255) & ~(size_t)255;
+  buf = DevBuf(off_diff + n * st * db);
+  walkers = R;
+  sweeps = k;
+  stride = st;
+  bytes_per_diff = (int)db;
+  return buf.bytes;
+}
+
+void LevelLog::fill(LvArgs& a) const
+{
+  a.log_sweeps = sweeps;
+  a.start = (uint32_t*)buf.ptr;
+  a.cost0 = (long long*)((char*)buf.ptr + off_cost);
+  a.diffs = (char*)buf.ptr + off_diff;
+  a.diff_stride = stride;
+  a.diff_bytes = bytes_per_diff;
+}
+
 // auto: large models (a lane group of them would not fit an SM's shared
 // memory many times over), counter streams
 bool levels_for(const Solver& s, const HostModel& m)
@@ -403,7 +434,7 @@ bool levels_for(const Solver& s, const HostModel& m)
     if (s.replay) fail(1, "parameter `kernel`: \"levels\" needs \"rng_mode\": \"counter\"");
     if (!levels_eligible(m))
       fail(1, "parameter `kernel`: \"levels\" needs an Ising model with integer coefficients whose "
-              "terms have at most two members and whose level schedule fits (see the model's lv_ok)");
+              "terms have at most two members (and differences within 32-bit integers)");
     return true;
   }
   if (s.kernel != 0) return false;
@@ -431,7 +462,7 @@ class SimulatedAnnealing : public Solver
   std::vector<double> betas;
   LaneRunner L;
   bool lanes = false, levels = false;
-  DevBuf lv_start;
+  LevelLog lvlog;
 
   std::string target() const override { return "simulatedannealing.qiotoolkit"; }
 
@@ -513,11 +544,7 @@ class SimulatedAnnealing : public Solver
     levels = levels_for(*this, *model);
     lanes = !levels && lanes_for(*this, *model, restarts);
     used_kernel = levels ? 3 : (lanes ? 2 : 1);
-    if (levels && !lv_start.ptr)
-    {
-      lv_start = DevBuf((size_t)R * P.pop.nw * 4);
-      device_bytes += (int64_t)lv_start.bytes;
-    }
+    if (levels && !lvlog.buf.ptr) device_bytes += (int64_t)lvlog.ensure(R, step_limit, *model, P.pop.nw);
     if (lanes && !L.ready)
     {
       L.setup({model->device_view(full_maxsat_sweep)}, {}, R, {}, smem_state);
@@ -556,7 +583,7 @@ class SimulatedAnnealing : public Solver
     v.seed = seed;
     v.key_base = 0;
     v.key_div = (long long)1 << 40;
-    v.start = (uint32_t*)lv_start.ptr;
+    lvlog.fill(v);
     return v;
   }
 

@@ -42,7 +42,28 @@ def _square_big(L, seed):
     return off, ids, coef * 3000.0
 
 
+def _ring(n, seed):
+    """+-J ring: two incidences per variable (4-word level entries)."""
+    rng = np.random.default_rng(seed)
+    off = np.arange(0, 2 * n + 1, 2)
+    ids = np.stack([np.arange(n), (np.arange(n) + 1) % n], 1).ravel()
+    return off, ids, rng.choice([-1.0, 1.0], n)
+
+
+def _hub(n, seed):
+    """ER couplings plus a hub joined to every fifth variable: more than 15
+    incidences at the hub (level entries without records)."""
+    off, ids, coef = _er_int(n, 2 * n, seed, 3)
+    hub = np.arange(1, n, 5)
+    off2 = np.concatenate([off, off[-1] + 2 * np.arange(1, len(hub) + 1)])
+    ids2 = np.concatenate([ids, np.stack([np.zeros_like(hub), hub], 1).ravel()])
+    rng = np.random.default_rng(seed + 1)
+    return off2, ids2.astype(ids.dtype), np.concatenate([coef, rng.integers(-3, 4, len(hub)).astype(float)])
+
+
 MODELS = {
+    "ring": lambda: _ring(200, 30),
+    "hub": lambda: _hub(150, 29),
     "square16": lambda: I.square_pm_j(16, seed=31),
     "square_fields": lambda: _square_fields(12, 32),
     "square_big": lambda: _square_big(10, 33),
@@ -84,12 +105,12 @@ def test_levels_sa_matches_oracle(name):
 
 
 LARGE = {
-    # name: (model, sweeps, restarts, kernel param); chunks per lane in brackets
-    "square64_auto": (lambda: I.square_pm_j(64, seed=38), 12, 30, None),      # [2], auto choice
-    "square128": (lambda: I.square_pm_j(128, seed=40), 6, 20, "levels"),      # [4]
-    "square256": (lambda: I.square_pm_j(256, seed=41), 3, 12, "levels"),      # [8], 16-bit sums
-    "square256_big": (lambda: _square_big(256, 42), 3, 12, "levels"),         # [8], 32-bit sums
-    "cubic20": (lambda: I.cubic_pm_j(20, seed=39), 6, 20, "levels"),          # [16]
+    # name: (model, sweeps, restarts, kernel param)
+    "square64_auto": (lambda: I.square_pm_j(64, seed=38), 12, 30, None),      # auto choice
+    "square128": (lambda: I.square_pm_j(128, seed=40), 6, 20, "levels"),
+    "square256": (lambda: I.square_pm_j(256, seed=41), 3, 12, "levels"),
+    "square256_big": (lambda: _square_big(256, 42), 3, 12, "levels"),         # int2 records
+    "cubic20": (lambda: I.cubic_pm_j(20, seed=39), 6, 20, "levels"),
 }
 
 
