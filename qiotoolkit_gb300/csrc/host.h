@@ -69,7 +69,7 @@ struct HostModel
   // level schedule (levels.cu): entries grouped by level, their offsets
   std::vector<int> lv_off, lv_pos;
   std::vector<uint32_t> lv_ent;
-  int n_levels = 0, lv_ew = 0, lv_width = 0;
+  int n_levels = 0, lv_recs = 0, lv_width = 0;
   bool lv_ok = false, lv_d8 = false;
   std::vector<uint32_t> nbr;
   // term -> members

@@ -45,7 +45,7 @@ using namespace qio::mc;
 __device__ double g_ln[1024];
 __device__ float g_scr[1024 * 3];
 
-__host__ __device__ __forceinline__ int phys(int w) { return w + (w >> 5); }
+__host__ __device__ __forceinline__ int phys(int w) { return lv_phys(w); }
 
 __device__ __forceinline__ int rec_other(unsigned int r) { return (int)(r >> 8); }
 __device__ __forceinline__ int rec_coef(unsigned int r) { return (int)(signed char)(r & 0xFFu); }
@@ -83,14 +83,13 @@ __device__ __forceinline__ bool accept_up(uint64_t key, unsigned long long ctr, 
   return d >= 0 ? d == 1 : lut_less_exact(g_ln, cur, rw, __dmul_rn((double)idE, -beta));
 }
 
-// EW: words per level entry (1: the variable only, records from row / rec;
-// 4, 8, 16: the variable and its packed records).  PACK: 32-bit records.
+// RECS: record slots of a level entry (0: the entry is the variable alone,
+// its terms come from row / rec).  PACK: 32-bit records in rec_p.
 // D8: every cost difference fits in 8 bits (logged as bytes, else as 32-bit
 // integers).
-template <int EW, bool PACK, bool D8>
+template <int RECS, bool PACK, bool D8>
 __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a, int stride)
 {
-  static_assert(EW == 1 || PACK, "entries with records hold packed records");
   extern __shared__ __align__(16) uint32_t lv_smem[];
   const unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -174,7 +173,7 @@ __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a,
     {
       const int e0 = e1;
       e1 = __ldg(loff + t + 1);
-      if constexpr (EW == 1)
+      if constexpr (RECS == 0)
       {
         for (int e = e0 + lane; e < e1; e += 32)
         {
@@ -186,7 +185,8 @@ __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a,
       {
         // entries of this level, one per lane at a time; the next entry's
         // words are loaded while this one is tried
-        constexpr int NQ = EW >= 4 ? EW / 4 : 1;
+        constexpr int EW = RECS ? lv_entry_words(RECS) : 4;
+        constexpr int NQ = EW / 4;
         int e = e0 + lane;
         uint4 nx[NQ];
         if (e < e1)
@@ -196,38 +196,32 @@ __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a,
         }
         while (e < e1)
         {
-          uint4 cu[NQ];
+          uint32_t w[4 * NQ];
 #pragma unroll
-          for (int j = 0; j < NQ; j++) cu[j] = nx[j];
+          for (int j = 0; j < NQ; j++)
+          {
+            w[4 * j] = nx[j].x;
+            w[4 * j + 1] = nx[j].y;
+            w[4 * j + 2] = nx[j].z;
+            w[4 * j + 3] = nx[j].w;
+          }
           const int en = e + 32;
           if (en < e1)
           {
 #pragma unroll
             for (int j = 0; j < NQ; j++) nx[j] = __ldg((const uint4*)(ent + (size_t)en * EW) + j);
           }
-          const int v = (int)cu[0].x;
+          const int v = (int)w[0];
           const uint32_t sv = spin(v);
           int iacc = 0;
 #pragma unroll
-          for (int j = 0; j < NQ; j++)
+          for (int j = 1; j <= RECS; j++)
           {
-            if (j > 0)
-            {
-              const int cf = rec_coef(cu[j].x);
-              iacc += (sv ^ spin(rec_other(cu[j].x))) ? -cf : cf;
-            }
-            {
-              const int cf = rec_coef(cu[j].y);
-              iacc += (sv ^ spin(rec_other(cu[j].y))) ? -cf : cf;
-            }
-            {
-              const int cf = rec_coef(cu[j].z);
-              iacc += (sv ^ spin(rec_other(cu[j].z))) ? -cf : cf;
-            }
-            {
-              const int cf = rec_coef(cu[j].w);
-              iacc += (sv ^ spin(rec_other(cu[j].w))) ? -cf : cf;
-            }
+            // record: shared-memory word << 13 | bit << 8 | 8-bit coefficient
+            const uint32_t rq = w[j];
+            const int cf = (int)(signed char)(rq & 0xFFu);
+            const uint32_t z = (sv ^ (sp[rq >> 13] >> ((rq >> 8) & 31u))) & 1u;
+            iacc += z ? -cf : cf;
           }
           attempt(e, v, iacc);
           e = en;
@@ -439,10 +433,10 @@ int lv_stride_words(int n_vars)
 // Warps (walkers) per block: as many as the shared memory and the register
 // budget allow, then evened out so that the last wave's blocks are as full
 // as the others.
-template <int EW, bool PACK, bool D8>
+template <int RECS, bool PACK, bool D8>
 static cudaError_t lv_go(const LvArgs& a, int stride, cudaStream_t s)
 {
-  auto k = lv::lv_sweep_kernel<EW, PACK, D8>;
+  auto k = lv::lv_sweep_kernel<RECS, PACK, D8>;
   const long long sms = 152;
   const int cap = std::min(kLvMaxWarps, kLvSmemBytes / (stride * 4));  // warps per SM
   const long long waves = ((long long)a.n_walkers + sms * cap - 1) / (sms * cap);
@@ -480,17 +474,17 @@ static cudaError_t lv_low(const LvArgs& a, cudaStream_t s)
 
 static cudaError_t lv_sweep_only(const LvArgs& a, int stride, bool d8, cudaStream_t s)
 {
-  switch (a.m.lv_ew)
+  if (a.m.lv_recs > 0 && !a.m.rec_p) return cudaErrorInvalidValue;
+  switch (a.m.lv_recs)
   {
-    case 4: return !a.m.rec_p ? cudaErrorInvalidValue
-                   : (d8 ? lv_go<4, true, true>(a, stride, s) : lv_go<4, true, false>(a, stride, s));
-    case 8: return !a.m.rec_p ? cudaErrorInvalidValue
-                   : (d8 ? lv_go<8, true, true>(a, stride, s) : lv_go<8, true, false>(a, stride, s));
-    case 16: return !a.m.rec_p ? cudaErrorInvalidValue
-                    : (d8 ? lv_go<16, true, true>(a, stride, s) : lv_go<16, true, false>(a, stride, s));
-    case 1:
-      if (a.m.rec_p) return d8 ? lv_go<1, true, true>(a, stride, s) : lv_go<1, true, false>(a, stride, s);
-      return d8 ? lv_go<1, false, true>(a, stride, s) : lv_go<1, false, false>(a, stride, s);
+    case 3: return d8 ? lv_go<3, true, true>(a, stride, s) : lv_go<3, true, false>(a, stride, s);
+    case 4: return d8 ? lv_go<4, true, true>(a, stride, s) : lv_go<4, true, false>(a, stride, s);
+    case 6: return d8 ? lv_go<6, true, true>(a, stride, s) : lv_go<6, true, false>(a, stride, s);
+    case 7: return d8 ? lv_go<7, true, true>(a, stride, s) : lv_go<7, true, false>(a, stride, s);
+    case 15: return d8 ? lv_go<15, true, true>(a, stride, s) : lv_go<15, true, false>(a, stride, s);
+    case 0:
+      if (a.m.rec_p) return d8 ? lv_go<0, true, true>(a, stride, s) : lv_go<0, true, false>(a, stride, s);
+      return d8 ? lv_go<0, false, true>(a, stride, s) : lv_go<0, false, false>(a, stride, s);
     default: return cudaErrorInvalidValue;
   }
 }

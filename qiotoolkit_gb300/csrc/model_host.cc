@@ -462,7 +462,7 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
 static void build_levels(HostModel& m)
 {
   m.lv_ok = m.lv_d8 = false;
-  m.n_levels = m.lv_ew = m.lv_width = 0;
+  m.n_levels = m.lv_recs = m.lv_width = 0;
   m.lv_off.clear();
   m.lv_ent.clear();
   m.lv_pos.clear();
@@ -496,25 +496,35 @@ static void build_levels(HostModel& m)
     width = std::max(width, off[t + 1]);
     off[t + 1] += off[t];
   }
-  int ew = 1;
-  if (!m.rec_p.empty()) ew = maxdeg <= 3 ? 4 : (maxdeg <= 7 ? 8 : (maxdeg <= 15 ? 16 : 1));
+  // record slots of an entry: the fewest of 3, 4, 6, 7, 15 that hold the
+  // largest row (8-bit coefficients only), else 0 (the variable alone)
+  int recs = 0;
+  if (!m.rec_p.empty())
+    for (int c : {3, 4, 6, 7, 15})
+      if (maxdeg <= c)
+      {
+        recs = c;
+        break;
+      }
+  const int ew = recs ? lv_entry_words(recs) : 1;
   const int pad = (int)(((m.N + 31) / 32) * 32);
   std::vector<int> fill(off.begin(), off.end() - 1);
-  std::vector<uint32_t> ent((size_t)m.N * ew, (uint32_t)pad << 8);
+  std::vector<uint32_t> ent((size_t)m.N * ew, recs ? lv_record(pad, 0) : 0u);
   std::vector<int> pos((size_t)((m.N + 31) / 32) * 32, 0);
   for (int64_t v = 0; v < m.N; v++)
   {
     pos[v] = fill[L[v]];
     uint32_t* e = &ent[(size_t)fill[L[v]]++ * ew];
     e[0] = (uint32_t)v;
-    if (ew > 1)
-      for (int q = m.row[v], j = 1; q < m.row[v + 1]; q++, j++) e[j] = m.rec_p[q];
+    if (recs)
+      for (int q = m.row[v], j = 1; q < m.row[v + 1]; q++, j++)
+        e[j] = lv_record(m.other[q] >= 0 ? m.other[q] : pad, m.coef_i[q]);
   }
   m.lv_off.swap(off);
   m.lv_ent.swap(ent);
   m.lv_pos.swap(pos);
   m.n_levels = nl;
-  m.lv_ew = ew;
+  m.lv_recs = recs;
   m.lv_width = width;
   m.lv_d8 = widest <= 127;
   m.lv_ok = true;
@@ -577,7 +587,7 @@ void HostModel::upload() const
   dev.lv_ent = lv_ok ? (const uint32_t*)(b + o_le) : nullptr;
   dev.lv_pos = lv_ok ? (const int*)(b + o_lp) : nullptr;
   dev.n_levels = lv_ok ? n_levels : 0;
-  dev.lv_ew = lv_ok ? lv_ew : 0;
+  dev.lv_recs = lv_ok ? lv_recs : 0;
   dev.lv_d8 = lv_d8 ? 1 : 0;
   uploaded = true;
 }

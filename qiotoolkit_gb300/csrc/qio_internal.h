@@ -66,13 +66,15 @@ struct DevModel
   // level schedule (levels.cu), integer pair-only Ising models: level(v) =
   // 1 + the largest level of v's lower neighbours (0 without one); the
   // variables of level t are entries lv_off[t] .. lv_off[t+1] of lv_ent, in
-  // index order, lv_ew words each: the variable, then (lv_ew > 1) its
-  // records as in rec_p, padded with zero-coefficient padding-spin records
+  // index order.  With lv_recs > 0 an entry is the variable and lv_recs
+  // records lv_record(u, c) of its terms (padded with zero-coefficient
+  // padding-spin records), lv_entry_words(lv_recs) words in all; with
+  // lv_recs == 0 it is the variable alone (records from row / rec)
   const int* lv_off;
   const uint32_t* lv_ent;
   const int* lv_pos;       // entry of each variable (n_vars rounded up to 32)
   int n_levels;
-  int lv_ew;               // words per entry: 1 (records from row / rec), 4, 8 or 16
+  int lv_recs;             // 0, 3, 4, 6, 7 or 15
   int lv_ok;               // the level kernel can run this model
   int lv_d8;               // every cost difference within -128 .. 127
   int scan32;              // 32 cost differences always sum within int32
@@ -214,6 +216,16 @@ struct LvArgs
 // in shared memory per block
 static const int kLvLowThreads = 512;
 static const int kLvRowBytes = 96 * 1024;
+// shared-memory word of spin word w in the level kernel's layout (one
+// padding word after every 32 so that lanes spread over the banks)
+__host__ __device__ inline int lv_phys(int w) { return w + (w >> 5); }
+// a term record of a level entry: the other member's shared-memory word and
+// bit, and the 8-bit coefficient
+inline uint32_t lv_record(int u, int c)
+{
+  return ((uint32_t)lv_phys(u >> 5) << 13) | ((uint32_t)(u & 31) << 8) | ((uint32_t)c & 0xFFu);
+}
+__host__ __device__ constexpr int lv_entry_words(int recs) { return recs <= 3 ? 4 : (recs <= 7 ? 8 : 16); }
 // bytes per logged difference for a model (1 or 4)
 inline int lv_diff_bytes(const DevModel& m) { return m.lv_d8 ? 1 : 4; }
 inline long long lv_diff_stride(int n_vars) { return ((long long)n_vars + 31) & ~31LL; }
