@@ -65,6 +65,10 @@ def batch_instances(n=512):
     return [(int(L), I.cubic_pm_j(int(L), seed=1000 + i)) for i, L in enumerate(Ls)]
 
 
+# the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
+KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel"}
+
+
 def make_workload(name):
     from qiotoolkit_gb300 import instances as I
     if name == "pt_pubo":
@@ -339,11 +343,13 @@ def main():
     barrier(ws)
     torch.cuda.synchronize()
     ms, sweep_ms, launches, att = [], [], 0, 0
+    kernel_used = 1
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             t, st, n_launch = one_step()
             ms.append(t)
             sweep_ms.append(st.sweep_kernel_ms)
+            kernel_used = int(st.sweep_kernel)
             launches += n_launch
             att += int(st.attempts)
     torch.cuda.synchronize()
@@ -357,7 +363,12 @@ def main():
     avg_sweep_launch_ms = statistics.mean(sweep_ms) / sweep_launches_per_step
     attempts_per_launch = A / sweep_launches_per_step
     K = model.info.n_incidences
-    bpa = 9.0 + 13.0 * K / n  # row bounds 8 + own state 1 + per incidence (id 4 + coef 8 + state 1)
+    info = model.info
+    # coefficient bytes: int8 for small integer weights, int32 for other
+    # integers, FP64 otherwise
+    w = 1.0 if info.integer_weights and info.max_coupling <= 127 else (4.0 if info.integer_weights else 8.0)
+    # row bounds 8 + own state 1 + per incidence (id 4 + coefficient w + state 1)
+    bpa = 9.0 + (5.0 + w) * K / n
     achieved = bpa * attempts_per_launch / (avg_sweep_launch_ms / 1e3) / 1e9
     peak, peak_src = peaks()
     traffic = committed_traffic(args.workload)
@@ -386,7 +397,7 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": peak_src, "kernel": "sweep_kernel",
+                         "peak_source": peak_src, "kernel": KERNEL_NAMES.get(kernel_used, "sweep_kernel"),
                          "bytes_per_attempt": bpa,
                          "avg_launch_ms": avg_sweep_launch_ms},
             "cpu_baseline": cpu,
