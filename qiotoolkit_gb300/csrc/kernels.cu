@@ -191,6 +191,85 @@ __device__ void warp_cost(const DevModel& m, const uint32_t* spins, int lane,
   icost = ic;
 }
 
+// Term state bytes (written to ts unless it is null) and the cost of a state
+// by one warp in a single pass over the terms; each lane takes four terms at
+// a time so that their loads overlap.  FP64 values are added in term order
+// (bit-identical to a loop), integers per lane and reduced.
+template <int FL, bool INT>
+__device__ void warp_terms_cost(const DevModel& m, const uint32_t* spins, uint8_t* ts, int lane,
+                                double& cost, long long& icost)
+{
+  constexpr int U = 4;
+  constexpr bool PAR = FL == F_PARITY || FL == F_PLAIN_ISING;
+  double c = 0.0;
+  long long ic = 0;
+  const int M = m.n_terms;
+  for (int t0 = 0; t0 < M; t0 += 32 * U)
+  {
+    int b[U], e[U];
+    uint32_t acc[U];
+#pragma unroll
+    for (int u = 0; u < U; u++)
+    {
+      const int t = t0 + u * 32 + lane;
+      b[u] = t < M ? __ldg(m.trow + t) : 0;
+      e[u] = t < M ? __ldg(m.trow + t + 1) : 0;
+      acc[u] = 0;
+    }
+    // the members of the four terms, position by position
+    for (int k = 0;; k++)
+    {
+      bool more = false;
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (b[u] + k < e[u])
+        {
+          const uint32_t x = __ldg(m.tvar + b[u] + k);
+          const uint32_t sx = spin_of(spins, (int)(x & ~kNegBit));
+          if (PAR) acc[u] ^= sx;
+          else acc[u] += sx ^ (x >> 31);
+          more = more || b[u] + k + 1 < e[u];
+        }
+      if (!more) break;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+    {
+      const int t = t0 + u * 32 + lane;
+      double v = 0.0;
+      long long iv = 0;
+      bool skip = true;
+      if (t < M)
+      {
+        if (ts && (FL == F_PARITY || FL == F_COUNTER)) ts[t] = (uint8_t)acc[u];
+        // parity: the term's sign; counter: the term counts when no literal is true
+        skip = PAR ? false : acc[u] != 0;
+        if (INT) iv = skip ? 0 : (PAR && acc[u] ? -(long long)m.tcost_i[t] : (long long)m.tcost_i[t]);
+        else v = skip ? 0.0 : (PAR && acc[u] ? -m.tcost[t] : m.tcost[t]);
+      }
+      if (INT)
+      {
+        if (!skip) ic += iv;
+        continue;
+      }
+      unsigned keep = __ballot_sync(kFull, !skip);
+      while (keep)
+      {
+        const int j = __ffs(keep) - 1;
+        keep &= keep - 1;
+        c = __dadd_rn(c, __shfl_sync(kFull, v, j));
+      }
+    }
+  }
+  if (INT)
+  {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) ic += __shfl_xor_sync(kFull, ic, d);
+  }
+  cost = c;
+  icost = ic;
+}
+
 // Term state byte from spins: parity (Ising) or true-literal count.
 template <int FL>
 __device__ __forceinline__ uint8_t term_state(const DevModel& m,
@@ -292,11 +371,9 @@ __global__ void __launch_bounds__(128) init_kernel(InitArgs a)
     a.rng[w] = jump_any(rs, var_uniform ? 2ULL * (unsigned long long)N
                                         : (unsigned long long)nwd);
   __syncwarp();
-  if (FL == F_PARITY || FL == F_COUNTER)
-    for (int t = lane; t < m.n_terms; t += 32) ts[t] = term_state<FL>(m, spins, t);
   double cost;
   long long icost;
-  warp_cost<FL, INT>(m, spins, lane, cost, icost);
+  warp_terms_cost<FL, INT>(m, spins, a.skip_terms ? nullptr : ts, lane, cost, icost);
   if (INT) cost = (double)icost;
   for (int q = lane; q < a.p.nw; q += 32) lsp[q] = spins[q];
   if (lane == 0)

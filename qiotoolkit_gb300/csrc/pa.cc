@@ -353,6 +353,8 @@ class PopulationAnnealing : public Solver
     a.m = model->device_view(full_maxsat_sweep);
     a.p = pools[cur].pop;
     a.n_walkers = (int)R;
+    // the lane and level sweeps work from the spins alone
+    a.skip_terms = (lanes || levels) ? 1 : 0;
     if (replay)
     {
       if (streams_on_device)

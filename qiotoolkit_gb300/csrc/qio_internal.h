@@ -137,6 +137,8 @@ struct InitArgs
   long long key_div;
   const uint8_t* given;     // optional: explicit states (n_walkers * n_vars)
   int keep_counters;        // 1: keep attempt/accept totals (population re-init)
+  int skip_terms;           // 1: leave the term state bytes alone (the sweeps
+                            //    that follow work from the spins)
 };
 
 // ---- launchers (kernels.cu) -------------------------------------------

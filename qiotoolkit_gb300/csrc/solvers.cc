@@ -539,11 +539,14 @@ class SimulatedAnnealing : public Solver
     a.seed = seed;
     a.key_base = 0;
     a.key_div = (long long)1 << 40;
-    cuda_check(launch_init(a, st), "init kernel");
-    launches++;
     levels = levels_for(*this, *model);
     lanes = !levels && lanes_for(*this, *model, restarts);
     used_kernel = levels ? 3 : (lanes ? 2 : 1);
+    // the lane and level sweeps work from the spins and rebuild the term
+    // bytes when they finish
+    a.skip_terms = (levels || lanes) ? 1 : 0;
+    cuda_check(launch_init(a, st), "init kernel");
+    launches++;
     if (levels && !lvlog.buf.ptr) device_bytes += (int64_t)lvlog.ensure(R, step_limit, *model, P.pop.nw);
     if (lanes && !L.ready)
     {
@@ -1314,6 +1317,7 @@ class SABatch : public Batch
       a.seed = seed;
       a.key_base = 0;
       a.key_div = (long long)1 << 40;
+      a.skip_terms = (lanes && n_sweeps > 0) ? 1 : 0;  // the lane store rebuilds them
       cuda_check(launch_init(a, st), "init kernel");
       n_launch++;
     }
