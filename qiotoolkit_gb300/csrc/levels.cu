@@ -18,9 +18,11 @@
 // and keeps the first state whose cost drops below the lowest seen
 // (markov/walker.h:209-229,269-280).  The sweep kernel adds up each sweep's
 // accepted differences for the cost and logs, per sweep, its start spins,
-// its start cost and the difference of every attempt (0 when rejected) at
-// the attempt's level entry, where consecutive lanes write consecutive
-// bytes.  The lowest kernel then replays the log sweep by sweep: it puts the
+// its start cost, the start cost plus its negative differences (a bound
+// below its running cost) and the difference of every attempt (0 when
+// rejected) at the attempt's level entry, where consecutive lanes write
+// consecutive bytes.  The lowest kernel then replays the log sweep by sweep
+// (skipping sweeps whose bound is not below the lowest): it puts the
 // differences back in variable order (through each variable's entry),
 // follows the running cost in index order -- integers, the reference's
 // exact sums --, and keeps the first variable where it drops below the
@@ -150,11 +152,11 @@ __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a,
     const size_t lk = (size_t)r * a.log_sweeps + k;
     uint32_t* st = a.start + lk * a.p.nw;
     for (int w = lane; w < nwd; w += 32) st[w] = sp[phys(w)];
-    if (lane == 0) a.cost0[lk] = icost;
+    const long long c_start = icost;
     signed char* de8 = (signed char*)a.diffs + lk * a.diff_stride;
     int* de32 = (int*)a.diffs + lk * a.diff_stride;
 
-    int tot = 0;  // this lane's accepted differences
+    int tot = 0, neg = 0;  // this lane's accepted differences, their negative part
     unsigned int sacc = 0;
     auto attempt = [&](int e, int v, int iacc) {
       const int idE = -2 * iacc;
@@ -166,6 +168,7 @@ __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a,
         atomicXor(&sp[phys(v >> 5)], 1u << (v & 31));
         sacc++;
         tot += idE;
+        neg += min(idE, 0);
       }
     };
     int e1 = __ldg(loff);
@@ -230,9 +233,19 @@ __global__ void __launch_bounds__(kLvMaxWarps * 32, 1) lv_sweep_kernel(LvArgs a,
       __syncwarp();
     }
     nacc += sacc;
-    long long total = tot;
+    long long total = tot, dip = neg;
 #pragma unroll
-    for (int d = 16; d; d >>= 1) total += __shfl_xor_sync(kFull, total, d);
+    for (int d = 16; d; d >>= 1)
+    {
+      total += __shfl_xor_sync(kFull, total, d);
+      dip += __shfl_xor_sync(kFull, dip, d);
+    }
+    // the start cost, and a bound below every running cost of the sweep
+    if (lane == 0)
+    {
+      a.cost0[2 * lk] = c_start;
+      a.cost0[2 * lk + 1] = c_start + dip;
+    }
     icost += total;
   }
 
@@ -284,12 +297,16 @@ __global__ void __launch_bounds__(kLvLowThreads, 2) lv_lowest_kernel(LvArgs a)
     for (int k = 0; k < a.n_sweeps; k++)
     {
       const size_t lk = (size_t)r * a.log_sweeps + k;
-      const long long c0 = a.cost0[lk];
+      const long long c0 = a.cost0[2 * lk];
       const signed char* de8 = (const signed char*)a.diffs + lk * a.diff_stride;
       const int* de32 = (const int*)a.diffs + lk * a.diff_stride;
+      // the previous sweep's readers are done with the row and s_low holds
+      // the lowest so far; a sweep whose running cost cannot get below it is
+      // skipped
+      __syncthreads();
+      if (a.cost0[2 * lk + 1] >= s_low) continue;
       if (STAGE)
       {
-        __syncthreads();  // the previous sweep's readers are done with the row
         const int n16 = (int)((a.diff_stride * (D8 ? 1 : 4)) >> 4);
         const uint4* src = D8 ? (const uint4*)de8 : (const uint4*)de32;
 #pragma unroll 4

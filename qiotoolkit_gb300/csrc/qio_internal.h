@@ -205,8 +205,9 @@ struct LvArgs
   unsigned long long key_base;  //                   key_base + r % key_div)
   long long key_div;
   // the sweep log, log_sweeps sweeps per walker (sweep k of walker r at
-  // r * log_sweeps + k): start spins (p.nw words), start cost, and the
-  // difference of every attempt (0 when rejected) at its level entry
+  // r * log_sweeps + k): start spins (p.nw words), start cost and a bound
+  // below the sweep's running cost (two per sweep), and the difference of
+  // every attempt (0 when rejected) at its level entry
   int log_sweeps;
   uint32_t* start;
   long long* cost0;

@@ -68,7 +68,7 @@ int64_t footprint_of(const HostModel& m, const Solver& s)
   int64_t lv = 0;
   if (m.lv_ok)
   {
-    const int64_t per_sweep = nw * 4 + 8 + ((m.N + 31) & ~31LL) * (m.lv_d8 ? 1 : 4);
+    const int64_t per_sweep = nw * 4 + 16 + ((m.N + 31) & ~31LL) * (m.lv_d8 ? 1 : 4);
     lv = std::min<int64_t>((int64_t)4 << 30, W * std::min<int64_t>(64, steps) * per_sweep);
   }
   return model_bytes(m) + W * per + steps * 8 + W * 64 + lv + 64 * 1024;

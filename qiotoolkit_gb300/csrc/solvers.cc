@@ -400,13 +400,13 @@ size_t LevelLog::ensure(int R, int64_t K, const HostModel& m, int nw)
 {
   const size_t db = m.lv_d8 ? 1 : 4;
   const long long st = lv_diff_stride((int)m.N);
-  const size_t per = (size_t)nw * 4 + 8 + (size_t)st * db;  // one walker, one sweep
+  const size_t per = (size_t)nw * 4 + 16 + (size_t)st * db;  // one walker, one sweep
   const int64_t fit = (int64_t)(kLevelLogBudget / std::max<size_t>(1, per * (size_t)std::max(1, R)));
   const int k = (int)std::max<int64_t>(1, std::min<int64_t>({K, fit, 64}));
   if (buf.ptr && R <= walkers && k <= sweeps) return buf.bytes;
   const size_t n = (size_t)R * k;
   off_cost = (n * nw * 4 + 255) & ~(size_t)255;
-  off_diff = (off_cost + n * 8 + 255) & ~(size_t)255;
+  off_diff = (off_cost + n * 16 + 255) & ~(size_t)255;
   buf = DevBuf(off_diff + n * st * db);
   walkers = R;
   sweeps = k;
