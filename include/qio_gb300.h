@@ -128,6 +128,11 @@ qio_status qio_model_create_dimacs(const char* text, qio_model** out);
  * utils::configure_from_proto_folder): the first file holds the type,
  * version and first terms, later files more terms. */
 qio_status qio_model_create_proto_folder(const char* folder_path, qio_model** out);
+/* Bounds on one flip's cost difference that the parameter-free solvers
+ * derive their temperature ranges from: GraphModel / Ising / Pubo
+ * estimate_min_cost_diff and estimate_max_cost_diff (model/ising.h:176-224,
+ * model/pubo.h:127-184, graph/graph.h:453-485).  Ising and PUBO models. */
+qio_status qio_model_cost_diff_bounds(const qio_model* model, double* min_diff, double* max_diff);
 
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out);
 /* Original variable name of each internal variable (Graph::output_map,

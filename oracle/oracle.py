@@ -47,7 +47,8 @@ class Params(C.Structure):
                 ("rng_mode", C.c_int), ("threads", C.c_int),
                 ("number_of_solutions", C.c_int),
                 ("has_cost_limit", C.c_int), ("cost_limit", C.c_double),
-                ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int)]
+                ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int),
+                ("master_skip", C.c_int64)]
 
 
 def build(force: bool = False) -> str:
@@ -301,7 +302,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         sched_count=None, sweeps_per_replica=1, population=16, alpha=2.0,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
-        full_maxsat_sweep=False, resampling="reference"):
+        full_maxsat_sweep=False, resampling="reference", master_skip=0):
     p = Params()
     p.solver = {"sa": SA, "pt": PT, "pa": PA}[solver]
     p.seed = seed & 0xFFFFFFFF
@@ -323,6 +324,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
     p.cost_limit = float(cost_limit or 0.0)
     p.full_maxsat_sweep = int(full_maxsat_sweep)
     p.resampling = {"reference": 0, "multinomial": 1}[resampling]
+    p.master_skip = int(master_skip)
     err = C.create_string_buffer(512)
     h = lib().orc_run(model.h, C.byref(p), err, 512)
     del keep
@@ -343,3 +345,145 @@ def pt_toy(seed, steps, temps, use_inverse=False):
     lib().orc_pt_toy(seed, steps, _p(t, C.c_double), len(t), int(use_inverse),
                      _p(obs, C.c_double), C.byref(best))
     return obs, best.value
+
+
+# ---------------------------------------------------------------- parameter-free SA
+MIN_DELTA_DEFAULT = 0.1  # model/graph_model.h:16
+
+
+def _least_diff_one(vals):
+    """utils::least_diff_method (one multiset), utils/utils.cc:43-53."""
+    s = sorted(vals)
+    while len(s) > 1:
+        a = s.pop()
+        b = s.pop()
+        d = a - b
+        # keep the list sorted
+        lo, hi = 0, len(s)
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if s[mid] <= d:
+                lo = mid + 1
+            else:
+                hi = mid
+        s.insert(lo, d)
+    return s[0]
+
+
+def _least_diff_two(a, b):
+    """utils::least_diff_method (two multisets), utils/utils.cc:55-100."""
+    a, b = sorted(a), sorted(b)
+    mn = float(np.finfo(np.float64).max)
+    if not a and b:
+        return b[0]
+    if a and not b:
+        return a[0]
+    import bisect
+    while a and b:
+        ca, cb = a.pop(), b.pop()
+        d = ca - cb
+        if d > 0:
+            bisect.insort(a, d)
+        elif d < 0:
+            d = -d
+            bisect.insort(b, d)
+        elif len(a) < len(b):
+            bisect.insort(a, ca)
+        else:
+            bisect.insort(b, cb)
+        if mn > d and d != 0:
+            mn = d
+    return mn
+
+
+def cost_diff_bounds(kind, terms):
+    """(estimate_min_cost_diff, estimate_max_cost_diff) of an Ising or PUBO
+    term list (model/ising.h:176-224, model/pubo.h:127-184, graph/graph.h:
+    453-485): per variable, the coefficients of the terms it appears in
+    (constant terms excluded)."""
+    inc = {}
+    for c, ids in terms:
+        for v in set(ids):
+            inc.setdefault(v, []).append(float(c))
+    ising = kind.startswith("ising")
+
+    def seq_abs_sum(cs):  # left to right in doubles (Python's sum() compensates)
+        t = 0.0
+        for c in cs:
+            t += abs(c)
+        return t
+    mx = max(seq_abs_sum(cs) for cs in inc.values())
+    big = float(np.finfo(np.float64).max)
+    mn = big
+    for cs in inc.values():
+        if ising:
+            local = _least_diff_one([abs(c) for c in cs])
+        else:
+            local = _least_diff_two([c for c in cs if c > 0], [-c for c in cs if c < 0])
+        if local == 0:
+            continue
+        mn = min(mn, local)
+    if mn == big:
+        mn = MIN_DELTA_DEFAULT
+    return (mn * 2, mx * 2) if ising else (mn, mx)
+
+
+def sa_parameter_free(model: Model, kind, terms, *, seed, min_num_restarts, samples=(10, 20, 30, 50),
+                      max_prob=0.5, min_prob=0.0001, adjust=0.001, change=1.5,
+                      nonimprovement_limit=8, max_runs=400, threads=4):
+    """ParameterFreeLinearSearchSolver<SAParameterFree> restated
+    (solver/parameter_free_solver.h:65-151, strategy/linear_search.cc,
+    solver/sa_parameter_free.h): repeated oracle SA runs whose restarts fork
+    from one continuing master stream.  Returns the per-run trace
+    [(sweeps, restarts, lowest)], the best cost and state, and the best run's
+    (sweeps, restarts).  Stops on the non-improvement rule (no time limit)."""
+    import math
+    mn, mx = cost_diff_bounds(kind, terms)
+    b0 = -math.log(max_prob) / mx
+    b1 = -math.log(min_prob) / (mn + adjust * (mx - mn))
+    points = list(samples)
+    objs = [float(np.finfo(np.float64).max)] * len(points)
+    init_min = points[0]
+    cur = -1
+    skip = 0
+    best = None
+    best_state = None
+    best_exec = 0.0
+    best_params = None
+    stable = 0
+    trace = []
+    for _ in range(max_runs):
+        cur += 1
+        if cur >= len(points):
+            cur = 0
+            lowest = objs.index(min(objs))
+            if lowest == 0:
+                if points[0] > init_min:
+                    points = [int(p / change) for p in points]
+            elif lowest == len(points) - 1:
+                points = [int(p * change) for p in points]
+            objs = [float(np.finfo(np.float64).max)] * len(points)
+        sweeps, back = points[cur], points[-1]
+        sl = max(sweeps, 2)
+        r = min_num_restarts * back // sweeps
+        res = run(model, "sa", seed=seed, step_limit=sl, restarts=r, use_inverse=True,
+                  sched=("linear", b0, b1), threads=threads, master_skip=skip)
+        skip += r
+        obj = float(res.best_cost)
+        objs[cur] = obj
+        trace.append((sl, r, obj))
+        exec_cost = float(sl) * float(r)
+        done = False
+        if best is not None and abs(best - obj) < 10E-12:
+            stable += 1
+            if exec_cost < best_exec:
+                best, best_state, best_exec, best_params = obj, res.best_state.copy(), exec_cost, (sl, r)
+        if stable >= nonimprovement_limit:
+            done = True
+        if best is None or best - obj > 10E-12:
+            stable = 0
+            best, best_state, best_exec, best_params = obj, res.best_state.copy(), exec_cost, (sl, r)
+        if done:
+            break
+    return {"trace": trace, "best": best, "best_state": best_state, "params": best_params,
+            "betas": (b0, b1)}

@@ -947,6 +947,7 @@ static Result run_sa(const Model& m, const orc_params& p)
   }
   size_t R = (size_t)p.restarts;
   PcgRng master(p.seed);
+  for (int64_t k = 0; k < p.master_skip; k++) master.uint32();
   std::vector<std::unique_ptr<Rng>> rngs(R);
   for (size_t i = 0; i < R; i++) rngs[i] = master.fork();
   std::vector<Walker> reps(R);

@@ -65,6 +65,10 @@ typedef struct orc_params {
   int resampling;             /* PA: 0 the reference's (Poisson / constant),
                                  1 multinomial on counter draws (the GB300
                                  library's device mode, restated here) */
+  int64_t master_skip;        /* SA: draws taken from the master stream before
+                                 the restarts fork (a run that continues the
+                                 stream of earlier runs, as the parameter-free
+                                 solvers' repeated SA runs do) */
 } orc_params;
 
 /* ---- random generator pins ---- */

@@ -72,6 +72,7 @@ def _signatures():
         "qio_model_create_json": (st, [cp, i32, P(vp)]),
         "qio_model_create_dimacs": (st, [cp, P(vp)]),
         "qio_model_create_proto_folder": (st, [cp, P(vp)]),
+        "qio_model_cost_diff_bounds": (st, [vp, P(C.c_double), P(C.c_double)]),
         "qio_model_get_info": (st, [vp, P(ModelInfo)]),
         "qio_model_get_var_names": (st, [vp, P(C.c_int32)]),
         "qio_model_destroy": (st, [vp]),

@@ -66,6 +66,12 @@ class Model:
         check(load().qio_model_create_json(doc.encode(), int(kind), C.byref(h)))
         return cls(None, _handle=h)
 
+    def cost_diff_bounds(self):
+        """(min, max) estimates of one flip's cost difference."""
+        lo, hi = C.c_double(), C.c_double()
+        check(load().qio_model_cost_diff_bounds(self._h, C.byref(lo), C.byref(hi)))
+        return lo.value, hi.value
+
     @classmethod
     def from_proto_folder(cls, path: str) -> "Model":
         """Model from a protobuf problem folder (<name>/<name>_<k>.pb)."""

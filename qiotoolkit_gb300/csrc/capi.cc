@@ -117,6 +117,15 @@ qio_status qio_model_create_proto_folder(const char* folder_path, qio_model** ou
   });
 }
 
+qio_status qio_model_cost_diff_bounds(const qio_model* model, double* min_diff, double* max_diff)
+{
+  return guard([&] {
+    if (!model || !min_diff || !max_diff) fail(1, "arguments must not be null");
+    *min_diff = estimate_min_cost_diff(*model->m);
+    *max_diff = estimate_max_cost_diff(*model->m);
+  });
+}
+
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out)
 {
   return guard([&] {

@@ -106,6 +106,9 @@ std::unique_ptr<HostModel> build_model_json(const json::Value& doc, int kind);
 std::unique_ptr<HostModel> build_model_dimacs(const std::string& text);
 // protobuf problem folder <name>/<name>_<k>.pb -> model (proto.cc)
 std::unique_ptr<HostModel> build_model_proto_folder(const std::string& folder_path);
+// bounds on one flip's cost difference (parameter-free solvers)
+double estimate_max_cost_diff(const HostModel& m);
+double estimate_min_cost_diff(const HostModel& m);
 
 // Schedule (schedule/schedule.cc, linear.cc, geometric.cc, segments.cc).
 struct Schedule
@@ -147,6 +150,8 @@ class Solver
   virtual bool historical_lowest(double&, std::vector<uint8_t>&) { return false; }
   virtual std::string target() const = 0;
   virtual uint64_t total_windows() { return 0; }
+  // extra members of the result's benchmark block (JSON, starting with ',')
+  virtual std::string extra_benchmark() { return ""; }
   // Serving: the solve in pieces.  After init(), advance() enqueues up to n
   // further steps on the stream and returns true once the step budget is
   // spent (results are read after the stream has finished).  The pieces

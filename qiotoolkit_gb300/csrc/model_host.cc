@@ -788,3 +788,115 @@ Schedule parse_schedule(const json::Value& v, const std::string& name)
   return s;
 }
 }  // namespace qio
+
+// ---------------------------------------------------------------------------
+// Bounds on a single flip's cost difference, used by the parameter-free
+// solvers to place their temperature ranges.
+// ---------------------------------------------------------------------------
+namespace qio
+{
+static const double kMinDeltaDefault = 0.1;  // MIN_DELTA_DEFAULT, model/graph_model.h:16
+
+// utils::least_diff_method, utils/utils.cc:43-53: replace the two largest
+// values by their difference until one value is left
+static double least_diff_one(std::multiset<double> s)
+{
+  while (s.size() > 1)
+  {
+    auto a = std::prev(s.end());
+    const double x = *a;
+    s.erase(a);
+    auto b = std::prev(s.end());
+    const double y = *b;
+    s.erase(b);
+    s.insert(x - y);
+  }
+  return *s.begin();
+}
+
+// the two-set form, utils/utils.cc:55-100: the largest of each set cancel;
+// the smallest non-zero remainder is kept
+static double least_diff_two(std::multiset<double> a, std::multiset<double> b)
+{
+  double mn = std::numeric_limits<double>::max();
+  if (a.empty() && !b.empty()) return *b.begin();
+  if (!a.empty() && b.empty()) return *a.begin();
+  while (!a.empty() && !b.empty())
+  {
+    auto ia = std::prev(a.end());
+    const double ca = *ia;
+    a.erase(ia);
+    auto ib = std::prev(b.end());
+    const double cb = *ib;
+    b.erase(ib);
+    double delta = ca - cb;
+    if (delta > 0)
+      a.insert(delta);
+    else if (delta < 0)
+    {
+      delta = -delta;
+      b.insert(delta);
+    }
+    else if (a.size() < b.size())
+      a.insert(ca);
+    else
+      b.insert(cb);
+    if (mn > delta && delta != 0) mn = delta;
+  }
+  return mn;
+}
+
+// Ising: twice the largest sum of |c| over a variable's terms
+// (model/ising.h:176-179, graph/graph.h:453-485); PUBO: that sum itself
+// (model/graph_model.h:194-197)
+double estimate_max_cost_diff(const HostModel& m)
+{
+  if (m.kind == K_MAXSAT) fail(1, "cost difference estimates are not available for maxsat models");
+  double mx = 0;
+  for (int64_t v = 0; v < m.N; v++)
+  {
+    double s = 0;
+    for (int q = m.row[v]; q < m.row[v + 1]; q++) s += std::abs(m.coef[q]);
+    mx = s > mx ? s : mx;
+  }
+  return (m.kind == K_ISING || m.kind == K_ISING_PLAIN) ? mx * 2 : mx;
+}
+
+// Ising (model/ising.h:181-224): per variable the single-set least
+// difference of its |c|, zeros skipped, the smallest doubled; PUBO
+// (model/pubo.h:127-184): the two-set least difference of its positive and
+// negated negative c.  No non-zero value: MIN_DELTA_DEFAULT (doubled for
+// Ising).
+double estimate_min_cost_diff(const HostModel& m)
+{
+  if (m.kind == K_MAXSAT) fail(1, "cost difference estimates are not available for maxsat models");
+  const bool ising = m.kind == K_ISING || m.kind == K_ISING_PLAIN;
+  double mn = std::numeric_limits<double>::max();
+  for (int64_t v = 0; v < m.N; v++)
+  {
+    double local;
+    if (ising)
+    {
+      std::multiset<double> s;
+      for (int q = m.row[v]; q < m.row[v + 1]; q++) s.insert(std::abs(m.coef[q]));
+      if (s.empty()) continue;
+      local = least_diff_one(s);
+    }
+    else
+    {
+      std::multiset<double> pos, neg;
+      for (int q = m.row[v]; q < m.row[v + 1]; q++)
+      {
+        const double c = m.coef[q];
+        if (c > 0) pos.insert(c);
+        else if (c < 0) neg.insert(-c);
+      }
+      local = least_diff_two(pos, neg);
+    }
+    if (local == 0) continue;
+    mn = local < mn ? local : mn;
+  }
+  if (mn == std::numeric_limits<double>::max()) mn = kMinDeltaDefault;
+  return ising ? mn * 2 : mn;
+}
+}  // namespace qio

@@ -1,6 +1,7 @@
 // solvers.cc -- host drivers of the simulated annealing and parallel
 // tempering solvers, configured from the reference's params JSON.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -463,8 +464,32 @@ class SimulatedAnnealing : public Solver
   LaneRunner L;
   bool lanes = false, levels = false;
   LevelLog lvlog;
+  Pcg* ext_master = nullptr;  // repeated runs: the restarts fork from this stream
 
   std::string target() const override { return "simulatedannealing.qiotoolkit"; }
+
+  // A new run of `sweeps` sweeps and `r` restarts on the linear beta schedule
+  // b0 -> b1 (SAParameterFree::update_parameters, solver/sa_parameter_free.h:
+  // 120-137); the population is sized afresh at the next init.
+  void retarget(int64_t sweeps, int64_t r, double b0, double b1)
+  {
+    step_limit = sweeps;
+    restarts = r;
+    use_inverse = true;
+    schedule = Schedule();
+    schedule.type = 0;
+    schedule.initial = b0;
+    schedule.final_ = b1;
+    schedule.has_stop = true;
+    schedule.stop_ = (double)std::max<int64_t>(1, sweeps - 1);
+    betas.resize(step_limit);
+    for (int64_t k = 0; k < step_limit; k++) betas[k] = beta_of(schedule.get_value((double)k), true);
+    P = Population();
+    L = LaneRunner();
+    lvlog = LevelLog();
+    initialized = ran = false;
+    step_pos = 0;
+  }
 
   void configure(const json::Value& doc)
   {
@@ -524,7 +549,8 @@ class SimulatedAnnealing : public Solver
     device_bytes = (int64_t)P.buf.bytes;
     // rngs_[i] = rng_->fork() in index order (solver/simulated_annealing.h:53-56)
     std::vector<uint64_t> rs(R);
-    Pcg master(seed);
+    Pcg own(seed);
+    Pcg& master = ext_master ? *ext_master : own;
     for (int i = 0; i < R; i++) rs[i] = Pcg(master.next()).state;
     cuda_check(cudaMemcpyAsync(P.rng, rs.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D rng");
     if (step_limit > 0)
@@ -1089,6 +1115,262 @@ class ParallelTempering : public Solver
 
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc);
 
+// ---------------------------------------------------------------------------
+// Parameter-free simulated annealing ("simulatedannealing-parameterfree.
+// qiotoolkit": solver/parameter_free_solver.h:9-257 with the linear search of
+// solver/parameter_free_linear_solver.h and strategy/linear_search.cc, the SA
+// adapter of solver/sa_parameter_free.h).  Repeated SA runs: run j takes
+// sweeps = the next sample point and restarts = min_num_restarts x the last
+// sample point / sweeps, on the linear beta schedule from -ln(max_prob) /
+// max cost difference to -ln(min_prob) / (adjusted min cost difference); after
+// each pass over the sample points they are stretched by the change factor
+// when the last one gave the lowest cost and shrunk when the first did.  The
+// restarts of every run fork from one master stream that continues across
+// runs.  The search stops when `nonimprovement_limit` runs in a row find no
+// lower cost, or at the time limit (default 5 s), checked between runs (the
+// reference also hands the remaining time to the run itself).  The result
+// is the lowest cost found and its state; the parameters shown are those of
+// the run that found it (with equal costs, the cheaper run's: sweeps x
+// restarts).
+// ---------------------------------------------------------------------------
+class SAParameterFree : public Solver
+{
+ public:
+  std::unique_ptr<SimulatedAnnealing> w;
+  double max_prob = 0.5, min_prob = 0.0001, adjust = 0.001, change = 1.5;
+  double beta_start = 0.01, beta_stop = 10.0;
+  std::vector<int> samples{10, 20, 30, 50};
+  int64_t min_restarts = 1;
+  int nonimprovement_limit = 8;
+  // linear search state (strategy/linear_search.cc)
+  std::vector<int> points;
+  std::vector<double> objs;
+  int cur = -1, init_min = 0;
+  Pcg master{0};
+  // best so far (ParameterFreeSolver::update_best)
+  bool has_best = false;
+  double best = 0, best_exec = 0;
+  int stable = 0;
+  int64_t best_sweeps = 0, best_restarts = 0;
+  std::vector<uint8_t> best_state;
+  std::vector<std::array<double, 3>> trace;  // per run: sweeps, restarts, lowest cost
+  uint64_t att_total = 0, acc_total = 0;
+  std::string stop_reason;
+
+  std::string target() const override { return "simulatedannealing-parameterfree.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    if (!replay) fail(1, "parameter-free solvers run with \"rng_mode\": \"replay\"");
+    if (number_of_solutions != 1) fail(1, "parameter-free solvers return one solution: `number_of_solutions` must be 1");
+    Params p(params);
+    auto prob = [&](const char* k, double def) {
+      const double v = p.num(k, def);
+      if (!(v > 0 && v <= 1)) fail(1, std::string("parameter `") + k + "`: must be in (0, 1], found " + json::number(v));
+      return v;
+    };
+    max_prob = prob("max_prob", 0.5);
+    min_prob = prob("min_prob", 0.0001);
+    adjust = prob("min_cost_diff_adjustment_factor", 0.001);
+    change = p.num("search_interval_change_factor", 1.5);
+    if (const json::Value* v = p.get("initial_sweeps_sample_points"))
+    {
+      if (!v->is_array() || v->arr.size() <= 2)
+        fail(1, "parameter `initial_sweeps_sample_points`: expected an array of more than 2 integers");
+      samples.clear();
+      for (const auto& x : v->arr)
+      {
+        if (!x.is_number() || x.num < 1) fail(1, "parameter `initial_sweeps_sample_points`: expected positive integers");
+        samples.push_back((int)x.num);
+      }
+    }
+    min_restarts = p.integer("min_num_restarts", threads);
+    if (min_restarts <= 0) fail(1, "parameter `min_num_restarts`: must be greater than 0");
+    nonimprovement_limit = (int)p.integer("nonimprovement_limit", 8);
+    if (nonimprovement_limit <= 0) fail(1, "parameter `nonimprovement_limit`: must be greater than 0");
+    if (!has_time_limit)
+    {
+      has_time_limit = true;  // a time limit must be set (parameter_free_solver.h:56-61)
+      time_limit = 5.0;
+    }
+    w.reset(new SimulatedAnnealing());
+    w->model = model;
+    w->configure(doc);
+    if (!model->empty())
+    {
+      const double mx = estimate_max_cost_diff(*model), mn = estimate_min_cost_diff(*model);
+      if (mx <= 0) fail(1, "max cost difference should be > 0, found :" + json::number(mx));
+      if (mn <= 0) fail(1, "min cost difference should be > 0, found :" + json::number(mn));
+      if (mn > mx)
+        fail(1, "min cost difference should be <= max cost difference, found :" + json::number(mn) + " > " +
+                    json::number(mx));
+      beta_start = -std::log(max_prob) / mx;
+      beta_stop = -std::log(min_prob) / (mn + adjust * (mx - mn));
+    }
+    render_params(samples[0], min_restarts);
+  }
+
+  void render_params(int64_t sweeps, int64_t r)
+  {
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"beta_start", json::number(beta_start)});
+    output_params.push_back({"beta_stop", json::number(beta_stop)});
+    output_params.push_back({"restarts", std::to_string(r)});
+    output_params.push_back({"sweeps", std::to_string(sweeps)});
+  }
+
+  int64_t n_walkers() const override { return (model->empty() || !has_best) ? 0 : 1; }
+
+  void init(cudaStream_t) override
+  {
+    initialized = true;
+    ran = false;
+    master = Pcg(seed);
+    points = samples;  // LinearSearchOpt::set_ranges
+    objs.assign(points.size(), std::numeric_limits<double>::max());
+    init_min = points[0];
+    cur = -1;
+    has_best = false;
+    stable = 0;
+    trace.clear();
+    att_total = acc_total = 0;
+    best_state.clear();
+    stop_reason.clear();
+    last_step = 0;
+  }
+
+  // LinearSearchOpt::fit_sample_points: shrink when the first point gave the
+  // lowest cost (unless already at the initial first point), stretch when
+  // the last one did
+  void fit_points()
+  {
+    const int lowest = (int)(std::min_element(objs.begin(), objs.end()) - objs.begin());
+    if (lowest == 0)
+    {
+      if (points[0] > init_min)
+        for (int& x : points) x = (int)((double)x / change);
+    }
+    else if (lowest == (int)points.size() - 1)
+      for (int& x : points) x = (int)((double)x * change);
+    objs.assign(points.size(), std::numeric_limits<double>::max());
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    auto t0 = std::chrono::steady_clock::now();
+    auto elapsed = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+    for (int64_t step = 0;; step++)
+    {
+      // LinearSearchOpt::recommend_parameter_values (two dimensions)
+      cur++;
+      if (cur >= (int)points.size())
+      {
+        cur = 0;
+        fit_points();
+      }
+      const int sweeps = points[cur], back = points.back();
+      if (elapsed() >= time_limit && has_best)
+      {
+        stop_reason = "time limit";
+        break;
+      }
+      // SAParameterFree::update_parameters
+      const int64_t sl = std::max(sweeps, 2);
+      const int64_t r = (int64_t)((int)min_restarts * back / sweeps);
+      if (r <= 0) fail(1, "parameter-free search reached a run with no restarts");
+      w->retarget(sl, r, beta_start, beta_stop);
+      w->ext_master = &master;
+      w->init(st);
+      w->run(st);
+      launches += w->launches;
+      std::vector<double> c, low;
+      std::vector<uint64_t> at, ac;
+      std::vector<uint8_t> ls;
+      w->fetch(c, low, at, ac, &ls, nullptr);
+      size_t b = 0;
+      for (size_t i = 1; i < low.size(); i++)
+        if (low[i] < low[b]) b = i;
+      const double obj = low[b];
+      for (size_t i = 0; i < at.size(); i++)
+      {
+        att_total += at[i];
+        acc_total += ac[i];
+      }
+      objs[cur] = obj;  // LinearSearchOpt::add_new_sample
+      trace.push_back({(double)sl, (double)r, obj + model->const_cost});
+      const double exec = (double)sl * (double)r;  // estimate_execution_cost, up to the thread divisor
+      auto update_best = [&] {
+        best = obj;
+        best_exec = exec;
+        best_sweeps = sl;
+        best_restarts = r;
+        best_state.assign(ls.begin() + b * model->N, ls.begin() + (b + 1) * model->N);
+      };
+      // ParameterFreeSolver::make_step, solver/parameter_free_solver.h:123-151
+      bool done = false;
+      if (has_best && std::abs(best - obj) < 10E-12)
+      {
+        stable++;
+        if (exec < best_exec) update_best();
+      }
+      if (stable >= nonimprovement_limit)
+      {
+        done = true;
+        stop_reason = "no improvement";
+      }
+      if (!has_best || best - obj > 10E-12)
+      {
+        stable = 0;
+        has_best = true;
+        update_best();
+      }
+      last_step = step + 1;
+      if (done) break;
+      if (has_cost_limit && best <= cost_limit)
+      {
+        stop_reason = "cost limit";
+        break;
+      }
+    }
+    render_params(best_sweeps, best_restarts);
+    run_ms = elapsed() * 1e3;
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
+             std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
+             std::vector<uint8_t>* states) override
+  {
+    // one entry: the best state found over all runs
+    cost.clear();
+    lowest.clear();
+    att.clear();
+    acc.clear();
+    if (model->empty() || !has_best) return;
+    cost.push_back(best);
+    lowest.push_back(best);
+    att.push_back(att_total);
+    acc.push_back(acc_total);
+    if (lowest_states) *lowest_states = best_state;
+    if (states) *states = best_state;
+  }
+
+  std::string extra_benchmark() override
+  {
+    std::string s = ",\"parameter_free\":{\"runs\":[";
+    for (size_t i = 0; i < trace.size(); i++)
+      s += (i ? "," : "") + std::string("{\"sweeps\":") + std::to_string((int64_t)trace[i][0]) +
+           ",\"restarts\":" + std::to_string((int64_t)trace[i][1]) + ",\"lowest\":" + json::number(trace[i][2]) +
+           "}";
+    s += "],\"stop\":" + json::quote(stop_reason) + "}";
+    return s;
+  }
+};
+
 std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& target,
                                     const json::Value& doc)
 {
@@ -1107,6 +1389,13 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
     return std::unique_ptr<Solver>(s.release());
   }
   if (target == "populationannealing.cpu") return make_pa_solver(m, doc);
+  if (target == "simulatedannealing-parameterfree.qiotoolkit")
+  {
+    std::unique_ptr<SAParameterFree> s(new SAParameterFree());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
   fail(1, "Unknown solver: " + target);
 }
 
@@ -1600,7 +1889,8 @@ std::string Solver::result_json()
                       (ran ? "" : ",\"not_run\":true") + "}" +
                       ",\"gb300\":{\"run_ms\":" + json::number(run_ms) +
                       ",\"kernel_launches\":" + std::to_string(launches) +
-                      ",\"rng_mode\":" + json::quote(replay ? "replay" : "counter") + "}}";
+                      ",\"rng_mode\":" + json::quote(replay ? "replay" : "counter") + "}" +
+                      extra_benchmark() + "}";
   return "{\"benchmark\":" + bench + ",\"solutions\":" + sol + "}";
 }
 }  // namespace qio

@@ -18,6 +18,9 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
   dimacs_pins.json   utils/test/dimacs_test.cc (inputs and expected parses)
+  estimator_pins.json  model/test/ising_test.cc, model/test/pubo_test.cc:
+                     the estimate_min_cost_diff / estimate_max_cost_diff tests
+                     (inline or fixture models, expected values)
   proto_pins.json    data/*_pb/*.pb (bytes as written by the reference's
                      protobuf serialiser) with the terms their writers put
                      in: utils/test/stream_test.h:145-168,
@@ -259,6 +262,43 @@ def proto_pins():
                 "ex_input_problem_pb": {"type": "softspin", "version": "0.1"}}}
 
 
+def estimator_pins():
+    """Tests that call estimate_min_cost_diff / estimate_max_cost_diff: the
+    model (inline JSON, or the test fixture's) and the expected values, with
+    MIN_DELTA_DEFAULT taken from model/graph_model.h."""
+    m = re.search(r"#define MIN_DELTA_DEFAULT ([0-9.]+)", read("model/graph_model.h"))
+    delta = float(m.group(1))
+    cases = []
+    for rel in ("model/test/ising_test.cc", "model/test/pubo_test.cc"):
+        src = read(rel)
+        fixtures = {}
+        for f in re.finditer(r"class (\w+) : public testing::Test(.*?)\n};", src, re.S):
+            j = re.search(r'R"\((.*?)\)"', f.group(2), re.S)
+            if j:
+                fixtures[f.group(1)] = j.group(1)
+        for t in re.finditer(r"TEST(_F)?\((\w+), (\w+)\)\s*\{(.*?)\n\}", src, re.S):
+            fixture, suite, name, body = t.group(1), t.group(2), t.group(3), t.group(4)
+            if "estimate_" not in body or "proto" in name:
+                continue
+            j = re.search(r'R"\((.*?)\)"', body, re.S)
+            text = j.group(1) if j else fixtures.get(suite) if fixture else None
+            if text is None:
+                continue
+            doc = json.loads(text)
+            exp = {}
+            for e in re.finditer(r"EXPECT_(?:DOUBLE_)?EQ\((.*?), (\w+)\);", body):
+                var = e.group(2)
+                call = re.search(r"double %s = \w+\.(estimate_\w+)\(\)" % var, body)
+                if not call:
+                    continue
+                val = e.group(1).replace("MIN_DELTA_DEFAULT", repr(delta))
+                exp[call.group(1)] = float(eval(val, {"__builtins__": {}}))
+            if exp:
+                cases.append({"source": f"{rel} {suite}.{name}", "model": terms_of(doc),
+                              "expected": exp})
+    return {"min_delta_default": delta, "cases": cases}
+
+
 def main():
     if not os.path.isdir(CPP):
         print("reference not found at", REFERENCE, file=sys.stderr)
@@ -266,7 +306,7 @@ def main():
     files = {"rng_pins.json": rng_pins(), "pt_toy_pin.json": pt_toy_pin(),
              "model_pins.json": model_pins(), "solver_pins.json": solver_pins(),
              "planted.json": planted(), "dimacs_pins.json": dimacs_pins(),
-             "proto_pins.json": proto_pins()}
+             "proto_pins.json": proto_pins(), "estimator_pins.json": estimator_pins()}
     for name, obj in files.items():
         with open(os.path.join(OUT, name), "w") as f:
             json.dump(obj, f, separators=(",", ":"))

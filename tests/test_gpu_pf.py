@@ -1,0 +1,50 @@
+"""Parameter-free simulated annealing on the GPU against the oracle.
+
+The library's search (linear search over sweep sample points, repeated SA
+runs whose restarts fork from one continuing master stream) must make the
+same runs with the same lowest costs as the oracle's restatement of
+ParameterFreeLinearSearchSolver<SAParameterFree>, and return the same best
+state and parameters.  The cases stop on the non-improvement rule, well
+inside the time limit, and have no constant term (lowest costs compare
+directly).
+"""
+import numpy as np
+import pytest
+
+import qiotoolkit_gb300 as q
+from qiotoolkit_gb300 import instances as I
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PF = "simulatedannealing-parameterfree.qiotoolkit"
+
+CASES = {
+    "er_ising": ("ising", lambda: I.er_ising(60, 150, seed=51), 11),
+    "pubo": ("pubo", lambda: I.random_pubo(40, 100, seed=52), 12),
+    "square_pm_j": ("ising", lambda: I.square_pm_j(8, seed=53), 13),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_sa_parameter_free_matches_oracle(name):
+    kind, gen, seed = CASES[name]
+    off, ids, coef = gen()
+    terms = [(float(coef[k]), [int(x) for x in ids[off[k]:off[k + 1]]]) for k in range(len(coef))]
+    g = q.Model(kind, off=off, ids=ids, coef=coef)
+    o = O.Model(kind, off=off, ids=ids, coef=coef)
+    params = {"seed": seed, "min_num_restarts": 4, "timeout": 120}
+    s = q.Solver(g, PF, {"params": params}).init().run()
+    res = s.result()
+    runs = res["benchmark"]["parameter_free"]["runs"]
+    assert res["benchmark"]["parameter_free"]["stop"] == "no improvement"
+    ref = O.sa_parameter_free(o, kind, terms, seed=seed, min_num_restarts=4)
+    assert [(r["sweeps"], r["restarts"], r["lowest"]) for r in runs] == \
+        [(sl, r, obj) for sl, r, obj in ref["trace"]]
+    sol = res["solutions"]
+    assert (sol["parameters"]["sweeps"], sol["parameters"]["restarts"]) == ref["params"]
+    b0, b1 = ref["betas"]
+    assert sol["parameters"]["beta_start"] == b0 and sol["parameters"]["beta_stop"] == b1
+    rep = s.replicas()
+    np.testing.assert_array_equal(rep["lowest"], [ref["best"]])
+    np.testing.assert_array_equal(rep["lowest_states"][0], ref["best_state"])
