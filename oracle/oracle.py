@@ -48,7 +48,8 @@ class Params(C.Structure):
                 ("number_of_solutions", C.c_int),
                 ("has_cost_limit", C.c_int), ("cost_limit", C.c_double),
                 ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int),
-                ("master_skip", C.c_int64)]
+                ("master_skip", C.c_int64), ("use_master_state", C.c_int),
+                ("master_state", C.c_uint64)]
 
 
 def build(force: bool = False) -> str:
@@ -108,6 +109,8 @@ def lib():
         L.orc_res_lowest_states.argtypes = [vp, P(C.c_uint8)]
         L.orc_res_best_cost.argtypes = [vp]
         L.orc_res_best_cost.restype = dbl
+        L.orc_res_master_state.argtypes = [vp]
+        L.orc_res_master_state.restype = C.c_uint64
         L.orc_res_best_state.argtypes = [vp, P(C.c_uint8)]
         L.orc_res_solutions.argtypes = [vp, P(dbl), P(C.c_uint8)]
         L.orc_res_pt_observables.argtypes = [vp, P(dbl)]
@@ -276,6 +279,7 @@ class Result:
             L.orc_res_states(h, _p(self.states, C.c_uint8))
             L.orc_res_lowest_states(h, _p(self.lowest_states, C.c_uint8))
         self.best_cost = L.orc_res_best_cost(h)
+        self.master_state = L.orc_res_master_state(h)
         self.best_state = np.zeros(self.n_vars, np.uint8)
         L.orc_res_best_state(h, _p(self.best_state, C.c_uint8))
         ns = L.orc_res_n_solutions(h)
@@ -302,7 +306,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         sched_count=None, sweeps_per_replica=1, population=16, alpha=2.0,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
-        full_maxsat_sweep=False, resampling="reference", master_skip=0):
+        full_maxsat_sweep=False, resampling="reference", master_skip=0, master_state=None):
     p = Params()
     p.solver = {"sa": SA, "pt": PT, "pa": PA}[solver]
     p.seed = seed & 0xFFFFFFFF
@@ -325,6 +329,8 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
     p.full_maxsat_sweep = int(full_maxsat_sweep)
     p.resampling = {"reference": 0, "multinomial": 1}[resampling]
     p.master_skip = int(master_skip)
+    p.use_master_state = 0 if master_state is None else 1
+    p.master_state = 0 if master_state is None else int(master_state)
     err = C.create_string_buffer(512)
     h = lib().orc_run(model.h, C.byref(p), err, 512)
     del keep
@@ -487,3 +493,77 @@ def sa_parameter_free(model: Model, kind, terms, *, seed, min_num_restarts, samp
             break
     return {"trace": trace, "best": best, "best_state": best_state, "params": best_params,
             "betas": (b0, b1)}
+
+
+def _pf_betas(b0, b1, num):
+    """PTParameterFree::determine_all_betas_ (solver/pt_parameter_free.h:
+    155-173): geometric ladders of 4, 9, 14, ... values from b0 to b1,
+    concatenated until `num` values."""
+    out = []
+    size = 5
+    while len(out) < num:
+        n = size - 1
+        for i in range(n):
+            p = min(1.0, max(0.0, i / (n - 1)))
+            out.append(b0 * (b1 / b0) ** p)
+            if len(out) >= num:
+                break
+        size += 5
+    return out
+
+
+def pt_parameter_free(model: Model, kind, terms, *, seed, min_num_betas, samples=(10, 20, 30, 50),
+                      max_prob=0.5, min_prob=0.0001, adjust=0.001, change=1.5,
+                      nonimprovement_limit=8, max_runs=400, threads=4):
+    """ParameterFreeLinearSearchSolver<PTParameterFree> restated
+    (solver/parameter_free_solver.h:65-151, strategy/linear_search.cc,
+    solver/pt_parameter_free.h): repeated oracle PT runs on one master stream
+    (replica forks and swap draws) that continues from run to run."""
+    import math
+    mn, mx = cost_diff_bounds(kind, terms)
+    b0 = -math.log(max_prob) / mx
+    b1 = -math.log(min_prob) / (mn + adjust * (mx - mn))
+    betas = _pf_betas(b0, b1, min_num_betas)
+    big = float(np.finfo(np.float64).max)
+    points = list(samples)
+    objs = [big] * len(points)
+    init_min = points[0]
+    cur = -1
+    state = None
+    best = best_state = best_params = None
+    best_exec = 0.0
+    stable = 0
+    trace = []
+    for _ in range(max_runs):
+        cur += 1
+        if cur >= len(points):
+            cur = 0
+            lowest = objs.index(min(objs))
+            if lowest == 0:
+                if points[0] > init_min:
+                    points = [int(p / change) for p in points]
+            elif lowest == len(points) - 1:
+                points = [int(p * change) for p in points]
+            objs = [big] * len(points)
+        sl = max(points[cur], 2)
+        res = run(model, "pt", seed=seed, step_limit=sl, use_inverse=True, sched=("list", 0.0, 0.0),
+                  sched_values=betas, threads=threads, master_state=state)
+        state = res.master_state
+        obj = float(res.best_cost)
+        objs[cur] = obj
+        trace.append((sl, len(betas), obj))
+        exec_cost = float(sl) * float(len(betas))
+        done = False
+        if best is not None and abs(best - obj) < 10E-12:
+            stable += 1
+            if exec_cost < best_exec:
+                best, best_state, best_exec, best_params = obj, res.best_state.copy(), exec_cost, sl
+        if stable >= nonimprovement_limit:
+            done = True
+        if best is None or best - obj > 10E-12:
+            stable = 0
+            best, best_state, best_exec, best_params = obj, res.best_state.copy(), exec_cost, sl
+        if done:
+            break
+    return {"trace": trace, "best": best, "best_state": best_state, "sweeps": best_params,
+            "betas": betas}

@@ -846,6 +846,7 @@ struct Result
   std::vector<double> pt_obs;  // n * 5
   std::vector<double> pa_beta;
   std::vector<int64_t> pa_pop;
+  uint64_t master_out = 0;  // PT: master stream state after the run
 };
 
 // ModelSolver::update_lowest_cost, solver/model_solver.h:247-259
@@ -1099,6 +1100,7 @@ static Result run_pt(const Model& m, const orc_params& p)
   }
   size_t n = temps.size();
   PcgRng master(p.seed);
+  if (p.use_master_state) master.pcg.state = p.master_state;
   std::vector<std::unique_ptr<Rng>> rngs(n);
   for (size_t i = 0; i < n; i++) rngs[i] = master.fork();
   std::vector<PtWalker> reps(n);
@@ -1132,6 +1134,7 @@ static Result run_pt(const Model& m, const orc_params& p)
   for (size_t i = 0; i < n; i++) wp[i] = &reps[i];
   fill_replicas(r, wp);
   populate(r, wp, low, p.number_of_solutions, m, false, false);
+  r.master_out = master.pcg.state;
   return r;
 }
 
@@ -1814,6 +1817,7 @@ void orc_res_lowest_states(void* r, uint8_t* out)
     memcpy(out + i * rr.n_vars, rr.lowest_states[i].data(), rr.n_vars);
 }
 double orc_res_best_cost(void* r) { return ((Result*)r)->best_cost; }
+uint64_t orc_res_master_state(void* r) { return ((Result*)r)->master_out; }
 void orc_res_best_state(void* r, uint8_t* out)
 {
   Result& rr = *(Result*)r;

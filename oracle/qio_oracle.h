@@ -69,6 +69,9 @@ typedef struct orc_params {
                                  the restarts fork (a run that continues the
                                  stream of earlier runs, as the parameter-free
                                  solvers' repeated SA runs do) */
+  int use_master_state;       /* PT: start the master stream at master_state
+                                 instead of seeding it (repeated runs) */
+  uint64_t master_state;
 } orc_params;
 
 /* ---- random generator pins ---- */
@@ -112,6 +115,8 @@ void orc_res_replicas(void* r, double* cost, double* lowest, uint64_t* attempts,
 void orc_res_states(void* r, uint8_t* out);
 void orc_res_lowest_states(void* r, uint8_t* out);
 double orc_res_best_cost(void* r);
+/* PT: the master stream's state after the run */
+uint64_t orc_res_master_state(void* r);
 void orc_res_best_state(void* r, uint8_t* out);
 int64_t orc_res_n_solutions(void* r);
 void orc_res_solutions(void* r, double* costs, uint8_t* states);

@@ -150,6 +150,15 @@ class Solver
   virtual bool historical_lowest(double&, std::vector<uint8_t>&) { return false; }
   virtual std::string target() const = 0;
   virtual uint64_t total_windows() { return 0; }
+  // the walker whose lowest is the solver's lowest (default: the first with
+  // the smallest lowest cost)
+  virtual size_t best_index(const std::vector<double>& low)
+  {
+    size_t b = 0;
+    for (size_t i = 1; i < low.size(); i++)
+      if (low[i] < low[b]) b = i;
+    return b;
+  }
   // extra members of the result's benchmark block (JSON, starting with ',')
   virtual std::string extra_benchmark() { return ""; }
   // Serving: the solve in pieces.  After init(), advance() enqueues up to n

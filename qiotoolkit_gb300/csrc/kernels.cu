@@ -380,6 +380,7 @@ __global__ void __launch_bounds__(128) init_kernel(InitArgs a)
   {
     a.p.cost[slot] = cost;
     a.p.lowest[w] = cost;
+    if (a.p.lowtag) a.p.lowtag[w] = -1;
     if (!a.keep_counters)
     {
       a.p.attempts[w] = 0;

@@ -102,6 +102,8 @@ struct DevPop
   unsigned long long* step_att;   // n (per walker, since last observation)
   unsigned long long* step_acc;   // n
   unsigned long long* windows;    // n (per walker: window iterations), or null
+  long long* lowtag;     // n (per walker): the tag of the launch in which its
+                         // lowest last dropped (-1: its initial state), or null
 };
 
 struct SweepArgs
@@ -122,6 +124,7 @@ struct SweepArgs
   long long key_div;
   int smem_state;       // stage spins + term state in shared memory
   int* err;             // device error flag (a bounded wait gave up)
+  long long tag;        // written to p.lowtag[walker] when its lowest drops
 };
 
 struct InitArgs

@@ -5,6 +5,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <numeric>
 #include <thread>
@@ -214,7 +215,7 @@ struct Population
            o_l = take(S * 8), o_ls = take(S * nw * 4), o_at = take(S * 8),
            o_ac = take(S * 8), o_sa = take(S * 8), o_sc = take(S * 8), o_wi = take(S * 8),
            o_rng = take((size_t)streams * 8), o_slot = take(need_slots ? S * 4 : 0),
-           o_beta = take((size_t)n_beta * 8);
+           o_beta = take((size_t)n_beta * 8), o_tag = take(need_slots ? S * 8 : 0);
     buf = DevBuf(off);
     char* b = (char*)buf.ptr;
     pop.n = slots;
@@ -233,6 +234,8 @@ struct Population
     rng = (uint64_t*)(b + o_rng);
     slot_of = need_slots ? (int*)(b + o_slot) : nullptr;
     beta = (double*)(b + o_beta);
+    // the lowest's launch tags: population kept by slot labels (tempering)
+    pop.lowtag = need_slots ? (long long*)(b + o_tag) : nullptr;
   }
 
   static void unpack(const std::vector<uint32_t>& words, int nw, int64_t N,
@@ -808,8 +811,61 @@ class ParallelTempering : public Solver
   unsigned long long *swap_acc = nullptr, *swap_cnt = nullptr, *ties = nullptr;
   uint64_t* master = nullptr;
   unsigned long long* swap_key = nullptr;
+  Pcg* ext_master = nullptr;  // repeated runs: ladder 0's streams fork from this stream
 
   std::string target() const override { return "paralleltempering.qiotoolkit"; }
+
+  // A new run of `sweeps` steps on the inverse temperatures `all_betas`, one
+  // ladder (PTParameterFree::update_parameters, solver/pt_parameter_free.h:
+  // 124-137); buffers are sized afresh at the next init.
+  void retarget(int64_t sweeps, const std::vector<double>& all_betas)
+  {
+    step_limit = sweeps;
+    use_inverse = true;
+    ladder = Schedule();
+    ladder.type = 3;
+    ladder.values = all_betas;
+    temps = all_betas;
+    std::sort(temps.begin(), temps.end(), std::greater<double>());
+    betas.resize(temps.size());
+    for (size_t i = 0; i < temps.size(); i++) betas[i] = beta_of(temps[i], true);
+    restarts = 1;
+    P = Population();
+    aux = DevBuf();
+    initialized = ran = false;
+    step_pos = 0;
+  }
+
+  size_t best_index(const std::vector<double>& low) override { return time_first_lowest(low); }
+
+  // The walker whose lowest the reference's tempering loop would hold: it
+  // offers every position's lowest after each step, in position order, and
+  // keeps the first strictly lower one (parallel_tempering.h:163-164 with
+  // ModelSolver::update_lowest_cost), so among equal lowest costs the one
+  // reached at the earliest step, then the lowest position, wins; position
+  // 0's initial state is offered first.
+  size_t time_first_lowest(const std::vector<double>& low)
+  {
+    std::vector<long long> tag(low.size(), 0);
+    if (P.pop.lowtag && !low.empty())
+      cuda_check(cudaMemcpy(tag.data(), P.pop.lowtag, low.size() * 8, cudaMemcpyDeviceToHost), "D2H");
+    // only position 0's initial state is offered before the first step
+    for (size_t i = 1; i < tag.size(); i++)
+      if (tag[i] < 0) tag[i] = 0;
+    size_t b = 0;
+    for (size_t i = 1; i < low.size(); i++)
+      if (low[i] < low[b] || (low[i] == low[b] && tag[i] < tag[b])) b = i;
+    return b;
+  }
+
+  // the master stream of ladder 0 after the run (the swaps draw from it)
+  uint64_t master_after(cudaStream_t st)
+  {
+    uint64_t v = 0;
+    cuda_check(cudaMemcpyAsync(&v, master, 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    return v;
+  }
 
   void configure(const json::Value& doc)
   {
@@ -880,7 +936,8 @@ class ParallelTempering : public Solver
     std::vector<double> bw(W);
     for (int k = 0; k < restarts; k++)
     {
-      Pcg m(seed + (uint32_t)k);
+      Pcg own(seed + (uint32_t)k);
+      Pcg& m = (ext_master && k == 0) ? *ext_master : own;
       for (int i = 0; i < T(); i++)
       {
         rs[k * T() + i] = Pcg(m.next()).state;
@@ -961,6 +1018,7 @@ class ParallelTempering : public Solver
     for (s = 0; s < step_limit;)
     {
       a.sweep_base = s * spr;
+      a.tag = s;  // the step, for the time order of equal lowest costs
       prof_begin(st);
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
       prof_end(st);
@@ -1040,6 +1098,7 @@ class ParallelTempering : public Solver
     for (; step_pos < end; step_pos++)
     {
       a.sweep_base = step_pos * spr;
+      a.tag = step_pos;
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
       sw.step = step_pos;
       cuda_check(launch_pt_swap(sw, st), "swap kernel");
@@ -1116,31 +1175,30 @@ class ParallelTempering : public Solver
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc);
 
 // ---------------------------------------------------------------------------
-// Parameter-free simulated annealing ("simulatedannealing-parameterfree.
-// qiotoolkit": solver/parameter_free_solver.h:9-257 with the linear search of
-// solver/parameter_free_linear_solver.h and strategy/linear_search.cc, the SA
-// adapter of solver/sa_parameter_free.h).  Repeated SA runs: run j takes
-// sweeps = the next sample point and restarts = min_num_restarts x the last
-// sample point / sweeps, on the linear beta schedule from -ln(max_prob) /
-// max cost difference to -ln(min_prob) / (adjusted min cost difference); after
-// each pass over the sample points they are stretched by the change factor
-// when the last one gave the lowest cost and shrunk when the first did.  The
-// restarts of every run fork from one master stream that continues across
-// runs.  The search stops when `nonimprovement_limit` runs in a row find no
+// Parameter-free solvers with the linear search ("simulatedannealing-
+// parameterfree.qiotoolkit", "paralleltempering-parameterfree.qiotoolkit":
+// solver/parameter_free_solver.h:9-257 with solver/parameter_free_linear_
+// solver.h and strategy/linear_search.cc; the adapters of
+// solver/sa_parameter_free.h and solver/pt_parameter_free.h).  Repeated runs
+// of the underlying solver: run j takes sweeps = the next sample point (and,
+// for SA, restarts = min_num_restarts x the last sample point / sweeps);
+// after each pass over the sample points they are stretched by the change
+// factor when the last one gave the lowest cost and shrunk when the first
+// did.  The temperature range runs from -ln(max_prob) / (max cost
+// difference) to -ln(min_prob) / (min cost difference + factor x (max -
+// min)).  The runs draw from one master stream that continues from run to
+// run.  The search stops when `nonimprovement_limit` runs in a row find no
 // lower cost, or at the time limit (default 5 s), checked between runs (the
-// reference also hands the remaining time to the run itself).  The result
-// is the lowest cost found and its state; the parameters shown are those of
-// the run that found it (with equal costs, the cheaper run's: sweeps x
-// restarts).
+// reference also hands the remaining time to the run itself).  The result is
+// the lowest cost found and its state; the parameters shown are those of the
+// run that found it (with equal costs, the cheaper run's).
 // ---------------------------------------------------------------------------
-class SAParameterFree : public Solver
+class ParameterFreeSearch : public Solver
 {
  public:
-  std::unique_ptr<SimulatedAnnealing> w;
   double max_prob = 0.5, min_prob = 0.0001, adjust = 0.001, change = 1.5;
   double beta_start = 0.01, beta_stop = 10.0;
   std::vector<int> samples{10, 20, 30, 50};
-  int64_t min_restarts = 1;
   int nonimprovement_limit = 8;
   // linear search state (strategy/linear_search.cc)
   std::vector<int> points;
@@ -1157,11 +1215,16 @@ class SAParameterFree : public Solver
   uint64_t att_total = 0, acc_total = 0;
   std::string stop_reason;
 
-  std::string target() const override { return "simulatedannealing-parameterfree.qiotoolkit"; }
+  // one run of the underlying solver with `sweeps` sweeps (the last sample
+  // point `back`), its master stream continuing `master`: the restarts used
+  // (or replicas), its lowest cost and state, and its cost estimate
+  virtual void one_run(int sweeps, int back, cudaStream_t st, int64_t& sl, int64_t& r, double& obj,
+                       std::vector<uint8_t>& state, double& exec) = 0;
+  virtual void render_params(int64_t sweeps, int64_t r) = 0;
 
-  void configure(const json::Value& doc)
+  // the parameters shared by both adapters, the time limit, the estimates
+  void configure_search()
   {
-    configure_common(*this, doc);
     if (!replay) fail(1, "parameter-free solvers run with \"rng_mode\": \"replay\"");
     if (number_of_solutions != 1) fail(1, "parameter-free solvers return one solution: `number_of_solutions` must be 1");
     Params p(params);
@@ -1185,8 +1248,6 @@ class SAParameterFree : public Solver
         samples.push_back((int)x.num);
       }
     }
-    min_restarts = p.integer("min_num_restarts", threads);
-    if (min_restarts <= 0) fail(1, "parameter `min_num_restarts`: must be greater than 0");
     nonimprovement_limit = (int)p.integer("nonimprovement_limit", 8);
     if (nonimprovement_limit <= 0) fail(1, "parameter `nonimprovement_limit`: must be greater than 0");
     if (!has_time_limit)
@@ -1194,9 +1255,6 @@ class SAParameterFree : public Solver
       has_time_limit = true;  // a time limit must be set (parameter_free_solver.h:56-61)
       time_limit = 5.0;
     }
-    w.reset(new SimulatedAnnealing());
-    w->model = model;
-    w->configure(doc);
     if (!model->empty())
     {
       const double mx = estimate_max_cost_diff(*model), mn = estimate_min_cost_diff(*model);
@@ -1208,17 +1266,6 @@ class SAParameterFree : public Solver
       beta_start = -std::log(max_prob) / mx;
       beta_stop = -std::log(min_prob) / (mn + adjust * (mx - mn));
     }
-    render_params(samples[0], min_restarts);
-  }
-
-  void render_params(int64_t sweeps, int64_t r)
-  {
-    output_params.clear();
-    output_params.push_back({"seed", std::to_string(seed)});
-    output_params.push_back({"beta_start", json::number(beta_start)});
-    output_params.push_back({"beta_stop", json::number(beta_stop)});
-    output_params.push_back({"restarts", std::to_string(r)});
-    output_params.push_back({"sweeps", std::to_string(sweeps)});
   }
 
   int64_t n_walkers() const override { return (model->empty() || !has_best) ? 0 : 1; }
@@ -1273,43 +1320,23 @@ class SAParameterFree : public Solver
         cur = 0;
         fit_points();
       }
-      const int sweeps = points[cur], back = points.back();
       if (elapsed() >= time_limit && has_best)
       {
         stop_reason = "time limit";
         break;
       }
-      // SAParameterFree::update_parameters
-      const int64_t sl = std::max(sweeps, 2);
-      const int64_t r = (int64_t)((int)min_restarts * back / sweeps);
-      if (r <= 0) fail(1, "parameter-free search reached a run with no restarts");
-      w->retarget(sl, r, beta_start, beta_stop);
-      w->ext_master = &master;
-      w->init(st);
-      w->run(st);
-      launches += w->launches;
-      std::vector<double> c, low;
-      std::vector<uint64_t> at, ac;
-      std::vector<uint8_t> ls;
-      w->fetch(c, low, at, ac, &ls, nullptr);
-      size_t b = 0;
-      for (size_t i = 1; i < low.size(); i++)
-        if (low[i] < low[b]) b = i;
-      const double obj = low[b];
-      for (size_t i = 0; i < at.size(); i++)
-      {
-        att_total += at[i];
-        acc_total += ac[i];
-      }
+      int64_t sl = 0, r = 0;
+      double obj = 0, exec = 0;
+      std::vector<uint8_t> state;
+      one_run(points[cur], points.back(), st, sl, r, obj, state, exec);
       objs[cur] = obj;  // LinearSearchOpt::add_new_sample
       trace.push_back({(double)sl, (double)r, obj + model->const_cost});
-      const double exec = (double)sl * (double)r;  // estimate_execution_cost, up to the thread divisor
       auto update_best = [&] {
         best = obj;
         best_exec = exec;
         best_sweeps = sl;
         best_restarts = r;
-        best_state.assign(ls.begin() + b * model->N, ls.begin() + (b + 1) * model->N);
+        best_state = state;
       };
       // ParameterFreeSolver::make_step, solver/parameter_free_solver.h:123-151
       bool done = false;
@@ -1339,6 +1366,31 @@ class SAParameterFree : public Solver
     }
     render_params(best_sweeps, best_restarts);
     run_ms = elapsed() * 1e3;
+  }
+
+  // the lowest state and cost of a finished run (the first walker holding
+  // the smallest lowest), with the run's counters added to the totals
+  void take_lowest(Solver& w, double& obj, std::vector<uint8_t>& state,
+                   const std::function<size_t(const std::vector<double>&)>& pick = nullptr)
+  {
+    std::vector<double> c, low;
+    std::vector<uint64_t> at, ac;
+    std::vector<uint8_t> ls;
+    w.fetch(c, low, at, ac, &ls, nullptr);
+    size_t b = 0;
+    if (pick)
+      b = pick(low);
+    else
+      for (size_t i = 1; i < low.size(); i++)
+        if (low[i] < low[b]) b = i;
+    obj = low[b];
+    state.assign(ls.begin() + b * model->N, ls.begin() + (b + 1) * model->N);
+    for (size_t i = 0; i < at.size(); i++)
+    {
+      att_total += at[i];
+      acc_total += ac[i];
+    }
+    launches += w.launches;
   }
 
   void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
@@ -1371,6 +1423,123 @@ class SAParameterFree : public Solver
   }
 };
 
+// SAParameterFree (solver/sa_parameter_free.h): restarts = min_num_restarts
+// x last sample point / sweeps, a linear beta schedule over the run
+class SAParameterFree : public ParameterFreeSearch
+{
+ public:
+  std::unique_ptr<SimulatedAnnealing> w;
+  int64_t min_restarts = 1;
+
+  std::string target() const override { return "simulatedannealing-parameterfree.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    Params p(params);
+    min_restarts = p.integer("min_num_restarts", threads);
+    if (min_restarts <= 0) fail(1, "parameter `min_num_restarts`: must be greater than 0");
+    configure_search();
+    w.reset(new SimulatedAnnealing());
+    w->model = model;
+    w->configure(doc);
+    render_params(samples[0], min_restarts);
+  }
+
+  void render_params(int64_t sweeps, int64_t r) override
+  {
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"beta_start", json::number(beta_start)});
+    output_params.push_back({"beta_stop", json::number(beta_stop)});
+    output_params.push_back({"restarts", std::to_string(r)});
+    output_params.push_back({"sweeps", std::to_string(sweeps)});
+  }
+
+  // SAParameterFree::update_parameters, solver/sa_parameter_free.h:120-137;
+  // estimate_execution_cost 139-145 (up to the thread divisor)
+  void one_run(int sweeps, int back, cudaStream_t st, int64_t& sl, int64_t& r, double& obj,
+               std::vector<uint8_t>& state, double& exec) override
+  {
+    sl = std::max(sweeps, 2);
+    r = (int64_t)((int)min_restarts * back / sweeps);
+    if (r <= 0) fail(1, "parameter-free search reached a run with no restarts");
+    w->retarget(sl, r, beta_start, beta_stop);
+    w->ext_master = &master;
+    w->init(st);
+    w->run(st);
+    take_lowest(*w, obj, state);
+    exec = (double)sl * (double)r;
+  }
+};
+
+// PTParameterFree (solver/pt_parameter_free.h): min_num_betas inverse
+// temperatures from geometric ladders of 4, 9, 14, ... values between the
+// two ends (determine_all_betas_, 155-173), the run length from the search
+class PTParameterFree : public ParameterFreeSearch
+{
+ public:
+  std::unique_ptr<ParallelTempering> w;
+  int64_t min_betas = 1;
+  std::vector<double> all_betas;
+  static const int kIncrement = 5;  // tempering_size_increment_
+
+  std::string target() const override { return "paralleltempering-parameterfree.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    Params p(params);
+    min_betas = p.integer("min_num_betas", threads);
+    if (min_betas <= 0) fail(1, "parameter `min_num_betas`: must be greater than 0");
+    configure_search();
+    w.reset(new ParallelTempering());
+    w->model = model;
+    w->configure(doc);
+    // determine_all_betas_
+    all_betas.clear();
+    Schedule g;
+    g.type = 1;
+    g.initial = beta_start;
+    g.final_ = beta_stop;
+    g.has_stop = true;
+    for (int size = kIncrement; (int64_t)all_betas.size() < min_betas; size += kIncrement)
+    {
+      const int n = size - 1;
+      g.stop_ = (double)(n - 1);
+      for (int i = 0; i < n && (int64_t)all_betas.size() < min_betas; i++) all_betas.push_back(g.get_value((double)i));
+    }
+    render_params(samples[0], (int64_t)all_betas.size());
+  }
+
+  void render_params(int64_t sweeps, int64_t) override
+  {
+    Schedule list;
+    list.type = 3;
+    list.values = all_betas;
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"all_betas", list.render()});
+    output_params.push_back({"sweeps", std::to_string(sweeps)});
+  }
+
+  // update_parameters 124-137; estimate_execution_cost 139-144 (up to the
+  // thread divisor)
+  void one_run(int sweeps, int, cudaStream_t st, int64_t& sl, int64_t& r, double& obj,
+               std::vector<uint8_t>& state, double& exec) override
+  {
+    sl = std::max(sweeps, 2);
+    r = (int64_t)all_betas.size();
+    w->retarget(sl, all_betas);
+    w->ext_master = &master;
+    w->init(st);
+    w->run(st);
+    master.state = w->master_after(st);
+    take_lowest(*w, obj, state, [&](const std::vector<double>& low) { return w->time_first_lowest(low); });
+    exec = (double)sl * (double)r;
+  }
+};
+
 std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& target,
                                     const json::Value& doc)
 {
@@ -1392,6 +1561,13 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
   if (target == "simulatedannealing-parameterfree.qiotoolkit")
   {
     std::unique_ptr<SAParameterFree> s(new SAParameterFree());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
+  if (target == "paralleltempering-parameterfree.qiotoolkit")
+  {
+    std::unique_ptr<PTParameterFree> s(new PTParameterFree());
     s->model = m;
     s->configure(doc);
     return std::unique_ptr<Solver>(s.release());
@@ -1818,9 +1994,7 @@ void Solver::best(double& cost, std::vector<uint8_t>& state)
     state.clear();
     return;
   }
-  size_t b = 0;
-  for (size_t i = 1; i < low.size(); i++)
-    if (low[i] < low[b]) b = i;
+  const size_t b = best_index(low);
   cost = low[b] + model->const_cost;
   state.assign(ls.begin() + b * model->N, ls.begin() + (b + 1) * model->N);
   double hc;
@@ -1850,6 +2024,11 @@ std::string Solver::result_json()
     std::vector<size_t> idx(low.size());
     std::iota(idx.begin(), idx.end(), 0);
     std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return low[a] < low[b]; });
+    // the solver's lowest first (ModelSolver::populate_solutions keeps it
+    // as the result's cost and configuration)
+    const size_t b0 = best_index(low);
+    idx.erase(std::find(idx.begin(), idx.end(), b0));
+    idx.insert(idx.begin(), b0);
     size_t k = std::min((size_t)number_of_solutions, idx.size());
     // population solvers may have lost their historical lowest
     // (solver/model_solver.h:280-290): it then comes first

@@ -1191,7 +1191,9 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
     if (lane == 0)
     {
       a.p.cost[slot] = INT ? (double)W.icost : W.cost;
-      a.p.lowest[r] = INT ? (double)W.ilow : W.low;
+      const double nlow = INT ? (double)W.ilow : W.low;
+      if (a.p.lowtag && nlow < a.p.lowest[r]) a.p.lowtag[r] = a.tag;
+      a.p.lowest[r] = nlow;
       a.p.attempts[r] += W.natt;
       a.p.accepts[r] += W.nacc;
       a.p.step_att[r] += W.natt;

@@ -48,3 +48,29 @@ def test_sa_parameter_free_matches_oracle(name):
     rep = s.replicas()
     np.testing.assert_array_equal(rep["lowest"], [ref["best"]])
     np.testing.assert_array_equal(rep["lowest_states"][0], ref["best_state"])
+
+
+PTPF = "paralleltempering-parameterfree.qiotoolkit"
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_pt_parameter_free_matches_oracle(name):
+    kind, gen, seed = CASES[name]
+    off, ids, coef = gen()
+    terms = [(float(coef[k]), [int(x) for x in ids[off[k]:off[k + 1]]]) for k in range(len(coef))]
+    g = q.Model(kind, off=off, ids=ids, coef=coef)
+    o = O.Model(kind, off=off, ids=ids, coef=coef)
+    params = {"seed": seed, "min_num_betas": 10, "timeout": 120}
+    s = q.Solver(g, PTPF, {"params": params}).init().run()
+    res = s.result()
+    runs = res["benchmark"]["parameter_free"]["runs"]
+    assert res["benchmark"]["parameter_free"]["stop"] == "no improvement"
+    ref = O.pt_parameter_free(o, kind, terms, seed=seed, min_num_betas=10)
+    assert [(r["sweeps"], r["restarts"], r["lowest"]) for r in runs] == list(ref["trace"])
+    sol = res["solutions"]
+    assert sol["parameters"]["sweeps"] == ref["sweeps"]
+    ladder = sol["parameters"]["all_betas"]  # a list schedule renders as segments
+    assert [seg["value"] for seg in ladder["segments"]] == ref["betas"]
+    rep = s.replicas()
+    np.testing.assert_array_equal(rep["lowest"], [ref["best"]])
+    np.testing.assert_array_equal(rep["lowest_states"][0], ref["best_state"])

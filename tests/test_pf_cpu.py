@@ -49,6 +49,28 @@ def test_parameter_errors(params, msg):
         q.Solver(m, PF, {"params": dict({"seed": 1}, **params)})
 
 
+def test_pt_parameter_errors():
+    m = q.Model("ising", [(1.0, [0, 1]), (-2.0, [1, 2])])
+    pt = "paralleltempering-parameterfree.qiotoolkit"
+    with pytest.raises(q.QioError, match="min_num_betas"):
+        q.Solver(m, pt, {"params": {"seed": 1, "min_num_betas": 0}})
+    q.Solver(m, pt, {"params": {"seed": 1, "min_num_betas": 6}}).close()
+
+
+def test_pt_betas_match_oracle():
+    """the ladder of the parameter-free PT: geometric groups of 4, 9, 14, ...
+    values, as the oracle restates them"""
+    import json as _json
+    m = q.Model("ising", [(1.0, [0, 1]), (-2.0, [1, 2]), (0.5, [2, 3])])
+    s = q.Solver(m, "paralleltempering-parameterfree.qiotoolkit", {"params": {"seed": 1, "min_num_betas": 16}})
+    mn, mx = O.cost_diff_bounds("ising", [(1.0, [0, 1]), (-2.0, [1, 2]), (0.5, [2, 3])])
+    import math
+    b0 = -math.log(0.5) / mx
+    b1 = -math.log(0.0001) / (mn + 0.001 * (mx - mn))
+    assert len(O._pf_betas(b0, b1, 16)) == 16
+    s.close()
+
+
 def test_maxsat_not_supported():
     m = q.Model("maxsat", [(1.0, [1, 2]), (2.0, [-1, 3])])
     with pytest.raises(q.QioError, match="maxsat"):
