@@ -9,7 +9,7 @@ One step = one complete solve (init + 500 sweeps + 500 swap phases of all 512
 walkers) = 1.05e9 flip attempts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload pt_pubo|sa_ising|pa_square]
+                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa]
 
 Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
 launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
@@ -47,6 +47,10 @@ WORKLOADS = {
                          "3 terms per variable), weighted 3-SAT (ratio 4.2, U[1,10]); N log-uniform "
                          "[100, 1e4]; sweeps U{200..5000}; SA (8 restarts) or PT (8 temperatures)",
                     target="mixed"),
+    "pf_sa": dict(desc="Parameter-free SA (linear search, repeated SA runs) on the sparse Ising "
+                       "N=1000, 3000 ER couplings +-1, 1000 fields U[-0.5,0.5], min_num_restarts 64, "
+                       "seed 0, timeout 3 s per solve",
+                  target="simulatedannealing-parameterfree.qiotoolkit"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
@@ -301,6 +305,9 @@ def main():
     if args.workload == "serving":
         main_serving(args, ws, rank)
         return
+    if args.workload == "pf_sa":
+        main_pf(args, ws, rank)
+        return
 
     import torch
     import qiotoolkit_gb300 as q
@@ -434,6 +441,128 @@ def serving_requests(n=48, rate=200.0, seed=4):
             params = {"seed": i, "sweeps": sweeps, "restarts": 8, "beta_start": 0.1, "beta_stop": 3.0}
         out.append((float(t[i]), k, inst, target, params))
     return out
+
+
+PF_PARAMS = {"seed": 0, "min_num_restarts": 64, "timeout": 3}
+
+
+def main_pf(args, ws, rank):
+    """Parameter-free SA: flip attempts/s over whole parameter-free solves
+    (every SA run of the search), the same solve through the C ABI from host
+    buffers, and the oracle's restatement of the search on the host cores."""
+    import torch
+    import qiotoolkit_gb300 as q
+    from qiotoolkit_gb300 import instances as I
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    q.load()
+    target = WORKLOADS["pf_sa"]["target"]
+    off, ids, coef = I.er_ising(1000, 3000, seed=0)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    model = q.Model("ising", off=off, ids=ids, coef=coef)
+    solver = q.Solver(model, target, {"params": PF_PARAMS})
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def one_step():
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.init(sh)
+        solver.run(sh)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), solver.stats()
+
+    for _ in range(args.warmup):
+        one_step()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ms, att, launches = [], 0, 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, st = one_step()
+            ms.append(t)
+            att += int(st.attempts)
+            launches += int(st.kernel_launches)
+    torch.cuda.synchronize()
+    barrier(ws)
+    total_s = reduce_max(sum(ms) / 1e3, ws)
+    value = att * ws / total_s
+    res = solver.result()
+    runs = res["benchmark"]["parameter_free"]["runs"]
+    best = res["solutions"]["cost"]
+
+    e2e = None
+    if not args.no_e2e:
+        times, h2d, d2h = [], 0, 0
+        for i in range(1 + min(args.steps, 3)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m = q.Model("ising", off=off, ids=ids, coef=coef)
+            s = q.Solver(m, target, {"params": PF_PARAMS})
+            s.init(sh)
+            s.run(sh)
+            r = s.result()
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(time.perf_counter() - t0)
+            h2d = int(m.info.device_bytes)
+            d2h = int(m.n_vars * 8 + 64)
+            s.close()
+            m.close()
+        e2e = {"value": att / args.steps / statistics.median(times), "unit": "flip attempts/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # the same SA runs (sweeps, restarts, continuing master stream) on
+        # the oracle, in order, until about 15 s of CPU time
+        import math
+        from oracle import oracle as O
+        o = O.Model("ising", off=off, ids=ids, coef=coef)
+        terms = [(float(coef[k]), [int(x) for x in ids[off[k]:off[k + 1]]]) for k in range(len(coef))]
+        mn, mx = O.cost_diff_bounds("ising", terms)
+        b0 = -math.log(0.5) / mx
+        b1 = -math.log(0.0001) / (mn + 0.001 * (mx - mn))
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        skip, a_cpu, same, k = 0, 0, True, 0
+        for x in runs:
+            r = O.run(o, "sa", seed=PF_PARAMS["seed"], step_limit=x["sweeps"], restarts=x["restarts"],
+                      use_inverse=True, sched=("linear", b0, b1), threads=cores, master_skip=skip)
+            skip += x["restarts"]
+            a_cpu += x["sweeps"] * x["restarts"] * model.n_vars
+            same = same and float(r.best_cost) == x["lowest"]
+            k += 1
+            if time.perf_counter() - t0 > 15.0:
+                break
+        dt = time.perf_counter() - t0
+        cpu = {"value": a_cpu / dt, "unit": "flip attempts/s", "cores": cores, "kind": "port",
+               "sample": f"the first {k} of the solve's {len(runs)} SA runs on the oracle (same sweeps, "
+                         f"restarts and master stream), {a_cpu:.3g} attempts in {dt:.2f} s; identical "
+                         f"lowest costs: {same}"}
+
+    if rank == 0:
+        kernel_s = sum(ms) / 1e3
+        bpa = 100.0  # SURVEY configuration-1 model: 8 + 7 x (4 + 8 + 1) + 1
+        achieved = bpa * att / kernel_s / 1e9
+        peak, peak_src = peaks()
+        line = {
+            "metric": "flip attempts/s", "value": value, "unit": "flip attempts/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOADS["pf_sa"]["desc"], "runs_per_solve": len(runs),
+                       "best_cost": best, "l2": "flushed before each step (256 MB write)"},
+            "e2e": e2e, "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "sweep_kernel (whole solves timed)", "bytes_per_attempt": bpa},
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
 
 
 def main_serving(args, ws, rank):

@@ -492,6 +492,7 @@ class SimulatedAnnealing : public Solver
     lvlog = LevelLog();
     initialized = ran = false;
     step_pos = 0;
+    launches = 0;
   }
 
   void configure(const json::Value& doc)
@@ -834,6 +835,7 @@ class ParallelTempering : public Solver
     aux = DevBuf();
     initialized = ran = false;
     step_pos = 0;
+    launches = 0;
   }
 
   size_t best_index(const std::vector<double>& low) override { return time_first_lowest(low); }
@@ -1286,6 +1288,7 @@ class ParameterFreeSearch : public Solver
     best_state.clear();
     stop_reason.clear();
     last_step = 0;
+    launches = 0;
   }
 
   // LinearSearchOpt::fit_sample_points: shrink when the first point gave the
