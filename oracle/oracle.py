@@ -19,7 +19,7 @@ _lock = threading.Lock()
 _lib = None
 
 ISING, ISING_PLAIN, PUBO, PUBO_PLAIN, MAXSAT = 0, 1, 2, 3, 4
-SA, PT, PA = 0, 1, 2
+SA, PT, PA, TABU = 0, 1, 2, 3
 RNG_REPLAY, RNG_COUNTER = 0, 1
 SCHED_LINEAR, SCHED_GEOMETRIC, SCHED_CONSTANT, SCHED_LIST = 0, 1, 2, 3
 
@@ -49,7 +49,7 @@ class Params(C.Structure):
                 ("has_cost_limit", C.c_int), ("cost_limit", C.c_double),
                 ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int),
                 ("master_skip", C.c_int64), ("use_master_state", C.c_int),
-                ("master_state", C.c_uint64)]
+                ("master_state", C.c_uint64), ("tabu_tenure", C.c_int64)]
 
 
 def build(force: bool = False) -> str:
@@ -306,9 +306,10 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         sched_count=None, sweeps_per_replica=1, population=16, alpha=2.0,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
-        full_maxsat_sweep=False, resampling="reference", master_skip=0, master_state=None):
+        full_maxsat_sweep=False, resampling="reference", master_skip=0, master_state=None,
+        tabu_tenure=0):
     p = Params()
-    p.solver = {"sa": SA, "pt": PT, "pa": PA}[solver]
+    p.solver = {"sa": SA, "pt": PT, "pa": PA, "tabu": TABU}[solver]
     p.seed = seed & 0xFFFFFFFF
     p.step_limit = step_limit
     p.restarts = restarts
@@ -331,6 +332,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
     p.master_skip = int(master_skip)
     p.use_master_state = 0 if master_state is None else 1
     p.master_state = 0 if master_state is None else int(master_state)
+    p.tabu_tenure = int(tabu_tenure)
     err = C.create_string_buffer(512)
     h = lib().orc_run(model.h, C.byref(p), err, 512)
     del keep

@@ -1010,6 +1010,168 @@ static Result run_sa(const Model& m, const orc_params& p)
 }
 
 // ---------------------------------------------------------------------------
+// Tabu search, solver/tabu.h:22-164 with markov/tabu_walker.h:14-218 and the
+// hill climber of markov/hill_climbing_walker.h.  Each restart scans the
+// variables in order: the first move that would put the cost below the
+// lowest is taken (and starts a hill-climbing local search), otherwise the
+// lowest-difference move not on the tabu list; a taken move stays tabu for
+// `tabu_tenure` sweeps.  Only the initial state draws random numbers.
+// ---------------------------------------------------------------------------
+struct TabuWalker : Walker
+{
+  std::vector<uint64_t> tabu;   // expiry iteration per variable
+  uint64_t iter = 0, incomplete = 0;
+  uint64_t tenure = 0;
+  bool local = false;
+  // the hill climber (a walker accepting differences <= 0) on a copy
+  State hc;
+  double hc_cost = 0, hc_low = 0;
+  std::vector<uint8_t> hc_low_spins;
+
+  void tabu_init()
+  {
+    init();
+    tabu.assign((size_t)model->N, 0);
+    iter = incomplete = 0;
+    local = false;
+  }
+  // local_search_init: HillClimbingWalker::init(state), markov/walker.h:63-69
+  void local_init()
+  {
+    local = true;
+    hc = state;
+    hc_cost = calculate_cost(*model, hc);
+    hc_low = hc_cost;
+    hc_low_spins = hc.spins;
+  }
+  // local_search_sweep: one ordered hill-climbing sweep on the copy; its
+  // lowest replaces the walker's when it improved, else local search ends
+  void local_sweep()
+  {
+    const double prev = hc_low;
+    for (int64_t v = 0; v < model->N; v++)
+    {
+      const double d = cost_difference(*model, hc, v);
+      diff_evals++;
+      total_attempts++;
+      if (d <= 0)
+      {
+        apply_transition(*model, v, hc);
+        accepted++;
+        total_accepts++;
+        hc_cost += d;
+        if (hc_cost < hc_low)
+        {
+          hc_low = hc_cost;
+          hc_low_spins = hc.spins;
+        }
+      }
+    }
+    if (hc_low < prev)
+    {
+      lowest_cost = hc_low;
+      lowest_spins = hc_low_spins;
+    }
+    else
+      local = false;
+  }
+  // TabuWalker::make_sweep, markov/tabu_walker.h:60-129
+  void tabu_sweep()
+  {
+    if (local)
+    {
+      local_sweep();
+      return;
+    }
+    const int64_t n = model->N;
+    bool has_best = false, taken = false;
+    double best_d = 0;
+    int64_t best = 0;
+    for (int64_t i = 0; i < n; i++)
+    {
+      const double cost_before = cost_, low_before = lowest_cost;
+      const double d = cost_difference(*model, state, i);
+      diff_evals++;
+      total_attempts++;
+      if (cost_before + d < low_before)
+      {
+        // attempt_transition accepted it (TabuWalker::accept)
+        apply_transition(*model, i, state);
+        accepted++;
+        total_accepts++;
+        cost_ += d;
+        check_lowest();
+        tabu[i] = iter + tenure;
+        local_init();
+        incomplete += (uint64_t)i;
+        if (incomplete < (uint64_t)n)
+          local_sweep();
+        else
+          incomplete -= (uint64_t)n;
+        taken = true;
+        break;
+      }
+      if (tabu[i] >= iter) continue;
+      if (!has_best || d < best_d)
+      {
+        has_best = true;
+        best_d = d;
+        best = i;
+      }
+    }
+    if (!taken && has_best)
+    {
+      // Walker::apply_transition(transition, diff)
+      apply_transition(*model, best, state);
+      cost_ += best_d;
+      check_lowest();
+      tabu[best] = iter + tenure;
+    }
+    iter++;
+  }
+};
+
+static Result run_tabu(const Model& m, const orc_params& p)
+{
+  Result r;
+  r.n_vars = m.N;
+  if (m.empty())
+  {
+    r.has_best = false;
+    r.best_cost = m.const_cost;
+    return r;
+  }
+  size_t R = (size_t)p.restarts;
+  PcgRng master(p.seed);
+  std::vector<std::unique_ptr<Rng>> rngs(R);
+  for (size_t i = 0; i < R; i++) rngs[i] = master.fork();
+  std::vector<TabuWalker> reps(R);
+  std::vector<Walker*> wp(R);
+  set_threads(p.threads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (size_t i = 0; i < R; i++)
+  {
+    TabuWalker& w = reps[i];
+    w.model = &m;
+    w.rng = rngs[i].get();
+    w.counter_mode = p.rng_mode == ORC_RNG_COUNTER;
+    w.key = counter_key(p.seed, i);
+    w.tenure = (uint64_t)p.tabu_tenure;
+    w.tabu_init();
+  }
+  for (size_t i = 0; i < R; i++) wp[i] = &reps[i];
+  Lowest low;
+  low.update(reps[0].cost_, reps[0].state.spins);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (size_t i = 0; i < R; i++)
+    for (int64_t s = 0; s < p.step_limit; s++) reps[i].tabu_sweep();
+  r.last_step = p.step_limit;
+  fill_replicas(r, wp);
+  populate(r, wp, low, p.number_of_solutions, m, false, false);
+  return r;
+}
+
+// ---------------------------------------------------------------------------
 // ParallelTempering, solver/parallel_tempering.h:68-189.  Generic over the
 // walker type so that the reference's toy model can reuse it for the pin.
 // ---------------------------------------------------------------------------
@@ -1779,6 +1941,7 @@ void* orc_run(void* m, const orc_params* p, char* err, int errlen)
     if (p->solver == ORC_SA) *r = run_sa(mm, *p);
     else if (p->solver == ORC_PT) *r = run_pt(mm, *p);
     else if (p->solver == ORC_PA) *r = run_pa(mm, *p);
+    else if (p->solver == ORC_TABU) *r = run_tabu(mm, *p);
     else throw std::runtime_error("unknown solver");
     return r.release();
   }

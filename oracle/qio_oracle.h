@@ -28,7 +28,7 @@ enum {
   ORC_MAXSAT = 4        /* model::MaxSat                               */
 };
 
-enum { ORC_SA = 0, ORC_PT = 1, ORC_PA = 2 };
+enum { ORC_SA = 0, ORC_PT = 1, ORC_PA = 2, ORC_TABU = 3 };
 enum { ORC_RNG_REPLAY = 0, ORC_RNG_COUNTER = 1 };
 enum { ORC_SCHED_LINEAR = 0, ORC_SCHED_GEOMETRIC = 1, ORC_SCHED_CONSTANT = 2,
        ORC_SCHED_LIST = 3 };
@@ -72,6 +72,7 @@ typedef struct orc_params {
   int use_master_state;       /* PT: start the master stream at master_state
                                  instead of seeding it (repeated runs) */
   uint64_t master_state;
+  int64_t tabu_tenure;        /* tabu: sweeps a taken move stays tabu */
 } orc_params;
 
 /* ---- random generator pins ---- */

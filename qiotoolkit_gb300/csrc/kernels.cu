@@ -483,6 +483,280 @@ __global__ void eval_diff_kernel(DevModel m, int n, const uint32_t* spins,
 }
 
 // ---------------------------------------------------------------------------
+// Tabu search (solver/tabu.h:22-164, markov/tabu_walker.h:14-218), one warp
+// per walker.  A tabu sweep prices every variable against the current state
+// (lanes take 32 variables at a time, each difference summed in the
+// reference's term order), takes the first move that puts the cost below the
+// lowest -- then hill-climbs on a copy (accepting differences <= 0, one
+// variable after the other) while that improves the lowest -- or else the
+// lowest-difference move not on the tabu list.  No random numbers after the
+// initial state.
+// ---------------------------------------------------------------------------
+// calculate_cost_difference of variable v by one thread, terms in row order
+template <int FL, bool INT>
+__device__ double lane_diff(const DevModel& m, const uint32_t* sp, int v)
+{
+  const uint32_t sv = spin_of(sp, v);
+  double diff = 0.0;
+  long long idiff = 0;
+  for (int q = m.row[v], qe = m.row[v + 1]; q < qe; q++)
+  {
+    const uint32_t e = m.inc[q];
+    const int t = (int)(e & ~kNegBit);
+    const int tb = m.trow[t], te = m.trow[t + 1];
+    if (FL == F_PARITY || FL == F_PLAIN_ISING)
+    {
+      uint32_t par = 0;
+      for (int u = tb; u < te; u++) par ^= spin_of(sp, (int)(m.tvar[u] & ~kNegBit));
+      if (INT) idiff += par ? -(long long)m.coef_i[q] : (long long)m.coef_i[q];
+      else diff = __dadd_rn(diff, par ? -m.coef[q] : m.coef[q]);
+    }
+    else
+    {
+      int cnt = 0;
+      for (int u = tb; u < te; u++)
+      {
+        const uint32_t x = m.tvar[u];
+        cnt += (int)(spin_of(sp, (int)(x & ~kNegBit)) ^ (x >> 31));
+      }
+      const bool lit = (sv ^ (e >> 31)) != 0;
+      if (lit && cnt == 1)
+      {
+        if (INT) idiff += m.coef_i[q];
+        else diff = __dadd_rn(diff, m.coef[q]);
+      }
+      else if (!lit && cnt == 0)
+      {
+        if (INT) idiff -= m.coef_i[q];
+        else diff = __dadd_rn(diff, -m.coef[q]);
+      }
+    }
+  }
+  if (FL == F_PARITY || FL == F_PLAIN_ISING) return INT ? (double)(-2 * idiff) : __dmul_rn(2.0, -diff);
+  return INT ? (double)idiff : diff;
+}
+
+// the same difference by a warp (lanes over the row, added in row order);
+// every lane returns it
+template <int FL, bool INT>
+__device__ double warp_diff(const DevModel& m, const uint32_t* sp, int v, int lane)
+{
+  const uint32_t sv = spin_of(sp, v);
+  const int rb = m.row[v], re = m.row[v + 1];
+  double diff = 0.0;
+  long long idiff = 0;
+  for (int q0 = rb; q0 < re; q0 += 32)
+  {
+    const int q = q0 + lane;
+    double val = 0.0;
+    long long ival = 0;
+    bool skip = true;
+    if (q < re)
+    {
+      const uint32_t e = m.inc[q];
+      const int t = (int)(e & ~kNegBit);
+      const int tb = m.trow[t], te = m.trow[t + 1];
+      if (FL == F_PARITY || FL == F_PLAIN_ISING)
+      {
+        uint32_t par = 0;
+        for (int u = tb; u < te; u++) par ^= spin_of(sp, (int)(m.tvar[u] & ~kNegBit));
+        skip = false;
+        if (INT) ival = par ? -(long long)m.coef_i[q] : (long long)m.coef_i[q];
+        else val = par ? -m.coef[q] : m.coef[q];
+      }
+      else
+      {
+        int cnt = 0;
+        for (int u = tb; u < te; u++)
+        {
+          const uint32_t x = m.tvar[u];
+          cnt += (int)(spin_of(sp, (int)(x & ~kNegBit)) ^ (x >> 31));
+        }
+        const bool lit = (sv ^ (e >> 31)) != 0;
+        if (lit && cnt == 1)
+        {
+          skip = false;
+          if (INT) ival = m.coef_i[q];
+          else val = m.coef[q];
+        }
+        else if (!lit && cnt == 0)
+        {
+          skip = false;
+          if (INT) ival = -(long long)m.coef_i[q];
+          else val = -m.coef[q];
+        }
+      }
+    }
+    unsigned keep = __ballot_sync(kFull, !skip);
+    while (keep)
+    {
+      const int j = __ffs(keep) - 1;
+      keep &= keep - 1;
+      if (INT) idiff += __shfl_sync(kFull, ival, j);
+      else diff = __dadd_rn(diff, __shfl_sync(kFull, val, j));
+    }
+  }
+  if (FL == F_PARITY || FL == F_PLAIN_ISING) return INT ? (double)(-2 * idiff) : __dmul_rn(2.0, -diff);
+  return INT ? (double)idiff : diff;
+}
+
+__device__ __forceinline__ void warp_copy(uint32_t* dst, const uint32_t* src, int n, int lane)
+{
+  for (int q = lane; q < n; q += 32) dst[q] = src[q];
+  __syncwarp();
+}
+
+template <int FL, bool INT>
+__global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
+{
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= a.n_walkers) return;  // whole warps leave together
+  const DevModel& m = a.m;
+  const int N = m.n_vars, nw = a.p.nw;
+  uint32_t* sp = a.p.spins + (size_t)w * nw;
+  uint32_t* ls = a.p.lspins + (size_t)w * nw;
+  uint32_t* hs = a.hc + (size_t)w * nw;
+  uint32_t* hl = a.hc_low + (size_t)w * nw;
+  unsigned long long* tb = a.tabu + (size_t)w * N;
+  TabuState S = a.st[w];
+  double cost = a.p.cost[w], low = a.p.lowest[w];
+  unsigned long long att = 0, acc = 0;
+
+  // HillClimbingWalker::make_sweep on the copy, then local_search_sweep's
+  // bookkeeping (markov/tabu_walker.h:183-207)
+  auto local_sweep = [&]() {
+    const double prev = S.hc_low;
+    for (int v = 0; v < N; v++)
+    {
+      const double d = warp_diff<FL, INT>(m, hs, v, lane);
+      att++;
+      if (d <= 0)
+      {
+        if (lane == 0) hs[v >> 5] ^= 1u << (v & 31);
+        __syncwarp();
+        acc++;
+        S.hc_cost = __dadd_rn(S.hc_cost, d);
+        if (S.hc_cost < S.hc_low)
+        {
+          S.hc_low = S.hc_cost;
+          warp_copy(hl, hs, nw, lane);
+        }
+      }
+    }
+    if (S.hc_low < prev)
+    {
+      low = S.hc_low;
+      warp_copy(ls, hl, nw, lane);
+    }
+    else
+      S.local = 0;
+  };
+
+  for (int step = 0; step < a.n_steps; step++)
+  {
+    if (S.local)
+    {
+      local_sweep();
+      continue;
+    }
+    // the scan, markov/tabu_walker.h:68-127
+    bool taken = false, has_best = false;
+    double best_d = 0.0;
+    int best = -1;
+    for (int c0 = 0; c0 < N && !taken; c0 += 32)
+    {
+      const int v = c0 + lane;
+      const bool ok = v < N;
+      const double d = ok ? lane_diff<FL, INT>(m, sp, v) : 0.0;
+      const unsigned take = __ballot_sync(kFull, ok && __dadd_rn(cost, d) < low);
+      if (take)
+      {
+        const int j = __ffs(take) - 1;
+        const int i = c0 + j;
+        const double di = __shfl_sync(kFull, d, j);
+        taken = true;
+        // attempt_transition accepted it: flip, cost, lowest
+        if (lane == 0) sp[i >> 5] ^= 1u << (i & 31);
+        __syncwarp();
+        acc++;
+        cost = __dadd_rn(cost, di);
+        if (cost < low)
+        {
+          low = cost;
+          warp_copy(ls, sp, nw, lane);
+        }
+        if (lane == 0) tb[i] = S.iter + a.tenure;
+        // local_search_init: a hill climber on a copy, its cost computed afresh
+        warp_copy(hs, sp, nw, lane);
+        warp_copy(hl, sp, nw, lane);
+        double c;
+        long long ic;
+        warp_terms_cost<FL, INT>(m, hs, nullptr, lane, c, ic);
+        S.hc_cost = INT ? (double)ic : c;
+        S.hc_low = S.hc_cost;
+        S.local = 1;
+        S.incomplete += (unsigned long long)i;
+        att += (unsigned long long)(i + 1);
+        if (S.incomplete < (unsigned long long)N)
+          local_sweep();
+        else
+          S.incomplete -= (unsigned long long)N;
+        break;
+      }
+      // the lowest difference off the tabu list, the first on ties
+      const bool cand = ok && !(tb[v] >= S.iter);
+      double cd = cand ? d : 0.0;
+      int cv = cand ? v : INT_MAX;
+#pragma unroll
+      for (int s = 16; s; s >>= 1)
+      {
+        const double od = __shfl_xor_sync(kFull, cd, s);
+        const int ov = __shfl_xor_sync(kFull, cv, s);
+        if (ov != INT_MAX && (cv == INT_MAX || od < cd || (od == cd && ov < cv)))
+        {
+          cd = od;
+          cv = ov;
+        }
+      }
+      if (cv != INT_MAX && (!has_best || cd < best_d))
+      {
+        has_best = true;
+        best_d = cd;
+        best = cv;
+      }
+    }
+    if (!taken)
+    {
+      att += (unsigned long long)N;
+      if (has_best)
+      {
+        // Walker::apply_transition(transition, diff)
+        if (lane == 0) sp[best >> 5] ^= 1u << (best & 31);
+        __syncwarp();
+        cost = __dadd_rn(cost, best_d);
+        if (cost < low)
+        {
+          low = cost;
+          warp_copy(ls, sp, nw, lane);
+        }
+        if (lane == 0) tb[best] = S.iter + a.tenure;
+      }
+    }
+    S.iter++;
+    __syncwarp();
+  }
+  if (lane == 0)
+  {
+    a.st[w] = S;
+    a.p.cost[w] = cost;
+    a.p.lowest[w] = low;
+    a.p.attempts[w] += att;
+    a.p.accepts[w] += acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // PT: observations then alternating-parity neighbour swaps of the slot
 // labels (solver/parallel_tempering.h:134-189); one thread per restart.
 // ---------------------------------------------------------------------------
@@ -795,6 +1069,26 @@ cudaError_t launch_eval_cost_noalloc(const DevModel& m, int n, const uint8_t* st
     case F_COUNTER: I ? cost_noalloc_dispatch<F_COUNTER, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_COUNTER, false>(m, n, states, n_vars, nw, scratch, out, s); break;
     case F_PLAIN_ISING: I ? cost_noalloc_dispatch<F_PLAIN_ISING, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_PLAIN_ISING, false>(m, n, states, n_vars, nw, scratch, out, s); break;
     default: I ? cost_noalloc_dispatch<F_PLAIN_PUBO, true>(m, n, states, n_vars, nw, scratch, out, s) : cost_noalloc_dispatch<F_PLAIN_PUBO, false>(m, n, states, n_vars, nw, scratch, out, s); break;
+  }
+  return cudaGetLastError();
+}
+template <int FL, bool I>
+static void tabu_dispatch(const TabuArgs& a, cudaStream_t s)
+{
+  const int blocks = (a.n_walkers + 3) / 4;
+  if (blocks > 0) tabu_kernel<FL, I><<<blocks, 128, 0, s>>>(a);
+}
+
+cudaError_t launch_tabu(const TabuArgs& a, cudaStream_t s)
+{
+  if (a.n_walkers <= 0 || a.n_steps <= 0) return cudaSuccess;
+  const bool I = a.m.int_mode != 0;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: I ? tabu_dispatch<F_PARITY, true>(a, s) : tabu_dispatch<F_PARITY, false>(a, s); break;
+    case F_COUNTER: I ? tabu_dispatch<F_COUNTER, true>(a, s) : tabu_dispatch<F_COUNTER, false>(a, s); break;
+    case F_PLAIN_ISING: I ? tabu_dispatch<F_PLAIN_ISING, true>(a, s) : tabu_dispatch<F_PLAIN_ISING, false>(a, s); break;
+    default: I ? tabu_dispatch<F_PLAIN_PUBO, true>(a, s) : tabu_dispatch<F_PLAIN_PUBO, false>(a, s); break;
   }
   return cudaGetLastError();
 }

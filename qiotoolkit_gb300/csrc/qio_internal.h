@@ -272,6 +272,31 @@ cudaError_t launch_eval_diff(const DevModel& m, int n, const uint32_t* spins,
                              int nw, const long long* vars, double* out,
                              cudaStream_t s);
 
+// Tabu search (kernels.cu): one warp per walker; per walker the tabu list
+// (expiry sweep per variable), the hill climber's copy and its lowest state,
+// and the scalars below.
+struct TabuState
+{
+  double hc_cost, hc_low;        // the hill climber's cost and lowest
+  unsigned long long iter;       // tabu sweeps so far
+  unsigned long long incomplete; // compensation count (markov/tabu_walker.h:88-101)
+  int local;                     // 1: local-search mode
+  int pad;
+};
+struct TabuArgs
+{
+  DevModel m;
+  DevPop p;
+  int n_walkers;
+  int n_steps;
+  unsigned long long tenure;
+  unsigned long long* tabu;  // n_walkers * n_vars
+  uint32_t* hc;              // n_walkers * p.nw
+  uint32_t* hc_low;          // n_walkers * p.nw
+  TabuState* st;             // n_walkers
+};
+cudaError_t launch_tabu(const TabuArgs& a, cudaStream_t s);
+
 // PT: label swaps + observables, one thread per restart.
 struct SwapArgs
 {

@@ -1177,6 +1177,150 @@ class ParallelTempering : public Solver
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc);
 
 // ---------------------------------------------------------------------------
+// Tabu search ("tabu.qiotoolkit": solver/tabu.h:22-164 with
+// markov/tabu_walker.h).  Restarts fork from the master stream and start
+// from random states exactly as the annealing walkers do; the sweeps are
+// deterministic (tabu_kernel).
+// ---------------------------------------------------------------------------
+class TabuSearch : public Solver
+{
+ public:
+  int64_t restarts = 1;
+  uint64_t tenure = 0;
+  Population P;
+  DevBuf aux;
+  TabuArgs ta{};
+
+  std::string target() const override { return "tabu.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    if (model->kind == K_MAXSAT) fail(1, "tabu search runs Ising and PUBO models here");
+    Params p(params);
+    const int64_t t = p.integer("tabu_tenure", 0);
+    if (t < 0) fail(1, "parameter `tabu_tenure`: must be greater than or equal to 0, found " + std::to_string(t));
+    tenure = (uint64_t)t;
+    restarts = p.integer("restarts", threads);
+    if (restarts <= 0) fail(1, "parameter `restarts`: must be greater than 0");
+    if (restarts > (1 << 24)) fail(1, "parameter `restarts` too large");
+    output_params.push_back({"tabu_tenure", std::to_string(tenure)});
+    output_params.push_back({"restarts", std::to_string(restarts)});
+  }
+
+  int64_t n_walkers() const override { return model->empty() ? 0 : restarts; }
+
+  void init(cudaStream_t st) override
+  {
+    initialized = true;
+    if (model->empty()) return;
+    ensure_device();
+    const int R = (int)restarts;
+    if (!P.buf.ptr) P.alloc(*model, R, R, false, 1);
+    const size_t nw = (size_t)P.pop.nw, N = (size_t)model->N;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+    const size_t o_t = take((size_t)R * N * 8), o_h = take((size_t)R * nw * 4), o_l = take((size_t)R * nw * 4),
+                 o_s = take((size_t)R * sizeof(TabuState));
+    if (!aux.ptr) aux = DevBuf(off);
+    char* b = (char*)aux.ptr;
+    cuda_check(cudaMemsetAsync(aux.ptr, 0, off, st), "memset");
+    device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
+    // rngs_[i] = rng_->fork() in index order (solver/tabu.h:56-60)
+    std::vector<uint64_t> rs(R);
+    Pcg master(seed);
+    for (int i = 0; i < R; i++) rs[i] = Pcg(master.next()).state;
+    cuda_check(cudaMemcpyAsync(P.rng, rs.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D rng");
+    InitArgs a{};
+    a.m = model->device_view(false);
+    a.p = P.pop;
+    a.n_walkers = R;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    a.skip_terms = 1;  // the tabu sweeps gather the member spins
+    cuda_check(launch_init(a, st), "init kernel");
+    launches++;
+    ta = TabuArgs{};
+    ta.m = model->device_view(false);
+    ta.p = P.pop;
+    ta.n_walkers = R;
+    ta.tenure = tenure;
+    ta.tabu = (unsigned long long*)(b + o_t);
+    ta.hc = (uint32_t*)(b + o_h);
+    ta.hc_low = (uint32_t*)(b + o_l);
+    ta.st = (TabuState*)(b + o_s);
+    step_pos = 0;
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    EventTimer total(st);
+    int64_t s = 0;
+    const int64_t chunk = (has_cost_limit || has_time_limit) ? std::max<int64_t>(1, step_limit / 100) : step_limit;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> low(restarts);
+    while (s < step_limit)
+    {
+      TabuArgs a = ta;
+      a.n_steps = (int)std::min(chunk, step_limit - s);
+      prof_begin(st);
+      cuda_check(launch_tabu(a, st), "tabu kernel");
+      prof_end(st);
+      launches++;
+      s += a.n_steps;
+      if (has_cost_limit)
+      {
+        cuda_check(cudaMemcpyAsync(low.data(), P.pop.lowest, restarts * 8, cudaMemcpyDeviceToHost, st), "D2H");
+        cuda_check(cudaStreamSynchronize(st), "sync");
+        if (*std::min_element(low.begin(), low.end()) <= cost_limit) break;
+      }
+      if (has_time_limit)
+      {
+        cuda_check(cudaStreamSynchronize(st), "sync");
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= time_limit) break;
+      }
+    }
+    last_step = s;
+    run_ms = total.stop();
+    sweep_ms = profile ? prof_total_ms() : run_ms;
+    check_device_error(st);
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
+             std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
+             std::vector<uint8_t>* states) override
+  {
+    const int R = (int)n_walkers();
+    cost.resize(R);
+    lowest.resize(R);
+    att.resize(R);
+    acc.resize(R);
+    if (!R) return;
+    cuda_check(cudaMemcpy(cost.data(), P.pop.cost, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(lowest.data(), P.pop.lowest, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), P.pop.attempts, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), P.pop.accepts, R * 8, cudaMemcpyDeviceToHost), "D2H");
+    std::vector<uint32_t> w((size_t)R * P.pop.nw);
+    if (lowest_states)
+    {
+      cuda_check(cudaMemcpy(w.data(), P.pop.lspins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, P.pop.nw, model->N, R, *lowest_states);
+    }
+    if (states)
+    {
+      cuda_check(cudaMemcpy(w.data(), P.pop.spins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, P.pop.nw, model->N, R, *states);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Parameter-free solvers with the linear search ("simulatedannealing-
 // parameterfree.qiotoolkit", "paralleltempering-parameterfree.qiotoolkit":
 // solver/parameter_free_solver.h:9-257 with solver/parameter_free_linear_
@@ -1564,6 +1708,13 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
   if (target == "simulatedannealing-parameterfree.qiotoolkit")
   {
     std::unique_ptr<SAParameterFree> s(new SAParameterFree());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
+  if (target == "tabu.qiotoolkit")
+  {
+    std::unique_ptr<TabuSearch> s(new TabuSearch());
     s->model = m;
     s->configure(doc);
     return std::unique_ptr<Solver>(s.release());
