@@ -9,7 +9,7 @@ One step = one complete solve (init + 500 sweeps + 500 swap phases of all 512
 walkers) = 1.05e9 flip attempts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa]
+                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising]
 
 Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
 launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
@@ -51,6 +51,10 @@ WORKLOADS = {
                        "N=1000, 3000 ER couplings +-1, 1000 fields U[-0.5,0.5], min_num_restarts 64, "
                        "seed 0, timeout 3 s per solve",
                   target="simulatedannealing-parameterfree.qiotoolkit"),
+    "tabu_ising": dict(desc="Tabu search on the sparse Ising N=1000, 3000 ER couplings +-1, 1000 fields "
+                            "U[-0.5,0.5], tabu_tenure 20, 200 sweeps, 1216 restarts, seed 0; attempts are "
+                            "cost-difference evaluations (scan and hill-climbing sweeps)",
+                       target="tabu.qiotoolkit"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
@@ -70,7 +74,8 @@ def batch_instances(n=512):
 
 
 # the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
-KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel"}
+KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel",
+                4: "tabu_kernel"}
 
 
 def make_workload(name):
@@ -85,6 +90,10 @@ def make_workload(name):
         off, ids, coef = I.er_ising(1000, 3000, seed=0)
         params = {"seed": 0, "sweeps": 1000, "restarts": 64, "beta_start": 0.1,
                   "beta_stop": 5.0}
+        return "ising", off, ids, coef, params
+    if name == "tabu_ising":
+        off, ids, coef = I.er_ising(1000, 3000, seed=0)
+        params = {"seed": 0, "sweeps": 200, "restarts": 1216, "tabu_tenure": 20}
         return "ising", off, ids, coef, params
     if name == "pa_square":
         off, ids, coef = I.square_pm_j(256, seed=3)
@@ -201,6 +210,11 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
                   resampling=params.get("resampling", "reference"))
             a = restarts * sweeps * params["sweeps_per_replica"] * n
             d = f"population {restarts} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
+        elif "tabu_tenure" in params:
+            r = O.run(m, "tabu", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
+                      tabu_tenure=params["tabu_tenure"])
+            a = int(np.sum(r.attempts))
+            d = f"{restarts} tabu walkers x {sweeps} sweeps"
         else:
             O.run(m, "sa", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
                   sched=("linear", params["beta_start"], params["beta_stop"]))
@@ -345,8 +359,15 @@ def main():
         last["launches"] = int(st.kernel_launches)
         return e0.elapsed_time(e1), st, n
 
+    st0 = None
     for _ in range(args.warmup):
-        one_step()
+        _, st0, _ = one_step()
+    if target == "tabu.qiotoolkit":
+        # a tabu scan stops at the first improving flip: count the
+        # evaluations (deterministic for the fixed seed)
+        if st0 is None:
+            _, st0, _ = one_step()
+        A = int(st0.attempts)
     barrier(ws)
     torch.cuda.synchronize()
     ms, sweep_ms, launches, att = [], [], 0, 0
@@ -363,7 +384,7 @@ def main():
     barrier(ws)
     total_s = reduce_max(sum(ms) / 1e3, ws)
     value = A * args.steps * ws / total_s
-    if target == "simulatedannealing.qiotoolkit":
+    if target in ("simulatedannealing.qiotoolkit", "tabu.qiotoolkit"):
         sweep_launches_per_step = 1
     else:
         sweep_launches_per_step = params["sweeps"]

@@ -87,7 +87,8 @@ typedef struct qio_solver_stats {
   uint64_t windows;        /* 32-variable evaluation windows committed; the
                               mean committed window is attempts / windows */
   int32_t sweep_kernel;    /* kernel of the last sweeps: 1 one walker per
-                              warp, 2 one walker per lane, 3 level schedule */
+                              warp, 2 one walker per lane, 3 level schedule,
+                              4 tabu search (one walker per warp) */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */

@@ -536,70 +536,6 @@ __device__ double lane_diff(const DevModel& m, const uint32_t* sp, int v)
   return INT ? (double)idiff : diff;
 }
 
-// the same difference by a warp (lanes over the row, added in row order);
-// every lane returns it
-template <int FL, bool INT>
-__device__ double warp_diff(const DevModel& m, const uint32_t* sp, int v, int lane)
-{
-  const uint32_t sv = spin_of(sp, v);
-  const int rb = m.row[v], re = m.row[v + 1];
-  double diff = 0.0;
-  long long idiff = 0;
-  for (int q0 = rb; q0 < re; q0 += 32)
-  {
-    const int q = q0 + lane;
-    double val = 0.0;
-    long long ival = 0;
-    bool skip = true;
-    if (q < re)
-    {
-      const uint32_t e = m.inc[q];
-      const int t = (int)(e & ~kNegBit);
-      const int tb = m.trow[t], te = m.trow[t + 1];
-      if (FL == F_PARITY || FL == F_PLAIN_ISING)
-      {
-        uint32_t par = 0;
-        for (int u = tb; u < te; u++) par ^= spin_of(sp, (int)(m.tvar[u] & ~kNegBit));
-        skip = false;
-        if (INT) ival = par ? -(long long)m.coef_i[q] : (long long)m.coef_i[q];
-        else val = par ? -m.coef[q] : m.coef[q];
-      }
-      else
-      {
-        int cnt = 0;
-        for (int u = tb; u < te; u++)
-        {
-          const uint32_t x = m.tvar[u];
-          cnt += (int)(spin_of(sp, (int)(x & ~kNegBit)) ^ (x >> 31));
-        }
-        const bool lit = (sv ^ (e >> 31)) != 0;
-        if (lit && cnt == 1)
-        {
-          skip = false;
-          if (INT) ival = m.coef_i[q];
-          else val = m.coef[q];
-        }
-        else if (!lit && cnt == 0)
-        {
-          skip = false;
-          if (INT) ival = -(long long)m.coef_i[q];
-          else val = -m.coef[q];
-        }
-      }
-    }
-    unsigned keep = __ballot_sync(kFull, !skip);
-    while (keep)
-    {
-      const int j = __ffs(keep) - 1;
-      keep &= keep - 1;
-      if (INT) idiff += __shfl_sync(kFull, ival, j);
-      else diff = __dadd_rn(diff, __shfl_sync(kFull, val, j));
-    }
-  }
-  if (FL == F_PARITY || FL == F_PLAIN_ISING) return INT ? (double)(-2 * idiff) : __dmul_rn(2.0, -diff);
-  return INT ? (double)idiff : diff;
-}
-
 __device__ __forceinline__ void warp_copy(uint32_t* dst, const uint32_t* src, int n, int lane)
 {
   for (int q = lane; q < n; q += 32) dst[q] = src[q];
@@ -624,25 +560,39 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
   unsigned long long att = 0, acc = 0;
 
   // HillClimbingWalker::make_sweep on the copy, then local_search_sweep's
-  // bookkeeping (markov/tabu_walker.h:183-207)
+  // bookkeeping (markov/tabu_walker.h:183-207).  The ordered sweep runs in
+  // windows of 32 variables evaluated at once: the lanes before the first
+  // accepted one (d <= 0) saw the same state as the sequential sweep would
+  // and were rejected; the window restarts after each accepted flip.
   auto local_sweep = [&]() {
     const double prev = S.hc_low;
-    for (int v = 0; v < N; v++)
+    int v0 = 0;
+    while (v0 < N)
     {
-      const double d = warp_diff<FL, INT>(m, hs, v, lane);
-      att++;
-      if (d <= 0)
+      const int v = v0 + lane;
+      const bool ok = v < N;
+      const double d = ok ? lane_diff<FL, INT>(m, hs, v) : 0.0;
+      const unsigned take = __ballot_sync(kFull, ok && d <= 0);
+      if (!take)
       {
-        if (lane == 0) hs[v >> 5] ^= 1u << (v & 31);
-        __syncwarp();
-        acc++;
-        S.hc_cost = __dadd_rn(S.hc_cost, d);
-        if (S.hc_cost < S.hc_low)
-        {
-          S.hc_low = S.hc_cost;
-          warp_copy(hl, hs, nw, lane);
-        }
+        att += (unsigned long long)min(32, N - v0);
+        v0 += 32;
+        continue;
       }
+      const int j = __ffs(take) - 1;
+      const double dj = __shfl_sync(kFull, d, j);
+      const int i = v0 + j;
+      att += (unsigned long long)(j + 1);
+      if (lane == 0) hs[i >> 5] ^= 1u << (i & 31);
+      __syncwarp();
+      acc++;
+      S.hc_cost = __dadd_rn(S.hc_cost, dj);
+      if (S.hc_cost < S.hc_low)
+      {
+        S.hc_low = S.hc_cost;
+        warp_copy(hl, hs, nw, lane);
+      }
+      v0 = i + 1;
     }
     if (S.hc_low < prev)
     {

@@ -1241,6 +1241,7 @@ class TabuSearch : public Solver
     a.key_base = 0;
     a.key_div = (long long)1 << 40;
     a.skip_terms = 1;  // the tabu sweeps gather the member spins
+    used_kernel = 4;
     cuda_check(launch_init(a, st), "init kernel");
     launches++;
     ta = TabuArgs{};

@@ -87,7 +87,7 @@ def test_params_validation_like_reference():
         q.Solver(m, "paralleltempering.qiotoolkit",
                  {"params": {"step_limit": 100, "temperatures": [], "seed": 42}})
     with pytest.raises(q.QioError, match="Unknown solver"):
-        q.Solver(m, "tabu.qiotoolkit", {"params": {}})
+        q.Solver(m, "substochasticmontecarlo.qiotoolkit", {"params": {}})
     with pytest.raises(q.QioError, match="number of sweeps must be greater than 1"):
         q.Solver(m, "simulatedannealing.qiotoolkit", {"params": {"step_limit": 1}})
     with pytest.raises(q.QioError, match="params"):
