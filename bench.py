@@ -397,6 +397,10 @@ def main():
     w = 1.0 if info.integer_weights and info.max_coupling <= 127 else (4.0 if info.integer_weights else 8.0)
     # row bounds 8 + own state 1 + per incidence (id 4 + coefficient w + state 1)
     bpa = 9.0 + (5.0 + w) * K / n
+    if target == "tabu.qiotoolkit":
+        # a tabu evaluation reads the variable's cached difference (FP64) and
+        # its tabu expiry (uint64)
+        bpa = 16.0
     achieved = bpa * attempts_per_launch / (avg_sweep_launch_ms / 1e3) / 1e9
     peak, peak_src = peaks()
     traffic = committed_traffic(args.workload)

@@ -542,6 +542,28 @@ __device__ __forceinline__ void warp_copy(uint32_t* dst, const uint32_t* src, in
   __syncwarp();
 }
 
+// Every walker keeps the cost difference of each of its variables (and its
+// hill climber those of the copy) in HBM.  A flip of variable i changes only
+// the differences of i and of the members of i's terms; those are summed
+// afresh from the spins (term order, as calculate_cost_difference), so a
+// cached value always equals a fresh evaluation bit for bit.
+template <int FL, bool INT>
+__device__ void tabu_refresh(const DevModel& m, const uint32_t* sp, double* df, int i, int lane)
+{
+  if (lane == 0) df[i] = lane_diff<FL, INT>(m, sp, i);
+  const int rb = m.row[i], re = m.row[i + 1];
+  for (int q = rb + lane; q < re; q += 32)
+  {
+    const int t = (int)(m.inc[q] & ~kNegBit);
+    for (int u = m.trow[t], ue = m.trow[t + 1]; u < ue; u++)
+    {
+      const int x = (int)(m.tvar[u] & ~kNegBit);
+      if (x != i) df[x] = lane_diff<FL, INT>(m, sp, x);
+    }
+  }
+  __syncwarp();
+}
+
 template <int FL, bool INT>
 __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
 {
@@ -555,15 +577,23 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
   uint32_t* hs = a.hc + (size_t)w * nw;
   uint32_t* hl = a.hc_low + (size_t)w * nw;
   unsigned long long* tb = a.tabu + (size_t)w * N;
+  double* df = a.diff + (size_t)w * N;
+  double* hd = a.hdiff + (size_t)w * N;
   TabuState S = a.st[w];
   double cost = a.p.cost[w], low = a.p.lowest[w];
   unsigned long long att = 0, acc = 0;
+  if (!S.ready)
+  {
+    for (int v = lane; v < N; v += 32) df[v] = lane_diff<FL, INT>(m, sp, v);
+    S.ready = 1;
+    __syncwarp();
+  }
 
   // HillClimbingWalker::make_sweep on the copy, then local_search_sweep's
   // bookkeeping (markov/tabu_walker.h:183-207).  The ordered sweep runs in
-  // windows of 32 variables evaluated at once: the lanes before the first
-  // accepted one (d <= 0) saw the same state as the sequential sweep would
-  // and were rejected; the window restarts after each accepted flip.
+  // windows of 32 variables read at once: the lanes before the first
+  // accepted one (d <= 0) hold what the sequential sweep would have seen and
+  // were rejected; the window restarts after each accepted flip.
   auto local_sweep = [&]() {
     const double prev = S.hc_low;
     int v0 = 0;
@@ -571,7 +601,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
     {
       const int v = v0 + lane;
       const bool ok = v < N;
-      const double d = ok ? lane_diff<FL, INT>(m, hs, v) : 0.0;
+      const double d = ok ? hd[v] : 0.0;
       const unsigned take = __ballot_sync(kFull, ok && d <= 0);
       if (!take)
       {
@@ -592,6 +622,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
         S.hc_low = S.hc_cost;
         warp_copy(hl, hs, nw, lane);
       }
+      tabu_refresh<FL, INT>(m, hs, hd, i, lane);
       v0 = i + 1;
     }
     if (S.hc_low < prev)
@@ -610,87 +641,99 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
       local_sweep();
       continue;
     }
-    // the scan, markov/tabu_walker.h:68-127
-    bool taken = false, has_best = false;
-    double best_d = 0.0;
-    int best = -1;
-    for (int c0 = 0; c0 < N && !taken; c0 += 32)
+    // the scan, markov/tabu_walker.h:68-127: 128 variables per round (four
+    // loads in flight per lane), each lane keeping its own first-lowest
+    // candidate off the tabu list
+    bool taken = false;
+    double bd = 0.0;
+    int bv = INT_MAX;
+    const unsigned long long it = S.iter;
+    for (int c0 = 0; c0 < N && !taken; c0 += 128)
     {
-      const int v = c0 + lane;
-      const bool ok = v < N;
-      const double d = ok ? lane_diff<FL, INT>(m, sp, v) : 0.0;
-      const unsigned take = __ballot_sync(kFull, ok && __dadd_rn(cost, d) < low);
-      if (take)
+      double d[4];
+      unsigned long long x[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
       {
-        const int j = __ffs(take) - 1;
-        const int i = c0 + j;
-        const double di = __shfl_sync(kFull, d, j);
-        taken = true;
-        // attempt_transition accepted it: flip, cost, lowest
-        if (lane == 0) sp[i >> 5] ^= 1u << (i & 31);
-        __syncwarp();
-        acc++;
-        cost = __dadd_rn(cost, di);
-        if (cost < low)
+        const int v = c0 + 32 * u + lane;
+        d[u] = v < N ? df[v] : 0.0;
+        x[u] = v < N ? tb[v] : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+      {
+        const int v = c0 + 32 * u + lane;
+        const bool ok = v < N;
+        const unsigned take = __ballot_sync(kFull, ok && __dadd_rn(cost, d[u]) < low);
+        if (take)
         {
+          const int j = __ffs(take) - 1;
+          const int i = c0 + 32 * u + j;
+          const double di = __shfl_sync(kFull, d[u], j);
+          taken = true;
+          // attempt_transition accepted it: flip, cost, lowest
+          if (lane == 0) sp[i >> 5] ^= 1u << (i & 31);
+          __syncwarp();
+          acc++;
+          cost = __dadd_rn(cost, di);
           low = cost;
           warp_copy(ls, sp, nw, lane);
+          if (lane == 0) tb[i] = it + a.tenure;
+          tabu_refresh<FL, INT>(m, sp, df, i, lane);
+          // local_search_init: a hill climber on a copy, its cost computed afresh
+          warp_copy(hs, sp, nw, lane);
+          warp_copy(hl, sp, nw, lane);
+          for (int q = lane; q < N; q += 32) hd[q] = df[q];
+          __syncwarp();
+          double c;
+          long long ic;
+          warp_terms_cost<FL, INT>(m, hs, nullptr, lane, c, ic);
+          S.hc_cost = INT ? (double)ic : c;
+          S.hc_low = S.hc_cost;
+          S.local = 1;
+          S.incomplete += (unsigned long long)i;
+          att += (unsigned long long)(i + 1);
+          if (S.incomplete < (unsigned long long)N)
+            local_sweep();
+          else
+            S.incomplete -= (unsigned long long)N;
+          break;
         }
-        if (lane == 0) tb[i] = S.iter + a.tenure;
-        // local_search_init: a hill climber on a copy, its cost computed afresh
-        warp_copy(hs, sp, nw, lane);
-        warp_copy(hl, sp, nw, lane);
-        double c;
-        long long ic;
-        warp_terms_cost<FL, INT>(m, hs, nullptr, lane, c, ic);
-        S.hc_cost = INT ? (double)ic : c;
-        S.hc_low = S.hc_cost;
-        S.local = 1;
-        S.incomplete += (unsigned long long)i;
-        att += (unsigned long long)(i + 1);
-        if (S.incomplete < (unsigned long long)N)
-          local_sweep();
-        else
-          S.incomplete -= (unsigned long long)N;
-        break;
-      }
-      // the lowest difference off the tabu list, the first on ties
-      const bool cand = ok && !(tb[v] >= S.iter);
-      double cd = cand ? d : 0.0;
-      int cv = cand ? v : INT_MAX;
-#pragma unroll
-      for (int s = 16; s; s >>= 1)
-      {
-        const double od = __shfl_xor_sync(kFull, cd, s);
-        const int ov = __shfl_xor_sync(kFull, cv, s);
-        if (ov != INT_MAX && (cv == INT_MAX || od < cd || (od == cd && ov < cv)))
+        if (ok && !(x[u] >= it) && (bv == INT_MAX || d[u] < bd))
         {
-          cd = od;
-          cv = ov;
+          bd = d[u];
+          bv = v;
         }
-      }
-      if (cv != INT_MAX && (!has_best || cd < best_d))
-      {
-        has_best = true;
-        best_d = cd;
-        best = cv;
       }
     }
     if (!taken)
     {
       att += (unsigned long long)N;
-      if (has_best)
+      // the lowest difference off the tabu list, the first on ties
+#pragma unroll
+      for (int s = 16; s; s >>= 1)
+      {
+        const double od = __shfl_xor_sync(kFull, bd, s);
+        const int ov = __shfl_xor_sync(kFull, bv, s);
+        if (ov != INT_MAX && (bv == INT_MAX || od < bd || (od == bd && ov < bv)))
+        {
+          bd = od;
+          bv = ov;
+        }
+      }
+      if (bv != INT_MAX)
       {
         // Walker::apply_transition(transition, diff)
-        if (lane == 0) sp[best >> 5] ^= 1u << (best & 31);
+        if (lane == 0) sp[bv >> 5] ^= 1u << (bv & 31);
         __syncwarp();
-        cost = __dadd_rn(cost, best_d);
+        cost = __dadd_rn(cost, bd);
         if (cost < low)
         {
           low = cost;
           warp_copy(ls, sp, nw, lane);
         }
-        if (lane == 0) tb[best] = S.iter + a.tenure;
+        if (lane == 0) tb[bv] = it + a.tenure;
+        tabu_refresh<FL, INT>(m, sp, df, bv, lane);
       }
     }
     S.iter++;

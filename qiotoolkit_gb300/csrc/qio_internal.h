@@ -281,7 +281,7 @@ struct TabuState
   unsigned long long iter;       // tabu sweeps so far
   unsigned long long incomplete; // compensation count (markov/tabu_walker.h:88-101)
   int local;                     // 1: local-search mode
-  int pad;
+  int ready;                     // 1: the cached differences are filled
 };
 struct TabuArgs
 {
@@ -293,6 +293,8 @@ struct TabuArgs
   unsigned long long* tabu;  // n_walkers * n_vars
   uint32_t* hc;              // n_walkers * p.nw
   uint32_t* hc_low;          // n_walkers * p.nw
+  double* diff;              // n_walkers * n_vars: each variable's cost difference
+  double* hdiff;             // n_walkers * n_vars: the same for the hill climber's copy
   TabuState* st;             // n_walkers
 };
 cudaError_t launch_tabu(const TabuArgs& a, cudaStream_t s);

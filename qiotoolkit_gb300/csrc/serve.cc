@@ -71,7 +71,10 @@ int64_t footprint_of(const HostModel& m, const Solver& s)
     const int64_t per_sweep = nw * 4 + 16 + ((m.N + 31) & ~31LL) * (m.lv_d8 ? 1 : 4);
     lv = std::min<int64_t>((int64_t)4 << 30, W * std::min<int64_t>(64, steps) * per_sweep);
   }
-  return model_bytes(m) + W * per + steps * 8 + W * 64 + lv + 64 * 1024;
+  // tabu search: tabu list and two cost-difference arrays per walker, the
+  // hill climber's spins and state
+  const int64_t tabu = s.target() == "tabu.qiotoolkit" ? W * (24 * m.N + 2 * nw * 4 + 64) : 0;
+  return model_bytes(m) + W * per + steps * 8 + W * 64 + lv + tabu + 64 * 1024;
 }
 }  // namespace
 

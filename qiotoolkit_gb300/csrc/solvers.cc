@@ -1221,7 +1221,8 @@ class TabuSearch : public Solver
     size_t off = 0;
     auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
     const size_t o_t = take((size_t)R * N * 8), o_h = take((size_t)R * nw * 4), o_l = take((size_t)R * nw * 4),
-                 o_s = take((size_t)R * sizeof(TabuState));
+                 o_s = take((size_t)R * sizeof(TabuState)), o_d = take((size_t)R * N * 8),
+                 o_hd = take((size_t)R * N * 8);
     if (!aux.ptr) aux = DevBuf(off);
     char* b = (char*)aux.ptr;
     cuda_check(cudaMemsetAsync(aux.ptr, 0, off, st), "memset");
@@ -1253,6 +1254,8 @@ class TabuSearch : public Solver
     ta.hc = (uint32_t*)(b + o_h);
     ta.hc_low = (uint32_t*)(b + o_l);
     ta.st = (TabuState*)(b + o_s);
+    ta.diff = (double*)(b + o_d);
+    ta.hdiff = (double*)(b + o_hd);
     step_pos = 0;
   }
 
@@ -1291,6 +1294,29 @@ class TabuSearch : public Solver
     run_ms = total.stop();
     sweep_ms = profile ? prof_total_ms() : run_ms;
     check_device_error(st);
+  }
+
+  // serving pieces: up to n further tabu sweeps per call
+  bool advance(cudaStream_t st, int64_t n) override
+  {
+    if (!initialized) fail(1, "init() must be called before advance()");
+    ran = true;
+    if (model->empty() || step_limit <= 0)
+    {
+      last_step = step_limit;
+      return true;
+    }
+    const int64_t todo = std::min(n, step_limit - step_pos);
+    if (todo > 0)
+    {
+      TabuArgs a = ta;
+      a.n_steps = (int)todo;
+      cuda_check(launch_tabu(a, st), "tabu kernel");
+      launches++;
+    }
+    step_pos += todo;
+    last_step = step_pos;
+    return step_pos >= step_limit;
   }
 
   void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,

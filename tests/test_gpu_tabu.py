@@ -83,3 +83,25 @@ def test_tabu_result_document():
     assert doc["solutions"]["parameters"]["restarts"] == 3
     c, st = s.best()
     assert g.calculate_cost(st[None, :])[0] == pytest.approx(c, abs=1e-9)
+
+
+def test_tabu_pieces_and_time_limit():
+    """A solve served in pieces of 7 sweeps (the walker state, cached
+    differences and tabu list stay on the device between launches) and a
+    solve under a time limit (launches of step_limit / 100 sweeps) give the
+    plain solve's walkers."""
+    off, ids, coef = I.random_pubo(200, 700, seed=6)
+    g = q.Model("pubo", off=off, ids=ids, coef=coef)
+    o = O.Model("pubo", off=off, ids=ids, coef=coef)
+    p = {"seed": 8, "sweeps": 60, "restarts": 5, "tabu_tenure": 4}
+    s = q.Solver(g, TABU, {"params": p}).init().run()
+    same(s, O.run(o, "tabu", seed=8, step_limit=60, restarts=5, tabu_tenure=4))
+    srv = q.Server(max_active=4, sa_sweeps_per_piece=7)
+    try:
+        res = srv.wait(srv.submit(g, TABU, {"params": p}))
+    finally:
+        srv.close()
+    assert res["solutions"] == s.result()["solutions"]
+    t = q.Solver(g, TABU, {"params": dict(p, timeout=1000)}).init().run()
+    same(t, O.run(o, "tabu", seed=8, step_limit=60, restarts=5, tabu_tenure=4))
+    assert t.stats().kernel_launches > s.stats().kernel_launches
