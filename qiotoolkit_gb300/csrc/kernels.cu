@@ -492,6 +492,26 @@ __global__ void eval_diff_kernel(DevModel m, int n, const uint32_t* spins,
 // lowest-difference move not on the tabu list.  No random numbers after the
 // initial state.
 // ---------------------------------------------------------------------------
+// FP64 instructions occupy a GB300 sub-partition's FP64 unit for ~64 cycles
+// each, so the tabu kernel orders, signs and scales differences with integer
+// bit operations where that is exact.
+// fkey: unsigned key ordered as the doubles (finite values; -0 keyed as +0,
+// as -0 == +0 compares)
+__device__ __forceinline__ unsigned long long fkey(double x)
+{
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+// -2 * x for a normal x by the exponent and sign bits (__dmul_rn otherwise)
+__device__ __forceinline__ double times_minus2(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+  if (e == 0 || e >= 0x7FEu) return __dmul_rn(2.0, -x);
+  return __longlong_as_double((long long)((b + (1ull << 52)) ^ 0x8000000000000000ull));
+}
+
 // calculate_cost_difference of variable v by one thread, terms in row order
 template <int FL, bool INT>
 __device__ double lane_diff(const DevModel& m, const uint32_t* sp, int v)
@@ -499,6 +519,35 @@ __device__ double lane_diff(const DevModel& m, const uint32_t* sp, int v)
   const uint32_t sv = spin_of(sp, v);
   double diff = 0.0;
   long long idiff = 0;
+  if (FL == F_PARITY && m.pair_only)
+  {
+    // one- or two-member terms: the parity is the spin of v xor that of the
+    // other member; four incidences' loads in flight, added in row order
+    const int qe = m.row[v + 1];
+    for (int q = m.row[v]; q < qe; q += 4)
+    {
+      int o[4];
+      double c[4];
+      int ci[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (q + u < qe)
+        {
+          o[u] = __ldg(m.other + q + u);
+          if (INT) ci[u] = __ldg(m.coef_i + q + u);
+          else c[u] = __ldg(m.coef + q + u);
+        }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (q + u < qe)
+        {
+          const uint32_t par = sv ^ (o[u] >= 0 ? spin_of(sp, o[u]) : 0u);
+          if (INT) idiff += par ? -(long long)ci[u] : (long long)ci[u];
+          else diff = __dadd_rn(diff, par ? -c[u] : c[u]);
+        }
+    }
+    return INT ? (double)(-2 * idiff) : times_minus2(diff);
+  }
   for (int q = m.row[v], qe = m.row[v + 1]; q < qe; q++)
   {
     const uint32_t e = m.inc[q];
@@ -532,7 +581,7 @@ __device__ double lane_diff(const DevModel& m, const uint32_t* sp, int v)
       }
     }
   }
-  if (FL == F_PARITY || FL == F_PLAIN_ISING) return INT ? (double)(-2 * idiff) : __dmul_rn(2.0, -diff);
+  if (FL == F_PARITY || FL == F_PLAIN_ISING) return INT ? (double)(-2 * idiff) : times_minus2(diff);
   return INT ? (double)idiff : diff;
 }
 
@@ -552,6 +601,16 @@ __device__ void tabu_refresh(const DevModel& m, const uint32_t* sp, double* df, 
 {
   if (lane == 0) df[i] = lane_diff<FL, INT>(m, sp, i);
   const int rb = m.row[i], re = m.row[i + 1];
+  if (FL == F_PARITY && m.pair_only)
+  {
+    for (int q = rb + lane; q < re; q += 32)
+    {
+      const int x = __ldg(m.other + q);
+      if (x >= 0) df[x] = lane_diff<FL, INT>(m, sp, x);
+    }
+    __syncwarp();
+    return;
+  }
   for (int q = rb + lane; q < re; q += 32)
   {
     const int t = (int)(m.inc[q] & ~kNegBit);
@@ -602,7 +661,8 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
       const int v = v0 + lane;
       const bool ok = v < N;
       const double d = ok ? hd[v] : 0.0;
-      const unsigned take = __ballot_sync(kFull, ok && d <= 0);
+      // d <= 0 for a non-NaN double: its bits as a signed integer are <= 0
+      const unsigned take = __ballot_sync(kFull, ok && __double_as_longlong(d) <= 0);
       if (!take)
       {
         att += (unsigned long long)min(32, N - v0);
@@ -643,11 +703,18 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
     }
     // the scan, markov/tabu_walker.h:68-127: 128 variables per round (four
     // loads in flight per lane), each lane keeping its own first-lowest
-    // candidate off the tabu list
+    // candidate off the tabu list.  fl(cost + d) < low is monotone in d, so
+    // with t = fl(low - cost) and e = 2^-48 max(|cost|, |low|, |t|) every
+    // d < fl(t - e) is taken and every d > fl(t + e) is not (the rounding
+    // errors are below e / 16); only differences in between are added in FP64.
     bool taken = false;
     double bd = 0.0;
+    unsigned long long bk = ~0ull;
     int bv = INT_MAX;
     const unsigned long long it = S.iter;
+    const double t = __dadd_rn(low, -cost);
+    const double e = fmax(__dmul_rn(fmax(fmax(fabs(cost), fabs(low)), fabs(t)), 0x1p-48), 0x1p-1000);
+    const unsigned long long klo = fkey(__dadd_rn(t, -e)), khi = fkey(__dadd_rn(t, e));
     for (int c0 = 0; c0 < N && !taken; c0 += 128)
     {
       double d[4];
@@ -664,7 +731,10 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
       {
         const int v = c0 + 32 * u + lane;
         const bool ok = v < N;
-        const unsigned take = __ballot_sync(kFull, ok && __dadd_rn(cost, d[u]) < low);
+        const unsigned long long k = fkey(d[u]);
+        unsigned take = __ballot_sync(kFull, ok && k < klo);
+        const unsigned near = __ballot_sync(kFull, ok && k >= klo && k <= khi);
+        if (near) take |= __ballot_sync(kFull, ((near >> lane) & 1) && __dadd_rn(cost, d[u]) < low);
         if (take)
         {
           const int j = __ffs(take) - 1;
@@ -699,8 +769,9 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
             S.incomplete -= (unsigned long long)N;
           break;
         }
-        if (ok && !(x[u] >= it) && (bv == INT_MAX || d[u] < bd))
+        if (ok && !(x[u] >= it) && k < bk)
         {
+          bk = k;
           bd = d[u];
           bv = v;
         }
@@ -711,12 +782,14 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
       att += (unsigned long long)N;
       // the lowest difference off the tabu list, the first on ties
 #pragma unroll
-      for (int s = 16; s; s >>= 1)
+      for (int sh = 16; sh; sh >>= 1)
       {
-        const double od = __shfl_xor_sync(kFull, bd, s);
-        const int ov = __shfl_xor_sync(kFull, bv, s);
-        if (ov != INT_MAX && (bv == INT_MAX || od < bd || (od == bd && ov < bv)))
+        const unsigned long long ok_ = __shfl_xor_sync(kFull, bk, sh);
+        const double od = __shfl_xor_sync(kFull, bd, sh);
+        const int ov = __shfl_xor_sync(kFull, bv, sh);
+        if (ov != INT_MAX && (bv == INT_MAX || ok_ < bk || (ok_ == bk && ov < bv)))
         {
+          bk = ok_;
           bd = od;
           bv = ov;
         }
