@@ -14,6 +14,7 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
   solver_pins.json   solver/test/simulated_annealing_test.cc:194-260,
                      solver/test/parallel_tempering_test.cc:239-281,
                      solver/test/population_annealing_test.cc:243-329,
+                     solver/test/tabu_test.cc:98-184,
                      with their data/ inputs and data/params1.json
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
@@ -165,6 +166,12 @@ def solver_pins():
         ("pa", "ising", "isingempty.json", 12, {}, "solver/test/population_annealing_test.cc:293-301"),
         ("pa", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/population_annealing_test.cc:303-315"),
         ("pa", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/population_annealing_test.cc:317-329"),
+        ("tabu", "pubo", "cpupubojobstest.json", "<=-12", {}, "solver/test/tabu_test.cc:98-106"),
+        ("tabu", "ising", "ising1.json", -10, {}, "solver/test/tabu_test.cc:118-126"),
+        ("tabu", "pubo", "puboempty.json", 2, {}, "solver/test/tabu_test.cc:138-146"),
+        ("tabu", "ising", "isingempty.json", 12, {}, "solver/test/tabu_test.cc:148-156"),
+        ("tabu", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/tabu_test.cc:158-170"),
+        ("tabu", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/tabu_test.cc:172-184"),
     ]
     for solver, kind, fname, cost, conf, source in specs:
         model = terms_of(json.loads(read(fname, DATA)))

@@ -114,7 +114,7 @@ def _params(p):
     return dict(seed=p["seed"], step_limit=p["sweeps"])
 
 
-@pytest.mark.parametrize("idx", range(15))
+@pytest.mark.parametrize("idx", range(21))
 def test_solver_end_results(idx, golden):
     case = golden("solver_pins.json")["cases"][idx]
     p = case["params"]
@@ -125,6 +125,9 @@ def test_solver_end_results(idx, golden):
     elif case["solver"] == "pt":
         r = O.run(m, "pt", seed=p["seed"], step_limit=p["sweeps"],
                   sched=("list", 0, 0), sched_values=p["all_betas"], threads=4)
+    elif case["solver"] == "tabu":
+        r = O.run(m, "tabu", seed=p["seed"], step_limit=p["sweeps"], restarts=p["restarts"],
+                  tabu_tenure=p["tabu_tenure"], threads=4)
     else:
         # params1.json leaves PA at its defaults: population = thread count,
         # beta 0 -> 5 linear (solver/population_annealing.h:632-735)
