@@ -19,7 +19,7 @@ _lock = threading.Lock()
 _lib = None
 
 ISING, ISING_PLAIN, PUBO, PUBO_PLAIN, MAXSAT = 0, 1, 2, 3, 4
-SA, PT, PA, TABU = 0, 1, 2, 3
+SA, PT, PA, TABU, SSMC = 0, 1, 2, 3, 4
 RNG_REPLAY, RNG_COUNTER = 0, 1
 SCHED_LINEAR, SCHED_GEOMETRIC, SCHED_CONSTANT, SCHED_LIST = 0, 1, 2, 3
 
@@ -49,7 +49,8 @@ class Params(C.Structure):
                 ("has_cost_limit", C.c_int), ("cost_limit", C.c_double),
                 ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int),
                 ("master_skip", C.c_int64), ("use_master_state", C.c_int),
-                ("master_state", C.c_uint64), ("tabu_tenure", C.c_int64)]
+                ("master_state", C.c_uint64), ("tabu_tenure", C.c_int64),
+                ("sched2", Schedule)]
 
 
 def build(force: bool = False) -> str:
@@ -307,16 +308,24 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
         full_maxsat_sweep=False, resampling="reference", master_skip=0, master_state=None,
-        tabu_tenure=0):
+        tabu_tenure=0, sched2=None, steps_per_walker=1):
+    """sched / sched2 are (kind, initial, final) or (kind, initial, final,
+    start, stop); SSMC takes alpha from sched and beta from sched2, the
+    target population from `population`, its streams from `pa_threads`."""
     p = Params()
-    p.solver = {"sa": SA, "pt": PT, "pa": PA, "tabu": TABU}[solver]
+    p.solver = {"sa": SA, "pt": PT, "pa": PA, "tabu": TABU, "ssmc": SSMC}[solver]
     p.seed = seed & 0xFFFFFFFF
     p.step_limit = step_limit
     p.restarts = restarts
     p.use_inverse = 1 if use_inverse else 0
-    kind, a, b = sched
-    p.sched, keep = schedule(kind, a, b, values=sched_values, count=sched_count)
-    p.sweeps_per_replica = sweeps_per_replica
+    kind, a, b, *rng_ = sched
+    p.sched, keep = schedule(kind, a, b, values=sched_values, count=sched_count,
+                             start=rng_[0] if rng_ else None, stop=rng_[1] if rng_ else None)
+    if sched2 is not None:
+        kind2, a2, b2, *rng2 = sched2
+        p.sched2, _ = schedule(kind2, a2, b2, start=rng2[0] if rng2 else None,
+                               stop=rng2[1] if rng2 else None)
+    p.sweeps_per_replica = sweeps_per_replica if solver != "ssmc" else steps_per_walker
     p.population = population
     p.alpha = alpha
     p.constant_population = int(constant_population)

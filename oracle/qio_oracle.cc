@@ -1395,6 +1395,199 @@ struct Selector
 };
 
 // ---------------------------------------------------------------------------
+// SubstochasticMonteCarlo, solver/substochastic_monte_carlo.h:36-240: a
+// population of random walkers (markov/random_walker.h: every proposed flip
+// is accepted).  Each step, every walker attempts steps_per_walker flips,
+// each taken with probability alpha(step) / steps_per_walker; then the
+// population is resampled with weights exp(beta(step) (max - cost) /
+// (max - min)): floor(target * w / W) copies each, the remaining slots drawn
+// without replacement by the residual weights (utils::RandomSelector on the
+// master stream), copies laid out as Population::resample does.
+// Replay streams emulate the reference's OpenMP threads: rngs[t] forked from
+// the master, thread t serving a contiguous block of walkers in index order
+// (schedule(static)); walker init draws on the same per-thread streams.
+// Counter mode: the walker in slot j draws counter_uniform(key_j, 2 c) and
+// (key_j, 2 c + 1) for its c-th attempt (c = step * steps_per_walker + k),
+// key_j = counter_key(seed, j).
+// ---------------------------------------------------------------------------
+static double counter_uniform(uint64_t key, uint64_t ctr)
+{
+  return (double)(counter_draw(key, ctr) >> 11) * 0x1p-53;
+}
+
+// libgomp's schedule(static) block of thread t among T for n iterations
+static void static_block(size_t n, size_t T, size_t t, size_t& b, size_t& e)
+{
+  size_t q = n / T, r = n % T;
+  if (t < r)
+  {
+    b = t * (q + 1);
+    e = b + q + 1;
+  }
+  else
+  {
+    b = t * q + r;
+    e = b + q;
+  }
+}
+
+static void ssmc_schedules(const orc_params& p, Schedule& alpha, Schedule& beta)
+{
+  alpha = to_schedule(p.sched);
+  beta = to_schedule(p.sched2);
+  // solver/substochastic_monte_carlo.h:177-227
+  if (alpha.get_count() <= 1 && beta.get_count() <= 1)
+  {
+    alpha.has_stop = beta.has_stop = true;
+    alpha.stop_ = beta.stop_ = (double)(int)p.step_limit;
+  }
+  else if (alpha.get_count() <= 1)
+  {
+    alpha.has_stop = true;
+    alpha.stop_ = (double)(int)beta.get_stop();
+  }
+  else if (beta.get_count() <= 1)
+  {
+    beta.has_stop = true;
+    beta.stop_ = (double)(int)alpha.get_stop();
+  }
+  else if (alpha.get_count() != beta.get_count())
+    throw std::runtime_error("The schedules for alpha and beta must have the same length");
+  if (alpha.progress_value(0) <= alpha.progress_value(1))
+    throw std::runtime_error("the schedule for alpha must be decreasing");
+  if (beta.progress_value(0) >= beta.progress_value(1))
+    throw std::runtime_error("the schedule for beta must be increasing");
+}
+
+static Result run_ssmc(const Model& m, const orc_params& p)
+{
+  Result r;
+  r.n_vars = m.N;
+  if (m.empty())
+  {
+    r.has_best = false;
+    r.best_cost = m.const_cost;
+    return r;
+  }
+  Schedule alpha, beta;
+  ssmc_schedules(p, alpha, beta);
+  const size_t R = (size_t)p.population;
+  const size_t T = (size_t)std::max(1, p.pa_threads);
+  const int64_t spw = std::max<int64_t>(1, p.sweeps_per_replica);
+  const bool counter = p.rng_mode == ORC_RNG_COUNTER;
+  PcgRng master(p.seed);
+  std::vector<std::unique_ptr<Rng>> rngs(T);
+  for (size_t t = 0; t < T; t++) rngs[t] = master.fork();
+  std::vector<Walker> pop(R);
+  for (size_t t = 0; t < T; t++)
+  {
+    size_t b, e;
+    static_block(R, T, t, b, e);
+    for (size_t i = b; i < e; i++)
+    {
+      Walker& w = pop[i];
+      w.model = &m;
+      w.rng = rngs[t].get();
+      w.counter_mode = counter;
+      w.key = counter_key(p.seed, i);
+      w.init();
+    }
+  }
+  Lowest low;
+  low.update(pop[0].cost_, pop[0].state.spins);
+  const int64_t n = m.N;
+  int64_t step = 0;
+  for (; step < p.step_limit; step++)
+  {
+    const double p_step = alpha.get_value((double)step) / (double)spw;
+    // make_walker_steps
+    for (size_t t = 0; t < T; t++)
+    {
+      size_t b, e;
+      static_block(R, T, t, b, e);
+      for (size_t i = b; i < e; i++)
+      {
+        Walker& w = pop[i];
+        const uint64_t key = counter_key(p.seed, i);
+        for (int64_t k = 0; k < spw; k++)
+        {
+          const uint64_t c = (uint64_t)(step * spw + k);
+          const double u = counter ? counter_uniform(key, 2 * c) : rngs[t]->uniform();
+          if (u < p_step)
+          {
+            const double u2 = counter ? counter_uniform(key, 2 * c + 1) : rngs[t]->uniform();
+            const int64_t v = (int64_t)(u2 * (double)n);
+            const double d = cost_difference(m, w.state, v);
+            w.diff_evals++;
+            w.total_attempts++;
+            apply_transition(m, v, w.state);
+            w.accepted++;
+            w.total_accepts++;
+            w.cost_ += d;
+            w.check_lowest();
+          }
+        }
+      }
+    }
+    // update_population_statistics
+    double mn = pop[0].cost_, mx = pop[0].cost_;
+    for (size_t i = 0; i < R; i++)
+    {
+      mn = std::min(mn, pop[i].cost_);
+      mx = std::max(mx, pop[i].cost_);
+      low.update(pop[i].lowest_cost, pop[i].lowest_spins);
+    }
+    // resample_population
+    const double b = beta.get_value((double)step);
+    const double range = mx - mn;
+    if (range > 0)
+    {
+      double total = 0;
+      std::vector<double> weight(R);
+      for (size_t i = 0; i < R; i++)
+      {
+        weight[i] = exp(b * (mx - pop[i].cost_) / range);
+        total += weight[i];
+      }
+      size_t resampled = 0;
+      std::vector<size_t> count(R);
+      Selector sel;
+      for (size_t i = 0; i < R; i++)
+      {
+        const double rel = (double)R * weight[i] / total;
+        const size_t iw = (size_t)floor(rel);
+        count[i] = iw;
+        resampled += iw;
+        sel.insert(i, rel - (double)iw);
+      }
+      while (resampled < R)
+      {
+        count[sel.select_and_remove(master.uniform())] += 1;
+        resampled++;
+      }
+      std::vector<Walker> next;
+      next.reserve(R);
+      for (size_t i = 0; i < R; i++)
+        for (size_t c = 0; c < count[i]; c++) next.push_back(pop[i]);
+      pop.swap(next);
+    }
+    if (p.has_cost_limit && low.has && low.cost <= p.cost_limit)
+    {
+      step++;
+      break;
+    }
+  }
+  r.last_step = step;
+  std::vector<Walker*> wp(R);
+  for (size_t i = 0; i < R; i++) wp[i] = &pop[i];
+  fill_replicas(r, wp);
+  populate(r, wp, low, p.number_of_solutions, m, true, true);
+  r.master_out = master.pcg.state;
+  return r;
+}
+
+
+// ---------------------------------------------------------------------------
 // Multinomial resampling mode of the GB300 library (params "resampling":
 // "multinomial", counter streams), restated: the library's exp (Cody-Waite
 // reduction with the fdlibm split of ln 2, degree-13 Taylor polynomial by
@@ -1942,6 +2135,7 @@ void* orc_run(void* m, const orc_params* p, char* err, int errlen)
     else if (p->solver == ORC_PT) *r = run_pt(mm, *p);
     else if (p->solver == ORC_PA) *r = run_pa(mm, *p);
     else if (p->solver == ORC_TABU) *r = run_tabu(mm, *p);
+    else if (p->solver == ORC_SSMC) *r = run_ssmc(mm, *p);
     else throw std::runtime_error("unknown solver");
     return r.release();
   }

@@ -28,7 +28,7 @@ enum {
   ORC_MAXSAT = 4        /* model::MaxSat                               */
 };
 
-enum { ORC_SA = 0, ORC_PT = 1, ORC_PA = 2, ORC_TABU = 3 };
+enum { ORC_SA = 0, ORC_PT = 1, ORC_PA = 2, ORC_TABU = 3, ORC_SSMC = 4 };
 enum { ORC_RNG_REPLAY = 0, ORC_RNG_COUNTER = 1 };
 enum { ORC_SCHED_LINEAR = 0, ORC_SCHED_GEOMETRIC = 1, ORC_SCHED_CONSTANT = 2,
        ORC_SCHED_LIST = 3 };
@@ -73,6 +73,11 @@ typedef struct orc_params {
                                  instead of seeding it (repeated runs) */
   uint64_t master_state;
   int64_t tabu_tenure;        /* tabu: sweeps a taken move stays tabu */
+  orc_schedule sched2;        /* SSMC: beta (resampling) schedule; `sched`
+                                 holds alpha, `sweeps_per_replica` the steps
+                                 per walker, `population` the target
+                                 population, `pa_threads` the emulated
+                                 OpenMP thread count (streams) */
 } orc_params;
 
 /* ---- random generator pins ---- */

@@ -19,7 +19,8 @@ from ._lib import ModelInfo, QioError, SolverStats, check, load
 KINDS = {"ising": 0, "ising_plain": 1, "pubo": 2, "pubo_plain": 3, "maxsat": 4}
 TARGETS = ("simulatedannealing.qiotoolkit", "paralleltempering.qiotoolkit",
            "populationannealing.cpu", "simulatedannealing-parameterfree.qiotoolkit",
-           "paralleltempering-parameterfree.qiotoolkit", "tabu.qiotoolkit")
+           "paralleltempering-parameterfree.qiotoolkit", "tabu.qiotoolkit",
+           "substochasticmontecarlo.cpu")
 
 
 def _ptr(a, ct):

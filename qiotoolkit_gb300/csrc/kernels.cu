@@ -823,6 +823,103 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// Substochastic Monte Carlo walker steps.  Replay: one thread per emulated
+// OpenMP thread t of the reference, serving walkers [b_t, e_t) (libgomp's
+// schedule(static) blocks) in index order on its PCG stream: per attempt one
+// uniform() against p_step, then, when taken, one uniform() for the variable
+// (floor(u * N), model/ising.h:138-143, model/pubo.h:102-107).  Counter
+// mode: one thread per walker slot j, its c-th attempt drawing
+// counter_draw(counter_key(seed, j), 2c) and (.., 2c + 1) as 53-bit uniforms.
+// Every flip is accepted: cost += the difference (term order), lowest kept.
+// ---------------------------------------------------------------------------
+template <int FL, bool INT>
+__device__ __forceinline__ void ssmc_flip(const DevModel& m, const DevPop& p, int w, int v)
+{
+  uint32_t* sp = p.spins + (size_t)w * p.nw;
+  const double d = lane_diff<FL, INT>(m, sp, v);
+  sp[v >> 5] ^= 1u << (v & 31);
+  const double c = __dadd_rn(p.cost[w], d);
+  p.cost[w] = c;
+  p.attempts[w] += 1;
+  p.accepts[w] += 1;
+  if (c < p.lowest[w])
+  {
+    p.lowest[w] = c;
+    uint32_t* ls = p.lspins + (size_t)w * p.nw;
+    for (int q = 0; q < p.nw; q++) ls[q] = sp[q];
+  }
+}
+
+template <int FL, bool INT>
+__global__ void __launch_bounds__(128) ssmc_walk_kernel(SsmcArgs a)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int N = a.m.n_vars;
+  const int spw = a.steps_per_walker;
+  if (a.replay)
+  {
+    if (t >= a.n_chains) return;
+    const int R = a.n_walkers, T = a.n_chains;
+    const int q = R / T, r = R % T;
+    const int b = t < r ? t * (q + 1) : t * q + r;
+    const int e = b + (t < r ? q + 1 : q);
+    uint64_t s = a.rng[t];
+    auto uni = [&]() {
+      const uint32_t d0 = pcg_out(s);
+      s = s * kMult + kInc;
+      const uint32_t d1 = pcg_out(s);
+      s = s * kMult + kInc;
+      return canonical(d0, d1);
+    };
+    for (int w = b; w < e; w++)
+      for (int k = 0; k < spw; k++)
+        if (uni() < a.p_step)
+        {
+          const int v = (int)__dmul_rn(uni(), (double)N);
+          ssmc_flip<FL, INT>(a.m, a.p, w, v);
+        }
+    a.rng[t] = s;
+  }
+  else
+  {
+    if (t >= a.n_walkers) return;
+    const uint64_t key = counter_key(a.seed, (uint64_t)t);
+    for (int k = 0; k < spw; k++)
+    {
+      const unsigned long long c = (unsigned long long)a.step * (unsigned long long)spw + (unsigned long long)k;
+      const double u = (double)(counter_draw(key, 2 * c) >> 11) * 0x1p-53;
+      if (u < a.p_step)
+      {
+        const double u2 = (double)(counter_draw(key, 2 * c + 1) >> 11) * 0x1p-53;
+        ssmc_flip<FL, INT>(a.m, a.p, t, (int)__dmul_rn(u2, (double)N));
+      }
+    }
+  }
+}
+
+template <int FL, bool I>
+static void ssmc_dispatch(const SsmcArgs& a, cudaStream_t s)
+{
+  const int n = a.replay ? a.n_chains : a.n_walkers;
+  const int blocks = (n + 127) / 128;
+  if (blocks > 0) ssmc_walk_kernel<FL, I><<<blocks, 128, 0, s>>>(a);
+}
+
+cudaError_t launch_ssmc_walk(const SsmcArgs& a, cudaStream_t s)
+{
+  if (a.n_walkers <= 0 || a.steps_per_walker <= 0) return cudaSuccess;
+  const bool I = a.m.int_mode != 0;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: I ? ssmc_dispatch<F_PARITY, true>(a, s) : ssmc_dispatch<F_PARITY, false>(a, s); break;
+    case F_COUNTER: I ? ssmc_dispatch<F_COUNTER, true>(a, s) : ssmc_dispatch<F_COUNTER, false>(a, s); break;
+    case F_PLAIN_ISING: I ? ssmc_dispatch<F_PLAIN_ISING, true>(a, s) : ssmc_dispatch<F_PLAIN_ISING, false>(a, s); break;
+    default: I ? ssmc_dispatch<F_PLAIN_PUBO, true>(a, s) : ssmc_dispatch<F_PLAIN_PUBO, false>(a, s); break;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // PT: observations then alternating-parity neighbour swaps of the slot
 // labels (solver/parallel_tempering.h:134-189); one thread per restart.
 // ---------------------------------------------------------------------------

@@ -8,6 +8,8 @@
 // reference exactly.  Only R doubles and R ints cross PCIe per step; the
 // O(R * N) state traffic stays in HBM.
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -863,6 +865,354 @@ void PopulationAnnealing::run(cudaStream_t st)
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   check_device_error(st);
+}
+
+// ---------------------------------------------------------------------------
+// Substochastic Monte Carlo ("substochasticmontecarlo.cpu",
+// solver/substochastic_monte_carlo.h:22-311): a population of random walkers
+// resampled every step.  The walker steps run on the device
+// (ssmc_walk_kernel); the O(R) statistics and resampling run on the host in
+// the reference's arithmetic (sequential sums, the C library's exp, the
+// RandomSelector on the master PCG stream), the copies on the device.
+// Replay streams emulate the reference's OpenMP threads (`threads` streams,
+// each serving a contiguous block of walkers); counter streams key each
+// walker slot.
+// ---------------------------------------------------------------------------
+class SubstochasticMonteCarlo : public Solver
+{
+ public:
+  int64_t target_pop = 1, spw = 1;
+  Schedule alpha, beta;
+  Pool pools[2];
+  int cur = 0;
+  DevBuf aux;  // src map (R ints), chain streams (T), init streams (R), best spins
+  int* d_src = nullptr;
+  uint64_t* d_chain = nullptr;
+  uint64_t* d_init = nullptr;
+  uint32_t* d_best = nullptr;
+  PcgEngine master{0};
+  bool has_low = false;
+  double low_cost = 0;
+  int T = 1;
+
+  std::string target() const override { return "substochasticmontecarlo.cpu"; }
+  int64_t n_walkers() const override { return model->empty() ? 0 : target_pop; }
+
+  static std::string num6(double x)
+  {
+    char b[64];
+    snprintf(b, sizeof b, "%g", x);
+    return b;
+  }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common_public(*this, doc);
+    if (model->kind == K_MAXSAT) fail(1, "substochastic Monte Carlo runs Ising and PUBO models here");
+    auto num = [&](const char* k, double def) {
+      const json::Value* v = params.find(k);
+      if (!v || v->is_null()) return def;
+      if (!v->is_number()) fail(1, std::string("parameter `") + k + "`: expected number");
+      return v->num;
+    };
+    target_pop = (int64_t)num("target_population", (double)threads);
+    if (target_pop <= 0) fail(1, "parameter `target_population`: must be greater than 0");
+    if (target_pop > (1 << 24)) fail(1, "parameter `target_population` too large");
+    spw = (int64_t)num("steps_per_walker", 1.0);
+    if (spw <= 0) fail(1, "parameter `steps_per_walker`: must be greater than 0");
+    alpha = Schedule{};
+    alpha.type = 0;
+    alpha.initial = 1.0;
+    alpha.final_ = 0.0;
+    beta = Schedule{};
+    beta.type = 0;
+    beta.initial = 0.0;
+    beta.final_ = 5.0;
+    if (params.find("alpha")) alpha = parse_schedule(params["alpha"], "alpha");
+    if (params.find("beta")) beta = parse_schedule(params["beta"], "beta");
+    // equal lengths (solver/substochastic_monte_carlo.h:177-209)
+    if (alpha.get_count() <= 1 && beta.get_count() <= 1)
+    {
+      alpha.has_stop = beta.has_stop = true;
+      alpha.stop_ = beta.stop_ = (double)(int)step_limit;
+    }
+    else if (alpha.get_count() <= 1)
+    {
+      alpha.has_stop = true;
+      alpha.stop_ = (double)(int)beta.get_stop();
+    }
+    else if (beta.get_count() <= 1)
+    {
+      beta.has_stop = true;
+      beta.stop_ = (double)(int)alpha.get_stop();
+    }
+    else if (alpha.get_count() != beta.get_count())
+      fail(1, "The schedules for alpha and beta must have the same length");
+    const double a0 = alpha.progress_value(0), a1 = alpha.progress_value(1);
+    if (a0 <= a1)
+      fail(1, "the schedule for alpha must be decreasing (i.e., alpha.initial > alpha.final). Found alpha.initial = " +
+                  num6(a0) + " <= " + num6(a1) + " = alpha.final.");
+    const double b0 = beta.progress_value(0), b1 = beta.progress_value(1);
+    if (b0 >= b1)
+      fail(1, "the schedule for beta must be increasing (i.e., beta.initial < beta.final). Found beta.initial = " +
+                  num6(b0) + " >= " + num6(b1) + " = beta.final.");
+    T = threads;
+    output_params.push_back({"target_population", std::to_string(target_pop)});
+    output_params.push_back({"steps_per_walker", std::to_string(spw)});
+    output_params.push_back({"alpha", alpha.render()});
+    output_params.push_back({"beta", beta.render()});
+  }
+
+  bool historical_lowest(double& c, std::vector<uint8_t>& st) override
+  {
+    if (!has_low) return false;
+    c = low_cost;
+    std::vector<uint32_t> w(pools[0].pop.nw);
+    cuda_check(cudaMemcpy(w.data(), d_best, w.size() * 4, cudaMemcpyDeviceToHost), "D2H best");
+    st.assign(model->N, 0);
+    for (int64_t v = 0; v < model->N; v++) st[v] = (w[v / 32] >> (v % 32)) & 1u;
+    return true;
+  }
+
+  void init(cudaStream_t st) override
+  {
+    initialized = true;
+    if (model->empty()) return;
+    ensure_device();
+    const int R = (int)target_pop;
+    if (!pools[0].buf.ptr)
+    {
+      pools[0].alloc(*model, R);
+      pools[1].alloc(*model, R);
+      size_t off = 0;
+      auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+      const size_t o_src = take((size_t)R * 4), o_ch = take((size_t)T * 8), o_in = take((size_t)R * 8),
+                   o_b = take((size_t)pools[0].pop.nw * 4);
+      aux = DevBuf(off);
+      char* b = (char*)aux.ptr;
+      d_src = (int*)(b + o_src);
+      d_chain = (uint64_t*)(b + o_ch);
+      d_init = (uint64_t*)(b + o_in);
+      d_best = (uint32_t*)(b + o_b);
+    }
+    device_bytes = (int64_t)(pools[0].buf.bytes + pools[1].buf.bytes + aux.bytes);
+    cur = 0;
+    has_low = false;
+    step_pos = 0;
+    // rngs_[t] = rng_->fork() (solver/substochastic_monte_carlo.h:47-51);
+    // thread t initialises its block of walkers in index order, each walker
+    // taking one draw per 32 variables (model/ising.h:23-41)
+    master = PcgEngine(seed);
+    const uint64_t per = (uint64_t)((model->N + 31) / 32);
+    std::vector<uint64_t> chain(T), wi(R);
+    for (int t = 0; t < T; t++)
+    {
+      uint64_t f = PcgEngine((uint32_t)master()).state;
+      const int q = R / T, r = R % T;
+      const int b0 = t < r ? t * (q + 1) : t * q + r, e0 = b0 + (t < r ? q + 1 : q);
+      for (int i = b0; i < e0; i++) wi[i] = jump(f, (uint64_t)(i - b0) * per);
+      chain[t] = jump(f, (uint64_t)(e0 - b0) * per);
+    }
+    cuda_check(cudaMemcpyAsync(d_chain, chain.data(), T * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(d_init, wi.data(), (size_t)R * 8, cudaMemcpyHostToDevice, st), "H2D");
+    InitArgs a{};
+    a.m = model->device_view(false);
+    a.p = pools[0].pop;
+    a.n_walkers = R;
+    a.replay = replay ? 1 : 0;
+    a.rng = d_init;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    a.skip_terms = 1;  // the walker steps work from the spins
+    cuda_check(launch_init(a, st), "init kernel");
+    launches++;
+    used_kernel = 5;
+    // update_lowest_cost(population_[0]->cost(), state())
+    cuda_check(cudaMemcpyAsync(&low_cost, pools[0].pop.cost, 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaMemcpyAsync(d_best, pools[0].pop.spins, pools[0].pop.nw * 4, cudaMemcpyDeviceToDevice, st),
+               "D2D");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    has_low = true;
+  }
+
+  // one step: walker steps, statistics, resampling (make_step, :67-84)
+  void step(cudaStream_t st, int64_t s, std::vector<double>& cost, std::vector<double>& low)
+  {
+    const int R = (int)target_pop;
+    SsmcArgs a{};
+    a.m = model->device_view(false);
+    a.p = pools[cur].pop;
+    a.n_walkers = R;
+    a.steps_per_walker = (int)spw;
+    a.p_step = alpha.get_value((double)s) / (double)spw;
+    a.step = s;
+    a.n_chains = T;
+    a.rng = d_chain;
+    a.seed = seed;
+    a.replay = replay ? 1 : 0;
+    prof_begin(st);
+    cuda_check(launch_ssmc_walk(a, st), "ssmc walk kernel");
+    prof_end(st);
+    launches++;
+    const DevPop& p = pools[cur].pop;
+    cuda_check(cudaMemcpyAsync(cost.data(), p.cost, (size_t)R * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaMemcpyAsync(low.data(), p.lowest, (size_t)R * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    // update_population_statistics (:114-126)
+    double mn = cost[0], mx = cost[0];
+    int best = -1;
+    for (int i = 0; i < R; i++)
+    {
+      mn = std::min(mn, cost[i]);
+      mx = std::max(mx, cost[i]);
+      if (low[i] < low_cost)
+      {
+        low_cost = low[i];
+        best = i;
+      }
+    }
+    if (best >= 0)
+      cuda_check(cudaMemcpyAsync(d_best, p.lspins + (size_t)best * p.nw, p.nw * 4, cudaMemcpyDeviceToDevice, st),
+                 "D2D");
+    // resample_population (:128-169)
+    const double b = beta.get_value((double)s);
+    const double range = mx - mn;
+    if (range > 0)
+    {
+      double total = 0;
+      std::vector<double> weight(R);
+      for (int i = 0; i < R; i++)
+      {
+        weight[i] = exp(b * (mx - cost[i]) / range);
+        total += weight[i];
+      }
+      size_t resampled = 0;
+      std::vector<size_t> count(R);
+      Selector sel;
+      for (int i = 0; i < R; i++)
+      {
+        const double rel = (double)target_pop * weight[i] / total;
+        const size_t iw = (size_t)floor(rel);
+        count[i] = iw;
+        resampled += iw;
+        sel.insert((size_t)i, rel - (double)iw);
+      }
+      while (resampled < (size_t)R)
+      {
+        count[sel.select_and_remove(master.uniform())] += 1;
+        resampled++;
+      }
+      std::vector<int> src;
+      src.reserve(R);
+      for (int i = 0; i < R; i++)
+        for (size_t c = 0; c < count[i]; c++) src.push_back(i);
+      cuda_check(cudaMemcpyAsync(d_src, src.data(), (size_t)R * 4, cudaMemcpyHostToDevice, st), "H2D");
+      cuda_check(launch_pa_copy(pools[cur].pop, pools[1 - cur].pop, d_src, R, st), "copy kernel");
+      launches++;
+      // the src map must stay alive until the copy has read it
+      cuda_check(cudaStreamSynchronize(st), "sync");
+      cur = 1 - cur;
+    }
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    std::vector<double> cost(target_pop), low(target_pop);
+    auto t0 = std::chrono::steady_clock::now();
+    int64_t s = step_pos;
+    for (; s < step_limit; s++)
+    {
+      step(st, s, cost, low);
+      if (has_cost_limit && low_cost <= cost_limit)
+      {
+        s++;
+        break;
+      }
+      if (has_time_limit &&
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= time_limit)
+      {
+        s++;
+        break;
+      }
+    }
+    step_pos = s;
+    last_step = s;
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    run_ms = ms;
+    sweep_ms = profile ? prof_total_ms() : ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_device_error(st);
+  }
+
+  bool advance(cudaStream_t st, int64_t n) override
+  {
+    if (!initialized) fail(1, "init() must be called before advance()");
+    ran = true;
+    if (model->empty() || step_limit <= 0)
+    {
+      last_step = step_limit;
+      return true;
+    }
+    std::vector<double> cost(target_pop), low(target_pop);
+    const int64_t end = std::min(step_limit, step_pos + n);
+    for (; step_pos < end; step_pos++) step(st, step_pos, cost, low);
+    last_step = step_pos;
+    return step_pos >= step_limit;
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
+             std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
+             std::vector<uint8_t>* states) override
+  {
+    const int n = (int)n_walkers();
+    cost.resize(n);
+    lowest.resize(n);
+    att.resize(n);
+    acc.resize(n);
+    if (!n) return;
+    const DevPop& p = pools[cur].pop;
+    cuda_check(cudaMemcpy(cost.data(), p.cost, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(lowest.data(), p.lowest, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), p.attempts, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), p.accepts, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    std::vector<uint32_t> w((size_t)n * p.nw);
+    auto unpack = [&](std::vector<uint8_t>& out) {
+      out.assign((size_t)n * model->N, 0);
+      for (int r = 0; r < n; r++)
+        for (int64_t v = 0; v < model->N; v++)
+          out[(size_t)r * model->N + v] = (w[(size_t)r * p.nw + v / 32] >> (v % 32)) & 1u;
+    };
+    if (lowest_states)
+    {
+      cuda_check(cudaMemcpy(w.data(), p.lspins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      unpack(*lowest_states);
+    }
+    if (states)
+    {
+      cuda_check(cudaMemcpy(w.data(), p.spins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      unpack(*states);
+    }
+  }
+};
+
+std::unique_ptr<Solver> make_ssmc_solver(const HostModel* m, const json::Value& doc)
+{
+  std::unique_ptr<SubstochasticMonteCarlo> s(new SubstochasticMonteCarlo());
+  s->model = m;
+  s->configure(doc);
+  return std::unique_ptr<Solver>(s.release());
 }
 
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc)

@@ -299,6 +299,25 @@ struct TabuArgs
 };
 cudaError_t launch_tabu(const TabuArgs& a, cudaStream_t s);
 
+// Substochastic Monte Carlo walker steps (solver/substochastic_monte_carlo.h:
+// 86-112): every walker attempts steps_per_walker random flips, each made
+// with probability p_step and always accepted (markov/random_walker.h).
+struct SsmcArgs
+{
+  DevModel m;
+  DevPop p;
+  int n_walkers;
+  int steps_per_walker;
+  double p_step;
+  long long step;           // absolute step (counter mode draw positions)
+  int n_chains;             // replay: emulated OpenMP threads, each serving a
+                            // contiguous block of walkers in index order
+  uint64_t* rng;            // replay: PCG state per chain
+  uint32_t seed;            // counter mode: slot j draws on counter_key(seed, j)
+  int replay;
+};
+cudaError_t launch_ssmc_walk(const SsmcArgs& a, cudaStream_t s);
+
 // PT: label swaps + observables, one thread per restart.
 struct SwapArgs
 {

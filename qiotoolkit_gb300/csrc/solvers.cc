@@ -1175,6 +1175,7 @@ class ParallelTempering : public Solver
 };
 
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc);
+std::unique_ptr<Solver> make_ssmc_solver(const HostModel* m, const json::Value& doc);
 
 // ---------------------------------------------------------------------------
 // Tabu search ("tabu.qiotoolkit": solver/tabu.h:22-164 with
@@ -1732,6 +1733,7 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
     return std::unique_ptr<Solver>(s.release());
   }
   if (target == "populationannealing.cpu") return make_pa_solver(m, doc);
+  if (target == "substochasticmontecarlo.cpu") return make_ssmc_solver(m, doc);
   if (target == "simulatedannealing-parameterfree.qiotoolkit")
   {
     std::unique_ptr<SAParameterFree> s(new SAParameterFree());

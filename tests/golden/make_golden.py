@@ -15,6 +15,7 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
                      solver/test/parallel_tempering_test.cc:239-281,
                      solver/test/population_annealing_test.cc:243-329,
                      solver/test/tabu_test.cc:98-184,
+                     solver/test/substochastic_monte_carlo_test.cc:104-176,
                      with their data/ inputs and data/params1.json
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
@@ -172,6 +173,12 @@ def solver_pins():
         ("tabu", "ising", "isingempty.json", 12, {}, "solver/test/tabu_test.cc:148-156"),
         ("tabu", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/tabu_test.cc:158-170"),
         ("tabu", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/tabu_test.cc:172-184"),
+        ("ssmc", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/substochastic_monte_carlo_test.cc:104-112"),
+        ("ssmc", "pubo", "puboempty.json", 2, {}, "solver/test/substochastic_monte_carlo_test.cc:114-122"),
+        ("ssmc", "ising", "isingempty.json", 12, {}, "solver/test/substochastic_monte_carlo_test.cc:124-132"),
+        ("ssmc", "ising", "ising1.json", -10, {}, "solver/test/substochastic_monte_carlo_test.cc:134-142"),
+        ("ssmc", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/substochastic_monte_carlo_test.cc:144-154"),
+        ("ssmc", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/substochastic_monte_carlo_test.cc:166-176"),
     ]
     for solver, kind, fname, cost, conf, source in specs:
         model = terms_of(json.loads(read(fname, DATA)))

@@ -159,7 +159,10 @@ def test_reference_solver_pins_on_gpu(golden):
                                  "terms": [{"c": c, "ids": ids} for c, ids in case["terms"]]}}
         if case["solver"] == "pa":
             p = {"seed": p["seed"], "sweeps": p["sweeps"], "population": 8, "threads": 4}
-        target = {"sa": SA, "pt": PT, "pa": PA, "tabu": "tabu.qiotoolkit"}[case["solver"]]
+        if case["solver"] == "ssmc":
+            p = {"seed": p["seed"], "sweeps": p["sweeps"], "target_population": 8, "threads": 8}
+        target = {"sa": SA, "pt": PT, "pa": PA, "tabu": "tabu.qiotoolkit",
+                  "ssmc": "substochasticmontecarlo.cpu"}[case["solver"]]
         res = q.run_json(doc, {"params": p}, target)
         cost = res["solutions"]["cost"]
         exp = case["expected_cost"]

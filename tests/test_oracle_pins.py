@@ -114,7 +114,7 @@ def _params(p):
     return dict(seed=p["seed"], step_limit=p["sweeps"])
 
 
-@pytest.mark.parametrize("idx", range(21))
+@pytest.mark.parametrize("idx", range(27))
 def test_solver_end_results(idx, golden):
     case = golden("solver_pins.json")["cases"][idx]
     p = case["params"]
@@ -125,6 +125,12 @@ def test_solver_end_results(idx, golden):
     elif case["solver"] == "pt":
         r = O.run(m, "pt", seed=p["seed"], step_limit=p["sweeps"],
                   sched=("list", 0, 0), sched_values=p["all_betas"], threads=4)
+    elif case["solver"] == "ssmc":
+        # params1.json leaves SSMC at its defaults: target population = thread
+        # count, alpha 1 -> 0 and beta 0 -> 5 linear over the step limit
+        # (solver/substochastic_monte_carlo.h:157-199)
+        r = O.run(m, "ssmc", seed=p["seed"], step_limit=p["sweeps"], population=8, pa_threads=8,
+                  sched=("linear", 1.0, 0.0), sched2=("linear", 0.0, 5.0))
     elif case["solver"] == "tabu":
         r = O.run(m, "tabu", seed=p["seed"], step_limit=p["sweeps"], restarts=p["restarts"],
                   tabu_tenure=p["tabu_tenure"], threads=4)
