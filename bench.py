@@ -9,7 +9,7 @@ One step = one complete solve (init + 500 sweeps + 500 swap phases of all 512
 walkers) = 1.05e9 flip attempts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising]
+                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising|ssmc_ising]
 
 Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
 launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
@@ -55,6 +55,11 @@ WORKLOADS = {
                             "U[-0.5,0.5], tabu_tenure 20, 200 sweeps, 1216 restarts, seed 0; attempts are "
                             "cost-difference evaluations (scan and hill-climbing sweeps)",
                        target="tabu.qiotoolkit"),
+    "ssmc_ising": dict(desc="Substochastic Monte Carlo on the sparse Ising N=1000, 3000 ER couplings +-1, "
+                            "1000 fields U[-0.5,0.5], target population 4096, 200 steps, 4 steps per walker, "
+                            "alpha 1->0 and beta 0->5 linear, counter streams, seed 0; attempts are the "
+                            "flips made (each a cost-difference evaluation)",
+                       target="substochasticmontecarlo.cpu"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
@@ -75,7 +80,7 @@ def batch_instances(n=512):
 
 # the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
 KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel",
-                4: "tabu_kernel"}
+                4: "tabu_kernel", 5: "ssmc_walk_kernel"}
 
 
 def make_workload(name):
@@ -95,6 +100,11 @@ def make_workload(name):
         off, ids, coef = I.er_ising(1000, 3000, seed=0)
         params = {"seed": 0, "sweeps": 200, "restarts": 1216, "tabu_tenure": 20}
         return "ising", off, ids, coef, params
+    if name == "ssmc_ising":
+        off, ids, coef = I.er_ising(1000, 3000, seed=0)
+        params = {"seed": 0, "sweeps": 200, "target_population": 4096, "steps_per_walker": 4,
+                  "threads": 16, "rng_mode": "counter"}
+        return "ising", off, ids, coef, params
     if name == "pa_square":
         off, ids, coef = I.square_pm_j(256, seed=3)
         params = {"seed": 0, "sweeps": 100, "population": 4096, "beta_start": 0.0,
@@ -105,6 +115,8 @@ def make_workload(name):
 
 
 def attempts_per_step(kind, n_vars, params):
+    if "target_population" in params or "tabu_tenure" in params:
+        return 0  # counted from the run (see main)
     if "temperatures" in params:
         return params["restarts"] * params["temperatures"]["count"] * params["sweeps"] * n_vars
     if "population" in params:
@@ -210,6 +222,13 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
                   resampling=params.get("resampling", "reference"))
             a = restarts * sweeps * params["sweeps_per_replica"] * n
             d = f"population {restarts} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
+        elif "target_population" in params:
+            r = O.run(m, "ssmc", seed=0, step_limit=sweeps, population=restarts, threads=threads,
+                      pa_threads=params["threads"], steps_per_walker=params["steps_per_walker"],
+                      sched=("linear", 1.0, 0.0), sched2=("linear", 0.0, 5.0),
+                      rng_mode=params.get("rng_mode", "replay"))
+            a = int(np.sum(r.attempts))
+            d = f"population {restarts} x {sweeps} steps x {params['steps_per_walker']} steps per walker"
         elif "tabu_tenure" in params:
             r = O.run(m, "tabu", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
                       tabu_tenure=params["tabu_tenure"])
@@ -222,7 +241,7 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
             d = f"{restarts} restarts x {sweeps} sweeps"
         return a, time.perf_counter() - t0, d
 
-    full_r = params.get("restarts", params.get("population", 1))
+    full_r = params.get("restarts", params.get("population", params.get("target_population", 1)))
     full_s = params["sweeps"]
     # the parallel dimension first (replicas keep the cores busy), then sweeps
     r0 = min(full_r, max(threads, 1)) if "temperatures" not in params else 1
@@ -362,9 +381,10 @@ def main():
     st0 = None
     for _ in range(args.warmup):
         _, st0, _ = one_step()
-    if target == "tabu.qiotoolkit":
-        # a tabu scan stops at the first improving flip: count the
-        # evaluations (deterministic for the fixed seed)
+    if target in ("tabu.qiotoolkit", "substochasticmontecarlo.cpu"):
+        # evaluations depend on the run (a tabu scan stops at the first
+        # improving flip; SSMC flips with probability alpha): count them
+        # (deterministic for the fixed seed)
         if st0 is None:
             _, st0, _ = one_step()
         A = int(st0.attempts)
@@ -386,6 +406,8 @@ def main():
     value = A * args.steps * ws / total_s
     if target in ("simulatedannealing.qiotoolkit", "tabu.qiotoolkit"):
         sweep_launches_per_step = 1
+    elif target == "substochasticmontecarlo.cpu":
+        sweep_launches_per_step = params["sweeps"]
     else:
         sweep_launches_per_step = params["sweeps"]
     avg_sweep_launch_ms = statistics.mean(sweep_ms) / sweep_launches_per_step

@@ -88,7 +88,8 @@ typedef struct qio_solver_stats {
                               mean committed window is attempts / windows */
   int32_t sweep_kernel;    /* kernel of the last sweeps: 1 one walker per
                               warp, 2 one walker per lane, 3 level schedule,
-                              4 tabu search (one walker per warp) */
+                              4 tabu search (one walker per warp),
+                              5 substochastic Monte Carlo walker steps */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */
