@@ -19,7 +19,7 @@ _lock = threading.Lock()
 _lib = None
 
 ISING, ISING_PLAIN, PUBO, PUBO_PLAIN, MAXSAT = 0, 1, 2, 3, 4
-SA, PT, PA, TABU, SSMC = 0, 1, 2, 3, 4
+SA, PT, PA, TABU, SSMC, QMC = 0, 1, 2, 3, 4, 5
 RNG_REPLAY, RNG_COUNTER = 0, 1
 SCHED_LINEAR, SCHED_GEOMETRIC, SCHED_CONSTANT, SCHED_LIST = 0, 1, 2, 3
 
@@ -50,7 +50,7 @@ class Params(C.Structure):
                 ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int),
                 ("master_skip", C.c_int64), ("use_master_state", C.c_int),
                 ("master_state", C.c_uint64), ("tabu_tenure", C.c_int64),
-                ("sched2", Schedule)]
+                ("sched2", Schedule), ("trotter_number", C.c_int64)]
 
 
 def build(force: bool = False) -> str:
@@ -308,12 +308,12 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
         full_maxsat_sweep=False, resampling="reference", master_skip=0, master_state=None,
-        tabu_tenure=0, sched2=None, steps_per_walker=1):
+        tabu_tenure=0, sched2=None, steps_per_walker=1, trotter_number=2):
     """sched / sched2 are (kind, initial, final) or (kind, initial, final,
     start, stop); SSMC takes alpha from sched and beta from sched2, the
     target population from `population`, its streams from `pa_threads`."""
     p = Params()
-    p.solver = {"sa": SA, "pt": PT, "pa": PA, "tabu": TABU, "ssmc": SSMC}[solver]
+    p.solver = {"sa": SA, "pt": PT, "pa": PA, "tabu": TABU, "ssmc": SSMC, "qmc": QMC}[solver]
     p.seed = seed & 0xFFFFFFFF
     p.step_limit = step_limit
     p.restarts = restarts
@@ -342,6 +342,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
     p.use_master_state = 0 if master_state is None else 1
     p.master_state = 0 if master_state is None else int(master_state)
     p.tabu_tenure = int(tabu_tenure)
+    p.trotter_number = int(trotter_number)
     err = C.create_string_buffer(512)
     h = lib().orc_run(model.h, C.byref(p), err, 512)
     del keep

@@ -1586,6 +1586,152 @@ static Result run_ssmc(const Model& m, const orc_params& p)
   return r;
 }
 
+// ---------------------------------------------------------------------------
+// QuantumMonteCarlo, solver/quantum_monte_carlo.h:44-233 with
+// markov/cluster_walker.h and markov/quantum_walker.h: each restart holds
+// `trotter_number` slices (imaginary-time copies).  A sweep visits the
+// variables in order; for variable v every slice k computes its difference,
+// slice k > 0 bonds to slice k-1 with probability bond_prob when both hold the
+// same value of v, each run of bonded slices (open boundary: slice 0 starts a
+// run) is flipped together when its summed difference (slice order) is below
+// 1e-11 or a uniform() of its first slice's stream is below
+// exp(-beta_eff * sum); then the flips apply.  beta_eff = beta(step) / P,
+// bond_prob = 1 - tanh(field(step) * beta(step) / P).  Slice i = r * P + k
+// draws on stream i (forked in that order), or, in counter mode, on
+// counter_key(seed, i) at 2 (step * N + v) and 2 (step * N + v) + 1.
+// Per slice: attempts count N per sweep, accepts the flips applied.
+// ---------------------------------------------------------------------------
+static Result run_qmc(const Model& m, const orc_params& p)
+{
+  Result r;
+  r.n_vars = m.N;
+  if (m.empty())
+  {
+    r.has_best = false;
+    r.best_cost = m.const_cost;
+    return r;
+  }
+  const size_t R = (size_t)p.restarts, P = (size_t)p.trotter_number, S = R * P;
+  const bool counter = p.rng_mode == ORC_RNG_COUNTER;
+  Schedule beta = to_schedule(p.sched), field = to_schedule(p.sched2);
+  beta.has_stop = field.has_stop = true;
+  beta.stop_ = field.stop_ = (double)std::max(1, (int)p.step_limit - 1);
+  PcgRng master(p.seed);
+  std::vector<std::unique_ptr<Rng>> rngs(S);
+  for (size_t i = 0; i < S; i++) rngs[i] = master.fork();
+  std::vector<Walker> sl(S);
+  for (size_t i = 0; i < S; i++)
+  {
+    sl[i].model = &m;
+    sl[i].rng = rngs[i].get();
+    sl[i].counter_mode = counter;
+    sl[i].key = counter_key(p.seed, i);
+    sl[i].init();
+  }
+  std::vector<double> low(R, std::numeric_limits<double>::max());
+  std::vector<std::vector<uint8_t>> low_state(R);
+  auto save_lowest = [&](size_t rr) {
+    size_t b = 0;
+    for (size_t k = 1; k < P; k++)
+      if (sl[rr * P + k].cost_ < sl[rr * P + b].cost_) b = k;
+    if (sl[rr * P + b].cost_ < low[rr])
+    {
+      low[rr] = sl[rr * P + b].cost_;
+      low_state[rr] = sl[rr * P + b].state.spins;
+    }
+  };
+  for (size_t rr = 0; rr < R; rr++) save_lowest(rr);
+  Lowest best;
+  best.update(low[0], low_state[0]);
+  const int64_t n = m.N;
+  std::vector<double> diff(P);
+  std::vector<char> bond(P), acc(P);
+  int64_t step = 0;
+  for (; step < p.step_limit; step++)
+  {
+    const double b = beta.get_value((double)step), g = field.get_value((double)step);
+    const double beta_eff = b / (double)P;
+    const double bond_prob = 1 - std::tanh(g * b / (double)P);
+    for (size_t rr = 0; rr < R; rr++)
+    {
+      Walker* w = &sl[rr * P];
+      for (int64_t v = 0; v < n; v++)
+      {
+        const uint64_t c = 2 * ((uint64_t)step * (uint64_t)n + (uint64_t)v);
+        for (size_t k = 0; k < P; k++)
+        {
+          diff[k] = cost_difference(m, w[k].state, v);
+          bond[k] = 0;
+          if (k != 0 && w[k - 1].state.spins[v] == w[k].state.spins[v])
+          {
+            const double u = counter ? counter_uniform(w[k].key, c) : w[k].rng->uniform();
+            bond[k] = u < bond_prob;
+          }
+        }
+        for (size_t k = 0; k < P; k++)
+        {
+          if (bond[k]) continue;
+          double sum = diff[k];
+          size_t e = k + 1;
+          for (; e < P && bond[e]; e++) sum += diff[e];
+          bool a = true;
+          if (!(sum < 10E-12))
+          {
+            const double u = counter ? counter_uniform(w[k].key, c + 1) : w[k].rng->uniform();
+            a = u < std::exp(-beta_eff * sum);
+          }
+          for (size_t i = k; i < e; i++) acc[i] = a;
+        }
+        for (size_t k = 0; k < P; k++)
+          if (acc[k])
+          {
+            apply_transition(m, v, w[k].state);
+            w[k].cost_ += diff[k];
+            w[k].total_accepts++;
+          }
+      }
+      for (size_t k = 0; k < P; k++) w[k].total_attempts += (uint64_t)n;
+      save_lowest(rr);
+    }
+    if (p.has_cost_limit)
+    {
+      for (size_t rr = 0; rr < R; rr++) best.update(low[rr], low_state[rr]);
+      if (best.has && best.cost <= p.cost_limit)
+      {
+        step++;
+        break;
+      }
+    }
+  }
+  r.last_step = step;
+  // per slice: its cost and state; its restart's lowest
+  for (size_t i = 0; i < S; i++)
+  {
+    r.cost.push_back(sl[i].cost_);
+    r.lowest.push_back(low[i / P]);
+    r.attempts.push_back(sl[i].total_attempts);
+    r.accepts.push_back(sl[i].total_accepts);
+    r.states.push_back(sl[i].state.spins);
+    r.lowest_states.push_back(low_state[i / P]);
+  }
+  // populate_solutions over the restarts (solver/model_solver.h:261-308)
+  std::vector<size_t> idx(R);
+  for (size_t i = 0; i < R; i++) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b2) { return low[a] < low[b2]; });
+  const size_t k = std::min((size_t)p.number_of_solutions, R);
+  for (size_t i = 0; i < k; i++)
+  {
+    r.sol_costs.push_back(low[idx[i]] + m.const_cost);
+    r.sol_states.push_back(low_state[idx[i]]);
+  }
+  best.update(low[idx[0]], low_state[idx[0]]);
+  r.has_best = best.has;
+  r.best_cost = best.cost + m.const_cost;
+  r.best_state = best.state;
+  return r;
+}
+
+
 
 // ---------------------------------------------------------------------------
 // Multinomial resampling mode of the GB300 library (params "resampling":
@@ -2136,6 +2282,7 @@ void* orc_run(void* m, const orc_params* p, char* err, int errlen)
     else if (p->solver == ORC_PA) *r = run_pa(mm, *p);
     else if (p->solver == ORC_TABU) *r = run_tabu(mm, *p);
     else if (p->solver == ORC_SSMC) *r = run_ssmc(mm, *p);
+    else if (p->solver == ORC_QMC) *r = run_qmc(mm, *p);
     else throw std::runtime_error("unknown solver");
     return r.release();
   }

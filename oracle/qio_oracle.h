@@ -28,7 +28,7 @@ enum {
   ORC_MAXSAT = 4        /* model::MaxSat                               */
 };
 
-enum { ORC_SA = 0, ORC_PT = 1, ORC_PA = 2, ORC_TABU = 3, ORC_SSMC = 4 };
+enum { ORC_SA = 0, ORC_PT = 1, ORC_PA = 2, ORC_TABU = 3, ORC_SSMC = 4, ORC_QMC = 5 };
 enum { ORC_RNG_REPLAY = 0, ORC_RNG_COUNTER = 1 };
 enum { ORC_SCHED_LINEAR = 0, ORC_SCHED_GEOMETRIC = 1, ORC_SCHED_CONSTANT = 2,
        ORC_SCHED_LIST = 3 };
@@ -78,6 +78,9 @@ typedef struct orc_params {
                                  per walker, `population` the target
                                  population, `pa_threads` the emulated
                                  OpenMP thread count (streams) */
+  int64_t trotter_number;     /* QMC: slices per restart; `sched` holds beta
+                                 (linear), `sched2` the transverse field
+                                 (linear), both stretched over the steps */
 } orc_params;
 
 /* ---- random generator pins ---- */

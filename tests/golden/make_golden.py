@@ -16,6 +16,7 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
                      solver/test/population_annealing_test.cc:243-329,
                      solver/test/tabu_test.cc:98-184,
                      solver/test/substochastic_monte_carlo_test.cc:104-176,
+                     solver/test/quantum_monte_carlo_test.cc:86-148 (data/params_qmc.json),
                      with their data/ inputs and data/params1.json
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
@@ -179,12 +180,19 @@ def solver_pins():
         ("ssmc", "ising", "ising1.json", -10, {}, "solver/test/substochastic_monte_carlo_test.cc:134-142"),
         ("ssmc", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/substochastic_monte_carlo_test.cc:144-154"),
         ("ssmc", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/substochastic_monte_carlo_test.cc:166-176"),
+        ("qmc", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/quantum_monte_carlo_test.cc:86-94"),
+        ("qmc", "pubo", "puboempty.json", 2, {}, "solver/test/quantum_monte_carlo_test.cc:96-104"),
+        ("qmc", "ising", "isingempty.json", 12, {}, "solver/test/quantum_monte_carlo_test.cc:106-114"),
+        ("qmc", "ising", "ising1.json", -10, {}, "solver/test/quantum_monte_carlo_test.cc:116-124"),
+        ("qmc", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/quantum_monte_carlo_test.cc:126-136"),
+        ("qmc", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/quantum_monte_carlo_test.cc:138-148"),
     ]
+    params_qmc = json.loads(read("params_qmc.json", DATA))["params"]
     for solver, kind, fname, cost, conf, source in specs:
         model = terms_of(json.loads(read(fname, DATA)))
         assert model["type"] == kind
         cases.append({"solver": solver, "kind": kind, "file": fname,
-                      "terms": model["terms"], "params": params1,
+                      "terms": model["terms"], "params": params_qmc if solver == "qmc" else params1,
                       "expected_cost": cost, "configuration": conf, "source": source})
     return {"params_file": "data/params1.json", "cases": cases}
 

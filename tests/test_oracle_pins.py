@@ -114,7 +114,7 @@ def _params(p):
     return dict(seed=p["seed"], step_limit=p["sweeps"])
 
 
-@pytest.mark.parametrize("idx", range(27))
+@pytest.mark.parametrize("idx", range(33))
 def test_solver_end_results(idx, golden):
     case = golden("solver_pins.json")["cases"][idx]
     p = case["params"]
@@ -131,6 +131,13 @@ def test_solver_end_results(idx, golden):
         # (solver/substochastic_monte_carlo.h:157-199)
         r = O.run(m, "ssmc", seed=p["seed"], step_limit=p["sweeps"], population=8, pa_threads=8,
                   sched=("linear", 1.0, 0.0), sched2=("linear", 0.0, 5.0))
+    elif case["solver"] == "qmc":
+        # params_qmc.json: beta_start defaults to beta_stop; the transverse
+        # field runs linear low -> high (solver/quantum_monte_carlo.h:185-222)
+        r = O.run(m, "qmc", seed=p["seed"], step_limit=p["sweeps"], restarts=p["restarts"],
+                  trotter_number=p["trotter_number"],
+                  sched=("linear", p["beta_stop"], p["beta_stop"]),
+                  sched2=("linear", p["transverse_field_low"], p["transverse_field_high"]), threads=4)
     elif case["solver"] == "tabu":
         r = O.run(m, "tabu", seed=p["seed"], step_limit=p["sweeps"], restarts=p["restarts"],
                   tabu_tenure=p["tabu_tenure"], threads=4)
