@@ -9,7 +9,8 @@ One step = one complete solve (init + 500 sweeps + 500 swap phases of all 512
 walkers) = 1.05e9 flip attempts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising|ssmc_ising]
+                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising|ssmc_ising|
+                              qmc_ising]
 
 Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
 launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
@@ -60,6 +61,10 @@ WORKLOADS = {
                             "alpha 1->0 and beta 0->5 linear, counter streams, seed 0; attempts are the "
                             "flips made (each a cost-difference evaluation)",
                        target="substochasticmontecarlo.cpu"),
+    "qmc_ising": dict(desc="Quantum Monte Carlo on the sparse Ising N=1000, 3000 ER couplings +-1, 1000 "
+                           "fields U[-0.5,0.5], 16 restarts x 32 Trotter slices, 200 sweeps, beta 1->5 and "
+                           "transverse field 0->3 linear, replayed PCG streams, seed 0",
+                      target="quantummontecarlo.qiotoolkit"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
@@ -80,7 +85,7 @@ def batch_instances(n=512):
 
 # the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
 KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel",
-                4: "tabu_kernel", 5: "ssmc_walk_kernel"}
+                4: "tabu_kernel", 5: "ssmc_walk_kernel", 6: "qmc_kernel"}
 
 
 def make_workload(name):
@@ -100,6 +105,11 @@ def make_workload(name):
         off, ids, coef = I.er_ising(1000, 3000, seed=0)
         params = {"seed": 0, "sweeps": 200, "restarts": 1216, "tabu_tenure": 20}
         return "ising", off, ids, coef, params
+    if name == "qmc_ising":
+        off, ids, coef = I.er_ising(1000, 3000, seed=0)
+        params = {"seed": 0, "sweeps": 200, "restarts": 16, "trotter_number": 32, "beta_start": 1.0,
+                  "beta_stop": 5.0, "transverse_field_low": 0.0, "transverse_field_high": 3.0}
+        return "ising", off, ids, coef, params
     if name == "ssmc_ising":
         off, ids, coef = I.er_ising(1000, 3000, seed=0)
         params = {"seed": 0, "sweeps": 200, "target_population": 4096, "steps_per_walker": 4,
@@ -117,6 +127,8 @@ def make_workload(name):
 def attempts_per_step(kind, n_vars, params):
     if "target_population" in params or "tabu_tenure" in params:
         return 0  # counted from the run (see main)
+    if "trotter_number" in params:
+        return params["restarts"] * params["trotter_number"] * params["sweeps"] * n_vars
     if "temperatures" in params:
         return params["restarts"] * params["temperatures"]["count"] * params["sweeps"] * n_vars
     if "population" in params:
@@ -222,6 +234,13 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
                   resampling=params.get("resampling", "reference"))
             a = restarts * sweeps * params["sweeps_per_replica"] * n
             d = f"population {restarts} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
+        elif "trotter_number" in params:
+            O.run(m, "qmc", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
+                  trotter_number=params["trotter_number"],
+                  sched=("linear", params["beta_start"], params["beta_stop"]),
+                  sched2=("linear", params["transverse_field_low"], params["transverse_field_high"]))
+            a = restarts * params["trotter_number"] * sweeps * n
+            d = f"{restarts} restarts x {params['trotter_number']} slices x {sweeps} sweeps"
         elif "target_population" in params:
             r = O.run(m, "ssmc", seed=0, step_limit=sweeps, population=restarts, threads=threads,
                       pa_threads=params["threads"], steps_per_walker=params["steps_per_walker"],
@@ -404,7 +423,7 @@ def main():
     barrier(ws)
     total_s = reduce_max(sum(ms) / 1e3, ws)
     value = A * args.steps * ws / total_s
-    if target in ("simulatedannealing.qiotoolkit", "tabu.qiotoolkit"):
+    if target in ("simulatedannealing.qiotoolkit", "tabu.qiotoolkit", "quantummontecarlo.qiotoolkit"):
         sweep_launches_per_step = 1
     elif target == "substochasticmontecarlo.cpu":
         sweep_launches_per_step = params["sweeps"]

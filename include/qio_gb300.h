@@ -89,7 +89,8 @@ typedef struct qio_solver_stats {
   int32_t sweep_kernel;    /* kernel of the last sweeps: 1 one walker per
                               warp, 2 one walker per lane, 3 level schedule,
                               4 tabu search (one walker per warp),
-                              5 substochastic Monte Carlo walker steps */
+                              5 substochastic Monte Carlo walker steps,
+                              6 quantum Monte Carlo (one warp per restart) */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */

@@ -161,6 +161,9 @@ class Solver
   }
   // extra members of the result's benchmark block (JSON, starting with ',')
   virtual std::string extra_benchmark() { return ""; }
+  // walkers per solution candidate: the solutions list takes walkers
+  // 0, stride, 2 stride, ... (QMC: one candidate per restart, not per slice)
+  virtual size_t solution_stride() const { return 1; }
   // Serving: the solve in pieces.  After init(), advance() enqueues up to n
   // further steps on the stream and returns true once the step budget is
   // spent (results are read after the stream has finished).  The pieces

@@ -920,6 +920,152 @@ cudaError_t launch_ssmc_walk(const SsmcArgs& a, cudaStream_t s)
 }
 
 // ---------------------------------------------------------------------------
+// Quantum Monte Carlo: one warp per restart, lanes over its slices (slice k
+// on lane k % 32).  For each variable v of the ordered sweep: every slice
+// computes its difference and, for k > 0 with the same value of v as slice
+// k-1, its bond (a uniform() below bond_prob); each run of bonded slices
+// (slice 0 and every unbonded slice start one) sums its differences in slice
+// order, is accepted below 1e-11 or on a uniform() of its first slice below
+// exp(-beta_eff * sum), and all its slices flip together.  The per-warp
+// differences, bonds and acceptances sit in shared memory.  After each sweep
+// the restart keeps the first lowest-cost slice if it beats its lowest.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double qmc_draw(const QmcArgs& a, int slot, unsigned long long ctr)
+{
+  if (a.replay)
+  {
+    uint64_t s = a.rng[slot];
+    const uint32_t d0 = pcg_out(s);
+    s = s * kMult + kInc;
+    const uint32_t d1 = pcg_out(s);
+    a.rng[slot] = s * kMult + kInc;
+    return canonical(d0, d1);
+  }
+  return (double)(counter_draw(counter_key(a.seed, (uint64_t)slot), ctr) >> 11) * 0x1p-53;
+}
+
+template <int FL, bool INT>
+__global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
+{
+  extern __shared__ unsigned char qsm[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int r = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (r >= a.restarts) return;  // whole warps leave together
+  const int P = a.trotter, N = a.m.n_vars, nw = a.p.nw;
+  const size_t per_warp = (size_t)P * 8 + (((size_t)P * 2 + 7) & ~(size_t)7);
+  double* dif = (double*)(qsm + (size_t)wib * per_warp);
+  uint8_t* bond = (uint8_t*)(dif + P);
+  uint8_t* acc = bond + P;
+  const int base = r * P;
+  for (int st = 0; st < a.n_steps; st++)
+  {
+    const long long S = a.step_base + st;
+    const double be = a.beta_eff[S], bp = a.bond_prob[S];
+    for (int v = 0; v < N; v++)
+    {
+      const unsigned long long c = 2ull * ((unsigned long long)S * (unsigned long long)N + (unsigned long long)v);
+      for (int k = lane; k < P; k += 32)
+      {
+        const uint32_t* sp = a.p.spins + (size_t)(base + k) * nw;
+        dif[k] = lane_diff<FL, INT>(a.m, sp, v);
+        uint8_t b = 0;
+        if (k > 0 && spin_of(sp - nw, v) == spin_of(sp, v)) b = qmc_draw(a, base + k, c) < bp;
+        bond[k] = b;
+      }
+      __syncwarp();
+      for (int k = lane; k < P; k += 32)
+      {
+        if (bond[k]) continue;
+        double sum = dif[k];
+        int e = k + 1;
+        for (; e < P && bond[e]; e++) sum = __dadd_rn(sum, dif[e]);
+        uint8_t ok = 1;
+        if (!(sum < 10E-12))
+        {
+          const double u = qmc_draw(a, base + k, c + 1);
+          const double x = exp(__dmul_rn(-be, sum));
+          if (fabs(u - x) <= 1e-15 * x) atomicAdd(a.near_ties, 1ULL);
+          ok = u < x;
+        }
+        for (int i = k; i < e; i++) acc[i] = ok;
+      }
+      __syncwarp();
+      for (int k = lane; k < P; k += 32)
+        if (acc[k])
+        {
+          uint32_t* sp = a.p.spins + (size_t)(base + k) * nw;
+          sp[v >> 5] ^= 1u << (v & 31);
+          a.p.cost[base + k] = __dadd_rn(a.p.cost[base + k], dif[k]);
+          a.p.accepts[base + k] += 1;
+        }
+      __syncwarp();
+    }
+    // add_difference_evaluations + save_lowest (first lowest slice)
+    double bc = 0.0;
+    int bk = INT_MAX;
+    for (int k = lane; k < P; k += 32)
+    {
+      a.p.attempts[base + k] += (unsigned long long)N;
+      const double ck = a.p.cost[base + k];
+      if (bk == INT_MAX || ck < bc)
+      {
+        bc = ck;
+        bk = k;
+      }
+    }
+#pragma unroll
+    for (int sh = 16; sh; sh >>= 1)
+    {
+      const double oc = __shfl_xor_sync(kFull, bc, sh);
+      const int ok = __shfl_xor_sync(kFull, bk, sh);
+      if (ok != INT_MAX && (bk == INT_MAX || oc < bc || (oc == bc && ok < bk)))
+      {
+        bc = oc;
+        bk = ok;
+      }
+    }
+    if (bc < a.low[r])
+    {
+      const uint32_t* src = a.p.spins + (size_t)(base + bk) * nw;
+      for (int q = lane; q < nw; q += 32) a.low_spins[(size_t)r * nw + q] = src[q];
+      __syncwarp();
+      if (lane == 0) a.low[r] = bc;
+    }
+    __syncwarp();
+  }
+}
+
+template <int FL, bool I>
+static cudaError_t qmc_dispatch(const QmcArgs& a, cudaStream_t s)
+{
+  const size_t per_warp = (size_t)a.trotter * 8 + (((size_t)a.trotter * 2 + 7) & ~(size_t)7);
+  const int blocks = (a.restarts + 3) / 4;
+  const size_t smem = 4 * per_warp;
+  if (smem > 48 * 1024)
+  {
+    cudaError_t e = cudaFuncSetAttribute(qmc_kernel<FL, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  if (blocks > 0) qmc_kernel<FL, I><<<blocks, 128, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_qmc(const QmcArgs& a, cudaStream_t s)
+{
+  if (a.restarts <= 0 || a.n_steps <= 0) return cudaSuccess;
+  if (a.trotter < 2 || a.trotter > kQmcMaxTrotter) return cudaErrorInvalidValue;
+  const bool I = a.m.int_mode != 0;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: return I ? qmc_dispatch<F_PARITY, true>(a, s) : qmc_dispatch<F_PARITY, false>(a, s);
+    case F_COUNTER: return I ? qmc_dispatch<F_COUNTER, true>(a, s) : qmc_dispatch<F_COUNTER, false>(a, s);
+    case F_PLAIN_ISING: return I ? qmc_dispatch<F_PLAIN_ISING, true>(a, s) : qmc_dispatch<F_PLAIN_ISING, false>(a, s);
+    default: return I ? qmc_dispatch<F_PLAIN_PUBO, true>(a, s) : qmc_dispatch<F_PLAIN_PUBO, false>(a, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // PT: observations then alternating-parity neighbour swaps of the slot
 // labels (solver/parallel_tempering.h:134-189); one thread per restart.
 // ---------------------------------------------------------------------------

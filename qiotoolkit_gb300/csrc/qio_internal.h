@@ -318,6 +318,28 @@ struct SsmcArgs
 };
 cudaError_t launch_ssmc_walk(const SsmcArgs& a, cudaStream_t s);
 
+// Quantum Monte Carlo sweeps (solver/quantum_monte_carlo.h:128-175 with
+// markov/cluster_walker.h): one warp per restart, slice k of restart r in
+// population slot r * trotter + k.
+static const int kQmcMaxTrotter = 1024;
+struct QmcArgs
+{
+  DevModel m;
+  DevPop p;                  // trotter * restarts slots
+  int restarts, trotter;
+  long long step_base;       // absolute step of the launch's first sweep
+  int n_steps;
+  const double* beta_eff;    // per absolute step: beta / trotter
+  const double* bond_prob;   // per absolute step: 1 - tanh(field * beta / trotter)
+  int replay;
+  uint64_t* rng;             // replay: PCG state per slot
+  uint32_t seed;             // counter mode: slot i draws on counter_key(seed, i)
+  double* low;               // per restart: lowest cost of its slices
+  uint32_t* low_spins;       // per restart: that slice's spins (p.nw words)
+  unsigned long long* near_ties;  // exp() within 1e-15 of its uniform draw
+};
+cudaError_t launch_qmc(const QmcArgs& a, cudaStream_t s);
+
 // PT: label swaps + observables, one thread per restart.
 struct SwapArgs
 {

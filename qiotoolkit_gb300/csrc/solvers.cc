@@ -1349,6 +1349,261 @@ class TabuSearch : public Solver
 };
 
 // ---------------------------------------------------------------------------
+// Quantum Monte Carlo ("quantummontecarlo.qiotoolkit",
+// solver/quantum_monte_carlo.h:22-260): restarts of `trotter_number`
+// imaginary-time slices swept by qmc_kernel, beta and the transverse field
+// linear over the steps.  Walkers are the slices (slot r * trotter + k); a
+// slice's lowest is its restart's.
+// ---------------------------------------------------------------------------
+class QuantumMonteCarlo : public Solver
+{
+ public:
+  int64_t restarts = 1, trotter = 2;
+  double beta_start = 1, beta_stop = 1, field_low = 0, field_high = 5;
+  Population P;
+  DevBuf aux;
+  double* d_low = nullptr;
+  uint32_t* d_lspins = nullptr;
+  unsigned long long* d_ties = nullptr;
+  double* d_beta = nullptr;
+  double* d_bond = nullptr;
+
+  std::string target() const override { return "quantummontecarlo.qiotoolkit"; }
+  int64_t n_walkers() const override { return model->empty() ? 0 : restarts * trotter; }
+  size_t solution_stride() const override { return (size_t)trotter; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    if (model->kind == K_MAXSAT) fail(1, "quantum Monte Carlo runs Ising and PUBO models here");
+    Params p(params);
+    // solver/quantum_monte_carlo.h:185-229
+    beta_stop = p.num("beta_stop", 1.0);
+    if (!(beta_stop > 0)) fail(1, "parameter `beta_stop`: must be greater than 0, found " + json::number(beta_stop));
+    beta_start = p.num("beta_start", beta_stop);
+    if (!(beta_start <= beta_stop))
+      fail(1, "parameter `beta_start`: must be less than or equal to " + json::number(beta_stop) + ", found " +
+                  json::number(beta_start));
+    if (!params.find("beta_stop") && params.find("beta_start")) beta_stop = beta_start;
+    field_low = p.num("transverse_field_low", 0.0);
+    if (!(field_low >= 0))
+      fail(1, "parameter `transverse_field_low`: must be greater than or equal to 0, found " + json::number(field_low));
+    field_high = p.num("transverse_field_high", 5.0);
+    if (!(field_high > field_low))
+      fail(1, "parameter `transverse_field_high`: must be greater than " + json::number(field_low) + ", found " +
+                  json::number(field_high));
+    trotter = p.integer("trotter_number", threads);
+    if (trotter <= 1) fail(1, "parameter `trotter_number`: must be greater than 1");
+    if (trotter > kQmcMaxTrotter) fail(1, "parameter `trotter_number`: at most 1024 slices here");
+    restarts = p.integer("restarts", 1);
+    if (restarts <= 0) fail(1, "parameter `restarts`: must be greater than 0");
+    restarts = std::min<int64_t>(restarts, std::max(threads, 16));
+    output_params.push_back({"beta_stop", json::number(beta_stop)});
+    output_params.push_back({"beta_start", json::number(beta_start)});
+    output_params.push_back({"transverse_field_low", json::number(field_low)});
+    output_params.push_back({"transverse_field_high", json::number(field_high)});
+    output_params.push_back({"trotter_number", std::to_string(trotter)});
+    output_params.push_back({"restarts", std::to_string(restarts)});
+  }
+
+  void init(cudaStream_t st) override
+  {
+    initialized = true;
+    if (model->empty()) return;
+    ensure_device();
+    const int S = (int)(restarts * trotter), R = (int)restarts;
+    const int64_t steps = std::max<int64_t>(1, step_limit);
+    if (!P.buf.ptr)
+    {
+      P.alloc(*model, S, S, false, 1);
+      size_t off = 0;
+      auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
+      const size_t o_l = take((size_t)R * 8), o_ls = take((size_t)R * P.pop.nw * 4), o_t = take(8),
+                   o_b = take((size_t)steps * 8), o_p = take((size_t)steps * 8);
+      aux = DevBuf(off);
+      char* b = (char*)aux.ptr;
+      d_low = (double*)(b + o_l);
+      d_lspins = (uint32_t*)(b + o_ls);
+      d_ties = (unsigned long long*)(b + o_t);
+      d_beta = (double*)(b + o_b);
+      d_bond = (double*)(b + o_p);
+    }
+    device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
+    // per step: beta / P and 1 - tanh(field * beta / P), both schedules
+    // linear with stop max(1, step_limit - 1)
+    Schedule bs, fs;
+    bs.type = fs.type = 0;
+    bs.initial = beta_start;
+    bs.final_ = beta_stop;
+    fs.initial = field_low;
+    fs.final_ = field_high;
+    bs.has_stop = fs.has_stop = true;
+    bs.stop_ = fs.stop_ = (double)std::max(1, (int)step_limit - 1);
+    std::vector<double> be(steps), bp(steps);
+    for (int64_t s = 0; s < steps; s++)
+    {
+      const double b = bs.get_value((double)s), g = fs.get_value((double)s);
+      be[s] = b / (double)trotter;
+      bp[s] = 1 - std::tanh(g * b / (double)trotter);
+    }
+    cuda_check(cudaMemcpyAsync(d_beta, be.data(), steps * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(d_bond, bp.data(), steps * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemsetAsync(d_ties, 0, 8, st), "memset");
+    // rngs_[i] = rng_->fork() for the R * P slices in order (:52-58)
+    std::vector<uint64_t> rs(S);
+    Pcg master(seed);
+    for (int i = 0; i < S; i++) rs[i] = Pcg(master.next()).state;
+    cuda_check(cudaMemcpyAsync(P.rng, rs.data(), (size_t)S * 8, cudaMemcpyHostToDevice, st), "H2D rng");
+    InitArgs a{};
+    a.m = model->device_view(false);
+    a.p = P.pop;
+    a.n_walkers = S;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    a.skip_terms = 1;
+    cuda_check(launch_init(a, st), "init kernel");
+    launches++;
+    used_kernel = 6;
+    // save_lowest of every restart on its initial slices
+    std::vector<double> c(S), low(R);
+    cuda_check(cudaMemcpyAsync(c.data(), P.pop.cost, (size_t)S * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    for (int r = 0; r < R; r++)
+    {
+      int b = 0;
+      for (int k = 1; k < trotter; k++)
+        if (c[(size_t)r * trotter + k] < c[(size_t)r * trotter + b]) b = k;
+      low[r] = c[(size_t)r * trotter + b];
+      cuda_check(cudaMemcpyAsync(d_lspins + (size_t)r * P.pop.nw, P.pop.spins + ((size_t)r * trotter + b) * P.pop.nw,
+                                 P.pop.nw * 4, cudaMemcpyDeviceToDevice, st),
+                 "D2D");
+    }
+    cuda_check(cudaMemcpyAsync(d_low, low.data(), (size_t)R * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaStreamSynchronize(st), "sync");
+    step_pos = 0;
+  }
+
+  QmcArgs args() const
+  {
+    QmcArgs a{};
+    a.m = model->device_view(false);
+    a.p = P.pop;
+    a.restarts = (int)restarts;
+    a.trotter = (int)trotter;
+    a.beta_eff = d_beta;
+    a.bond_prob = d_bond;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng;
+    a.seed = seed;
+    a.low = d_low;
+    a.low_spins = d_lspins;
+    a.near_ties = d_ties;
+    return a;
+  }
+
+  void launch(cudaStream_t st, int64_t base, int64_t n)
+  {
+    QmcArgs a = args();
+    a.step_base = base;
+    a.n_steps = (int)n;
+    prof_begin(st);
+    cuda_check(launch_qmc(a, st), "qmc kernel");
+    prof_end(st);
+    launches++;
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    EventTimer total(st);
+    const int64_t chunk = (has_cost_limit || has_time_limit) ? std::max<int64_t>(1, step_limit / 100) : step_limit;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> low(restarts);
+    int64_t s = step_pos;
+    while (s < step_limit)
+    {
+      const int64_t n = std::min(chunk, step_limit - s);
+      launch(st, s, n);
+      s += n;
+      if (has_cost_limit)
+      {
+        cuda_check(cudaMemcpyAsync(low.data(), d_low, restarts * 8, cudaMemcpyDeviceToHost, st), "D2H");
+        cuda_check(cudaStreamSynchronize(st), "sync");
+        if (*std::min_element(low.begin(), low.end()) <= cost_limit) break;
+      }
+      if (has_time_limit)
+      {
+        cuda_check(cudaStreamSynchronize(st), "sync");
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= time_limit) break;
+      }
+    }
+    step_pos = s;
+    last_step = s;
+    run_ms = total.stop();
+    sweep_ms = profile ? prof_total_ms() : run_ms;
+    cuda_check(cudaMemcpy(&near_ties, d_ties, 8, cudaMemcpyDeviceToHost), "D2H");
+    check_device_error(st);
+  }
+
+  bool advance(cudaStream_t st, int64_t n) override
+  {
+    if (!initialized) fail(1, "init() must be called before advance()");
+    ran = true;
+    if (model->empty() || step_limit <= 0)
+    {
+      last_step = step_limit;
+      return true;
+    }
+    const int64_t todo = std::min(n, step_limit - step_pos);
+    if (todo > 0) launch(st, step_pos, todo);
+    step_pos += todo;
+    last_step = step_pos;
+    return step_pos >= step_limit;
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
+             std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
+             std::vector<uint8_t>* states) override
+  {
+    const int S = (int)n_walkers(), R = (int)restarts;
+    cost.resize(S);
+    lowest.resize(S);
+    att.resize(S);
+    acc.resize(S);
+    if (!S) return;
+    std::vector<double> low(R);
+    cuda_check(cudaMemcpy(cost.data(), P.pop.cost, (size_t)S * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(low.data(), d_low, (size_t)R * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(att.data(), P.pop.attempts, (size_t)S * 8, cudaMemcpyDeviceToHost), "D2H");
+    cuda_check(cudaMemcpy(acc.data(), P.pop.accepts, (size_t)S * 8, cudaMemcpyDeviceToHost), "D2H");
+    for (int i = 0; i < S; i++) lowest[i] = low[i / trotter];
+    const int nw = P.pop.nw;
+    if (lowest_states)
+    {
+      std::vector<uint32_t> w((size_t)R * nw);
+      cuda_check(cudaMemcpy(w.data(), d_lspins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      std::vector<uint8_t> per;
+      Population::unpack(w, nw, model->N, R, per);
+      lowest_states->resize((size_t)S * model->N);
+      for (int i = 0; i < S; i++)
+        std::copy(per.begin() + (size_t)(i / trotter) * model->N, per.begin() + (size_t)(i / trotter + 1) * model->N,
+                  lowest_states->begin() + (size_t)i * model->N);
+    }
+    if (states)
+    {
+      std::vector<uint32_t> w((size_t)S * nw);
+      cuda_check(cudaMemcpy(w.data(), P.pop.spins, w.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+      Population::unpack(w, nw, model->N, S, *states);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Parameter-free solvers with the linear search ("simulatedannealing-
 // parameterfree.qiotoolkit", "paralleltempering-parameterfree.qiotoolkit":
 // solver/parameter_free_solver.h:9-257 with solver/parameter_free_linear_
@@ -1737,6 +1992,13 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
   if (target == "simulatedannealing-parameterfree.qiotoolkit")
   {
     std::unique_ptr<SAParameterFree> s(new SAParameterFree());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
+  if (target == "quantummontecarlo.qiotoolkit")
+  {
+    std::unique_ptr<QuantumMonteCarlo> s(new QuantumMonteCarlo());
     s->model = m;
     s->configure(doc);
     return std::unique_ptr<Solver>(s.release());
@@ -2204,8 +2466,9 @@ std::string Solver::result_json()
   std::string sol = "{\"version\":\"1.0\"";
   if (!low.empty())
   {
-    std::vector<size_t> idx(low.size());
-    std::iota(idx.begin(), idx.end(), 0);
+    const size_t stride = solution_stride();
+    std::vector<size_t> idx;
+    for (size_t i = 0; i < low.size(); i += stride) idx.push_back(i);
     std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return low[a] < low[b]; });
     // the solver's lowest first (ModelSolver::populate_solutions keeps it
     // as the result's cost and configuration)

@@ -162,7 +162,8 @@ def test_reference_solver_pins_on_gpu(golden):
         if case["solver"] == "ssmc":
             p = {"seed": p["seed"], "sweeps": p["sweeps"], "target_population": 8, "threads": 8}
         target = {"sa": SA, "pt": PT, "pa": PA, "tabu": "tabu.qiotoolkit",
-                  "ssmc": "substochasticmontecarlo.cpu"}[case["solver"]]
+                  "ssmc": "substochasticmontecarlo.cpu",
+                  "qmc": "quantummontecarlo.qiotoolkit"}[case["solver"]]
         res = q.run_json(doc, {"params": p}, target)
         cost = res["solutions"]["cost"]
         exp = case["expected_cost"]
