@@ -984,9 +984,21 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
         if (!(sum < 10E-12))
         {
           const double u = qmc_draw(a, base + k, c + 1);
-          const double x = exp(__dmul_rn(-be, sum));
-          if (fabs(u - x) <= 1e-15 * x) atomicAdd(a.near_ties, 1ULL);
-          ok = u < x;
+          const double x = __dmul_rn(-be, sum);
+          // FP32 screen: expf's error plus x's rounding to float stay far
+          // below tol; the FP64 exp decides only near the draw
+          const float xf = (float)x, ef = expf(xf);
+          const double tol = (double)ef * (double)(fabsf(xf) + 2.0f) * 0x1p-20 + 1e-300;
+          if ((double)u < (double)ef - tol)
+            ok = 1;
+          else if ((double)u > (double)ef + tol)
+            ok = 0;
+          else
+          {
+            const double e = exp(x);
+            if (fabs(u - e) <= 1e-15 * e) atomicAdd(a.near_ties, 1ULL);
+            ok = u < e;
+          }
         }
         for (int i = k; i < e; i++) acc[i] = ok;
       }
