@@ -1475,6 +1475,7 @@ static Result run_ssmc(const Model& m, const orc_params& p)
   const size_t T = (size_t)std::max(1, p.pa_threads);
   const int64_t spw = std::max<int64_t>(1, p.sweeps_per_replica);
   const bool counter = p.rng_mode == ORC_RNG_COUNTER;
+  set_threads(p.threads);
   PcgRng master(p.seed);
   std::vector<std::unique_ptr<Rng>> rngs(T);
   for (size_t t = 0; t < T; t++) rngs[t] = master.fork();
@@ -1500,7 +1501,8 @@ static Result run_ssmc(const Model& m, const orc_params& p)
   for (; step < p.step_limit; step++)
   {
     const double p_step = alpha.get_value((double)step) / (double)spw;
-    // make_walker_steps
+    // make_walker_steps: each emulated thread owns its block and stream
+#pragma omp parallel for schedule(dynamic, 1)
     for (size_t t = 0; t < T; t++)
     {
       size_t b, e;
@@ -1644,16 +1646,19 @@ static Result run_qmc(const Model& m, const orc_params& p)
   Lowest best;
   best.update(low[0], low_state[0]);
   const int64_t n = m.N;
-  std::vector<double> diff(P);
-  std::vector<char> bond(P), acc(P);
+  set_threads(p.threads);
   int64_t step = 0;
   for (; step < p.step_limit; step++)
   {
     const double b = beta.get_value((double)step), g = field.get_value((double)step);
     const double beta_eff = b / (double)P;
     const double bond_prob = 1 - std::tanh(g * b / (double)P);
+    // restarts are independent within a step (own slices and streams)
+#pragma omp parallel for schedule(dynamic, 1)
     for (size_t rr = 0; rr < R; rr++)
     {
+      std::vector<double> diff(P);
+      std::vector<char> bond(P), acc(P);
       Walker* w = &sl[rr * P];
       for (int64_t v = 0; v < n; v++)
       {
