@@ -50,7 +50,8 @@ class Params(C.Structure):
                 ("full_maxsat_sweep", C.c_int), ("resampling", C.c_int),
                 ("master_skip", C.c_int64), ("use_master_state", C.c_int),
                 ("master_state", C.c_uint64), ("tabu_tenure", C.c_int64),
-                ("sched2", Schedule), ("trotter_number", C.c_int64)]
+                ("sched2", Schedule), ("tabu_tenures", C.POINTER(C.c_int64)),
+                ("n_tabu_tenures", C.c_int64), ("trotter_number", C.c_int64)]
 
 
 def build(force: bool = False) -> str:
@@ -308,7 +309,7 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         constant_population=False, exp_repopulation=False, pa_threads=1,
         rng_mode="replay", threads=1, number_of_solutions=1, cost_limit=None,
         full_maxsat_sweep=False, resampling="reference", master_skip=0, master_state=None,
-        tabu_tenure=0, sched2=None, steps_per_walker=1, trotter_number=2):
+        tabu_tenure=0, sched2=None, steps_per_walker=1, trotter_number=2, tabu_tenures=None):
     """sched / sched2 are (kind, initial, final) or (kind, initial, final,
     start, stop); SSMC takes alpha from sched and beta from sched2, the
     target population from `population`, its streams from `pa_threads`."""
@@ -342,10 +343,15 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
     p.use_master_state = 0 if master_state is None else 1
     p.master_state = 0 if master_state is None else int(master_state)
     p.tabu_tenure = int(tabu_tenure)
+    keep_ten = None
+    if tabu_tenures is not None:
+        keep_ten = np.ascontiguousarray(tabu_tenures, np.int64)
+        p.tabu_tenures = _p(keep_ten, C.c_int64)
+        p.n_tabu_tenures = len(keep_ten)
     p.trotter_number = int(trotter_number)
     err = C.create_string_buffer(512)
     h = lib().orc_run(model.h, C.byref(p), err, 512)
-    del keep
+    del keep, keep_ten
     if not h:
         raise ValueError(err.value.decode())
     return Result(h)
@@ -505,6 +511,85 @@ def sa_parameter_free(model: Model, kind, terms, *, seed, min_num_restarts, samp
             break
     return {"trace": trace, "best": best, "best_state": best_state, "params": best_params,
             "betas": (b0, b1)}
+
+
+def tabu_tenures(n_tenures, n_vars, denominator=4, max_optimal=20):
+    """TabuParameterFree::determine_all_tenures_ (solver/tabu_parameter_free.h:
+    86-124): the optimal tenure min(20, N / 4), its half when above 10, then
+    tenures stepping by max((N - optimal) / (remaining * 4), 1) below N,
+    repeated until n_tenures values."""
+    opt = min(max_optimal, n_vars // denominator)
+    out = []
+    todo = n_tenures
+    while todo > 0:
+        out.append(opt)
+        todo -= 1
+        if todo > 0 and opt > max_optimal // 2:
+            out.append(opt // 2)
+            todo -= 1
+        if todo > 0:
+            inc = max((n_vars - opt) // (todo * denominator), 1)
+            t = opt + inc
+            while todo > 0 and t < n_vars:
+                out.append(t)
+                todo -= 1
+                t += inc
+    return out
+
+
+def tabu_parameter_free(model: Model, *, seed, min_num_restarts, samples=(10, 20, 30, 50),
+                        change=1.5, nonimprovement_limit=8, max_runs=400, threads=4):
+    """ParameterFreeLinearSearchSolver<TabuParameterFree> restated
+    (solver/parameter_free_solver.h:65-151, strategy/linear_search.cc,
+    solver/tabu_parameter_free.h): repeated oracle tabu runs with the
+    tenure list, restarts forking from one master stream that configure()
+    already drew once from (replica_rng_ = rng_->fork()).  Returns the trace
+    [(sweeps, restarts, lowest)], the best cost and state and its run's
+    (sweeps, restarts).  Stops on the non-improvement rule."""
+    n_vars = model.n_vars
+    points = list(samples)
+    objs = [float(np.finfo(np.float64).max)] * len(points)
+    init_min = points[0]
+    cur = -1
+    skip = 1
+    best = best_state = best_params = None
+    best_exec = 0.0
+    stable = 0
+    trace = []
+    for _ in range(max_runs):
+        cur += 1
+        if cur >= len(points):
+            cur = 0
+            lowest = objs.index(min(objs))
+            if lowest == 0:
+                if points[0] > init_min:
+                    points = [int(p / change) for p in points]
+            elif lowest == len(points) - 1:
+                points = [int(p * change) for p in points]
+            objs = [float(np.finfo(np.float64).max)] * len(points)
+        sweeps, back = points[cur], points[-1]
+        sl = max(sweeps, 2)
+        r = min_num_restarts * back // sweeps
+        res = run(model, "tabu", seed=seed, step_limit=sl, restarts=r, threads=threads,
+                  master_skip=skip, tabu_tenures=tabu_tenures(r, n_vars))
+        skip += r
+        obj = float(res.best_cost)
+        objs[cur] = obj
+        trace.append((sl, r, obj))
+        exec_cost = float(sl) * float(r)
+        done = False
+        if best is not None and abs(best - obj) < 10E-12:
+            stable += 1
+            if exec_cost < best_exec:
+                best, best_state, best_exec, best_params = obj, res.best_state.copy(), exec_cost, (sl, r)
+        if stable >= nonimprovement_limit:
+            done = True
+        if best is None or best - obj > 10E-12:
+            stable = 0
+            best, best_state, best_exec, best_params = obj, res.best_state.copy(), exec_cost, (sl, r)
+        if done:
+            break
+    return {"trace": trace, "best": best, "best_state": best_state, "params": best_params}
 
 
 def _pf_betas(b0, b1, num):

@@ -1143,6 +1143,7 @@ static Result run_tabu(const Model& m, const orc_params& p)
   }
   size_t R = (size_t)p.restarts;
   PcgRng master(p.seed);
+  for (int64_t k = 0; k < p.master_skip; k++) master.uint32();
   std::vector<std::unique_ptr<Rng>> rngs(R);
   for (size_t i = 0; i < R; i++) rngs[i] = master.fork();
   std::vector<TabuWalker> reps(R);
@@ -1156,7 +1157,8 @@ static Result run_tabu(const Model& m, const orc_params& p)
     w.rng = rngs[i].get();
     w.counter_mode = p.rng_mode == ORC_RNG_COUNTER;
     w.key = counter_key(p.seed, i);
-    w.tenure = (uint64_t)p.tabu_tenure;
+    // Tabu::make_step sets tabu_tenures_[i] when the list is given
+    w.tenure = (uint64_t)(p.tabu_tenures && (int64_t)i < p.n_tabu_tenures ? p.tabu_tenures[i] : p.tabu_tenure);
     w.tabu_init();
   }
   for (size_t i = 0; i < R; i++) wp[i] = &reps[i];

@@ -78,6 +78,9 @@ typedef struct orc_params {
                                  per walker, `population` the target
                                  population, `pa_threads` the emulated
                                  OpenMP thread count (streams) */
+  const int64_t* tabu_tenures;/* tabu: per-restart tenures (parameter-free
+                                 runs), or NULL for tabu_tenure everywhere */
+  int64_t n_tabu_tenures;
   int64_t trotter_number;     /* QMC: slices per restart; `sched` holds beta
                                  (linear), `sched2` the transverse field
                                  (linear), both stretched over the steps */

@@ -20,7 +20,8 @@ KINDS = {"ising": 0, "ising_plain": 1, "pubo": 2, "pubo_plain": 3, "maxsat": 4}
 TARGETS = ("simulatedannealing.qiotoolkit", "paralleltempering.qiotoolkit",
            "populationannealing.cpu", "simulatedannealing-parameterfree.qiotoolkit",
            "paralleltempering-parameterfree.qiotoolkit", "tabu.qiotoolkit",
-           "substochasticmontecarlo.cpu", "quantummontecarlo.qiotoolkit")
+           "substochasticmontecarlo.cpu", "quantummontecarlo.qiotoolkit",
+           "tabu-parameterfree.qiotoolkit")
 
 
 def _ptr(a, ct):

@@ -641,6 +641,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
   TabuState S = a.st[w];
   double cost = a.p.cost[w], low = a.p.lowest[w];
   unsigned long long att = 0, acc = 0;
+  const unsigned long long tenure = a.tenures ? a.tenures[w] : a.tenure;
   if (!S.ready)
   {
     for (int v = lane; v < N; v += 32) df[v] = lane_diff<FL, INT>(m, sp, v);
@@ -748,7 +749,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
           cost = __dadd_rn(cost, di);
           low = cost;
           warp_copy(ls, sp, nw, lane);
-          if (lane == 0) tb[i] = it + a.tenure;
+          if (lane == 0) tb[i] = it + tenure;
           tabu_refresh<FL, INT>(m, sp, df, i, lane);
           // local_search_init: a hill climber on a copy, its cost computed afresh
           warp_copy(hs, sp, nw, lane);
@@ -805,7 +806,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
           low = cost;
           warp_copy(ls, sp, nw, lane);
         }
-        if (lane == 0) tb[bv] = it + a.tenure;
+        if (lane == 0) tb[bv] = it + tenure;
         tabu_refresh<FL, INT>(m, sp, df, bv, lane);
       }
     }

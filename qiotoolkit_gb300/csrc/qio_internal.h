@@ -290,6 +290,7 @@ struct TabuArgs
   int n_walkers;
   int n_steps;
   unsigned long long tenure;
+  const unsigned long long* tenures;  // per walker (parameter-free runs), or null
   unsigned long long* tabu;  // n_walkers * n_vars
   uint32_t* hc;              // n_walkers * p.nw
   uint32_t* hc_low;          // n_walkers * p.nw

@@ -1188,9 +1188,24 @@ class TabuSearch : public Solver
  public:
   int64_t restarts = 1;
   uint64_t tenure = 0;
+  std::vector<uint64_t> tenure_list;  // per restart (parameter-free runs)
+  Pcg* ext_master = nullptr;          // repeated runs: the restarts fork from this stream
   Population P;
   DevBuf aux;
   TabuArgs ta{};
+
+  // another run of the parameter-free search: its sweeps, restarts, tenures
+  void retarget(int64_t sweeps, int64_t r, const std::vector<uint64_t>& tenures)
+  {
+    step_limit = sweeps;
+    restarts = r;
+    tenure_list = tenures;
+    P = Population();
+    aux = DevBuf();
+    initialized = ran = false;
+    step_pos = 0;
+    launches = 0;
+  }
 
   std::string target() const override { return "tabu.qiotoolkit"; }
 
@@ -1223,15 +1238,21 @@ class TabuSearch : public Solver
     auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
     const size_t o_t = take((size_t)R * N * 8), o_h = take((size_t)R * nw * 4), o_l = take((size_t)R * nw * 4),
                  o_s = take((size_t)R * sizeof(TabuState)), o_d = take((size_t)R * N * 8),
-                 o_hd = take((size_t)R * N * 8);
+                 o_hd = take((size_t)R * N * 8), o_tn = take((size_t)R * 8);
     if (!aux.ptr) aux = DevBuf(off);
     char* b = (char*)aux.ptr;
     cuda_check(cudaMemsetAsync(aux.ptr, 0, off, st), "memset");
     device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
     // rngs_[i] = rng_->fork() in index order (solver/tabu.h:56-60)
     std::vector<uint64_t> rs(R);
-    Pcg master(seed);
+    Pcg own(seed);
+    Pcg& master = ext_master ? *ext_master : own;
     for (int i = 0; i < R; i++) rs[i] = Pcg(master.next()).state;
+    if (!tenure_list.empty())
+    {
+      if ((int64_t)tenure_list.size() < R) fail(6, "tabu: fewer tenures than restarts");
+      cuda_check(cudaMemcpyAsync(b + o_tn, tenure_list.data(), (size_t)R * 8, cudaMemcpyHostToDevice, st), "H2D");
+    }
     cuda_check(cudaMemcpyAsync(P.rng, rs.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D rng");
     InitArgs a{};
     a.m = model->device_view(false);
@@ -1255,6 +1276,7 @@ class TabuSearch : public Solver
     ta.hc = (uint32_t*)(b + o_h);
     ta.hc_low = (uint32_t*)(b + o_l);
     ta.st = (TabuState*)(b + o_s);
+    ta.tenures = tenure_list.empty() ? nullptr : (const unsigned long long*)(b + o_tn);
     ta.diff = (double*)(b + o_d);
     ta.hdiff = (double*)(b + o_hd);
     step_pos = 0;
@@ -1652,7 +1674,7 @@ class ParameterFreeSearch : public Solver
   virtual void render_params(int64_t sweeps, int64_t r) = 0;
 
   // the parameters shared by both adapters, the time limit, the estimates
-  void configure_search()
+  void configure_search(bool estimates = true)
   {
     if (!replay) fail(1, "parameter-free solvers run with \"rng_mode\": \"replay\"");
     if (number_of_solutions != 1) fail(1, "parameter-free solvers return one solution: `number_of_solutions` must be 1");
@@ -1684,7 +1706,7 @@ class ParameterFreeSearch : public Solver
       has_time_limit = true;  // a time limit must be set (parameter_free_solver.h:56-61)
       time_limit = 5.0;
     }
-    if (!model->empty())
+    if (!model->empty() && estimates)
     {
       const double mx = estimate_max_cost_diff(*model), mn = estimate_min_cost_diff(*model);
       if (mx <= 0) fail(1, "max cost difference should be > 0, found :" + json::number(mx));
@@ -1903,6 +1925,92 @@ class SAParameterFree : public ParameterFreeSearch
   }
 };
 
+// TabuParameterFree (solver/tabu_parameter_free.h): restarts as the SA
+// adapter, each restart with its own tenure (determine_all_tenures_, 86-124);
+// configure() already forked replica_rng_ from the master, so the runs'
+// restarts fork from the master's second draw on.
+class TabuParameterFree : public ParameterFreeSearch
+{
+ public:
+  std::unique_ptr<TabuSearch> w;
+  int64_t min_restarts = 1;
+
+  std::string target() const override { return "tabu-parameterfree.qiotoolkit"; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common(*this, doc);
+    if (model->kind == K_MAXSAT) fail(1, "tabu search runs Ising and PUBO models here");
+    Params p(params);
+    min_restarts = p.integer("min_num_restarts", threads);
+    if (min_restarts <= 0) fail(1, "parameter `min_num_restarts`: must be greater than 0");
+    configure_search(false);
+    w.reset(new TabuSearch());
+    w->model = model;
+    w->configure(doc);
+    render_params(samples[0], min_restarts);
+  }
+
+  void init(cudaStream_t st) override
+  {
+    ParameterFreeSearch::init(st);
+    master.next();  // replica_rng_ = rng_->fork()
+  }
+
+  void render_params(int64_t sweeps, int64_t r) override
+  {
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"restarts", std::to_string(r)});
+    output_params.push_back({"sweeps", std::to_string(sweeps)});
+  }
+
+  static std::vector<uint64_t> tenures(size_t n, size_t nv)
+  {
+    const size_t den = 4, cap = 20;
+    const size_t opt = std::min(cap, nv / den);
+    std::vector<uint64_t> out;
+    size_t todo = n;
+    while (todo > 0)
+    {
+      out.push_back(opt);
+      todo--;
+      if (todo > 0 && opt > cap / 2)
+      {
+        out.push_back(opt / 2);
+        todo--;
+      }
+      if (todo > 0)
+      {
+        const size_t inc = std::max((nv - opt) / (todo * den), (size_t)1);
+        size_t t = opt + inc;
+        while (todo > 0 && t < nv)
+        {
+          out.push_back(t);
+          todo--;
+          t += inc;
+        }
+      }
+    }
+    return out;
+  }
+
+  // TabuParameterFree::update_parameters, solver/tabu_parameter_free.h:48-60
+  void one_run(int sweeps, int back, cudaStream_t st, int64_t& sl, int64_t& r, double& obj,
+               std::vector<uint8_t>& state, double& exec) override
+  {
+    sl = std::max(sweeps, 2);
+    r = (int64_t)((int)min_restarts * back / sweeps);
+    if (r <= 0) fail(1, "parameter-free search reached a run with no restarts");
+    w->retarget(sl, r, tenures((size_t)r, (size_t)model->N));
+    w->ext_master = &master;
+    w->init(st);
+    w->run(st);
+    take_lowest(*w, obj, state);
+    exec = (double)sl * (double)r;
+  }
+};
+
 // PTParameterFree (solver/pt_parameter_free.h): min_num_betas inverse
 // temperatures from geometric ladders of 4, 9, 14, ... values between the
 // two ends (determine_all_betas_, 155-173), the run length from the search
@@ -1992,6 +2100,13 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
   if (target == "simulatedannealing-parameterfree.qiotoolkit")
   {
     std::unique_ptr<SAParameterFree> s(new SAParameterFree());
+    s->model = m;
+    s->configure(doc);
+    return std::unique_ptr<Solver>(s.release());
+  }
+  if (target == "tabu-parameterfree.qiotoolkit")
+  {
+    std::unique_ptr<TabuParameterFree> s(new TabuParameterFree());
     s->model = m;
     s->configure(doc);
     return std::unique_ptr<Solver>(s.release());

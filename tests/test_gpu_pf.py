@@ -74,3 +74,34 @@ def test_pt_parameter_free_matches_oracle(name):
     rep = s.replicas()
     np.testing.assert_array_equal(rep["lowest"], [ref["best"]])
     np.testing.assert_array_equal(rep["lowest_states"][0], ref["best_state"])
+
+
+TABU_CASES = {
+    "er_ising": ("ising", lambda: I.er_ising(60, 150, seed=1), 3),
+    "cubic": ("ising", lambda: I.cubic_pm_j(4, seed=2), 3),
+    "pubo": ("pubo", lambda: I.random_pubo(50, 150, seed=3), 3),
+}
+
+
+@pytest.mark.parametrize("name", list(TABU_CASES))
+def test_tabu_parameter_free_matches_oracle(name):
+    """ParameterFreeLinearSearchSolver<TabuParameterFree>: the same runs
+    (sweeps, restarts, per-restart tenures, lowest costs), best state and
+    parameters as the oracle's restatement."""
+    kind, gen, seed = TABU_CASES[name]
+    off, ids, coef = gen()
+    g = q.Model(kind, off=off, ids=ids, coef=coef)
+    o = O.Model(kind, off=off, ids=ids, coef=coef)
+    s = q.Solver(g, "tabu-parameterfree.qiotoolkit",
+                 {"params": {"seed": seed, "min_num_restarts": 8, "timeout": 120}}).init().run()
+    res = s.result()
+    pf = res["benchmark"]["parameter_free"]
+    assert pf["stop"] == "no improvement"
+    ref = O.tabu_parameter_free(o, seed=seed, min_num_restarts=8)
+    assert [(r["sweeps"], r["restarts"], r["lowest"]) for r in pf["runs"]] == \
+        [(sl, r, obj) for sl, r, obj in ref["trace"]]
+    sol = res["solutions"]
+    assert (sol["parameters"]["sweeps"], sol["parameters"]["restarts"]) == ref["params"]
+    c, st = s.best()
+    assert c == ref["best"]
+    np.testing.assert_array_equal(st, ref["best_state"])

@@ -114,7 +114,7 @@ def _params(p):
     return dict(seed=p["seed"], step_limit=p["sweeps"])
 
 
-@pytest.mark.parametrize("idx", range(33))
+@pytest.mark.parametrize("idx", range(39))
 def test_solver_end_results(idx, golden):
     case = golden("solver_pins.json")["cases"][idx]
     p = case["params"]
@@ -131,6 +131,15 @@ def test_solver_end_results(idx, golden):
         # (solver/substochastic_monte_carlo.h:157-199)
         r = O.run(m, "ssmc", seed=p["seed"], step_limit=p["sweeps"], population=8, pa_threads=8,
                   sched=("linear", 1.0, 0.0), sched2=("linear", 0.0, 5.0))
+    elif case["solver"] == "tabu_pf":
+        # pf5s.json sets only a 5 s timeout: seed 0 and 8 restarts here; the
+        # restatement stops on the non-improvement rule
+        res = O.tabu_parameter_free(m, seed=0, min_num_restarts=8)
+
+        class _R:
+            best_cost = res["best"]
+            best_state = res["best_state"]
+        r = _R()
     elif case["solver"] == "qmc":
         # params_qmc.json: beta_start defaults to beta_stop; the transverse
         # field runs linear low -> high (solver/quantum_monte_carlo.h:185-222)

@@ -136,3 +136,22 @@ def test_oracle_matches_restatement(kind, gen, tenure):
         assert (t.att, t.acc) == (r.attempts[w], r.accepts[w])
         np.testing.assert_array_equal(t.s, r.states[w])
         np.testing.assert_array_equal(t.low_s, r.lowest_states[w])
+
+
+def test_parameter_free_tenures_like_the_reference():
+    """determine_all_tenures_ (solver/tabu_parameter_free.h:86-124) as the
+    oracle restates it: the optimal min(20, N/4), its half above 10, then
+    steps below N."""
+    assert O.tabu_tenures(10, 1000) == [20, 10, 50, 80, 110, 140, 170, 200, 230, 260]
+    assert O.tabu_tenures(7, 30) == [7, 8, 9, 10, 11, 12, 13]
+    assert O.tabu_tenures(5, 3) == [0, 1, 2, 0, 1]
+
+
+def test_parameter_free_configuration_errors():
+    m = q.Model("ising", [(1.0, [0, 1]), (-2.0, [1, 2])])
+    pf = "tabu-parameterfree.qiotoolkit"
+    with pytest.raises(q.QioError, match="min_num_restarts"):
+        q.Solver(m, pf, {"params": {"seed": 1, "min_num_restarts": 0}})
+    with pytest.raises(q.QioError, match="rng_mode"):
+        q.Solver(m, pf, {"params": {"seed": 1, "rng_mode": "counter"}})
+    q.Solver(m, pf, {"params": {"seed": 1}}).close()
