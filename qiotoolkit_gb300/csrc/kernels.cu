@@ -931,7 +931,10 @@ cudaError_t launch_ssmc_walk(const SsmcArgs& a, cudaStream_t s)
 // differences, bonds and acceptances sit in shared memory.  After each sweep
 // the restart keeps the first lowest-cost slice if it beats its lowest.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double qmc_draw(const QmcArgs& a, int slot, unsigned long long ctr)
+// the 64 random bits of one uniform(): replay, the stream's next two
+// outputs X = d0 + d1 2^32 (canonical(d0, d1) = fl(X) 2^-64, clamped below
+// 1); counter, one counter draw (uniform = (draw >> 11) 2^-53)
+__device__ __forceinline__ unsigned long long qmc_bits(const QmcArgs& a, int slot, unsigned long long ctr)
 {
   if (a.replay)
   {
@@ -940,9 +943,14 @@ __device__ __forceinline__ double qmc_draw(const QmcArgs& a, int slot, unsigned 
     s = s * kMult + kInc;
     const uint32_t d1 = pcg_out(s);
     a.rng[slot] = s * kMult + kInc;
-    return canonical(d0, d1);
+    return ((unsigned long long)d1 << 32) | d0;
   }
-  return (double)(counter_draw(counter_key(a.seed, (uint64_t)slot), ctr) >> 11) * 0x1p-53;
+  return counter_draw(counter_key(a.seed, (uint64_t)slot), ctr);
+}
+__device__ __forceinline__ double qmc_uniform(const QmcArgs& a, unsigned long long x)
+{
+  if (a.replay) return canonical((uint32_t)x, (uint32_t)(x >> 32));
+  return (double)(x >> 11) * 0x1p-53;
 }
 
 template <int FL, bool INT>
@@ -962,7 +970,10 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
   for (int st = 0; st < a.n_steps; st++)
   {
     const long long S = a.step_base + st;
-    const double be = a.beta_eff[S], bp = a.bond_prob[S];
+    const double be = a.beta_eff[S];
+    const float bef = (float)be;
+    const unsigned long long blim = a.bond_lim[S];
+    const bool ball = a.bond_all[S] != 0;
     for (int v = 0; v < N; v++)
     {
       const unsigned long long c = 2ull * ((unsigned long long)S * (unsigned long long)N + (unsigned long long)v);
@@ -971,7 +982,11 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
         const uint32_t* sp = a.p.spins + (size_t)(base + k) * nw;
         dif[k] = lane_diff<FL, INT>(a.m, sp, v);
         uint8_t b = 0;
-        if (k > 0 && spin_of(sp - nw, v) == spin_of(sp, v)) b = qmc_draw(a, base + k, c) < bp;
+        if (k > 0 && spin_of(sp - nw, v) == spin_of(sp, v))
+        {
+          const unsigned long long x = qmc_bits(a, base + k, c);
+          b = a.replay ? (ball || x < blim) : ((x >> 11) < blim);
+        }
         bond[k] = b;
       }
       __syncwarp();
@@ -984,19 +999,21 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
         uint8_t ok = 1;
         if (!(sum < 10E-12))
         {
-          const double u = qmc_draw(a, base + k, c + 1);
-          const double x = __dmul_rn(-be, sum);
-          // FP32 screen: expf's error plus x's rounding to float stay far
-          // below tol; the FP64 exp decides only near the draw
-          const float xf = (float)x, ef = expf(xf);
-          const double tol = (double)ef * (double)(fabsf(xf) + 2.0f) * 0x1p-20 + 1e-300;
-          if ((double)u < (double)ef - tol)
+          const unsigned long long ub = qmc_bits(a, base + k, c + 1);
+          // FP32 screen: the draw's top 24 bits are within 2^-23 of it;
+          // x = -be sum rounded through float and expf's error stay below
+          // ef (|xf| + 2) 2^-20; the FP64 exp decides only near the draw
+          const float uf = (float)(uint32_t)(ub >> 40) * 0x1p-24f;
+          const float xf = -bef * (float)sum, ef = expf(xf);
+          const float te = ef * (fabsf(xf) + 2.0f) * 0x1p-20f;
+          if (uf + 0x1p-23f < ef - te)
             ok = 1;
-          else if ((double)u > (double)ef + tol)
+          else if (uf - 0x1p-23f > ef + te)
             ok = 0;
           else
           {
-            const double e = exp(x);
+            const double u = qmc_uniform(a, ub);
+            const double e = exp(__dmul_rn(-be, sum));
             if (fabs(u - e) <= 1e-15 * e) atomicAdd(a.near_ties, 1ULL);
             ok = u < e;
           }

@@ -331,7 +331,12 @@ struct QmcArgs
   long long step_base;       // absolute step of the launch's first sweep
   int n_steps;
   const double* beta_eff;    // per absolute step: beta / trotter
-  const double* bond_prob;   // per absolute step: 1 - tanh(field * beta / trotter)
+  // per absolute step, the bond probability bp = 1 - tanh(field * beta /
+  // trotter) as an integer limit on the draw: replay, uniform() < bp exactly
+  // when the two 32-bit outputs X = d0 + d1 2^32 lie below bond_lim (all X
+  // when bond_all); counter, when draw >> 11 lies below bond_lim
+  const unsigned long long* bond_lim;
+  const unsigned char* bond_all;
   int replay;
   uint64_t* rng;             // replay: PCG state per slot
   uint32_t seed;             // counter mode: slot i draws on counter_key(seed, i)

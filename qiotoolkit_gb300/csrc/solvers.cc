@@ -1388,7 +1388,8 @@ class QuantumMonteCarlo : public Solver
   uint32_t* d_lspins = nullptr;
   unsigned long long* d_ties = nullptr;
   double* d_beta = nullptr;
-  double* d_bond = nullptr;
+  unsigned long long* d_blim = nullptr;
+  unsigned char* d_ball = nullptr;
 
   std::string target() const override { return "quantummontecarlo.qiotoolkit"; }
   int64_t n_walkers() const override { return model->empty() ? 0 : restarts * trotter; }
@@ -1441,14 +1442,15 @@ class QuantumMonteCarlo : public Solver
       size_t off = 0;
       auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
       const size_t o_l = take((size_t)R * 8), o_ls = take((size_t)R * P.pop.nw * 4), o_t = take(8),
-                   o_b = take((size_t)steps * 8), o_p = take((size_t)steps * 8);
+                   o_b = take((size_t)steps * 8), o_p = take((size_t)steps * 8), o_a = take((size_t)steps);
       aux = DevBuf(off);
       char* b = (char*)aux.ptr;
       d_low = (double*)(b + o_l);
       d_lspins = (uint32_t*)(b + o_ls);
       d_ties = (unsigned long long*)(b + o_t);
       d_beta = (double*)(b + o_b);
-      d_bond = (double*)(b + o_p);
+      d_blim = (unsigned long long*)(b + o_p);
+      d_ball = (unsigned char*)(b + o_a);
     }
     device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
     // per step: beta / P and 1 - tanh(field * beta / P), both schedules
@@ -1461,15 +1463,49 @@ class QuantumMonteCarlo : public Solver
     fs.final_ = field_high;
     bs.has_stop = fs.has_stop = true;
     bs.stop_ = fs.stop_ = (double)std::max(1, (int)step_limit - 1);
-    std::vector<double> be(steps), bp(steps);
+    std::vector<double> be(steps);
+    std::vector<unsigned long long> lim(steps);
+    std::vector<unsigned char> all(steps, 0);
+    // uniform() of the two 32-bit outputs X = d0 + d1 2^32 (libstdc++'s
+    // generate_canonical), monotone in X
+    auto canon = [](unsigned long long x) {
+      const double sum = (double)(uint32_t)x + (double)(uint32_t)(x >> 32) * 4294967296.0;
+      const double u = sum * 5.421010862427522170037e-20;
+      return u >= 1.0 ? 0.99999999999999988898 : u;
+    };
     for (int64_t s = 0; s < steps; s++)
     {
       const double b = bs.get_value((double)s), g = fs.get_value((double)s);
       be[s] = b / (double)trotter;
-      bp[s] = 1 - std::tanh(g * b / (double)trotter);
+      const double bp = 1 - std::tanh(g * b / (double)trotter);
+      if (replay)
+      {
+        // the least X with uniform() >= bp (uniform() < bp below it)
+        if (canon(~0ULL) < bp)
+          all[s] = 1, lim[s] = ~0ULL;
+        else
+        {
+          unsigned long long lo = 0, hi = ~0ULL;
+          while (lo < hi)
+          {
+            const unsigned long long mid = lo + (hi - lo) / 2;
+            if (canon(mid) >= bp) hi = mid;
+            else lo = mid + 1;
+          }
+          lim[s] = lo;
+        }
+      }
+      else
+      {
+        // (draw >> 11) 2^-53 < bp  <=>  draw >> 11 < ceil(bp 2^53)
+        const double t = std::ceil(std::max(0.0, std::min(1.0, bp)) * 9007199254740992.0);
+        lim[s] = (unsigned long long)t;
+      }
     }
     cuda_check(cudaMemcpyAsync(d_beta, be.data(), steps * 8, cudaMemcpyHostToDevice, st), "H2D");
-    cuda_check(cudaMemcpyAsync(d_bond, bp.data(), steps * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(d_blim, lim.data(), steps * 8, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(d_ball, all.data(), steps, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaStreamSynchronize(st), "sync");
     cuda_check(cudaMemsetAsync(d_ties, 0, 8, st), "memset");
     // rngs_[i] = rng_->fork() for the R * P slices in order (:52-58)
     std::vector<uint64_t> rs(S);
@@ -1516,7 +1552,8 @@ class QuantumMonteCarlo : public Solver
     a.restarts = (int)restarts;
     a.trotter = (int)trotter;
     a.beta_eff = d_beta;
-    a.bond_prob = d_bond;
+    a.bond_lim = d_blim;
+    a.bond_all = d_ball;
     a.replay = replay ? 1 : 0;
     a.rng = P.rng;
     a.seed = seed;
