@@ -894,6 +894,17 @@ class SubstochasticMonteCarlo : public Solver
   bool has_low = false;
   double low_cost = 0;
   int T = 1;
+  // page-locked host copies of the costs, lowest costs and the copy map
+  double* h_cost = nullptr;
+  double* h_low = nullptr;
+  int* h_src = nullptr;
+
+  ~SubstochasticMonteCarlo() override
+  {
+    if (h_cost) cudaFreeHost(h_cost);
+    if (h_low) cudaFreeHost(h_low);
+    if (h_src) cudaFreeHost(h_src);
+  }
 
   std::string target() const override { return "substochasticmontecarlo.cpu"; }
   int64_t n_walkers() const override { return model->empty() ? 0 : target_pop; }
@@ -995,6 +1006,12 @@ class SubstochasticMonteCarlo : public Solver
       d_init = (uint64_t*)(b + o_in);
       d_best = (uint32_t*)(b + o_b);
     }
+    if (!h_cost)
+    {
+      cuda_check(cudaMallocHost((void**)&h_cost, (size_t)R * 8), "cudaMallocHost");
+      cuda_check(cudaMallocHost((void**)&h_low, (size_t)R * 8), "cudaMallocHost");
+      cuda_check(cudaMallocHost((void**)&h_src, (size_t)R * 4), "cudaMallocHost");
+    }
     device_bytes = (int64_t)(pools[0].buf.bytes + pools[1].buf.bytes + aux.bytes);
     cur = 0;
     has_low = false;
@@ -1037,8 +1054,10 @@ class SubstochasticMonteCarlo : public Solver
   }
 
   // one step: walker steps, statistics, resampling (make_step, :67-84)
-  void step(cudaStream_t st, int64_t s, std::vector<double>& cost, std::vector<double>& low)
+  void step(cudaStream_t st, int64_t s)
   {
+    const double* cost = h_cost;
+    const double* low = h_low;
     const int R = (int)target_pop;
     SsmcArgs a{};
     a.m = model->device_view(false);
@@ -1056,8 +1075,8 @@ class SubstochasticMonteCarlo : public Solver
     prof_end(st);
     launches++;
     const DevPop& p = pools[cur].pop;
-    cuda_check(cudaMemcpyAsync(cost.data(), p.cost, (size_t)R * 8, cudaMemcpyDeviceToHost, st), "D2H");
-    cuda_check(cudaMemcpyAsync(low.data(), p.lowest, (size_t)R * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaMemcpyAsync(h_cost, p.cost, (size_t)R * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    cuda_check(cudaMemcpyAsync(h_low, p.lowest, (size_t)R * 8, cudaMemcpyDeviceToHost, st), "D2H");
     cuda_check(cudaStreamSynchronize(st), "sync");
     // update_population_statistics (:114-126)
     double mn = cost[0], mx = cost[0];
@@ -1103,15 +1122,14 @@ class SubstochasticMonteCarlo : public Solver
         count[sel.select_and_remove(master.uniform())] += 1;
         resampled++;
       }
-      std::vector<int> src;
-      src.reserve(R);
+      // the previous step's sync (the D2H above) has retired the last
+      // upload of the map, so the page-locked buffer is free to refill
+      int n_src = 0;
       for (int i = 0; i < R; i++)
-        for (size_t c = 0; c < count[i]; c++) src.push_back(i);
-      cuda_check(cudaMemcpyAsync(d_src, src.data(), (size_t)R * 4, cudaMemcpyHostToDevice, st), "H2D");
+        for (size_t c = 0; c < count[i]; c++) h_src[n_src++] = i;
+      cuda_check(cudaMemcpyAsync(d_src, h_src, (size_t)R * 4, cudaMemcpyHostToDevice, st), "H2D");
       cuda_check(launch_pa_copy(pools[cur].pop, pools[1 - cur].pop, d_src, R, st), "copy kernel");
       launches++;
-      // the src map must stay alive until the copy has read it
-      cuda_check(cudaStreamSynchronize(st), "sync");
       cur = 1 - cur;
     }
   }
@@ -1125,12 +1143,11 @@ class SubstochasticMonteCarlo : public Solver
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    std::vector<double> cost(target_pop), low(target_pop);
     auto t0 = std::chrono::steady_clock::now();
     int64_t s = step_pos;
     for (; s < step_limit; s++)
     {
-      step(st, s, cost, low);
+      step(st, s);
       if (has_cost_limit && low_cost <= cost_limit)
       {
         s++;
@@ -1165,9 +1182,8 @@ class SubstochasticMonteCarlo : public Solver
       last_step = step_limit;
       return true;
     }
-    std::vector<double> cost(target_pop), low(target_pop);
     const int64_t end = std::min(step_limit, step_pos + n);
-    for (; step_pos < end; step_pos++) step(st, step_pos, cost, low);
+    for (; step_pos < end; step_pos++) step(st, step_pos);
     last_step = step_pos;
     return step_pos >= step_limit;
   }

@@ -74,7 +74,13 @@ int64_t footprint_of(const HostModel& m, const Solver& s)
   // tabu search: tabu list and two cost-difference arrays per walker, the
   // hill climber's spins and state
   const int64_t tabu = s.target() == "tabu.qiotoolkit" ? W * (24 * m.N + 2 * nw * 4 + 64) : 0;
-  return model_bytes(m) + W * per + steps * 8 + W * 64 + lv + tabu + 64 * 1024;
+  // substochastic Monte Carlo: a second population (the resampling copies
+  // into it), the copy map and init streams; quantum Monte Carlo: per step
+  // beta and bond limits, per restart its lowest (walkers are its slices)
+  int64_t extra = 0;
+  if (s.target() == "substochasticmontecarlo.cpu") extra = W * (per + 12) + nw * 4;
+  if (s.target() == "quantummontecarlo.qiotoolkit") extra = steps * 17 + W * (8 + nw * 4);
+  return model_bytes(m) + W * per + steps * 8 + W * 64 + lv + tabu + extra + 64 * 1024;
 }
 }  // namespace
 
