@@ -612,7 +612,7 @@ def main_pf(args, ws, rank):
 
     if rank == 0:
         kernel_s = sum(ms) / 1e3
-        bpa = 100.0  # SURVEY configuration-1 model: 8 + 7 x (4 + 8 + 1) + 1
+        bpa = 100.0  # the sparse Ising N=1000 model: 8 + 7 x (4 + 8 + 1) + 1 bytes per attempt
         achieved = bpa * att / kernel_s / 1e9
         peak, peak_src = peaks()
         line = {
