@@ -599,8 +599,10 @@ __device__ __forceinline__ void warp_copy(uint32_t* dst, const uint32_t* src, in
 template <int FL, bool INT>
 __device__ void tabu_refresh(const DevModel& m, const uint32_t* sp, double* df, int i, int lane)
 {
-  if (lane == 0) df[i] = lane_diff<FL, INT>(m, sp, i);
   const int rb = m.row[i], re = m.row[i + 1];
+  // i itself on the first lane without an incidence of i's row, so its sum
+  // runs beside the co-members' instead of after one of them
+  if (lane == min(re - rb, 31)) df[i] = lane_diff<FL, INT>(m, sp, i);
   if (FL == F_PARITY && m.pair_only)
   {
     for (int q = rb + lane; q < re; q += 32)
