@@ -10,7 +10,7 @@ walkers) = 1.05e9 flip attempts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising|ssmc_ising|
-                              qmc_ising]
+                              qmc_ising|qmc_ising_counter]
 
 Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
 launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
@@ -65,6 +65,11 @@ WORKLOADS = {
                            "fields U[-0.5,0.5], 16 restarts x 32 Trotter slices, 200 sweeps, beta 1->5 and "
                            "transverse field 0->3 linear, replayed PCG streams, seed 0",
                       target="quantummontecarlo.qiotoolkit"),
+    "qmc_ising_counter": dict(desc="Quantum Monte Carlo on the sparse Ising N=1000, 3000 ER couplings +-1, "
+                                   "1000 fields U[-0.5,0.5], 16 restarts x 32 Trotter slices, 200 sweeps, "
+                                   "beta 1->5 and transverse field 0->3 linear, counter streams (level-parallel "
+                                   "kernel), seed 0",
+                              target="quantummontecarlo.qiotoolkit"),
     "batch_cubic": dict(desc="Batched SA: 512 periodic cubic +-J instances, L uniform in [4,20] "
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
@@ -85,7 +90,7 @@ def batch_instances(n=512):
 
 # the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
 KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel",
-                4: "tabu_kernel", 5: "ssmc_walk_kernel", 6: "qmc_kernel"}
+                4: "tabu_kernel", 5: "ssmc_walk_kernel", 6: "qmc_kernel", 7: "qmc_level_kernel"}
 
 
 def make_workload(name):
@@ -110,6 +115,9 @@ def make_workload(name):
         params = {"seed": 0, "sweeps": 200, "restarts": 16, "trotter_number": 32, "beta_start": 1.0,
                   "beta_stop": 5.0, "transverse_field_low": 0.0, "transverse_field_high": 3.0}
         return "ising", off, ids, coef, params
+    if name == "qmc_ising_counter":
+        kind, off, ids, coef, params = make_workload("qmc_ising")
+        return kind, off, ids, coef, dict(params, rng_mode="counter")
     if name == "ssmc_ising":
         off, ids, coef = I.er_ising(1000, 3000, seed=0)
         params = {"seed": 0, "sweeps": 200, "target_population": 4096, "steps_per_walker": 4,
@@ -236,7 +244,7 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
             d = f"population {restarts} x {sweeps} steps x {params['sweeps_per_replica']} sweeps"
         elif "trotter_number" in params:
             O.run(m, "qmc", seed=0, step_limit=sweeps, restarts=restarts, threads=threads,
-                  trotter_number=params["trotter_number"],
+                  trotter_number=params["trotter_number"], rng_mode=params.get("rng_mode", "replay"),
                   sched=("linear", params["beta_start"], params["beta_stop"]),
                   sched2=("linear", params["transverse_field_low"], params["transverse_field_high"]))
             a = restarts * params["trotter_number"] * sweeps * n

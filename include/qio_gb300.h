@@ -90,7 +90,9 @@ typedef struct qio_solver_stats {
                               warp, 2 one walker per lane, 3 level schedule,
                               4 tabu search (one walker per warp),
                               5 substochastic Monte Carlo walker steps,
-                              6 quantum Monte Carlo (one warp per restart) */
+                              6 quantum Monte Carlo (one warp per restart),
+                              7 quantum Monte Carlo level schedule (counter
+                              streams, one block per restart) */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */

@@ -1068,6 +1068,190 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
   }
 }
 
+// Level-parallel QMC sweeps for counter streams (positional draws): one
+// block per restart, its slices' spins in shared memory, the warps taking the
+// variables of one level at a time (no two share a term, and every
+// lower-index neighbour sits in an earlier level, so each variable sees the
+// spins the ordered sweep would).  Flips are logged per slice; after the
+// sweep each slice adds its flips' differences to its cost in variable order,
+// as the ordered sweep's cost += diff does.
+size_t qmc_level_smem(int trotter, int nw)
+{
+  if (trotter < 2 || trotter > 256) return 0;
+  const size_t per_warp = (size_t)trotter * 8 + (((size_t)trotter * 2 + 7) & ~(size_t)7);
+  const size_t b = 2 * (size_t)trotter * nw * 4 + kQmcLevelWarps * per_warp;
+  return b <= 200 * 1024 ? b : 0;
+}
+
+template <int FL, bool INT>
+__global__ void __launch_bounds__(kQmcLevelWarps * 32) qmc_level_kernel(QmcArgs a)
+{
+  extern __shared__ __align__(16) unsigned char qls[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int r = blockIdx.x;
+  const int P = a.trotter, N = a.m.n_vars, nw = a.p.nw;
+  uint32_t* sps = (uint32_t*)qls;
+  uint32_t* flp = sps + (size_t)P * nw;
+  const size_t per_warp = (size_t)P * 8 + (((size_t)P * 2 + 7) & ~(size_t)7);
+  double* dif = (double*)((unsigned char*)(flp + (size_t)P * nw) + (size_t)wib * per_warp);
+  uint8_t* bond = (uint8_t*)(dif + P);
+  uint8_t* acc = bond + P;
+  const int base = r * P;
+  double* dl = a.dlog + (size_t)base * N;
+  for (int i = threadIdx.x; i < P * nw; i += blockDim.x) sps[i] = a.p.spins[(size_t)base * nw + i];
+  __syncthreads();
+  for (int st = 0; st < a.n_steps; st++)
+  {
+    const long long S = a.step_base + st;
+    const double be = a.beta_eff[S];
+    const float bef = (float)be;
+    const unsigned long long blim = a.bond_lim[S];
+    for (int i = threadIdx.x; i < P * nw; i += blockDim.x) flp[i] = 0;
+    __syncthreads();
+    for (int L = 0; L < a.n_levels; L++)
+    {
+      const int e1 = a.lv_off[L + 1];
+      for (int e = a.lv_off[L] + wib; e < e1; e += nwarps)
+      {
+        const int v = a.lv_var[e];
+        const unsigned long long c =
+            2ull * ((unsigned long long)S * (unsigned long long)N + (unsigned long long)v);
+        for (int k = lane; k < P; k += 32)
+        {
+          const uint32_t* sp = sps + (size_t)k * nw;
+          dif[k] = lane_diff<FL, INT>(a.m, sp, v);
+          uint8_t b = 0;
+          if (k > 0 && spin_of(sp - nw, v) == spin_of(sp, v))
+            b = (counter_draw(counter_key(a.seed, (uint64_t)(base + k)), c) >> 11) < blim;
+          bond[k] = b;
+        }
+        __syncwarp();
+        for (int k = lane; k < P; k += 32)
+        {
+          if (bond[k]) continue;
+          double sum = dif[k];
+          int q = k + 1;
+          for (; q < P && bond[q]; q++) sum = __dadd_rn(sum, dif[q]);
+          uint8_t ok = 1;
+          if (!(sum < 10E-12))
+          {
+            const unsigned long long ub = counter_draw(counter_key(a.seed, (uint64_t)(base + k)), c + 1);
+            const float uf = (float)(uint32_t)(ub >> 40) * 0x1p-24f;
+            const float xf = -bef * (float)sum, ef = expf(xf);
+            const float te = ef * (fabsf(xf) + 2.0f) * 0x1p-20f;
+            if (uf + 0x1p-23f < ef - te)
+              ok = 1;
+            else if (uf - 0x1p-23f > ef + te)
+              ok = 0;
+            else
+            {
+              const double u = (double)(ub >> 11) * 0x1p-53;
+              const double x = exp(__dmul_rn(-be, sum));
+              if (fabs(u - x) <= 1e-15 * x) atomicAdd(a.near_ties, 1ULL);
+              ok = u < x;
+            }
+          }
+          for (int i = k; i < q; i++) acc[i] = ok;
+        }
+        __syncwarp();
+        for (int k = lane; k < P; k += 32)
+          if (acc[k])
+          {
+            atomicXor(&sps[(size_t)k * nw + (v >> 5)], 1u << (v & 31));
+            atomicOr(&flp[(size_t)k * nw + (v >> 5)], 1u << (v & 31));
+            dl[(size_t)k * N + v] = dif[k];
+          }
+        __syncwarp();
+      }
+      __syncthreads();
+    }
+    // cost += diff over the sweep's flips in variable order, per slice
+    for (int k = threadIdx.x; k < P; k += blockDim.x)
+    {
+      double cst = a.p.cost[base + k];
+      unsigned long long nf = 0;
+      for (int q = 0; q < nw; q++)
+      {
+        uint32_t f = flp[(size_t)k * nw + q];
+        while (f)
+        {
+          const int b = __ffs(f) - 1;
+          f &= f - 1;
+          cst = __dadd_rn(cst, dl[(size_t)k * N + q * 32 + b]);
+          nf++;
+        }
+      }
+      a.p.cost[base + k] = cst;
+      a.p.accepts[base + k] += nf;
+      a.p.attempts[base + k] += (unsigned long long)N;
+    }
+    __syncthreads();
+    if (wib == 0)
+    {
+      double bc = 0.0;
+      int bk = INT_MAX;
+      for (int k = lane; k < P; k += 32)
+      {
+        const double ck = a.p.cost[base + k];
+        if (bk == INT_MAX || ck < bc)
+        {
+          bc = ck;
+          bk = k;
+        }
+      }
+#pragma unroll
+      for (int sh = 16; sh; sh >>= 1)
+      {
+        const double oc = __shfl_xor_sync(kFull, bc, sh);
+        const int ok = __shfl_xor_sync(kFull, bk, sh);
+        if (ok != INT_MAX && (bk == INT_MAX || oc < bc || (oc == bc && ok < bk)))
+        {
+          bc = oc;
+          bk = ok;
+        }
+      }
+      if (bc < a.low[r])
+      {
+        for (int q = lane; q < nw; q += 32) a.low_spins[(size_t)r * nw + q] = sps[(size_t)bk * nw + q];
+        __syncwarp();
+        if (lane == 0) a.low[r] = bc;
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < P * nw; i += blockDim.x) a.p.spins[(size_t)base * nw + i] = sps[i];
+}
+
+template <int FL, bool I>
+static cudaError_t qmc_level_dispatch(const QmcArgs& a, cudaStream_t s)
+{
+  const size_t smem = qmc_level_smem(a.trotter, a.p.nw);
+  if (smem > 48 * 1024)
+  {
+    cudaError_t e =
+        cudaFuncSetAttribute(qmc_level_kernel<FL, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  qmc_level_kernel<FL, I><<<a.restarts, kQmcLevelWarps * 32, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_qmc_levels(const QmcArgs& a, cudaStream_t s)
+{
+  if (a.restarts <= 0 || a.n_steps <= 0) return cudaSuccess;
+  if (a.replay || !qmc_level_smem(a.trotter, a.p.nw) || !a.lv_off || !a.lv_var || !a.dlog)
+    return cudaErrorInvalidValue;
+  const bool I = a.m.int_mode != 0;
+  switch (a.m.flavor)
+  {
+    case F_PARITY: return I ? qmc_level_dispatch<F_PARITY, true>(a, s) : qmc_level_dispatch<F_PARITY, false>(a, s);
+    case F_COUNTER: return I ? qmc_level_dispatch<F_COUNTER, true>(a, s) : qmc_level_dispatch<F_COUNTER, false>(a, s);
+    case F_PLAIN_ISING:
+      return I ? qmc_level_dispatch<F_PLAIN_ISING, true>(a, s) : qmc_level_dispatch<F_PLAIN_ISING, false>(a, s);
+    default: return I ? qmc_level_dispatch<F_PLAIN_PUBO, true>(a, s) : qmc_level_dispatch<F_PLAIN_PUBO, false>(a, s);
+  }
+}
+
 template <int FL, bool I>
 static cudaError_t qmc_dispatch(const QmcArgs& a, cudaStream_t s)
 {

@@ -343,8 +343,20 @@ struct QmcArgs
   double* low;               // per restart: lowest cost of its slices
   uint32_t* low_spins;       // per restart: that slice's spins (p.nw words)
   unsigned long long* near_ties;  // exp() within 1e-15 of its uniform draw
+  // level schedule (counter streams only): variables lv_var[lv_off[t] ..
+  // lv_off[t+1]) share no term and follow all their lower-index neighbours'
+  // levels; dlog holds each slice's flip differences of a sweep (restarts *
+  // trotter * n_vars) for the cost sums in variable order
+  int n_levels;
+  const int* lv_off;
+  const int* lv_var;
+  double* dlog;
 };
 cudaError_t launch_qmc(const QmcArgs& a, cudaStream_t s);
+static const int kQmcLevelWarps = 16;
+// dynamic shared memory of the level kernel (0 when it cannot run)
+size_t qmc_level_smem(int trotter, int nw);
+cudaError_t launch_qmc_levels(const QmcArgs& a, cudaStream_t s);
 
 // PT: label swaps + observables, one thread per restart.
 struct SwapArgs

@@ -1390,6 +1390,56 @@ class QuantumMonteCarlo : public Solver
   double* d_beta = nullptr;
   unsigned long long* d_blim = nullptr;
   unsigned char* d_ball = nullptr;
+  // level schedule of the counter-stream kernel
+  bool use_levels = false;
+  int n_levels = 0;
+  DevBuf lvbuf;
+  int* d_lv_off = nullptr;
+  int* d_lv_var = nullptr;
+  double* d_dlog = nullptr;
+
+  // level(v) = 1 + the largest level of v's lower-index term co-members (0
+  // without one); variables listed by level, in index order within a level
+  void build_levels(cudaStream_t st)
+  {
+    const HostModel& m = *model;
+    const int N = (int)m.N;
+    std::vector<int> lev(N, 0);
+    int top = 0;
+    for (int v = 0; v < N; v++)
+    {
+      int L = 0;
+      for (int q = m.row[v]; q < m.row[v + 1]; q++)
+      {
+        const uint32_t t = m.inc[q] & ~kNegBit;
+        for (int u = m.trow[t]; u < m.trow[t + 1]; u++)
+        {
+          const int x = (int)(m.tvar[u] & ~kNegBit);
+          if (x < v) L = std::max(L, lev[x] + 1);
+        }
+      }
+      lev[v] = L;
+      top = std::max(top, L);
+    }
+    n_levels = top + 1;
+    std::vector<int> off(n_levels + 1, 0), var(N);
+    for (int v = 0; v < N; v++) off[lev[v] + 1]++;
+    for (int L = 0; L < n_levels; L++) off[L + 1] += off[L];
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (int v = 0; v < N; v++) var[fill[lev[v]]++] = v;
+    const size_t S = (size_t)restarts * trotter;
+    size_t o = 0;
+    auto take = [&](size_t b) { size_t r = o; o = (o + b + 255) & ~(size_t)255; return r; };
+    const size_t o_off = take((size_t)(n_levels + 1) * 4), o_var = take((size_t)N * 4),
+                 o_log = take(S * (size_t)N * 8);
+    lvbuf = DevBuf(o);
+    char* b = (char*)lvbuf.ptr;
+    d_lv_off = (int*)(b + o_off);
+    d_lv_var = (int*)(b + o_var);
+    d_dlog = (double*)(b + o_log);
+    cuda_check(cudaMemcpyAsync(d_lv_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st), "H2D");
+    cuda_check(cudaMemcpyAsync(d_lv_var, var.data(), var.size() * 4, cudaMemcpyHostToDevice, st), "H2D");
+  }
 
   std::string target() const override { return "quantummontecarlo.qiotoolkit"; }
   int64_t n_walkers() const override { return model->empty() ? 0 : restarts * trotter; }
@@ -1452,7 +1502,11 @@ class QuantumMonteCarlo : public Solver
       d_blim = (unsigned long long*)(b + o_p);
       d_ball = (unsigned char*)(b + o_a);
     }
-    device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
+    // counter streams draw by position: the level-parallel kernel runs them
+    // ("kernel": "warp" keeps one warp per restart)
+    use_levels = !replay && kernel != 1 && kernel != 2 && qmc_level_smem((int)trotter, P.pop.nw) > 0;
+    if (use_levels && !lvbuf.ptr) build_levels(st);
+    device_bytes = (int64_t)(P.buf.bytes + aux.bytes + lvbuf.bytes);
     // per step: beta / P and 1 - tanh(field * beta / P), both schedules
     // linear with stop max(1, step_limit - 1)
     Schedule bs, fs;
@@ -1524,7 +1578,7 @@ class QuantumMonteCarlo : public Solver
     a.skip_terms = 1;
     cuda_check(launch_init(a, st), "init kernel");
     launches++;
-    used_kernel = 6;
+    used_kernel = use_levels ? 7 : 6;
     // save_lowest of every restart on its initial slices
     std::vector<double> c(S), low(R);
     cuda_check(cudaMemcpyAsync(c.data(), P.pop.cost, (size_t)S * 8, cudaMemcpyDeviceToHost, st), "D2H");
@@ -1560,6 +1614,10 @@ class QuantumMonteCarlo : public Solver
     a.low = d_low;
     a.low_spins = d_lspins;
     a.near_ties = d_ties;
+    a.n_levels = n_levels;
+    a.lv_off = d_lv_off;
+    a.lv_var = d_lv_var;
+    a.dlog = d_dlog;
     return a;
   }
 
@@ -1569,7 +1627,7 @@ class QuantumMonteCarlo : public Solver
     a.step_base = base;
     a.n_steps = (int)n;
     prof_begin(st);
-    cuda_check(launch_qmc(a, st), "qmc kernel");
+    cuda_check(use_levels ? launch_qmc_levels(a, st) : launch_qmc(a, st), "qmc kernel");
     prof_end(st);
     launches++;
   }

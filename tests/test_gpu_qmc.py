@@ -94,3 +94,25 @@ def test_qmc_pieces():
     finally:
         srv.close()
     assert res["solutions"] == s.result()["solutions"]
+
+
+@pytest.mark.parametrize("trotter", [12, 70])
+def test_qmc_level_kernel_counter_streams(trotter):
+    """Counter streams run the level-parallel kernel (variables of one level
+    at once, costs summed per slice in variable order after each sweep): the
+    same slices as the oracle and as the one-warp-per-restart kernel."""
+    off, ids, coef = I.er_ising(150, 450, seed=31)
+    g = q.Model("ising", off=off, ids=ids, coef=coef)
+    o = O.Model("ising", off=off, ids=ids, coef=coef)
+    params = {"seed": 13, "sweeps": 25, "restarts": 4, "trotter_number": trotter,
+              "beta_start": 0.5, "beta_stop": 3.0, "transverse_field_low": 0.2,
+              "transverse_field_high": 2.0, "rng_mode": "counter"}
+    s = q.Solver(g, QMC, {"params": params}).init().run()
+    assert s.stats().sweep_kernel == 7
+    r = O.run(o, "qmc", seed=13, step_limit=25, restarts=4, trotter_number=trotter,
+              sched=("linear", 0.5, 3.0), sched2=("linear", 0.2, 2.0), rng_mode="counter")
+    same(s, r)
+    w = q.Solver(g, QMC, {"params": dict(params, kernel="warp")}).init().run()
+    assert w.stats().sweep_kernel == 6
+    np.testing.assert_array_equal(w.replicas()["states"], s.replicas()["states"])
+    np.testing.assert_array_equal(w.replicas()["cost"], s.replicas()["cost"])
