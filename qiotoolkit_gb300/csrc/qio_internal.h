@@ -353,7 +353,7 @@ struct QmcArgs
   double* dlog;
 };
 cudaError_t launch_qmc(const QmcArgs& a, cudaStream_t s);
-static const int kQmcLevelWarps = 16;
+static const int kQmcLevelWarps = 32;
 // dynamic shared memory of the level kernel (0 when it cannot run)
 size_t qmc_level_smem(int trotter, int nw);
 cudaError_t launch_qmc_levels(const QmcArgs& a, cudaStream_t s);
