@@ -17,7 +17,7 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
                      solver/test/tabu_test.cc:98-184,
                      solver/test/substochastic_monte_carlo_test.cc:104-176,
                      solver/test/quantum_monte_carlo_test.cc:86-148 (data/params_qmc.json),
-                     solver/test/tabu_pf_test.cc:23-115 (data/pf5s.json),
+                     solver/test/{tabu,sa,pt}_pf_test.cc:23-115 (data/pf5s.json),
                      with their data/ inputs and data/params1.json
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
@@ -193,6 +193,18 @@ def solver_pins():
         ("tabu_pf", "ising", "ising1.json", -10, {}, "solver/test/tabu_pf_test.cc:68-81"),
         ("tabu_pf", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/tabu_pf_test.cc:83-98"),
         ("tabu_pf", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/tabu_pf_test.cc:100-115"),
+        ("sa_pf", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/sa_pf_test.cc:23-36"),
+        ("sa_pf", "pubo", "puboempty.json", 2, {}, "solver/test/sa_pf_test.cc:38-51"),
+        ("sa_pf", "ising", "isingempty.json", 12, {}, "solver/test/sa_pf_test.cc:53-66"),
+        ("sa_pf", "ising", "ising1.json", -10, {}, "solver/test/sa_pf_test.cc:68-81"),
+        ("sa_pf", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/sa_pf_test.cc:83-98"),
+        ("sa_pf", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/sa_pf_test.cc:100-115"),
+        ("pt_pf", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/pt_pf_test.cc:23-36"),
+        ("pt_pf", "pubo", "puboempty.json", 2, {}, "solver/test/pt_pf_test.cc:38-51"),
+        ("pt_pf", "ising", "isingempty.json", 12, {}, "solver/test/pt_pf_test.cc:53-66"),
+        ("pt_pf", "ising", "ising1.json", -10, {}, "solver/test/pt_pf_test.cc:68-81"),
+        ("pt_pf", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/pt_pf_test.cc:83-98"),
+        ("pt_pf", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/pt_pf_test.cc:100-115"),
     ]
     params_qmc = json.loads(read("params_qmc.json", DATA))["params"]
     params_pf = json.loads(read("pf5s.json", DATA))["params"]
@@ -201,7 +213,8 @@ def solver_pins():
         assert model["type"] == kind
         cases.append({"solver": solver, "kind": kind, "file": fname,
                       "terms": model["terms"],
-                      "params": {"qmc": params_qmc, "tabu_pf": params_pf}.get(solver, params1),
+                      "params": {"qmc": params_qmc, "tabu_pf": params_pf, "sa_pf": params_pf,
+                                 "pt_pf": params_pf}.get(solver, params1),
                       "expected_cost": cost, "configuration": conf, "source": source})
     return {"params_file": "data/params1.json", "cases": cases}
 

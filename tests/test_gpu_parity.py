@@ -159,14 +159,18 @@ def test_reference_solver_pins_on_gpu(golden):
                                  "terms": [{"c": c, "ids": ids} for c, ids in case["terms"]]}}
         if case["solver"] == "pa":
             p = {"seed": p["seed"], "sweeps": p["sweeps"], "population": 8, "threads": 4}
-        if case["solver"] == "tabu_pf":
+        if case["solver"] in ("tabu_pf", "sa_pf"):
             p = {"seed": 0, "min_num_restarts": 8, "timeout": p["timeout"]}
+        if case["solver"] == "pt_pf":
+            p = {"seed": 0, "min_num_betas": 8, "timeout": p["timeout"]}
         if case["solver"] == "ssmc":
             p = {"seed": p["seed"], "sweeps": p["sweeps"], "target_population": 8, "threads": 8}
         target = {"sa": SA, "pt": PT, "pa": PA, "tabu": "tabu.qiotoolkit",
                   "ssmc": "substochasticmontecarlo.cpu",
                   "qmc": "quantummontecarlo.qiotoolkit",
-                  "tabu_pf": "tabu-parameterfree.qiotoolkit"}[case["solver"]]
+                  "tabu_pf": "tabu-parameterfree.qiotoolkit",
+                  "sa_pf": "simulatedannealing-parameterfree.qiotoolkit",
+                  "pt_pf": "paralleltempering-parameterfree.qiotoolkit"}[case["solver"]]
         res = q.run_json(doc, {"params": p}, target)
         cost = res["solutions"]["cost"]
         exp = case["expected_cost"]
