@@ -1028,10 +1028,13 @@ struct TabuWalker : Walker
   double hc_cost = 0, hc_low = 0;
   std::vector<uint8_t> hc_low_spins;
 
+  // get_sweep_size(): N, or 1 for MaxSat (markov/model.h:169) unless the
+  // full MaxSat sweep is asked for
+  int64_t sweep() const { return model->sweep_size(full_maxsat); }
   void tabu_init()
   {
     init();
-    tabu.assign((size_t)model->N, 0);
+    tabu.assign((size_t)sweep(), 0);
     iter = incomplete = 0;
     local = false;
   }
@@ -1049,7 +1052,7 @@ struct TabuWalker : Walker
   void local_sweep()
   {
     const double prev = hc_low;
-    for (int64_t v = 0; v < model->N; v++)
+    for (int64_t v = 0; v < sweep(); v++)
     {
       const double d = cost_difference(*model, hc, v);
       diff_evals++;
@@ -1083,7 +1086,7 @@ struct TabuWalker : Walker
       local_sweep();
       return;
     }
-    const int64_t n = model->N;
+    const int64_t n = sweep();
     bool has_best = false, taken = false;
     double best_d = 0;
     int64_t best = 0;
@@ -1156,6 +1159,7 @@ static Result run_tabu(const Model& m, const orc_params& p)
     w.model = &m;
     w.rng = rngs[i].get();
     w.counter_mode = p.rng_mode == ORC_RNG_COUNTER;
+    w.full_maxsat = p.full_maxsat_sweep != 0;
     w.key = counter_key(p.seed, i);
     // Tabu::make_step sets tabu_tenures_[i] when the list is given
     w.tenure = (uint64_t)(p.tabu_tenures && (int64_t)i < p.n_tabu_tenures ? p.tabu_tenures[i] : p.tabu_tenure);
@@ -1648,6 +1652,9 @@ static Result run_qmc(const Model& m, const orc_params& p)
   Lowest best;
   best.update(low[0], low_state[0]);
   const int64_t n = m.N;
+  // the sweep visits get_sweep_size() variables (1 for MaxSat unless the
+  // full sweep is asked for); draw positions stay indexed by N
+  const int64_t sw = m.sweep_size(p.full_maxsat_sweep != 0);
   set_threads(p.threads);
   int64_t step = 0;
   for (; step < p.step_limit; step++)
@@ -1662,7 +1669,7 @@ static Result run_qmc(const Model& m, const orc_params& p)
       std::vector<double> diff(P);
       std::vector<char> bond(P), acc(P);
       Walker* w = &sl[rr * P];
-      for (int64_t v = 0; v < n; v++)
+      for (int64_t v = 0; v < sw; v++)
       {
         const uint64_t c = 2 * ((uint64_t)step * (uint64_t)n + (uint64_t)v);
         for (size_t k = 0; k < P; k++)
@@ -1697,7 +1704,7 @@ static Result run_qmc(const Model& m, const orc_params& p)
             w[k].total_accepts++;
           }
       }
-      for (size_t k = 0; k < P; k++) w[k].total_attempts += (uint64_t)n;
+      for (size_t k = 0; k < P; k++) w[k].total_attempts += (uint64_t)sw;
       save_lowest(rr);
     }
     if (p.has_cost_limit)

@@ -632,7 +632,9 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= a.n_walkers) return;  // whole warps leave together
   const DevModel& m = a.m;
-  const int N = m.n_vars, nw = a.p.nw;
+  // N strides the per-walker arrays; SW variables are swept (get_sweep_size:
+  // N, or 1 for MaxSat unless the full sweep is asked for)
+  const int N = m.n_vars, SW = m.sweep_size, nw = a.p.nw;
   uint32_t* sp = a.p.spins + (size_t)w * nw;
   uint32_t* ls = a.p.lspins + (size_t)w * nw;
   uint32_t* hs = a.hc + (size_t)w * nw;
@@ -659,16 +661,16 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
   auto local_sweep = [&]() {
     const double prev = S.hc_low;
     int v0 = 0;
-    while (v0 < N)
+    while (v0 < SW)
     {
       const int v = v0 + lane;
-      const bool ok = v < N;
+      const bool ok = v < SW;
       const double d = ok ? hd[v] : 0.0;
       // d <= 0 for a non-NaN double: its bits as a signed integer are <= 0
       const unsigned take = __ballot_sync(kFull, ok && __double_as_longlong(d) <= 0);
       if (!take)
       {
-        att += (unsigned long long)min(32, N - v0);
+        att += (unsigned long long)min(32, SW - v0);
         v0 += 32;
         continue;
       }
@@ -718,7 +720,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
     const double t = __dadd_rn(low, -cost);
     const double e = fmax(__dmul_rn(fmax(fmax(fabs(cost), fabs(low)), fabs(t)), 0x1p-48), 0x1p-1000);
     const unsigned long long klo = fkey(__dadd_rn(t, -e)), khi = fkey(__dadd_rn(t, e));
-    for (int c0 = 0; c0 < N && !taken; c0 += 128)
+    for (int c0 = 0; c0 < SW && !taken; c0 += 128)
     {
       double d[4];
       unsigned long long x[4];
@@ -726,14 +728,14 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
       for (int u = 0; u < 4; u++)
       {
         const int v = c0 + 32 * u + lane;
-        d[u] = v < N ? df[v] : 0.0;
-        x[u] = v < N ? tb[v] : 0ull;
+        d[u] = v < SW ? df[v] : 0.0;
+        x[u] = v < SW ? tb[v] : 0ull;
       }
 #pragma unroll
       for (int u = 0; u < 4; u++)
       {
         const int v = c0 + 32 * u + lane;
-        const bool ok = v < N;
+        const bool ok = v < SW;
         const unsigned long long k = fkey(d[u]);
         unsigned take = __ballot_sync(kFull, ok && k < klo);
         const unsigned near = __ballot_sync(kFull, ok && k >= klo && k <= khi);
@@ -766,10 +768,10 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
           S.local = 1;
           S.incomplete += (unsigned long long)i;
           att += (unsigned long long)(i + 1);
-          if (S.incomplete < (unsigned long long)N)
+          if (S.incomplete < (unsigned long long)SW)
             local_sweep();
           else
-            S.incomplete -= (unsigned long long)N;
+            S.incomplete -= (unsigned long long)SW;
           break;
         }
         if (ok && !(x[u] >= it) && k < bk)
@@ -782,7 +784,7 @@ __global__ void __launch_bounds__(128) tabu_kernel(TabuArgs a)
     }
     if (!taken)
     {
-      att += (unsigned long long)N;
+      att += (unsigned long long)SW;
       // the lowest difference off the tabu list, the first on ties
 #pragma unroll
       for (int sh = 16; sh; sh >>= 1)
@@ -963,7 +965,9 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
   const int wib = threadIdx.x >> 5;
   const int r = blockIdx.x * (blockDim.x >> 5) + wib;
   if (r >= a.restarts) return;  // whole warps leave together
-  const int P = a.trotter, N = a.m.n_vars, nw = a.p.nw;
+  // SW variables are swept (1 for MaxSat unless the full sweep is asked
+  // for); draw positions stay indexed by N
+  const int P = a.trotter, N = a.m.n_vars, SW = a.m.sweep_size, nw = a.p.nw;
   const size_t per_warp = (size_t)P * 8 + (((size_t)P * 2 + 7) & ~(size_t)7);
   double* dif = (double*)(qsm + (size_t)wib * per_warp);
   uint8_t* bond = (uint8_t*)(dif + P);
@@ -976,7 +980,7 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
     const float bef = (float)be;
     const unsigned long long blim = a.bond_lim[S];
     const bool ball = a.bond_all[S] != 0;
-    for (int v = 0; v < N; v++)
+    for (int v = 0; v < SW; v++)
     {
       const unsigned long long c = 2ull * ((unsigned long long)S * (unsigned long long)N + (unsigned long long)v);
       for (int k = lane; k < P; k += 32)
@@ -1038,7 +1042,7 @@ __global__ void __launch_bounds__(128) qmc_kernel(QmcArgs a)
     int bk = INT_MAX;
     for (int k = lane; k < P; k += 32)
     {
-      a.p.attempts[base + k] += (unsigned long long)N;
+      a.p.attempts[base + k] += (unsigned long long)SW;
       const double ck = a.p.cost[base + k];
       if (bk == INT_MAX || ck < bc)
       {

@@ -1212,7 +1212,6 @@ class TabuSearch : public Solver
   void configure(const json::Value& doc)
   {
     configure_common(*this, doc);
-    if (model->kind == K_MAXSAT) fail(1, "tabu search runs Ising and PUBO models here");
     Params p(params);
     const int64_t t = p.integer("tabu_tenure", 0);
     if (t < 0) fail(1, "parameter `tabu_tenure`: must be greater than or equal to 0, found " + std::to_string(t));
@@ -1255,10 +1254,11 @@ class TabuSearch : public Solver
     }
     cuda_check(cudaMemcpyAsync(P.rng, rs.data(), R * 8, cudaMemcpyHostToDevice, st), "H2D rng");
     InitArgs a{};
-    a.m = model->device_view(false);
+    a.m = model->device_view(full_maxsat_sweep);
     a.p = P.pop;
     a.n_walkers = R;
-    a.replay = replay ? 1 : 0;
+    // MaxSat states draw one uniform() per variable (model/max_sat.h:144-150)
+    a.replay = replay ? (model->kind == K_MAXSAT ? 2 : 1) : (model->kind == K_MAXSAT ? 3 : 0);
     a.rng = P.rng;
     a.seed = seed;
     a.key_base = 0;
@@ -1268,7 +1268,7 @@ class TabuSearch : public Solver
     cuda_check(launch_init(a, st), "init kernel");
     launches++;
     ta = TabuArgs{};
-    ta.m = model->device_view(false);
+    ta.m = model->device_view(full_maxsat_sweep);
     ta.p = P.pop;
     ta.n_walkers = R;
     ta.tenure = tenure;
@@ -1448,7 +1448,6 @@ class QuantumMonteCarlo : public Solver
   void configure(const json::Value& doc)
   {
     configure_common(*this, doc);
-    if (model->kind == K_MAXSAT) fail(1, "quantum Monte Carlo runs Ising and PUBO models here");
     Params p(params);
     // solver/quantum_monte_carlo.h:185-229
     beta_stop = p.num("beta_stop", 1.0);
@@ -1504,7 +1503,8 @@ class QuantumMonteCarlo : public Solver
     }
     // counter streams draw by position: the level-parallel kernel runs them
     // ("kernel": "warp" keeps one warp per restart)
-    use_levels = !replay && kernel != 1 && kernel != 2 && qmc_level_smem((int)trotter, P.pop.nw) > 0;
+    use_levels = !replay && kernel != 1 && kernel != 2 && qmc_level_smem((int)trotter, P.pop.nw) > 0 &&
+                 (model->kind != K_MAXSAT || full_maxsat_sweep);
     if (use_levels && !lvbuf.ptr) build_levels(st);
     device_bytes = (int64_t)(P.buf.bytes + aux.bytes + lvbuf.bytes);
     // per step: beta / P and 1 - tanh(field * beta / P), both schedules
@@ -1567,10 +1567,10 @@ class QuantumMonteCarlo : public Solver
     for (int i = 0; i < S; i++) rs[i] = Pcg(master.next()).state;
     cuda_check(cudaMemcpyAsync(P.rng, rs.data(), (size_t)S * 8, cudaMemcpyHostToDevice, st), "H2D rng");
     InitArgs a{};
-    a.m = model->device_view(false);
+    a.m = model->device_view(full_maxsat_sweep);
     a.p = P.pop;
     a.n_walkers = S;
-    a.replay = replay ? 1 : 0;
+    a.replay = replay ? (model->kind == K_MAXSAT ? 2 : 1) : (model->kind == K_MAXSAT ? 3 : 0);
     a.rng = P.rng;
     a.seed = seed;
     a.key_base = 0;
@@ -1601,7 +1601,7 @@ class QuantumMonteCarlo : public Solver
   QmcArgs args() const
   {
     QmcArgs a{};
-    a.m = model->device_view(false);
+    a.m = model->device_view(full_maxsat_sweep);
     a.p = P.pop;
     a.restarts = (int)restarts;
     a.trotter = (int)trotter;
@@ -2035,7 +2035,6 @@ class TabuParameterFree : public ParameterFreeSearch
   void configure(const json::Value& doc)
   {
     configure_common(*this, doc);
-    if (model->kind == K_MAXSAT) fail(1, "tabu search runs Ising and PUBO models here");
     Params p(params);
     min_restarts = p.integer("min_num_restarts", threads);
     if (min_restarts <= 0) fail(1, "parameter `min_num_restarts`: must be greater than 0");
@@ -2097,7 +2096,9 @@ class TabuParameterFree : public ParameterFreeSearch
     sl = std::max(sweeps, 2);
     r = (int64_t)((int)min_restarts * back / sweeps);
     if (r <= 0) fail(1, "parameter-free search reached a run with no restarts");
-    w->retarget(sl, r, tenures((size_t)r, (size_t)model->N));
+    // num_variables = get_sweep_size() (solver/tabu_parameter_free.h:78-83)
+    const size_t nv = model->kind == K_MAXSAT && !full_maxsat_sweep ? 1 : (size_t)model->N;
+    w->retarget(sl, r, tenures((size_t)r, nv));
     w->ext_master = &master;
     w->init(st);
     w->run(st);

@@ -116,3 +116,20 @@ def test_qmc_level_kernel_counter_streams(trotter):
     assert w.stats().sweep_kernel == 6
     np.testing.assert_array_equal(w.replicas()["states"], s.replicas()["states"])
     np.testing.assert_array_equal(w.replicas()["cost"], s.replicas()["cost"])
+
+
+@pytest.mark.parametrize("full", [False, True])
+@pytest.mark.parametrize("mode", ["replay", "counter"])
+def test_qmc_maxsat(full, mode):
+    """MaxSat: the sweep visits get_sweep_size() variables (1 by default)."""
+    off, ids, coef = I.weighted_maxsat(100, seed=18)
+    g = q.Model("maxsat", off=off, ids=ids, coef=coef)
+    o = O.Model("maxsat", off=off, ids=ids, coef=coef)
+    params = {"seed": 3, "sweeps": 15, "restarts": 3, "trotter_number": 8, "beta_start": 0.5,
+              "beta_stop": 3.0, "transverse_field_low": 0.2, "transverse_field_high": 2.0,
+              "rng_mode": mode, "maxsat_full_sweep": full}
+    s = q.Solver(g, QMC, {"params": params}).init().run()
+    r = O.run(o, "qmc", seed=3, step_limit=15, restarts=3, trotter_number=8,
+              sched=("linear", 0.5, 3.0), sched2=("linear", 0.2, 2.0), rng_mode=mode,
+              full_maxsat_sweep=full)
+    same(s, r)

@@ -105,3 +105,19 @@ def test_tabu_pieces_and_time_limit():
     t = q.Solver(g, TABU, {"params": dict(p, timeout=1000)}).init().run()
     same(t, O.run(o, "tabu", seed=8, step_limit=60, restarts=5, tabu_tenure=4))
     assert t.stats().kernel_launches > s.stats().kernel_launches
+
+
+@pytest.mark.parametrize("full", [False, True])
+@pytest.mark.parametrize("mode", ["replay", "counter"])
+def test_tabu_maxsat(full, mode):
+    """MaxSat sweeps get_sweep_size() variables (1, the reference's default,
+    or all with maxsat_full_sweep); states drawn one uniform() per variable."""
+    off, ids, coef = I.weighted_maxsat(120, seed=17)
+    g = q.Model("maxsat", off=off, ids=ids, coef=coef)
+    o = O.Model("maxsat", off=off, ids=ids, coef=coef)
+    params = {"seed": 5, "sweeps": 30, "restarts": 7, "tabu_tenure": 3, "rng_mode": mode,
+              "maxsat_full_sweep": full}
+    s = q.Solver(g, TABU, {"params": params}).init().run()
+    r = O.run(o, "tabu", seed=5, step_limit=30, restarts=7, tabu_tenure=3, rng_mode=mode,
+              full_maxsat_sweep=full)
+    same(s, r)

@@ -22,10 +22,9 @@ def test_parameter_errors(params, msg):
         q.Solver(m, QMC, {"params": dict({"seed": 1, "sweeps": 10}, **params)})
 
 
-def test_maxsat_refused():
+def test_maxsat_accepted():
     m = q.Model("maxsat", [(1.0, [1, 2]), (2.0, [-1, 3])])
-    with pytest.raises(q.QioError, match="Ising and PUBO"):
-        q.Solver(m, QMC, {"params": {"seed": 1}})
+    q.Solver(m, QMC, {"params": {"seed": 1, "sweeps": 5, "trotter_number": 4}}).close()
 
 
 def test_restarts_capped_like_the_reference():

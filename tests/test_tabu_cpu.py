@@ -25,10 +25,12 @@ def test_parameter_errors(params, msg):
         q.Solver(m, TABU, {"params": dict({"seed": 1}, **params)})
 
 
-def test_maxsat_refused():
+def test_maxsat_accepted():
+    """MaxSat sweeps get_sweep_size() variables: 1 unless the full sweep is
+    asked for (markov/model.h:169)."""
     m = q.Model("maxsat", [(1.0, [1, 2]), (2.0, [-1, 3])])
-    with pytest.raises(q.QioError, match="Ising and PUBO"):
-        q.Solver(m, TABU, {"params": {"seed": 1}})
+    q.Solver(m, TABU, {"params": {"seed": 1, "sweeps": 5}}).close()
+    q.Solver(m, TABU, {"params": {"seed": 1, "sweeps": 5, "maxsat_full_sweep": True}}).close()
 
 
 def test_defaults_accepted():
