@@ -114,6 +114,7 @@ def linear(a, b, stop):
 @pytest.mark.parametrize("kind,gen", [
     ("ising", lambda: I.er_ising(40, 100, seed=21)),
     ("pubo", lambda: I.random_pubo(30, 90, seed=22)),
+    ("maxsat", lambda: I.weighted_maxsat(30, seed=25)),
 ])
 def test_ssmc_oracle_matches_restatement(kind, gen):
     off, ids, coef = gen()
@@ -176,19 +177,23 @@ def test_ssmc_oracle_matches_restatement(kind, gen):
     assert best[0] + 0.0 == ref.best_cost - 0.0
 
 
-@pytest.mark.parametrize("kind,gen", [
-    ("ising", lambda: I.er_ising(30, 80, seed=23)),
-    ("pubo", lambda: I.random_pubo(25, 70, seed=24)),
+@pytest.mark.parametrize("kind,gen,full", [
+    ("ising", lambda: I.er_ising(30, 80, seed=23), False),
+    ("pubo", lambda: I.random_pubo(25, 70, seed=24), False),
+    ("maxsat", lambda: I.weighted_maxsat(25, seed=26), False),
+    ("maxsat", lambda: I.weighted_maxsat(25, seed=26), True),
 ])
-def test_qmc_oracle_matches_restatement(kind, gen):
+def test_qmc_oracle_matches_restatement(kind, gen, full):
     off, ids, coef = gen()
     m = O.Model(kind, off=off, ids=ids, coef=coef)
     seed, R, P, steps = 9, 3, 6, 12
     kw = dict(seed=seed, restarts=R, trotter_number=P, rng_mode="counter",
-              sched=("linear", 0.5, 3.0), sched2=("linear", 0.2, 2.0))
+              sched=("linear", 0.5, 3.0), sched2=("linear", 0.2, 2.0), full_maxsat_sweep=full)
     start = O.run(m, "qmc", step_limit=0, **kw)
     ref = O.run(m, "qmc", step_limit=steps, **kw)
     n = m.n_vars
+    # get_sweep_size(): 1 for MaxSat unless the full sweep is asked for
+    sw = 1 if kind == "maxsat" and not full else n
     stop = max(1, steps - 1)
     bsch, fsch = linear(0.5, 3.0, stop), linear(0.2, 2.0, stop)
     S = [np.array(start.states[i], np.uint8) for i in range(R * P)]
@@ -203,7 +208,7 @@ def test_qmc_oracle_matches_restatement(kind, gen):
         b, g = bsch(step), fsch(step)
         be, bp = b / P, 1 - math.tanh(g * b / P)
         for r in range(R):
-            for v in range(n):
+            for v in range(sw):
                 c = 2 * (step * n + v)
                 diff, bond = [], []
                 for k in range(P):
