@@ -41,7 +41,7 @@ WORKLOADS = {
                           "linear beta 0.1->5.0 over 1000 sweeps, 64 restarts, seed 0",
                      target="simulatedannealing.qiotoolkit"),
     "pa_square": dict(desc="PA on 2D periodic 256x256 +-J Ising, R=4096, 100 beta steps 0->3.0, "
-                           "10 sweeps per step, device-side multinomial resampling, counter streams",
+                           "10 sweeps per step, the reference's Poisson resampling, counter streams",
                       target="populationannealing.cpu"),
     "serving": dict(desc="Serving: Poisson arrivals at 200 req/s, 48 requests; kinds uniform over "
                          "ER Ising (mean degree U[4,16], N(0,1) FP32), PUBO (orders U{1,2,3}, N(0,1), "
@@ -125,9 +125,10 @@ def make_workload(name):
         return "ising", off, ids, coef, params
     if name == "pa_square":
         off, ids, coef = I.square_pm_j(256, seed=3)
+        # the reference's resampling (Poisson on the master PCG stream, host
+        # side) with counter walker streams (level-parallel sweeps)
         params = {"seed": 0, "sweeps": 100, "population": 4096, "beta_start": 0.0,
-                  "beta_stop": 3.0, "sweeps_per_replica": 10, "rng_mode": "counter",
-                  "resampling": "multinomial"}
+                  "beta_stop": 3.0, "sweeps_per_replica": 10, "rng_mode": "counter"}
         return "ising", off, ids, coef, params
     raise SystemExit(f"unknown workload {name}")
 
@@ -220,7 +221,9 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
     host threads (OpenMP over replicas, as the reference); default all."""
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
-    m = O.Model(kind, off=off, ids=ids, coef=coef)
+    # the Release-flag build of the oracle (the reference's cpp/CMakeLists.txt
+    # flags); the parity build checks results, this one is only timed
+    m = O.Model(kind, off=off, ids=ids, coef=coef, release=True)
     n = m.n_vars
 
     def run(restarts, sweeps):
@@ -285,8 +288,44 @@ def cpu_baseline(kind, off, ids, coef, params, budget_s=15.0, threads=None):
         a, dt, desc = run(restarts, sweeps)
     full = restarts == full_r and sweeps == full_s
     return {"value": a / dt, "unit": "flip attempts/s", "cores": threads, "kind": "port",
-            "sample": f"oracle (C++ restatement, OpenMP over replicas) {desc}"
+            "sample": f"oracle (C++ restatement, OpenMP over replicas; built with "
+                      f"{O.release_flags()}) {desc}"
                       f"{' (the full workload)' if full else ''}, {a:.3g} attempts in {dt:.2f} s"}
+
+
+def parity_check(kind, off, ids, coef, params, solver):
+    """Recompute the timed solve's walkers on the oracle (outside the timed
+    region) and compare them with the GPU's: costs, lowest costs, counts and
+    states must be equal (the parity build of the oracle, replayed streams
+    restated exactly).  PT checks the first ladder (the reference run seeded
+    `seed`), SA every restart; other solvers report checked: false."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    mode = params.get("rng_mode", "replay")
+    if "temperatures" in params:
+        t = params["temperatures"]
+        sl, what = slice(0, t["count"]), f"first ladder ({t['count']} walkers)"
+        run = dict(solver="pt", step_limit=params["sweeps"], sched=(t["type"], t["initial"], t["final"]),
+                   sched_count=t["count"], use_inverse=False)
+    elif "beta_start" in params and not any(k in params for k in ("population", "trotter_number",
+                                                                   "target_population", "tabu_tenure")):
+        sl, what = slice(None), f"all {params['restarts']} restarts"
+        run = dict(solver="sa", step_limit=params["sweeps"], restarts=params["restarts"],
+                   sched=("linear", params["beta_start"], params["beta_stop"]))
+    else:
+        return {"checked": False, "why": "no in-bench oracle recompute for this solver "
+                                         "(its parity is in tests/)"}
+    t0 = time.perf_counter()
+    m = O.Model(kind, off=off, ids=ids, coef=coef)
+    r = O.run(m, seed=params["seed"], threads=threads, rng_mode=mode, **run)
+    dt = time.perf_counter() - t0
+    rep = solver.replicas()
+    fields = {"cost": r.cost, "lowest": r.lowest, "attempts": r.attempts, "accepts": r.accepts,
+              "states": r.states, "lowest_states": r.lowest_states}
+    bad = [k for k, v in fields.items() if not np.array_equal(np.asarray(rep[k])[sl], v)]
+    return {"checked": True, "equal": not bad, "mismatched": bad, "walkers": what,
+            "compared": "final and lowest costs, attempt/accept counts, final and lowest states",
+            "oracle_s": round(dt, 2)}
 
 
 def dist_setup():
@@ -339,7 +378,8 @@ def run_reference(args, ws, rank):
                     "d2h_bytes_per_step": 0},
             "note": "the reference's own build needs rapidjson/pcg-cpp/googletest/protobuf "
                     "fetched at configure time (no network); timed: the oracle's C++ "
-                    "restatement of its CPU path with OpenMP over replicas"}
+                    "restatement of its CPU path with OpenMP over replicas, built with the "
+                    "reference's Release flags (" + O.release_flags() + ")"}
     print(json.dumps(line), flush=True)
 
 
@@ -352,6 +392,8 @@ def main():
     ap.add_argument("--workload", default="pt_pubo", choices=list(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle recompute of the timed solve")
     ap.add_argument("--sweeps", type=int, default=None,
                     help="override the workload's sweeps (small cases for profiler captures)")
     args = ap.parse_args()
@@ -408,10 +450,12 @@ def main():
     st0 = None
     for _ in range(args.warmup):
         _, st0, _ = one_step()
-    if target in ("tabu.qiotoolkit", "substochasticmontecarlo.cpu"):
+    if target in ("tabu.qiotoolkit", "substochasticmontecarlo.cpu") or \
+            (target == "populationannealing.cpu" and params.get("resampling") != "multinomial"):
         # evaluations depend on the run (a tabu scan stops at the first
-        # improving flip; SSMC flips with probability alpha): count them
-        # (deterministic for the fixed seed)
+        # improving flip; SSMC flips with probability alpha; a Poisson-resampled
+        # population varies in size): count them (deterministic for the fixed
+        # seed)
         if st0 is None:
             _, st0, _ = one_step()
         A = int(st0.attempts)
@@ -454,6 +498,10 @@ def main():
     peak, peak_src = peaks()
     traffic = committed_traffic(args.workload)
 
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = parity_check(kind, off, ids, coef, params, solver)
+
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(q, kind, off, ids, coef, params, target, A, args, stream)
@@ -483,8 +531,11 @@ def main():
                          "avg_launch_ms": avg_sweep_launch_ms},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
+            "parity": parity,
         }
         print(json.dumps(line), flush=True)
+        if parity and parity.get("checked") and not parity["equal"]:
+            sys.exit(f"parity check failed: {parity['mismatched']}")
 
 
 def serving_requests(n=48, rate=200.0, seed=4):
@@ -685,7 +736,7 @@ def main_serving(args, ws, rank):
         t_cpu, a_cpu = 0.0, 0
         for j in range(0, len(reqs), 6):
             _, k, (o, i, c), target, p = reqs[j]
-            om = O.Model(k, off=o, ids=i, coef=c)
+            om = O.Model(k, off=o, ids=i, coef=c, release=True)
             t0 = time.perf_counter()
             if target.startswith("parallel"):
                 O.run(om, "pt", seed=p["seed"], step_limit=p["sweeps"], threads=threads,
@@ -822,7 +873,7 @@ def main_batch(args, ws, rank):
             if L in L_seen or L % 4:
                 continue
             L_seen.add(L)
-            om = O.Model("ising", off=o, ids=i, coef=c)
+            om = O.Model("ising", off=o, ids=i, coef=c, release=True)
             t0 = time.perf_counter()
             O.run(om, "sa", seed=0, step_limit=params["sweeps"], restarts=params["restarts"],
                   threads=threads, sched=("linear", params["beta_start"], params["beta_stop"]))

@@ -160,10 +160,13 @@ qio_status qio_states_cost(const qio_model* model, int64_t n_states,
  * 1 MiB array inside the library: n_states * ceil(n_vars / 32) must not
  * exceed 262144 words (QIO_INVALID_ARGUMENT otherwise).  All calls share it:
  * overlapping calls (other streams or threads) race and must be serialised
- * by the caller.  The first call on a device looks up the array's address;
- * make it before any stream capture.  The model must already be on the
- * current device (an earlier qio_states_cost or solver call).  Results equal
- * qio_states_cost's; the call is asynchronous on `stream`. */
+ * by the caller.  The first call on a device looks up the array's address
+ * and loads the kernels of every model flavour; make it before any stream
+ * capture.  The model must already be on the current device (an earlier
+ * qio_states_cost or solver call there; another current device is
+ * QIO_INVALID_ARGUMENT), and states / costs must be device (or managed)
+ * memory of that device (host pointers are QIO_INVALID_ARGUMENT).  Results
+ * equal qio_states_cost's; the call is asynchronous on `stream`. */
 qio_status qio_states_cost_noalloc(const qio_model* model, int64_t n_states,
                                    const uint8_t* states, double* costs, void* stream);
 /* calculate_cost_difference(state q, vars[q]) for n queries. */

@@ -15,8 +15,11 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libqio_oracle.so")
+# the same source built with the reference's Release flags (-Ofast,
+# -march=native): for timing the CPU baseline only, never for checking results
+_REL_PATH = os.path.join(_HERE, "_build", "libqio_oracle_release.so")
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 ISING, ISING_PLAIN, PUBO, PUBO_PLAIN, MAXSAT = 0, 1, 2, 3, 4
 SA, PT, PA, TABU, SSMC, QMC = 0, 1, 2, 3, 4, 5
@@ -55,20 +58,33 @@ class Params(C.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with make (g++; a few seconds)."""
+    """Compile the oracle with make (g++; a few seconds): the parity build and
+    the Release-flag timing build."""
     with _lock:
         src = os.path.join(_HERE, "qio_oracle.cc")
-        if force or not os.path.exists(_LIB_PATH) or \
-                os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
-            subprocess.run(["make", "-s", "-C", _HERE], check=True)
+        stale = any(not os.path.exists(f) or os.path.getmtime(f) < os.path.getmtime(src)
+                    for f in (_LIB_PATH, _REL_PATH))
+        if force or stale:
+            subprocess.run(["make", "-s", "-j2", "-C", _HERE] + (["-B"] if force else []),
+                           check=True)
     return _LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def release_flags() -> str:
+    """The compiler flags of the Release-flag timing build."""
+    try:
+        with open(os.path.join(_HERE, "_build", "release_flags.txt")) as f:
+            return f.read().strip()
+    except OSError:
+        return ""
+
+
+def lib(release: bool = False):
+    """The oracle library: the parity build, or with release=True the
+    Release-flag build (timing only)."""
+    if release not in _libs:
         build()
-        L = C.CDLL(_LIB_PATH)
+        L = C.CDLL(_REL_PATH if release else _LIB_PATH)
         vp, i64, u32, dbl, ip = C.c_void_p, C.c_int64, C.c_uint32, C.c_double, C.c_int
         P = C.POINTER
         L.orc_pcg_stream.argtypes = [u32, ip, ip, P(C.c_uint32)]
@@ -120,8 +136,8 @@ def lib():
         L.orc_res_destroy.argtypes = [vp]
         L.orc_pt_toy.argtypes = [u32, i64, P(dbl), ip, ip, P(dbl), P(dbl)]
         L.orc_pt_toy.restype = ip
-        _lib = L
-    return _lib
+        _libs[release] = L
+    return _libs[release]
 
 
 def _p(a, ct):
@@ -190,7 +206,10 @@ def flatten_terms(terms):
 
 
 class Model:
-    def __init__(self, kind, terms=None, *, off=None, ids=None, coef=None):
+    """release=True builds the model in the Release-flag library (timing
+    only); run() then uses that library too."""
+
+    def __init__(self, kind, terms=None, *, off=None, ids=None, coef=None, release=False):
         if isinstance(kind, str):
             kind = KIND_BY_NAME[kind]
         if terms is not None:
@@ -199,49 +218,50 @@ class Model:
         self.ids = np.ascontiguousarray(ids, np.int32)
         self.coef = np.ascontiguousarray(coef, np.float64)
         self.kind = kind
+        self.L = lib(release)
         err = C.create_string_buffer(512)
-        self.h = lib().orc_model_create(kind, len(self.coef), _p(self.off, C.c_int64),
+        self.h = self.L.orc_model_create(kind, len(self.coef), _p(self.off, C.c_int64),
                                         _p(self.ids, C.c_int32), _p(self.coef, C.c_double),
                                         err, 512)
         if not self.h:
             raise ValueError(err.value.decode())
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
-            _lib.orc_model_destroy(self.h)
+        if getattr(self, "h", None) and getattr(self, "L", None) is not None:
+            self.L.orc_model_destroy(self.h)
             self.h = None
 
     @property
     def n_vars(self):
-        return lib().orc_model_n_vars(self.h)
+        return self.L.orc_model_n_vars(self.h)
 
     @property
     def n_terms(self):
-        return lib().orc_model_n_terms(self.h)
+        return self.L.orc_model_n_terms(self.h)
 
     @property
     def const_cost(self):
-        return lib().orc_model_const_cost(self.h)
+        return self.L.orc_model_const_cost(self.h)
 
     @property
     def scale_factor(self):
-        return lib().orc_model_scale_factor(self.h)
+        return self.L.orc_model_scale_factor(self.h)
 
     def var_names(self):
         out = np.zeros(self.n_vars, np.int32)
-        lib().orc_model_var_names(self.h, _p(out, C.c_int32))
+        self.L.orc_model_var_names(self.h, _p(out, C.c_int32))
         return out
 
     def cost(self, spins):
         s = np.ascontiguousarray(spins, np.uint8)
-        return lib().orc_state_cost(self.h, _p(s, C.c_uint8))
+        return self.L.orc_state_cost(self.h, _p(s, C.c_uint8))
 
     def cost_difference(self, spins, var):
         s = np.ascontiguousarray(spins, np.uint8)
-        return lib().orc_state_cost_difference(self.h, _p(s, C.c_uint8), int(var))
+        return self.L.orc_state_cost_difference(self.h, _p(s, C.c_uint8), int(var))
 
     def twister_min(self, seed, iters, T):
-        return lib().orc_model_twister_min(self.h, seed, iters, T)
+        return self.L.orc_model_twister_min(self.h, seed, iters, T)
 
 
 def schedule(kind="linear", initial=0.0, final=0.0, values=None, start=None,
@@ -262,9 +282,8 @@ def schedule(kind="linear", initial=0.0, final=0.0, values=None, start=None,
 
 
 class Result:
-    def __init__(self, h):
+    def __init__(self, h, L):
         self.h = h
-        L = lib()
         n = L.orc_res_n_replicas(h)
         self.n_vars = L.orc_res_n_vars(h)
         self.last_step = L.orc_res_last_step(h)
@@ -350,11 +369,11 @@ def run(model: Model, solver="sa", *, seed=0, step_limit=100, restarts=1,
         p.n_tabu_tenures = len(keep_ten)
     p.trotter_number = int(trotter_number)
     err = C.create_string_buffer(512)
-    h = lib().orc_run(model.h, C.byref(p), err, 512)
+    h = model.L.orc_run(model.h, C.byref(p), err, 512)
     del keep, keep_ten
     if not h:
         raise ValueError(err.value.decode())
-    return Result(h)
+    return Result(h, model.L)
 
 
 def qexp(x):

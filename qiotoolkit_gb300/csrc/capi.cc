@@ -227,6 +227,25 @@ qio_status qio_states_cost_noalloc(const qio_model* model, int64_t n, const uint
     if (!m.uploaded)
       fail(1, "qio_states_cost_noalloc: the model is not on the device yet; run it on the GPU "
               "once (qio_states_cost or a solver) before the allocation-free call");
+    int cur = -1;
+    cuda_check(cudaGetDevice(&cur), "cudaGetDevice");
+    if (cur != m.upload_device)
+      fail(1, "qio_states_cost_noalloc: the model is on device " + std::to_string(m.upload_device) +
+                  " but device " + std::to_string(cur) + " is current");
+    // both buffers must be device memory: a host pointer would fault the kernel
+    for (const void* ptr : {(const void*)states, (const void*)costs})
+    {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess)
+      {
+        (void)cudaGetLastError();
+        fail(1, "qio_states_cost_noalloc: states and costs must be device pointers");
+      }
+      if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+        fail(1, "qio_states_cost_noalloc: states and costs must be device pointers");
+      if (at.type == cudaMemoryTypeDevice && at.device != cur)
+        fail(1, "qio_states_cost_noalloc: states and costs must be on the current device");
+    }
     const int64_t nw = m.N > 0 ? (m.N + 31) / 32 : 1;
     if (n > INT32_MAX || n * nw > (int64_t)kNoAllocScratchWords)
       fail(1, "qio_states_cost_noalloc: " + std::to_string(n) + " states of " + std::to_string(m.N) +

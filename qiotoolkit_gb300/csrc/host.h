@@ -86,6 +86,7 @@ struct HostModel
   mutable DevBuf dmem;
   mutable DevModel dev{};
   mutable bool uploaded = false;
+  mutable int upload_device = -1;  // CUDA ordinal that holds dmem
 
   bool empty() const { return N == 0; }
   void upload() const;

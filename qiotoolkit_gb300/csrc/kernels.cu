@@ -1532,8 +1532,9 @@ cudaError_t launch_pt_swap(const SwapArgs& a, cudaStream_t s)
 // zero.  All calls on one device share the array: calls that overlap in
 // time (different streams or host threads) race on it and must be
 // serialised by the caller.  The first call on each device looks up the
-// array's device address (cudaGetSymbolAddress) with that device current;
-// make that first call before any stream capture.
+// array's device address (cudaGetSymbolAddress) with that device current and
+// loads the kernel of every model flavour (cudaFuncGetAttributes), so later
+// calls load nothing; make that first call before any stream capture.
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords];
 
@@ -1587,6 +1588,23 @@ cudaError_t launch_eval_cost_noalloc(const DevModel& m, int n, const uint8_t* st
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess) return e;
+      // load every flavour's kernel now, so that no later call (another model
+      // flavour) loads a module lazily inside a capture
+      cudaFuncAttributes fa;
+      const void* fns[] = {
+          (const void*)eval_cost_noalloc_kernel<F_PARITY, true>,
+          (const void*)eval_cost_noalloc_kernel<F_PARITY, false>,
+          (const void*)eval_cost_noalloc_kernel<F_COUNTER, true>,
+          (const void*)eval_cost_noalloc_kernel<F_COUNTER, false>,
+          (const void*)eval_cost_noalloc_kernel<F_PLAIN_ISING, true>,
+          (const void*)eval_cost_noalloc_kernel<F_PLAIN_ISING, false>,
+          (const void*)eval_cost_noalloc_kernel<F_PLAIN_PUBO, true>,
+          (const void*)eval_cost_noalloc_kernel<F_PLAIN_PUBO, false>};
+      for (const void* f : fns)
+      {
+        e = cudaFuncGetAttributes(&fa, f);
+        if (e != cudaSuccess) return e;
+      }
       addr[dev] = (uint32_t*)p;
     }
     scratch = addr[dev];

@@ -589,6 +589,9 @@ void HostModel::upload() const
   dev.n_levels = lv_ok ? n_levels : 0;
   dev.lv_recs = lv_ok ? lv_recs : 0;
   dev.lv_d8 = lv_d8 ? 1 : 0;
+  int ordinal = -1;
+  cuda_check(cudaGetDevice(&ordinal), "cudaGetDevice");
+  upload_device = ordinal;
   uploaded = true;
 }
 

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own tests.
 
-Run in a container where the QIOToolkit reference is mounted (read-only) at
-REFERENCE (default /root/reference).  The GPU machine never runs this script; it
-uses the committed JSON files.
+Run where a QIOToolkit checkout is readable, giving its root directory as the
+first argument or in QIO_REFERENCE.  Tests never run this script; they use
+the committed JSON files.
 
 Sources (paths relative to the reference's cpp/ or data/ directory):
   rng_pins.json      utils/test/random_generator_test.cc:18-79
@@ -43,7 +43,9 @@ import os
 import re
 import sys
 
-REFERENCE = os.environ.get("QIO_REFERENCE", "/root/reference")
+REFERENCE = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QIO_REFERENCE", "")
+if not REFERENCE:
+    sys.exit("usage: make_golden.py <QIOToolkit checkout> (or set QIO_REFERENCE)")
 CPP = os.path.join(REFERENCE, "cpp")
 DATA = os.path.join(REFERENCE, "data")
 OUT = os.path.dirname(os.path.abspath(__file__))

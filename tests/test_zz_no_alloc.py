@@ -37,10 +37,19 @@ def _models():
     yield "ising", q.Model("ising", off=off, ids=ids, coef=coef)
     off, ids, coef = I.random_pubo(257, 800, seed=7, integer=True)
     yield "pubo_int", q.Model("pubo", off=off, ids=ids, coef=coef)
+    off, ids, coef = I.er_ising(200, 600, seed=9)
+    yield "ising_plain", q.Model("ising_plain", off=off, ids=ids, coef=coef)
+    off, ids, coef = I.random_pubo(220, 700, seed=10)
+    yield "pubo_plain", q.Model("pubo_plain", off=off, ids=ids, coef=coef)
+    off, ids, coef = I.weighted_maxsat(150, seed=12)
+    yield "maxsat", q.Model("maxsat", off=off, ids=ids, coef=coef)
+
+
+NAMES = ["pubo", "ising", "pubo_int", "ising_plain", "pubo_plain", "maxsat"]
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["pubo", "ising", "pubo_int"])
+@pytest.mark.parametrize("name", NAMES)
 def test_noalloc_cost_equals_states_cost(name):
     model = dict(_models())[name]
     rng = np.random.default_rng(11)
@@ -64,3 +73,28 @@ def test_noalloc_rejects_oversized_batches():
     d_out = torch.zeros(n, dtype=torch.float64, device="cuda")
     with pytest.raises(QioError, match="scratch words; the maximum is 262144"):
         _noalloc(model, d_states, d_out)
+
+
+@pytest.mark.gpu
+def test_noalloc_refuses_a_model_not_yet_on_the_device():
+    off, ids, coef = I.er_ising(64, 150, seed=13)
+    model = q.Model("ising", off=off, ids=ids, coef=coef)  # never run on the GPU
+    d_states = torch.zeros((2, model.n_vars), dtype=torch.uint8, device="cuda")
+    d_out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    with pytest.raises(QioError, match="not on the device yet"):
+        _noalloc(model, d_states, d_out)
+
+
+@pytest.mark.gpu
+def test_noalloc_refuses_host_buffers():
+    off, ids, coef = I.er_ising(64, 150, seed=14)
+    model = q.Model("ising", off=off, ids=ids, coef=coef)
+    model.calculate_cost(np.zeros((1, model.n_vars), np.uint8))
+    states = np.zeros((2, model.n_vars), np.uint8)
+    out = np.zeros(2)
+    stream = torch.cuda.current_stream().cuda_stream
+    with pytest.raises(QioError, match="must be device pointers"):
+        check(load().qio_states_cost_noalloc(model._h, 2,
+                                             ctypes.c_void_p(states.ctypes.data),
+                                             ctypes.c_void_p(out.ctypes.data),
+                                             ctypes.c_void_p(stream)))
