@@ -90,7 +90,8 @@ def batch_instances(n=512):
 
 # the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
 KERNEL_NAMES = {1: "sweep_kernel", 2: "lw_sweep_kernel", 3: "lv_sweep_kernel + lv_lowest_kernel",
-                4: "tabu_kernel", 5: "ssmc_walk_kernel", 6: "qmc_kernel", 7: "qmc_level_kernel"}
+                4: "tabu_kernel", 5: "ssmc_walk_kernel", 6: "qmc_kernel", 7: "qmc_level_kernel",
+                8: "fc_sweep_kernel"}
 
 
 def make_workload(name):
@@ -463,12 +464,14 @@ def main():
     torch.cuda.synchronize()
     ms, sweep_ms, launches, att = [], [], 0, 0
     kernel_used = 1
+    windows = (0, 0)
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             t, st, n_launch = one_step()
             ms.append(t)
             sweep_ms.append(st.sweep_kernel_ms)
             kernel_used = int(st.sweep_kernel)
+            windows = (int(st.windows), int(st.attempts))
             launches += n_launch
             att += int(st.attempts)
     torch.cuda.synchronize()
@@ -528,7 +531,8 @@ def main():
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_src, "kernel": KERNEL_NAMES.get(kernel_used, "sweep_kernel"),
                          "bytes_per_attempt": bpa,
-                         "avg_launch_ms": avg_sweep_launch_ms},
+                         "avg_launch_ms": avg_sweep_launch_ms,
+                         "attempts_per_window": (windows[1] / windows[0]) if windows[0] else None},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "parity": parity,

@@ -92,7 +92,8 @@ typedef struct qio_solver_stats {
                               5 substochastic Monte Carlo walker steps,
                               6 quantum Monte Carlo (one warp per restart),
                               7 quantum Monte Carlo level schedule (counter
-                              streams, one block per restart) */
+                              streams, one block per restart), 8 cached
+                              local fields (two warps per walker) */
 } qio_solver_stats;
 
 /* ---- library ---------------------------------------------------------- */

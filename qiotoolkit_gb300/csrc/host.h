@@ -66,6 +66,10 @@ struct HostModel
   std::vector<int> rec_i;     // 2 ints per incidence (integer mode)
   std::vector<double> rec_f;  // 2 doubles per incidence: (other as bits, coef)
   std::vector<unsigned int> rec_p;  // other << 8 | coefficient, when |coef| <= 127
+  // field-cached sweep records (16 bytes per incidence; see DevModel::fc_rec)
+  std::vector<uint32_t> fc_rec;
+  int fc_S = 0;
+  bool fc_pack = false;
   // level schedule (levels.cu): entries grouped by level, their offsets
   std::vector<int> lv_off, lv_pos;
   std::vector<uint32_t> lv_ent;
@@ -198,7 +202,8 @@ class Solver
   bool profile = false;  // bracket every sweep launch with CUDA events
   bool smem_state = true;  // walker state in shared memory when it fits
   int kernel = 0;          // sweep kernel: 0 auto, 1 one walker per warp, 2 one walker per lane,
-                           // 3 level schedule (one walker per warp, counter streams)
+                           // 3 level schedule (one walker per warp, counter streams),
+                           // 4 cached local fields (two warps per walker)
   // CUDA-event pairs around sweep launches (profile mode)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   size_t prof_used = 0;

@@ -1391,6 +1391,8 @@ cudaError_t launch_pa_copy(const DevPop& src, const DevPop& dst, const int* src_
 // ---------------------------------------------------------------------------
 void sw_upload(const double* ln, const float* scr, const unsigned long long* jA,
                const unsigned long long* jC);
+void fc_upload(const double* ln, const float* scr, const unsigned long long* jA,
+               const unsigned long long* jC);
 
 void upload_tables(int)
 {
@@ -1438,6 +1440,7 @@ void upload_tables(int)
       e[2] = (float)(ldexp(fabs(y0) + fabs(dy), -19));
     }
   sw_upload(ln, scr, jA, jC);
+  fc_upload(ln, scr, jA, jC);
   lw_upload(ln, scr);
   lv_upload(ln, scr);
 }

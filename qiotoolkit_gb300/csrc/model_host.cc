@@ -312,6 +312,65 @@ static void build_near(HostModel& m)
     }
 }
 
+// Records of the field-cached sweep.  The local field of a variable is the
+// sum, over its contributing incidences, of the coefficients in fixed point
+// q = round(c * 2^S): Ising, every incidence, +q for a term whose parity bit
+// is clear and -q otherwise (the cost difference is -2 times the sum);
+// counter models, the incidences whose term the flip would switch, +q when
+// the variable's literal is true and -q otherwise.  S is the largest scale
+// with 2^S * max_v sum_row |c| <= 2^30 (2^22 when the field also carries the
+// count of contributing incidences in its low 8 bits), so a field never
+// overflows and differs from the reference's FP64 sum by less than deg + 1
+// units.  Integer models use S = 0: the field is then the exact difference.
+// Eligible: Ising with the term cache or counter models, fewer than 32766
+// variables, rows of at most 255 incidences.
+static void build_fields(HostModel& m)
+{
+  m.fc_rec.clear();
+  if (!(m.flavor == F_PARITY || m.flavor == F_COUNTER) || m.N == 0 || m.N >= 32766) return;
+  double amax = 0;
+  for (int64_t v = 0; v < m.N; v++)
+  {
+    if (m.row[v + 1] - m.row[v] > 255) return;
+    double s = 0;
+    for (int q = m.row[v]; q < m.row[v + 1]; q++) s += std::fabs(m.coef[q]);
+    amax = std::max(amax, s);
+  }
+  m.fc_pack = !m.int_mode && m.flavor == F_COUNTER;
+  if (m.int_mode) m.fc_S = 0;
+  else
+  {
+    const int top = m.fc_pack ? 22 : 30;
+    int e = 0;
+    if (amax > 0) std::frexp(amax, &e);  // amax < 2^e
+    m.fc_S = amax > 0 ? top - e : 0;
+    if (m.fc_S < -900 || m.fc_S > 900) return;  // 2^-S must stay a normal double
+  }
+  m.fc_rec.assign((size_t)m.K * 4, 0u);
+  for (int64_t v = 0; v < m.N; v++)
+    for (int q = m.row[v]; q < m.row[v + 1]; q++)
+    {
+      const uint32_t t = m.inc[q] & ~kNegBit;
+      long long fq = m.int_mode ? (long long)m.coef_i[q] : std::llrint(std::ldexp(m.coef[q], m.fc_S));
+      if (m.fc_pack) fq *= 256;
+      uint32_t co[3] = {0xFFFFu, 0xFFFFu, 0xFFFFu};
+      int nco = 0;
+      for (int j = m.trow[t]; j < m.trow[t + 1]; j++)
+      {
+        const uint32_t u = m.tvar[j] & ~kNegBit;
+        if ((int64_t)u == v) continue;
+        if (nco < 3) co[nco] = u | ((m.tvar[j] & kNegBit) ? 0x8000u : 0u);
+        nco++;
+      }
+      if (nco > 3) nco = 15;
+      uint32_t* r = &m.fc_rec[(size_t)q * 4];
+      r[0] = m.inc[q];
+      r[1] = (uint32_t)(int32_t)fq;
+      r[2] = co[0] | (co[1] << 16);
+      r[3] = co[2] | ((uint32_t)nco << 16);
+    }
+}
+
 // Integer mode: every coefficient is an integer of magnitude <= 2^20 and the
 // per-variable sums stay below 2^30, so int32/int64 arithmetic gives the same
 // values as the reference's FP64 sums (all partial sums are exact).
@@ -393,6 +452,7 @@ std::unique_ptr<HostModel> build_model(int kind, int64_t n_terms,
                         : 1.0 / m->max_coupling;
   build_nbr(*m);
   detect_int_mode(*m);
+  build_fields(*m);
   if (m->flavor == F_PARITY || m->flavor == F_COUNTER) build_near(*m);
   if (m->flavor == F_PARITY)
   {
@@ -548,7 +608,8 @@ void HostModel::upload() const
          o_tvar = put(blob, tvar), o_tc = put(blob, tcost), o_tci = put(blob, tcost_i),
          o_cf = put(blob, coef_f), o_near = put(blob, near), o_oth = put(blob, other),
          o_ri = put(blob, rec_i), o_rf = put(blob, rec_f), o_rp = put(blob, rec_p),
-         o_lo = put(blob, lv_off), o_le = put(blob, lv_ent), o_lp = put(blob, lv_pos);
+         o_lo = put(blob, lv_off), o_le = put(blob, lv_ent), o_lp = put(blob, lv_pos),
+         o_fc = put(blob, fc_rec);
   // 256 bytes of tail padding: bulk copies of incidence ranges round their
   // end up to 16 bytes
   blob.resize(((blob.size() + 255) & ~(size_t)255) + 256);
@@ -589,6 +650,10 @@ void HostModel::upload() const
   dev.n_levels = lv_ok ? n_levels : 0;
   dev.lv_recs = lv_ok ? lv_recs : 0;
   dev.lv_d8 = lv_d8 ? 1 : 0;
+  dev.fc_rec = fc_rec.empty() ? nullptr : (const uint4*)(b + o_fc);
+  dev.fc_S = fc_S;
+  dev.fc_pack = fc_pack ? 1 : 0;
+  dev.fc_inv = std::ldexp(1.0, -fc_S);
   int ordinal = -1;
   cuda_check(cudaGetDevice(&ordinal), "cudaGetDevice");
   upload_device = ordinal;

@@ -83,6 +83,15 @@ struct DevModel
   const uint32_t* tvar;    // K  members (| kNegBit for negated literals)
   const double* tcost;     // n_terms
   const int* tcost_i;      // n_terms
+  // field-cached sweep (fields.cu): one 16-byte record per incidence, in
+  // row order: x = inc (term | kNegBit), y = the coefficient in fixed point
+  // (round(c * 2^fc_S), shifted left 8 when fc_pack), z = co-members 0 and 1,
+  // w = co-member 2 | count << 16 (count 15: more than three, read trow /
+  // tvar); a co-member is id | 0x8000 for a negated literal, 0xFFFF none
+  const uint4* fc_rec;     // K, or null when the model does not qualify
+  int fc_S;                // fixed-point scale exponent
+  int fc_pack;             // FP64 counter models: field = fixed << 8 | count
+  double fc_inv;           // 2^-fc_S
 };
 
 // Walker population in HBM (structure of arrays).  Spins are bit-packed,
@@ -125,6 +134,11 @@ struct SweepArgs
   int smem_state;       // stage spins + term state in shared memory
   int* err;             // device error flag (a bounded wait gave up)
   long long tag;        // written to p.lowtag[walker] when its lowest drops
+  // field-cached sweep: per slot the fixed-point local field of every
+  // variable (fc_words(N) ints), kept between launches; null selects the
+  // windowed kernel.  field_valid = 0: rebuild the fields from the state.
+  int* field;
+  int field_valid;
 };
 
 struct InitArgs
@@ -148,6 +162,11 @@ struct InitArgs
 void upload_tables(int device);  // ln table + PCG jump tables
 cudaError_t launch_init(const InitArgs& a, cudaStream_t s);
 cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int warps_per_block);
+// field-cached sweep (fields.cu): ints of one slot's fields, and whether the
+// kernel can run this model with this population layout
+int64_t fc_words(int n_vars);
+bool fc_fits(const DevModel& m, int nw, int mp);
+cudaError_t launch_fc_sweep(const SweepArgs& a, cudaStream_t s);
 cudaError_t launch_eval_cost(const DevModel& m, int n_states,
                              const uint32_t* spins, int nw, double* out,
                              cudaStream_t s);

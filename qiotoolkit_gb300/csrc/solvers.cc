@@ -133,7 +133,8 @@ static void configure_common(Solver& s, const json::Value& doc)
   else if (kern == "warp") s.kernel = 1;
   else if (kern == "lanes") s.kernel = 2;
   else if (kern == "levels") s.kernel = 3;
-  else fail(1, "parameter `kernel` must be \"auto\", \"warp\", \"lanes\" or \"levels\"");
+  else if (kern == "fields") s.kernel = 4;
+  else fail(1, "parameter `kernel` must be \"auto\", \"warp\", \"lanes\", \"levels\" or \"fields\"");
   s.output_params.push_back({"seed", std::to_string(s.seed)});
   s.output_params.push_back({"step_limit", std::to_string(s.step_limit)});
 }
@@ -190,6 +191,18 @@ struct Population
   uint64_t* rng = nullptr;
   int* slot_of = nullptr;
   double* beta = nullptr;
+  // cached local fields of the field-cached sweep, per slot; fvalid: they
+  // match the slots' states (false after anything else changed the states)
+  DevBuf fbuf;
+  int* field = nullptr;
+  bool fvalid = false;
+
+  void ensure_fields(int64_t N)
+  {
+    if (field) return;
+    fbuf = DevBuf((size_t)n * (size_t)fc_words((int)N) * 4);
+    field = (int*)fbuf.ptr;
+  }
 
   void alloc(const HostModel& m, int slots, int streams, bool need_slots,
              int64_t n_beta)
@@ -445,6 +458,25 @@ bool levels_for(const Solver& s, const HostModel& m)
   return !s.replay && levels_eligible(m) && m.N >= 4096;
 }
 
+// The field-cached sweep: Ising with the term cache or counter models
+// (PUBO, MaxSat with full sweeps) whose walker state, fields and record tiles
+// fit a block's shared memory.  auto: whenever it fits; "warp" keeps the
+// windowed kernel.
+bool fields_for(const Solver& s, const HostModel& m, const Population& P, bool full_maxsat_sweep)
+{
+  const bool ok = !m.empty() && !m.fc_rec.empty() && s.smem_state &&
+                  fc_fits(m.device_view(full_maxsat_sweep), P.pop.nw, P.pop.mp);
+  if (s.kernel == 4)
+  {
+    if (!ok)
+      fail(1, "parameter `kernel`: \"fields\" needs an Ising (term-cached) or counter model of fewer "
+              "than 32766 variables with rows of at most 255 incidences, every variable in a sweep, "
+              "and walker state that fits shared memory");
+    return true;
+  }
+  return s.kernel == 0 && ok;
+}
+
 // beta as Metropolis::set_beta / set_temperature store it
 // (markov/metropolis.h:35-61)
 static double beta_of(double value, bool inverse)
@@ -465,7 +497,7 @@ class SimulatedAnnealing : public Solver
   Population P;
   std::vector<double> betas;
   LaneRunner L;
-  bool lanes = false, levels = false;
+  bool lanes = false, levels = false, fields = false;
   LevelLog lvlog;
   Pcg* ext_master = nullptr;  // repeated runs: the restarts fork from this stream
 
@@ -571,7 +603,14 @@ class SimulatedAnnealing : public Solver
     a.key_div = (long long)1 << 40;
     levels = levels_for(*this, *model);
     lanes = !levels && lanes_for(*this, *model, restarts);
-    used_kernel = levels ? 3 : (lanes ? 2 : 1);
+    fields = !levels && !lanes && fields_for(*this, *model, P, full_maxsat_sweep);
+    if (fields)
+    {
+      P.ensure_fields(model->N);
+      P.fvalid = false;
+      device_bytes = (int64_t)(P.buf.bytes + P.fbuf.bytes);
+    }
+    used_kernel = levels ? 3 : (lanes ? 2 : (fields ? 8 : 1));
     // the lane and level sweeps work from the spins and rebuild the term
     // bytes when they finish
     a.skip_terms = (levels || lanes) ? 1 : 0;
@@ -644,7 +683,10 @@ class SimulatedAnnealing : public Solver
     {
       a.sweep_base = base;
       a.n_sweeps = (int)n;
+      a.field = fields ? P.field : nullptr;
+      a.field_valid = P.fvalid ? 1 : 0;
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+      P.fvalid = fields;
     }
     prof_end(st);
     launches++;
@@ -806,6 +848,7 @@ class ParallelTempering : public Solver
   std::vector<double> temps;   // sorted
   std::vector<double> betas;   // per position
   Population P;
+  bool fields = false;         // field-cached sweep
   DevBuf aux;
   int* dir = nullptr;
   double *obs_acc = nullptr, *obs_cost = nullptr, *obs_dir = nullptr;
@@ -965,6 +1008,14 @@ class ParallelTempering : public Solver
     a.key_base = 0;
     a.key_div = T();
     cuda_check(launch_init(a, st), "init kernel");
+    fields = fields_for(*this, *model, P, full_maxsat_sweep);
+    if (fields)
+    {
+      P.ensure_fields(model->N);
+      device_bytes += (int64_t)P.fbuf.bytes;
+    }
+    P.fvalid = false;
+    used_kernel = fields ? 8 : 1;
     cuda_check(cudaStreamSynchronize(st), "sync");
     // the sweep/swap loop keeps its own copies of the stream so that a
     // host-side pageable copy above cannot race with kernels
@@ -1021,9 +1072,12 @@ class ParallelTempering : public Solver
     {
       a.sweep_base = s * spr;
       a.tag = s;  // the step, for the time order of equal lowest costs
+      a.field = fields ? P.field : nullptr;
+      a.field_valid = P.fvalid ? 1 : 0;
       prof_begin(st);
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
       prof_end(st);
+      P.fvalid = fields;
       sw.step = s;
       cuda_check(launch_pt_swap(sw, st), "swap kernel");
       launches += 2;
@@ -1101,7 +1155,10 @@ class ParallelTempering : public Solver
     {
       a.sweep_base = step_pos * spr;
       a.tag = step_pos;
+      a.field = fields ? P.field : nullptr;
+      a.field_valid = P.fvalid ? 1 : 0;
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
+      P.fvalid = fields;
       sw.step = step_pos;
       cuda_check(launch_pt_swap(sw, st), "swap kernel");
       launches += 2;

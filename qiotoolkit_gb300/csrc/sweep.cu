@@ -1264,6 +1264,8 @@ void upload_sweep_tables(const double* ln, const float* scr, const unsigned long
 cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int wpb)
 {
   using namespace sw;
+  // the field-cached sweep when the caller keeps fields for this population
+  if (a.field && a.smem_state && fc_fits(a.m, a.p.nw, a.p.mp)) return launch_fc_sweep(a, s);
   if (wpb < 1) wpb = 1;
   if (wpb > 8) wpb = 8;
   const int max_smem = 227 * 1024;

@@ -130,7 +130,7 @@ def test_kernel_parameter_validation():
     from qiotoolkit_gb300 import instances as I
     off, ids, coef = I.cubic_pm_j(3, seed=1)
     m = q.Model("ising", off=off, ids=ids, coef=coef)
-    with pytest.raises(q.QioError, match='must be "auto", "warp", "lanes" or "levels"'):
+    with pytest.raises(q.QioError, match='must be "auto", "warp", "lanes", "levels" or "fields"'):
         q.Solver(m, "simulatedannealing.qiotoolkit", {"params": {"sweeps": 5, "kernel": "fast"}})
     with pytest.raises(q.QioError, match="not available for parallel tempering"):
         q.Solver(m, "paralleltempering.qiotoolkit", {"params": {"sweeps": 5, "kernel": "lanes"}})
