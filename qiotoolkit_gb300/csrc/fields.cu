@@ -141,6 +141,44 @@ __device__ __forceinline__ int screen(const float* scr, uint32_t r, int row, flo
   return -1;
 }
 
+// the exact ln-table comparison (markov/metropolis.h:96-103), kept out of
+// line: the FP64 instructions stay off the common path
+__device__ __noinline__ bool exact_less(const double* ln, uint32_t r, int row, double dE, double beta)
+{
+  return lut_less_exact(ln, r, row, __dmul_rn(dE, -beta));
+}
+
+// The redraw chain of an uphill attempt whose first replayed draw had
+// bucket 0 (markov/metropolis.h:93-103): draws at positions pos, pos + 1, ...
+// Returns 1 accept / 0 reject, the draws used in *used.
+__device__ __noinline__ int redraw_chain(const unsigned long long* jA, const unsigned long long* jC,
+                                         uint64_t rs, int pos, const double* s_ln0, bool beta_inf,
+                                         double dE, double beta, int* used)
+{
+  int row = -1, b = 0, u = 0;
+  uint32_t cur = 0;
+  bool decided = false;
+  while (b == 0)
+  {
+    if (row < 3)
+    {
+      cur = pcg_out(jA[pos + u] * rs + jC[pos + u]);
+      u++;
+      b = (int)(cur & 255u);
+      row++;
+    }
+    else
+    {
+      decided = true;
+      break;
+    }
+  }
+  *used = u;
+  if (decided) return 1;
+  if (beta_inf) return 0;
+  return lut_less_exact(row ? c_ln : s_ln0, cur, row, __dmul_rn(dE, -beta)) ? 1 : 0;
+}
+
 __device__ __forceinline__ uint32_t spin_of(const uint32_t* spins, int v)
 {
   return (spins[v >> 5] >> (v & 31)) & 1u;
@@ -149,7 +187,7 @@ __device__ __forceinline__ uint32_t spin_of(const uint32_t* spins, int v)
 // Exact cost difference of flipping v (FP64 models): the reference's sum
 // over the row in ascending term id, from the current term states.
 template <int FL>
-__device__ double exact_dE(const DevModel& m, int v, uint32_t sv, const uint8_t* z)
+__device__ __noinline__ double exact_dE(const DevModel& m, int v, uint32_t sv, const uint8_t* z)
 {
   const int rb = __ldg(m.row + v), re = __ldg(m.row + v + 1);
   double d = 0.0;
@@ -311,11 +349,37 @@ __device__ __forceinline__ int co_delta(uint32_t cw, uint32_t zo, uint32_t zn, i
 // Returns this incidence's bits for the flip's log masks: bit 0 = the
 // incidence contributes to the flip's cost difference, bit 1 = its sign.
 template <int FL>
+__device__ __noinline__ void apply_overflow(const DevModel& m, const Region& R, uint32_t e, uint32_t zo,
+                                            uint32_t zn, int q, int vj, int pack)
+{
+  for (int x = __ldg(m.trow + e); x < __ldg(m.trow + e + 1); x++)
+  {
+    const uint32_t tv = __ldg(m.tvar + x);
+    const uint32_t u = tv & ~kNegBit;
+    if ((int)u == vj) continue;
+    const uint32_t cw = u | ((tv & kNegBit) ? 0x8000u : 0u);
+    const int d = co_delta<FL>(cw, zo, zn, q, pack, R.spins);
+    if (d) atomicAdd(R.G + u, d);
+  }
+}
+
+template <int FL>
 __device__ __forceinline__ unsigned apply_incidence(const DevModel& m, const Region& R, const uint4 rec,
                                                     uint32_t sv, int vj, int pack)
 {
+  // every shared-memory load before the stores: the term state and the
+  // co-members' spin words
   const uint32_t e = rec.x & ~kNegBit;
+  const int nco = (int)(rec.w >> 16);
+  const uint32_t cws[3] = {rec.z & 0xFFFFu, rec.z >> 16, rec.w & 0xFFFFu};
   const uint32_t zo = R.z[e];
+  uint32_t sw[3] = {0u, 0u, 0u};
+  if (FL != F_PARITY)
+  {
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      if (i < nco) sw[i] = R.spins[(cws[i] & 0x7FFFu) >> 5];
+  }
   const int q = (int)rec.y;
   uint32_t zn;
   unsigned bits;
@@ -330,32 +394,271 @@ __device__ __forceinline__ unsigned apply_incidence(const DevModel& m, const Reg
     bits = ((lit ? (zo == 1u) : (zo == 0u)) ? 1u : 0u) | (lit << 1);
     zn = lit ? zo - 1u : zo + 1u;
   }
-  R.z[e] = (uint8_t)zn;
-  const int nco = (int)(rec.w >> 16);
-  if (nco <= 3)
-  {
-    const uint32_t cws[3] = {rec.z & 0xFFFFu, rec.z >> 16, rec.w & 0xFFFFu};
+  int d[3] = {0, 0, 0};
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-      if (i < nco)
+  for (int i = 0; i < 3; i++)
+    if (i < nco && nco <= 3)
+    {
+      if (FL == F_PARITY) d[i] = zo ? 2 * q : -2 * q;  // the term's contribution changes sign
+      else
       {
-        const int d = co_delta<FL>(cws[i], zo, zn, q, pack, R.spins);
-        if (d) atomicAdd(R.G + (cws[i] & 0x7FFFu), d);
+        const uint32_t litw = ((sw[i] >> (cws[i] & 31u)) ^ (cws[i] >> 15)) & 1u;
+        const int qo = litw ? (zo == 1u) : (zo == 0u);
+        const int qn = litw ? (zn == 1u) : (zn == 0u);
+        d[i] = (qn - qo) * ((litw ? q : -q) + pack);
       }
+    }
+  R.z[e] = (uint8_t)zn;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    if (d[i]) atomicAdd(R.G + (cws[i] & 0x7FFFu), d[i]);
+  // terms of more than three co-members (count 15): after the pass
+  return bits | ((nco > 3) ? 4u : 0u) | (zo << 8) | (zn << 16);
+}
+
+// The co-members of a term with more than three (read from the term lists),
+// for the incidences the pass marked; called by the whole warp after it.
+template <int FL>
+__device__ __noinline__ void apply_overflow_lane(const DevModel& m, const Region& R, bool mine, uint4 rec,
+                                                 unsigned bits, int vj, int pack)
+{
+  if (!mine) return;
+  const uint32_t e = rec.x & ~kNegBit;
+  const uint32_t zo = (bits >> 8) & 255u, zn = (bits >> 16) & 255u;
+  apply_overflow<FL>(m, R, e, zo, zn, (int)rec.y, vj, pack);
+}
+
+// Counter-stream draw of an attempt whose first byte was 0 (rare): the
+// reference's redraw loop over the two 64-bit counter words.  Returns the
+// draw and its ln-table row; *all_zero when every try came up 0.
+__device__ __noinline__ uint32_t counter_redraw(uint64_t key, unsigned long long ctr, uint64_t w0, int* row_out,
+                                               bool* all_zero)
+{
+  int row = -1, b = 0, used = 0;
+  uint32_t cur = 0;
+  *all_zero = false;
+  while (b == 0)
+  {
+    if (row < 3)
+    {
+      if (used == 0) cur = (uint32_t)w0;
+      else if (used == 1) cur = (uint32_t)(w0 >> 32);
+      else
+      {
+        const uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
+        cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
+      }
+      used++;
+      b = (int)(cur & 255u);
+      row++;
+    }
+    else
+    {
+      *all_zero = true;
+      break;
+    }
+  }
+  *row_out = row;
+  return cur;
+}
+
+// One wide flip (a row of more than 32 incidences): the warp over its
+// incidences, 32 at a time.  Its log entry carries the exact difference.
+template <int FL>
+__device__ __noinline__ void apply_wide(const DevModel& m, const Region& R, const uint4* tile, bool staged,
+                                        int b_q0, int rbj, int dj, uint32_t svj, int vj, int pack)
+{
+  const int lane = threadIdx.x & 31;
+  for (int k0 = 0; k0 < dj; k0 += 32)
+  {
+    const int kk = k0 + lane;
+    uint4 rec = make_uint4(0u, 0u, 0u, 0u);
+    unsigned bits = 0;
+    if (kk < dj)
+    {
+      rec = staged ? tile[rbj - b_q0 + kk] : __ldg(m.fc_rec + rbj + kk);
+      bits = apply_incidence<FL>(m, R, rec, svj, vj, pack);
+    }
+    if (bits & 4u)
+      apply_overflow<FL>(m, R, rec.x & ~kNegBit, (bits >> 8) & 255u, (bits >> 16) & 255u, (int)rec.y, vj, pack);
+  }
+}
+
+// One window round in full generality (out of line): exact differences for
+// fields inside their margin, ln-table comparisons inside the screen's
+// margin, counter draws that needed the redraw loop, the replayed redraw
+// chain of a zero bucket.  The fast path hands a round here whenever any
+// of these occurs in it; this function decides the round from scratch.
+struct RoundIo
+{
+  // in (per lane)
+  bool active;
+  int v, cursor, nvalid, bnd, g;
+  uint32_t nb, sv, pd;
+  uint64_t w0;
+  float xmargin;
+  // in (uniform)
+  uint64_t rs, key;
+  unsigned long long ctr0;
+  double beta;
+  bool beta_inf;
+  float nbeta_f, fscale;
+  // out
+  unsigned flips;
+  int draws, adv;
+  bool have_exact;
+  double dE;
+  long long idE;
+};
+
+template <int FL, bool REPLAY, bool INT>
+__device__ __noinline__ void general_round(const DevModel& m, const uint8_t* z, const double* s_ln0,
+                                           const float* s_scr0, const unsigned long long* s_jA,
+                                           const unsigned long long* s_jC, RoundIo& io)
+{
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const bool active = io.active;
+  const int v = io.v, cursor = io.cursor, bnd = io.bnd, g = io.g;
+  const uint32_t nb = io.nb, sv = io.sv;
+  const double beta = io.beta;
+  const bool beta_inf = io.beta_inf;
+  const float nbeta_f = io.nbeta_f, fscale = io.fscale;
+  bool have_exact = false, uphill = false;
+  double dE = 0.0;
+  long long idE = 0;
+  int F = 0;
+  if (INT)
+  {
+    idE = (FL == F_PARITY) ? -2LL * (long long)g : (long long)g;
+    uphill = active && idE > 0;
   }
   else
   {
-    for (int x = __ldg(m.trow + e); x < __ldg(m.trow + e + 1); x++)
+    bool need = false;
+    if (FL == F_PARITY)
     {
-      const uint32_t tv = __ldg(m.tvar + x);
-      const uint32_t u = tv & ~kNegBit;
-      if ((int)u == vj) continue;
-      const uint32_t cw = u | ((tv & kNegBit) ? 0x8000u : 0u);
-      const int d = co_delta<FL>(cw, zo, zn, q, pack, R.spins);
-      if (d) atomicAdd(R.G + u, d);
+      F = g;
+      need = active && F <= bnd && F >= -bnd;
+      uphill = active && F < -bnd;
+    }
+    else
+    {
+      F = g >> 8;
+      if (active && (g & 255) == 0) have_exact = true;  // nothing contributes: +0.0
+      need = active && !have_exact && F <= bnd && F >= -bnd;
+      uphill = active && !have_exact && F > bnd;
+    }
+    if (need)
+    {
+      dE = exact_dE<FL>(m, v, sv, z);
+      have_exact = true;
+      uphill = !le_zero(dE);
     }
   }
-  return bits;
+  bool acc = active && !uphill;
+  const unsigned before = lt & ~((1u << cursor) - 1u);
+  unsigned U = 0;
+  int pos = 0;
+  if (REPLAY)
+  {
+    U = __ballot_sync(kFull, uphill);
+    pos = __popc(U & before);
+  }
+  auto decide = [&](uint32_t rr, int row) -> int {
+    if (beta_inf) return 0;
+    const float* sc = scr_base(s_scr0, row);
+    if (INT) return screen(sc, rr, row, __fmul_rn((float)idE, nbeta_f), 0.f);
+    if (have_exact) return screen(sc, rr, row, __fmul_rn(approx_float(dE), nbeta_f), 0.f);
+    return screen(sc, rr, row, __fmul_rn((float)F, fscale), io.xmargin);
+  };
+  uint32_t dr = 0;
+  int drow = 0;
+  bool redraw = false;
+  int dec = 1;
+  if (REPLAY)
+  {
+    const uint32_t d0 = __shfl_sync(kFull, io.pd, pos & 31);
+    if (uphill)
+    {
+      dr = d0;
+      redraw = (dr & 255u) == 0;
+      if (!redraw) dec = decide(dr, 0);
+    }
+  }
+  else if (uphill)
+  {
+    const uint32_t cur0 = io.pd;
+    if ((cur0 & 255u) != 0u)
+    {
+      dr = cur0;
+      dec = decide(cur0, 0);
+    }
+    else
+    {
+      bool all_zero;
+      dr = counter_redraw(io.key, io.ctr0 + (unsigned long long)v, io.w0, &drow, &all_zero);
+      dec = all_zero ? 1 : decide(dr, drow);
+    }
+  }
+  const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
+  if (!INT && __any_sync(kFull, uphill && !redraw && dec < 0))
+  {
+    // exact differences for the lanes inside the margin that can still be
+    // committed: up to the first stop under the surely accepted lanes (more
+    // acceptances can only move the stop earlier)
+    const bool sure = active && (!uphill || (!redraw && dec == 1));
+    const unsigned As = __ballot_sync(kFull, sure);
+    bool cs = false;
+    if (active && lane > cursor)
+      cs = (nb & (__brev(As) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+    const unsigned stop_s = __ballot_sync(kFull, cs) | Rm;
+    const int fs = stop_s ? (__ffs(stop_s) - 1) : 32;
+    const bool cand = active && lane <= fs && !have_exact && uphill && !redraw && dec < 0;
+    if (cand)
+    {
+      dE = exact_dE<FL>(m, v, sv, z);
+      have_exact = true;
+    }
+    if (lane > fs && dec < 0) dec = 0;  // not committed this round
+  }
+  if (uphill && !redraw && dec < 0)
+    dec = exact_less(ln_base(s_ln0, drow), dr, drow, INT ? (double)idE : dE, beta) ? 1 : 0;
+  if (uphill && !redraw) acc = dec == 1;
+  const unsigned A = __ballot_sync(kFull, acc);
+  bool conf = false;
+  if (active && lane > cursor)
+    conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
+  const unsigned Cm = __ballot_sync(kFull, conf);
+  const unsigned stop = Cm | Rm;
+  int f = stop ? (__ffs(stop) - 1) : 32;
+  if (f > io.nvalid) f = io.nvalid;
+  const bool slow = REPLAY && f < io.nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
+  const unsigned commit = ((f >= 32) ? kFull : ((1u << f) - 1u)) & ~((1u << cursor) - 1u);
+  unsigned flips = A & commit;
+  int draws = REPLAY ? __popc(U & commit) : 0;
+  if (REPLAY && slow)
+  {
+    // lane f drew a zero bucket: its redraw chain (markov/metropolis.h:93-103)
+    if (!INT && lane == f && !have_exact)
+    {
+      dE = exact_dE<FL>(m, v, sv, z);
+      have_exact = true;
+    }
+    int sacc = 0, used = 0;
+    if (lane == f)
+      sacc = redraw_chain(s_jA, s_jC, io.rs, pos, s_ln0, beta_inf, INT ? (double)idE : dE, beta, &used);
+    sacc = __shfl_sync(kFull, sacc, f);
+    used = __shfl_sync(kFull, used, f);
+    if (sacc) flips |= 1u << f;
+    draws += used;
+  }
+  io.flips = flips;
+  io.draws = draws;
+  io.adv = f + (slow ? 1 : 0) - cursor;
+  io.have_exact = have_exact;
+  io.dE = dE;
+  io.idE = idE;
 }
 
 // ---------------------------------------------------------------------------
@@ -363,11 +666,18 @@ __device__ __forceinline__ unsigned apply_incidence(const DevModel& m, const Reg
 // Committed flips are logged at head + i and published to the accountant at
 // the end of each 32-variable block (a block logs at most 32 flips; the log
 // is checked for room for them when the block starts).
+//
+// A window round, common path: every lane turns the draw at stream position
+// `lane` into the screen interval [lo, hi] of the ln-table value; each
+// uphill lane takes the interval of its position (the uphill lanes before it)
+// and compares it with its threshold field * fscale +- margin.  Inside the
+// margin, the exact FP64 difference and comparison are taken (rare).  Flips
+// are applied in lane segments of 8, 16 or 32 per flip.
 // ---------------------------------------------------------------------------
 template <int FL, bool REPLAY, bool INT>
-__device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double* s_ln0, const float* s_scr0,
+__device__ __forceinline__ bool decide_sweeps(const SweepArgs& a, const Region R, const double* s_ln0, const float* s_scr0,
                               const unsigned long long* s_jA, const unsigned long long* s_jC, int r,
-                              unsigned* phase, uint64_t& rs, unsigned long long& natt,
+                              unsigned& phases, uint64_t& rs, unsigned long long& natt,
                               unsigned long long& nacc, unsigned long long& nwin)
 {
   const DevModel& m = a.m;
@@ -382,7 +692,7 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
   const int total = nblocks * a.n_sweeps;
   unsigned head = 0;       // entries written (published at block ends)
   unsigned tail_seen = 0;  // lane 0: the accountant's count last seen
-  // per-lane row data of the current and the next block (prefetched)
+  // per-lane row data of the next block (prefetched a block ahead)
   auto row_data = [&](int blk, int& rb, int& deg, uint32_t& nb) {
     const int v = (blk << 5) + lane;
     rb = 0;
@@ -398,26 +708,40 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
   int n_rb, n_deg;
   uint32_t n_nb;
   row_data(0, n_rb, n_deg, n_nb);
-  int tq0 = 0, tq1 = 0;  // lane 0: record range of the tile in flight
+  // lane 0: record range of the tile in flight (tq) and of the next one (nq),
+  // loaded a block ahead of its copy
+  int tq0 = 0, tq1 = 0, nq0 = 0, nq1 = 0;
+  auto range_of = [&](int blk, int& q0, int& q1) {
+    q0 = __ldg(m.row + (blk << 5));
+    q1 = __ldg(m.row + min((blk << 5) + 32, N));
+  };
   if (total > 0 && lane == 0)
   {
-    tq0 = __ldg(m.row + 0);
-    tq1 = __ldg(m.row + min(32, N));
+    range_of(0, tq0, tq1);
     tile_issue(R.tiles, m.fc_rec + tq0, min(tq1 - tq0, kCap), &R.bars[0]);
+    if (total > 1) range_of(nblocks > 1 ? 1 : 0, nq0, nq1);
   }
   double beta = 0.0;
   bool beta_inf = false;
   float nbeta_f = 0.f, fscale = 0.f, fsa = 0.f;
   unsigned long long ctr0 = 0;
-  for (int gb = 0; gb < total; gb++)
+  // the sweep's beta, loaded a block ahead of its first use
+  const double* betas = a.beta + (long long)r * a.bs_w;
+  double beta_next = total > 0 ? betas[a.sweep_base * a.bs_s] : 0.0;
+  int k = 0, bi = 0;                              // sweep and block of gb
+  int bi2 = nblocks > 2 ? 2 : (nblocks == 2 ? 0 : 0);  // block of gb + 2
+  for (int gb = 0; gb < total; gb++, bi++)
   {
-    const int k = gb / nblocks;
-    const int bi = gb - k * nblocks;
+    if (bi == nblocks)
+    {
+      bi = 0;
+      k++;
+    }
     const int buf = gb & 1;
     if (bi == 0)
     {
       const long long swp = a.sweep_base + k;
-      beta = a.beta[(long long)r * a.bs_w + swp * a.bs_s];
+      beta = beta_next;
       beta_inf = ((unsigned long long)__double_as_longlong(beta) & 0x7FFFFFFFFFFFFFFFULL) ==
                  0x7FF0000000000000ULL;
       nbeta_f = -approx_float(beta);
@@ -426,17 +750,19 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
       fsa = fabsf(fscale) * 1.0001f;
       ctr0 = (unsigned long long)swp * (unsigned long long)N;
     }
+    if (bi == nblocks - 1 && gb + 1 < total) beta_next = betas[(a.sweep_base + k + 1) * a.bs_s];
     const int i0 = bi << 5;
     // this block's record range, then the next block's tile into the other buffer
     const int b_q0 = __shfl_sync(kFull, tq0, 0);
     const int b_q1 = __shfl_sync(kFull, tq1, 0);
     if (gb + 1 < total && lane == 0)
     {
-      const int nbk = (bi + 1 < nblocks) ? bi + 1 : 0;
-      tq0 = __ldg(m.row + (nbk << 5));
-      tq1 = __ldg(m.row + min((nbk << 5) + 32, N));
+      tq0 = nq0;
+      tq1 = nq1;
       tile_issue(R.tiles + (buf ^ 1) * kCap, m.fc_rec + tq0, min(tq1 - tq0, kCap), &R.bars[buf ^ 1]);
+      if (gb + 2 < total) range_of(bi2, nq0, nq1);
     }
+    bi2 = (bi2 + 1 == nblocks) ? 0 : bi2 + 1;
     const int rb = n_rb, deg = n_deg;
     const uint32_t nb = n_nb;
     if (gb + 1 < total) row_data((bi + 1 < nblocks) ? bi + 1 : 0, n_rb, n_deg, n_nb);
@@ -471,8 +797,8 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
         __nanosleep(64);
       }
     }
-    const bool tile_ok = mbar_wait(&R.bars[buf], phase[buf]);
-    phase[buf] ^= 1u;
+    const bool tile_ok = mbar_wait(&R.bars[buf], (phases >> buf) & 1u);
+    phases ^= 1u << buf;
     if (!__all_sync(kFull, ok && tile_ok))
     {
       if (lane == 0)
@@ -481,8 +807,8 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
         // the copy in flight lands before the walker's region is given up
         if (gb + 1 < total)
         {
-          mbar_wait(&R.bars[buf ^ 1], phase[buf ^ 1]);
-          phase[buf ^ 1] ^= 1u;
+          mbar_wait(&R.bars[buf ^ 1], (phases >> (buf ^ 1)) & 1u);
+          phases ^= 1u << (buf ^ 1);
         }
       }
       __syncwarp();
@@ -496,170 +822,85 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
     const int nvalid = min(32, N - i0);
     uint32_t sv = valid ? spin_of(R.spins, v) : 0u;
     const int bnd = deg + 1;  // |field - exact| < bnd units
+    const float xmargin = INT ? 0.f : fsa * (float)(bnd + 1);
     const unsigned head0 = head;
+    unsigned b_att = 0, b_acc = 0, b_win = 0;
+
+    // the draws of the first round (replay: stream positions 0..31)
+    uint32_t pd = 0;
+    uint64_t w0 = 0;
+    float plo = 0.f, phi = 0.f;
+    unsigned Zm = 0;
+    auto draws_for = [&](int cur) {
+      if (REPLAY) pd = pcg_out(s_jA[lane] * rs + s_jC[lane]);
+      else
+      {
+        w0 = counter_draw(key, 2ULL * (ctr0 + (unsigned long long)(i0 + lane)));
+        pd = (uint32_t)w0;
+      }
+      const int pb = (int)(pd & 255u);
+      const float* e = s_scr0 + pb * 3;
+      const float val = __fmaf_rn(__fmul_rn((float)(pd >> 8), 5.96046483e-08f), e[1], e[0]);
+      plo = pb == 1 ? INFINITY : __fsub_rn(val, e[2]);
+      phi = pb == 1 ? INFINITY : __fadd_rn(val, e[2]);
+      Zm = __ballot_sync(kFull, pb == 0);
+      (void)cur;
+    };
+    if (!REPLAY) draws_for(0);  // counter draws: fixed for the block
 
     int cursor = 0;
     while (cursor < nvalid)
     {
+      if (REPLAY) draws_for(0);
       const bool active = valid && lane >= cursor;
-      // replay: the draw at stream position `lane` and its screen value,
-      // ahead of the field (an uphill lane takes the draw of its position)
-      uint32_t pd = 0;
-      float pval = 0.f, pev = 0.f;
-      if (REPLAY)
-      {
-        pd = pcg_out(s_jA[lane] * rs + s_jC[lane]);
-        const int b = (int)(pd & 255u);
-        if (b >= 2)
-        {
-          const float* e = s_scr0 + b * 3;
-          pval = __fmaf_rn(__fmul_rn((float)(pd >> 8), 5.96046483e-08f), e[1], e[0]);
-          pev = e[2];
-        }
-      }
+      const unsigned before = lt & ~((1u << cursor) - 1u);
       const int g = active ? R.G[v] : 0;
-      // ---- cost difference: sign from the field, exact inside its margin
-      bool have_exact = false, uphill = false;
-      double dE = 0.0;
-      long long idE = 0;
-      int F = 0;
+      // ---- fast path: the field's sign and the screened comparison
+      bool up, rare;
+      float thr, xm;
       if (INT)
       {
-        idE = (FL == F_PARITY) ? -2LL * (long long)g : (long long)g;
-        uphill = active && idE > 0;
+        const long long idE = (FL == F_PARITY) ? -2LL * (long long)g : (long long)g;
+        up = active && idE > 0;
+        thr = __fmul_rn((float)idE, nbeta_f);
+        xm = 0.f;
+        rare = false;
+      }
+      else if (FL == F_PARITY)
+      {
+        up = active && g < -bnd;
+        rare = active && g <= bnd && g >= -bnd;
+        thr = __fmul_rn((float)g, fscale);
+        xm = xmargin;
       }
       else
       {
-        bool need = false;
-        if (FL == F_PARITY)
-        {
-          F = g;
-          need = active && F <= bnd && F >= -bnd;
-          uphill = active && F < -bnd;
-        }
-        else
-        {
-          F = g >> 8;
-          if (active && (g & 255) == 0) have_exact = true;  // nothing contributes: +0.0
-          need = active && !have_exact && F <= bnd && F >= -bnd;
-          uphill = active && !have_exact && F > bnd;
-        }
-        if (__any_sync(kFull, need))
-        {
-          if (need)
-          {
-            dE = exact_dE<FL>(m, v, sv, R.z);
-            have_exact = true;
-            uphill = !le_zero(dE);
-          }
-        }
+        const int F = g >> 8;
+        const bool zero = (g & 255) == 0;  // nothing contributes: +0.0
+        up = active && !zero && F > bnd;
+        rare = active && !zero && F <= bnd && F >= -bnd;
+        thr = __fmul_rn((float)F, fscale);
+        xm = xmargin;
       }
-      bool acc = active && !uphill;
-      const unsigned before = lt & ~((1u << cursor) - 1u);
       unsigned U = 0;
-      int pos = 0;
+      float lo = plo, hi = phi;
+      bool rd = false;
       if (REPLAY)
       {
-        U = __ballot_sync(kFull, uphill);
-        pos = __popc(U & before);
+        U = __ballot_sync(kFull, up);
+        const int pos = __popc(U & before);
+        lo = __shfl_sync(kFull, plo, pos);
+        hi = __shfl_sync(kFull, phi, pos);
+        rd = up && ((Zm >> pos) & 1u);
       }
-      uint32_t dr = 0;
-      int drow = 0;
-      bool redraw = false;
-      int dec = 1;
-      auto decide = [&](uint32_t rr, int row) -> int {
-        if (beta_inf) return 0;
-        const float* sc = scr_base(s_scr0, row);
-        if (INT) return screen(sc, rr, row, __fmul_rn((float)idE, nbeta_f), 0.f);
-        if (have_exact) return screen(sc, rr, row, __fmul_rn(approx_float(dE), nbeta_f), 0.f);
-        return screen(sc, rr, row, __fmul_rn((float)F, fscale), fsa * (float)(bnd + 1));
-      };
-      if (REPLAY)
-      {
-        const uint32_t d0 = __shfl_sync(kFull, pd, pos & 31);
-        const float v0 = __shfl_sync(kFull, pval, pos & 31);
-        const float e0 = __shfl_sync(kFull, pev, pos & 31);
-        if (uphill)
-        {
-          dr = d0;
-          redraw = (dr & 255u) == 0;
-          if (!redraw)
-          {
-            if (beta_inf || (dr & 255u) == 1u) dec = 0;
-            else
-            {
-              float thr, extra = 0.f;
-              if (INT) thr = __fmul_rn((float)idE, nbeta_f);
-              else if (have_exact) thr = __fmul_rn(approx_float(dE), nbeta_f);
-              else
-              {
-                thr = __fmul_rn((float)F, fscale);
-                extra = fsa * (float)(bnd + 1);
-              }
-              const float et = __fmaf_rn(fabsf(thr), 1.9073486328125e-06f, 1e-30f) + extra;  // 2^-19
-              if (__fadd_rn(v0, e0) < __fsub_rn(thr, et)) dec = 1;
-              else if (__fsub_rn(v0, e0) > __fadd_rn(thr, et)) dec = 0;
-              else dec = -1;
-            }
-          }
-        }
-      }
-      else if (uphill)
-      {
-        const unsigned long long ctr = ctr0 + (unsigned long long)v;
-        const uint64_t w0 = counter_draw(key, 2ULL * ctr);
-        int row = -1, b = 0, used = 0;
-        uint32_t cur = 0;
-        bool all_zero = false;
-        while (b == 0)
-        {
-          if (row < 3)
-          {
-            if (used == 0) cur = (uint32_t)w0;
-            else if (used == 1) cur = (uint32_t)(w0 >> 32);
-            else
-            {
-              const uint64_t w1 = counter_draw(key, 2ULL * ctr + 1ULL);
-              cur = used == 2 ? (uint32_t)w1 : (uint32_t)(w1 >> 32);
-            }
-            used++;
-            b = (int)(cur & 255u);
-            row++;
-          }
-          else
-          {
-            all_zero = true;
-            break;
-          }
-        }
-        dr = cur;
-        drow = row;
-        dec = all_zero ? 1 : decide(cur, row);
-      }
-      const unsigned Rm = REPLAY ? __ballot_sync(kFull, redraw) : 0u;
-      if (!INT && __any_sync(kFull, uphill && !redraw && dec < 0))
-      {
-        // exact differences for the lanes inside the margin that can still
-        // be committed: up to the first stop under the surely accepted lanes
-        const bool sure = active && (!uphill || (!redraw && dec == 1));
-        const unsigned As = __ballot_sync(kFull, sure);
-        bool cs = false;
-        if (active && lane > cursor)
-          cs = (nb & (__brev(As) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
-        const unsigned stop_s = __ballot_sync(kFull, cs) | Rm;
-        const int fs = stop_s ? (__ffs(stop_s) - 1) : 32;
-        const bool cand = active && lane <= fs && !have_exact && uphill && !redraw && dec < 0;
-        if (cand)
-        {
-          dE = exact_dE<FL>(m, v, sv, R.z);
-          have_exact = true;
-        }
-        if (lane > fs && dec < 0) dec = 0;  // not committed this round
-      }
-      if (uphill && !redraw && dec < 0)
-        dec = lut_less_exact(ln_base(s_ln0, drow), dr, drow, __dmul_rn(INT ? (double)idE : dE, -beta)) ? 1 : 0;
-      if (uphill && !redraw) acc = dec == 1;
-      const unsigned A = __ballot_sync(kFull, acc);
+      else
+        rare = rare || (up && (pd & 255u) == 0u);
+      const float et = __fmaf_rn(fabsf(thr), 1.9073486328125e-06f, 1e-30f) + xm;  // 2^-19
+      const bool acc_u = up && !rd && !beta_inf && hi < __fsub_rn(thr, et);
+      const bool rej_u = up && !rd && (beta_inf || lo > __fadd_rn(thr, et));
+      rare = rare || (up && !rd && !acc_u && !rej_u);
+      const unsigned A = __ballot_sync(kFull, active && (!up || acc_u));
+      const unsigned Rm = __ballot_sync(kFull, rd);
       bool conf = false;
       if (active && lane > cursor)
         conf = (nb & (__brev(A) >> (32 - lane)) & ((1u << (lane - cursor)) - 1u)) != 0u;
@@ -667,66 +908,84 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
       const unsigned stop = Cm | Rm;
       int f = stop ? (__ffs(stop) - 1) : 32;
       if (f > nvalid) f = nvalid;
-      const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
       const unsigned commit = ((f >= 32) ? kFull : ((1u << f) - 1u)) & ~((1u << cursor) - 1u);
       unsigned flips = A & commit;
       int draws = REPLAY ? __popc(U & commit) : 0;
-      if (REPLAY && slow)
+      int adv = f - cursor;
+      bool have_exact = false;
+      double dE = 0.0;
+      long long idE = (FL == F_PARITY) ? -2LL * (long long)g : (long long)g;
+      if (!INT && FL == F_COUNTER && active && (g & 255) == 0) have_exact = true;  // dE = +0.0
+      // the general round: a field inside its margin, a comparison inside
+      // the screen's margin, a counter redraw, or a replayed zero bucket at
+      // the stop
+      const bool slow = REPLAY && f < nvalid && ((Rm >> f) & 1u) && !((Cm >> f) & 1u);
+      const bool any_rare = __any_sync(kFull, rare);
+      if (!any_rare && slow)
       {
         // lane f drew a zero bucket: its redraw chain (markov/metropolis.h:93-103)
-        if (!INT && lane == f && !have_exact)
-        {
-          dE = exact_dE<FL>(m, v, sv, R.z);
-          have_exact = true;
-        }
         int sacc = 0, used = 0;
         if (lane == f)
         {
-          int row = -1, b = 0;
-          uint32_t cur = 0;
-          bool decided = false;
-          while (b == 0)
-          {
-            if (row < 3)
-            {
-              cur = pcg_out(s_jA[pos + used] * rs + s_jC[pos + used]);
-              used++;
-              b = (int)(cur & 255u);
-              row++;
-            }
-            else
-            {
-              decided = true;
-              break;
-            }
-          }
-          bool okk;
-          if (decided) okk = true;
-          else if (beta_inf) okk = false;
-          else
-            okk = lut_less_exact(ln_base(s_ln0, row), cur, row, __dmul_rn(INT ? (double)idE : dE, -beta));
-          sacc = okk ? 1 : 0;
+          double d = 0.0;
+          if (!INT) d = exact_dE<FL>(m, v, sv, R.z);
+          const int pos = __popc(U & before);
+          sacc = redraw_chain(s_jA, s_jC, rs, pos, s_ln0, beta_inf, INT ? (double)idE : d, beta, &used);
+          have_exact = !INT;
+          dE = d;
         }
         sacc = __shfl_sync(kFull, sacc, f);
         used = __shfl_sync(kFull, used, f);
         if (sacc) flips |= 1u << f;
         draws += used;
+        adv += 1;
       }
-      const int adv = f + (slow ? 1 : 0) - cursor;
+      if (any_rare)
+      {
+        RoundIo io;
+        io.active = active;
+        io.v = v;
+        io.cursor = cursor;
+        io.nvalid = nvalid;
+        io.bnd = bnd;
+        io.g = g;
+        io.nb = nb;
+        io.sv = sv;
+        io.pd = pd;
+        io.w0 = w0;
+        io.xmargin = xmargin;
+        io.rs = rs;
+        io.key = key;
+        io.ctr0 = ctr0;
+        io.beta = beta;
+        io.beta_inf = beta_inf;
+        io.nbeta_f = nbeta_f;
+        io.fscale = fscale;
+        general_round<FL, REPLAY, INT>(m, R.z, s_ln0, s_scr0, s_jA, s_jC, io);
+        flips = io.flips;
+        draws = io.draws;
+        adv = io.adv;
+        have_exact = io.have_exact;
+        dE = io.dE;
+        idE = io.idE;
+      }
       const bool mine = ((flips >> lane) & 1u) != 0u;
       const int nfl = __popc(flips);
+      // the next round's draws, ahead of the apply (independent of it)
+      if (REPLAY) rs = s_jA[draws] * rs + s_jC[draws];
 
       if (nfl)
       {
         // a wide row keeps no masks: its exact difference is taken now,
         // before the flips change the term states
-        if (!INT && mine && !have_exact && deg > 32)
-        {
-          dE = exact_dE<FL>(m, v, sv, R.z);
-          have_exact = true;
-        }
-        const bool keep_masks = !INT && mine && !have_exact;
-        const int eslot = (int)((head + (unsigned)__popc(flips & lt)) & (unsigned)(kLog - 1));
+        const bool wide = mine && deg > 32;
+        if (!INT && __any_sync(kFull, wide && !have_exact))
+          if (wide && !have_exact)
+          {
+            dE = exact_dE<FL>(m, v, sv, R.z);
+            have_exact = true;
+          }
+        const int fi = __popc(flips & lt);  // this flip's index among the round's
         // the log entry: x = v | deg << 16 | kind, y/z = masks or the difference
         uint4 ent;
         ent.x = (unsigned)v | ((unsigned)deg << 16);
@@ -746,9 +1005,65 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
           ent.y = (unsigned)bits;
           ent.z = (unsigned)(bits >> 32);
         }
-        if (nfl <= 2)
+        const int maxdeg = (int)__reduce_max_sync(kFull, (unsigned)(mine ? deg : 0));
+        if (maxdeg <= 32)
         {
-          // one flip at a time, the warp over its incidences (masks by ballot)
+          // segments of sg lanes, one flip each, pp flips per pass
+          const int lsg = maxdeg <= 8 ? 3 : (maxdeg <= 16 ? 4 : 5);
+          const int sg = 1 << lsg;
+          const int pp = 32 >> lsg;
+          const int grp = lane >> lsg;
+          const int kk = lane & (sg - 1);
+          unsigned qm = 0, sm = 0;
+          unsigned fw = flips;  // flips not yet applied
+          for (int p0 = 0; p0 < nfl; p0 += pp)
+          {
+            // the lanes of the pass's first pp flips: successive lowest bits
+            const int q0 = __ffs(fw) - 1;
+            const unsigned f1 = fw & (fw - 1);
+            const int q1 = f1 ? __ffs(f1) - 1 : q0;
+            const unsigned f2 = f1 & (f1 - 1);
+            const int q2 = f2 ? __ffs(f2) - 1 : q0;
+            const unsigned f3 = f2 & (f2 - 1);
+            const int q3 = f3 ? __ffs(f3) - 1 : q0;
+            const int j = grp == 0 ? q0 : (grp == 1 ? q1 : (grp == 2 ? q2 : q3));
+            const bool live = p0 + grp < nfl;
+            fw = (pp == 1) ? f1 : ((pp == 2) ? f2 : (f3 & (f3 - 1)));
+            const int dj = __shfl_sync(kFull, deg, j);
+            const int rbj = __shfl_sync(kFull, rb, j);
+            const uint32_t svj = __shfl_sync(kFull, sv, j);
+            unsigned bits = 0;
+            const bool act = live && kk < dj;
+            uint4 rec = make_uint4(0u, 0u, 0u, 0u);
+            if (act)
+            {
+              rec = staged ? tile[rbj - b_q0 + kk] : __ldg(m.fc_rec + rbj + kk);
+              bits = apply_incidence<FL>(m, R, rec, svj, i0 + j, pack);
+            }
+            if (__any_sync(kFull, bits & 4u))
+              apply_overflow_lane<FL>(m, R, (bits & 4u) != 0u, rec, bits, i0 + j, pack);
+            if (!INT)
+            {
+              const unsigned Bq = __ballot_sync(kFull, bits & 1u);
+              const unsigned Bs = __ballot_sync(kFull, (bits >> 1) & 1u);
+              if (mine && fi >= p0 && fi < p0 + pp)
+              {
+                const int sh = (fi - p0) << lsg;
+                const unsigned w = (sg == 32) ? kFull : ((1u << sg) - 1u);
+                qm = (Bq >> sh) & w;
+                sm = (Bs >> sh) & w;
+              }
+            }
+          }
+          if (mine && !INT && !have_exact)
+          {
+            ent.y = (FL == F_PARITY) ? 0u : qm;
+            ent.z = sm;
+          }
+        }
+        else
+        {
+          // a wide flip among them (rare): one flip at a time
           unsigned fl = flips;
           while (fl)
           {
@@ -757,70 +1072,28 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
             const int dj = __shfl_sync(kFull, deg, j);
             const int rbj = __shfl_sync(kFull, rb, j);
             const uint32_t svj = __shfl_sync(kFull, sv, j);
-            unsigned qm = 0, sm = 0;
-            for (int k0 = 0; k0 < dj; k0 += 32)
+            unsigned bits = 0;
+            if (dj <= 32)
             {
-              const int kk = k0 + lane;
-              unsigned bits = 0;
-              if (kk < dj)
+              uint4 rec = make_uint4(0u, 0u, 0u, 0u);
+              if (lane < dj)
               {
-                const uint4 rec = staged ? tile[rbj - b_q0 + kk] : __ldg(m.fc_rec + rbj + kk);
+                rec = staged ? tile[rbj - b_q0 + lane] : __ldg(m.fc_rec + rbj + lane);
                 bits = apply_incidence<FL>(m, R, rec, svj, i0 + j, pack);
               }
-              if (k0 == 0)
-              {
-                qm = __ballot_sync(kFull, bits & 1u);
-                sm = __ballot_sync(kFull, (bits >> 1) & 1u);
-              }
+              if (__any_sync(kFull, bits & 4u))
+                apply_overflow_lane<FL>(m, R, (bits & 4u) != 0u, rec, bits, i0 + j, pack);
             }
-            if (lane == j)
+            else
+              apply_wide<FL>(m, R, tile, staged, b_q0, rbj, dj, svj, i0 + j, pack);
+            if (!INT)
             {
-              if (keep_masks)
+              const unsigned Bq = __ballot_sync(kFull, bits & 1u);
+              const unsigned Bs = __ballot_sync(kFull, (bits >> 1) & 1u);
+              if (lane == j && !have_exact)
               {
-                ent.y = (FL == F_PARITY) ? 0u : qm;
-                ent.z = sm;
-              }
-              R.log[eslot] = ent;
-            }
-          }
-        }
-        else
-        {
-          // many flips: their incidences laid out back to back over the warp
-          if (mine) R.log[eslot] = ent;
-          __syncwarp();
-          const int mydeg = mine ? deg : 0;
-          const int incl = warp_scan32(mydeg, lane);
-          const int excl = incl - mydeg;
-          const int tot = __shfl_sync(kFull, incl, 31);
-          const unsigned Fm = __ballot_sync(kFull, mine && mydeg > 0);
-          const unsigned KM = __ballot_sync(kFull, keep_masks);
-          for (int base = 0; base < tot; base += 32)
-          {
-            const int rel = excl - base;
-            const unsigned starts =
-                __reduce_or_sync(kFull, (mine && mydeg > 0 && rel >= 0 && rel < 32) ? (1u << rel) : 0u);
-            const int nbefore = __popc(__ballot_sync(kFull, mine && mydeg > 0 && rel < 0));
-            const int gi = base + lane;
-            const int idx = nbefore + __popc(starts & ((2u << lane) - 1u)) - 1;
-            int j = 0;
-#pragma unroll
-            for (int step = 16; step; step >>= 1)
-              if (__popc(Fm & ((2u << (j + step - 1)) - 1u)) <= idx) j += step;
-            j &= 31;
-            const int ej = __shfl_sync(kFull, excl, j);
-            const int rbj = __shfl_sync(kFull, rb, j);
-            const uint32_t svj = __shfl_sync(kFull, sv, j);
-            const int slj = __shfl_sync(kFull, eslot, j);
-            if (gi < tot)
-            {
-              const int kk = gi - ej;
-              const uint4 rec = staged ? tile[rbj - b_q0 + kk] : __ldg(m.fc_rec + rbj + kk);
-              const unsigned bits = apply_incidence<FL>(m, R, rec, svj, i0 + j, pack);
-              if ((KM >> j) & 1u)
-              {
-                if (FL != F_PARITY && (bits & 1u)) atomicOr(&R.log[slj].y, 1u << kk);
-                if (bits & 2u) atomicOr(&R.log[slj].z, 1u << kk);
+                ent.y = (FL == F_PARITY) ? 0u : Bq;
+                ent.z = Bs;
               }
             }
           }
@@ -828,6 +1101,7 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
         __syncwarp();
         if (mine)
         {
+          R.log[(head + (unsigned)fi) & (unsigned)(kLog - 1)] = ent;
           // the flipped variable's own field changes sign (the same terms
           // contribute, with the other sign); the count stays
           const int gv = R.G[v];
@@ -838,12 +1112,14 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
         __syncwarp();
         head += (unsigned)nfl;
       }
-      natt += (unsigned long long)adv;
-      nacc += (unsigned long long)nfl;
-      nwin++;
-      if (REPLAY) rs = s_jA[draws] * rs + s_jC[draws];
+      b_att += (unsigned)adv;
+      b_acc += (unsigned)nfl;
+      b_win++;
       cursor += adv;
     }
+    natt += b_att;
+    nacc += b_acc;
+    nwin += b_win;
     // publish the block's flips
     if (head != head0)
     {
@@ -863,7 +1139,7 @@ __device__ bool decide_sweeps(const SweepArgs& a, const Region& R, const double*
 // The accountant: running cost, lowest cost and lowest state from the log.
 // ---------------------------------------------------------------------------
 template <int FL, bool INT>
-__device__ bool account(const SweepArgs& a, const Region& R, double& cost, double& low, long long& icost,
+__device__ __forceinline__ bool account(const SweepArgs& a, const Region R, double& cost, double& low, long long& icost,
                         long long& ilow, uint32_t* g_lsp)
 {
   const DevModel& m = a.m;
@@ -1020,7 +1296,7 @@ __global__ void __launch_bounds__(256, 1) fc_sweep_kernel(SweepArgs a, int wpc)
     mbar_init(&R.bars[1]);
   }
   uint64_t rs = (REPLAY && decider) ? a.rng[w] : 0;
-  unsigned phase[2] = {0u, 0u};  // mbarrier phases, kept across walkers
+  unsigned phases = 0u;  // mbarrier phase bits of the two tile buffers, kept across walkers
 
   for (int r = w; r < a.n_walkers; r += a.n_streams)
   {
@@ -1057,7 +1333,7 @@ __global__ void __launch_bounds__(256, 1) fc_sweep_kernel(SweepArgs a, int wpc)
     if (decider)
     {
       unsigned long long natt = 0, nacc = 0, nwin = 0;
-      ok = decide_sweeps<FL, REPLAY, INT>(a, R, s_ln0, s_scr0, s_jA, s_jC, r, phase, rs, natt, nacc,
+      ok = decide_sweeps<FL, REPLAY, INT>(a, R, s_ln0, s_scr0, s_jA, s_jC, r, phases, rs, natt, nacc,
                                           nwin);
       if (lane == 0) st_release(R.done, 1u);
       pair_sync(bar_id);
