@@ -393,6 +393,8 @@ def main():
     ap.add_argument("--workload", default="pt_pubo", choices=list(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--kernel", default=None, choices=["auto", "warp", "lanes", "levels", "fields"],
+                    help="override the sweep kernel choice (params `kernel`)")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the oracle recompute of the timed solve")
     ap.add_argument("--sweeps", type=int, default=None,
@@ -420,6 +422,8 @@ def main():
     kind, off, ids, coef, params = make_workload(args.workload)
     if args.sweeps:
         params["sweeps"] = args.sweeps
+    if args.kernel:
+        params["kernel"] = args.kernel
     target = WORKLOADS[args.workload]["target"]
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream

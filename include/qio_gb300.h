@@ -71,6 +71,13 @@ typedef struct qio_model_info {
                               level, or 0                                 */
   int32_t max_level_width;
   int32_t level_kernel;    /* 1: the level kernel can run this model      */
+  /* graph::Size properties (graph/properties.h:52-68; graph models only):
+   * the mean term order over non-constant terms, the sum of term orders,
+   * the sum of order * (order - 1), the smallest |coefficient| */
+  double avg_locality;
+  int64_t sum_coefficient_degrees_total;
+  int64_t accumulated_dependent_vars;
+  double min_coupling;
 } qio_model_info;
 
 typedef struct qio_solver_stats {

@@ -33,7 +33,9 @@ class ModelInfo(C.Structure):
                 ("min_locality", C.c_int32), ("const_cost", C.c_double),
                 ("scale_factor", C.c_double), ("max_coupling", C.c_double),
                 ("device_bytes", C.c_int64), ("n_levels", C.c_int32),
-                ("max_level_width", C.c_int32), ("level_kernel", C.c_int32)]
+                ("max_level_width", C.c_int32), ("level_kernel", C.c_int32),
+                ("avg_locality", C.c_double), ("sum_coefficient_degrees_total", C.c_int64),
+                ("accumulated_dependent_vars", C.c_int64), ("min_coupling", C.c_double)]
 
 
 class SolverStats(C.Structure):

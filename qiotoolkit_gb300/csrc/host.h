@@ -83,6 +83,11 @@ struct HostModel
   std::vector<int> tcost_i;
   double const_cost = 0, max_coupling = 0, scale_factor = 1.0;
   int max_loc = 0, min_loc = 0;
+  // graph::Size properties (graph/properties.h:52-68, accumulated in
+  // normalize_edges, graph/graph.h:134-176): sum of term orders, sum of
+  // order * (order - 1) over non-constant terms, smallest |c| of those
+  int64_t total_loc = 0, accum_dep = 0;
+  double min_coupling = 0;
   std::vector<int32_t> names;  // internal id -> input name
   std::vector<int32_t> free_vars;  // MaxSat free variables
   bool int_mode = false;
@@ -176,6 +181,8 @@ class Solver
   virtual bool advance(cudaStream_t s, int64_t n);
   int64_t step_pos = 0;
   std::string result_json();
+  // keys a runner adds to the benchmark object (app/runner.cc:546-631)
+  std::string runner_benchmark;
   void best(double& cost, std::vector<uint8_t>& state);
 
   const HostModel* model = nullptr;

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <set>
@@ -107,6 +108,7 @@ static void build_graph(HostModel& m, int64_t n_terms, const int64_t* off,
   std::vector<std::vector<int>> members;
   std::vector<std::vector<int>> node_edges;
   m.min_loc = INT32_MAX;
+  m.min_coupling = std::numeric_limits<double>::max();
   for (int64_t t = 0; t < n_terms; t++)
   {
     if (off[t + 1] < off[t]) fail(1, "term offsets must be non-decreasing");
@@ -136,8 +138,11 @@ static void build_graph(HostModel& m, int64_t n_terms, const int64_t* off,
     int loc = (int)mem.size();
     m.max_loc = std::max(m.max_loc, loc);
     m.min_loc = std::min(m.min_loc, loc);
+    m.total_loc += loc;
     if (!mem.empty())
     {
+      m.accum_dep += (int64_t)loc * (loc - 1);
+      m.min_coupling = std::min(m.min_coupling, std::fabs(coef[t]));
       m.max_coupling = std::max(m.max_coupling, std::fabs(coef[t]));
       members.push_back(std::move(mem));
       m.tcost.push_back(coef[t]);

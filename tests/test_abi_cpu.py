@@ -153,3 +153,20 @@ def test_kernel_parameter_validation():
                  {"params": {"sweeps": 5, "kernel": "levels", "rng_mode": "counter"}})
     # eligible: created without complaint (no device needed before init)
     q.Solver(m, sa, {"params": {"sweeps": 5, "kernel": "levels", "rng_mode": "counter"}}).close()
+
+
+def test_graph_size_properties_pin():
+    """graph/test/properties_test.cc:30-66: the graph::Size properties of the
+    reference's seven-term graph (max / min / mean term order, sum of orders,
+    sum of order * (order - 1), largest and smallest |coefficient|), which the
+    benchmark block reports under the keys of utils/config.h."""
+    terms = [(1, [0, 1]), (0.2, [0, 2]), (1, [0, 3]), (1, [1, 4]), (1, [2, 3, 4]), (1, [3]),
+             (-10, [4, 5])]
+    m = q.Model("pubo", terms)
+    info = m.info
+    assert info.n_terms == 7 and info.n_vars == 6
+    assert info.max_locality == 3 and info.min_locality == 1
+    assert info.avg_locality == 2.0
+    assert info.accumulated_dependent_vars == 16
+    assert info.sum_coefficient_degrees_total == 14
+    assert info.max_coupling == 10.0 and info.min_coupling == 0.2
