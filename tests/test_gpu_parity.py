@@ -205,3 +205,27 @@ def test_ks_independent_streams():
               threads=8)
     p = scipy_stats.ks_2samp(s.replicas(states=False)["lowest"], r.lowest).pvalue
     assert p > 0.01
+
+
+def test_pt_near_tie_swaps_follow_the_c_library_exp():
+    """Replica swaps whose uniform draw lies within 1e-15 of exp(x) are
+    decided again on the host with the C library's exp, as the reference
+    does (solver/parallel_tempering.h:126-131).  A one-spin model with field
+    1 and the ladder beta = {0, b}: with costs +1 / -1 the swap argument is
+    x = -2b, and b = -log(u) / 2 for the step-0 swap draw u of the master
+    stream puts exp(x) on u to rounding.  Every seed's trajectory and
+    observables equal the oracle's, and near ties did occur."""
+    g, o = both("ising", *O.flatten_terms([(1.0, [0])]))
+    ties = 0
+    for seed in range(48):
+        u = float(O.pcg_uniform(seed, 2)[1])  # the master's draw after the two forks
+        b = -np.log(u) / 2.0
+        params = {"seed": seed, "sweeps": 1, "all_betas": [0.0, b]}
+        s = q.Solver(g, PT, {"params": params}).init().run()
+        r = O.run(o, "pt", seed=seed, step_limit=1, sched=("list", 0, 0), sched_values=[0.0, b])
+        rep = s.replicas()
+        np.testing.assert_array_equal(rep["cost"], r.cost)
+        np.testing.assert_array_equal(rep["states"], r.states)
+        np.testing.assert_array_equal(s.pt_observables(), r.pt_obs)
+        ties += int(s.stats().near_ties)
+    assert ties > 0
