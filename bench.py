@@ -43,7 +43,13 @@ WORKLOADS = {
     "pa_square": dict(desc="PA on 2D periodic 256x256 +-J Ising, R=4096, 100 beta steps 0->3.0, "
                            "10 sweeps per step, the reference's Poisson resampling, counter streams",
                       target="populationannealing.cpu"),
-    "serving": dict(desc="Serving: Poisson arrivals at 200 req/s, 48 requests; kinds uniform over "
+    "serving_1e5": dict(desc="Serving under HBM pressure: Poisson arrivals at 200 req/s, 300 requests; "
+                             "kinds uniform over ER Ising (mean degree U[4,16], N(0,1) FP32), PUBO (orders "
+                             "U{1,2,3}, N(0,1), 3 terms per variable), weighted 3-SAT (ratio 4.2, U[1,10]); "
+                             "N log-uniform [100, 1e5]; sweeps U{200..5000}; SA (8 restarts) or PT (8 "
+                             "temperatures); admission budget 1 GiB of HBM",
+                        target="mixed"),
+    "serving": dict(desc="Serving: Poisson arrivals at 200 req/s, 200 requests; kinds uniform over "
                          "ER Ising (mean degree U[4,16], N(0,1) FP32), PUBO (orders U{1,2,3}, N(0,1), "
                          "3 terms per variable), weighted 3-SAT (ratio 4.2, U[1,10]); N log-uniform "
                          "[100, 1e4]; sweeps U{200..5000}; SA (8 restarts) or PT (8 temperatures)",
@@ -390,7 +396,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pt_pubo", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default=None, choices=list(WORKLOADS),
+                    help="one workload; without it every configuration's line is printed, "
+                         "the parallel-tempering headline last")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--kernel", default=None, choices=["auto", "warp", "lanes", "levels", "fields"],
@@ -402,8 +410,38 @@ def main():
     args = ap.parse_args()
     ws, rank = dist_setup()
     if args.impl == "reference":
+        if args.workload is None:
+            args.workload = "pt_pubo"
         run_reference(args, ws, rank)
         return
+    if args.workload is not None:
+        run_workload(args, ws, rank)
+        return
+    # the suite: one line per configuration, each with at least 3 warm-up
+    # steps and at most 3 timed steps; the headline (configuration 2) last,
+    # with the step counts given
+    import copy
+    for w in SUITE:
+        sub = copy.copy(args)
+        sub.workload = w
+        sub.steps = min(args.steps, 3)
+        sub.warmup = 3
+        try:
+            run_workload(sub, ws, rank)
+        except Exception as e:  # a failed line is reported, the suite goes on
+            if rank == 0:
+                print(json.dumps({"workload": w, "error": f"{type(e).__name__}: {e}"}), flush=True)
+        import gc
+        gc.collect()
+    args.workload = "pt_pubo"
+    run_workload(args, ws, rank)
+
+
+# configurations printed before the headline by a run without --workload
+SUITE = ["sa_ising", "pa_square", "batch_cubic", "serving"]
+
+
+def run_workload(args, ws, rank):
     if args.workload == "batch_cubic":
         main_batch(args, ws, rank)
         return
@@ -412,6 +450,9 @@ def main():
         return
     if args.workload == "pf_sa":
         main_pf(args, ws, rank)
+        return
+    if args.workload == "serving_1e5":
+        main_serving(args, ws, rank)
         return
 
     import torch
@@ -546,8 +587,9 @@ def main():
             sys.exit(f"parity check failed: {parity['mismatched']}")
 
 
-def serving_requests(n=48, rate=200.0, seed=4):
-    """Requests of the serving configuration (bounded sample: N up to 1e4)."""
+def serving_requests(n=48, rate=200.0, seed=4, nmax=1e4):
+    """Requests of the serving configuration: Poisson arrivals at `rate`, the
+    first n of them, N log-uniform in [100, nmax]."""
     import numpy as np
     from qiotoolkit_gb300 import instances as I
     rng = np.random.default_rng(seed)
@@ -555,7 +597,7 @@ def serving_requests(n=48, rate=200.0, seed=4):
     out = []
     for i in range(n):
         kind = int(rng.integers(0, 3))
-        N = int(np.exp(rng.uniform(np.log(100), np.log(1e4))))
+        N = int(np.exp(rng.uniform(np.log(100), np.log(nmax))))
         sweeps = int(rng.integers(200, 5001))
         pt = bool(rng.integers(0, 2))
         if kind == 0:
@@ -707,7 +749,9 @@ def main_serving(args, ws, rank):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     q.load()
-    reqs = serving_requests()
+    big = args.workload == "serving_1e5"
+    reqs = serving_requests(n=300, nmax=1e5) if big else serving_requests(n=200)
+    budget = (1 << 30) if big else 0
     models = [q.Model(k, off=o, ids=i, coef=c) for _, k, (o, i, c), _, _ in reqs]
 
     def attempts(m, target, p):
@@ -717,11 +761,13 @@ def main_serving(args, ws, rank):
 
     n_att = sum(attempts(m, t, p) for m, (_, _, _, t, p) in zip(models, reqs))
 
-    def serve(max_active):
-        srv = q.Server(max_active=max_active)
+    foot = []
+
+    def serve(max_active, count=None):
+        srv = q.Server(memory_budget_bytes=budget, max_active=max_active)
         t0 = time.perf_counter()
         ids = []
-        for m, (ta, _, _, target, p) in zip(models, reqs):
+        for m, (ta, _, _, target, p) in list(zip(models, reqs))[:count]:
             d = t0 + ta - time.perf_counter()
             if d > 0:
                 time.sleep(d)
@@ -729,20 +775,27 @@ def main_serving(args, ws, rank):
         best = [srv.wait(i)["solutions"]["cost"] for i in ids]
         dt = time.perf_counter() - t0
         st = srv.stats()
+        foot.extend(srv.request_bytes(i) for i in ids)
         srv.close()
         return dt, st, best
 
-    serve(64)  # warm-up: module loading, table uploads
+    serve(64, 8)  # warm-up: module loading, table uploads
     with ClockSampler(local) as clk:
         dt_mix, st_mix, best_mix = serve(64)
-    dt_one, st_one, best_one = serve(1)
-    same = best_mix == best_one
+    # continuous batching against a queue alone, on the first 48 requests
+    # (the queue alone serves them one after another)
+    nq = 0 if big else 48
+    if nq:
+        dt_q48, st_q48, best_q48 = serve(64, nq)
+        dt_one, st_one, best_one = serve(1, nq)
+        same = best_q48 == best_one
+    
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as O
         threads = os.cpu_count() or 1
         t_cpu, a_cpu = 0.0, 0
-        for j in range(0, len(reqs), 6):
+        for j in range(0, len(reqs), 20):
             _, k, (o, i, c), target, p = reqs[j]
             om = O.Model(k, off=o, ids=i, coef=c, release=True)
             t0 = time.perf_counter()
@@ -757,7 +810,7 @@ def main_serving(args, ws, rank):
         rate = a_cpu / t_cpu
         cpu = {"value": len(reqs) / (n_att / rate), "unit": "instances/s", "cores": threads,
                "kind": "port",
-               "sample": f"oracle on every 6th request ({a_cpu:.3g} attempts in {t_cpu:.1f} s), "
+               "sample": f"oracle on every 20th request ({a_cpu:.3g} attempts in {t_cpu:.1f} s), "
                          f"requests one after another, extrapolated by attempts"}
     if rank == 0:
         line = {
@@ -765,15 +818,20 @@ def main_serving(args, ws, rank):
             "unit": "instances/s", "n_gpus": ws, "steps": 1, "warmup": 1,
             "ms_per_step": dt_mix * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS["serving"]["desc"], "requests": len(reqs),
-                       "attempts": n_att, "max_active": 64},
+            "config": {"workload": WORKLOADS[args.workload]["desc"], "requests": len(reqs),
+                       "attempts": n_att, "max_active": 64, "memory_budget_bytes": budget,
+                       "largest_request_vars": int(max(m.n_vars for m in models))},
             "latency_ms": {"p50": st_mix.p50_ms, "p99": st_mix.p99_ms, "max": st_mix.max_ms},
             "attempts_per_s": n_att / dt_mix,
             "peak_active": int(st_mix.peak_active),
-            "queue_alone": {"value": len(reqs) / dt_one, "unit": "instances/s",
-                            "latency_ms": {"p50": st_one.p50_ms, "p99": st_one.p99_ms}},
-            "speedup_vs_queue_alone": dt_one / dt_mix,
-            "same_results_alone_and_in_mix": bool(same),
+            "admission": {"budget_bytes": int(st_mix.budget_bytes),
+                          "largest_request_bytes": int(max(foot)) if foot else None,
+                          "sum_request_bytes": int(sum(foot[8:8 + len(reqs)])) if foot else None},
+            "queue_alone": ({"requests": nq, "value": nq / dt_one, "unit": "instances/s",
+                             "latency_ms": {"p50": st_one.p50_ms, "p99": st_one.p99_ms},
+                             "continuous_batching_value": nq / dt_q48,
+                             "speedup": dt_one / dt_q48,
+                             "same_results_alone_and_in_mix": bool(same)} if nq else None),
             "e2e": {"value": len(reqs) / dt_mix, "unit": "instances/s",
                     "h2d_bytes_per_step": int(sum(m.info.device_bytes for m in models)),
                     "d2h_bytes_per_step": int(sum(8 * m.n_vars for m in models))},
