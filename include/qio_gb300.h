@@ -88,8 +88,9 @@ typedef struct qio_solver_stats {
   uint64_t kernel_launches;/* kernels launched by qio_solver_run           */
   double sweep_kernel_ms;  /* CUDA-event time of the sweep kernels         */
   double run_ms;           /* CUDA-event time of the whole run             */
-  uint64_t near_ties;      /* PT swaps whose device exp() was within 1e-15 of
-                              the uniform draw (replay parity caveat)      */
+  uint64_t near_ties;      /* PT swaps whose uniform draw was within 1e-15 of
+                              the device exp(), decided with the correctly
+                              rounded exp instead                          */
   int64_t device_bytes;    /* HBM held by the solver                       */
   uint64_t windows;        /* 32-variable evaluation windows committed; the
                               mean committed window is attempts / windows */

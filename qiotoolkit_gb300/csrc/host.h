@@ -211,6 +211,7 @@ class Solver
   int kernel = 0;          // sweep kernel: 0 auto, 1 one walker per warp, 2 one walker per lane,
                            // 3 level schedule (one walker per warp, counter streams),
                            // 4 cached local fields (two warps per walker)
+  bool auto_fields = true;  // "auto" may pick the cached-field sweep (the server's solves do not)
   // CUDA-event pairs around sweep launches (profile mode)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
   size_t prof_used = 0;

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <mutex>
 
+#include "exp_cr.cuh"
 #include "qio_internal.h"
 
 namespace qio
@@ -1328,31 +1329,15 @@ __global__ void pt_swap_kernel(SwapArgs a)
     const int wa = base + i, wb = base + i + 1;
     const double x = __dmul_rn(__dsub_rn(a.cost[a.slot_of[wa]], a.cost[a.slot_of[wb]]),
                                __dsub_rn(a.beta[wa], a.beta[wb]));
-    const double e = exp(x);
-    const bool accept = u < e;
+    double e = exp(x);
     if (fabs(u - e) <= 1e-15 * e)
     {
+      // near tie: the correctly rounded exp, which the C library's exp
+      // (the reference's) returns except for its rare misroundings
+      e = dd::exp_cr(x);
       atomicAdd(a.near_ties, 1ULL);
-      if (a.replay && a.ties)
-      {
-        const int idx = atomicAdd(a.tie_n, 1);
-        if (idx < kPtTieCap)
-        {
-          PtTie t;
-          t.w = wa;
-          t.dec = accept ? 1 : 0;
-          t.slot_a = a.slot_of[wa];
-          t.slot_b = a.slot_of[wb];
-          t.dir_a = a.dir[wa];
-          t.dir_b = a.dir[wb];
-          t.x = x;
-          t.u = u;
-          t.acc_a = a.swap_acc[wa];
-          a.ties[idx] = t;
-        }
-      }
     }
-    if (accept)
+    if (u < e)
     {
       int t = a.slot_of[wa];
       a.slot_of[wa] = a.slot_of[wb];

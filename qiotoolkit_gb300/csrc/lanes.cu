@@ -161,21 +161,28 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
     const float nbeta_f = -approx_float(beta);
     const unsigned long long ctr0 = (unsigned long long)swp * (unsigned long long)Sz;
     natt += (unsigned long long)Sz;
+    // records two attempts ahead and row offsets three ahead: no attempt
+    // waits on a dependent pair of L2 loads (row offset, then records)
+    const int nrow = md->n_vars;  // row has nrow + 1 entries
     int qb = __ldg(row), qe = __ldg(row + 1);
-    R cur[kPre];
+    int qe1 = (Sz > 1) ? __ldg(row + min(2, nrow)) : qe;
+    int qe2 = (Sz > 2) ? __ldg(row + min(3, nrow)) : qe1;
+    R cur[kPre], nx1[kPre];
 #pragma unroll
     for (int j = 0; j < kPre; j++)
+    {
       if (qb + j < qe) cur[j] = __ldg(rec + qb + j);
+      if (qe + j < qe1) nx1[j] = __ldg(rec + qe + j);
+    }
     uint32_t cw = 0;  // current word of v
     for (int v = 0; v < Sz; v++)
     {
-      // the next variable's records, one attempt ahead
-      const int qb1 = qe;
-      const int qe1 = (v + 1 < Sz) ? __ldg(row + v + 2) : qe;
-      R nxt[kPre];
+      // variable v + 2's records and v + 4's row end
+      const int qe3 = (v + 3 < Sz) ? __ldg(row + min(v + 4, nrow)) : qe2;
+      R nx2[kPre];
 #pragma unroll
       for (int j = 0; j < kPre; j++)
-        if (qb1 + j < qe1) nxt[j] = __ldg(rec + qb1 + j);
+        if (qe1 + j < qe2) nx2[j] = __ldg(rec + qe1 + j);
       if ((v & 31) == 0) cw = sp[(size_t)(v >> 5) * G];
       const uint32_t sv = (cw >> (v & 31)) & 1u;
       long long idE = 0;
@@ -218,9 +225,15 @@ __global__ void __launch_bounds__(128) lw_sweep_kernel(LwArgs a)
         else dE = neg2x(diff);
       }
 #pragma unroll
-      for (int j = 0; j < kPre; j++) cur[j] = nxt[j];
-      qb = qb1;
+      for (int j = 0; j < kPre; j++)
+      {
+        cur[j] = nx1[j];
+        nx1[j] = nx2[j];
+      }
+      qb = qe;
       qe = qe1;
+      qe1 = qe2;
+      qe2 = qe3;
       bool acc;
       if (INT ? idE <= 0 : le_zero(dE)) acc = true;
       else

@@ -378,21 +378,6 @@ size_t qmc_level_smem(int trotter, int nw);
 cudaError_t launch_qmc_levels(const QmcArgs& a, cudaStream_t s);
 
 // PT: label swaps + observables, one thread per restart.
-// A replica swap whose uniform draw fell within 1e-15 of the device's
-// exp(x): the kernel decides it provisionally and records the pair as it was
-// before the decision; the host decides it again with the C library's exp
-// (the reference's, solver/parallel_tempering.h:126-131) and rewrites the
-// pair when the decisions differ.
-struct PtTie
-{
-  int w;            // walker of the pair's lower position
-  int dec;          // the kernel's decision
-  int slot_a, slot_b, dir_a, dir_b;  // before the decision
-  double x, u;      // exp argument and uniform draw
-  unsigned long long acc_a;          // swap_acc[w] before the decision
-};
-static const int kPtTieCap = 256;
-
 struct SwapArgs
 {
   int restarts;
@@ -414,8 +399,6 @@ struct SwapArgs
   int replay;
   uint64_t* master;         // replay: per restart master PCG state
   const unsigned long long* swap_key;  // counter: per restart key
-  PtTie* ties;              // replay: near-tie records (kPtTieCap), or null
-  int* tie_n;               // records written this launch (reset by the host)
 };
 cudaError_t launch_pt_swap(const SwapArgs& a, cudaStream_t s);
 

@@ -113,6 +113,11 @@ class ServerImpl : public Server
     std::unique_ptr<Request> r(new Request());
     r->model = m;
     r->solver = make_solver(m, target, doc);  // params are validated here
+    // "auto" keeps the windowed sweep for served solves: a mix is bound by
+    // its longest chain, where the field-cached sweep gains nothing, and one
+    // run with 200 solves in flight on it ended in an illegal-address fault
+    // that was not located (a request may still ask for "fields")
+    r->solver->auto_fields = false;
     if (r->solver->has_cost_limit || r->solver->has_time_limit)
       fail(1, "served solves run their full sweep budget: `cost_limit` and `timeout` are not supported");
     r->footprint = footprint_of(*m, *r->solver);

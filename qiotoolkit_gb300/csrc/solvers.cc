@@ -476,7 +476,7 @@ bool fields_for(const Solver& s, const HostModel& m, const Population& P, bool f
               "and walker state that fits shared memory");
     return true;
   }
-  return s.kernel == 0 && ok && m.flavor == F_PARITY;
+  return s.kernel == 0 && s.auto_fields && ok && m.flavor == F_PARITY;
 }
 
 // beta as Metropolis::set_beta / set_temperature store it
@@ -855,44 +855,6 @@ class ParallelTempering : public Solver
   int* dir = nullptr;
   double *obs_acc = nullptr, *obs_cost = nullptr, *obs_dir = nullptr;
   unsigned long long *swap_acc = nullptr, *swap_cnt = nullptr, *ties = nullptr;
-  PtTie* tie_rec = nullptr;  // near-tie records of the last swap launch
-  int* tie_n = nullptr;
-  uint64_t resolved_ties = 0, changed_ties = 0;
-
-  // The host decides the last swap launch's near ties again with the C
-  // library's exp, as the reference does (solver/parallel_tempering.h:
-  // 126-131), and rewrites each pair whose decision differs: slot labels,
-  // directions and swap count as they were before the decision, swapped or
-  // not, then the end directions of the ladder (solver/parallel_tempering.h:
-  // 185-186).  Replay mode only (counter mode has no reference stream).
-  void resolve_ties(cudaStream_t st)
-  {
-    int n = 0;
-    cuda_check(cudaMemcpyAsync(&n, tie_n, 4, cudaMemcpyDeviceToHost, st), "D2H");
-    cuda_check(cudaStreamSynchronize(st), "sync");
-    if (n == 0) return;
-    if (n > kPtTieCap) fail(4, "parallel tempering: more near-tie swaps in one step than can be resolved");
-    std::vector<PtTie> t(n);
-    cuda_check(cudaMemcpy(t.data(), tie_rec, (size_t)n * sizeof(PtTie), cudaMemcpyDeviceToHost), "D2H");
-    const int TT = T();
-    for (const PtTie& r : t)
-    {
-      resolved_ties++;
-      const int dec = r.u < std::exp(r.x) ? 1 : 0;
-      if (dec == r.dec) continue;
-      changed_ties++;
-      const int sl[2] = {dec ? r.slot_b : r.slot_a, dec ? r.slot_a : r.slot_b};
-      int dr[2] = {dec ? r.dir_b : r.dir_a, dec ? r.dir_a : r.dir_b};
-      const int base = (r.w / TT) * TT;
-      if (r.w == base) dr[0] = 0;
-      if (r.w + 1 == base + TT - 1) dr[1] = 1;
-      const unsigned long long acc = r.acc_a + (unsigned long long)dec;
-      cuda_check(cudaMemcpy(P.slot_of + r.w, sl, 8, cudaMemcpyHostToDevice), "H2D");
-      cuda_check(cudaMemcpy(dir + r.w, dr, 8, cudaMemcpyHostToDevice), "H2D");
-      cuda_check(cudaMemcpy(swap_acc + r.w, &acc, 8, cudaMemcpyHostToDevice), "H2D");
-    }
-    cuda_check(cudaMemsetAsync(tie_n, 0, 4, st), "memset");
-  }
   uint64_t* master = nullptr;
   unsigned long long* swap_key = nullptr;
   Pcg* ext_master = nullptr;  // repeated runs: ladder 0's streams fork from this stream
@@ -1002,7 +964,7 @@ class ParallelTempering : public Solver
     auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
     size_t o_dir = take(W * 4), o_oa = take(W * 8), o_oc = take(W * 8), o_od = take(W * 8),
            o_sa = take(W * 8), o_sc = take(W * 8), o_t = take(8), o_m = take(K * 8),
-           o_k = take(K * 8), o_tr = take(kPtTieCap * sizeof(PtTie)), o_tn = take(4);
+           o_k = take(K * 8);
     if (!aux.ptr) aux = DevBuf(off);
     char* b = (char*)aux.ptr;
     dir = (int*)(b + o_dir);
@@ -1012,8 +974,6 @@ class ParallelTempering : public Solver
     swap_acc = (unsigned long long*)(b + o_sa);
     swap_cnt = (unsigned long long*)(b + o_sc);
     ties = (unsigned long long*)(b + o_t);
-    tie_rec = (PtTie*)(b + o_tr);
-    tie_n = (int*)(b + o_tn);
     master = (uint64_t*)(b + o_m);
     swap_key = (unsigned long long*)(b + o_k);
     cuda_check(cudaMemsetAsync(aux.ptr, 0, off, st), "memset");
@@ -1103,8 +1063,6 @@ class ParallelTempering : public Solver
     sw.swap_acc = swap_acc;
     sw.swap_cnt = swap_cnt;
     sw.near_ties = ties;
-    sw.ties = replay ? tie_rec : nullptr;
-    sw.tie_n = tie_n;
     sw.replay = replay ? 1 : 0;
     sw.master = master;
     sw.swap_key = swap_key;
@@ -1124,7 +1082,6 @@ class ParallelTempering : public Solver
       P.fvalid = fields;
       sw.step = s;
       cuda_check(launch_pt_swap(sw, st), "swap kernel");
-      if (replay) resolve_ties(st);
       launches += 2;
       s++;
       if (has_cost_limit)
@@ -1191,8 +1148,6 @@ class ParallelTempering : public Solver
     sw.swap_acc = swap_acc;
     sw.swap_cnt = swap_cnt;
     sw.near_ties = ties;
-    sw.ties = replay ? tie_rec : nullptr;
-    sw.tie_n = tie_n;
     sw.replay = replay ? 1 : 0;
     sw.master = master;
     sw.swap_key = swap_key;
@@ -1208,7 +1163,6 @@ class ParallelTempering : public Solver
       P.fvalid = fields;
       sw.step = step_pos;
       cuda_check(launch_pt_swap(sw, st), "swap kernel");
-      if (replay) resolve_ties(st);
       launches += 2;
     }
     last_step = step_pos;
@@ -2416,6 +2370,10 @@ class SABatch : public Batch
   cudaStream_t graph_stream = nullptr;
   int plan_wpb = 0, plan_smem = 1;
   int64_t graph_launches = 0;
+  // the population's layout: instances longest first (largest N first), so
+  // that the warps of the lane kernel hold instances of equal size and the
+  // longest solves start first; instance i's walkers are block pos[i]
+  std::vector<int> order, pos;
   bool profile = false;  // events around the sweep launches (runs without a graph)
   double sweep_ms = 0;
 
@@ -2478,10 +2436,16 @@ class SABatch : public Batch
     P.alloc_sizes(N, M, W, W, false, std::max<int64_t>(1, steps));
     // every model on the device before any capture (uploads allocate)
     for (auto* m : models) m->device_view(false);
-    for (auto& v : views)
+    order.resize(models.size());
+    for (size_t i = 0; i < models.size(); i++) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return models[x]->N > models[y]->N; });
+    pos.resize(models.size());
+    for (size_t k = 0; k < order.size(); k++) pos[order[k]] = (int)k;
+    for (size_t i = 0; i < views.size(); i++)
     {
-      v->BP = &P;
-      v->first = (int)(&v - &views[0]) * R;
+      views[i]->BP = &P;
+      views[i]->first = pos[i] * R;
     }
     // stream forks of each instance: rngs_[i] = rng_->fork() in index order
     // (solver/simulated_annealing.h:53-56), the same for every instance
@@ -2501,7 +2465,7 @@ class SABatch : public Batch
       std::vector<int> model_of(W), local_of(W);
       for (int r = 0; r < W; r++)
       {
-        model_of[r] = r / R;
+        model_of[r] = order[r / R];
         local_of[r] = r % R;
       }
       L.setup(dm, model_of, W, local_of, smem);
@@ -2536,10 +2500,10 @@ class SABatch : public Batch
     {
       InitArgs a{};
       a.m = models[i]->device_view(false);
-      a.p = pop_slice(P.pop, (int)i * R, R);
+      a.p = pop_slice(P.pop, pos[i] * R, R);
       a.n_walkers = R;
       a.replay = replay ? 1 : 0;
-      a.rng = P.rng + (size_t)i * R;
+      a.rng = P.rng + (size_t)pos[i] * R;
       a.seed = seed;
       a.key_base = 0;
       a.key_div = (long long)1 << 40;
@@ -2568,14 +2532,14 @@ class SABatch : public Batch
       {
         SweepArgs a{};
         a.m = models[i]->device_view(false);
-        a.p = pop_slice(P.pop, (int)i * R, R);
+        a.p = pop_slice(P.pop, pos[i] * R, R);
         a.n_streams = R;
         a.n_walkers = R;
         a.beta = P.beta;
         a.bs_w = 0;
         a.bs_s = 1;
         a.replay = replay ? 1 : 0;
-        a.rng = P.rng + (size_t)i * R;
+        a.rng = P.rng + (size_t)pos[i] * R;
         a.seed = seed;
         a.key_base = 0;
         a.key_div = (long long)1 << 40;
@@ -2705,8 +2669,9 @@ class SABatch : public Batch
     cuda_check(cudaMemcpy(low.data(), P.pop.lowest, (size_t)W * 8, cudaMemcpyDeviceToHost), "D2H");
     for (size_t i = 0; i < models.size(); i++)
     {
-      double b = low[i * R];
-      for (int k = 1; k < R; k++) b = std::min(b, low[i * R + k]);
+      const size_t f = (size_t)pos[i] * R;
+      double b = low[f];
+      for (int k = 1; k < R; k++) b = std::min(b, low[f + k]);
       out[i] = b + models[i]->const_cost;
     }
   }

@@ -208,9 +208,11 @@ def test_ks_independent_streams():
 
 
 def test_pt_near_tie_swaps_follow_the_c_library_exp():
-    """Replica swaps whose uniform draw lies within 1e-15 of exp(x) are
-    decided again on the host with the C library's exp, as the reference
-    does (solver/parallel_tempering.h:126-131).  A one-spin model with field
+    """Replica swaps whose uniform draw lies within 1e-15 of the device's
+    exp(x) are decided with the correctly rounded exp (double-double
+    evaluation), the value the C library's exp returns in the reference
+    (solver/parallel_tempering.h:126-131) but for its rare misroundings.  A
+    one-spin model with field
     1 and the ladder beta = {0, b}: with costs +1 / -1 the swap argument is
     x = -2b, and b = -log(u) / 2 for the step-0 swap draw u of the master
     stream puts exp(x) on u to rounding.  Every seed's trajectory and
