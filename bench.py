@@ -9,10 +9,12 @@ One step = one complete solve (init + 500 sweeps + 500 swap phases of all 512
 walkers) = 1.05e9 flip attempts.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|serving|pf_sa|tabu_ising|ssmc_ising|
-                              qmc_ising|qmc_ising_counter]
+                  [--workload pt_pubo|sa_ising|pa_square|batch_cubic|batch_pubo|serving|serving_1e5|
+                              pf_sa|tabu_ising|ssmc_ising|qmc_ising|qmc_ising_counter]
 
-Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
+Without --workload: one JSON line per configuration (SA, PA, batch, serving),
+each from a child process, then the PT headline.  With --workload: that
+workload's JSON line (rank 0).  `value` is device-timed (CUDA events on the
 launch stream, inputs resident in HBM, L2 flushed before each step); `e2e`
 goes through the C ABI from host buffers (model build + upload, solve,
 results back to the host) on the host clock.
@@ -80,9 +82,15 @@ WORKLOADS = {
                              "(64-8000 spins), 16 restarts each, linear beta 0.1->3.0 over 2000 "
                              "sweeps, one captured CUDA graph",
                         target="simulatedannealing.qiotoolkit"),
+    "batch_pubo": dict(desc="Batched SA on many-body models: 512 random PUBO instances, N log-uniform "
+                            "in [100, 2000], 3N terms of orders 1-4 with N(0,1) FP64 coefficients, 16 "
+                            "restarts each, linear beta 0.1->3.0 over 500 sweeps, one captured CUDA "
+                            "graph (the windowed kernel's persistent queue)",
+                       target="simulatedannealing.qiotoolkit"),
 }
 
 BATCH_PARAMS = {"seed": 0, "sweeps": 2000, "restarts": 16, "beta_start": 0.1, "beta_stop": 3.0}
+BATCH_PUBO_PARAMS = {"seed": 0, "sweeps": 500, "restarts": 16, "beta_start": 0.1, "beta_stop": 3.0}
 
 
 def batch_instances(n=512):
@@ -92,6 +100,16 @@ def batch_instances(n=512):
     rng = np.random.default_rng(2)
     Ls = rng.integers(4, 21, size=n)
     return [(int(L), I.cubic_pm_j(int(L), seed=1000 + i)) for i, L in enumerate(Ls)]
+
+
+def batch_pubo_instances(n=512):
+    """512 random PUBO instances, N log-uniform in [100, 2000] from seed 3,
+    3N terms each, seeded per instance; keyed by N."""
+    import numpy as np
+    from qiotoolkit_gb300 import instances as I
+    rng = np.random.default_rng(3)
+    Ns = np.exp(rng.uniform(np.log(100), np.log(2000), size=n)).astype(int)
+    return [(int(N), I.random_pubo(int(N), 3 * int(N), seed=2000 + i)) for i, N in enumerate(Ns)]
 
 
 # the sweep kernel a solver used (qio_solver_stats.sweep_kernel)
@@ -465,7 +483,7 @@ SUITE = ["sa_ising", "pa_square", "batch_cubic", "serving"]
 
 
 def run_workload(args, ws, rank):
-    if args.workload == "batch_cubic":
+    if args.workload in ("batch_cubic", "batch_pubo"):
         main_batch(args, ws, rank)
         return
     if args.workload == "serving":
@@ -869,21 +887,24 @@ def main_serving(args, ws, rank):
 def main_batch(args, ws, rank):
     """Batched workload: instances/s of one captured graph over all instances,
     beside the plain path (one solve per instance) timed on one instance per
-    distinct L and extrapolated to the batch's L distribution."""
+    distinct L (cubic lattices) or on every 32nd instance (PUBO) and
+    extrapolated to the whole batch by its variable counts."""
     import numpy as np
     import torch
     import qiotoolkit_gb300 as q
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     q.load()
-    params = dict(BATCH_PARAMS)
+    pubo = args.workload == "batch_pubo"
+    params = dict(BATCH_PUBO_PARAMS if pubo else BATCH_PARAMS)
     if args.sweeps:
         params["sweeps"] = args.sweeps
-    target = WORKLOADS["batch_cubic"]["target"]
+    target = WORKLOADS[args.workload]["target"]
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
-    inst = batch_instances()
-    models = [q.Model("ising", off=o, ids=i, coef=c) for _, (o, i, c) in inst]
+    inst = batch_pubo_instances() if pubo else batch_instances()
+    kind = "pubo" if pubo else "ising"
+    models = [q.Model(kind, off=o, ids=i, coef=c) for _, (o, i, c) in inst]
     n_att = sum(m.n_vars for m in models) * params["restarts"] * params["sweeps"]
     batch = q.Batch(models, target, {"params": params})
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -919,7 +940,12 @@ def main_batch(args, ws, rank):
     pst = prof.stats()
     kernel_ms = pst.sweep_kernel_ms if pst.sweep_kernel_ms > 0 else st.run_ms
     prof.close()
-    bpa = 45.0  # 8 row bounds + 6 x (4 id + 1 coefficient + 1 state) + 1 own state
+    if pubo:
+        # 8 row bounds + per incidence (4 term id + 8 coefficient + 1 term state) + 1 own state
+        kbar = sum(m.info.n_incidences for m in models) / sum(m.n_vars for m in models)
+        bpa = 8.0 + 13.0 * kbar + 1.0
+    else:
+        bpa = 45.0  # 8 row bounds + 6 x (4 id + 1 coefficient + 1 state) + 1 own state
     achieved = bpa * n_att / (kernel_ms / 1e3) / 1e9
     peak, peak_src = peaks()
 
@@ -928,7 +954,7 @@ def main_batch(args, ws, rank):
     # the stream), model and solver resident, after a warm-up solve
     per_L, rel = {}, []
     for idx, (L, _) in enumerate(inst):
-        if L in per_L:
+        if L in per_L or (pubo and idx % 32):
             continue
         s = q.Solver(models[idx], target, {"params": params})
         s.init(sh).run(sh)
@@ -947,7 +973,12 @@ def main_batch(args, ws, rank):
         per_L[L] = best_ms / 1e3
         rel.append(abs(low_batch[idx] - c) / max(abs(c), 1e-12))
         s.close()
-    plain_s = sum(per_L[L] for L, _ in inst)
+    if pubo:
+        # seconds per variable on the sampled instances, over the batch's sizes
+        xs = sorted(per_L)
+        plain_s = sum(float(np.interp(L, xs, [per_L[x] / x for x in xs])) * L for L, _ in inst)
+    else:
+        plain_s = sum(per_L[L] for L, _ in inst)
     plain_value = len(models) / plain_s
 
     e2e = None
@@ -971,29 +1002,31 @@ def main_batch(args, ws, rank):
         from oracle import oracle as O
         threads = os.cpu_count() or 1
         t_cpu, L_seen = {}, set()
+        nv = (lambda L: L) if pubo else (lambda L: L ** 3)
         for idx, (L, (o, i, c)) in enumerate(inst):
-            if L in L_seen or L % 4:
+            if L in L_seen or (idx % 64 if pubo else L % 4):
                 continue
             L_seen.add(L)
-            om = O.Model("ising", off=o, ids=i, coef=c, release=True)
+            om = O.Model(kind, off=o, ids=i, coef=c, release=True)
             t0 = time.perf_counter()
             O.run(om, "sa", seed=0, step_limit=params["sweeps"], restarts=params["restarts"],
                   threads=threads, sched=("linear", params["beta_start"], params["beta_stop"]))
-            t_cpu[L] = (time.perf_counter() - t0) / (L ** 3)
-        # seconds per spin at each sampled L, interpolated over the batch's sizes
+            t_cpu[L] = (time.perf_counter() - t0) / nv(L)
+        # seconds per variable at each sampled size, interpolated over the batch's sizes
         xs = sorted(t_cpu)
-        cpu_s = sum(float(np.interp(L, xs, [t_cpu[x] for x in xs])) * L ** 3 for L, _ in inst)
+        cpu_s = sum(float(np.interp(L, xs, [t_cpu[x] for x in xs])) * nv(L) for L, _ in inst)
+        what = "every 64th instance (N in %s)" % xs if pubo else "one instance for each L in %s" % xs
         cpu = {"value": len(models) / cpu_s, "unit": "instances/s", "cores": threads, "kind": "port",
-               "sample": f"oracle SA (OpenMP over restarts) on one instance for each L in {xs}, "
-                         f"full sweeps and restarts; per-spin time interpolated over the 512 sizes"}
+               "sample": f"oracle SA (OpenMP over restarts) on {what}, full sweeps and restarts; "
+                         f"per-variable time interpolated over the 512 sizes"}
 
     if rank == 0:
         line = {
             "metric": "instances/s batched", "value": value, "unit": "instances/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": WORKLOADS["batch_cubic"]["desc"], "instances": len(models),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if pubo else "int32", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload]["desc"], "instances": len(models),
                        "total_spins": int(sum(m.n_vars for m in models)),
                        "attempts_per_step": n_att, "rng_mode": "replay",
                        "plan": {"kernel": "lanes" if st.kernel == 2 else "warp",
@@ -1002,8 +1035,10 @@ def main_batch(args, ws, rank):
                        "l2": "flushed before each step (256 MB write)"},
             "attempts_per_s": n_att * args.steps * ws / total_s,
             "plain_per_instance": {"value": plain_value, "unit": "instances/s",
-                                   "sample": "one plain solve (default kernel choice) per distinct L, "
-                                             "device-timed like the batch (CUDA events around init + run, "
+                                   "sample": ("one plain solve (default kernel choice) on every 32nd "
+                                              "instance" if pubo else
+                                              "one plain solve (default kernel choice) per distinct L") +
+                                             ", device-timed like the batch (CUDA events around init + run, "
                                              "model resident, best of 2 after a warm-up), extrapolated "
                                              "over the 512 instances"},
             "speedup_vs_plain": value / plain_value,
@@ -1012,7 +1047,8 @@ def main_batch(args, ws, rank):
             "gpu_launches": int(st.launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
-                         "kernel": "lw_sweep_kernel", "bytes_per_attempt": bpa,
+                         "kernel": "sweep_kernel" if st.kernel == 1 else "lw_sweep_kernel",
+                         "bytes_per_attempt": bpa,
                          "avg_launch_ms": kernel_ms},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),

@@ -242,11 +242,16 @@ qio_status qio_solver_destroy(qio_solver* s);
 typedef struct qio_batch qio_batch;
 typedef struct qio_batch_stats {
   double run_ms;            /* last run: CUDA events around it              */
-  int64_t launches;         /* kernel launches per run                      */
+  int64_t launches;         /* kernel launches per run (one init per
+                               instance; one sweep launch per kind of model
+                               with the windowed kernel's queue, else one
+                               per instance)                               */
   int64_t walkers;          /* instances x restarts                         */
   int64_t device_bytes;     /* population + lane groups                     */
   int32_t kernel;           /* 1: one walker per warp, 2: one walker per lane */
-  int32_t warps_per_block;  /* lane plan (0: spread the groups over the SMs) */
+  int32_t warps_per_block;  /* lane plan (0: spread the groups over the SMs);
+                               windowed kernel: walkers per block of its
+                               persistent queue launches                   */
   int32_t smem;             /* 1: walker words in shared memory             */
   int32_t graph;            /* 1: each run is one captured CUDA graph       */
   double sweep_kernel_ms;   /* "graph": false with "profile_kernels": true:

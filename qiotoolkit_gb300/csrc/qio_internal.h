@@ -139,6 +139,16 @@ struct SweepArgs
   // windowed kernel.  field_valid = 0: rebuild the fields from the state.
   int* field;
   int field_valid;
+  // batches (windowed kernel): walker r runs models[model_of[r]] with the
+  // counter key of walker local_of[r] of its own solve; with `queue` set,
+  // each warp takes walkers from the counter *queue (reset to 0 before the
+  // launch) until n_walkers are taken, in index order, and keeps walker r's
+  // PCG state in rng[r].  Null: a.m for every walker, stream w serving
+  // walkers w, w + n_streams, ...
+  const DevModel* models;
+  const int* model_of;
+  const int* local_of;
+  int* queue;
 };
 
 struct InitArgs
@@ -162,6 +172,9 @@ struct InitArgs
 void upload_tables(int device);  // ln table + PCG jump tables
 cudaError_t launch_init(const InitArgs& a, cudaStream_t s);
 cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int warps_per_block);
+// one warp's walker state (term bytes, spins, lowest) fits shared memory
+// beside the windowed kernel's tables and tiles (required by batch queues)
+bool sweep_state_fits(const SweepArgs& a);
 // field-cached sweep (fields.cu): ints of one slot's fields, and whether the
 // kernel can run this model with this population layout
 int64_t fc_words(int n_vars);

@@ -2359,6 +2359,7 @@ class SABatch : public Batch
   int R = 0, W = 0;
   int64_t steps = 0;
   bool replay = true, lanes = false, autotune = true, use_graph = true, smem = true;
+  bool full_sweep = false;  // maxsat_full_sweep: every MaxSat variable in a sweep
   uint32_t seed = 0;
   int kernel = 0;
   Population P;
@@ -2370,10 +2371,26 @@ class SABatch : public Batch
   cudaStream_t graph_stream = nullptr;
   int plan_wpb = 0, plan_smem = 1;
   int64_t graph_launches = 0;
-  // the population's layout: instances longest first (largest N first), so
+  // the population's layout: instances grouped by kernel flavour and
+  // coefficient kind, longest first within a group (largest N first), so
   // that the warps of the lane kernel hold instances of equal size and the
   // longest solves start first; instance i's walkers are block pos[i]
   std::vector<int> order, pos;
+  // windowed-kernel batches: one persistent launch per group of walkers
+  // [first, last) that share a flavour and coefficient kind, fed by a device
+  // queue in population order (so longest first)
+  bool queued = false;
+  struct Group
+  {
+    int first, last;
+    const HostModel* model;  // any member (flavour and coefficient kind)
+  };
+  std::vector<Group> groups;
+  DevBuf qbuf;  // DevModel per instance, model_of, local_of, one queue counter per group
+  const DevModel* d_models = nullptr;
+  int* d_model_of = nullptr;
+  int* d_local_of = nullptr;
+  int* d_queue = nullptr;
   bool profile = false;  // events around the sweep launches (runs without a graph)
   double sweep_ms = 0;
 
@@ -2407,6 +2424,7 @@ class SABatch : public Batch
     seed = v0.seed;
     kernel = v0.kernel;
     smem = v0.smem_state;
+    full_sweep = v0.full_maxsat_sweep;
     Params p(doc["params"]);
     autotune = p.boolean("autotune", true);
     use_graph = p.boolean("graph", true);
@@ -2435,11 +2453,14 @@ class SABatch : public Batch
     }
     P.alloc_sizes(N, M, W, W, false, std::max<int64_t>(1, steps));
     // every model on the device before any capture (uploads allocate)
-    for (auto* m : models) m->device_view(false);
+    for (auto* m : models) m->device_view(full_sweep);
     order.resize(models.size());
     for (size_t i = 0; i < models.size(); i++) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return models[x]->N > models[y]->N; });
+    auto kind_of = [&](int x) { return models[x]->flavor * 2 + (models[x]->int_mode ? 1 : 0); };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      if (kind_of(x) != kind_of(y)) return kind_of(x) < kind_of(y);
+      return models[x]->N > models[y]->N;
+    });
     pos.resize(models.size());
     for (size_t k = 0; k < order.size(); k++) pos[order[k]] = (int)k;
     for (size_t i = 0; i < views.size(); i++)
@@ -2461,7 +2482,7 @@ class SABatch : public Batch
     if (lanes)
     {
       std::vector<DevModel> dm;
-      for (auto* m : models) dm.push_back(m->device_view(false));
+      for (auto* m : models) dm.push_back(m->device_view(full_sweep));
       std::vector<int> model_of(W), local_of(W);
       for (int r = 0; r < W; r++)
       {
@@ -2470,8 +2491,88 @@ class SABatch : public Batch
       }
       L.setup(dm, model_of, W, local_of, smem);
     }
+    else
+      plan_queue();
     (void)st;
     prepared = true;
+  }
+
+  // The windowed kernel's queue plan: groups of one flavour and coefficient
+  // kind whose walker state fits a warp's shared memory; otherwise (or with
+  // `smem_state` off) one launch per instance.
+  void plan_queue()
+  {
+    groups.clear();
+    queued = smem;
+    for (size_t k = 0; k < order.size() && queued; k++)
+    {
+      const HostModel* m = models[order[k]];
+      const int first = (int)k * R;
+      if (groups.empty() || groups.back().model->flavor != m->flavor ||
+          groups.back().model->int_mode != m->int_mode)
+        groups.push_back({first, first + R, m});
+      else
+        groups.back().last = first + R;
+      SweepArgs a{};
+      a.m = m->device_view(full_sweep);
+      a.p = P.pop;
+      queued = sweep_state_fits(a);
+    }
+    if (!queued)
+    {
+      groups.clear();
+      return;
+    }
+    const size_t n = models.size();
+    const size_t o_mo = (n * sizeof(DevModel) + 255) & ~(size_t)255;
+    const size_t o_lo = o_mo + (((size_t)W * 4 + 255) & ~(size_t)255);
+    const size_t o_q = o_lo + (((size_t)W * 4 + 255) & ~(size_t)255);
+    qbuf = DevBuf(o_q + groups.size() * 4);
+    std::vector<DevModel> dm(n);
+    for (size_t i = 0; i < n; i++) dm[i] = models[i]->device_view(full_sweep);
+    std::vector<int> model_of(W), local_of(W);
+    for (int r = 0; r < W; r++)
+    {
+      model_of[r] = order[r / R];
+      local_of[r] = r % R;
+    }
+    char* b = (char*)qbuf.ptr;
+    cuda_check(cudaMemcpy(b, dm.data(), n * sizeof(DevModel), cudaMemcpyHostToDevice), "H2D models");
+    cuda_check(cudaMemcpy(b + o_mo, model_of.data(), (size_t)W * 4, cudaMemcpyHostToDevice), "H2D");
+    cuda_check(cudaMemcpy(b + o_lo, local_of.data(), (size_t)W * 4, cudaMemcpyHostToDevice), "H2D");
+    d_models = (const DevModel*)b;
+    d_model_of = (int*)(b + o_mo);
+    d_local_of = (int*)(b + o_lo);
+    d_queue = (int*)(b + o_q);
+  }
+
+  // one group's persistent sweep launch (its queue reset first)
+  void launch_group(size_t g, int64_t sweeps, int wpb, cudaStream_t st)
+  {
+    const Group& G = groups[g];
+    cuda_check(cudaMemsetAsync(d_queue + g, 0, 4, st), "memset");
+    SweepArgs a{};
+    a.m = G.model->device_view(full_sweep);
+    a.p = pop_slice(P.pop, G.first, G.last - G.first);
+    a.n_streams = G.last - G.first;
+    a.n_walkers = G.last - G.first;
+    a.beta = P.beta;
+    a.bs_w = 0;
+    a.bs_s = 1;
+    a.replay = replay ? 1 : 0;
+    a.rng = P.rng + G.first;
+    a.seed = seed;
+    a.key_base = 0;
+    a.key_div = (long long)1 << 40;
+    a.smem_state = 1;
+    a.err = device_error_flag();
+    a.sweep_base = 0;
+    a.n_sweeps = (int)sweeps;
+    a.models = d_models;
+    a.model_of = d_model_of + G.first;
+    a.local_of = d_local_of + G.first;
+    a.queue = d_queue + g;
+    cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
   }
 
   LwArgs lane_args() const
@@ -2499,10 +2600,13 @@ class SABatch : public Batch
     for (size_t i = 0; i < models.size(); i++)
     {
       InitArgs a{};
-      a.m = models[i]->device_view(false);
+      a.m = models[i]->device_view(full_sweep);
       a.p = pop_slice(P.pop, pos[i] * R, R);
       a.n_walkers = R;
-      a.replay = replay ? 1 : 0;
+      // a MaxSat walker draws its state one uniform() per variable
+      // (model/max_sat.h:144-150)
+      const bool ms = models[i]->kind == K_MAXSAT;
+      a.replay = replay ? (ms ? 2 : 1) : (ms ? 3 : 0);
       a.rng = P.rng + (size_t)pos[i] * R;
       a.seed = seed;
       a.key_base = 0;
@@ -2525,13 +2629,23 @@ class SABatch : public Batch
       cuda_check(launch_lw_store(la, L.max_words, L.max_terms, st), "lane store");
       n_launch += 3;
     }
+    else if (queued)
+    {
+      std::unique_ptr<EventTimer> t(profile ? new EventTimer(st) : nullptr);
+      for (size_t g = 0; g < groups.size(); g++)
+      {
+        launch_group(g, n_sweeps, plan_wpb > 0 ? plan_wpb : 4, st);
+        n_launch++;
+      }
+      if (t) sweep_ms = t->stop();
+    }
     else
     {
       std::unique_ptr<EventTimer> t(profile ? new EventTimer(st) : nullptr);
       for (size_t i = 0; i < models.size(); i++)
       {
         SweepArgs a{};
-        a.m = models[i]->device_view(false);
+        a.m = models[i]->device_view(full_sweep);
         a.p = pop_slice(P.pop, pos[i] * R, R);
         a.n_streams = R;
         a.n_walkers = R;
@@ -2554,14 +2668,36 @@ class SABatch : public Batch
     }
   }
 
-  // Launch plan for the lane kernel: warps per block and shared-memory
-  // groups, timed on a short trial of the batch itself.
+  // Launch plan, timed on a short trial of the batch itself: for the lane
+  // kernel warps per block and shared-memory groups; for the windowed
+  // kernel's queues warps per block (walkers per block: 1, 2, 4 or 8).
   void tune(cudaStream_t st)
   {
     plan_smem = smem ? 1 : 0;
     plan_wpb = 0;
-    if (!autotune || !lanes || steps <= 0) return;
+    if (!autotune || steps <= 0) return;
     const int64_t trial = std::max<int64_t>(1, std::min<int64_t>(steps, (steps + 99) / 100));
+    if (queued)
+    {
+      double best = 1e300;
+      int best_wpb = 4;
+      for (int wpb : {1, 2, 4, 8})
+      {
+        int n;
+        enqueue(st, 0, n);
+        EventTimer t(st);
+        for (size_t g = 0; g < groups.size(); g++) launch_group(g, trial, wpb, st);
+        const double ms = t.stop();
+        if (ms < best)
+        {
+          best = ms;
+          best_wpb = wpb;
+        }
+      }
+      plan_wpb = best_wpb;
+      return;
+    }
+    if (!lanes) return;
     double best = 1e300;
     int best_wpb = 0, best_sm = plan_smem;
     for (int sm = L.a.smem_words > 0 ? 1 : 0; sm >= 0; sm--)
@@ -2651,7 +2787,7 @@ class SABatch : public Batch
     stats_.smem = plan_smem;
     stats_.graph = use_graph ? 1 : 0;
     stats_.walkers = W;
-    stats_.device_bytes = (int64_t)(P.buf.bytes + L.bytes() + rng0.bytes);
+    stats_.device_bytes = (int64_t)(P.buf.bytes + L.bytes() + rng0.bytes + qbuf.bytes);
     stats_.sweep_kernel_ms = profile ? sweep_ms : 0.0;
   }
 

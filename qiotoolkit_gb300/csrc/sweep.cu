@@ -19,6 +19,7 @@
 // the ln-table comparison runs in FP32 with a rigorous error margin, falling
 // back to the exact FP64 expression only inside the margin.  Walker state
 // (term bytes, spins, lowest spins) lives in shared memory when it fits.
+#include <algorithm>
 #include <climits>
 #include <type_traits>
 
@@ -1030,7 +1031,7 @@ __device__ __forceinline__ void block_rounds_plain(const Smem& S, const DevModel
   __syncwarp();
 }
 
-template <int FL, bool REPLAY, bool INT, bool SMEM>
+template <int FL, bool REPLAY, bool INT, bool SMEM, bool BATCH>
 __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
 {
   using C = typename std::conditional<INT, int, double>::type;
@@ -1054,9 +1055,6 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
   const int wib = threadIdx.x >> 5;
   const int w = blockIdx.x * (blockDim.x >> 5) + wib;
   if (w >= a.n_streams) return;
-  const DevModel m = a.m;
-  const int Sz = m.sweep_size;
-  const int nwd = (m.n_vars + 31) >> 5;
   const bool staged = (FL == F_PARITY || FL == F_COUNTER);
   // per-warp region: [bars 16][dirty words 144][tiles 2][term bytes][spins][lowest]
   const int tile_bytes = staged ? (int)((sizeof(Tile<INT>) + 15) & ~15) : 0;
@@ -1074,10 +1072,21 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
   __syncwarp();
   unsigned phase0 = 0, phase1 = 0;
   Walk W;
-  W.rs = REPLAY ? a.rng[w] : 0;
+  W.rs = (REPLAY && !BATCH) ? a.rng[w] : 0;
+  // batches: the warp takes walkers from the queue in index order (the
+  // population lies longest instance first) until every walker is taken
+  auto take = [&]() -> int {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(a.queue, 1);
+    return __shfl_sync(kFull, q, 0);
+  };
 
-  for (int r = w; r < a.n_walkers; r += a.n_streams)
+  for (int r = BATCH ? take() : w; r < a.n_walkers; r = BATCH ? take() : r + a.n_streams)
   {
+    const DevModel m = BATCH ? a.models[a.model_of[r]] : a.m;
+    const int Sz = m.sweep_size;
+    const int nwd = (m.n_vars + 31) >> 5;
+    if (BATCH && REPLAY) W.rs = a.rng[r];
     const int slot = a.slot_of ? a.slot_of[r] : r;
     uint32_t* g_spins = a.p.spins + (size_t)slot * a.p.nw;
     uint8_t* g_ts = a.p.tstate + (size_t)slot * a.p.mp;
@@ -1109,8 +1118,11 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
     W.natt = W.nacc = W.nwin = 0;
     W.key = 0;
     if (!REPLAY)
-      W.key = counter_key(a.seed + (uint32_t)(r / a.key_div),
-                          a.key_base + (unsigned long long)(r % a.key_div));
+    {
+      const long long lr = BATCH ? a.local_of[r] : r;
+      W.key = counter_key(a.seed + (uint32_t)(lr / a.key_div),
+                          a.key_base + (unsigned long long)(lr % a.key_div));
+    }
     const int nblocks = (Sz + 31) >> 5;
     const int total_blocks = nblocks * a.n_sweeps;
     int toff[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, tq0[2] = {0, 0}, tq1[2] = {0, 0};
@@ -1199,10 +1211,11 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
       a.p.step_att[r] += W.natt;
       a.p.step_acc[r] += W.nacc;
       if (a.p.windows) a.p.windows[r] += W.nwin;
+      if (BATCH && REPLAY) a.rng[r] = W.rs;
     }
     __syncwarp();
   }
-  if (REPLAY && lane == 0) a.rng[w] = W.rs;
+  if (REPLAY && !BATCH && lane == 0) a.rng[w] = W.rs;
 }
 
 // ---------------------------------------------------------------------------
@@ -1218,10 +1231,10 @@ int warp_region_bytes(const SweepArgs& a, bool smem_state)
   return kHdr + 2 * tile + (smem_state ? a.p.mp + 8 * a.p.nw : 0);
 }
 
-template <int FL, bool R, bool I, bool SM>
+template <int FL, bool R, bool I, bool SM, bool B>
 static cudaError_t go(const SweepArgs& a, cudaStream_t s, int wpb, int smem)
 {
-  auto k = sweep2_kernel<FL, R, I, SM>;
+  auto k = sweep2_kernel<FL, R, I, SM, B>;
   static int configured = -1;
   if (smem > 48 * 1024 && configured < smem)
   {
@@ -1230,6 +1243,21 @@ static cudaError_t go(const SweepArgs& a, cudaStream_t s, int wpb, int smem)
     configured = smem;
   }
   int blocks = (a.n_streams + wpb - 1) / wpb;
+  if (B)
+  {
+    // persistent: as many blocks as stay resident, the queue feeds them
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * wpb, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    blocks = std::max(1, std::min((a.n_walkers + wpb - 1) / wpb, std::max(1, per_sm) * sms));
+    SweepArgs b = a;
+    b.n_streams = blocks * wpb;
+    k<<<blocks, 32 * wpb, smem, s>>>(b);
+    return cudaGetLastError();
+  }
   if (blocks > 0) k<<<blocks, 32 * wpb, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -1237,7 +1265,8 @@ static cudaError_t go(const SweepArgs& a, cudaStream_t s, int wpb, int smem)
 template <int FL, bool R, bool I>
 static cudaError_t go_sm(const SweepArgs& a, cudaStream_t s, int wpb, int smem, bool sm)
 {
-  return sm ? go<FL, R, I, true>(a, s, wpb, smem) : go<FL, R, I, false>(a, s, wpb, smem);
+  if (a.queue) return go<FL, R, I, true, true>(a, s, wpb, smem);  // batches stage their state
+  return sm ? go<FL, R, I, true, false>(a, s, wpb, smem) : go<FL, R, I, false, false>(a, s, wpb, smem);
 }
 
 template <int FL>
@@ -1258,6 +1287,11 @@ void upload_sweep_tables(const double* ln, const float* scr, const unsigned long
   cudaMemcpyToSymbol(c_jC, jC, 65 * sizeof(unsigned long long));
 }
 }  // namespace sw
+
+bool sweep_state_fits(const SweepArgs& a)
+{
+  return sw::kTableBytes + sw::warp_region_bytes(a, true) <= 227 * 1024;
+}
 
 // Launch: warps per block chosen so that the grid spreads over the SMs;
 // walker state goes to shared memory when the per-warp region fits.
@@ -1280,6 +1314,7 @@ cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int wpb)
       per = warp_region_bytes(a, false);
     }
   }
+  if (a.queue && !sm) return cudaErrorInvalidValue;  // batches stage their state
   int smem = kTableBytes + wpb * per;
   switch (a.m.flavor)
   {
