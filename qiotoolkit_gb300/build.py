@@ -61,15 +61,16 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     objs = []
+    tag = str(os.getpid())  # builds running at once keep apart
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         futs = []
         for s in SOURCES:
-            obj = os.path.join(OUT_DIR, os.path.splitext(s)[0] + ".o")
+            obj = os.path.join(OUT_DIR, os.path.splitext(s)[0] + "." + tag + ".o")
             objs.append(obj)
             futs.append(ex.submit(_compile, s, obj, verbose))
         for f in futs:
             f.result()
-    tmp = LIB + ".tmp"
+    tmp = LIB + "." + tag + ".tmp"
     cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart_static",
                                                            "-lpthread", "-ldl", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)

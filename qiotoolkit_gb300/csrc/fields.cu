@@ -1281,8 +1281,9 @@ __global__ void __launch_bounds__(256, 1) fc_sweep_kernel(SweepArgs a, int wpc)
   const int wib = threadIdx.x >> 5;
   const bool decider = wib < wpc;
   const int ws = decider ? wib : wib - wpc;  // walker slot in the block
-  const int w = blockIdx.x * wpc + ws;
-  if (w >= a.n_streams) return;
+  const int ws0 = blockIdx.x * wpc + ws;
+  if (ws0 >= a.n_streams) return;
+  const int w = a.order ? a.order[ws0] : ws0;
   const DevModel& m = a.m;
   const int N = m.n_vars;
   const int nw = a.p.nw, mp = a.p.mp;

@@ -149,6 +149,10 @@ struct SweepArgs
   const int* model_of;
   const int* local_of;
   int* queue;
+  // field-cached sweep: stream w runs walker order[w] (null: walker w); set
+  // only with one walker per stream.  Tempering puts its hottest replicas
+  // first, so that their long chains start in the first wave of blocks.
+  const int* order;
 };
 
 struct InitArgs

@@ -855,6 +855,7 @@ class ParallelTempering : public Solver
   int* dir = nullptr;
   double *obs_acc = nullptr, *obs_cost = nullptr, *obs_dir = nullptr;
   unsigned long long *swap_acc = nullptr, *swap_cnt = nullptr, *ties = nullptr;
+  int* hot_first = nullptr;  // walkers by ascending beta (device)
   uint64_t* master = nullptr;
   unsigned long long* swap_key = nullptr;
   Pcg* ext_master = nullptr;  // repeated runs: ladder 0's streams fork from this stream
@@ -964,7 +965,7 @@ class ParallelTempering : public Solver
     auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) & ~(size_t)255; return o; };
     size_t o_dir = take(W * 4), o_oa = take(W * 8), o_oc = take(W * 8), o_od = take(W * 8),
            o_sa = take(W * 8), o_sc = take(W * 8), o_t = take(8), o_m = take(K * 8),
-           o_k = take(K * 8);
+           o_k = take(K * 8), o_ord = take(W * 4);
     if (!aux.ptr) aux = DevBuf(off);
     char* b = (char*)aux.ptr;
     dir = (int*)(b + o_dir);
@@ -976,6 +977,7 @@ class ParallelTempering : public Solver
     ties = (unsigned long long*)(b + o_t);
     master = (uint64_t*)(b + o_m);
     swap_key = (unsigned long long*)(b + o_k);
+    hot_first = (int*)(b + o_ord);
     cuda_check(cudaMemsetAsync(aux.ptr, 0, off, st), "memset");
     device_bytes = (int64_t)(P.buf.bytes + aux.bytes);
     std::vector<uint64_t> rs(W), ms(K), keys(K);
@@ -999,6 +1001,12 @@ class ParallelTempering : public Solver
     cuda_check(cudaMemcpyAsync(P.beta, bw.data(), W * 8, cudaMemcpyHostToDevice, st), "H2D");
     cuda_check(cudaMemcpyAsync(master, ms.data(), K * 8, cudaMemcpyHostToDevice, st), "H2D");
     cuda_check(cudaMemcpyAsync(swap_key, keys.data(), K * 8, cudaMemcpyHostToDevice, st), "H2D");
+    // walkers hottest first (smallest beta; stable): the field-cached
+    // sweep's blocks take them in this order
+    std::vector<int> ord(W);
+    for (int w = 0; w < W; w++) ord[w] = w;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return bw[x] < bw[y]; });
+    cuda_check(cudaMemcpyAsync(hot_first, ord.data(), W * 4, cudaMemcpyHostToDevice, st), "H2D");
     InitArgs a{};
     a.m = model->device_view(full_maxsat_sweep);
     a.p = P.pop;
@@ -1075,6 +1083,7 @@ class ParallelTempering : public Solver
       a.sweep_base = s * spr;
       a.tag = s;  // the step, for the time order of equal lowest costs
       a.field = fields ? P.field : nullptr;
+      a.order = fields ? hot_first : nullptr;
       a.field_valid = P.fvalid ? 1 : 0;
       prof_begin(st);
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
@@ -1158,6 +1167,7 @@ class ParallelTempering : public Solver
       a.sweep_base = step_pos * spr;
       a.tag = step_pos;
       a.field = fields ? P.field : nullptr;
+      a.order = fields ? hot_first : nullptr;
       a.field_valid = P.fvalid ? 1 : 0;
       cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
       P.fvalid = fields;

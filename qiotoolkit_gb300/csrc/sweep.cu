@@ -37,7 +37,11 @@ static const int kHdr = 160;  // per-warp header: 2 mbarriers, 33 dirty words
 __constant__ double c_ln[1024];
 __constant__ float c_scr[1024 * 3];  // y0, dy, err per (row, bucket)
 __constant__ unsigned long long c_jA[65], c_jC[65];
+static const int kTableBytes = 6208;  // per block: ln and screen row 0, jump tables
 
+// Per-block tables: row 0 of the ln table and of its FP32 screen (every
+// uphill attempt reads them) in shared memory; rows 1-3 (redraws after a
+// zero bucket, 1 in 256 uphill attempts) stay in constant memory.
 struct Smem
 {
   double* ln;
@@ -45,15 +49,17 @@ struct Smem
   unsigned long long* jA;
   unsigned long long* jC;
 };
+__device__ __forceinline__ const double* ln_rows(const Smem& S, int row) { return row ? c_ln : S.ln; }
+__device__ __forceinline__ const float* scr_rows(const Smem& S, int row) { return row ? c_scr : S.scr; }
 
 template <bool INT>
 __device__ __forceinline__ bool uphill_accept(const Smem& S, uint32_t r0, int row, double dE,
                                               long long idE, double beta, float nbeta_f)
 {
   float thr_f = INT ? __fmul_rn((float)idE, nbeta_f) : __fmul_rn(approx_float(dE), nbeta_f);
-  int d = lut_screen(S.scr, r0, row, thr_f);
+  int d = lut_screen(scr_rows(S, row), r0, row, thr_f);
   if (d >= 0) return d == 1;
-  return lut_less_exact(S.ln, r0, row, __dmul_rn(INT ? (double)idE : dE, -beta));
+  return lut_less_exact(ln_rows(S, row), r0, row, __dmul_rn(INT ? (double)idE : dE, -beta));
 }
 
 __device__ __forceinline__ uint32_t spin_of(const uint32_t* spins, int v)
@@ -496,7 +502,7 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
       if (INT || have_exact)
       {
         const float thr_f = INT ? __fmul_rn((float)idE, nbeta_f) : __fmul_rn(approx_float(dE), nbeta_f);
-        return lut_screen(S.scr, r, row, thr_f);
+        return lut_screen(scr_rows(S, row), r, row, thr_f);
       }
       const float thr_f = __fmul_rn(dEf, nbeta_f);
       // widen the margin by the screen's own error times beta
@@ -504,7 +510,8 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
       const int b = (int)(r & 255u);
       if (b == 1) return 0;
       const int kk = (row * 256 + b) * 3;
-      const float y0 = S.scr[kk], dy = S.scr[kk + 1], ev = S.scr[kk + 2];
+      const float* scr = scr_rows(S, row);
+      const float y0 = scr[kk], dy = scr[kk + 1], ev = scr[kk + 2];
       const float dist = __fmul_rn((float)(r >> 8), 5.96046483e-08f);
       const float value = __fmaf_rn(dist, dy, y0);
       const float et = __fmaf_rn(fabsf(thr_f), 1.9073486328125e-06f, 1e-30f) + et_extra;
@@ -592,7 +599,7 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
     }
     // lanes inside the screen's margin: exact comparison
     if (uphill && !redraw && dec < 0)
-      dec = lut_less_exact(S.ln, dr, drow, __dmul_rn(INT ? (double)idE : dE, -beta)) ? 1 : 0;
+      dec = lut_less_exact(ln_rows(S, drow), dr, drow, __dmul_rn(INT ? (double)idE : dE, -beta)) ? 1 : 0;
     if (uphill && !redraw) acc = dec == 1;
     const unsigned A = __ballot_sync(kFull, acc);
     bool conf = false;
@@ -646,7 +653,7 @@ __device__ __forceinline__ void block_rounds(const Smem& S, const DevModel& m, W
         bool ok;
         if (decided) ok = true;
         else if (beta_inf) ok = false;
-        else ok = lut_less_exact(S.ln, cur, row, __dmul_rn(INT ? (double)idE : dE, -beta));
+        else ok = lut_less_exact(ln_rows(S, row), cur, row, __dmul_rn(INT ? (double)idE : dE, -beta));
         sacc = ok ? 1 : 0;
       }
       sacc = __shfl_sync(kFull, sacc, f);
@@ -1036,13 +1043,13 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
 {
   using C = typename std::conditional<INT, int, double>::type;
   extern __shared__ __align__(16) unsigned char smem[];
-  double* s_ln = (double*)smem;                                    // 8192 B
-  float* s_scr = (float*)(smem + 8192);                            // 12288 B
-  unsigned long long* s_A = (unsigned long long*)(smem + 20480);  // 520 B
-  unsigned long long* s_C = s_A + 65;                              // 520 B
-  unsigned char* s_warp = smem + 21760;
-  for (int t = threadIdx.x; t < 1024; t += blockDim.x) s_ln[t] = c_ln[t];
-  for (int t = threadIdx.x; t < 3072; t += blockDim.x) s_scr[t] = c_scr[t];
+  double* s_ln = (double*)smem;                                   // row 0: 2048 B
+  float* s_scr = (float*)(smem + 2048);                           // row 0: 3072 B
+  unsigned long long* s_A = (unsigned long long*)(smem + 5120);  // 520 B
+  unsigned long long* s_C = s_A + 65;                             // 520 B
+  unsigned char* s_warp = smem + kTableBytes;
+  for (int t = threadIdx.x; t < 256; t += blockDim.x) s_ln[t] = c_ln[t];
+  for (int t = threadIdx.x; t < 768; t += blockDim.x) s_scr[t] = c_scr[t];
   for (int t = threadIdx.x; t < 65; t += blockDim.x)
   {
     s_A[t] = c_jA[t];
@@ -1221,7 +1228,6 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static const int kTableBytes = 21760;
 
 int warp_region_bytes(const SweepArgs& a, bool smem_state)
 {
