@@ -1292,11 +1292,14 @@ cudaError_t launch_qmc(const QmcArgs& a, cudaStream_t s)
 // ---------------------------------------------------------------------------
 __global__ void pt_swap_kernel(SwapArgs a)
 {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per restart: lanes over the ladder's walkers, then over the
+  // step's pairs (pairs of one parity share no walker)
+  const int lane = threadIdx.x & 31;
+  const int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (k >= a.restarts) return;
   const int T = a.n_temps;
   const int base = k * T;
-  for (int p = 0; p < T; p++)
+  for (int p = lane; p < T; p += 32)
   {
     const int w = base + p;
     const double att = (double)a.step_att_reset[w];
@@ -1307,51 +1310,68 @@ __global__ void pt_swap_kernel(SwapArgs a)
     a.step_att_reset[w] = 0;
     a.step_acc_reset[w] = 0;
   }
+  __syncwarp();
+  // pair j of the step is (i, i + 1), i = (step & 1) + 2j; replayed, it
+  // takes draws 2j and 2j + 1 of the master stream (the reference's loop
+  // draws them in pair order)
+  const int first = (int)(a.step & 1);
+  const int npairs = T - 1 > first ? (T - first) / 2 : 0;
   uint64_t ms = a.replay ? a.master[k] : 0;
-  for (int i = (int)(a.step & 1); i < T - 1; i += 2)
+  for (int j0 = 0; j0 < npairs; j0 += 32)
   {
-    double u;
-    if (a.replay)
+    const int j = j0 + lane;
+    if (j < npairs)
     {
-      uint32_t d0 = pcg_out(ms);
-      ms = ms * kMult + kInc;
-      uint32_t d1 = pcg_out(ms);
-      ms = ms * kMult + kInc;
-      u = canonical(d0, d1);
+      const int i = first + 2 * j;
+      double u;
+      if (a.replay)
+      {
+        uint64_t sj = c_jA[2 * lane] * ms + c_jC[2 * lane];
+        const uint32_t d0 = pcg_out(sj);
+        sj = sj * kMult + kInc;
+        const uint32_t d1 = pcg_out(sj);
+        u = canonical(d0, d1);
+      }
+      else
+      {
+        const uint64_t wd = counter_draw(a.swap_key[k], (unsigned long long)a.step * (unsigned long long)T +
+                                                            (unsigned long long)i);
+        u = __dmul_rn((double)(wd >> 11), 1.0 / 9007199254740992.0);
+      }
+      const int wa = base + i, wb = base + i + 1;
+      const double x = __dmul_rn(__dsub_rn(a.cost[a.slot_of[wa]], a.cost[a.slot_of[wb]]),
+                                 __dsub_rn(a.beta[wa], a.beta[wb]));
+      double e = exp(x);
+      if (fabs(u - e) <= 1e-15 * e)
+      {
+        // near tie: the correctly rounded exp, which the C library's exp
+        // (the reference's) returns except for its rare misroundings
+        e = dd::exp_cr(x);
+        atomicAdd(a.near_ties, 1ULL);
+      }
+      if (u < e)
+      {
+        const int t = a.slot_of[wa];
+        a.slot_of[wa] = a.slot_of[wb];
+        a.slot_of[wb] = t;
+        const int d = a.dir[wa];
+        a.dir[wa] = a.dir[wb];
+        a.dir[wb] = d;
+        a.swap_acc[wa] += 1;
+      }
+      a.swap_cnt[wa] += 1;
     }
-    else
-    {
-      uint64_t wd = counter_draw(a.swap_key[k],
-                                 (unsigned long long)a.step * (unsigned long long)T +
-                                     (unsigned long long)i);
-      u = __dmul_rn((double)(wd >> 11), 1.0 / 9007199254740992.0);
-    }
-    const int wa = base + i, wb = base + i + 1;
-    const double x = __dmul_rn(__dsub_rn(a.cost[a.slot_of[wa]], a.cost[a.slot_of[wb]]),
-                               __dsub_rn(a.beta[wa], a.beta[wb]));
-    double e = exp(x);
-    if (fabs(u - e) <= 1e-15 * e)
-    {
-      // near tie: the correctly rounded exp, which the C library's exp
-      // (the reference's) returns except for its rare misroundings
-      e = dd::exp_cr(x);
-      atomicAdd(a.near_ties, 1ULL);
-    }
-    if (u < e)
-    {
-      int t = a.slot_of[wa];
-      a.slot_of[wa] = a.slot_of[wb];
-      a.slot_of[wb] = t;
-      int d = a.dir[wa];
-      a.dir[wa] = a.dir[wb];
-      a.dir[wb] = d;
-      a.swap_acc[wa] += 1;
-    }
-    a.swap_cnt[wa] += 1;
+    // the master stream moves past this chunk's draws (at most 64)
+    const int nin = min(32, npairs - j0);
+    if (a.replay) ms = c_jA[2 * nin] * ms + c_jC[2 * nin];
   }
-  a.dir[base] = 0;
-  a.dir[base + T - 1] = 1;
-  if (a.replay) a.master[k] = ms;
+  __syncwarp();
+  if (lane == 0)
+  {
+    a.dir[base] = 0;
+    a.dir[base + T - 1] = 1;
+    if (a.replay) a.master[k] = ms;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1520,9 +1540,9 @@ cudaError_t launch_eval_diff(const DevModel& m, int n, const uint32_t* sp,
 
 cudaError_t launch_pt_swap(const SwapArgs& a, cudaStream_t s)
 {
-  int threads = 64;
-  int blocks = (a.restarts + threads - 1) / threads;
-  pt_swap_kernel<<<blocks, threads, 0, s>>>(a);
+  const int threads = 128;  // four restarts per block, a warp each
+  const int blocks = (a.restarts * 32 + threads - 1) / threads;
+  if (blocks > 0) pt_swap_kernel<<<blocks, threads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

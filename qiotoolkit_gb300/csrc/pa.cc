@@ -919,7 +919,6 @@ class SubstochasticMonteCarlo : public Solver
   void configure(const json::Value& doc)
   {
     configure_common_public(*this, doc);
-    if (model->kind == K_MAXSAT) fail(1, "substochastic Monte Carlo runs Ising and PUBO models here");
     auto num = [&](const char* k, double def) {
       const json::Value* v = params.find(k);
       if (!v || v->is_null()) return def;
@@ -1018,9 +1017,12 @@ class SubstochasticMonteCarlo : public Solver
     step_pos = 0;
     // rngs_[t] = rng_->fork() (solver/substochastic_monte_carlo.h:47-51);
     // thread t initialises its block of walkers in index order, each walker
-    // taking one draw per 32 variables (model/ising.h:23-41)
+    // taking one draw per 32 variables (model/ising.h:23-41), or one
+    // uniform() -- two draws -- per variable for MaxSat (model/max_sat.h:
+    // 144-150)
     master = PcgEngine(seed);
-    const uint64_t per = (uint64_t)((model->N + 31) / 32);
+    const bool ms = model->kind == K_MAXSAT;
+    const uint64_t per = ms ? (uint64_t)(2 * model->N) : (uint64_t)((model->N + 31) / 32);
     std::vector<uint64_t> chain(T), wi(R);
     for (int t = 0; t < T; t++)
     {
@@ -1036,7 +1038,7 @@ class SubstochasticMonteCarlo : public Solver
     a.m = model->device_view(false);
     a.p = pools[0].pop;
     a.n_walkers = R;
-    a.replay = replay ? 1 : 0;
+    a.replay = replay ? (ms ? 2 : 1) : (ms ? 3 : 0);
     a.rng = d_init;
     a.seed = seed;
     a.key_base = 0;

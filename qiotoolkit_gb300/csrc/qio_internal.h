@@ -394,7 +394,8 @@ static const int kQmcLevelWarps = 32;
 size_t qmc_level_smem(int trotter, int nw);
 cudaError_t launch_qmc_levels(const QmcArgs& a, cudaStream_t s);
 
-// PT: label swaps + observables, one thread per restart.
+// PT: label swaps + observables, one warp per restart (lanes over the ladder,
+// then over the step's pairs).
 struct SwapArgs
 {
   int restarts;

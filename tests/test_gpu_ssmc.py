@@ -25,6 +25,8 @@ MODELS = {
     "pubo_real": ("pubo", lambda: I.random_pubo(400, 1600, seed=14)),
     "pubo_int": ("pubo", lambda: I.random_pubo(300, 1200, seed=15, integer=True)),
     "pubo_plain": ("pubo_plain", lambda: I.random_pubo(200, 700, seed=16)),
+    "maxsat_real": ("maxsat", lambda: I.weighted_maxsat(150, seed=17)),
+    "maxsat_int": ("maxsat", lambda: I.weighted_maxsat(120, seed=18, integer=True)),
 }
 
 

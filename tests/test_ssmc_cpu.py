@@ -26,10 +26,13 @@ def test_parameter_errors(params, msg):
         q.Solver(m, SSMC, {"params": dict({"seed": 1, "step_limit": 100}, **params)})
 
 
-def test_maxsat_refused():
+def test_maxsat_configures():
+    """MaxSat models are taken (their walkers draw one uniform() per
+    variable at init); the params are validated on the host."""
     m = q.Model("maxsat", [(1.0, [1, 2]), (2.0, [-1, 3])])
-    with pytest.raises(q.QioError, match="Ising and PUBO"):
-        q.Solver(m, SSMC, {"params": {"seed": 1}})
+    q.Solver(m, SSMC, {"params": {"seed": 1, "target_population": 8}}).close()
+    with pytest.raises(q.QioError, match="target_population"):
+        q.Solver(m, SSMC, {"params": {"seed": 1, "target_population": 0}})
 
 
 def test_one_schedule_with_a_range_lends_it_to_the_other():
