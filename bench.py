@@ -225,6 +225,18 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def onchip(achieved, clocks):
+    """The same algorithmic bytes against shared-memory bandwidth, the level
+    where the sweeps keep their models' rows and the walkers' state (HBM
+    carries a few percent of those bytes): 152 SMs x 128 bytes per clock at
+    the SM clock sampled under load -- a nominal figure, not a measured one."""
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = 152 * 128 * float(mhz) * 1e6 / 1e9
+    return {"level": "shared memory", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved is not None else None,
+            "peak_source": "nominal: 152 SMs x 128 B per clock x sampled SM clock"}
+
+
 def committed_traffic(workload):
     """dram bytes per sweep launch from the committed ncu summary, if any
     (the `dram_bytes_per_launch:` line of profiles/sweep_<workload>_ncu.md)."""
@@ -619,6 +631,7 @@ def run_workload(args, ws, rank):
                          "bytes_per_attempt": bpa,
                          "avg_launch_ms": avg_sweep_launch_ms,
                          "attempts_per_window": (windows[1] / windows[0]) if windows[0] else None},
+            "roofline_onchip": onchip(achieved, clk.summary()),
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "parity": parity,
@@ -776,6 +789,7 @@ def main_pf(args, ws, rank):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
                          "kernel": "sweep_kernel (whole solves timed)", "bytes_per_attempt": bpa},
+            "roofline_onchip": onchip(achieved, clk.summary()),
             "cpu_baseline": cpu, "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -803,6 +817,7 @@ def main_serving(args, ws, rank):
     n_att = sum(attempts(m, t, p) for m, (_, _, _, t, p) in zip(models, reqs))
 
     foot = []
+    launched = [0]  # kernel launches of the last serve() (the solves' own counts)
 
     def serve(max_active, count=None):
         srv = q.Server(memory_budget_bytes=budget, max_active=max_active)
@@ -814,8 +829,10 @@ def main_serving(args, ws, rank):
                 time.sleep(d)
             pp = dict(p, kernel=args.kernel) if args.kernel else p
             ids.append(srv.submit(m, target, {"params": pp}))
-        best = [srv.wait(i)["solutions"]["cost"] for i in ids]
+        results = [srv.wait(i) for i in ids]
         dt = time.perf_counter() - t0
+        best = [r["solutions"]["cost"] for r in results]
+        launched[0] = sum(int(r["benchmark"]["gb300"]["kernel_launches"]) for r in results)
         st = srv.stats()
         foot.extend(srv.request_bytes(i) for i in ids)
         srv.close()
@@ -825,6 +842,7 @@ def main_serving(args, ws, rank):
     serve(MAXA, 8)  # warm-up: module loading, table uploads
     with ClockSampler(local) as clk:
         dt_mix, st_mix, best_mix = serve(MAXA)
+    launches_mix = launched[0]
     # continuous batching against a queue alone, on the first 48 requests
     # (the queue alone serves them one after another)
     nq = 0 if big else 48
@@ -878,6 +896,7 @@ def main_serving(args, ws, rank):
             "e2e": {"value": len(reqs) / dt_mix, "unit": "instances/s",
                     "h2d_bytes_per_step": int(sum(m.info.device_bytes for m in models)),
                     "d2h_bytes_per_step": int(sum(8 * m.n_vars for m in models))},
+            "gpu_launches": launches_mix,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
@@ -1050,6 +1069,7 @@ def main_batch(args, ws, rank):
                          "kernel": "sweep_kernel" if st.kernel == 1 else "lw_sweep_kernel",
                          "bytes_per_attempt": bpa,
                          "avg_launch_ms": kernel_ms},
+            "roofline_onchip": onchip(achieved, clk.summary()),
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
