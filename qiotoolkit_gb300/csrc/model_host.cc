@@ -644,6 +644,9 @@ void HostModel::upload() const
   int md = 0;
   for (int64_t v = 0; v < N; v++) md = std::max(md, row[v + 1] - row[v]);
   dev.max_deg = md;
+  int mb = 0;
+  for (int64_t b = 0; b < N; b += 32) mb = std::max(mb, row[std::min<int64_t>(b + 32, N)] - row[b]);
+  dev.max_block_inc = mb;
   dev.other = other.empty() ? nullptr : (const int*)(b + o_oth);
   dev.rec_i = rec_i.empty() ? nullptr : (const int2*)(b + o_ri);
   dev.rec_f = rec_f.empty() ? nullptr : (const double2*)(b + o_rf);

@@ -63,6 +63,7 @@ struct DevModel
   const double2* rec_f;    // K  (other as an integer in the low word, coefficient)
   const unsigned int* rec_p;  // K  other << 8 | 8-bit coefficient (small integer ones)
   int max_deg;             // largest row (incidences of one variable)
+  int max_block_inc;       // most incidences of one 32-variable block of the sweep
   // level schedule (levels.cu), integer pair-only Ising models: level(v) =
   // 1 + the largest level of v's lower neighbours (0 without one); the
   // variables of level t are entries lv_off[t] .. lv_off[t+1] of lv_ent, in
@@ -149,6 +150,10 @@ struct SweepArgs
   const int* model_of;
   const int* local_of;
   int* queue;
+  // windowed kernel: incidences a shared-memory record tile holds (a
+  // multiple of 8; 0: launch_sweep sizes it to the model's largest block,
+  // at most 640, 768 for integer models); larger blocks are read from HBM
+  int tile_cap;
   // field-cached sweep: stream w runs walker order[w] (null: walker w); set
   // only with one walker per stream.  Tempering puts its hottest replicas
   // first, so that their long chains start in the first wave of blocks.

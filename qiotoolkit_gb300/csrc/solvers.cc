@@ -2394,6 +2394,7 @@ class SABatch : public Batch
   {
     int first, last;
     const HostModel* model;  // any member (flavour and coefficient kind)
+    int max_block_inc;       // the members' largest 32-variable block
   };
   std::vector<Group> groups;
   DevBuf qbuf;  // DevModel per instance, model_of, local_of, one queue counter per group
@@ -2518,13 +2519,18 @@ class SABatch : public Batch
     {
       const HostModel* m = models[order[k]];
       const int first = (int)k * R;
+      const int mb = m->device_view(full_sweep).max_block_inc;
       if (groups.empty() || groups.back().model->flavor != m->flavor ||
           groups.back().model->int_mode != m->int_mode)
-        groups.push_back({first, first + R, m});
+        groups.push_back({first, first + R, m, mb});
       else
+      {
         groups.back().last = first + R;
+        groups.back().max_block_inc = std::max(groups.back().max_block_inc, mb);
+      }
       SweepArgs a{};
       a.m = m->device_view(full_sweep);
+      a.m.max_block_inc = groups.back().max_block_inc;
       a.p = P.pop;
       queued = sweep_state_fits(a);
     }
@@ -2582,6 +2588,7 @@ class SABatch : public Batch
     a.model_of = d_model_of + G.first;
     a.local_of = d_local_of + G.first;
     a.queue = d_queue + g;
+    a.m.max_block_inc = G.max_block_inc;  // tiles sized for the group's largest block
     cuda_check(launch_sweep(a, st, wpb), "sweep kernel");
   }
 

@@ -151,27 +151,48 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 // starts at the aligned address below its first element and records the
 // element offset.  FP64 models carry the coefficients twice: rounded to float
 // for the screen and exact for the reference-order sums.
+// The capacity is set per launch (a multiple of 8, the model's largest block
+// or less); each array starts on a 16-byte boundary and holds cap + 8
+// entries, the slack that the rounding of the copies' ends needs.
 template <bool INT>
 struct Tile
 {
-  static const int kCap = INT ? 768 : 640;  // incidences held in shared memory
-  uint32_t inc[kCap + 8];
-  float coef_f[INT ? 4 : kCap + 8];
-  typename std::conditional<INT, int, double>::type coef[kCap + 8];
-  unsigned long long near[kCap + 8];
+  static const int kMaxCap = INT ? 768 : 640;  // incidences held in shared memory, at most
+  uint32_t* inc;
+  float* coef_f;
+  typename std::conditional<INT, int, double>::type* coef;
+  unsigned long long* near;
 };
-
 template <bool INT>
-__device__ __forceinline__ void tile_issue(Tile<INT>* t, unsigned long long* bar, const DevModel& m,
-                                           int q0, int q1, int* off)
+__host__ __device__ inline int tile_bytes(int cap)
+{
+  const int e = cap + 8;
+  return e * 4 + (INT ? 16 : e * 4) + e * (INT ? 4 : 8) + e * 8;
+}
+template <bool INT>
+__device__ __forceinline__ Tile<INT> tile_at(unsigned char* base, int cap)
 {
   using C = typename std::conditional<INT, int, double>::type;
-  const int n = min(q1 - q0, Tile<INT>::kCap);
+  const int e = cap + 8;
+  Tile<INT> t;
+  t.inc = (uint32_t*)base;
+  t.coef_f = (float*)(base + e * 4);
+  t.coef = (C*)(base + e * 4 + (INT ? 16 : e * 4));
+  t.near = (unsigned long long*)(base + e * 4 + (INT ? 16 : e * 4) + e * (INT ? 4 : 8));
+  return t;
+}
+
+template <bool INT>
+__device__ __forceinline__ void tile_issue(const Tile<INT>& t, int cap, unsigned long long* bar,
+                                           const DevModel& m, int q0, int q1, int* off)
+{
+  using C = typename std::conditional<INT, int, double>::type;
+  const int n = min(q1 - q0, cap);
   const C* cbase = INT ? (const C*)m.coef_i : (const C*)m.coef;
   const void* src[4] = {m.inc + q0, cbase + q0, m.near + q0,
                         INT ? (const void*)m.inc : (const void*)(m.coef_f + q0)};
   const int esz[4] = {4, (int)sizeof(C), 8, 4};
-  void* dst[4] = {t->inc, t->coef, t->near, t->coef_f};
+  void* dst[4] = {t.inc, t.coef, t.near, t.coef_f};
   const int ncopy = INT ? 3 : 4;
   unsigned bytes[4];
   const char* start[4];
@@ -1064,13 +1085,14 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
   if (w >= a.n_streams) return;
   const bool staged = (FL == F_PARITY || FL == F_COUNTER);
   // per-warp region: [bars 16][dirty words 144][tiles 2][term bytes][spins][lowest]
-  const int tile_bytes = staged ? (int)((sizeof(Tile<INT>) + 15) & ~15) : 0;
+  const int cap = a.tile_cap > 0 ? a.tile_cap : Tile<INT>::kMaxCap;
+  const int tile_b = staged ? tile_bytes<INT>(cap) : 0;
   const int state_bytes = SMEM ? (a.p.mp + 8 * a.p.nw) : 0;
-  unsigned char* my = s_warp + (size_t)wib * (kHdr + 2 * tile_bytes + state_bytes);
+  unsigned char* my = s_warp + (size_t)wib * (kHdr + 2 * tile_b + state_bytes);
   unsigned long long* bars = (unsigned long long*)my;
   uint32_t* dirty = (uint32_t*)(my + 16);
-  Tile<INT>* tiles = (Tile<INT>*)(my + kHdr);
-  unsigned char* my_state = my + kHdr + 2 * tile_bytes;
+  unsigned char* tile_base = my + kHdr;  // tile b at tile_base + b * tile_b
+  unsigned char* my_state = my + kHdr + 2 * tile_b;
   if (staged && lane == 0)
   {
     mbar_init(&bars[0]);
@@ -1136,7 +1158,7 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
     if (staged && total_blocks > 0 && lane == 0)
     {
       int q0 = __ldg(m.row + 0), q1 = __ldg(m.row + min(32, Sz));
-      tile_issue<INT>(&tiles[0], &bars[0], m, q0, q1, toff[0]);
+      tile_issue<INT>(tile_at<INT>(tile_base, cap), cap, &bars[0], m, q0, q1, toff[0]);
       tq0[0] = q0;
       tq1[0] = q1;
     }
@@ -1161,7 +1183,8 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
         {
           int nb = (bi + 1 < nblocks) ? bi + 1 : 0;
           int q0 = __ldg(m.row + (nb << 5)), q1 = __ldg(m.row + min((nb << 5) + 32, Sz));
-          tile_issue<INT>(&tiles[buf ^ 1], &bars[buf ^ 1], m, q0, q1, toff[buf ^ 1]);
+          tile_issue<INT>(tile_at<INT>(tile_base + (buf ^ 1) * tile_b, cap), cap, &bars[buf ^ 1], m, q0, q1,
+                          toff[buf ^ 1]);
           tq0[buf ^ 1] = q0;
           tq1[buf ^ 1] = q1;
         }
@@ -1178,16 +1201,16 @@ __global__ void __launch_bounds__(256, 1) sweep2_kernel(SweepArgs a)
         const int t_oc = __shfl_sync(kFull, toff[buf][1], 0);
         const int t_on = __shfl_sync(kFull, toff[buf][2], 0);
         const int t_of = __shfl_sync(kFull, toff[buf][3], 0);
-        if (t_q1 - t_q0 <= Tile<INT>::kCap)
+        if (t_q1 - t_q0 <= cap)
         {
           const int v = i0 + lane;
           const int rb = (v < Sz) ? __ldg(m.row + v) : t_q0;
-          const Tile<INT>* tile = &tiles[buf];
+          const Tile<INT> tile = tile_at<INT>(tile_base + buf * tile_b, cap);
           block_rounds<FL, REPLAY, INT, true>(S, m, W, ts, spins, lsp, dirty,
-                                              tile->inc + t_oi + (rb - t_q0),
-                                              tile->coef + t_oc + (rb - t_q0),
-                                              tile->coef_f + t_of + (rb - t_q0),
-                                              tile->near + t_on + (rb - t_q0), i0, Sz, nwd,
+                                              tile.inc + t_oi + (rb - t_q0),
+                                              tile.coef + t_oc + (rb - t_q0),
+                                              tile.coef_f + t_of + (rb - t_q0),
+                                              tile.near + t_on + (rb - t_q0), i0, Sz, nwd,
                                               beta, nbeta_f, beta_inf, ctr0);
         }
         else
@@ -1233,8 +1256,17 @@ int warp_region_bytes(const SweepArgs& a, bool smem_state)
 {
   const bool INT = a.m.int_mode != 0;
   const bool staged = (a.m.flavor == F_PARITY || a.m.flavor == F_COUNTER);
-  const int tile = staged ? (int)(((INT ? sizeof(Tile<true>) : sizeof(Tile<false>)) + 15) & ~15) : 0;
+  const int cap = a.tile_cap > 0 ? a.tile_cap : (INT ? Tile<true>::kMaxCap : Tile<false>::kMaxCap);
+  const int tile = staged ? (INT ? tile_bytes<true>(cap) : tile_bytes<false>(cap)) : 0;
   return kHdr + 2 * tile + (smem_state ? a.p.mp + 8 * a.p.nw : 0);
+}
+
+// the tile capacity for a model: its largest block, rounded up to a
+// multiple of 8, at most the kernel's maximum
+int tile_cap_for(const DevModel& m)
+{
+  const int mx = m.int_mode ? Tile<true>::kMaxCap : Tile<false>::kMaxCap;
+  return std::max(8, std::min(mx, (m.max_block_inc + 7) & ~7));
 }
 
 template <int FL, bool R, bool I, bool SM, bool B>
@@ -1296,16 +1328,21 @@ void upload_sweep_tables(const double* ln, const float* scr, const unsigned long
 
 bool sweep_state_fits(const SweepArgs& a)
 {
-  return sw::kTableBytes + sw::warp_region_bytes(a, true) <= 227 * 1024;
+  SweepArgs b = a;
+  if (b.tile_cap <= 0) b.tile_cap = sw::tile_cap_for(b.m);
+  return sw::kTableBytes + sw::warp_region_bytes(b, true) <= 227 * 1024;
 }
 
 // Launch: warps per block chosen so that the grid spreads over the SMs;
 // walker state goes to shared memory when the per-warp region fits.
-cudaError_t launch_sweep(const SweepArgs& a, cudaStream_t s, int wpb)
+cudaError_t launch_sweep(const SweepArgs& a_in, cudaStream_t s, int wpb)
 {
   using namespace sw;
   // the field-cached sweep when the caller keeps fields for this population
-  if (a.field && a.smem_state && fc_fits(a.m, a.p.nw, a.p.mp)) return launch_fc_sweep(a, s);
+  if (a_in.field && a_in.smem_state && fc_fits(a_in.m, a_in.p.nw, a_in.p.mp)) return launch_fc_sweep(a_in, s);
+  // record tiles sized to the largest block (a batch passes its largest)
+  SweepArgs a = a_in;
+  if (a.tile_cap <= 0) a.tile_cap = tile_cap_for(a.m);
   if (wpb < 1) wpb = 1;
   if (wpb > 8) wpb = 8;
   const int max_smem = 227 * 1024;
