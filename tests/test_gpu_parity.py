@@ -119,6 +119,28 @@ def test_pt_trajectories_and_observables(name, mode):
     np.testing.assert_array_equal(obs[:-1, 4], r.pt_obs[:-1, 4])
 
 
+@pytest.mark.parametrize("mode", ["replay", "counter"])
+def test_pt_long_ladder_swaps(mode):
+    """80 temperatures: a step tries 40 or 39 pairs, more than the swap
+    kernel's 32 lanes, so the pairs run in two chunks and (replayed) the
+    master stream moves past 64 draws, then the rest."""
+    off, ids, coef = MODELS["ising_real"][1]()
+    g, o = both("ising", off, ids, coef)
+    temps = {"type": "geometric", "initial": 0.05, "final": 3.0, "count": 80}
+    params = {"seed": 11, "sweeps": 12, "temperatures": temps, "rng_mode": mode, "restarts": 2}
+    s = q.Solver(g, PT, {"params": params}).init().run()
+    rep = s.replicas()
+    obs = s.pt_observables()
+    for k in range(2):
+        r = O.run(o, "pt", seed=11 + k, step_limit=12, use_inverse=False,
+                  sched=("geometric", 0.05, 3.0), sched_count=80, rng_mode=mode, threads=4)
+        sl = slice(80 * k, 80 * k + 80)
+        np.testing.assert_array_equal(rep["cost"][sl], r.cost)
+        np.testing.assert_array_equal(rep["states"][sl], r.states)
+        np.testing.assert_array_equal(rep["lowest"][sl], r.lowest)
+        np.testing.assert_array_equal(obs[sl, :4], r.pt_obs[:, :4])
+
+
 def test_pt_restarts_are_independent_seeds():
     off, ids, coef = MODELS["pubo_real"][1]()
     g, o = both("pubo", off, ids, coef)
