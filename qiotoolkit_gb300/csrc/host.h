@@ -41,6 +41,9 @@ struct DevBuf
 };
 
 void ensure_device();  // selects the device, uploads tables once per device
+// bit-packed walker states (32 variables per word, rows of nw words) to one
+// byte per variable, `count` rows of N bytes
+void unpack_states(const uint32_t* words, int nw, int64_t N, int64_t count, uint8_t* out);
 int* device_error_flag();       // per-device int set by kernels whose bounded waits gave up
 void check_device_error(cudaStream_t s);  // throws QIO_TIMEOUT (status 4) when set
 

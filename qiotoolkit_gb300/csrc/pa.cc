@@ -452,10 +452,8 @@ class PopulationAnnealing : public Solver
     cuda_check(cudaMemcpy(acc.data(), p.accepts, n * 8, cudaMemcpyDeviceToHost), "D2H");
     std::vector<uint32_t> w((size_t)n * p.nw);
     auto unpack = [&](std::vector<uint8_t>& out) {
-      out.assign((size_t)n * model->N, 0);
-      for (int r = 0; r < n; r++)
-        for (int64_t v = 0; v < model->N; v++)
-          out[(size_t)r * model->N + v] = (w[(size_t)r * p.nw + v / 32] >> (v % 32)) & 1u;
+      out.resize((size_t)n * model->N);
+      unpack_states(w.data(), p.nw, model->N, n, out.data());
     };
     if (lowest_states)
     {
@@ -1207,10 +1205,8 @@ class SubstochasticMonteCarlo : public Solver
     cuda_check(cudaMemcpy(acc.data(), p.accepts, n * 8, cudaMemcpyDeviceToHost), "D2H");
     std::vector<uint32_t> w((size_t)n * p.nw);
     auto unpack = [&](std::vector<uint8_t>& out) {
-      out.assign((size_t)n * model->N, 0);
-      for (int r = 0; r < n; r++)
-        for (int64_t v = 0; v < model->N; v++)
-          out[(size_t)r * model->N + v] = (w[(size_t)r * p.nw + v / 32] >> (v % 32)) & 1u;
+      out.resize((size_t)n * model->N);
+      unpack_states(w.data(), p.nw, model->N, n, out.data());
     };
     if (lowest_states)
     {

@@ -254,12 +254,34 @@ struct Population
   static void unpack(const std::vector<uint32_t>& words, int nw, int64_t N,
                      int64_t count, std::vector<uint8_t>& out)
   {
-    out.assign((size_t)count * N, 0);
-    for (int64_t r = 0; r < count; r++)
-      for (int64_t v = 0; v < N; v++)
-        out[r * N + v] = (words[r * nw + v / 32] >> (v % 32)) & 1u;
+    out.resize((size_t)count * N);
+    unpack_states(words.data(), nw, N, count, out.data());
   }
 };
+
+// eight variables per table lookup: byte b of a state word expands to the
+// eight output bytes of its bits (hosts are little-endian: x86-64, aarch64)
+void unpack_states(const uint32_t* words, int nw, int64_t N, int64_t count, uint8_t* out)
+{
+  static const std::array<uint64_t, 256> lut = [] {
+    std::array<uint64_t, 256> t{};
+    for (int b = 0; b < 256; b++)
+      for (int k = 0; k < 8; k++) t[b] |= (uint64_t)((b >> k) & 1) << (8 * k);
+    return t;
+  }();
+  const int64_t whole = N / 8;
+  for (int64_t r = 0; r < count; r++)
+  {
+    const uint32_t* w = words + r * nw;
+    uint8_t* o = out + r * N;
+    for (int64_t q = 0; q < whole; q++)
+    {
+      const uint32_t byte = (w[q >> 2] >> ((q & 3) * 8)) & 255u;
+      memcpy(o + 8 * q, &lut[byte], 8);
+    }
+    for (int64_t v = whole * 8; v < N; v++) o[v] = (uint8_t)((w[v >> 5] >> (v & 31)) & 1u);
+  }
+}
 
 uint64_t sum_windows(const DevPop& p, int n)
 {
