@@ -1006,7 +1006,10 @@ def main_batch(args, ws, rank):
         for i in range(2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            b = q.Batch(models, target, {"params": dict(params, autotune=False)})
+            # the plan the timed batch found, reused as a caller would
+            plan = dict(params, autotune=False, warps_per_block=int(st.warps_per_block),
+                        smem_state=bool(st.smem))
+            b = q.Batch(models, target, {"params": plan})
             b.run(sh)
             lo = b.lowest()
             torch.cuda.synchronize()

@@ -2392,6 +2392,7 @@ class SABatch : public Batch
   int64_t steps = 0;
   bool replay = true, lanes = false, autotune = true, use_graph = true, smem = true;
   bool full_sweep = false;  // maxsat_full_sweep: every MaxSat variable in a sweep
+  int wpb_param = 0;         // warps_per_block: the plan without autotune (0: spread)
   uint32_t seed = 0;
   int kernel = 0;
   Population P;
@@ -2458,6 +2459,7 @@ class SABatch : public Batch
     kernel = v0.kernel;
     smem = v0.smem_state;
     full_sweep = v0.full_maxsat_sweep;
+    wpb_param = v0.warps_per_block;
     Params p(doc["params"]);
     autotune = p.boolean("autotune", true);
     use_graph = p.boolean("graph", true);
@@ -2713,7 +2715,7 @@ class SABatch : public Batch
   void tune(cudaStream_t st)
   {
     plan_smem = smem ? 1 : 0;
-    plan_wpb = 0;
+    plan_wpb = wpb_param;
     if (!autotune || steps <= 0) return;
     const int64_t trial = std::max<int64_t>(1, std::min<int64_t>(steps, (steps + 99) / 100));
     if (queued)
