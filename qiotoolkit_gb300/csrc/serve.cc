@@ -37,6 +37,7 @@ struct Request
   const HostModel* model = nullptr;
   std::unique_ptr<Solver> solver;
   int64_t footprint = 0;
+  double work = 0;  // one walker's chain: incidences x sweeps
   int state = 0;  // 0 pending, 1 running, 2 done, 3 failed
   Clock::time_point t_submit, t_admit, t_done;
   std::string result, error;
@@ -121,6 +122,7 @@ class ServerImpl : public Server
     if (r->solver->has_cost_limit || r->solver->has_time_limit)
       fail(1, "served solves run their full sweep budget: `cost_limit` and `timeout` are not supported");
     r->footprint = footprint_of(*m, *r->solver);
+    r->work = (double)std::max<int64_t>(1, m->K) * (double)std::max<int64_t>(1, r->solver->step_limit);
     if (r->footprint > budget_)
       fail(2, "request needs " + std::to_string(r->footprint) + " device bytes; the server's budget is " +
                   std::to_string(budget_));
@@ -262,7 +264,16 @@ class ServerImpl : public Server
   {
     try
     {
-      cuda_check(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      // the longer a walker's chain, the higher its stream's priority: when
+      // the admitted solves' blocks outnumber the GPU's slots, the block
+      // scheduler starts the pieces of the longest chains first (a mix ends
+      // with its longest chain)
+      int least = 0, greatest = 0;
+      cuda_check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange");
+      const int levels = least - greatest;
+      const int level = (int)std::max(0.0, std::min((double)levels, std::floor(std::log2(r->work / 1e6))));
+      cuda_check(cudaStreamCreateWithPriority(&r->stream, cudaStreamNonBlocking, least - level),
+                 "cudaStreamCreate");
       cuda_check(cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming), "cudaEventCreate");
       r->solver->init(r->stream);
       r->finished = r->solver->advance(r->stream, r->piece);
