@@ -147,6 +147,16 @@ qio_status qio_model_create_proto_folder(const char* folder_path, qio_model** ou
  * estimate_min_cost_diff and estimate_max_cost_diff (model/ising.h:176-224,
  * model/pubo.h:127-184, graph/graph.h:453-485).  Ising and PUBO models. */
 qio_status qio_model_cost_diff_bounds(const qio_model* model, double* min_diff, double* max_diff);
+/* The Bayesian search strategy of the population-annealing and
+ * substochastic parameter-free solvers (strategy/bayesian.h:14-78,
+ * BayesianOpt::add_new_sample + recommend_parameter_values), for callers
+ * that run their own parameter searches: from n >= 2 samples xs (n x dims,
+ * row-major) with objectives ys, `count` points (count x dims) inside the
+ * box [lo, hi] that a Gaussian-process model expects to improve on the
+ * lowest objective.  Deterministic for a seed; host only. */
+qio_status qio_bayes_recommend(int32_t dims, const double* lo, const double* hi, int32_t n,
+                               const double* xs, const double* ys, uint32_t seed, int32_t count,
+                               double* out);
 
 qio_status qio_model_get_info(const qio_model* model, qio_model_info* out);
 /* Original variable name of each internal variable (Graph::output_map,

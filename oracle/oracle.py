@@ -7,6 +7,7 @@ imports this module.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 import threading
@@ -90,6 +91,8 @@ def lib(release: bool = False):
         L.orc_pcg_stream.argtypes = [u32, ip, ip, P(C.c_uint32)]
         L.orc_pcg_uniform.argtypes = [u32, ip, ip, P(dbl)]
         L.orc_pcg_fork_uniform.argtypes = [u32, ip, ip, P(dbl)]
+        L.orc_pcg_state_uniform.argtypes = [P(C.c_uint64)]
+        L.orc_pcg_state_uniform.restype = dbl
         L.orc_twister_uniform.argtypes = [u32, ip, ip, P(dbl)]
         L.orc_uniform_ln.argtypes = [P(dbl)]
         L.orc_metropolis_accept.argtypes = [dbl, dbl, P(C.c_uint32), ip, P(ip)]
@@ -683,3 +686,96 @@ def pt_parameter_free(model: Model, kind, terms, *, seed, min_num_betas, samples
             break
     return {"trace": trace, "best": best, "best_state": best_state, "sweeps": best_params,
             "betas": betas}
+
+
+# ------------------------------------------- parameter-free PA / SSMC (replay)
+_PCG_MULT, _PCG_INC = 6364136223846793005, 1442695040888963407
+
+
+def _pcg_seed_state(seed):
+    """The state of a PCG32 stream seeded with `seed` (Pcg32::seed64)."""
+    return ((seed + _PCG_INC) * _PCG_MULT + _PCG_INC) % (1 << 64)
+
+
+def _pcg_draw(state):
+    """One uniform() of the stream in `state`: (value, next state)."""
+    st = C.c_uint64(state)
+    u = lib().orc_pcg_state_uniform(C.byref(st))
+    return u, st.value
+
+
+def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, initial_samples=4,
+                             initial_sweeps=20, initial_alpha=2.0, initial_min_prob_log=2.0,
+                             max_prob=0.5, max_population_mult=128, alpha_low=1.00000001):
+    """The runs of a parameter-free population-annealing search
+    (solver/parameter_free_solver.h:65-151 with solver/pa_parameter_free.h)
+    replayed on one master stream: the first `initial_samples` parameter
+    vectors from the adapter's initial values (get_initial_parameter_values,
+    :228-260, the alpha jitter drawn from the master), later ones as given
+    in `runs` (the strategy's picks), each applied as update_parameters
+    (:262-330) and run by the oracle's PA from the master's state.  Returns
+    [(params, step_limit, lowest)] for as many runs as `runs` lists.  The
+    walker cap is threads x max_population_mult (memory is not the limit)."""
+    mn_mx = cost_diff_bounds(kind, terms)
+    mn, mx = mn_mx
+    beta_start = -math.log(max_prob) / mx
+    cap = threads * max_population_mult
+
+    def adjust(x):
+        r = min(int(x), cap)
+        return max(r, threads) if cap > threads else cap
+
+    state = _pcg_seed_state(seed & 0xFFFFFFFF)
+    out = []
+    for k, given in enumerate(runs):
+        if k < initial_samples:
+            u, state = _pcg_draw(state)
+            v = [float(initial_sweeps + k * 10), float(adjust(threads * (k + 1))),
+                 initial_alpha + 0.5 * (u - 0.5), k + 1.0, initial_min_prob_log + k * 2]
+        else:
+            v = list(given)
+        spr = max(1, int(round(v[3])))
+        sl = max(int(math.ceil(v[0] / spr)), 2)
+        pop = adjust(v[1])
+        alpha = max(v[2], alpha_low)
+        b1 = v[4] / mn
+        res = run(model, "pa", seed=seed, master_state=state, step_limit=sl, sweeps_per_replica=spr,
+                  population=pop, alpha=alpha, sched=("geometric", beta_start, b1), pa_threads=threads,
+                  threads=min(threads, 16))
+        state = res.master_state
+        out.append((v, sl, float(res.best_cost)))
+    return out
+
+
+def ssmc_parameter_free_replay(model: Model, *, seed, threads, runs, sweep_size, initial_samples=4,
+                               initial_sweeps=20, initial_spw=1, initial_alpha_final=0.00001,
+                               initial_alpha_scope=0.8, initial_beta_initial=0.00001,
+                               initial_beta_scope=5.0, max_replica_mult=3):
+    """The runs of a parameter-free SSMC search (solver/ssmc_parameter_free.h
+    get_initial_parameter_values :160-178, update_parameters :180-224) on one
+    master stream, as pa_parameter_free_replay does for PA."""
+    cap = threads * max_replica_mult
+
+    def adjust(x):
+        r = min(int(x), cap)
+        return max(r, threads) if cap > threads else cap
+
+    state = _pcg_seed_state(seed & 0xFFFFFFFF)
+    out = []
+    for k, given in enumerate(runs):
+        if k < initial_samples:
+            u, state = _pcg_draw(state)
+            v = [float(initial_sweeps * sweep_size * (1 + k)), float(min(threads + k, cap)), float(initial_spw),
+                 initial_alpha_final, initial_alpha_scope, initial_beta_initial, initial_beta_scope + u]
+        else:
+            v = list(given)
+        sl = max(int(math.floor(v[0])), 2)
+        pop = adjust(v[1])
+        spw = max(int(v[2]), 1)
+        res = run(model, "ssmc", seed=seed, master_state=state, step_limit=sl, population=pop,
+                  pa_threads=threads, threads=min(threads, 16), steps_per_walker=spw,
+                  sched=("linear", v[3] + v[4], v[3]), sched2=("linear", v[5], v[5] + v[6]))
+        state = res.master_state
+        out.append((v, sl, float(res.best_cost)))
+    return out
+

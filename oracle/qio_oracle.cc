@@ -1483,6 +1483,7 @@ static Result run_ssmc(const Model& m, const orc_params& p)
   const bool counter = p.rng_mode == ORC_RNG_COUNTER;
   set_threads(p.threads);
   PcgRng master(p.seed);
+  if (p.use_master_state) master.pcg.state = p.master_state;
   std::vector<std::unique_ptr<Rng>> rngs(T);
   for (size_t t = 0; t < T; t++) rngs[t] = master.fork();
   std::vector<Walker> pop(R);
@@ -1810,6 +1811,7 @@ static Result run_pa(Model& m, const orc_params& p)
   size_t T = (size_t)std::max(1, p.pa_threads);
   size_t target = (size_t)p.population;
   PcgRng master(p.seed);
+  if (p.use_master_state) master.pcg.state = p.master_state;
   std::vector<std::unique_ptr<Rng>> rngs(T);
   for (size_t t = 0; t < T; t++) rngs[t] = master.fork();
   // GraphProperties::rescale, graph/graph_properties.h:24-40
@@ -2033,6 +2035,7 @@ static Result run_pa(Model& m, const orc_params& p)
     if (p.has_cost_limit && low.has && low.cost <= p.cost_limit) break;
   }
   r.last_step = step;
+  r.master_out = master.pcg.state;
   std::vector<Walker*> wp;
   for (auto& c : pop) wp.push_back(&c->w);
   fill_replicas(r, wp);
@@ -2134,6 +2137,16 @@ void orc_pcg_stream(uint32_t seed, int use_default_seed, int n, uint32_t* out)
   Pcg32 g;
   if (!use_default_seed) g = Pcg32(seed);
   for (int i = 0; i < n; i++) out[i] = g();
+}
+
+// one uniform() of the PCG stream in the given state, the state advanced
+double orc_pcg_state_uniform(uint64_t* state)
+{
+  PcgRng g;
+  g.pcg.state = *state;
+  const double u = g.uniform();
+  *state = g.pcg.state;
+  return u;
 }
 
 void orc_pcg_uniform(uint32_t seed, int use_default_seed, int n, double* out)

@@ -6,7 +6,7 @@ ABI in include/qio_gb300.h (libqio_gb300.so).  This package is the Python
 mirror of the reference's model/solver interface over that ABI.
 """
 from ._lib import QioError, SYMBOLS, lib_path, load  # noqa: F401
-from .api import KINDS, TARGETS, Batch, Model, Server, Solver, flatten_terms, run_json  # noqa: F401
+from .api import KINDS, TARGETS, Batch, Model, Server, Solver, bayes_recommend, flatten_terms, run_json  # noqa: F401
 
 __all__ = ["Model", "Solver", "Batch", "Server", "run_json", "QioError", "load", "lib_path", "KINDS",
-           "TARGETS", "flatten_terms", "SYMBOLS"]
+           "TARGETS", "flatten_terms", "SYMBOLS", "bayes_recommend"]

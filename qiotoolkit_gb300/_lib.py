@@ -75,6 +75,8 @@ def _signatures():
         "qio_model_create_dimacs": (st, [cp, P(vp)]),
         "qio_model_create_proto_folder": (st, [cp, P(vp)]),
         "qio_model_cost_diff_bounds": (st, [vp, P(C.c_double), P(C.c_double)]),
+        "qio_bayes_recommend": (st, [C.c_int32, P(C.c_double), P(C.c_double), C.c_int32, P(C.c_double),
+                                     P(C.c_double), C.c_uint32, C.c_int32, P(C.c_double)]),
         "qio_model_get_info": (st, [vp, P(ModelInfo)]),
         "qio_model_get_var_names": (st, [vp, P(C.c_int32)]),
         "qio_model_destroy": (st, [vp]),

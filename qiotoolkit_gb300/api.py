@@ -21,7 +21,8 @@ TARGETS = ("simulatedannealing.qiotoolkit", "paralleltempering.qiotoolkit",
            "populationannealing.cpu", "simulatedannealing-parameterfree.qiotoolkit",
            "paralleltempering-parameterfree.qiotoolkit", "tabu.qiotoolkit",
            "substochasticmontecarlo.cpu", "quantummontecarlo.qiotoolkit",
-           "tabu-parameterfree.qiotoolkit")
+           "tabu-parameterfree.qiotoolkit", "populationannealing-parameterfree.cpu",
+           "substochasticmontecarlo-parameterfree.cpu")
 
 
 def _ptr(a, ct):
@@ -238,6 +239,24 @@ def run_json(input_json, params_json, target: str) -> dict:
         return json.loads(C.string_at(p).decode())
     finally:
         L.qio_free(p)
+
+
+def bayes_recommend(ranges, xs, ys, *, seed: int = 0, count: int = 1) -> np.ndarray:
+    """The parameter-free solvers' Bayesian strategy on caller samples:
+    `count` points in the box `ranges` [(lo, hi), ...] expected to improve on
+    the lowest of the objectives ys at the points xs (n x dims)."""
+    r = np.ascontiguousarray(ranges, np.float64).reshape(-1, 2)
+    d = r.shape[0]
+    x = np.ascontiguousarray(xs, np.float64).reshape(-1, d)
+    y = np.ascontiguousarray(ys, np.float64).reshape(-1)
+    if x.shape[0] != y.shape[0]:
+        raise ValueError("xs and ys differ in length")
+    lo, hi = np.ascontiguousarray(r[:, 0]), np.ascontiguousarray(r[:, 1])
+    out = np.zeros((count, d))
+    D = C.c_double
+    check(load().qio_bayes_recommend(d, _ptr(lo, D), _ptr(hi, D), x.shape[0], _ptr(x, D), _ptr(y, D),
+                                     seed & 0xFFFFFFFF, count, _ptr(out, D)))
+    return out
 
 
 class Batch:

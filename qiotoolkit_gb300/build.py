@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libqio_gb300.so")
-SOURCES = ["kernels.cu", "sweep.cu", "fields.cu", "lanes.cu", "levels.cu", "pa_device.cu", "model_host.cc", "solvers.cc", "pa.cc", "serve.cc", "capi.cc", "json.cc", "dimacs.cc", "proto.cc"]
+SOURCES = ["kernels.cu", "sweep.cu", "fields.cu", "lanes.cu", "levels.cu", "pa_device.cu", "model_host.cc", "solvers.cc", "pa.cc", "bayes.cc", "serve.cc", "capi.cc", "json.cc", "dimacs.cc", "proto.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "qio_gb300.h"
+#include "bayes.h"
 #include "host.h"
 
 using namespace qio;
@@ -128,6 +129,21 @@ qio_status qio_model_cost_diff_bounds(const qio_model* model, double* min_diff, 
     if (!model || !min_diff || !max_diff) fail(1, "arguments must not be null");
     *min_diff = estimate_min_cost_diff(*model->m);
     *max_diff = estimate_max_cost_diff(*model->m);
+  });
+}
+
+qio_status qio_bayes_recommend(int32_t dims, const double* lo, const double* hi, int32_t n, const double* xs,
+                               const double* ys, uint32_t seed, int32_t count, double* out)
+{
+  return guard([&] {
+    if (!lo || !hi || !xs || !ys || !out) fail(1, "arguments must not be null");
+    if (dims <= 0 || dims > 64) fail(1, "`dims` must be in [1, 64]");
+    if (n < 2) fail(1, "at least two samples are needed");
+    if (count <= 0 || count > 64) fail(1, "`count` must be in [1, 64]");
+    for (int c = 0; c < dims; c++)
+      if (!(hi[c] >= lo[c])) fail(1, "each range needs lo <= hi");
+    if (!bayes_recommend(dims, lo, hi, n, xs, ys, seed, count, out))
+      fail(1, "the Gaussian-process model could not be fitted to these samples");
   });
 }
 

@@ -17,6 +17,7 @@
 #include <numeric>
 #include <random>
 
+#include "bayes.h"
 #include "host.h"
 
 namespace qio
@@ -201,6 +202,7 @@ class PopulationAnnealing : public Solver
   int aux_cap = 0;
 
   PcgEngine master{0};
+  PcgEngine* ext_master = nullptr;  // repeated runs: the master stream continues from run to run
   std::vector<uint64_t> streams;  // host mirror of the replay streams
   std::vector<size_t> family;
   std::vector<double> wbeta;
@@ -410,7 +412,7 @@ class PopulationAnnealing : public Solver
     trace_pop.clear();
     epoch = 0;
     target_pop = target_initial;
-    master = PcgEngine(seed);
+    master = ext_master ? *ext_master : PcgEngine(seed);
     streams.assign(T, 0);
     for (int t = 0; t < T; t++) streams[t] = PcgEngine(master()).state;  // rngs_[t] = fork()
     cur_beta = beta_start;
@@ -618,6 +620,12 @@ void PopulationAnnealing::run(cudaStream_t st)
   const double scale = model->scale_factor;  // rescale() at init
   std::vector<double> after, lowest;
   int64_t step = 0;
+  const auto t0 = std::chrono::steady_clock::now();
+  // the time limit, checked between steps (SteppingSolver::run)
+  auto out_of_time = [&] {
+    return has_time_limit &&
+           std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= time_limit;
+  };
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -710,6 +718,7 @@ void PopulationAnnealing::run(cudaStream_t st)
       step_multinomial(st, step);
       step++;
       if (has_cost_limit && has_low && low_cost <= cost_limit) break;
+      if (out_of_time()) break;
       continue;
     }
     cuda_check(cudaMemcpyAsync(after.data(), P.pop.cost, Rn * 8, cudaMemcpyDeviceToHost, st), "D2H");
@@ -852,8 +861,10 @@ void PopulationAnnealing::run(cudaStream_t st)
     }
     step++;
     if (has_cost_limit && has_low && low_cost <= cost_limit) break;
+    if (out_of_time()) break;
   }
   last_step = step;
+  if (ext_master) *ext_master = master;
   cudaEventRecord(e1, st);
   cudaEventSynchronize(e1);
   float ms = 0;
@@ -889,13 +900,16 @@ class SubstochasticMonteCarlo : public Solver
   uint64_t* d_init = nullptr;
   uint32_t* d_best = nullptr;
   PcgEngine master{0};
+  PcgEngine* ext_master = nullptr;  // repeated runs: the master stream continues from run to run
   bool has_low = false;
   double low_cost = 0;
   int T = 1;
+  int cap_R = 0;  // walkers the buffers hold
   // page-locked host copies of the costs, lowest costs and the copy map
   double* h_cost = nullptr;
   double* h_low = nullptr;
   int* h_src = nullptr;
+  int host_R = 0;
 
   ~SubstochasticMonteCarlo() override
   {
@@ -988,8 +1002,9 @@ class SubstochasticMonteCarlo : public Solver
     if (model->empty()) return;
     ensure_device();
     const int R = (int)target_pop;
-    if (!pools[0].buf.ptr)
+    if (!pools[0].buf.ptr || cap_R < R)
     {
+      cap_R = R;
       pools[0].alloc(*model, R);
       pools[1].alloc(*model, R);
       size_t off = 0;
@@ -1003,8 +1018,17 @@ class SubstochasticMonteCarlo : public Solver
       d_init = (uint64_t*)(b + o_in);
       d_best = (uint32_t*)(b + o_b);
     }
+    if (h_cost && host_R < R)
+    {
+      cudaFreeHost(h_cost);
+      cudaFreeHost(h_low);
+      cudaFreeHost(h_src);
+      h_cost = h_low = nullptr;
+      h_src = nullptr;
+    }
     if (!h_cost)
     {
+      host_R = R;
       cuda_check(cudaMallocHost((void**)&h_cost, (size_t)R * 8), "cudaMallocHost");
       cuda_check(cudaMallocHost((void**)&h_low, (size_t)R * 8), "cudaMallocHost");
       cuda_check(cudaMallocHost((void**)&h_src, (size_t)R * 4), "cudaMallocHost");
@@ -1018,7 +1042,7 @@ class SubstochasticMonteCarlo : public Solver
     // taking one draw per 32 variables (model/ising.h:23-41), or one
     // uniform() -- two draws -- per variable for MaxSat (model/max_sat.h:
     // 144-150)
-    master = PcgEngine(seed);
+    master = ext_master ? *ext_master : PcgEngine(seed);
     const bool ms = model->kind == K_MAXSAT;
     const uint64_t per = ms ? (uint64_t)(2 * model->N) : (uint64_t)((model->N + 31) / 32);
     std::vector<uint64_t> chain(T), wi(R);
@@ -1162,6 +1186,7 @@ class SubstochasticMonteCarlo : public Solver
     }
     step_pos = s;
     last_step = s;
+    if (ext_master) *ext_master = master;
     cudaEventRecord(e1, st);
     cudaEventSynchronize(e1);
     float ms = 0;
@@ -1220,6 +1245,652 @@ class SubstochasticMonteCarlo : public Solver
     }
   }
 };
+
+// ---------------------------------------------------------------------------
+// Parameter-free population annealing and substochastic Monte Carlo
+// ("populationannealing-parameterfree.cpu", "substochasticmontecarlo-
+// parameterfree.cpu"): solver/parameter_free_solver.h:9-257 with the
+// Bayesian strategy (bayes.h) and the adapters of solver/pa_parameter_free.h
+// and solver/ssmc_parameter_free.h.  Repeated runs of the underlying solver
+// on one master stream that continues from run to run (the adapter's rng_,
+// which also draws the initial samples' jitter).  The first
+// `initial_samples` runs take the adapter's initial parameter vectors; later
+// runs take the strategy's recommendations over the adapter's ranges (whose
+// step range follows the measured seconds per step), or, when the strategy
+// cannot fit its model, the best vector so far with its first entry x 1.5.
+// Each run is handed the time left as its time limit.  The search stops at
+// the time limit (default 5 s), when the time left is shorter than the last
+// search step took (the reference's tick then holds no step), after
+// `nonimprovement_limit` runs in a row without a lower cost, or after
+// `step_limit` runs.  The result is the lowest cost found and its state; the
+// parameters shown are those of the best run (with equal costs, the cheaper
+// run's), as ParameterFreeSolver::finalize renders them.
+// ---------------------------------------------------------------------------
+class BayesParameterFree : public Solver
+{
+ public:
+  BayesOpt strategy;
+  int initial_samples = 4, nonimprovement_limit = 8;
+  PcgEngine master{0};
+  double min_diff = 0, max_diff = 0;
+  int initial_counter = 0;
+  double worker_time_limit = 0;  // the adapter's time limit: the time left at its last run
+  double steps_accum = 0, secs_accum = 0;
+  bool has_best = false;
+  double best = 0, best_exec = 0;
+  int stable = 0;
+  std::vector<double> best_params;
+  std::vector<uint8_t> best_state;
+  struct Run
+  {
+    std::vector<double> params;
+    int64_t steps = 0, step_limit = 0;
+    double lowest = 0;
+    bool recommended = false;
+  };
+  std::vector<Run> trace;
+  std::string stop_reason;
+  uint64_t att_total = 0, acc_total = 0;
+
+  virtual Solver& worker() = 0;
+  virtual int dims() const = 0;
+  virtual std::vector<std::pair<double, double>> ranges() = 0;
+  virtual void initial_values(std::vector<double>& v) = 0;
+  virtual void update(const std::vector<double>& v) = 0;
+  virtual double exec_cost() = 0;
+  virtual void render() = 0;
+  virtual void prepare() {}
+
+  int64_t sweep_size() const { return model->kind == K_MAXSAT ? 1 : model->N; }
+
+  // ModelSolver::max_replicas_adjusted_state: the walkers that 58 % of the
+  // free device memory holds (a walker's two population slots), at most
+  // threads x mult, at least one
+  size_t max_states(uint32_t mult) const
+  {
+    const size_t cap = (size_t)threads * mult;
+    size_t free_b = 0, total_b = 0;
+    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    const double nw = (double)((model->N + 31) / 32 + 4);
+    const double per = 2.0 * (2.0 * nw * 4.0 + (double)model->M + 80.0);
+    const double adjust = (double)free_b / per * 0.58;
+    if (adjust < 1.0) return 1;
+    return std::min((size_t)adjust, cap);
+  }
+  // ModelSolver::adjust_states
+  size_t adjust_states(double x, uint32_t mult) const
+  {
+    const size_t mx = max_states(mult);
+    size_t r = std::min((size_t)x, mx);
+    if (mx > (size_t)threads)
+      r = std::max(r, (size_t)threads);
+    else
+      r = mx;
+    return r;
+  }
+
+  // parameters of the search itself (ParameterFreeSolver::training_parameters,
+  // BayesianOpt::configure)
+  void configure_search(const json::Value& p)
+  {
+    if (!replay) fail(1, "parameter-free solvers run with \"rng_mode\": \"replay\"");
+    if (number_of_solutions != 1)
+      fail(1, "parameter-free solvers return one solution: `number_of_solutions` must be 1");
+    auto integer = [&](const char* k, int64_t def) -> int64_t {
+      const json::Value* v = p.find(k);
+      if (!v || v->is_null()) return def;
+      if (!v->is_number()) fail(1, std::string("parameter `") + k + "`: expected integer");
+      return (int64_t)v->num;
+    };
+    initial_samples = (int)integer("initial_samples", 4);
+    if (initial_samples <= 0) fail(1, "parameter `initial_samples`: must be greater than 0");
+    nonimprovement_limit = (int)integer("nonimprovement_limit", 8);
+    if (nonimprovement_limit <= 0) fail(1, "parameter `nonimprovement_limit`: must be greater than 0");
+    const int64_t rs = integer("reserved_samples", 64);
+    if (rs <= 10) fail(1, "parameter `reserved_samples`: must be greater than 10");
+    // BayesianOpt::init resets the reserve to 128 samples whatever the
+    // parameter says (strategy/bayesian.cc:25-51, 53-57)
+    strategy.reserved = 128;
+    if (const json::Value* st = p.find("search_training"))
+      if (st->is_object())
+        if (const json::Value* v = st->find("num_to_sample"))
+        {
+          if (!v->is_number() || v->num < 1) fail(1, "parameter `num_to_sample`: expected a positive integer");
+          strategy.num_to_sample = (int)v->num;
+        }
+    if (!has_time_limit)
+    {
+      has_time_limit = true;  // a time limit must be set (parameter_free_solver.h:56-61)
+      time_limit = 5.0;
+    }
+  }
+
+  int64_t n_walkers() const override { return (model->empty() || !has_best) ? 0 : 1; }
+
+  void init(cudaStream_t) override
+  {
+    initialized = true;
+    ran = false;
+    master = PcgEngine(seed);
+    strategy.init(dims(), seed);
+    initial_counter = 0;
+    worker_time_limit = time_limit;
+    steps_accum = secs_accum = 0;
+    has_best = false;
+    best = best_exec = 0;
+    stable = 0;
+    best_params.clear();
+    best_state.clear();
+    trace.clear();
+    stop_reason.clear();
+    att_total = acc_total = 0;
+    last_step = 0;
+    launches = 0;
+    if (!model->empty()) prepare();
+  }
+
+  void run(cudaStream_t st) override
+  {
+    if (!initialized) fail(1, "init() must be called before run()");
+    ran = true;
+    if (model->empty()) return;
+    using clock = std::chrono::steady_clock;
+    const auto t0 = clock::now();
+    auto since = [](clock::time_point a) { return std::chrono::duration<double>(clock::now() - a).count(); };
+    double last = 0;
+    for (int64_t step = 0; step < step_limit; step++)
+    {
+      const double left0 = time_limit - since(t0);
+      if (left0 <= 0 || (step > 0 && left0 < last))
+      {
+        stop_reason = "time limit";
+        break;
+      }
+      const auto ts = clock::now();
+      // ParameterFreeSolver::make_step, solver/parameter_free_solver.h:65-151
+      std::vector<double> v;
+      bool rec = false;
+      if (step < initial_samples)
+        initial_values(v);
+      else
+      {
+        strategy.set_ranges(ranges());
+        rec = strategy.recommend(v);
+        if (!rec)
+        {
+          if (stable < nonimprovement_limit)
+          {
+            v = best_params;
+            v[0] *= 1.5;  // update_parameters_linearly
+          }
+          else
+          {
+            stop_reason = "no improvement";
+            break;
+          }
+        }
+      }
+      const double left = time_limit - since(t0);
+      if (left <= 0 && has_best)
+      {
+        stop_reason = "time limit";
+        break;
+      }
+      update(v);
+      Solver& w = worker();
+      w.has_time_limit = true;
+      w.time_limit = left;
+      worker_time_limit = left;
+      w.init(st);
+      const auto tr = clock::now();
+      w.run(st);
+      secs_accum += since(tr);  // update_accumulated_info
+      steps_accum += (double)w.last_step;
+      launches += w.launches;
+      double obj = 0;
+      std::vector<uint8_t> state;
+      lowest_of(w, obj, state);
+      strategy.add_sample(v, obj);
+      Run r;
+      r.params = v;
+      r.steps = w.last_step;
+      r.step_limit = w.step_limit;
+      r.lowest = obj + model->const_cost;
+      r.recommended = rec;
+      trace.push_back(r);
+      const double exec = exec_cost();
+      auto update_best = [&] {
+        best = obj;
+        best_exec = exec;
+        best_params = v;
+        best_state = state;
+      };
+      bool done = false;
+      if (has_best && std::abs(best - obj) < 10E-12)
+      {
+        stable++;
+        if (exec < best_exec) update_best();
+      }
+      if (stable >= nonimprovement_limit)
+      {
+        done = true;
+        stop_reason = "no improvement";
+      }
+      if (!has_best || best - obj > 10E-12)
+      {
+        stable = 0;
+        has_best = true;
+        update_best();
+      }
+      last_step = step + 1;
+      last = since(ts);
+      if (done) break;
+      if (has_cost_limit && best <= cost_limit)
+      {
+        stop_reason = "cost limit";
+        break;
+      }
+    }
+    if (stop_reason.empty()) stop_reason = "step limit";
+    if (has_best)
+    {
+      update(best_params);  // finalize: the best run's parameters
+      render();
+    }
+    run_ms = since(t0) * 1e3;
+  }
+
+  // a finished run's lowest cost and state (the lowest it ever saw), with its
+  // counters added to the totals
+  void lowest_of(Solver& w, double& obj, std::vector<uint8_t>& state)
+  {
+    std::vector<double> c, low;
+    std::vector<uint64_t> at, ac;
+    std::vector<uint8_t> ls;
+    w.fetch(c, low, at, ac, &ls, nullptr);
+    for (size_t i = 0; i < at.size(); i++)
+    {
+      att_total += at[i];
+      acc_total += ac[i];
+    }
+    if (w.historical_lowest(obj, state)) return;
+    size_t b = 0;
+    for (size_t i = 1; i < low.size(); i++)
+      if (low[i] < low[b]) b = i;
+    obj = low[b];
+    state.assign(ls.begin() + b * model->N, ls.begin() + (b + 1) * model->N);
+  }
+
+  void fetch(std::vector<double>& cost, std::vector<double>& lowest, std::vector<uint64_t>& att,
+             std::vector<uint64_t>& acc, std::vector<uint8_t>* lowest_states,
+             std::vector<uint8_t>* states) override
+  {
+    cost.clear();
+    lowest.clear();
+    att.clear();
+    acc.clear();
+    if (model->empty() || !has_best) return;
+    cost.push_back(best);
+    lowest.push_back(best);
+    att.push_back(att_total);
+    acc.push_back(acc_total);
+    if (lowest_states) *lowest_states = best_state;
+    if (states) *states = best_state;
+  }
+
+  std::string extra_benchmark() override
+  {
+    std::string s = ",\"parameter_free\":{\"runs\":[";
+    for (size_t i = 0; i < trace.size(); i++)
+    {
+      const Run& r = trace[i];
+      s += (i ? "," : "") + std::string("{\"params\":[");
+      for (size_t k = 0; k < r.params.size(); k++) s += (k ? "," : "") + json::number(r.params[k]);
+      s += "],\"steps\":" + std::to_string(r.steps) + ",\"step_limit\":" + std::to_string(r.step_limit) +
+           ",\"lowest\":" + json::number(r.lowest) + ",\"recommended\":" + (r.recommended ? "true" : "false") + "}";
+    }
+    s += "],\"stop\":" + json::quote(stop_reason) + ",\"training\":{\"learning_time_ms\":" +
+         json::number(strategy.learning_ms) + ",\"model_time_ms\":" + json::number(strategy.model_ms) + "}}";
+    return s;
+  }
+
+ protected:
+  // a range parameter {"initial": a, "final": b} (utils/range.cc:16-30)
+  static void range_param(const json::Value& p, const char* k, std::pair<double, double>& r)
+  {
+    const json::Value* v = p.find(k);
+    if (!v || v->is_null()) return;
+    const json::Value* a = v->is_object() ? v->find("initial") : nullptr;
+    const json::Value* b = v->is_object() ? v->find("final") : nullptr;
+    if (!a || !b || !a->is_number() || !b->is_number())
+      fail(1, std::string("parameter `") + k + "`: expected {\"initial\": number, \"final\": number}");
+    if (a->num > b->num)
+      fail(1, "initial value: " + json::number(a->num) + ", is larger than final value:" + json::number(b->num));
+    r = {a->num, b->num};
+  }
+  static double num_param(const json::Value& p, const char* k, double def)
+  {
+    const json::Value* v = p.find(k);
+    if (!v || v->is_null()) return def;
+    if (!v->is_number()) fail(1, std::string("parameter `") + k + "`: expected number");
+    return v->num;
+  }
+};
+
+// PAParameterFree (solver/pa_parameter_free.h:18-410): five parameters --
+// sweeps, population, alpha, sweeps per replica and the negative log of the
+// smallest acceptance probability, which sets beta_stop; a geometric beta
+// schedule from -ln(max_prob) / (max cost difference).  The linear-schedule
+// resampling strategy (the reference's default; its other strategies are
+// experimental and not built).
+class PAParameterFree : public BayesParameterFree
+{
+ public:
+  std::unique_ptr<PopulationAnnealing> w;
+  double max_step_divider = 160, min_population_mult = 4, initial_alpha = 2, initial_min_prob_log = 2;
+  double max_prob = 0.5, final_min_prob_log = 15, start_min_prob_log = 0, beta_start = 0;
+  uint32_t initial_sweeps = 20, max_population_mult = 128;
+  std::pair<double, double> alpha_range{1.00000001, 3}, spr_range{1, 4};
+  uint64_t max_steps = std::numeric_limits<uint32_t>::max() / 8;
+  double population_start = 0, population_end = 0;
+
+  std::string target() const override { return "populationannealing-parameterfree.cpu"; }
+  Solver& worker() override { return *w; }
+  int dims() const override { return 5; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common_public(*this, doc);
+    w.reset(new PopulationAnnealing());
+    w->model = model;
+    w->configure(doc);
+    if (w->strategy != "linear_schedule")
+      fail(1, "parameter-free population annealing supports `resampling_strategy` \"linear_schedule\" only");
+    if (w->multinomial) fail(1, "parameter-free population annealing uses the reference resampling");
+    const json::Value& p = params;
+    configure_search(p);
+    max_step_divider = num_param(p, "max_step_divider", 160.);
+    if (!(max_step_divider > 1.0)) fail(1, "parameter `max_step_divider`: must be greater than 1");
+    min_population_mult = num_param(p, "min_population_mult", 4);
+    if (!(min_population_mult > 0)) fail(1, "parameter `min_population_mult`: must be greater than 0");
+    const double is = num_param(p, "initial_sweeps", 20);
+    if (!(is >= 1)) fail(1, "parameter `initial_sweeps`: must be greater than 0");
+    initial_sweeps = (uint32_t)is;
+    initial_alpha = num_param(p, "initial_alpha", 2);
+    if (!(initial_alpha > 1)) fail(1, "parameter `initial_alpha`: must be greater than 1");
+    initial_min_prob_log = num_param(p, "initial_min_prob_log", 2);
+    if (!(initial_min_prob_log >= 0)) fail(1, "parameter `initial_min_prob_log`: must be at least 0");
+    max_prob = num_param(p, "max_prob", 0.5);
+    if (!(max_prob > 0 && max_prob <= 1)) fail(1, "parameter `max_prob`: must be in (0, 1]");
+    const double mpm = num_param(p, "max_population_mult", 128);
+    if (!(mpm > (double)((uint32_t)min_population_mult + 1)))
+      fail(1, "parameter `max_population_mult`: must be greater than min_population_mult + 1");
+    max_population_mult = (uint32_t)mpm;
+    range_param(p, "alpha_range", alpha_range);
+    range_param(p, "sweeps_per_replica_range", spr_range);
+    if (num_param(p, "reserved_population", 0) != 0)
+      fail(1, "parameter `reserved_population`: only 0 (no replicas carried between runs) is supported");
+    const double limit = std::sqrt((double)sweep_size()) * (double)model->M;
+    if (limit < (double)std::numeric_limits<uint32_t>::max())
+      max_steps = std::max<uint64_t>(max_steps, (uint64_t)limit);
+    else
+      max_steps = std::numeric_limits<uint32_t>::max();
+    if (p.find("max_steps"))
+    {
+      const double ms = num_param(p, "max_steps", (double)max_steps);
+      if (!(ms > 65535)) fail(1, "parameter `max_steps`: must be greater than 65535");
+      max_steps = (uint64_t)ms;
+    }
+    if (!model->empty())
+    {
+      if (model->kind == K_MAXSAT)
+        fail(1, "parameter-free population annealing runs Ising and PUBO models (it needs cost-difference "
+                "estimates)");
+      max_diff = estimate_max_cost_diff(*model);
+      min_diff = estimate_min_cost_diff(*model);
+      if (!(max_diff > 0)) fail(1, "max cost difference should be > 0, found :" + json::number(max_diff));
+      if (!(min_diff > 0)) fail(1, "min cost difference should be > 0, found :" + json::number(min_diff));
+      beta_start = -std::log(max_prob) / max_diff;
+      start_min_prob_log = min_diff * beta_start * 2;
+      const json::Value* f = p.find("final_min_prob_log");
+      if (f && !f->is_null())
+      {
+        if (!f->is_number() || !(f->num > start_min_prob_log))
+          fail(1, "parameter `final_min_prob_log`: must be greater than " + json::number(start_min_prob_log));
+        final_min_prob_log = f->num;
+      }
+      start_min_prob_log = std::max(initial_min_prob_log, start_min_prob_log);
+      final_min_prob_log = std::max(final_min_prob_log, start_min_prob_log * 5);
+    }
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"beta_start", json::number(beta_start)});
+  }
+
+  void prepare() override
+  {
+    ensure_device();
+    population_end = (double)max_states(max_population_mult);
+    population_start = (double)threads * min_population_mult;
+    if (population_start >= population_end) population_start = population_end - 1.;
+    w->ext_master = &master;
+  }
+
+  std::vector<std::pair<double, double>> ranges() override
+  {
+    const double sps = secs_accum / steps_accum;
+    double ms = worker_time_limit / (sps * max_step_divider);
+    ms = std::max(ms, (double)initial_sweeps + 1);
+    ms = std::min((double)max_steps, ms);
+    return {{(double)initial_sweeps, ms},
+            {population_start, population_end},
+            alpha_range,
+            spr_range,
+            {start_min_prob_log, final_min_prob_log}};
+  }
+
+  void initial_values(std::vector<double>& v) override
+  {
+    const int k = initial_counter;
+    v.clear();
+    v.push_back((double)(initial_sweeps + k * 10));
+    v.push_back((double)adjust_states((double)threads * (k + 1), max_population_mult));
+    v.push_back(initial_alpha + 0.5 * (master.uniform() - 0.5));
+    v.push_back(k + 1.0);
+    v.push_back(initial_min_prob_log + k * 2);
+    initial_counter++;
+  }
+
+  void update(const std::vector<double>& v) override
+  {
+    w->spr = std::max<int64_t>(1, std::lround(v[3]));
+    w->step_limit = std::max<int64_t>((int64_t)std::ceil(v[0] / (double)w->spr), 2);
+    w->target_initial = adjust_states(v[1], max_population_mult);
+    w->alpha = std::max(v[2], alpha_range.first);
+    const double beta_stop = v[4] / min_diff;
+    Schedule b;
+    b.type = 1;
+    b.initial = beta_start;
+    b.final_ = beta_stop;
+    b.has_stop = true;
+    b.stop_ = std::max(1, (int)w->step_limit - 1);
+    w->beta = b;
+    w->beta_start = b.get_value(0);
+  }
+
+  double exec_cost() override
+  {
+    const size_t t = (size_t)threads;
+    return (double)w->step_limit * (double)w->spr * (double)((w->target_initial + t - 1) / t);
+  }
+
+  void render() override
+  {
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"beta_start", json::number(beta_start)});
+    output_params.push_back({"beta_stop", json::number(w->beta.final_)});
+    output_params.push_back({"beta", w->beta.render()});
+    output_params.push_back({"sweeps", std::to_string(w->step_limit)});
+    output_params.push_back({"sweeps_per_replica", std::to_string(w->spr)});
+    output_params.push_back({"population", std::to_string(w->target_initial)});
+    output_params.push_back({"alpha", json::number(w->alpha)});
+  }
+};
+
+// SSMCParameterFree (solver/ssmc_parameter_free.h:10-280): seven parameters
+// -- steps, target population, steps per walker, alpha's final value and
+// scope (a linear schedule from final + scope down to final) and beta's
+// initial value and scope (linear, initial up to initial + scope).
+class SSMCParameterFree : public BayesParameterFree
+{
+ public:
+  std::unique_ptr<SubstochasticMonteCarlo> w;
+  uint32_t max_replica_mult = 3, initial_sweeps = 20, initial_spw = 1;
+  double max_step_divider = 40, initial_alpha_final = 0.00001, initial_alpha_scope = 0.8;
+  double initial_beta_initial = 0.00001, initial_beta_scope = 5;
+  uint64_t max_steps = std::numeric_limits<uint16_t>::max();
+  std::pair<double, double> steps_range{1., 5.}, alpha_final_range{0.00001, 0.2}, alpha_scope_range{0.8, 1.0},
+      beta_initial_range{0.00001, 8.0}, beta_scope_range{1, 8.0};
+  double population_start = 0, population_end = 0;
+
+  std::string target() const override { return "substochasticmontecarlo-parameterfree.cpu"; }
+  Solver& worker() override { return *w; }
+  int dims() const override { return 7; }
+
+  void configure(const json::Value& doc)
+  {
+    configure_common_public(*this, doc);
+    w.reset(new SubstochasticMonteCarlo());
+    w->model = model;
+    w->configure(doc);
+    const json::Value& p = params;
+    configure_search(p);
+    range_param(p, "steps_range", steps_range);
+    range_param(p, "alpha_final_range", alpha_final_range);
+    range_param(p, "alpha_scope_range", alpha_scope_range);
+    range_param(p, "beta_initial_range", beta_initial_range);
+    range_param(p, "beta_scope_range", beta_scope_range);
+    auto positive = [&](const char* k, double def) {
+      const double x = num_param(p, k, def);
+      if (!(x > 0)) fail(1, std::string("parameter `") + k + "`: must be greater than 0");
+      return x;
+    };
+    max_replica_mult = (uint32_t)positive("max_replica_mult", 3);
+    max_step_divider = num_param(p, "max_step_divider", 40.);
+    if (!(max_step_divider > 1.0)) fail(1, "parameter `max_step_divider`: must be greater than 1");
+    initial_sweeps = (uint32_t)positive("initial_sweeps", 20);
+    initial_spw = (uint32_t)positive("initial_steps_per_walker", 1);
+    initial_alpha_final = positive("initial_alpha_final", 0.00001);
+    initial_alpha_scope = positive("initial_alpha_scope", 0.8);
+    initial_beta_initial = positive("initial_beta_initial", 0.00001);
+    initial_beta_scope = positive("initial_beta_scope", 5);
+    if (num_param(p, "reserved_population", 0) != 0)
+      fail(1, "parameter `reserved_population`: only 0 (no walkers carried between runs) is supported");
+    const double ss = (double)sweep_size();
+    const double limit = std::sqrt(ss) * (double)model->M * ss;
+    if (limit < (double)std::numeric_limits<uint32_t>::max())
+      max_steps = std::max<uint64_t>(max_steps, (uint64_t)limit);
+    else
+      max_steps = std::numeric_limits<uint32_t>::max();
+    if (p.find("max_steps"))
+    {
+      const double ms = num_param(p, "max_steps", (double)max_steps);
+      if (!(ms > 65535)) fail(1, "parameter `max_steps`: must be greater than 65535");
+      max_steps = (uint64_t)ms;
+    }
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+  }
+
+  void prepare() override
+  {
+    ensure_device();
+    population_end = (double)max_states(max_replica_mult);
+    population_start = (double)threads;
+    if (population_start >= population_end) population_start = population_end - 1.;
+    w->ext_master = &master;
+  }
+
+  std::vector<std::pair<double, double>> ranges() override
+  {
+    const double sps = secs_accum / steps_accum;
+    const double ss = (double)sweep_size();
+    double ms = worker_time_limit / (sps * max_step_divider);
+    ms = std::max(ms, 100.0);
+    ms = std::max(ms, initial_sweeps * ss + 1.0);
+    ms = std::min((double)max_steps, ms);
+    return {{initial_sweeps * ss, ms},    {population_start, population_end}, steps_range, alpha_final_range,
+            alpha_scope_range,            beta_initial_range,                 beta_scope_range};
+  }
+
+  void initial_values(std::vector<double>& v) override
+  {
+    const int k = initial_counter;
+    v.clear();
+    v.push_back((double)((uint64_t)initial_sweeps * (uint64_t)sweep_size() * (uint64_t)(1 + k)));
+    v.push_back(std::min((double)threads + k, (double)max_states(max_replica_mult)));
+    v.push_back((double)initial_spw);
+    v.push_back(initial_alpha_final);
+    v.push_back(initial_alpha_scope);
+    v.push_back(initial_beta_initial);
+    v.push_back(initial_beta_scope + 1.0 * master.uniform());
+    initial_counter++;
+  }
+
+  void update(const std::vector<double>& v) override
+  {
+    w->step_limit = std::max<int64_t>((int64_t)std::floor(v[0]), 2);
+    w->target_pop = (int64_t)adjust_states(v[1], max_replica_mult);
+    w->spw = std::max<int64_t>((int64_t)(size_t)v[2], 1);
+    Schedule a, b;
+    a.type = 0;
+    a.initial = v[3] + v[4];
+    a.final_ = v[3];
+    a.has_stop = true;
+    a.stop_ = (double)w->step_limit;
+    b.type = 0;
+    b.initial = v[5];
+    b.final_ = v[5] + v[6];
+    b.has_stop = true;
+    b.stop_ = (double)w->step_limit;
+    w->alpha = a;
+    w->beta = b;
+  }
+
+  double exec_cost() override
+  {
+    const int64_t t = threads;
+    return (double)w->step_limit * (double)w->spw * (double)((w->target_pop + t - 1) / t);
+  }
+
+  void render() override
+  {
+    output_params.clear();
+    output_params.push_back({"seed", std::to_string(seed)});
+    output_params.push_back({"step_limit", std::to_string(w->step_limit)});
+    output_params.push_back({"target_population", std::to_string(w->target_pop)});
+    output_params.push_back({"steps_per_walker", std::to_string(w->spw)});
+    output_params.push_back({"alpha", w->alpha.render()});
+    output_params.push_back({"beta", w->beta.render()});
+  }
+};
+
+std::unique_ptr<Solver> make_pa_pf_solver(const HostModel* m, const json::Value& doc)
+{
+  std::unique_ptr<PAParameterFree> s(new PAParameterFree());
+  s->model = m;
+  s->configure(doc);
+  return std::unique_ptr<Solver>(s.release());
+}
+
+std::unique_ptr<Solver> make_ssmc_pf_solver(const HostModel* m, const json::Value& doc)
+{
+  std::unique_ptr<SSMCParameterFree> s(new SSMCParameterFree());
+  s->model = m;
+  s->configure(doc);
+  return std::unique_ptr<Solver>(s.release());
+}
 
 std::unique_ptr<Solver> make_ssmc_solver(const HostModel* m, const json::Value& doc)
 {

@@ -1267,6 +1267,8 @@ class ParallelTempering : public Solver
 
 std::unique_ptr<Solver> make_pa_solver(const HostModel* m, const json::Value& doc);
 std::unique_ptr<Solver> make_ssmc_solver(const HostModel* m, const json::Value& doc);
+std::unique_ptr<Solver> make_pa_pf_solver(const HostModel* m, const json::Value& doc);
+std::unique_ptr<Solver> make_ssmc_pf_solver(const HostModel* m, const json::Value& doc);
 
 // ---------------------------------------------------------------------------
 // Tabu search ("tabu.qiotoolkit": solver/tabu.h:22-164 with
@@ -2284,6 +2286,8 @@ std::unique_ptr<Solver> make_solver(const HostModel* m, const std::string& targe
   }
   if (target == "populationannealing.cpu") return make_pa_solver(m, doc);
   if (target == "substochasticmontecarlo.cpu") return make_ssmc_solver(m, doc);
+  if (target == "populationannealing-parameterfree.cpu") return make_pa_pf_solver(m, doc);
+  if (target == "substochasticmontecarlo-parameterfree.cpu") return make_ssmc_pf_solver(m, doc);
   if (target == "simulatedannealing-parameterfree.qiotoolkit")
   {
     std::unique_ptr<SAParameterFree> s(new SAParameterFree());

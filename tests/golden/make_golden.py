@@ -17,7 +17,7 @@ Sources (paths relative to the reference's cpp/ or data/ directory):
                      solver/test/tabu_test.cc:98-184,
                      solver/test/substochastic_monte_carlo_test.cc:104-176,
                      solver/test/quantum_monte_carlo_test.cc:86-148 (data/params_qmc.json),
-                     solver/test/{tabu,sa,pt}_pf_test.cc:23-115 (data/pf5s.json),
+                     solver/test/{tabu,sa,pt,pa,ssmc}_pf_test.cc:23-115 (data/pf5s.json),
                      with their data/ inputs and data/params1.json
   planted.json       data/input_e2e_pipeline/{wishart_planting_N_16_alpha_0.81,
                      combined_4_local_N_16}_qualitytest (instances + energies)
@@ -207,6 +207,18 @@ def solver_pins():
         ("pt_pf", "ising", "ising1.json", -10, {}, "solver/test/pt_pf_test.cc:68-81"),
         ("pt_pf", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/pt_pf_test.cc:83-98"),
         ("pt_pf", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/pt_pf_test.cc:100-115"),
+        ("pa_pf", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/pa_pf_test.cc:23-36"),
+        ("pa_pf", "pubo", "puboempty.json", 2, {}, "solver/test/pa_pf_test.cc:38-51"),
+        ("pa_pf", "ising", "isingempty.json", 12, {}, "solver/test/pa_pf_test.cc:53-66"),
+        ("pa_pf", "ising", "ising1.json", -10, {}, "solver/test/pa_pf_test.cc:68-81"),
+        ("pa_pf", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/pa_pf_test.cc:83-98"),
+        ("pa_pf", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/pa_pf_test.cc:100-115"),
+        ("ssmc_pf", "pubo", "cpupubojobstest.json", -12, {}, "solver/test/ssmc_pf_test.cc:23-36"),
+        ("ssmc_pf", "pubo", "puboempty.json", 2, {}, "solver/test/ssmc_pf_test.cc:38-51"),
+        ("ssmc_pf", "ising", "isingempty.json", 12, {}, "solver/test/ssmc_pf_test.cc:53-65"),
+        ("ssmc_pf", "ising", "ising1.json", -10, {}, "solver/test/ssmc_pf_test.cc:67-79"),
+        ("ssmc_pf", "pubo", "puboemptymixed.json", -104, {"1": 1, "12": 1}, "solver/test/ssmc_pf_test.cc:81-96"),
+        ("ssmc_pf", "ising", "isingemptymixed.json", -100, {"1": -1, "10": 1}, "solver/test/ssmc_pf_test.cc:98-112"),
     ]
     params_qmc = json.loads(read("params_qmc.json", DATA))["params"]
     params_pf = json.loads(read("pf5s.json", DATA))["params"]
@@ -216,7 +228,8 @@ def solver_pins():
         cases.append({"solver": solver, "kind": kind, "file": fname,
                       "terms": model["terms"],
                       "params": {"qmc": params_qmc, "tabu_pf": params_pf, "sa_pf": params_pf,
-                                 "pt_pf": params_pf}.get(solver, params1),
+                                 "pt_pf": params_pf, "pa_pf": params_pf,
+                                 "ssmc_pf": params_pf}.get(solver, params1),
                       "expected_cost": cost, "configuration": conf, "source": source})
     return {"params_file": "data/params1.json", "cases": cases}
 

@@ -185,6 +185,8 @@ def test_reference_solver_pins_on_gpu(golden):
             p = {"seed": 0, "min_num_restarts": 8, "timeout": p["timeout"]}
         if case["solver"] == "pt_pf":
             p = {"seed": 0, "min_num_betas": 8, "timeout": p["timeout"]}
+        if case["solver"] in ("pa_pf", "ssmc_pf"):
+            p = {"seed": 0, "threads": 4, "timeout": p["timeout"]}
         if case["solver"] == "ssmc":
             p = {"seed": p["seed"], "sweeps": p["sweeps"], "target_population": 8, "threads": 8}
         target = {"sa": SA, "pt": PT, "pa": PA, "tabu": "tabu.qiotoolkit",
@@ -192,7 +194,9 @@ def test_reference_solver_pins_on_gpu(golden):
                   "qmc": "quantummontecarlo.qiotoolkit",
                   "tabu_pf": "tabu-parameterfree.qiotoolkit",
                   "sa_pf": "simulatedannealing-parameterfree.qiotoolkit",
-                  "pt_pf": "paralleltempering-parameterfree.qiotoolkit"}[case["solver"]]
+                  "pt_pf": "paralleltempering-parameterfree.qiotoolkit",
+                  "pa_pf": "populationannealing-parameterfree.cpu",
+                  "ssmc_pf": "substochasticmontecarlo-parameterfree.cpu"}[case["solver"]]
         res = q.run_json(doc, {"params": p}, target)
         cost = res["solutions"]["cost"]
         exp = case["expected_cost"]
