@@ -622,6 +622,11 @@ qio_status qio_run_json(const char* input_json, const char* params_json, const c
     bool memory_saving = false;
     if (ef && ef->is_array())
       for (const auto& x : ef->arr) memory_saving = memory_saving || (x.is_number() && x.num == 3);
+    // Runner::target_support_memory_saving (app/runner.h:143-147): not for
+    // the SSMC targets
+    const std::string tgt(target);
+    if (tgt == "substochasticmontecarlo.cpu" || tgt == "substochasticmontecarlo-parameterfree.cpu")
+      memory_saving = false;
     if (memory_saving && doc.is_object() && doc.find("cost_function"))
     {
       const json::Value* t = doc["cost_function"].find("type");

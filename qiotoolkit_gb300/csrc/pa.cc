@@ -1441,12 +1441,13 @@ class BayesParameterFree : public Solver
       w.has_time_limit = true;
       w.time_limit = left;
       worker_time_limit = left;
+      const uint64_t l0 = w.launches;  // the workers count on across runs
       w.init(st);
       const auto tr = clock::now();
       w.run(st);
       secs_accum += since(tr);  // update_accumulated_info
       steps_accum += (double)w.last_step;
-      launches += w.launches;
+      launches += w.launches - l0;
       double obj = 0;
       std::vector<uint8_t> state;
       lowest_of(w, obj, state);
