@@ -5,6 +5,7 @@
 // --gpu it also runs the model + solver binding and the whole-runner
 // binding on the device and prints their costs.
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -63,6 +64,20 @@ int main(int argc, char** argv)
         "bad params refused");
   CHECK(qio_solver_create(model, "no-such-solver", R"({"params": {}})", &solver) != QIO_OK,
         "unknown target refused");
+
+  // the parameter-free search strategy on caller samples (host only): a
+  // parabola in one dimension with its minimum at 2
+  {
+    const double lo[1] = {0.0}, hi[1] = {5.0};
+    const double xs[5] = {0.0, 1.0, 3.0, 4.0, 5.0};
+    double ys[5];
+    for (int i = 0; i < 5; i++) ys[i] = (xs[i] - 2.0) * (xs[i] - 2.0);
+    double pick[2] = {-1, -1};
+    CHECK(qio_bayes_recommend(1, lo, hi, 5, xs, ys, 7, 2, pick) == QIO_OK, "strategy recommends");
+    CHECK(pick[0] >= 0.0 && pick[0] <= 5.0 && pick[1] >= 0.0 && pick[1] <= 5.0, "picks in the box");
+    CHECK(std::fabs(pick[0] - 2.0) < 1.0, "first pick near the minimum");
+    CHECK(qio_bayes_recommend(1, lo, hi, 1, xs, ys, 7, 1, pick) == QIO_INVALID_ARGUMENT, "one sample refused");
+  }
 
   if (gpu)
   {
