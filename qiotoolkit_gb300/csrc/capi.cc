@@ -636,7 +636,30 @@ qio_status qio_run_json(const char* input_json, const char* params_json, const c
     std::unique_ptr<HostModel> m = build_model_json(doc, kind);
     std::unique_ptr<Solver> s = make_solver(m.get(), target, pdoc);
     cudaStream_t st = 0;
-    s->init(st);
+    bool retried = false;
+    try
+    {
+      s->init(st);
+    }
+    catch (const Error& e)
+    {
+      // Runner::get_run_output (app/runner.cc:517-535, memory_saving_retry
+      // 500-505): an init that runs out of memory is tried once more with the
+      // memory-saving models, when memory saving was off and the target and
+      // the model kind support it
+      const json::Value* t = doc.is_object() && doc.find("cost_function") ? doc["cost_function"].find("type")
+                                                                          : nullptr;
+      const bool ising = t && t->is_string() && t->str == "ising";
+      const bool pubo = t && t->is_string() && t->str == "pubo";
+      const bool ssmc = tgt == "substochasticmontecarlo.cpu" || tgt == "substochasticmontecarlo-parameterfree.cpu";
+      if (e.status != 2 || memory_saving || ssmc || !(ising || pubo)) throw;
+      s.reset();
+      m.reset();
+      m = build_model_json(doc, ising ? K_ISING_PLAIN : K_PUBO_PLAIN);
+      s = make_solver(m.get(), target, pdoc);
+      s->init(st);
+      retried = true;
+    }
     cuda_check(cudaStreamSynchronize(st), "sync");
     // Runner::get_run_output (app/runner.cc:530-631): solver wall and CPU
     // time, threads, peak memory, input and output sizes, the stages' times
@@ -660,7 +683,8 @@ qio_status qio_run_json(const char* input_json, const char* params_json, const c
           ",\"end2end_time_ms\":" + json::number(pre_ms + run_ms + post_ms) +
           ",\"end2end_cputime_ms\":" + json::number(1000.0 * ((double)std::clock() / CLOCKS_PER_SEC - cpu0)) +
           ",\"preprocessing_time_ms\":" + json::number(pre_ms) +
-          ",\"postprocessing_time_ms\":" + json::number(post_ms);
+          ",\"postprocessing_time_ms\":" + json::number(post_ms) +
+          (retried ? ",\"memory_saving_retry\":true" : "");
       (void)cpu1;
       return s->result_json();
     };

@@ -1,6 +1,8 @@
 // model_host.cc -- model construction and upload, schedules, device setup.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -23,19 +25,44 @@ void cuda_check(cudaError_t e, const char* what)
   fail(3, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Device bytes held in buffers.  QIO_DEVICE_MEMORY_LIMIT (bytes, read at
+// each allocation) caps them, for callers that share a GPU: an allocation
+// past the cap fails as out of device memory (status 2), as it would on a
+// full device.
+static std::atomic<long long> g_held{0};
+
+static long long device_memory_limit()
+{
+  const char* e = std::getenv("QIO_DEVICE_MEMORY_LIMIT");
+  return e ? std::atoll(e) : 0;
+}
+
 DevBuf::DevBuf(size_t n) : bytes(n)
 {
-  if (n) cuda_check(cudaMalloc(&ptr, n), "cudaMalloc");
+  if (!n) return;
+  const long long cap = device_memory_limit();
+  if (cap > 0 && g_held.load() + (long long)n > cap)
+    fail(2, "cudaMalloc: out of device memory (over QIO_DEVICE_MEMORY_LIMIT)");
+  cuda_check(cudaMalloc(&ptr, n), "cudaMalloc");
+  g_held += (long long)n;
 }
 DevBuf::~DevBuf()
 {
-  if (ptr) cudaFree(ptr);
+  if (ptr)
+  {
+    cudaFree(ptr);
+    g_held -= (long long)bytes;
+  }
 }
 DevBuf& DevBuf::operator=(DevBuf&& o) noexcept
 {
   if (this != &o)
   {
-    if (ptr) cudaFree(ptr);
+    if (ptr)
+    {
+      cudaFree(ptr);
+      g_held -= (long long)bytes;
+    }
     ptr = o.ptr;
     bytes = o.bytes;
     o.ptr = nullptr;
