@@ -60,6 +60,11 @@ WORKLOADS = {
                        "N=1000, 3000 ER couplings +-1, 1000 fields U[-0.5,0.5], min_num_restarts 64, "
                        "seed 0, timeout 3 s per solve",
                   target="simulatedannealing-parameterfree.qiotoolkit"),
+    "pf_pa": dict(desc="Parameter-free PA (Bayesian search, repeated PA runs) on the sparse Ising "
+                       "N=1000, 3000 ER couplings +-1, 1000 fields U[-0.5,0.5], counter streams (each walker "
+                       "its own; threads 16), "
+                       "seed 0, timeout 3 s per solve",
+                  target="populationannealing-parameterfree.cpu"),
     "tabu_ising": dict(desc="Tabu search on the sparse Ising N=1000, 3000 ER couplings +-1, 1000 fields "
                             "U[-0.5,0.5], tabu_tenure 20, 200 sweeps, 1216 restarts, seed 0; attempts are "
                             "cost-difference evaluations (scan and hill-climbing sweeps)",
@@ -504,6 +509,9 @@ def run_workload(args, ws, rank):
     if args.workload == "pf_sa":
         main_pf(args, ws, rank)
         return
+    if args.workload == "pf_pa":
+        main_pf_pa(args, ws, rank)
+        return
     if args.workload == "serving_1e5":
         main_serving(args, ws, rank)
         return
@@ -784,6 +792,130 @@ def main_pf(args, ws, rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": WORKLOADS["pf_sa"]["desc"], "runs_per_solve": len(runs),
+                       "best_cost": best, "l2": "flushed before each step (256 MB write)"},
+            "e2e": e2e, "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "sweep_kernel (whole solves timed)", "bytes_per_attempt": bpa},
+            "roofline_onchip": onchip(achieved, clk.summary()),
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+PF_PA_PARAMS = {"seed": 0, "timeout": 3, "threads": 16, "rng_mode": "counter"}
+
+
+def main_pf_pa(args, ws, rank):
+    """Parameter-free PA: flip attempts/s over whole parameter-free solves
+    (every PA run of the search, its attempts counted as walkers x sweeps x
+    N per step), the same solve through the C ABI from host buffers, and the
+    same runs replayed by the oracle on the host cores."""
+    import torch
+    import qiotoolkit_gb300 as q
+    from qiotoolkit_gb300 import instances as I
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    q.load()
+    target = WORKLOADS["pf_pa"]["target"]
+    off, ids, coef = I.er_ising(1000, 3000, seed=0)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    model = q.Model("ising", off=off, ids=ids, coef=coef)
+    solver = q.Solver(model, target, {"params": PF_PA_PARAMS})
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def one_step():
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.init(sh)
+        solver.run(sh)
+        e1.record(stream)
+        e1.synchronize()
+        runs = solver.result()["benchmark"]["parameter_free"]["runs"]
+        return e0.elapsed_time(e1), sum(int(r["attempts"]) for r in runs), solver.stats()
+
+    for _ in range(args.warmup):
+        one_step()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ms, att, launches = [], 0, 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, a, st = one_step()
+            ms.append(t)
+            att += a
+            launches += int(st.kernel_launches)
+    torch.cuda.synchronize()
+    barrier(ws)
+    total_s = reduce_max(sum(ms) / 1e3, ws)
+    value = att * ws / total_s
+    res = solver.result()
+    runs = res["benchmark"]["parameter_free"]["runs"]
+    best = res["solutions"]["cost"]
+
+    e2e = None
+    if not args.no_e2e:
+        times, h2d, d2h, att_e = [], 0, 0, []
+        for i in range(1 + min(args.steps, 3)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m = q.Model("ising", off=off, ids=ids, coef=coef)
+            s = q.Solver(m, target, {"params": PF_PA_PARAMS})
+            s.init(sh)
+            s.run(sh)
+            r = s.result()
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(time.perf_counter() - t0)
+                att_e.append(sum(int(x["attempts"]) for x in r["benchmark"]["parameter_free"]["runs"]))
+            h2d = int(m.info.device_bytes)
+            d2h = int(m.n_vars * 8 + 64)
+            s.close()
+            m.close()
+        e2e = {"value": sum(att_e) / sum(times), "unit": "flip attempts/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # the same PA runs (parameters, continuing master stream) on the
+        # oracle, in order, until about 15 s of CPU time
+        from oracle import oracle as O
+        o = O.Model("ising", off=off, ids=ids, coef=coef)
+        terms = [(float(coef[k]), [int(x) for x in ids[off[k]:off[k + 1]]]) for k in range(len(coef))]
+        cores = min(PF_PA_PARAMS["threads"], os.cpu_count() or 1)
+        whole = []
+        for x in runs:
+            if x["steps"] < x["step_limit"]:
+                break  # a run the time limit cut short ends the replayable prefix
+            whole.append(x)
+        t0 = time.perf_counter()
+        ref = O.pa_parameter_free_replay(o, "ising", terms, seed=PF_PA_PARAMS["seed"],
+                                         threads=PF_PA_PARAMS["threads"], runs=[x["params"] for x in whole],
+                                         budget_s=15.0, rng_mode=PF_PA_PARAMS["rng_mode"])
+        k = len(ref)
+        a_cpu = sum(int(x["attempts"]) for x in whole[:k])
+        same = all(r[2] == x["lowest"] for r, x in zip(ref, whole))
+        dt = time.perf_counter() - t0
+        cpu = {"value": a_cpu / dt if dt > 0 else None, "unit": "flip attempts/s", "cores": cores,
+               "kind": "port",
+               "sample": f"the first {k} of the solve's {len(runs)} PA runs replayed by the oracle "
+                         f"(same parameters and master stream); {a_cpu:.3g} attempts; identical lowest "
+                         f"costs: {same}"}
+
+    if rank == 0:
+        kernel_s = sum(ms) / 1e3
+        bpa = 100.0  # the sparse Ising N=1000 model: 8 + 7 x (4 + 8 + 1) + 1 bytes per attempt
+        achieved = bpa * att / kernel_s / 1e9
+        peak, peak_src = peaks()
+        line = {
+            "metric": "flip attempts/s", "value": value, "unit": "flip attempts/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOADS["pf_pa"]["desc"], "runs_per_solve": len(runs),
                        "best_cost": best, "l2": "flushed before each step (256 MB write)"},
             "e2e": e2e, "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

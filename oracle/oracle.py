@@ -93,6 +93,8 @@ def lib(release: bool = False):
         L.orc_pcg_fork_uniform.argtypes = [u32, ip, ip, P(dbl)]
         L.orc_pcg_state_uniform.argtypes = [P(C.c_uint64)]
         L.orc_pcg_state_uniform.restype = dbl
+        L.orc_pcg_state_u32.argtypes = [P(C.c_uint64)]
+        L.orc_pcg_state_u32.restype = u32
         L.orc_twister_uniform.argtypes = [u32, ip, ip, P(dbl)]
         L.orc_uniform_ln.argtypes = [P(dbl)]
         L.orc_metropolis_accept.argtypes = [dbl, dbl, P(C.c_uint32), ip, P(ip)]
@@ -697,6 +699,13 @@ def _pcg_seed_state(seed):
     return ((seed + _PCG_INC) * _PCG_MULT + _PCG_INC) % (1 << 64)
 
 
+def _pcg_u32(state):
+    """One 32-bit output of the stream in `state`: (value, next state)."""
+    st = C.c_uint64(state)
+    x = lib().orc_pcg_state_u32(C.byref(st))
+    return int(x), st.value
+
+
 def _pcg_draw(state):
     """One uniform() of the stream in `state`: (value, next state)."""
     st = C.c_uint64(state)
@@ -706,16 +715,21 @@ def _pcg_draw(state):
 
 def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, initial_samples=4,
                              initial_sweeps=20, initial_alpha=2.0, initial_min_prob_log=2.0,
-                             max_prob=0.5, max_population_mult=128, alpha_low=1.00000001):
+                             max_prob=0.5, max_population_mult=128, alpha_low=1.00000001,
+                             budget_s=None, rng_mode="replay"):
     """The runs of a parameter-free population-annealing search
     (solver/parameter_free_solver.h:65-151 with solver/pa_parameter_free.h)
     replayed on one master stream: the first `initial_samples` parameter
     vectors from the adapter's initial values (get_initial_parameter_values,
     :228-260, the alpha jitter drawn from the master), later ones as given
     in `runs` (the strategy's picks), each applied as update_parameters
-    (:262-330) and run by the oracle's PA from the master's state.  Returns
-    [(params, step_limit, lowest)] for as many runs as `runs` lists.  The
-    walker cap is threads x max_population_mult (memory is not the limit)."""
+    (:262-330) and run by the oracle's PA from the master's state (with
+    counter streams, each run keys them with one master draw).  Returns
+    [(params, step_limit, lowest)] for as many runs as `runs` lists (fewer
+    when `budget_s` seconds have passed).  The walker cap is threads x
+    max_population_mult (memory is not the limit)."""
+    import time
+    t_start = time.perf_counter()
     mn_mx = cost_diff_bounds(kind, terms)
     mn, mx = mn_mx
     beta_start = -math.log(max_prob) / mx
@@ -739,18 +753,23 @@ def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, 
         pop = adjust(v[1])
         alpha = max(v[2], alpha_low)
         b1 = v[4] / mn
-        res = run(model, "pa", seed=seed, master_state=state, step_limit=sl, sweeps_per_replica=spr,
+        run_seed = seed
+        if rng_mode == "counter":
+            run_seed, state = _pcg_u32(state)
+        res = run(model, "pa", seed=run_seed, master_state=state, step_limit=sl, sweeps_per_replica=spr,
                   population=pop, alpha=alpha, sched=("geometric", beta_start, b1), pa_threads=threads,
-                  threads=min(threads, 16))
+                  threads=min(threads, 16), rng_mode=rng_mode)
         state = res.master_state
         out.append((v, sl, float(res.best_cost)))
+        if budget_s is not None and time.perf_counter() - t_start > budget_s:
+            break
     return out
 
 
 def ssmc_parameter_free_replay(model: Model, *, seed, threads, runs, sweep_size, initial_samples=4,
                                initial_sweeps=20, initial_spw=1, initial_alpha_final=0.00001,
                                initial_alpha_scope=0.8, initial_beta_initial=0.00001,
-                               initial_beta_scope=5.0, max_replica_mult=3):
+                               initial_beta_scope=5.0, max_replica_mult=3, rng_mode="replay"):
     """The runs of a parameter-free SSMC search (solver/ssmc_parameter_free.h
     get_initial_parameter_values :160-178, update_parameters :180-224) on one
     master stream, as pa_parameter_free_replay does for PA."""
@@ -772,9 +791,13 @@ def ssmc_parameter_free_replay(model: Model, *, seed, threads, runs, sweep_size,
         sl = max(int(math.floor(v[0])), 2)
         pop = adjust(v[1])
         spw = max(int(v[2]), 1)
-        res = run(model, "ssmc", seed=seed, master_state=state, step_limit=sl, population=pop,
+        run_seed = seed
+        if rng_mode == "counter":
+            run_seed, state = _pcg_u32(state)
+        res = run(model, "ssmc", seed=run_seed, master_state=state, step_limit=sl, population=pop,
                   pa_threads=threads, threads=min(threads, 16), steps_per_walker=spw,
-                  sched=("linear", v[3] + v[4], v[3]), sched2=("linear", v[5], v[5] + v[6]))
+                  sched=("linear", v[3] + v[4], v[3]), sched2=("linear", v[5], v[5] + v[6]),
+                  rng_mode=rng_mode)
         state = res.master_state
         out.append((v, sl, float(res.best_cost)))
     return out

@@ -2139,6 +2139,16 @@ void orc_pcg_stream(uint32_t seed, int use_default_seed, int n, uint32_t* out)
   for (int i = 0; i < n; i++) out[i] = g();
 }
 
+// one 32-bit output of the PCG stream in the given state, the state advanced
+uint32_t orc_pcg_state_u32(uint64_t* state)
+{
+  Pcg32 g;
+  g.state = *state;
+  const uint32_t x = g();
+  *state = g.state;
+  return x;
+}
+
 // one uniform() of the PCG stream in the given state, the state advanced
 double orc_pcg_state_uniform(uint64_t* state)
 {

@@ -203,6 +203,7 @@ class PopulationAnnealing : public Solver
 
   PcgEngine master{0};
   PcgEngine* ext_master = nullptr;  // repeated runs: the master stream continues from run to run
+  uint64_t swept = 0;  // attempts made since init (walkers swept x sweeps x sweep size)
   std::vector<uint64_t> streams;  // host mirror of the replay streams
   std::vector<size_t> family;
   std::vector<double> wbeta;
@@ -410,6 +411,7 @@ class PopulationAnnealing : public Solver
     has_low = false;
     trace_beta.clear();
     trace_pop.clear();
+    swept = 0;
     epoch = 0;
     target_pop = target_initial;
     master = ext_master ? *ext_master : PcgEngine(seed);
@@ -646,6 +648,8 @@ void PopulationAnnealing::run(cudaStream_t st)
     a.bs_s = 0;
     a.sweep_base = 0;
     a.n_sweeps = (int)spr;
+    swept += (uint64_t)Rn * (uint64_t)spr *
+             (uint64_t)((model->kind == K_MAXSAT && !full_maxsat_sweep) ? 1 : model->N);
     a.replay = replay ? 1 : 0;
     a.rng = d_streams;
     a.seed = seed;
@@ -901,6 +905,7 @@ class SubstochasticMonteCarlo : public Solver
   uint32_t* d_best = nullptr;
   PcgEngine master{0};
   PcgEngine* ext_master = nullptr;  // repeated runs: the master stream continues from run to run
+  uint64_t swept = 0;  // walker steps since init (each attempts a move with probability p_step)
   bool has_low = false;
   double low_cost = 0;
   int T = 1;
@@ -1037,6 +1042,7 @@ class SubstochasticMonteCarlo : public Solver
     cur = 0;
     has_low = false;
     step_pos = 0;
+    swept = 0;
     // rngs_[t] = rng_->fork() (solver/substochastic_monte_carlo.h:47-51);
     // thread t initialises its block of walkers in index order, each walker
     // taking one draw per 32 variables (model/ising.h:23-41), or one
@@ -1096,6 +1102,7 @@ class SubstochasticMonteCarlo : public Solver
     a.replay = replay ? 1 : 0;
     prof_begin(st);
     cuda_check(launch_ssmc_walk(a, st), "ssmc walk kernel");
+    swept += (uint64_t)R * (uint64_t)spw;
     prof_end(st);
     launches++;
     const DevPop& p = pools[cur].pop;
@@ -1285,6 +1292,7 @@ class BayesParameterFree : public Solver
   {
     std::vector<double> params;
     int64_t steps = 0, step_limit = 0;
+    uint64_t attempts = 0;
     double lowest = 0;
     bool recommended = false;
   };
@@ -1293,6 +1301,10 @@ class BayesParameterFree : public Solver
   uint64_t att_total = 0, acc_total = 0;
 
   virtual Solver& worker() = 0;
+  // the work of the worker's last run, under the trace key work_key():
+  // flip attempts (PA) or walker steps (SSMC)
+  virtual uint64_t worker_attempts() const = 0;
+  virtual const char* work_key() const = 0;
   virtual int dims() const = 0;
   virtual std::vector<std::pair<double, double>> ranges() = 0;
   virtual void initial_values(std::vector<double>& v) = 0;
@@ -1333,7 +1345,6 @@ class BayesParameterFree : public Solver
   // BayesianOpt::configure)
   void configure_search(const json::Value& p)
   {
-    if (!replay) fail(1, "parameter-free solvers run with \"rng_mode\": \"replay\"");
     if (number_of_solutions != 1)
       fail(1, "parameter-free solvers return one solution: `number_of_solutions` must be 1");
     auto integer = [&](const char* k, int64_t def) -> int64_t {
@@ -1438,6 +1449,9 @@ class BayesParameterFree : public Solver
       }
       update(v);
       Solver& w = worker();
+      // counter streams: each run keys them with one master draw, so that the
+      // runs' walkers draw independently
+      if (!replay) w.seed = master();
       w.has_time_limit = true;
       w.time_limit = left;
       worker_time_limit = left;
@@ -1457,6 +1471,7 @@ class BayesParameterFree : public Solver
       r.steps = w.last_step;
       r.step_limit = w.step_limit;
       r.lowest = obj + model->const_cost;
+      r.attempts = worker_attempts();
       r.recommended = rec;
       trace.push_back(r);
       const double exec = exec_cost();
@@ -1548,6 +1563,7 @@ class BayesParameterFree : public Solver
       s += (i ? "," : "") + std::string("{\"params\":[");
       for (size_t k = 0; k < r.params.size(); k++) s += (k ? "," : "") + json::number(r.params[k]);
       s += "],\"steps\":" + std::to_string(r.steps) + ",\"step_limit\":" + std::to_string(r.step_limit) +
+           ",\"" + work_key() + "\":" + std::to_string(r.attempts) +
            ",\"lowest\":" + json::number(r.lowest) + ",\"recommended\":" + (r.recommended ? "true" : "false") + "}";
     }
     s += "],\"stop\":" + json::quote(stop_reason) + ",\"training\":{\"learning_time_ms\":" +
@@ -1597,6 +1613,8 @@ class PAParameterFree : public BayesParameterFree
 
   std::string target() const override { return "populationannealing-parameterfree.cpu"; }
   Solver& worker() override { return *w; }
+  uint64_t worker_attempts() const override { return w->swept; }
+  const char* work_key() const override { return "attempts"; }
   int dims() const override { return 5; }
 
   void configure(const json::Value& doc)
@@ -1757,6 +1775,8 @@ class SSMCParameterFree : public BayesParameterFree
 
   std::string target() const override { return "substochasticmontecarlo-parameterfree.cpu"; }
   Solver& worker() override { return *w; }
+  uint64_t worker_attempts() const override { return w->swept; }
+  const char* work_key() const override { return "walker_steps"; }
   int dims() const override { return 7; }
 
   void configure(const json::Value& doc)

@@ -52,7 +52,8 @@ def test_strategy_argument_errors():
 def test_parameter_free_configuration_errors(target):
     m = q.Model("ising", [(1.0, [0, 1]), (-2.0, [1, 2])])
     with pytest.raises(q.QioError, match="rng_mode"):
-        q.Solver(m, target, {"params": {"seed": 1, "rng_mode": "counter"}})
+        q.Solver(m, target, {"params": {"seed": 1, "rng_mode": "sobol"}})
+    q.Solver(m, target, {"params": {"seed": 1, "rng_mode": "counter"}}).close()
     with pytest.raises(q.QioError, match="nonimprovement_limit"):
         q.Solver(m, target, {"params": {"seed": 1, "nonimprovement_limit": 0}})
     with pytest.raises(q.QioError, match="max_step_divider"):

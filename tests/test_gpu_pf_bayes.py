@@ -1,5 +1,6 @@
 """Parameter-free population annealing and SSMC (the Bayesian searches) on
-the GPU against the oracle.
+the GPU against the oracle, with the reference's replayed streams and with
+counter streams (each run keyed by one draw of the master stream).
 
 The search's runs share one master stream.  The first four take the
 adapter's initial parameter vectors, whose alpha or beta jitter is drawn from
@@ -51,17 +52,19 @@ def _check(res, ref, n_init=4):
     assert abs(cost - min(r["lowest"] for r in runs)) <= 1e-11
 
 
+@pytest.mark.parametrize("mode", ["replay", "counter"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_pa_parameter_free_runs_match_oracle(name):
+def test_pa_parameter_free_runs_match_oracle(name, mode):
     kind, gen, seed = CASES[name]
     off, ids, coef = gen()
     g = q.Model(kind, off=off, ids=ids, coef=coef)
     o = O.Model(kind, off=off, ids=ids, coef=coef)
-    s = q.Solver(g, PAPF, {"params": {"seed": seed, "timeout": 20, "threads": 4}}).init().run()
+    s = q.Solver(g, PAPF, {"params": {"seed": seed, "timeout": 20, "threads": 4,
+                                      "rng_mode": mode}}).init().run()
     res = s.result()
     runs = res["benchmark"]["parameter_free"]["runs"]
     ref = O.pa_parameter_free_replay(o, kind, _terms(off, ids, coef), seed=seed, threads=4,
-                                     runs=[r["params"] for r in runs])
+                                     runs=[r["params"] for r in runs], rng_mode=mode)
     _check(res, ref)
     for r in runs:
         v = r["params"]
@@ -70,17 +73,19 @@ def test_pa_parameter_free_runs_match_oracle(name):
     assert par["beta_stop"] > par["beta_start"] > 0 and par["population"] >= 4
 
 
+@pytest.mark.parametrize("mode", ["replay", "counter"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_ssmc_parameter_free_runs_match_oracle(name):
+def test_ssmc_parameter_free_runs_match_oracle(name, mode):
     kind, gen, seed = CASES[name]
     off, ids, coef = gen()
     g = q.Model(kind, off=off, ids=ids, coef=coef)
     o = O.Model(kind, off=off, ids=ids, coef=coef)
-    s = q.Solver(g, SSMCPF, {"params": {"seed": seed, "timeout": 20, "threads": 4}}).init().run()
+    s = q.Solver(g, SSMCPF, {"params": {"seed": seed, "timeout": 20, "threads": 4,
+                                        "rng_mode": mode}}).init().run()
     res = s.result()
     runs = res["benchmark"]["parameter_free"]["runs"]
     ref = O.ssmc_parameter_free_replay(o, seed=seed, threads=4, runs=[r["params"] for r in runs],
-                                       sweep_size=g.n_vars)
+                                       sweep_size=g.n_vars, rng_mode=mode)
     _check(res, ref)
     for r in runs:
         v = r["params"]
