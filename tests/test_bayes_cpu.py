@@ -80,3 +80,24 @@ def test_pa_parameter_free_refusals():
     ms = q.Model("maxsat", [(1.0, [1, -2]), (2.0, [2, 3])])
     with pytest.raises(q.QioError, match="Ising and PUBO"):
         q.Solver(ms, pf, {"params": {"seed": 1}})
+
+
+def test_oracle_replay_initial_vectors():
+    """The oracle's initial parameter vectors follow the adapters'
+    get_initial_parameter_values (solver/pa_parameter_free.h:228-260,
+    solver/ssmc_parameter_free.h:160-178), the jitter drawn from the seeded
+    master stream before each run's forks."""
+    from oracle import oracle as O
+    terms = [(1.0, [0, 1]), (-2.0, [1, 2]), (0.5, [2, 3]), (1.5, [3, 0]), (0.25, [1])]
+    off = np.cumsum([0] + [len(t) for _, t in terms])
+    ids = np.array([i for _, t in terms for i in t], np.int32)
+    coef = np.array([c for c, _ in terms])
+    o = O.Model("ising", off=off, ids=ids, coef=coef)
+    pa = O.pa_parameter_free_replay(o, "ising", terms, seed=5, threads=2, runs=[None] * 2)
+    u0, st = O._pcg_draw(O._pcg_seed_state(5))
+    assert pa[0][0] == [20.0, 2.0, 2.0 + 0.5 * (u0 - 0.5), 1.0, 2.0]
+    assert pa[1][0][:2] == [30.0, 4.0] and pa[1][0][3:] == [2.0, 4.0]
+    assert pa[0][1] == 20 and pa[1][1] == 15  # ceil(sweeps / sweeps_per_replica)
+    ss = O.ssmc_parameter_free_replay(o, seed=5, threads=2, runs=[None] * 2, sweep_size=4)
+    assert ss[0][0] == [80.0, 2.0, 1.0, 0.00001, 0.8, 0.00001, 5.0 + u0]
+    assert ss[1][0][:2] == [160.0, 3.0]
