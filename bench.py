@@ -803,7 +803,7 @@ def main_pf(args, ws, rank):
         print(json.dumps(line), flush=True)
 
 
-PF_PA_PARAMS = {"seed": 0, "timeout": 3, "threads": 16, "rng_mode": "counter"}
+PF_PA_PARAMS = {"seed": 0, "timeout": 3, "threads": 16, "rng_mode": "counter", "resampling": "reference"}
 
 
 def main_pf_pa(args, ws, rank):
@@ -894,7 +894,8 @@ def main_pf_pa(args, ws, rank):
         t0 = time.perf_counter()
         ref = O.pa_parameter_free_replay(o, "ising", terms, seed=PF_PA_PARAMS["seed"],
                                          threads=PF_PA_PARAMS["threads"], runs=[x["params"] for x in whole],
-                                         budget_s=15.0, rng_mode=PF_PA_PARAMS["rng_mode"])
+                                         budget_s=15.0, rng_mode=PF_PA_PARAMS["rng_mode"],
+                                         resampling=PF_PA_PARAMS["resampling"])
         k = len(ref)
         a_cpu = sum(int(x["attempts"]) for x in whole[:k])
         same = all(r[2] == x["lowest"] for r, x in zip(ref, whole))

@@ -716,7 +716,7 @@ def _pcg_draw(state):
 def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, initial_samples=4,
                              initial_sweeps=20, initial_alpha=2.0, initial_min_prob_log=2.0,
                              max_prob=0.5, max_population_mult=128, alpha_low=1.00000001,
-                             budget_s=None, rng_mode="replay"):
+                             budget_s=None, rng_mode="replay", resampling="reference"):
     """The runs of a parameter-free population-annealing search
     (solver/parameter_free_solver.h:65-151 with solver/pa_parameter_free.h)
     replayed on one master stream: the first `initial_samples` parameter
@@ -758,7 +758,7 @@ def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, 
             run_seed, state = _pcg_u32(state)
         res = run(model, "pa", seed=run_seed, master_state=state, step_limit=sl, sweeps_per_replica=spr,
                   population=pop, alpha=alpha, sched=("geometric", beta_start, b1), pa_threads=threads,
-                  threads=min(threads, 16), rng_mode=rng_mode)
+                  threads=min(threads, 16), rng_mode=rng_mode, resampling=resampling)
         state = res.master_state
         out.append((v, sl, float(res.best_cost)))
         if budget_s is not None and time.perf_counter() - t_start > budget_s:

@@ -1625,7 +1625,6 @@ class PAParameterFree : public BayesParameterFree
     w->configure(doc);
     if (w->strategy != "linear_schedule")
       fail(1, "parameter-free population annealing supports `resampling_strategy` \"linear_schedule\" only");
-    if (w->multinomial) fail(1, "parameter-free population annealing uses the reference resampling");
     const json::Value& p = params;
     configure_search(p);
     max_step_divider = num_param(p, "max_step_divider", 160.);

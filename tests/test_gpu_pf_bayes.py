@@ -52,19 +52,21 @@ def _check(res, ref, n_init=4):
     assert abs(cost - min(r["lowest"] for r in runs)) <= 1e-11
 
 
-@pytest.mark.parametrize("mode", ["replay", "counter"])
+@pytest.mark.parametrize("mode", ["replay", "counter", "multinomial"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_pa_parameter_free_runs_match_oracle(name, mode):
     kind, gen, seed = CASES[name]
     off, ids, coef = gen()
     g = q.Model(kind, off=off, ids=ids, coef=coef)
     o = O.Model(kind, off=off, ids=ids, coef=coef)
-    s = q.Solver(g, PAPF, {"params": {"seed": seed, "timeout": 20, "threads": 4,
-                                      "rng_mode": mode}}).init().run()
+    rng = "replay" if mode == "replay" else "counter"
+    rs = "multinomial" if mode == "multinomial" else "reference"
+    s = q.Solver(g, PAPF, {"params": {"seed": seed, "timeout": 20, "threads": 4, "rng_mode": rng,
+                                      "resampling": rs}}).init().run()
     res = s.result()
     runs = res["benchmark"]["parameter_free"]["runs"]
     ref = O.pa_parameter_free_replay(o, kind, _terms(off, ids, coef), seed=seed, threads=4,
-                                     runs=[r["params"] for r in runs], rng_mode=mode)
+                                     runs=[r["params"] for r in runs], rng_mode=rng, resampling=rs)
     _check(res, ref)
     for r in runs:
         v = r["params"]
