@@ -200,7 +200,13 @@ qio_status qio_states_apply(const qio_model* model, int64_t n,
 /* ---- solvers ---------------------------------------------------------- */
 
 /* Create a solver for `target` ("simulatedannealing.qiotoolkit",
- * "paralleltempering.qiotoolkit", "populationannealing.cpu") configured from
+ * "paralleltempering.qiotoolkit", "populationannealing.cpu", and beside the
+ * path "tabu.qiotoolkit", "substochasticmontecarlo.cpu",
+ * "quantummontecarlo.qiotoolkit" and the parameter-free searches
+ * "simulatedannealing-parameterfree.qiotoolkit",
+ * "paralleltempering-parameterfree.qiotoolkit",
+ * "tabu-parameterfree.qiotoolkit", "populationannealing-parameterfree.cpu",
+ * "substochasticmontecarlo-parameterfree.cpu") configured from
  * the reference's params JSON ({"params": {...}}): replaces
  * create_model_solver (app/runner.cc:134-193) + Solver::configure
  * (solver/solver.h:156-218 and the solver-specific configure()).  Options
