@@ -725,7 +725,8 @@ def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, 
     in `runs` (the strategy's picks), each applied as update_parameters
     (:262-330) and run by the oracle's PA from the master's state (with
     counter streams, each run keys them with one master draw).  Returns
-    [(params, step_limit, lowest)] for as many runs as `runs` lists (fewer
+    [(params, step_limit, lowest, lowest state)] for as many runs as `runs`
+    lists (fewer
     when `budget_s` seconds have passed).  The walker cap is threads x
     max_population_mult (memory is not the limit)."""
     import time
@@ -760,7 +761,7 @@ def pa_parameter_free_replay(model: Model, kind, terms, *, seed, threads, runs, 
                   population=pop, alpha=alpha, sched=("geometric", beta_start, b1), pa_threads=threads,
                   threads=min(threads, 16), rng_mode=rng_mode, resampling=resampling)
         state = res.master_state
-        out.append((v, sl, float(res.best_cost)))
+        out.append((v, sl, float(res.best_cost), res.best_state.copy()))
         if budget_s is not None and time.perf_counter() - t_start > budget_s:
             break
     return out
@@ -799,6 +800,6 @@ def ssmc_parameter_free_replay(model: Model, *, seed, threads, runs, sweep_size,
                   sched=("linear", v[3] + v[4], v[3]), sched2=("linear", v[5], v[5] + v[6]),
                   rng_mode=rng_mode)
         state = res.master_state
-        out.append((v, sl, float(res.best_cost)))
+        out.append((v, sl, float(res.best_cost), res.best_state.copy()))
     return out
 

@@ -38,7 +38,7 @@ def _check(res, ref, n_init=4):
     pf = res["benchmark"]["parameter_free"]
     runs = pf["runs"]
     assert len(runs) > n_init and any(r["recommended"] for r in runs)
-    for k, (r, (v, sl, low)) in enumerate(zip(runs, ref)):
+    for k, (r, (v, sl, low, _)) in enumerate(zip(runs, ref)):
         if k < n_init:
             assert r["params"] == v
         assert r["step_limit"] == sl
