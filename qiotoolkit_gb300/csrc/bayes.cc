@@ -30,6 +30,7 @@ struct Gp
   double sf2 = 1, sn2 = 1e-3;
   std::vector<double> inv_l2;  // 1 / length scale^2
   std::vector<double> L;       // lower Cholesky factor of K, n x n
+  std::vector<double> Kf;      // the signal part of K (lower triangle), n x n
   std::vector<double> alpha;   // K^-1 y
 
   void set_theta(const std::vector<double>& th)
@@ -54,6 +55,9 @@ struct Gp
   bool factor()
   {
     L.assign((size_t)n * n, 0.0);
+    Kf.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j <= i; j++) Kf[(size_t)i * n + j] = kern(&u[(size_t)i * d], &u[(size_t)j * d]);
     for (int attempt = 0; attempt < 4; attempt++)
     {
       const double jitter = attempt == 0 ? 0.0 : sf2 * std::pow(10.0, -10 + 2 * attempt);
@@ -61,7 +65,7 @@ struct Gp
       for (int i = 0; i < n && ok; i++)
         for (int j = 0; j <= i; j++)
         {
-          double s = kern(&u[(size_t)i * d], &u[(size_t)j * d]);
+          double s = Kf[(size_t)i * n + j];
           if (i == j) s += ((i < (int)pseudo.size() && pseudo[i]) ? 1e-8 * sf2 : sn2) + jitter;
           for (int k = 0; k < j; k++) s -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
           if (i == j)
@@ -146,31 +150,43 @@ double lml(Gp& g, const std::vector<double>& th, std::vector<double>* grad)
   for (int i = 0; i < n; i++) v -= 0.5 * g.y[i] * g.alpha[i] + std::log(g.L[(size_t)i * n + i]);
   v -= 0.5 * n * kLog2Pi;
   if (!grad) return v;
-  // W = alpha alpha^T - K^-1 (columns of K^-1 by solves)
-  std::vector<double> Kinv((size_t)n * n), col(n);
+  // W = alpha alpha^T - K^-1, with K^-1 = L^-T L^-1 from the triangular
+  // inverse (lower triangles only: W and dK/dtheta are symmetric)
+  std::vector<double> Li((size_t)n * n, 0.0), Kinv((size_t)n * n, 0.0);
   for (int j = 0; j < n; j++)
   {
-    std::fill(col.begin(), col.end(), 0.0);
-    col[j] = 1.0;
-    g.solve(col);
-    for (int i = 0; i < n; i++) Kinv[(size_t)i * n + j] = col[i];
+    Li[(size_t)j * n + j] = 1.0 / g.L[(size_t)j * n + j];
+    for (int i = j + 1; i < n; i++)
+    {
+      double s = 0;
+      for (int k = j; k < i; k++) s -= g.L[(size_t)i * n + k] * Li[(size_t)k * n + j];
+      Li[(size_t)i * n + j] = s / g.L[(size_t)i * n + i];
+    }
   }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j <= i; j++)
+    {
+      double s = 0;
+      for (int k = i; k < n; k++) s += Li[(size_t)k * n + i] * Li[(size_t)k * n + j];
+      Kinv[(size_t)i * n + j] = s;
+    }
   grad->assign(d + 2, 0.0);
   std::vector<double>& gr = *grad;
   for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++)
+    for (int j = 0; j <= i; j++)
     {
-      const double w = g.alpha[i] * g.alpha[j] - Kinv[(size_t)i * n + j];
+      const double m = i == j ? 0.5 : 1.0;  // off-diagonal pairs count twice
+      const double w = m * (g.alpha[i] * g.alpha[j] - Kinv[(size_t)i * n + j]);
       const double* a = &g.u[(size_t)i * d];
       const double* b = &g.u[(size_t)j * d];
-      const double kf = g.kern(a, b);
-      gr[0] += 0.5 * w * kf;
+      const double kf = g.Kf[(size_t)i * n + j];
+      gr[0] += w * kf;
       for (int c = 0; c < d; c++)
       {
         const double t = a[c] - b[c];
-        gr[1 + c] += 0.5 * w * kf * t * t * g.inv_l2[c];
+        gr[1 + c] += w * kf * t * t * g.inv_l2[c];
       }
-      if (i == j) gr[1 + d] += 0.5 * w * g.sn2;
+      if (i == j) gr[1 + d] += w * g.sn2;
     }
   return v;
 }

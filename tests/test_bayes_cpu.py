@@ -101,3 +101,23 @@ def test_oracle_replay_initial_vectors():
     ss = O.ssmc_parameter_free_replay(o, seed=5, threads=2, runs=[None] * 2, sweep_size=4)
     assert ss[0][0] == [80.0, 2.0, 1.0, 0.00001, 0.8, 0.00001, 5.0 + u0]
     assert ss[1][0][:2] == [160.0, 3.0]
+
+
+def test_strategy_gradients_match_finite_differences(tmp_path):
+    """The analytic gradients the strategy ascends (log marginal likelihood
+    in the hyperparameters, expected improvement in the point) agree with
+    central differences."""
+    import os
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = str(tmp_path / "grad")
+    subprocess.run([cxx, "-std=c++17", "-O2", os.path.join(root, "tests", "integration", "bayes_gradients.cc"),
+                    "-o", out], check=True, capture_output=True, text=True)
+    r = subprocess.run([out], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    _, lml, _, ei = r.stdout.split()
+    assert float(lml) < 1e-6 and float(ei) < 1e-6
